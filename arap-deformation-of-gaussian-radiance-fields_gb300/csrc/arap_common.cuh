@@ -1,0 +1,500 @@
+// Shared device code for the sm_103a ARAP library: status word, bounded grid
+// barrier with a deterministic FP64 reduction, small 3x3 / quaternion math,
+// polar factors and real-SH band rotation.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <utility>
+
+#include "../../include/arap_gb300.h"
+
+#define ARAP_CUDA_TRY(expr)                   \
+  do {                                        \
+    cudaError_t _e = (expr);                  \
+    if (_e != cudaSuccess) return ARAP_ECUDA; \
+  } while (0)
+
+#define ARAP_LAUNCH_CHECK()                                  \
+  do {                                                       \
+    if (cudaPeekAtLastError() != cudaSuccess) {              \
+      (void)cudaGetLastError();                              \
+      return ARAP_ECUDA;                                     \
+    }                                                        \
+  } while (0)
+
+namespace arap {
+
+// Sticky device-side error word (ARAP_* code, first error wins).  Defined in
+// api.cu; read and cleared by arap_get_device_status.
+extern __device__ int g_status;
+
+__device__ __forceinline__ void raise_status(int code) { atomicCAS(&g_status, 0, code); }
+
+// ------------------------------------------------------------ barrier ----
+// Grid-wide barrier for cooperative launches (all CTAs co-resident).  Every
+// wait is bounded: after kSpinLimit polls a waiting CTA records ARAP_ETIMEOUT,
+// marks the barrier failed and returns false; callers then leave the kernel.
+// The barrier carries NSLOT deterministic FP64 sums: every CTA leaves one
+// partial per slot; the last CTA to arrive adds them in CTA order, publishes
+// the totals and only then releases the waiters.
+struct GridBarrier {
+  unsigned int count;
+  unsigned int gen;
+  int failed;
+  int pad;
+};
+
+constexpr long long kSpinLimit = 1ll << 23;
+
+__device__ __forceinline__ unsigned int ld_acquire_u32(const unsigned int* p) {
+  unsigned int v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_release_u32(unsigned int* p, unsigned int v) {
+  asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ int ld_relaxed_i32(const int* p) {
+  int v;
+  asm volatile("ld.relaxed.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+// Sums are returned in out[] to every thread of every CTA.
+template <int NSLOT>
+__device__ bool grid_sync_reduce(GridBarrier* bar, double* partials, double* results,
+                                 const double (&mine)[NSLOT], double (&out)[NSLOT]) {
+  __shared__ int s_last;
+  __shared__ int s_ok;
+  __shared__ double s_out[NSLOT > 0 ? NSLOT : 1];
+  const unsigned int nb = gridDim.x;
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int s = 0; s < NSLOT; ++s) partials[s * nb + blockIdx.x] = mine[s];
+  }
+  __syncthreads();
+  unsigned int g = 0;
+  if (threadIdx.x == 0) {
+    g = ld_acquire_u32(&bar->gen);  // cannot advance before this CTA arrives
+    __threadfence();
+    unsigned int arrived = atomicAdd(&bar->count, 1u);
+    s_last = (arrived == nb - 1);
+    s_ok = 1;
+  }
+  __syncthreads();
+  if (s_last) {
+    if (threadIdx.x < 32) {
+      __threadfence();
+#pragma unroll
+      for (int s = 0; s < NSLOT; ++s) {
+        double acc = 0.0;
+        for (unsigned int c = threadIdx.x; c < nb; c += 32) acc += __ldcg(partials + s * nb + c);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+        if (threadIdx.x == 0) {
+          results[s] = acc;
+          s_out[s] = acc;
+        }
+      }
+      if (threadIdx.x == 0) {
+        atomicExch(&bar->count, 0u);
+        __threadfence();
+        st_release_u32(&bar->gen, g + 1u);
+        s_ok = ld_relaxed_i32(&bar->failed) == 0;
+      }
+    }
+  } else if (threadIdx.x == 0) {
+    long long it = 0;
+    int ok = 1;
+    while (ld_acquire_u32(&bar->gen) == g) {
+      if (ld_relaxed_i32(&bar->failed)) {
+        ok = 0;
+        break;
+      }
+      if (++it > kSpinLimit) {
+        atomicExch(&bar->failed, 1);
+        raise_status(ARAP_ETIMEOUT);
+        ok = 0;
+        break;
+      }
+      if (it > 256) __nanosleep(40);
+    }
+    if (ok) {
+#pragma unroll
+      for (int s = 0; s < NSLOT; ++s) s_out[s] = __ldcg(results + s);
+    }
+    s_ok = ok;
+  }
+  __syncthreads();
+#pragma unroll
+  for (int s = 0; s < NSLOT; ++s) out[s] = s_out[s];
+  const bool ok = s_ok != 0;
+  __syncthreads();
+  return ok;
+}
+
+__device__ __forceinline__ bool grid_sync(GridBarrier* bar, double* partials, double* results) {
+  double none[1] = {0.0}, o[1];
+  return grid_sync_reduce<1>(bar, partials, results, none, o);
+}
+
+// Marks the barrier failed so that peers waiting in it leave promptly.
+__device__ __forceinline__ void grid_fail(GridBarrier* bar, int code) {
+  raise_status(code);
+  atomicExch(&bar->failed, 1);
+}
+
+// Block-wide FP64 sum (blockDim.x multiple of 32, <= 1024); all threads get it.
+template <int NV>
+__device__ __forceinline__ void block_sum(double (&v)[NV]) {
+  __shared__ double s_red[32][NV];
+#pragma unroll
+  for (int i = 0; i < NV; ++i) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v[i] += __shfl_xor_sync(0xffffffffu, v[i], o);
+  }
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  if (l == 0) {
+#pragma unroll
+    for (int i = 0; i < NV; ++i) s_red[w][i] = v[i];
+  }
+  __syncthreads();
+  const int nw = blockDim.x >> 5;
+#pragma unroll
+  for (int i = 0; i < NV; ++i) {
+    double a = 0.0;
+    for (int j = 0; j < nw; ++j) a += s_red[j][i];
+    v[i] = a;
+  }
+  __syncthreads();
+}
+
+// ----------------------------------------------------------- 3x3 math ----
+// Row-major 3x3 in m[r*3+c].
+template <typename T>
+__device__ __forceinline__ T det3(const T* m) {
+  return m[0] * (m[4] * m[8] - m[5] * m[7]) - m[1] * (m[3] * m[8] - m[5] * m[6]) +
+         m[2] * (m[3] * m[7] - m[4] * m[6]);
+}
+
+// Inverse-transpose by cofactors: out = (m^{-1})^T = cof(m)/det.
+template <typename T>
+__device__ __forceinline__ bool inv_transpose3(const T* m, T* out) {
+  T c[9];
+  c[0] = m[4] * m[8] - m[5] * m[7];
+  c[1] = m[5] * m[6] - m[3] * m[8];
+  c[2] = m[3] * m[7] - m[4] * m[6];
+  c[3] = m[2] * m[7] - m[1] * m[8];
+  c[4] = m[0] * m[8] - m[2] * m[6];
+  c[5] = m[1] * m[6] - m[0] * m[7];
+  c[6] = m[1] * m[5] - m[2] * m[4];
+  c[7] = m[2] * m[3] - m[0] * m[5];
+  c[8] = m[0] * m[4] - m[1] * m[3];
+  const T det = m[0] * c[0] + m[1] * c[1] + m[2] * c[2];
+  if (!(det != T(0))) return false;
+  const T inv = T(1) / det;
+#pragma unroll
+  for (int i = 0; i < 9; ++i) out[i] = c[i] * inv;
+  return true;
+}
+
+// Orthogonal polar factor U V^T of a non-singular M by Newton's iteration
+// X <- (g X + X^{-T}/g)/2 with Higham's Frobenius-norm scaling g for the first
+// steps (N. J. Higham, "Computing the polar decomposition -- with
+// applications", SIAM J. Sci. Stat. Comput. 7 (1986)).  Keeps det's sign, so a
+// reflection stays a reflection, as U V^T of an SVD does.  Returns false when
+// an iterate is singular.
+template <typename T>
+__device__ __forceinline__ bool polar_factor(const T* M, T* R, int max_it, T tol) {
+  T X[9];
+#pragma unroll
+  for (int i = 0; i < 9; ++i) X[i] = M[i];
+  for (int it = 0; it < max_it; ++it) {
+    T Y[9];
+    if (!inv_transpose3(X, Y)) return false;
+    T g = T(1);
+    if (it < 3) {
+      T nx = 0, ny = 0;
+#pragma unroll
+      for (int i = 0; i < 9; ++i) {
+        nx += X[i] * X[i];
+        ny += Y[i] * Y[i];
+      }
+      g = sqrt(sqrt(ny / nx));
+    }
+    T delta = 0;
+#pragma unroll
+    for (int i = 0; i < 9; ++i) {
+      const T xn = T(0.5) * (g * X[i] + Y[i] / g);
+      delta = fmax(delta, fabs(xn - X[i]));
+      X[i] = xn;
+    }
+    if (delta < tol) break;
+  }
+#pragma unroll
+  for (int i = 0; i < 9; ++i) R[i] = X[i];
+  return true;
+}
+
+// Unscaled Newton iteration M <- (M + M^{-T})/2 stopped when max|dM| < 1e-6,
+// returning the iterate before the final update (helper.cpp:506-517).
+template <typename T>
+__device__ __forceinline__ bool newton_polar_ref(T* M, int max_it) {
+  for (int it = 0; it < max_it; ++it) {
+    T Y[9];
+    if (!inv_transpose3(M, Y)) return false;
+    T delta = 0;
+    T nxt[9];
+#pragma unroll
+    for (int i = 0; i < 9; ++i) {
+      nxt[i] = T(0.5) * (M[i] + Y[i]);
+      delta = fmax(delta, fabs(M[i] - nxt[i]));
+    }
+    if (delta < T(1e-6)) return true;
+#pragma unroll
+    for (int i = 0; i < 9; ++i) M[i] = nxt[i];
+  }
+  return true;
+}
+
+// ---------------------------------------------------------- quaternions --
+// (w,x,y,z).  Matrix -> quaternion by Shoemake's trace / largest-diagonal
+// method (K. Shoemake, "Animating rotation with quaternion curves",
+// SIGGRAPH 1985).  Not normalised.
+__device__ __forceinline__ float4 quat_from_rowmajor(const float* m) {
+  float4 q;
+  const float tr = m[0] + m[4] + m[8];
+  if (tr > 0.0f) {
+    float t = sqrtf(tr + 1.0f);
+    q.x = 0.5f * t;
+    t = 0.5f / t;
+    q.y = (m[7] - m[5]) * t;
+    q.z = (m[2] - m[6]) * t;
+    q.w = (m[3] - m[1]) * t;
+  } else {
+    int i = 0;
+    if (m[4] > m[0]) i = 1;
+    if (m[8] > m[i * 4]) i = 2;
+    const int j = (i + 1) % 3, k = (j + 1) % 3;
+    float t = sqrtf(m[i * 4] - m[j * 4] - m[k * 4] + 1.0f);
+    float v[3];
+    v[i] = 0.5f * t;
+    t = 0.5f / t;
+    const float w = (m[k * 3 + j] - m[j * 3 + k]) * t;
+    v[j] = (m[j * 3 + i] + m[i * 3 + j]) * t;
+    v[k] = (m[k * 3 + i] + m[i * 3 + k]) * t;
+    q.x = w;
+    q.y = v[0];
+    q.z = v[1];
+    q.w = v[2];
+  }
+  return q;  // .x=w .y=x .z=y .w=z
+}
+
+__device__ __forceinline__ float4 quat_normalize(float4 q) {
+  const float n = sqrtf(q.x * q.x + q.y * q.y + q.z * q.z + q.w * q.w);
+  const float inv = 1.0f / n;
+  return make_float4(q.x * inv, q.y * inv, q.z * inv, q.w * inv);
+}
+
+// Hamilton product a*b, (w,x,y,z) stored in (.x,.y,.z,.w).
+__device__ __forceinline__ float4 quat_mul(float4 a, float4 b) {
+  return make_float4(a.x * b.x - a.y * b.y - a.z * b.z - a.w * b.w,
+                     a.x * b.y + a.y * b.x + a.z * b.w - a.w * b.z,
+                     a.x * b.z - a.y * b.w + a.z * b.x + a.w * b.y,
+                     a.x * b.w + a.y * b.z - a.z * b.y + a.w * b.x);
+}
+
+__device__ __forceinline__ float4 quat_inverse(float4 q) {
+  const float n2 = q.x * q.x + q.y * q.y + q.z * q.z + q.w * q.w;
+  const float inv = 1.0f / n2;
+  return make_float4(q.x * inv, -q.y * inv, -q.z * inv, -q.w * inv);
+}
+
+// Unit quaternion -> row-major rotation.
+__device__ __forceinline__ void quat_to_rowmajor(float4 q, float* R) {
+  const float w = q.x, x = q.y, y = q.z, z = q.w;
+  R[0] = 1.0f - 2.0f * (y * y + z * z);
+  R[1] = 2.0f * (x * y - w * z);
+  R[2] = 2.0f * (x * z + w * y);
+  R[3] = 2.0f * (x * y + w * z);
+  R[4] = 1.0f - 2.0f * (x * x + z * z);
+  R[5] = 2.0f * (y * z - w * x);
+  R[6] = 2.0f * (x * z - w * y);
+  R[7] = 2.0f * (y * z + w * x);
+  R[8] = 1.0f - 2.0f * (x * x + y * y);
+}
+
+// ------------------------------------------------------- SH rotation -----
+// Real spherical-harmonic band rotation for bands 1..3 from the recurrence of
+// Ivanic and Ruedenberg (J. Phys. Chem. 100 (1996) 6342; erratum 102 (1998)
+// 9099).  Coefficients are evaluated at compile time; band 1 uses the
+// (y, z, x) ordering of the 3DGS / reference layout.
+__host__ __device__ constexpr double csqrt_newton(double x, double cur, double prev) {
+  return cur == prev ? cur : csqrt_newton(x, 0.5 * (cur + x / cur), cur);
+}
+__host__ __device__ constexpr double csqrt(double x) {
+  return x <= 0.0 ? 0.0 : csqrt_newton(x, x > 1.0 ? x : 1.0, 0.0);
+}
+
+template <int L>
+struct ShBand {
+  float v[2 * L + 1][2 * L + 1];
+};
+
+// P term of the recurrence: r1 is band 1 indexed [i+1][j+1], prev band L-1
+// indexed [a+L-1][b+L-1].
+template <int L, int I, int A, int B>
+__device__ __forceinline__ float sh_p(const ShBand<1>& r1, const ShBand<L - 1>& prev) {
+  if constexpr (B == L) {
+    return r1.v[I + 1][2] * prev.v[A + L - 1][2 * L - 2] - r1.v[I + 1][0] * prev.v[A + L - 1][0];
+  } else if constexpr (B == -L) {
+    return r1.v[I + 1][2] * prev.v[A + L - 1][0] + r1.v[I + 1][0] * prev.v[A + L - 1][2 * L - 2];
+  } else {
+    return r1.v[I + 1][1] * prev.v[A + L - 1][B + L - 1];
+  }
+}
+
+template <int L, int M, int N>
+__device__ __forceinline__ float sh_elem(const ShBand<1>& r1, const ShBand<L - 1>& prev) {
+  constexpr double d = (M == 0) ? 1.0 : 0.0;
+  constexpr int am = M < 0 ? -M : M;
+  constexpr double den = (N < L && N > -L) ? double((L + N) * (L - N)) : double(2 * L * (2 * L - 1));
+  constexpr double u = csqrt(double((L + M) * (L - M)) / den);
+  constexpr double v = 0.5 * csqrt((1.0 + d) * double((L + am - 1) * (L + am)) / den) * (1.0 - 2.0 * d);
+  constexpr double w = -0.5 * csqrt(double((L - am - 1) * (L - am)) / den) * (1.0 - d);
+  float acc = 0.0f;
+  if constexpr (u != 0.0) acc += float(u) * sh_p<L, 0, M, N>(r1, prev);
+  if constexpr (v != 0.0) {
+    float V;
+    if constexpr (M == 0) {
+      V = sh_p<L, 1, 1, N>(r1, prev) + sh_p<L, -1, -1, N>(r1, prev);
+    } else if constexpr (M > 0) {
+      constexpr float c1 = float(csqrt(1.0 + (M == 1 ? 1.0 : 0.0)));
+      if constexpr (M == 1) {
+        V = sh_p<L, 1, M - 1, N>(r1, prev) * c1;
+      } else {
+        V = sh_p<L, 1, M - 1, N>(r1, prev) * c1 - sh_p<L, -1, -M + 1, N>(r1, prev);
+      }
+    } else {
+      constexpr float c2 = float(csqrt(1.0 + (M == -1 ? 1.0 : 0.0)));
+      if constexpr (M == -1) {
+        V = sh_p<L, -1, -M - 1, N>(r1, prev) * c2;
+      } else {
+        V = sh_p<L, 1, M + 1, N>(r1, prev) + sh_p<L, -1, -M - 1, N>(r1, prev) * c2;
+      }
+    }
+    acc += float(v) * V;
+  }
+  if constexpr (w != 0.0) {
+    float W;
+    if constexpr (M > 0) {
+      W = sh_p<L, 1, M + 1, N>(r1, prev) + sh_p<L, -1, -M - 1, N>(r1, prev);
+    } else {
+      W = sh_p<L, 1, M - 1, N>(r1, prev) - sh_p<L, -1, -M + 1, N>(r1, prev);
+    }
+    acc += float(w) * W;
+  }
+  return acc;
+}
+
+template <int L, int... Is>
+__device__ __forceinline__ void sh_fill(ShBand<L>& out, const ShBand<1>& r1, const ShBand<L - 1>& prev,
+                                        std::integer_sequence<int, Is...>) {
+  ((out.v[Is / (2 * L + 1)][Is % (2 * L + 1)] =
+        sh_elem<L, Is / (2 * L + 1) - L, Is % (2 * L + 1) - L>(r1, prev)),
+   ...);
+}
+
+// Rotate interleaved SH s[coef*3 + rgb] (16 coefficients) by row-major R.
+// With FLIP the odd coefficients are negated before and after the band
+// rotation (the sign convention of cudakdtree.cu:160-196 and
+// GaussianView.cpp:3138-3154).
+template <bool FLIP>
+__device__ __forceinline__ void rotate_sh48(const float* R, float* s) {
+  ShBand<1> b1;
+  const int perm[3] = {1, 2, 0};
+#pragma unroll
+  for (int a = 0; a < 3; ++a)
+#pragma unroll
+    for (int b = 0; b < 3; ++b) b1.v[a][b] = R[perm[a] * 3 + perm[b]];
+  if (FLIP) {
+#pragma unroll
+    for (int k = 1; k < 16; k += 2) {
+      s[k * 3 + 0] = -s[k * 3 + 0];
+      s[k * 3 + 1] = -s[k * 3 + 1];
+      s[k * 3 + 2] = -s[k * 3 + 2];
+    }
+  }
+  // band 1: coefficients 1..3
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    float in[3], out[3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) in[i] = s[(1 + i) * 3 + c];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) out[i] = b1.v[i][0] * in[0] + b1.v[i][1] * in[1] + b1.v[i][2] * in[2];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) s[(1 + i) * 3 + c] = out[i];
+  }
+  ShBand<2> b2;
+  sh_fill<2>(b2, b1, b1, std::make_integer_sequence<int, 25>{});
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    float in[5], out[5];
+#pragma unroll
+    for (int i = 0; i < 5; ++i) in[i] = s[(4 + i) * 3 + c];
+#pragma unroll
+    for (int i = 0; i < 5; ++i) {
+      float a = 0.0f;
+#pragma unroll
+      for (int j = 0; j < 5; ++j) a += b2.v[i][j] * in[j];
+      out[i] = a;
+    }
+#pragma unroll
+    for (int i = 0; i < 5; ++i) s[(4 + i) * 3 + c] = out[i];
+  }
+  ShBand<3> b3;
+  sh_fill<3>(b3, b1, b2, std::make_integer_sequence<int, 49>{});
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    float in[7], out[7];
+#pragma unroll
+    for (int i = 0; i < 7; ++i) in[i] = s[(9 + i) * 3 + c];
+#pragma unroll
+    for (int i = 0; i < 7; ++i) {
+      float a = 0.0f;
+#pragma unroll
+      for (int j = 0; j < 7; ++j) a += b3.v[i][j] * in[j];
+      out[i] = a;
+    }
+#pragma unroll
+    for (int i = 0; i < 7; ++i) s[(9 + i) * 3 + c] = out[i];
+  }
+  if (FLIP) {
+#pragma unroll
+    for (int k = 1; k < 16; k += 2) {
+      s[k * 3 + 0] = -s[k * 3 + 0];
+      s[k * 3 + 1] = -s[k * 3 + 1];
+      s[k * 3 + 2] = -s[k * 3 + 2];
+    }
+  }
+}
+
+// ------------------------------------------------------------ helpers ----
+__device__ __forceinline__ float4 ldg4(const float* p) { return __ldg(reinterpret_cast<const float4*>(p)); }
+
+// Exactly rounded float32 distance as (dx*dx + dy*dy) + dz*dz without FMA
+// contraction (Deform.hpp:164-165).
+__device__ __forceinline__ float dist2_rn(float dx, float dy, float dz) {
+  return __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
+}
+
+inline int grid_for(long long n, int block) {
+  long long g = (n + block - 1) / block;
+  return (int)(g > 0x7fffffffll ? 0x7fffffff : (g < 1 ? 1 : g));
+}
+
+}  // namespace arap

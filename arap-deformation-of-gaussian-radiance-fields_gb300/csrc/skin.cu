@@ -1,0 +1,593 @@
+// Per-frame skinning kernels (sm_103a): node transform table, endpoint
+// creation, fused Gaussian skinning + refit + SH rotation, node quaternions,
+// fused sample skinning + slerp blend + SH rotation, node update, static masks
+// and control-target generators.
+//
+// Layouts: per-item state the library owns (endpoints, kNN) is in planes
+// [C][P] so that every warp load is one 128-byte line; per-item outputs that
+// the rasteriser consumes keep the reference's AoS records (pos float3,
+// rot float4 (w,x,y,z), scale float3, SH 48 floats [coef*3 + rgb]).
+#include "arap_common.cuh"
+
+namespace arap {
+
+constexpr int kSkinThreads = 128;
+
+// Node table entry: [R row-major 9 | g 3 | t+g 3 | 0] as four float4.
+struct NodeXf {
+  float4 a, b, c, d;
+};
+
+__device__ __forceinline__ NodeXf load_node(const float* __restrict__ table, int j) {
+  const float4* t = reinterpret_cast<const float4*>(table) + 4 * (size_t)j;
+  NodeXf x;
+  x.a = __ldg(t);
+  x.b = __ldg(t + 1);
+  x.c = __ldg(t + 2);
+  x.d = __ldg(t + 3);
+  return x;
+}
+
+// w * (R (p - g) + t + g), the summand of DeformGraph::predict_mesh
+// (Deform.hpp:238-246).
+__device__ __forceinline__ void ed_term(const NodeXf& x, float w, float px, float py, float pz,
+                                        float& ox, float& oy, float& oz) {
+  const float dx = px - x.c.y, dy = py - x.c.z, dz = pz - x.c.w;
+  const float mx = fmaf(x.a.x, dx, fmaf(x.a.y, dy, x.a.z * dz)) + x.d.x;
+  const float my = fmaf(x.a.w, dx, fmaf(x.b.x, dy, x.b.y * dz)) + x.d.y;
+  const float mz = fmaf(x.b.z, dx, fmaf(x.b.w, dy, x.c.x * dz)) + x.d.z;
+  ox = fmaf(w, mx, ox);
+  oy = fmaf(w, my, oy);
+  oz = fmaf(w, mz, oz);
+}
+
+__global__ void node_table_kernel(int n, const float* __restrict__ rot,
+                                  const float* __restrict__ trans,
+                                  const float* __restrict__ pos, float* __restrict__ table) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= n) return;
+  const float* r = rot + 9 * (size_t)j;  // column-major
+  float4* t = reinterpret_cast<float4*>(table) + 4 * (size_t)j;
+  const float gx = pos[3 * (size_t)j], gy = pos[3 * (size_t)j + 1], gz = pos[3 * (size_t)j + 2];
+  const double cx = (double)trans[3 * (size_t)j] + gx;
+  const double cy = (double)trans[3 * (size_t)j + 1] + gy;
+  const double cz = (double)trans[3 * (size_t)j + 2] + gz;
+  t[0] = make_float4(r[0], r[3], r[6], r[1]);
+  t[1] = make_float4(r[4], r[7], r[2], r[5]);
+  t[2] = make_float4(r[8], gx, gy, gz);
+  t[3] = make_float4((float)cx, (float)cy, (float)cz, 0.f);
+}
+
+// GetEndPoints (GaussianView.cpp:4643-4668).
+__global__ void end_points_kernel(int N, const float* __restrict__ pos,
+                                  const float* __restrict__ rot, const float* __restrict__ scale,
+                                  float* __restrict__ ends, float* __restrict__ ends_xyz) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= N) return;
+  const float4 q = quat_normalize(__ldg(reinterpret_cast<const float4*>(rot) + i));
+  float R[9];
+  quat_to_rowmajor(q, R);
+  const float mu[3] = {pos[3 * (size_t)i], pos[3 * (size_t)i + 1], pos[3 * (size_t)i + 2]};
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    const float h = (scale[3 * (size_t)i + a] + 1e-3f) * 2.0f;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const float e = R[c * 3 + a] * h;
+      const float plus = mu[c] + e, minus = mu[c] - e;
+      ends[(size_t)(3 * (2 * a) + c) * N + i] = plus;
+      ends[(size_t)(3 * (2 * a + 1) + c) * N + i] = minus;
+      if (ends_xyz) {
+        ends_xyz[((size_t)(2 * a) * N + i) * 3 + c] = plus;
+        ends_xyz[((size_t)(2 * a + 1) * N + i) * 3 + c] = minus;
+      }
+    }
+  }
+}
+
+// Fused UpdatePosition (endpoint part, GaussianView.cpp:3022-3040) and
+// UpdateAsSixPointsWithdrawBad (GaussianView.cpp:3081-3166).
+template <int K, bool MIXED>
+__global__ void __launch_bounds__(kSkinThreads)
+    skin_gaussians_kernel(int N, float* __restrict__ ends, const int32_t* __restrict__ eidx,
+                          const float* __restrict__ ew, const float* __restrict__ table,
+                          const float* __restrict__ scale0, const uint8_t* __restrict__ static_mask,
+                          float* __restrict__ pos_out, float* __restrict__ rot_inout,
+                          float* __restrict__ scale_out, float* __restrict__ shs,
+                          float* __restrict__ cov_out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= N) return;
+  float e[18];
+#pragma unroll
+  for (int c = 0; c < 18; ++c) e[c] = __ldcs(ends + (size_t)c * N + i);
+#pragma unroll
+  for (int ep = 0; ep < 6; ++ep) {
+    float ox = 0.f, oy = 0.f, oz = 0.f;
+#pragma unroll
+    for (int j = 0; j < K; ++j) {
+      const size_t o = (size_t)(j * 6 + ep) * N + i;
+      const int nid = __ldcs(eidx + o);
+      const float w = __ldcs(ew + o);
+      const NodeXf x = load_node(table, nid);
+      ed_term(x, w, e[3 * ep], e[3 * ep + 1], e[3 * ep + 2], ox, oy, oz);
+    }
+    e[3 * ep] = ox;
+    e[3 * ep + 1] = oy;
+    e[3 * ep + 2] = oz;
+  }
+#pragma unroll
+  for (int c = 0; c < 18; ++c) __stcs(ends + (size_t)c * N + i, e[c]);
+  if (static_mask && static_mask[i]) return;
+
+  float cx = 0.f, cy = 0.f, cz = 0.f;
+#pragma unroll
+  for (int ep = 0; ep < 6; ++ep) {
+    cx += e[3 * ep];
+    cy += e[3 * ep + 1];
+    cz += e[3 * ep + 2];
+  }
+  cx *= (1.0f / 6.0f);
+  cy *= (1.0f / 6.0f);
+  cz *= (1.0f / 6.0f);
+  // M = (P - c) Q^+ with Q = [e0 -e0 e1 -e1 e2 -e2], Q^+ = Q^T / 2:
+  // column a of M is (P_{2a} - P_{2a+1}) / 2.
+  float M[9];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+#pragma unroll
+    for (int r = 0; r < 3; ++r) M[r * 3 + a] = 0.5f * (e[3 * (2 * a) + r] - e[3 * (2 * a + 1) + r]);
+  }
+  float R[9];
+  bool ok;
+  if (MIXED) {
+    // FP64 polar factor when M is ill-conditioned (sigma_min/sigma_max < 1e-3)
+    float nx = 0.f, ny = 0.f, Y[9];
+    ok = inv_transpose3(M, Y);
+#pragma unroll
+    for (int t = 0; t < 9; ++t) {
+      nx += M[t] * M[t];
+      ny += Y[t] * Y[t];
+    }
+    if (!ok || nx * ny > 1e6f) {
+      double Md[9], Rd[9];
+#pragma unroll
+      for (int t = 0; t < 9; ++t) Md[t] = M[t];
+      ok = polar_factor<double>(Md, Rd, 40, 1e-15);
+#pragma unroll
+      for (int t = 0; t < 9; ++t) R[t] = (float)Rd[t];
+    } else {
+      ok = polar_factor<float>(M, R, 20, 2e-7f);
+    }
+  } else {
+    ok = polar_factor<float>(M, R, 20, 2e-7f);
+  }
+  if (!ok) raise_status(ARAP_ENONFINITE);
+  // K = diag(R^T M) = diag(V S V^T)
+  float Kd[3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) Kd[a] = R[a] * M[a] + R[3 + a] * M[3 + a] + R[6 + a] * M[6 + a];
+  const float4 q = quat_normalize(quat_from_rowmajor(R));
+  float s[3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    const float s0 = scale0[3 * (size_t)i + a];
+    s[a] = Kd[a] / ((s0 + 1e-3f) * 2.0f) * s0;
+  }
+  pos_out[3 * (size_t)i] = cx;
+  pos_out[3 * (size_t)i + 1] = cy;
+  pos_out[3 * (size_t)i + 2] = cz;
+  scale_out[3 * (size_t)i] = s[0];
+  scale_out[3 * (size_t)i + 1] = s[1];
+  scale_out[3 * (size_t)i + 2] = s[2];
+  float4* rq = reinterpret_cast<float4*>(rot_inout) + i;
+  const float4 q_old = *rq;
+  *rq = q;
+  if (shs) {
+    const float4 qr = quat_normalize(quat_mul(q, quat_inverse(q_old)));
+    float Rr[9];
+    quat_to_rowmajor(qr, Rr);
+    float4* sp = reinterpret_cast<float4*>(shs + 48 * (size_t)i);
+    float v[48];
+#pragma unroll
+    for (int t = 0; t < 12; ++t) {
+      const float4 u = __ldcs(sp + t);
+      v[4 * t] = u.x;
+      v[4 * t + 1] = u.y;
+      v[4 * t + 2] = u.z;
+      v[4 * t + 3] = u.w;
+    }
+    rotate_sh48<true>(Rr, v);
+#pragma unroll
+    for (int t = 0; t < 12; ++t) __stcs(sp + t, make_float4(v[4 * t], v[4 * t + 1], v[4 * t + 2], v[4 * t + 3]));
+  }
+  if (cov_out) {
+    float Rq[9];
+    quat_to_rowmajor(q, Rq);
+    const float s2[3] = {s[0] * s[0], s[1] * s[1], s[2] * s[2]};
+    float S[6];
+    int o = 0;
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+#pragma unroll
+      for (int c = r; c < 3; ++c)
+        S[o++] = Rq[r * 3] * s2[0] * Rq[c * 3] + Rq[r * 3 + 1] * s2[1] * Rq[c * 3 + 1] +
+                 Rq[r * 3 + 2] * s2[2] * Rq[c * 3 + 2];
+#pragma unroll
+    for (int t = 0; t < 6; ++t) cov_out[6 * (size_t)i + t] = S[t];
+  }
+}
+
+// Per-node quaternion of the polar factor (GaussianView.cpp:3172-3181).
+template <bool MIXED>
+__global__ void node_quat_kernel(int n, const float* __restrict__ rot, float* __restrict__ quat) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= n) return;
+  const float* r = rot + 9 * (size_t)j;
+  float M[9] = {r[0], r[3], r[6], r[1], r[4], r[7], r[2], r[5], r[8]};
+  bool ok;
+  if (MIXED) {
+    // FP64 Newton when the smallest singular value is tiny (|det| / |M|^3 small)
+    float nrm = 0.f;
+#pragma unroll
+    for (int t = 0; t < 9; ++t) nrm += M[t] * M[t];
+    const float det = det3(M);
+    if (fabsf(det) < 1e-6f * nrm * sqrtf(nrm)) {
+      double Md[9];
+#pragma unroll
+      for (int t = 0; t < 9; ++t) Md[t] = M[t];
+      ok = newton_polar_ref<double>(Md, 200);
+#pragma unroll
+      for (int t = 0; t < 9; ++t) M[t] = (float)Md[t];
+    } else {
+      ok = newton_polar_ref<float>(M, 100);
+    }
+  } else {
+    ok = newton_polar_ref<float>(M, 100);
+  }
+  if (!ok) raise_status(ARAP_ENONFINITE);
+  const float4 q = quat_normalize(quat_from_rowmajor(M));
+  reinterpret_cast<float4*>(quat)[j] = q;
+}
+
+// Q_SlerpCUDA (cudakdtree.cu:113-148) in float32; the cosine is the float32
+// dot in the reference's (x,y,z,w) order.
+__device__ __forceinline__ float4 slerp(float4 s, float4 e, float t) {
+  float c = __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(s.y, e.y), __fmul_rn(s.z, e.z)), __fmul_rn(s.w, e.w)),
+                      __fmul_rn(s.x, e.x));
+  if (c < 0.f) {
+    e = make_float4(-e.x, -e.y, -e.z, -e.w);
+    c = -c;
+  }
+  float ra, rb;
+  if (c > 0.99995f) {
+    ra = 1.0f - t;
+    rb = t;
+  } else {
+    const float sa = sqrtf(1.0f - c * c);
+    const float ang = atan2f(sa, c);
+    const float inv = 1.0f / sa;
+    ra = sinf((1.0f - t) * ang) * inv;
+    rb = sinf(t * ang) * inv;
+  }
+  return quat_normalize(make_float4(ra * s.x + rb * e.x, ra * s.y + rb * e.y, ra * s.z + rb * e.z,
+                                    ra * s.w + rb * e.w));
+}
+
+// Fused UpdatePositionforSamples (GaussianView.cpp:3060-3077) and RotateSHs
+// (cudakdtree.cu:201-222).
+template <int K>
+__global__ void __launch_bounds__(kSkinThreads)
+    skin_samples_kernel(int S, float* __restrict__ spos, const int32_t* __restrict__ idx,
+                        const float* __restrict__ w, const float* __restrict__ table,
+                        const float* __restrict__ nquat, float* __restrict__ feature,
+                        const uint8_t* __restrict__ static_mask) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= S) return;
+  if (static_mask && static_mask[i]) return;
+  const float px = spos[3 * (size_t)i], py = spos[3 * (size_t)i + 1], pz = spos[3 * (size_t)i + 2];
+  float ox = 0.f, oy = 0.f, oz = 0.f;
+  float4 wq = make_float4(1.f, 0.f, 0.f, 0.f);
+  float last = 0.f;
+#pragma unroll
+  for (int j = 0; j < K; ++j) {
+    const int nid = __ldcs(idx + (size_t)j * S + i);
+    const float wj = __ldcs(w + (size_t)j * S + i);
+    const NodeXf x = load_node(table, nid);
+    ed_term(x, wj, px, py, pz, ox, oy, oz);
+    if (feature) {
+      const float t = wj / (wj + last);
+      wq = slerp(wq, __ldg(reinterpret_cast<const float4*>(nquat) + nid), t);
+      last += wj;
+    }
+  }
+  spos[3 * (size_t)i] = ox;
+  spos[3 * (size_t)i + 1] = oy;
+  spos[3 * (size_t)i + 2] = oz;
+  if (feature) {
+    float Rr[9];
+    quat_to_rowmajor(quat_normalize(wq), Rr);
+    float4* fp = reinterpret_cast<float4*>(feature + 48 * (size_t)i);
+    float v[48];
+#pragma unroll
+    for (int t = 0; t < 12; ++t) {
+      const float4 u = __ldcs(fp + t);
+      v[4 * t] = u.x;
+      v[4 * t + 1] = u.y;
+      v[4 * t + 2] = u.z;
+      v[4 * t + 3] = u.w;
+    }
+    rotate_sh48<true>(Rr, v);
+#pragma unroll
+    for (int t = 0; t < 12; ++t) __stcs(fp + t, make_float4(v[4 * t], v[4 * t + 1], v[4 * t + 2], v[4 * t + 3]));
+  }
+}
+
+// GaussianView.cpp:3042-3052: next node position from its anchor kNN.
+__global__ void update_nodes_kernel(int n, int k, const float* __restrict__ pos,
+                                    const int32_t* __restrict__ aidx, const float* __restrict__ aw,
+                                    const float* __restrict__ table, float* __restrict__ out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float px = pos[3 * (size_t)i], py = pos[3 * (size_t)i + 1], pz = pos[3 * (size_t)i + 2];
+  float ox = 0.f, oy = 0.f, oz = 0.f;
+  for (int j = 0; j < k; ++j) {
+    const NodeXf x = load_node(table, aidx[(size_t)j * n + i]);
+    ed_term(x, aw[(size_t)j * n + i], px, py, pz, ox, oy, oz);
+  }
+  out[3 * (size_t)i] = ox;
+  out[3 * (size_t)i + 1] = oy;
+  out[3 * (size_t)i + 2] = oz;
+}
+
+__global__ void static_mask_kernel(int P, int planes, const int32_t* __restrict__ idx,
+                                   const uint8_t* __restrict__ node_static, uint8_t* __restrict__ out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= P) return;
+  uint8_t all = 1;
+  for (int p = 0; p < planes; ++p) all &= node_static[idx[(size_t)p * P + i]] ? 1 : 0;
+  out[i] = all;
+}
+
+// ---------------------------------------------------- control targets ----
+// One CTA; the centroid is summed in float64 over the listed nodes.
+__device__ void block_centroid(const float* __restrict__ pos, const int32_t* __restrict__ ids, int m,
+                               float* c) {
+  double v[3] = {0.0, 0.0, 0.0};
+  for (int t = threadIdx.x; t < m; t += blockDim.x) {
+    const int j = ids[t];
+    v[0] += pos[3 * (size_t)j];
+    v[1] += pos[3 * (size_t)j + 1];
+    v[2] += pos[3 * (size_t)j + 2];
+  }
+  block_sum<3>(v);
+  c[0] = (float)(v[0] / m);
+  c[1] = (float)(v[1] / m);
+  c[2] = (float)(v[2] / m);
+}
+
+// PointRotateByAxis (helper.cpp:1077-1100): rotation by `rad` about the unit
+// axis (x,y,z) through the point (a,b,c), the closed form of the rotation of a
+// point about an arbitrary line.
+__device__ __forceinline__ void rotate_about_line(float* p, const float* ctr, float ax, float ay,
+                                                  float az, float rad) {
+  const float ct = cosf(rad), st = sinf(rad);
+  const float nrm = sqrtf(ax * ax + ay * ay + az * az);
+  const float x = ax / nrm, y = ay / nrm, z = az / nrm;
+  const float a = ctr[0], b = ctr[1], c = ctr[2];
+  const float u = 1.0f - ct;
+  const float px = p[0], py = p[1], pz = p[2];
+  float o0 = (x * x * u + ct) * px + (x * y * u - z * st) * py + (x * z * u + y * st) * pz;
+  float o1 = (y * x * u + z * st) * px + (y * y * u + ct) * py + (y * z * u - x * st) * pz;
+  float o2 = (z * x * u - y * st) * px + (z * y * u + x * st) * py + (z * z * u + ct) * pz;
+  o0 += (a * (y * y + z * z) - x * (b * y + c * z)) * u + (b * z - c * y) * st;
+  o1 += (b * (x * x + z * z) - y * (a * x + c * z)) * u + (c * x - a * z) * st;
+  o2 += (c * (x * x + y * y) - z * (a * x + b * y)) * u + (a * y - b * x) * st;
+  p[0] = o0;
+  p[1] = o1;
+  p[2] = o2;
+}
+
+// op: 0 translate (v = delta), 1 twist (v = axis, s = radian), 2 scale (s).
+__global__ void aims_kernel(int op, float* __restrict__ aims, const float* __restrict__ pos,
+                            const int32_t* __restrict__ ids, int m, float v0, float v1, float v2,
+                            float s) {
+  __shared__ float ctr[3];
+  if (op != 0) {
+    float c[3];
+    block_centroid(pos, ids, m, c);
+    if (threadIdx.x == 0) {
+      ctr[0] = c[0];
+      ctr[1] = c[1];
+      ctr[2] = c[2];
+    }
+    __syncthreads();
+  }
+  for (int t = threadIdx.x; t < m; t += blockDim.x) {
+    const int j = ids[t];
+    bool first = true;
+    int reps = 0;
+    for (int u = 0; u < m; ++u) {
+      if (ids[u] == j) {
+        if (u < t) first = false;
+        ++reps;
+      }
+    }
+    if (!first) continue;
+    float p[3] = {aims[3 * (size_t)j], aims[3 * (size_t)j + 1], aims[3 * (size_t)j + 2]};
+    for (int r = 0; r < reps; ++r) {
+      if (op == 0) {
+        p[0] += v0;
+        p[1] += v1;
+        p[2] += v2;
+      } else if (op == 1) {
+        rotate_about_line(p, ctr, v0, v1, v2, s);
+      } else {
+        p[0] = ctr[0] + s * (p[0] - ctr[0]);
+        p[1] = ctr[1] + s * (p[1] - ctr[1]);
+        p[2] = ctr[2] + s * (p[2] - ctr[2]);
+      }
+    }
+    aims[3 * (size_t)j] = p[0];
+    aims[3 * (size_t)j + 1] = p[1];
+    aims[3 * (size_t)j + 2] = p[2];
+  }
+}
+
+template <int K>
+static void launch_skin_g(bool mixed, int N, float* ends, const int32_t* eidx, const float* ew,
+                          const float* table, const float* scale0, const uint8_t* st, float* pos,
+                          float* rot, float* scale, float* shs, float* cov, cudaStream_t s) {
+  const int grid = grid_for(N, kSkinThreads);
+  if (mixed)
+    skin_gaussians_kernel<K, true><<<grid, kSkinThreads, 0, s>>>(N, ends, eidx, ew, table, scale0, st,
+                                                                  pos, rot, scale, shs, cov);
+  else
+    skin_gaussians_kernel<K, false><<<grid, kSkinThreads, 0, s>>>(N, ends, eidx, ew, table, scale0, st,
+                                                                   pos, rot, scale, shs, cov);
+}
+
+template <int K>
+static void launch_skin_s(int S, float* spos, const int32_t* idx, const float* w, const float* table,
+                          const float* nq, float* feat, const uint8_t* st, cudaStream_t s) {
+  skin_samples_kernel<K><<<grid_for(S, kSkinThreads), kSkinThreads, 0, s>>>(S, spos, idx, w, table, nq,
+                                                                            feat, st);
+}
+
+}  // namespace arap
+
+using namespace arap;
+
+extern "C" int arap_node_table(int n, const float* rot, const float* trans, const float* node_pos,
+                               float* table_out, arap_stream_t stream) {
+  if (n <= 0 || !rot || !trans || !node_pos || !table_out) return n == 0 ? ARAP_OK : ARAP_EBADINPUT;
+  if (reinterpret_cast<uintptr_t>(table_out) & 15) return ARAP_EBADINPUT;
+  node_table_kernel<<<grid_for(n, 128), 128, 0, (cudaStream_t)stream>>>(n, rot, trans, node_pos, table_out);
+  ARAP_LAUNCH_CHECK();
+  return ARAP_OK;
+}
+
+extern "C" int arap_end_points(int N, const float* pos, const float* rot, const float* scale,
+                               float* ends_out, float* ends_xyz_out, arap_stream_t stream) {
+  if (N == 0) return ARAP_OK;
+  if (N < 0 || !pos || !rot || !scale || !ends_out) return ARAP_EBADINPUT;
+  if (reinterpret_cast<uintptr_t>(rot) & 15) return ARAP_EBADINPUT;
+  end_points_kernel<<<grid_for(N, 128), 128, 0, (cudaStream_t)stream>>>(N, pos, rot, scale, ends_out,
+                                                                         ends_xyz_out);
+  ARAP_LAUNCH_CHECK();
+  return ARAP_OK;
+}
+
+extern "C" int arap_skin_gaussians(int N, int k, float* ends, const int32_t* ends_idx,
+                                   const float* ends_w, const float* node_table, const float* scale0,
+                                   const uint8_t* static_mask, float* pos_out, float* rot_inout,
+                                   float* scale_out, float* shs_inout, float* cov_out, int precision,
+                                   arap_stream_t stream) {
+  if (N == 0) return ARAP_OK;
+  if (N < 0 || !ends || !ends_idx || !ends_w || !node_table || !scale0 || !pos_out || !rot_inout ||
+      !scale_out)
+    return ARAP_EBADINPUT;
+  if ((reinterpret_cast<uintptr_t>(node_table) | reinterpret_cast<uintptr_t>(rot_inout) |
+       reinterpret_cast<uintptr_t>(shs_inout)) & 15)
+    return ARAP_EBADINPUT;
+  const bool mixed = precision == ARAP_PRECISION_MIXED;
+  cudaStream_t s = (cudaStream_t)stream;
+  switch (k) {
+#define ARAP_SKG(K)                                                                                   \
+  case K:                                                                                             \
+    launch_skin_g<K>(mixed, N, ends, ends_idx, ends_w, node_table, scale0, static_mask, pos_out,      \
+                     rot_inout, scale_out, shs_inout, cov_out, s);                                    \
+    break;
+    ARAP_SKG(1) ARAP_SKG(2) ARAP_SKG(3) ARAP_SKG(4) ARAP_SKG(5) ARAP_SKG(6)
+    ARAP_SKG(7) ARAP_SKG(8) ARAP_SKG(9) ARAP_SKG(10) ARAP_SKG(11) ARAP_SKG(12)
+#undef ARAP_SKG
+    default:
+      return ARAP_EUNSUPPORTED;
+  }
+  ARAP_LAUNCH_CHECK();
+  return ARAP_OK;
+}
+
+extern "C" int arap_node_quaternions(int n, const float* rot, float* quat_out, int precision,
+                                     arap_stream_t stream) {
+  if (n == 0) return ARAP_OK;
+  if (n < 0 || !rot || !quat_out || (reinterpret_cast<uintptr_t>(quat_out) & 15)) return ARAP_EBADINPUT;
+  if (precision == ARAP_PRECISION_MIXED)
+    node_quat_kernel<true><<<grid_for(n, 128), 128, 0, (cudaStream_t)stream>>>(n, rot, quat_out);
+  else
+    node_quat_kernel<false><<<grid_for(n, 128), 128, 0, (cudaStream_t)stream>>>(n, rot, quat_out);
+  ARAP_LAUNCH_CHECK();
+  return ARAP_OK;
+}
+
+extern "C" int arap_skin_samples(int S, int k, float* sample_pos, const int32_t* idx, const float* w,
+                                 const float* node_table, const float* node_quat, float* feature,
+                                 const uint8_t* static_mask, arap_stream_t stream) {
+  if (S == 0) return ARAP_OK;
+  if (S < 0 || !sample_pos || !idx || !w || !node_table || (feature && !node_quat)) return ARAP_EBADINPUT;
+  if ((reinterpret_cast<uintptr_t>(node_table) | reinterpret_cast<uintptr_t>(node_quat) |
+       reinterpret_cast<uintptr_t>(feature)) & 15)
+    return ARAP_EBADINPUT;
+  cudaStream_t s = (cudaStream_t)stream;
+  switch (k) {
+#define ARAP_SKS(K)                                                                  \
+  case K:                                                                            \
+    launch_skin_s<K>(S, sample_pos, idx, w, node_table, node_quat, feature, static_mask, s); \
+    break;
+    ARAP_SKS(1) ARAP_SKS(2) ARAP_SKS(3) ARAP_SKS(4) ARAP_SKS(5) ARAP_SKS(6)
+    ARAP_SKS(7) ARAP_SKS(8) ARAP_SKS(9) ARAP_SKS(10) ARAP_SKS(11) ARAP_SKS(12)
+#undef ARAP_SKS
+    default:
+      return ARAP_EUNSUPPORTED;
+  }
+  ARAP_LAUNCH_CHECK();
+  return ARAP_OK;
+}
+
+extern "C" int arap_update_nodes(int n, int k, const float* node_pos, const int32_t* anchor_idx,
+                                 const float* anchor_w, const float* node_table, float* node_pos_out,
+                                 arap_stream_t stream) {
+  if (n == 0) return ARAP_OK;
+  if (n < 0 || k < 1 || k > ARAP_KNN_MAX || !node_pos || !anchor_idx || !anchor_w || !node_table ||
+      !node_pos_out || node_pos_out == node_pos)
+    return ARAP_EBADINPUT;
+  update_nodes_kernel<<<grid_for(n, 128), 128, 0, (cudaStream_t)stream>>>(n, k, node_pos, anchor_idx,
+                                                                          anchor_w, node_table, node_pos_out);
+  ARAP_LAUNCH_CHECK();
+  return ARAP_OK;
+}
+
+extern "C" int arap_static_mask(int P, int k, int groups, const int32_t* idx,
+                                const uint8_t* node_is_static, uint8_t* mask_out, arap_stream_t stream) {
+  if (P == 0) return ARAP_OK;
+  if (P < 0 || k < 1 || groups < 1 || !idx || !node_is_static || !mask_out) return ARAP_EBADINPUT;
+  static_mask_kernel<<<grid_for(P, 256), 256, 0, (cudaStream_t)stream>>>(P, k * groups, idx, node_is_static,
+                                                                         mask_out);
+  ARAP_LAUNCH_CHECK();
+  return ARAP_OK;
+}
+
+static int launch_aims(int op, float* aims, const float* pos, const int32_t* ids, int m, float a,
+                       float b, float c, float s, cudaStream_t st) {
+  if (m == 0) return ARAP_OK;
+  if (m < 0 || !aims || !ids || (op != 0 && !pos)) return ARAP_EBADINPUT;
+  aims_kernel<<<1, 256, 0, st>>>(op, aims, pos, ids, m, a, b, c, s);
+  ARAP_LAUNCH_CHECK();
+  return ARAP_OK;
+}
+
+extern "C" int arap_aims_translate(float* aims, const int32_t* active_nodes, int n_active, float dx,
+                                   float dy, float dz, arap_stream_t stream) {
+  return launch_aims(0, aims, nullptr, active_nodes, n_active, dx, dy, dz, 0.f, (cudaStream_t)stream);
+}
+
+extern "C" int arap_aims_twist(float* aims, const float* node_pos, const int32_t* active_nodes,
+                               int n_active, float ax, float ay, float az, float radian,
+                               arap_stream_t stream) {
+  if (!(ax * ax + ay * ay + az * az > 0.f)) return ARAP_EBADINPUT;
+  return launch_aims(1, aims, node_pos, active_nodes, n_active, ax, ay, az, radian, (cudaStream_t)stream);
+}
+
+extern "C" int arap_aims_scale(float* aims, const float* node_pos, const int32_t* active_nodes,
+                               int n_active, float s, arap_stream_t stream) {
+  return launch_aims(2, aims, node_pos, active_nodes, n_active, 0.f, 0.f, 0.f, s, (cudaStream_t)stream);
+}

@@ -1,0 +1,391 @@
+// Host side of the Gauss-Newton solver: solve-plan construction (the
+// bookkeeping of the Deform constructor, Deform.hpp:414-455 and
+// Deform.cpp:6-75) and the C ABI.
+#include <algorithm>
+#include <cstring>
+#include <new>
+#include <set>
+#include <vector>
+
+#include "solver_kernel.cuh"
+
+using namespace arap;
+
+struct arap_solver {
+  int n = 0, k = 0, F = 0, S = 0, G = 0, U = 0, n_items = 0, n_rows = 0;
+  arap_solve_config cfg{};
+  int grid = 0;
+  void* block = nullptr;  // one device allocation holding everything below
+  SolveParams P{};
+  std::vector<int32_t> free_host;
+};
+
+namespace {
+
+struct Carver {
+  char* base;
+  size_t off = 0;
+  template <typename T>
+  T* take(size_t count) {
+    off = (off + 255) & ~size_t(255);
+    T* p = reinterpret_cast<T*>(base ? base + off : nullptr);
+    off += sizeof(T) * (count ? count : 1);
+    return p;
+  }
+};
+
+int bits_of(float f) {
+  int i;
+  std::memcpy(&i, &f, sizeof(i));
+  return i;
+}
+
+template <typename RT>
+int occupancy_grid(int per_sm_cap) {
+  int dev = 0, sms = 0, per_sm = 0, coop = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return -1;
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return -1;
+  if (cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev) != cudaSuccess || !coop) return -1;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, gn_solve_kernel<RT>, kSolveThreads, 0) !=
+      cudaSuccess)
+    return -1;
+  if (per_sm < 1) return -1;
+  return sms * std::min(per_sm, per_sm_cap);
+}
+
+}  // namespace
+
+extern "C" int arap_solver_create(arap_solver** out, int n, int k, const int32_t* neighbors,
+                                  const int32_t* anchor_idx, const float* anchor_w,
+                                  const int32_t* block_offsets_host, const int32_t* block_nodes_host,
+                                  const int32_t* block_type_host, int n_blocks,
+                                  const arap_solve_config* cfg_in, arap_stream_t stream) {
+  if (!out) return ARAP_EBADINPUT;
+  *out = nullptr;
+  if (n < 2 || k < 1 || k > ARAP_KNN_MAX || !neighbors || !anchor_idx || !anchor_w || n_blocks < 0 ||
+      (n_blocks > 0 && (!block_offsets_host || !block_nodes_host || !block_type_host)))
+    return ARAP_EBADINPUT;
+  arap_solve_config cfg;
+  if (cfg_in)
+    cfg = *cfg_in;
+  else
+    arap_solve_config_default(&cfg);
+  if (cfg.max_iters < 0) return ARAP_EBADINPUT;
+  cudaStream_t st = (cudaStream_t)stream;
+
+  // inputs to host
+  std::vector<int32_t> nb((size_t)n * k), aidx((size_t)n * k);
+  std::vector<float> aw((size_t)n * k);
+  ARAP_CUDA_TRY(cudaMemcpyAsync(nb.data(), neighbors, nb.size() * 4, cudaMemcpyDeviceToHost, st));
+  ARAP_CUDA_TRY(cudaMemcpyAsync(aidx.data(), anchor_idx, aidx.size() * 4, cudaMemcpyDeviceToHost, st));
+  ARAP_CUDA_TRY(cudaMemcpyAsync(aw.data(), anchor_w, aw.size() * 4, cudaMemcpyDeviceToHost, st));
+  ARAP_CUDA_TRY(cudaStreamSynchronize(st));
+  for (size_t i = 0; i < nb.size(); ++i)
+    if (nb[i] < 0 || nb[i] >= n || aidx[i] < 0 || aidx[i] >= n) return ARAP_EBADINPUT;
+  std::vector<std::vector<int32_t>> blocks(n_blocks);
+  for (int b = 0; b < n_blocks; ++b) {
+    const int a0 = block_offsets_host[b], a1 = block_offsets_host[b + 1];
+    if (a0 < 0 || a1 < a0) return ARAP_EBADINPUT;
+    for (int a = a0; a < a1; ++a) {
+      if (block_nodes_host[a] < 0 || block_nodes_host[a] >= n) return ARAP_EBADINPUT;
+      blocks[b].push_back(block_nodes_host[a]);
+    }
+  }
+
+  // free / static sets (UpdateIndicies, GaussianView.cpp:2010-2035)
+  std::vector<char> is_static(n, 0);
+  for (int b = 0; b < n_blocks; ++b)
+    if (block_type_host[b] < 0)
+      for (int v : blocks[b]) is_static[v] = 1;
+  std::vector<int32_t> rank(n, -1), free_ids;
+  for (int i = 0; i < n; ++i)
+    if (!is_static[i]) {
+      rank[i] = (int32_t)free_ids.size();
+      free_ids.push_back(i);
+    }
+  const int F = (int)free_ids.size();
+  const int S = n - F;
+  if (F == 0) return ARAP_EBADINPUT;
+
+  // block membership for BelongsToSameBlock (Deform.cpp:20-32)
+  std::vector<std::vector<int>> node_blocks(n);
+  for (int b = 0; b < n_blocks; ++b)
+    if (block_type_host[b] != -1)
+      for (int v : blocks[b])
+        if (node_blocks[v].empty() || node_blocks[v].back() != b) node_blocks[v].push_back(b);
+  auto same_block = [&](int i, int j) {
+    for (int a : node_blocks[i])
+      for (int b : node_blocks[j])
+        if (a == b) return true;
+    return false;
+  };
+  const float wf = cfg.weighting_factor;
+
+  // constraint groups (Deform.cpp:299-371 / 484-580)
+  std::vector<int32_t> grp_off{0}, grp_member, tsrc_off{0}, tsrc;
+  std::vector<float> grp_mult;
+  for (int b = 0; b < n_blocks; ++b) {
+    if (block_type_host[b] == -1) continue;
+    if (!cfg.cons_on_center) {
+      for (int c : blocks[b]) {
+        grp_member.push_back(c);
+        grp_off.push_back((int32_t)grp_member.size());
+        tsrc.push_back(c);
+        tsrc_off.push_back((int32_t)tsrc.size());
+        grp_mult.push_back(1.f);
+      }
+    } else {
+      // SelectKeyControls (Deform.cpp:34-75): the first min(20,|block|) ids,
+      // as a set; the target is the mean of their aims
+      const int m = std::min<int>(20, (int)blocks[b].size());
+      if (m == 0) continue;
+      std::set<int32_t> sel(blocks[b].begin(), blocks[b].begin() + m);
+      for (int c : sel) grp_member.push_back(c);
+      grp_off.push_back((int32_t)grp_member.size());
+      for (int a = 0; a < m; ++a) tsrc.push_back(blocks[b][a]);
+      tsrc_off.push_back((int32_t)tsrc.size());
+      grp_mult.push_back((float)sel.size());
+    }
+  }
+  const int G = (int)grp_mult.size();
+  const int U = (int)grp_member.size();
+  std::vector<int32_t> mem_rank((size_t)U * k), mem_node((size_t)U * k);
+  std::vector<float> mem_w((size_t)U * k);
+  for (int u = 0; u < U; ++u)
+    for (int t = 0; t < k; ++t) {
+      const int c = grp_member[u];
+      const int l = aidx[(size_t)t * n + c];
+      mem_node[(size_t)u * k + t] = l;
+      mem_rank[(size_t)u * k + t] = rank[l];
+      mem_w[(size_t)u * k + t] = aw[(size_t)t * n + c];
+    }
+
+  // coupling items per free node
+  std::vector<std::vector<int4>> items(F);
+  for (int r = 0; r < F; ++r) {
+    const int j = free_ids[r];
+    for (int t = 0; t < k; ++t) {
+      const int kn = nb[(size_t)j * k + t];
+      items[r].push_back(make_int4(ITEM_OUT, rank[kn], kn, bits_of(same_block(j, kn) ? wf : 1.f)));
+    }
+  }
+  for (int i = 0; i < n; ++i)
+    for (int t = 0; t < k; ++t) {
+      const int j = nb[(size_t)i * k + t];
+      if (rank[j] < 0) continue;
+      if (rank[i] >= 0)
+        items[rank[j]].push_back(make_int4(ITEM_IN, rank[i], i, bits_of(same_block(i, j) ? wf : 1.f)));
+      else
+        items[rank[j]].push_back(make_int4(ITEM_STATIC, -1, i, 0));
+    }
+  for (int g = 0; g < G; ++g)
+    for (int u = grp_off[g]; u < grp_off[g + 1]; ++u)
+      for (int t = 0; t < k; ++t) {
+        const int l = mem_node[(size_t)u * k + t];
+        if (rank[l] >= 0) items[rank[l]].push_back(make_int4(ITEM_CON, u * k + t, g, 0));
+      }
+  std::vector<int32_t> item_off(F + 1, 0);
+  std::vector<int4> item_flat;
+  for (int r = 0; r < F; ++r) {
+    auto& v = items[r];
+    std::stable_sort(v.begin(), v.end(), [](const int4& a, const int4& b) {
+      if (a.x != b.x) return a.x < b.x;
+      if (a.x == ITEM_CON) return a.z < b.z;
+      return false;
+    });
+    item_flat.insert(item_flat.end(), v.begin(), v.end());
+    item_off[r + 1] = (int32_t)item_flat.size();
+  }
+
+  auto* s = new (std::nothrow) arap_solver();
+  if (!s) return ARAP_ENOMEM;
+  s->n = n;
+  s->k = k;
+  s->F = F;
+  s->S = S;
+  s->G = G;
+  s->U = U;
+  s->n_items = (int)item_flat.size();
+  s->n_rows = F * (6 + 3 * k) + S * 3 * k + 3 * G;
+  s->cfg = cfg;
+  s->free_host = free_ids;
+  if (s->cfg.pcg_tol <= 0.f) s->cfg.pcg_tol = cfg.precision == ARAP_PRECISION_MIXED ? 1e-6f : 1e-6f;
+  if (s->cfg.pcg_max_iters <= 0) s->cfg.pcg_max_iters = 2000;
+  const int grid = cfg.precision == ARAP_PRECISION_MIXED ? occupancy_grid<double>(2) : occupancy_grid<float>(2);
+  if (grid <= 0) {
+    delete s;
+    return ARAP_ECUDA;
+  }
+  s->grid = grid;
+
+  // device layout
+  auto carve = [&](Carver& cv, SolveParams& P) {
+    P.free_ids = cv.take<int32_t>(F);
+    P.rank = cv.take<int32_t>(n);
+    P.item_off = cv.take<int32_t>(F + 1);
+    P.items = cv.take<int4>(item_flat.size());
+    P.grp_off = cv.take<int32_t>(G + 1);
+    P.grp_member = cv.take<int32_t>(U);
+    P.grp_mult = cv.take<float>(G);
+    P.tsrc_off = cv.take<int32_t>(G + 1);
+    P.tsrc = cv.take<int32_t>(tsrc.size());
+    P.mem_rank = cv.take<int32_t>((size_t)U * k);
+    P.mem_node = cv.take<int32_t>((size_t)U * k);
+    P.mem_w = cv.take<float>((size_t)U * k);
+    P.mem_geo = cv.take<float4>((size_t)U * k);
+    P.grp_target = cv.take<float4>(G);
+    P.x = cv.take<double>((size_t)F * 12);
+    P.xf = cv.take<float>((size_t)F * 12);
+    P.h = cv.take<float>((size_t)F * 12);
+    P.r = cv.take<float>((size_t)F * 12);
+    P.z = cv.take<float>((size_t)F * 12);
+    P.p0 = cv.take<float>((size_t)F * 12);
+    P.p1 = cv.take<float>((size_t)F * 12);
+    P.q = cv.take<float>((size_t)F * 12);
+    P.g = cv.take<float>((size_t)F * 12);
+    P.dinv = cv.take<float>((size_t)F * 144);
+    P.partials = cv.take<double>((size_t)8 * grid);
+    P.results = cv.take<double>(8);
+    P.stats = cv.take<double>(8);
+    P.bar = cv.take<GridBarrier>(1);
+  };
+  Carver sizing{nullptr};
+  SolveParams dummy{};
+  carve(sizing, dummy);
+  if (cudaMalloc(&s->block, sizing.off + 256) != cudaSuccess) {
+    (void)cudaGetLastError();
+    delete s;
+    return ARAP_ENOMEM;
+  }
+  Carver cv{static_cast<char*>(s->block)};
+  SolveParams& P = s->P;
+  carve(cv, P);
+  auto up = [&](const void* dst, const void* src, size_t bytes) {
+    return bytes ? cudaMemcpyAsync(const_cast<void*>(dst), src, bytes, cudaMemcpyHostToDevice, st) : cudaSuccess;
+  };
+  cudaError_t e = cudaSuccess;
+  e = e ? e : up(P.free_ids, free_ids.data(), free_ids.size() * 4);
+  e = e ? e : up(P.rank, rank.data(), rank.size() * 4);
+  e = e ? e : up(P.item_off, item_off.data(), item_off.size() * 4);
+  e = e ? e : up(P.items, item_flat.data(), item_flat.size() * sizeof(int4));
+  e = e ? e : up(P.grp_off, grp_off.data(), grp_off.size() * 4);
+  e = e ? e : up(P.grp_member, grp_member.data(), grp_member.size() * 4);
+  e = e ? e : up(P.grp_mult, grp_mult.data(), grp_mult.size() * 4);
+  e = e ? e : up(P.tsrc_off, tsrc_off.data(), tsrc_off.size() * 4);
+  e = e ? e : up(P.tsrc, tsrc.data(), tsrc.size() * 4);
+  e = e ? e : up(P.mem_rank, mem_rank.data(), mem_rank.size() * 4);
+  e = e ? e : up(P.mem_node, mem_node.data(), mem_node.size() * 4);
+  e = e ? e : up(P.mem_w, mem_w.data(), mem_w.size() * 4);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) {
+    cudaFree(s->block);
+    delete s;
+    return ARAP_ECUDA;
+  }
+  P.n = n;
+  P.k = k;
+  P.F = F;
+  P.G = G;
+  P.U = U;
+  P.wr = sqrtf(cfg.w_rot);
+  P.wg = sqrtf(cfg.w_reg);
+  P.wc = sqrtf(cfg.w_con);
+  P.wf = wf;
+  P.max_iters = cfg.max_iters;
+  P.early_exit = cfg.early_exit;
+  P.pcg_max = s->cfg.pcg_max_iters;
+  P.pcg_tol = s->cfg.pcg_tol;
+  P.mode = 0;
+  P.refine = 0;
+  *out = s;
+  return ARAP_OK;
+}
+
+static int launch_solver(arap_solver* s, cudaStream_t st) {
+  if (cudaMemsetAsync(s->P.bar, 0, sizeof(GridBarrier), st) != cudaSuccess) return ARAP_ECUDA;
+  void* args[] = {&s->P};
+  cudaError_t e;
+  if (s->cfg.precision == ARAP_PRECISION_MIXED)
+    e = cudaLaunchCooperativeKernel((const void*)gn_solve_kernel<double>, s->grid, kSolveThreads, args, 0, st);
+  else
+    e = cudaLaunchCooperativeKernel((const void*)gn_solve_kernel<float>, s->grid, kSolveThreads, args, 0, st);
+  if (e != cudaSuccess) {
+    (void)cudaGetLastError();
+    return ARAP_ECUDA;
+  }
+  return ARAP_OK;
+}
+
+extern "C" int arap_solver_solve(arap_solver* s, const float* node_pos, const float* aims, float* rot_out,
+                                 float* trans_out, arap_solve_stats* stats_host, arap_stream_t stream) {
+  if (!s || !node_pos || !aims || !rot_out || !trans_out) return ARAP_EBADINPUT;
+  cudaStream_t st = (cudaStream_t)stream;
+  s->P.node_pos = node_pos;
+  s->P.aims = aims;
+  s->P.rot_out = rot_out;
+  s->P.trans_out = trans_out;
+  s->P.mode = 0;
+  s->P.x_in = nullptr;
+  s->P.grad_out = nullptr;
+  int rc = launch_solver(s, st);
+  if (rc != ARAP_OK) return rc;
+  if (!stats_host) return ARAP_OK;
+  double st8[8];
+  ARAP_CUDA_TRY(cudaMemcpyAsync(st8, s->P.stats, sizeof(st8), cudaMemcpyDeviceToHost, st));
+  const int dev_status = arap_get_device_status(stream);  // synchronises
+  std::memset(stats_host, 0, sizeof(*stats_host));
+  stats_host->gn_iterations = (int)st8[ST_ITERS];
+  stats_host->pcg_iterations = (int)st8[ST_PCG];
+  stats_host->halvings = (int)st8[ST_HALV];
+  stats_host->initial_energy = st8[ST_E0];
+  stats_host->final_energy = st8[ST_E];
+  stats_host->n_free = s->F;
+  stats_host->n_static = s->S;
+  stats_host->n_rows = s->n_rows;
+  int status = dev_status;
+  if (status == ARAP_OK && s->cfg.early_exit && st8[ST_CONV] == 0.0 && s->cfg.max_iters > 0)
+    status = ARAP_NOT_CONVERGED;
+  stats_host->status = status;
+  return status == ARAP_NOT_CONVERGED ? ARAP_OK : status;
+}
+
+extern "C" int arap_solver_energy_grad(arap_solver* s, const float* node_pos, const float* aims, const double* x,
+                                       double* grad_out, double* energy_host, arap_stream_t stream) {
+  if (!s || !node_pos || !aims || !x || !grad_out) return ARAP_EBADINPUT;
+  cudaStream_t st = (cudaStream_t)stream;
+  SolveParams saved = s->P;
+  s->P.node_pos = node_pos;
+  s->P.aims = aims;
+  s->P.mode = 1;
+  s->P.x_in = x;
+  s->P.grad_out = grad_out;
+  s->P.max_iters = 1;
+  int rc = launch_solver(s, st);
+  const SolveParams used = s->P;
+  s->P = saved;
+  s->P.node_pos = used.node_pos;
+  s->P.aims = used.aims;
+  if (rc != ARAP_OK) return rc;
+  if (energy_host) {
+    double st8[8];
+    ARAP_CUDA_TRY(cudaMemcpyAsync(st8, used.stats, sizeof(st8), cudaMemcpyDeviceToHost, st));
+    const int dev_status = arap_get_device_status(stream);
+    *energy_host = st8[ST_E];
+    return dev_status;
+  }
+  return ARAP_OK;
+}
+
+extern "C" int arap_solver_free_count(const arap_solver* s) { return s ? s->F : -1; }
+
+extern "C" int arap_solver_free_ids(const arap_solver* s, int32_t* free_ids_host) {
+  if (!s || !free_ids_host) return ARAP_EBADINPUT;
+  std::memcpy(free_ids_host, s->free_host.data(), s->free_host.size() * 4);
+  return ARAP_OK;
+}
+
+extern "C" void arap_solver_destroy(arap_solver* s) {
+  if (!s) return;
+  if (s->block) cudaFree(s->block);
+  delete s;
+}

@@ -1,0 +1,63 @@
+// Plan and parameter layout of the persistent Gauss-Newton / PCG solver.
+#pragma once
+
+#include "arap_common.cuh"
+
+namespace arap {
+
+// Coupling items of one free node j (all rows of J that touch x_j besides its
+// own rotation rows).  int4 {kind, a, b, c}:
+//   ITEM_OUT    regularisation rows (j -> k), k = Neighbor[t] of j
+//               a = free rank of k (-1 if static), b = node k, c = bits(scale)
+//   ITEM_IN     regularisation rows (i -> j) of a free node i
+//               a = free rank of i, b = node i, c = bits(scale)
+//   ITEM_STATIC rows (i -> j) of a static node i: f = -w t_j
+//               a = -1, b = node i, c = 0
+//   ITEM_CON    constraint group g whose member anchors contain j
+//               a = member-anchor slot (u*k + t), b = g, c = 0
+enum { ITEM_OUT = 0, ITEM_IN = 1, ITEM_STATIC = 2, ITEM_CON = 3 };
+
+struct SolveParams {
+  int n, k, F, G, U;
+  const int32_t* free_ids;   // [F]
+  const int32_t* rank;       // [n]
+  const int32_t* item_off;   // [F+1]
+  const int4* items;         // [n_items]
+  const int32_t* grp_off;    // [G+1] member slots per group
+  const int32_t* grp_member; // [U] node id of member u
+  const float* grp_mult;     // [G] number of members (|S_b| or 1)
+  const int32_t* tsrc_off;   // [G+1] target sources per group
+  const int32_t* tsrc;       // aims indices (first min(20,|b|) block entries, or the node)
+  const int32_t* mem_rank;   // [U*k] free rank of anchor l (-1 when not free)
+  const int32_t* mem_node;   // [U*k] anchor node l
+  const float* mem_w;        // [U*k] anchor weight a_cl
+  float4* mem_geo;           // [U*k] per frame {a, v_c - g_l}
+  float4* grp_target;        // [G] per frame {target xyz, mult}
+  const float* node_pos;     // [n*3]
+  const float* aims;         // [n*3]
+  double* x;                 // [F*12] Gauss-Newton iterate
+  float* xf;                 // [F*12] float copy of x
+  float* h;                  // [F*12] step
+  float* r;                  // [F*12] PCG residual
+  float* z;                  // [F*12] preconditioned residual
+  float* p0;                 // [F*12] search direction, even iterations
+  float* p1;                 // [F*12] search direction, odd iterations
+  float* q;                  // [F*12] A p
+  float* g;                  // [F*12] right-hand side -J^T f
+  float* dinv;               // [F*144] inverse of the 12x12 diagonal block of J^T J
+  double* partials;          // [8 * gridDim]
+  double* results;           // [8]
+  GridBarrier* bar;
+  double* stats;             // [8] device-side stats (see solver.cu)
+  float* rot_out;            // [n*9]
+  float* trans_out;          // [n*3]
+  const double* x_in;        // grad-only mode: evaluation point
+  double* grad_out;          // grad-only mode: J^T f
+  float wr, wg, wc, wf;      // square roots of w_rot, w_reg, w_con; weighting factor
+  int max_iters, early_exit, pcg_max;
+  float pcg_tol;
+  int mode;                  // 0 solve, 1 gradient/energy only
+  int refine;                // mixed precision: FP64 refinement sweeps per solve
+};
+
+}  // namespace arap

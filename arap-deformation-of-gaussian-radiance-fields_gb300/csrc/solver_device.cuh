@@ -1,0 +1,525 @@
+// Device side of the Gauss-Newton / PCG solver: per-node residual, gradient
+// and energy of the reference's energy (Deform.cpp:378-581) with its Jacobian
+// (Deform.cpp:180-376), the matrix-free product (J^T J) p, and the 12x12
+// block-Jacobi preconditioner.  One warp owns one free node at a time; lanes
+// stride over the node's coupling items and the warp reduces the 12-vector.
+#pragma once
+
+#include "solver.cuh"
+
+namespace arap {
+
+constexpr int kSolveThreads = 256;
+constexpr int kSolveWarps = kSolveThreads / 32;
+
+// Mutable per-node vectors are read through L2 (ld.global.cg): other CTAs
+// write them between grid barriers, and L1 is not coherent across SMs.
+__device__ __forceinline__ void ld12cg(const float* base, int r, float (&v)[12]) {
+  const float4* p = reinterpret_cast<const float4*>(base + 12 * (size_t)r);
+  const float4 a = __ldcg(p), b = __ldcg(p + 1), c = __ldcg(p + 2);
+  v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
+  v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
+  v[8] = c.x; v[9] = c.y; v[10] = c.z; v[11] = c.w;
+}
+
+__device__ __forceinline__ void ld3t_cg(const float* base, int r, float (&v)[3]) {
+  const float4 c = __ldcg(reinterpret_cast<const float4*>(base + 12 * (size_t)r) + 2);
+  v[0] = c.y; v[1] = c.z; v[2] = c.w;
+}
+
+// Search direction of free node rr for this PCG iteration, formed on the fly:
+// p = z + beta * p_old (p = z on the first iteration).
+__device__ __forceinline__ void load_p(const SolveParams& P, int rr, bool first, float beta,
+                                       const float* pold, float (&v)[12]) {
+  ld12cg(P.z, rr, v);
+  if (!first) {
+    float o[12];
+    ld12cg(pold, rr, o);
+#pragma unroll
+    for (int i = 0; i < 12; ++i) v[i] = fmaf(beta, o[i], v[i]);
+  }
+}
+
+__device__ __forceinline__ void load_pt(const SolveParams& P, int rr, bool first, float beta,
+                                        const float* pold, float (&v)[3]) {
+  ld3t_cg(P.z, rr, v);
+  if (!first) {
+    float o[3];
+    ld3t_cg(pold, rr, o);
+#pragma unroll
+    for (int i = 0; i < 3; ++i) v[i] = fmaf(beta, o[i], v[i]);
+  }
+}
+
+// x + scale * h of free node rr (all 12, or the translation part).
+template <typename RT>
+__device__ __forceinline__ void load_x(const SolveParams& P, int rr, RT scale, RT (&v)[12]) {
+  const double* xp = P.x + 12 * (size_t)rr;
+  if (scale != RT(0)) {
+    float hv[12];
+    ld12cg(P.h, rr, hv);
+#pragma unroll
+    for (int i = 0; i < 12; ++i) v[i] = RT(__ldcg(xp + i)) + scale * RT(hv[i]);
+  } else {
+#pragma unroll
+    for (int i = 0; i < 12; ++i) v[i] = RT(__ldcg(xp + i));
+  }
+}
+
+template <typename RT>
+__device__ __forceinline__ void load_xt(const SolveParams& P, int rr, RT scale, RT (&v)[3]) {
+  const double* xp = P.x + 12 * (size_t)rr + 9;
+  if (scale != RT(0)) {
+    float hv[3];
+    ld3t_cg(P.h, rr, hv);
+#pragma unroll
+    for (int i = 0; i < 3; ++i) v[i] = RT(__ldcg(xp + i)) + scale * RT(hv[i]);
+  } else {
+#pragma unroll
+    for (int i = 0; i < 3; ++i) v[i] = RT(__ldcg(xp + i));
+  }
+}
+
+template <typename RT>
+__device__ __forceinline__ void load_pos(const SolveParams& P, int node, RT (&v)[3]) {
+  const float* p = P.node_pos + 3 * (size_t)node;
+  v[0] = RT(__ldg(p));
+  v[1] = RT(__ldg(p + 1));
+  v[2] = RT(__ldg(p + 2));
+}
+
+// Constraint-group residual f_g (Deform.cpp:484-580) at x + scale*h:
+// wc * (sum_members sum_anchors a (R_l (v_c - g_l) + g_l + t_l)  [free l]
+//                                 a v_c                           [other l]
+//        - mult * target).
+template <typename RT>
+__device__ void con_residual(const SolveParams& P, int g, RT scale, RT (&f)[3]) {
+  f[0] = f[1] = f[2] = RT(0);
+  const int k = P.k;
+  const int s0 = __ldg(P.grp_off + g), s1 = __ldg(P.grp_off + g + 1);
+  for (int s = s0; s < s1; ++s) {
+    RT v[3];
+    load_pos<RT>(P, __ldg(P.grp_member + s), v);
+    for (int t = 0; t < k; ++t) {
+      const int slot = s * k + t;
+      const RT a = RT(__ldg(P.mem_w + slot));
+      const int rk = __ldg(P.mem_rank + slot);
+      if (rk < 0) {
+#pragma unroll
+        for (int c = 0; c < 3; ++c) f[c] += a * v[c];
+      } else {
+        RT gl[3], X[12];
+        load_pos<RT>(P, __ldg(P.mem_node + slot), gl);
+        load_x<RT>(P, rk, scale, X);
+        const RT d0 = v[0] - gl[0], d1 = v[1] - gl[1], d2 = v[2] - gl[2];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) f[c] += a * (X[c] * d0 + X[3 + c] * d1 + X[6 + c] * d2 + gl[c] + X[9 + c]);
+      }
+    }
+  }
+  const float4 tg = P.grp_target[g];
+  const RT wc = RT(P.wc);
+  f[0] = wc * (f[0] - RT(tg.w) * RT(tg.x));
+  f[1] = wc * (f[1] - RT(tg.w) * RT(tg.y));
+  f[2] = wc * (f[2] - RT(tg.w) * RT(tg.z));
+}
+
+// J_g p of a constraint group (linear part only).
+__device__ void con_jp(const SolveParams& P, int g, bool first, float beta, const float* pold, float (&u)[3]) {
+  u[0] = u[1] = u[2] = 0.f;
+  const int k = P.k;
+  const int s0 = __ldg(P.grp_off + g), s1 = __ldg(P.grp_off + g + 1);
+  for (int s = s0; s < s1; ++s) {
+    for (int t = 0; t < k; ++t) {
+      const int slot = s * k + t;
+      const int rk = __ldg(P.mem_rank + slot);
+      if (rk < 0) continue;
+      const float4 geo = __ldcg(P.mem_geo + slot);
+      float pl[12];
+      load_p(P, rk, first, beta, pold, pl);
+#pragma unroll
+      for (int c = 0; c < 3; ++c)
+        u[c] = fmaf(geo.x, fmaf(geo.y, pl[c], fmaf(geo.z, pl[3 + c], fmaf(geo.w, pl[6 + c], pl[9 + c]))), u[c]);
+    }
+  }
+  u[0] *= P.wc;
+  u[1] *= P.wc;
+  u[2] *= P.wc;
+}
+
+template <typename T>
+__device__ __forceinline__ T warp_sum(T v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// 4x4 symmetric accumulator index (a <= b).
+__device__ __forceinline__ constexpr int qi(int a, int b) {
+  return a == 0 ? b : (a == 1 ? 3 + b : (a == 2 ? 5 + b : 9));
+}
+
+__device__ __forceinline__ void q_add(float (&Q)[10], float v0, float v1, float v2, float v3) {
+  const float v[4] = {v0, v1, v2, v3};
+#pragma unroll
+  for (int a = 0; a < 4; ++a)
+#pragma unroll
+    for (int b = a; b < 4; ++b) Q[qi(a, b)] = fmaf(v[a], v[b], Q[qi(a, b)]);
+}
+
+enum { PASS_GRAD = 0, PASS_ENERGY = 1 };
+
+// Residual rows owned by free node r, at x + scale*h.  PASS_GRAD also returns
+// acc = (J^T f)_r (every item touching x_r) and Q, the 4x4 kernel of the
+// non-rotation part of the diagonal block of J^T J.  All lanes of the warp
+// call it; the outputs are warp-reduced and valid in every lane.
+template <typename RT, int PASS>
+__device__ void residual_node(const SolveParams& P, int r, RT scale, RT (&acc)[12], float (&Q)[10],
+                              double& energy) {
+  const int lane = threadIdx.x & 31;
+  const int j = __ldg(P.free_ids + r);
+  RT gj[3];
+  load_pos<RT>(P, j, gj);
+  const float gjf[3] = {__ldg(P.node_pos + 3 * (size_t)j), __ldg(P.node_pos + 3 * (size_t)j + 1),
+                        __ldg(P.node_pos + 3 * (size_t)j + 2)};
+  RT xj[12];
+  load_x<RT>(P, r, scale, xj);
+#pragma unroll
+  for (int i = 0; i < 12; ++i) acc[i] = RT(0);
+#pragma unroll
+  for (int i = 0; i < 10; ++i) Q[i] = 0.f;
+  double e = 0.0;
+  const RT w = RT(P.wg);
+  const int b0 = __ldg(P.item_off + r), b1 = __ldg(P.item_off + r + 1);
+  for (int it = b0 + lane; it < b1; it += 32) {
+    const int4 m = __ldg(P.items + it);
+    if (m.x == ITEM_OUT) {
+      // f = w s (R_j d + g_j + t_j - g_k - t_k), d = g_k - g_j (Deform.cpp:421-449)
+      const float s = __int_as_float(m.w);
+      const RT ws = w * RT(s);
+      RT gk[3];
+      load_pos<RT>(P, m.z, gk);
+      const RT d[3] = {gk[0] - gj[0], gk[1] - gj[1], gk[2] - gj[2]};
+      RT tk[3] = {RT(0), RT(0), RT(0)};
+      if (m.y >= 0) load_xt<RT>(P, m.y, scale, tk);
+      RT f[3];
+#pragma unroll
+      for (int c = 0; c < 3; ++c) f[c] = ws * (xj[c] * d[0] + xj[3 + c] * d[1] + xj[6 + c] * d[2] + xj[9 + c] - tk[c] - d[c]);
+      e += double(f[0]) * double(f[0]) + double(f[1]) * double(f[1]) + double(f[2]) * double(f[2]);
+      if (PASS == PASS_GRAD) {
+        // Jacobian entries use the float difference (Deform.cpp:254-257) and
+        // an unscaled t_j column (Deform.cpp:257)
+        const float dJ[3] = {__ldg(P.node_pos + 3 * (size_t)m.z) - gjf[0],
+                             __ldg(P.node_pos + 3 * (size_t)m.z + 1) - gjf[1],
+                             __ldg(P.node_pos + 3 * (size_t)m.z + 2) - gjf[2]};
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
+#pragma unroll
+          for (int rr = 0; rr < 3; ++rr) acc[3 * c + rr] += ws * RT(dJ[c]) * f[rr];
+#pragma unroll
+        for (int rr = 0; rr < 3; ++rr) acc[9 + rr] += w * f[rr];
+        const float wsf = P.wg * s;
+        q_add(Q, wsf * dJ[0], wsf * dJ[1], wsf * dJ[2], P.wg);
+      }
+    } else if (m.x == ITEM_STATIC) {
+      // f = -w t_j (Deform.cpp:458-482)
+      RT f[3] = {-w * xj[9], -w * xj[10], -w * xj[11]};
+      e += double(f[0]) * double(f[0]) + double(f[1]) * double(f[1]) + double(f[2]) * double(f[2]);
+      if (PASS == PASS_GRAD) {
+#pragma unroll
+        for (int rr = 0; rr < 3; ++rr) acc[9 + rr] += -w * f[rr];
+        Q[9] += P.wg * P.wg;
+      }
+    } else if (PASS == PASS_GRAD) {
+      if (m.x == ITEM_IN) {
+        const float s = __int_as_float(m.w);
+        const RT ws = w * RT(s);
+        RT gi[3], xi[12];
+        load_pos<RT>(P, m.z, gi);
+        load_x<RT>(P, m.y, scale, xi);
+        const RT d[3] = {gj[0] - gi[0], gj[1] - gi[1], gj[2] - gi[2]};
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          const RT f = ws * (xi[c] * d[0] + xi[3 + c] * d[1] + xi[6 + c] * d[2] + xi[9 + c] - xj[9 + c] - d[c]);
+          acc[9 + c] += -ws * f;
+        }
+        Q[9] += (P.wg * s) * (P.wg * s);
+      } else {  // ITEM_CON
+        const int g = m.z;
+        RT fg[3];
+        con_residual<RT>(P, g, scale, fg);
+        const float4 geo = __ldcg(P.mem_geo + m.y);
+        const RT wa = RT(P.wc) * RT(geo.x);
+        const float dv[3] = {geo.y, geo.z, geo.w};
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
+#pragma unroll
+          for (int rr = 0; rr < 3; ++rr) acc[3 * c + rr] += wa * RT(dv[c]) * fg[rr];
+#pragma unroll
+        for (int rr = 0; rr < 3; ++rr) acc[9 + rr] += wa * fg[rr];
+        // diagonal block: aggregate all anchors of this group equal to j, once
+        // per (group, node) run (items are sorted by group)
+        bool first_of_run = true;
+        if (it > b0) {
+          const int4 pm = __ldg(P.items + it - 1);
+          first_of_run = !(pm.x == ITEM_CON && pm.z == g);
+        }
+        if (first_of_run) {
+          float ev[3] = {0.f, 0.f, 0.f}, al = 0.f;
+          const int s0 = __ldg(P.grp_off + g), s1 = __ldg(P.grp_off + g + 1);
+          for (int s = s0; s < s1; ++s)
+            for (int t = 0; t < P.k; ++t) {
+              const int slot = s * P.k + t;
+              if (__ldg(P.mem_node + slot) != j) continue;
+              const float4 gg = __ldcg(P.mem_geo + slot);
+              ev[0] = fmaf(gg.x, gg.y, ev[0]);
+              ev[1] = fmaf(gg.x, gg.z, ev[1]);
+              ev[2] = fmaf(gg.x, gg.w, ev[2]);
+              al += gg.x;
+            }
+          q_add(Q, P.wc * ev[0], P.wc * ev[1], P.wc * ev[2], P.wc * al);
+        }
+      }
+    }
+  }
+  if (lane == 0) {
+    // orthogonality rows (Deform.cpp:384-404)
+    const RT wr = RT(P.wr);
+    const RT* c0 = xj;
+    const RT* c1 = xj + 3;
+    const RT* c2 = xj + 6;
+    const RT f[6] = {wr * (c0[0] * c1[0] + c0[1] * c1[1] + c0[2] * c1[2]),
+                     wr * (c0[0] * c2[0] + c0[1] * c2[1] + c0[2] * c2[2]),
+                     wr * (c1[0] * c2[0] + c1[1] * c2[1] + c1[2] * c2[2]),
+                     wr * (c0[0] * c0[0] + c0[1] * c0[1] + c0[2] * c0[2] - RT(1)),
+                     wr * (c1[0] * c1[0] + c1[1] * c1[1] + c1[2] * c1[2] - RT(1)),
+                     wr * (c2[0] * c2[0] + c2[1] * c2[1] + c2[2] * c2[2] - RT(1))};
+#pragma unroll
+    for (int i = 0; i < 6; ++i) e += double(f[i]) * double(f[i]);
+    if (PASS == PASS_GRAD) {
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        acc[c] += wr * (f[0] * c1[c] + f[1] * c2[c] + RT(2) * f[3] * c0[c]);
+        acc[3 + c] += wr * (f[0] * c0[c] + f[2] * c2[c] + RT(2) * f[4] * c1[c]);
+        acc[6 + c] += wr * (f[1] * c0[c] + f[2] * c1[c] + RT(2) * f[5] * c2[c]);
+      }
+    }
+  }
+  if (PASS == PASS_GRAD) {
+#pragma unroll
+    for (int i = 0; i < 12; ++i) acc[i] = warp_sum(acc[i]);
+#pragma unroll
+    for (int i = 0; i < 10; ++i) Q[i] = warp_sum(Q[i]);
+  }
+  energy = warp_sum(e);
+}
+
+// q = (J^T J p)_r for free node r; also returns this node's p (all lanes).
+__device__ void spmv_node(const SolveParams& P, int r, bool first, float beta, const float* pold,
+                          float (&acc)[12], float (&pj)[12]) {
+  const int lane = threadIdx.x & 31;
+  const int j = __ldg(P.free_ids + r);
+  const float gj[3] = {__ldg(P.node_pos + 3 * (size_t)j), __ldg(P.node_pos + 3 * (size_t)j + 1),
+                       __ldg(P.node_pos + 3 * (size_t)j + 2)};
+  load_p(P, r, first, beta, pold, pj);
+#pragma unroll
+  for (int i = 0; i < 12; ++i) acc[i] = 0.f;
+  const float w = P.wg;
+  const int b0 = __ldg(P.item_off + r), b1 = __ldg(P.item_off + r + 1);
+  for (int it = b0 + lane; it < b1; it += 32) {
+    const int4 m = __ldg(P.items + it);
+    if (m.x == ITEM_OUT) {
+      const float ws = w * __int_as_float(m.w);
+      const float d[3] = {__ldg(P.node_pos + 3 * (size_t)m.z) - gj[0],
+                          __ldg(P.node_pos + 3 * (size_t)m.z + 1) - gj[1],
+                          __ldg(P.node_pos + 3 * (size_t)m.z + 2) - gj[2]};
+      float pk[3] = {0.f, 0.f, 0.f};
+      if (m.y >= 0) load_pt(P, m.y, first, beta, pold, pk);
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        const float u = ws * fmaf(pj[c], d[0], fmaf(pj[3 + c], d[1], pj[6 + c] * d[2])) + w * pj[9 + c] - ws * pk[c];
+        acc[c] = fmaf(ws * d[0], u, acc[c]);
+        acc[3 + c] = fmaf(ws * d[1], u, acc[3 + c]);
+        acc[6 + c] = fmaf(ws * d[2], u, acc[6 + c]);
+        acc[9 + c] = fmaf(w, u, acc[9 + c]);
+      }
+    } else if (m.x == ITEM_IN) {
+      const float ws = w * __int_as_float(m.w);
+      const float d[3] = {gj[0] - __ldg(P.node_pos + 3 * (size_t)m.z),
+                          gj[1] - __ldg(P.node_pos + 3 * (size_t)m.z + 1),
+                          gj[2] - __ldg(P.node_pos + 3 * (size_t)m.z + 2)};
+      float pi[12];
+      load_p(P, m.y, first, beta, pold, pi);
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        const float u = ws * fmaf(pi[c], d[0], fmaf(pi[3 + c], d[1], pi[6 + c] * d[2])) + w * pi[9 + c] - ws * pj[9 + c];
+        acc[9 + c] = fmaf(-ws, u, acc[9 + c]);
+      }
+    } else if (m.x == ITEM_STATIC) {
+#pragma unroll
+      for (int c = 0; c < 3; ++c) acc[9 + c] = fmaf(w * w, pj[9 + c], acc[9 + c]);
+    } else {
+      float u[3];
+      con_jp(P, m.z, first, beta, pold, u);
+      const float4 geo = __ldcg(P.mem_geo + m.y);
+      const float wa = P.wc * geo.x;
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        acc[c] = fmaf(wa * geo.y, u[c], acc[c]);
+        acc[3 + c] = fmaf(wa * geo.z, u[c], acc[3 + c]);
+        acc[6 + c] = fmaf(wa * geo.w, u[c], acc[6 + c]);
+        acc[9 + c] = fmaf(wa, u[c], acc[9 + c]);
+      }
+    }
+  }
+  if (lane == 0) {
+    // J_rot^T J_rot p with J_rot at the current x (float copy)
+    float X[9];
+    const float4* xp = reinterpret_cast<const float4*>(P.xf + 12 * (size_t)r);
+    const float4 a = __ldcg(xp), b = __ldcg(xp + 1), c = __ldcg(xp + 2);
+    X[0] = a.x; X[1] = a.y; X[2] = a.z; X[3] = a.w; X[4] = b.x; X[5] = b.y; X[6] = b.z; X[7] = b.w; X[8] = c.x;
+    const float* c0 = X;
+    const float* c1 = X + 3;
+    const float* c2 = X + 6;
+    const float* p0 = pj;
+    const float* p1 = pj + 3;
+    const float* p2 = pj + 6;
+    const float wr = P.wr;
+    auto dot = [](const float* a3, const float* b3) { return a3[0] * b3[0] + a3[1] * b3[1] + a3[2] * b3[2]; };
+    const float u0 = wr * (dot(c1, p0) + dot(c0, p1));
+    const float u1 = wr * (dot(c2, p0) + dot(c0, p2));
+    const float u2 = wr * (dot(c2, p1) + dot(c1, p2));
+    const float u3 = 2.f * wr * dot(c0, p0);
+    const float u4 = 2.f * wr * dot(c1, p1);
+    const float u5 = 2.f * wr * dot(c2, p2);
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      acc[i] += wr * (u0 * c1[i] + u1 * c2[i] + 2.f * u3 * c0[i]);
+      acc[3 + i] += wr * (u0 * c0[i] + u2 * c2[i] + 2.f * u4 * c1[i]);
+      acc[6 + i] += wr * (u1 * c0[i] + u2 * c1[i] + 2.f * u5 * c2[i]);
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < 12; ++i) acc[i] = warp_sum(acc[i]);
+}
+
+// Diagonal 12x12 block of J^T J for free node r from Q and the rotation
+// rows at x (float copy), Cholesky-factored by lane 0 and inverted column by
+// column by lanes 0..11 into P.dinv (row-major, symmetric).
+__device__ void build_dinv(const SolveParams& P, int r, const float (&Q)[10], float* D) {
+  const int lane = threadIdx.x & 31;
+  if (lane == 0) {
+    float X[9];
+#pragma unroll
+    for (int i = 0; i < 9; ++i) X[i] = __ldcg(P.xf + 12 * (size_t)r + i);
+#pragma unroll
+    for (int i = 0; i < 144; ++i) D[i] = 0.f;
+#pragma unroll
+    for (int rr = 0; rr < 3; ++rr) {
+#pragma unroll
+      for (int a = 0; a < 3; ++a) {
+#pragma unroll
+        for (int b = 0; b < 3; ++b) D[(3 * a + rr) * 12 + 3 * b + rr] = Q[a <= b ? qi(a, b) : qi(b, a)];
+        D[(3 * a + rr) * 12 + 9 + rr] = Q[qi(a, 3)];
+        D[(9 + rr) * 12 + 3 * a + rr] = Q[qi(a, 3)];
+      }
+      D[(9 + rr) * 12 + 9 + rr] = Q[9];
+    }
+    // rotation rows: [c1|c0|0], [c2|0|c0], [0|c2|c1], [2c0|0|0], [0|2c1|0], [0|0|2c2]
+    const float wr = P.wr;
+    float J[6][9];
+#pragma unroll
+    for (int a = 0; a < 6; ++a)
+#pragma unroll
+      for (int b = 0; b < 9; ++b) J[a][b] = 0.f;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      J[0][c] = wr * X[3 + c]; J[0][3 + c] = wr * X[c];
+      J[1][c] = wr * X[6 + c]; J[1][6 + c] = wr * X[c];
+      J[2][3 + c] = wr * X[6 + c]; J[2][6 + c] = wr * X[3 + c];
+      J[3][c] = 2.f * wr * X[c];
+      J[4][3 + c] = 2.f * wr * X[3 + c];
+      J[5][6 + c] = 2.f * wr * X[6 + c];
+    }
+#pragma unroll
+    for (int a = 0; a < 9; ++a)
+#pragma unroll
+      for (int b = 0; b < 9; ++b) {
+        float s = 0.f;
+#pragma unroll
+        for (int t = 0; t < 6; ++t) s = fmaf(J[t][a], J[t][b], s);
+        D[a * 12 + b] += s;
+      }
+    // Cholesky, lower triangle in place
+    bool ok = true;
+    for (int c = 0; c < 12 && ok; ++c) {
+      float s = D[c * 12 + c];
+      for (int t = 0; t < c; ++t) s -= D[c * 12 + t] * D[c * 12 + t];
+      if (!(s > 0.f)) {
+        ok = false;
+        break;
+      }
+      const float l = sqrtf(s);
+      D[c * 12 + c] = l;
+      const float il = 1.f / l;
+      for (int i = c + 1; i < 12; ++i) {
+        float v = D[i * 12 + c];
+        for (int t = 0; t < c; ++t) v -= D[i * 12 + t] * D[c * 12 + t];
+        D[i * 12 + c] = v * il;
+      }
+    }
+    if (!ok) {
+      // Jacobi fallback: diagonal of the block
+      for (int a = 0; a < 12; ++a) {
+        float dg = 0.f;
+        if (a < 9) {
+          float s = 0.f;
+          for (int t = 0; t < 6; ++t) s += J[t][a] * J[t][a];
+          dg = s;
+        }
+        const int rr = a < 9 ? a % 3 : a - 9;
+        dg += (a < 9) ? Q[qi(a / 3, a / 3)] : Q[9];
+        (void)rr;
+        for (int b = 0; b < 12; ++b) D[a * 12 + b] = 0.f;
+        D[a * 12 + a] = sqrtf(fmaxf(dg, 1e-20f));
+      }
+    }
+  }
+  __syncwarp();
+  if (lane < 12) {
+    float y[12], xs[12];
+#pragma unroll
+    for (int i = 0; i < 12; ++i) {
+      float s = (i == lane) ? 1.f : 0.f;
+#pragma unroll
+      for (int t = 0; t < i; ++t) s -= D[i * 12 + t] * y[t];
+      y[i] = s / D[i * 12 + i];
+    }
+#pragma unroll
+    for (int i = 11; i >= 0; --i) {
+      float s = y[i];
+#pragma unroll
+      for (int t = i + 1; t < 12; ++t) s -= D[t * 12 + i] * xs[t];
+      xs[i] = s / D[i * 12 + i];
+    }
+    float* out = P.dinv + 144 * (size_t)r + 12 * lane;
+#pragma unroll
+    for (int i = 0; i < 12; ++i) out[i] = xs[i];
+  }
+  __syncwarp();
+}
+
+// z = Dinv r for free node rr; lane c < 12 holds r_c and returns z_c.
+__device__ __forceinline__ float apply_dinv(const SolveParams& P, int rr, float rc) {
+  const int lane = threadIdx.x & 31;
+  float zc = 0.f;
+  const float* row = P.dinv + 144 * (size_t)rr + 12 * (lane < 12 ? lane : 0);
+#pragma unroll
+  for (int i = 0; i < 12; ++i) {
+    const float ri = __shfl_sync(0xffffffffu, rc, i);
+    zc = fmaf(__ldcg(row + i), ri, zc);
+  }
+  return lane < 12 ? zc : 0.f;
+}
+
+}  // namespace arap

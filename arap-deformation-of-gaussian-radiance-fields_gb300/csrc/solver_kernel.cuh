@@ -1,0 +1,266 @@
+// The persistent Gauss-Newton kernel: one cooperative launch runs the whole
+// Deform::optimize loop (Deform.cpp:95-169) -- gradient and energy, block
+// preconditioner, PCG for (J^T J) h = -J^T f, halving line search, stop test
+// -- and writes the node transforms (Deform.hpp:140-151).
+#pragma once
+
+#include "solver_device.cuh"
+
+namespace arap {
+
+// stats slots written by CTA 0
+enum { ST_ITERS = 0, ST_PCG = 1, ST_HALV = 2, ST_E0 = 3, ST_E = 4, ST_CONV = 5, ST_NONFINITE = 6 };
+
+template <int N>
+__device__ __forceinline__ bool reduce_all(const SolveParams& P, double (&v)[N], double (&out)[N]) {
+  block_sum<N>(v);
+  return grid_sync_reduce<N>(P.bar, P.partials, P.results, v, out);
+}
+
+template <typename RT>
+__global__ void __launch_bounds__(kSolveThreads) gn_solve_kernel(SolveParams P) {
+  __shared__ float s_D[kSolveWarps][144];
+  const int lane = threadIdx.x & 31;
+  const int wib = threadIdx.x >> 5;
+  const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int nw = (gridDim.x * blockDim.x) >> 5;
+  const int gt = blockIdx.x * blockDim.x + threadIdx.x;
+  const int nt = gridDim.x * blockDim.x;
+  const int F = P.F, k = P.k;
+
+  // ---- per-frame geometry: member anchors, group targets, x = identity
+  for (int slot = gt; slot < P.U * k; slot += nt) {
+    const int c = P.grp_member[slot / k];
+    const int l = P.mem_node[slot];
+    P.mem_geo[slot] = make_float4(P.mem_w[slot], P.node_pos[3 * c] - P.node_pos[3 * l],
+                                  P.node_pos[3 * c + 1] - P.node_pos[3 * l + 1],
+                                  P.node_pos[3 * c + 2] - P.node_pos[3 * l + 2]);
+  }
+  for (int g = gt; g < P.G; g += nt) {
+    // centre = float sum of the listed aims / count (Deform.cpp:56-64)
+    const int a0 = P.tsrc_off[g], a1 = P.tsrc_off[g + 1];
+    float cx = 0.f, cy = 0.f, cz = 0.f;
+    for (int a = a0; a < a1; ++a) {
+      const int s = P.tsrc[a];
+      cx += P.aims[3 * s];
+      cy += P.aims[3 * s + 1];
+      cz += P.aims[3 * s + 2];
+    }
+    const float m = (float)(a1 - a0);
+    P.grp_target[g] = make_float4(cx / m, cy / m, cz / m, P.grp_mult[g]);
+  }
+  for (int e = gt; e < F * 12; e += nt) {
+    const int c = e % 12;
+    const double v = P.mode == 1 ? P.x_in[e] : ((c == 0 || c == 4 || c == 8) ? 1.0 : 0.0);
+    P.x[e] = v;
+    P.xf[e] = (float)v;
+  }
+  {
+    double d0[1] = {0.0}, o0[1];
+    if (!grid_sync_reduce<1>(P.bar, P.partials, P.results, d0, o0)) return;
+  }
+
+  double e_first = 0.0, e_last = 0.0;
+  int iters = 0, pcg_total = 0, halvings = 0, converged = 0;
+  for (int it = 0; it < P.max_iters; ++it) {
+    // ---- gradient -J^T f, energy, preconditioner, PCG start (h=0, r=g, z=M^-1 g)
+    double red[4] = {0.0, 0.0, 0.0, 0.0}, out[4];
+    for (int r = gw; r < F; r += nw) {
+      RT acc[12];
+      float Q[10];
+      double en;
+      residual_node<RT, PASS_GRAD>(P, r, RT(0), acc, Q, en);
+      if (lane == 0) red[0] += en;
+      if (P.mode == 1) {
+        if (lane < 12) {
+          double a = 0.0;
+#pragma unroll
+          for (int i = 0; i < 12; ++i)
+            if (i == lane) a = (double)acc[i];
+          P.grad_out[12 * (size_t)r + lane] = a;
+        }
+        continue;
+      }
+      build_dinv(P, r, Q, s_D[wib]);
+      float gc = 0.f;
+#pragma unroll
+      for (int i = 0; i < 12; ++i)
+        if (i == lane) gc = -(float)acc[i];
+      const float zc = apply_dinv(P, r, gc);
+      if (lane < 12) {
+        const size_t o = 12 * (size_t)r + lane;
+        P.g[o] = gc;
+        P.r[o] = gc;
+        P.z[o] = zc;
+        P.h[o] = 0.f;
+        red[2] += (double)gc * (double)zc;
+        red[3] += (double)gc * (double)gc;
+      }
+    }
+    for (int g = gt; g < P.G; g += nt) {
+      RT f[3];
+      con_residual<RT>(P, g, RT(0), f);
+      red[0] += double(f[0]) * double(f[0]) + double(f[1]) * double(f[1]) + double(f[2]) * double(f[2]);
+    }
+    for (int e = gt; e < F * 12; e += nt) {
+      const double v = __ldcg(P.x + e);
+      red[1] += v * v;
+    }
+    if (!reduce_all<4>(P, red, out)) return;
+    const double e_old = out[0];
+    const double normv = sqrt(out[1]);
+    if (it == 0) e_first = e_old;
+    e_last = e_old;
+    if (P.mode == 1) {
+      if (gt == 0) P.stats[ST_E] = e_old;
+      return;
+    }
+
+    // ---- PCG on (J^T J) h = g, two barriers per iteration
+    double rz = out[2];
+    const double rr0 = out[3];
+    double rr = rr0;
+    const double tol2 = (double)P.pcg_tol * (double)P.pcg_tol * rr0;
+    float beta = 0.f;
+    int pi = 0;
+    while (rr > tol2 && pi < P.pcg_max && rz > 0.0) {
+      const bool first = pi == 0;
+      float* pcur = (pi & 1) ? P.p1 : P.p0;
+      const float* pold = (pi & 1) ? P.p0 : P.p1;
+      double pq[1] = {0.0}, opq[1];
+      for (int r = gw; r < F; r += nw) {
+        float acc[12], pj[12];
+        spmv_node(P, r, first, beta, pold, acc, pj);
+        if (lane < 12) {
+          float pc = 0.f, qc = 0.f;
+#pragma unroll
+          for (int i = 0; i < 12; ++i)
+            if (i == lane) {
+              pc = pj[i];
+              qc = acc[i];
+            }
+          const size_t o = 12 * (size_t)r + lane;
+          pcur[o] = pc;
+          P.q[o] = qc;
+          pq[0] += (double)pc * (double)qc;
+        }
+      }
+      if (!reduce_all<1>(P, pq, opq)) return;
+      if (!(opq[0] > 0.0)) break;
+      const float alpha = (float)(rz / opq[0]);
+      double rzr[2] = {0.0, 0.0}, orz[2];
+      for (int r = gw; r < F; r += nw) {
+        float rc = 0.f;
+        if (lane < 12) {
+          const size_t o = 12 * (size_t)r + lane;
+          P.h[o] = fmaf(alpha, __ldcg(pcur + o), __ldcg(P.h + o));
+          rc = fmaf(-alpha, __ldcg(P.q + o), __ldcg(P.r + o));
+          P.r[o] = rc;
+        }
+        const float zc = apply_dinv(P, r, rc);
+        if (lane < 12) {
+          P.z[12 * (size_t)r + lane] = zc;
+          rzr[0] += (double)rc * (double)zc;
+          rzr[1] += (double)rc * (double)rc;
+        }
+      }
+      if (!reduce_all<2>(P, rzr, orz)) return;
+      beta = (float)(orz[0] / rz);
+      rz = orz[0];
+      rr = orz[1];
+      ++pi;
+    }
+    pcg_total += pi;
+
+    // ---- line search: x + 2^-m h, m = 0..49 (Deform.cpp:144-156)
+    RT scale = RT(1);
+    bool accepted = false;
+    double hh = 0.0;
+    for (int ls = 0; ls < 50; ++ls) {
+      double en2[2] = {0.0, 0.0}, oen[2];
+      for (int r = gw; r < F; r += nw) {
+        RT acc[12];
+        float Q[10];
+        double en;
+        residual_node<RT, PASS_ENERGY>(P, r, scale, acc, Q, en);
+        if (lane == 0) en2[0] += en;
+      }
+      for (int g = gt; g < P.G; g += nt) {
+        RT f[3];
+        con_residual<RT>(P, g, scale, f);
+        en2[0] += double(f[0]) * double(f[0]) + double(f[1]) * double(f[1]) + double(f[2]) * double(f[2]);
+      }
+      if (ls == 0) {
+        for (int e = gt; e < F * 12; e += nt) {
+          const double v = __ldcg(P.h + e);
+          en2[1] += v * v;
+        }
+      }
+      if (!reduce_all<2>(P, en2, oen)) return;
+      if (ls == 0) hh = oen[1];
+      if (oen[0] > e_old) {
+        scale *= RT(0.5);
+        ++halvings;
+      } else {
+        accepted = true;
+        e_last = oen[0];
+        break;
+      }
+    }
+    if (accepted) {
+      for (int e = gt; e < F * 12; e += nt) {
+        const double v = __ldcg(P.x + e) + (double)scale * (double)__ldcg(P.h + e);
+        P.x[e] = v;
+        P.xf[e] = (float)v;
+      }
+    }
+    const double normh = (double)scale * sqrt(hh);
+    iters = it + 1;
+    {
+      double d0[1] = {0.0}, o0[1];
+      if (!reduce_all<1>(P, d0, o0)) return;
+    }
+    if (P.early_exit && normh < (normv + 1e-6) * 1e-6) {
+      converged = 1;
+      break;
+    }
+  }
+
+  // ---- putFreeInputs / resetRT: node transforms for every node
+  int nonfinite = 0;
+  for (int node = gt; node < P.n; node += nt) {
+    const int rk = P.rank[node];
+    float* ro = P.rot_out + 9 * (size_t)node;
+    float* to = P.trans_out + 3 * (size_t)node;
+    if (rk >= 0) {
+      const double* xp = P.x + 12 * (size_t)rk;
+#pragma unroll
+      for (int i = 0; i < 9; ++i) {
+        const double v = __ldcg(xp + i);
+        ro[i] = (float)v;
+        if (!isfinite(v)) nonfinite = 1;
+      }
+#pragma unroll
+      for (int i = 0; i < 3; ++i) {
+        const double v = __ldcg(xp + 9 + i);
+        to[i] = (float)v;
+        if (!isfinite(v)) nonfinite = 1;
+      }
+    } else {
+#pragma unroll
+      for (int i = 0; i < 9; ++i) ro[i] = (i == 0 || i == 4 || i == 8) ? 1.f : 0.f;
+      to[0] = to[1] = to[2] = 0.f;
+    }
+  }
+  if (nonfinite) raise_status(ARAP_ENONFINITE);
+  if (gt == 0) {
+    P.stats[ST_ITERS] = iters;
+    P.stats[ST_PCG] = pcg_total;
+    P.stats[ST_HALV] = halvings;
+    P.stats[ST_E0] = e_first;
+    P.stats[ST_E] = e_last;
+    P.stats[ST_CONV] = converged;
+  }
+}
+
+}  // namespace arap

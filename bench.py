@@ -1,0 +1,339 @@
+"""Benchmark: deform ms/frame on the 300k-Gaussian / 64^3 twist workload.
+
+One step = one deformation frame through the library, in the reference's
+order (GaussianView.cpp:1481-1522): 20-iteration Gauss-Newton solve of the
+node transforms (early exit off), skinning of the grid samples (position +
+slerp-blended SH rotation of the 48-float features), skinning of all Gaussians
+(6-endpoint ED blend, refit, SH rotation, covariance), node update and target
+re-anchoring.  Every step starts from the same rest state (restored by device
+copies inside the step) so each step does identical work.
+
+--impl ours       the CUDA library (default)
+--impl reference  the reference's algorithm on the host cores (the oracle
+                  port: the reference itself needs Eigen/SIBR and cannot be
+                  built here), a bounded sample per step
+
+Prints one JSON line (rank 0).
+"""
+from __future__ import annotations
+
+import argparse
+import importlib
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+PKG = "arap-deformation-of-gaussian-radiance-fields_gb300"
+METRIC = "deform ms/frame, 300k Gaussians 64³ grid: mixed+adjoint vs plain GPU @≤1e-5"
+
+
+def _args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--scene", default="twist300k")
+    ap.add_argument("--precision", default="mixed", choices=["plain", "mixed"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-samples", action="store_true")
+    return ap.parse_args()
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+    Q = ("clocks.sm,clocks.max.sm,clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.rows = []
+        self._stop = threading.Event()
+        self._t = None
+
+    def _run(self):
+        while not self._stop.is_set():
+            try:
+                out = subprocess.run(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                                      "--format=csv,noheader,nounits"], capture_output=True, text=True,
+                                     timeout=5).stdout.strip()
+                if out:
+                    self.rows.append([v.strip() for v in out.split(",")])
+            except Exception:
+                pass
+            self._stop.wait(0.2)
+
+    def __enter__(self):
+        self._t = threading.Thread(target=self._run, daemon=True)
+        self._t.start()
+        return self
+
+    def __exit__(self, *a):
+        self._stop.set()
+        if self._t:
+            self._t.join(timeout=6)
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = sorted(float(r[0]) for r in self.rows if r[0].replace(".", "").isdigit())
+        mx = max((float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()), default=None)
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows for i in range(4) if len(r) > 2 + i and "Active" in r[2 + i]})
+        return {"sm_mhz": sm[len(sm) // 2] if sm else None, "sm_max_mhz": mx, "reasons": reasons,
+                "samples": len(self.rows)}
+
+
+def _peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    return ws, rank
+
+
+# ------------------------------------------------------------ workload ----
+
+def build_state(scene_name, precision, with_samples):
+    import numpy as np
+    import torch
+    dev = importlib.import_module(PKG + ".deform")
+    synth = importlib.import_module(PKG + ".synth")
+    sc = synth.make_scene(scene_name)
+    sample_pos = feature = None
+    if with_samples:
+        grid = importlib.import_module(PKG + ".grid")
+        g = grid.build_grid(torch.as_tensor(sc.pos).cuda(), torch.as_tensor(sc.rot).cuda(),
+                            torch.as_tensor(sc.scale).cuda(), torch.as_tensor(sc.opacity).cuda(), sc.grid_num)
+        sample_pos = g.sample_pos
+        rng = np.random.default_rng(5)
+        feature = torch.as_tensor((0.2 * rng.standard_normal((sample_pos.shape[0], 48))).astype(np.float32)).cuda()
+    cfg = dev.default_config(max_iters=sc.iters, early_exit=0,
+                             precision=1 if precision == "mixed" else 0)
+    st = dev.GaussianDeformer(torch.as_tensor(sc.pos), torch.as_tensor(sc.rot), torch.as_tensor(sc.scale),
+                              torch.as_tensor(sc.shs), sc.node_vertex, sc.k, sc.blocks, sc.block_type,
+                              sample_pos=sample_pos, feature=feature, config=cfg)
+    st.apply_op(sc.op)
+    torch.cuda.synchronize()
+    return sc, st
+
+
+def snapshot(st):
+    names = ["ends", "pos", "rot", "scale", "shs", "node_pos", "aims", "sample_pos", "feature"]
+    return {n: getattr(st, n).clone() for n in names if getattr(st, n, None) is not None}
+
+
+def restore(st, snap):
+    for n, t in snap.items():
+        getattr(st, n).copy_(t)
+
+
+def skin_bytes_per_gaussian(k, with_shs=True, with_cov=True):
+    """Algorithmic bytes of arap_skin_gaussians per Gaussian: read 6 endpoints
+    (72), 6k indices + 6k weights (48k), scale0 (12), previous q (16), SH (192);
+    write endpoints (72), mu (12), q (16), scale (12), SH (192), Sigma (24)."""
+    rd = 72 + 48 * k + 12 + 16 + (192 if with_shs else 0)
+    wr = 72 + 12 + 16 + 12 + (192 if with_shs else 0) + (24 if with_cov else 0)
+    return rd + wr
+
+
+def run_ours(a):
+    import torch
+    import numpy as np
+    ws, rank = _dist()
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    if ws > 1:
+        import torch.distributed as tdist
+        tdist.init_process_group("nccl")
+    dev = importlib.import_module(PKG + ".deform")
+    sc, st = build_state(a.scene, a.precision, not a.no_samples)
+    snap = snapshot(st)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    s = torch.cuda.current_stream()
+
+    skin_ev = []
+
+    def step(record):
+        restore(st, snap)
+        ev = (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) if record else None
+        st.frame(stats=False, with_cov=True, skin_events=ev)
+        if record:
+            skin_ev.append(ev)
+
+    for _ in range(max(3, a.warmup)):
+        step(False)
+    torch.cuda.synchronize()
+    assert dev.device_status() == 0
+    step_ev = []
+    if ws > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    with ClockSampler(torch.cuda.current_device()) as clk:
+        for _ in range(a.steps):
+            flush.fill_(1.0)  # L2 flush between steps (256 MB > 129 MB L2)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(s)
+            step(True)
+            e1.record(s)
+            step_ev.append((e0, e1))
+        torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    if ws > 1:
+        torch.distributed.barrier()
+    ms = [a0.elapsed_time(b0) for a0, b0 in step_ev]
+    ms_step = float(np.mean(ms))
+    if ws > 1:
+        t = torch.tensor([ms_step], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms_step = float(t.item())
+    skin_ms = float(np.mean([a0.elapsed_time(b0) for a0, b0 in skin_ev]))
+    status = dev.device_status()
+
+    # e2e: public API with host buffers (aims H2D, node transforms + energy D2H)
+    aims_host = snap["aims"].cpu().pin_memory()
+    rot_host = torch.empty((st.n, 9), dtype=torch.float32).pin_memory()
+    tr_host = torch.empty((st.n, 3), dtype=torch.float32).pin_memory()
+    e2e_ms = []
+    for i in range(a.warmup + a.steps):
+        restore(st, snap)
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        st.aims.copy_(aims_host, non_blocking=True)
+        st.frame(stats=False, with_cov=True)
+        rot_host.copy_(st.rot_nodes, non_blocking=True)
+        tr_host.copy_(st.trans_nodes, non_blocking=True)
+        torch.cuda.synchronize()
+        if i >= a.warmup:
+            e2e_ms.append((time.perf_counter() - t1) * 1e3)
+    # stats of one frame (PCG iterations) for the record
+    restore(st, snap)
+    stats = st.frame(stats=True)
+    torch.cuda.synchronize()
+
+    peak, peak_kind = _peaks()
+    k = sc.k
+    bytes_launch = skin_bytes_per_gaussian(k) * sc.n_gauss
+    achieved = bytes_launch / (skin_ms * 1e-3) / 1e9
+    launches_per_step = 5 + (1 if st.sample_pos is not None else 0) + (1 if st.feature is not None else 0)
+    line = {
+        "metric": METRIC,
+        "value": round(ms_step, 4),
+        "unit": "ms/frame",
+        "n_gpus": ws,
+        "steps": a.steps,
+        "warmup": a.warmup,
+        "ms_per_step": round(ms_step, 4),
+        "higher_is_better": False,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32+f64" if a.precision == "mixed" else "f32",
+        "data": "synthetic (seeded two-bars-and-sphere field; reference datasets absent)",
+        "config": {"workload": "%s: %d Gaussians, %d^3 grid, %d nodes, k=%d, %d GN iterations, "
+                               "twist 90 deg, precision=%s" % (sc.name, sc.n_gauss, sc.grid_num,
+                                                                sc.n_nodes, k, sc.iters, a.precision),
+                   "samples": int(st.sample_pos.shape[0]) if st.sample_pos is not None else 0,
+                   "l2": "flushed between steps (256 MB write)",
+                   "state": "restored to the rest pose inside each step",
+                   "wall_s_timed_region": round(wall, 3)},
+        "e2e": {"value": round(float(np.mean(e2e_ms)), 4), "unit": "ms/frame",
+                "h2d_bytes_per_step": int(st.n * 12), "d2h_bytes_per_step": int(st.n * 48)},
+        "roofline": {"kernel": "arap_skin_gaussians", "bound": "hbm", "achieved": round(achieved, 1),
+                     "peak": peak, "peak_kind": peak_kind, "unit": "GB/s", "frac": round(achieved / peak, 4),
+                     "traffic": None, "bytes_per_launch": bytes_launch, "ms_per_launch": round(skin_ms, 5)},
+        "gpu_launches": launches_per_step * a.steps,
+        "solve": {"pcg_iterations": stats["pcg_iterations"], "gn_iterations": stats["gn_iterations"],
+                  "final_energy": stats["final_energy"]},
+        "status": status,
+        "clocks": clk.summary(),
+    }
+    if rank == 0 and not a.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(sc, samples=1)
+    if rank == 0:
+        print(json.dumps(line))
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+
+
+# ------------------------------------------------------- CPU baseline ----
+
+def _oracle_frame_sample(sc, gn_iters=1, skin_n=50_000):
+    """Time the oracle port on a bounded sample of one frame: gn_iters
+    Gauss-Newton iterations of the full solve (exact sparse solve) and the
+    skinning of skin_n Gaussians; returns the extrapolated ms/frame."""
+    import numpy as np
+    from oracle import ed, skin, targets
+    t0 = time.perf_counter()
+    nb = ed.build_graph(sc.node_pos, sc.k)
+    aidx, aw = ed.knn_weights(sc.pos[sc.node_vertex], sc.node_pos, sc.k)
+    act = np.concatenate([b for b, t in zip(sc.blocks, sc.block_type) if t == 1])
+    aims = targets.twist(sc.node_pos, sc.node_pos, act, sc.op[1], sc.op[2]) if sc.op[0] == "twist" else \
+        targets.translate(sc.node_pos, act, sc.op[1])
+    pr = ed.EDProblem(sc.node_pos, nb, aidx, aw, sc.blocks, sc.block_type, aims)
+    t_setup = time.perf_counter() - t0
+    t1 = time.perf_counter()
+    x, _ = ed.gauss_newton(pr, max_iters=gn_iters, early_exit=False)
+    t_gn = (time.perf_counter() - t1) / gn_iters
+    rot, tr = ed.put_free_inputs(pr, x)
+    m = min(skin_n, sc.n_gauss)
+    E = skin.end_points(sc.pos[:m], sc.rot[:m], sc.scale[:m])
+    idx, w = ed.knn_weights(E.reshape(-1, 3), sc.node_pos, sc.k)
+    t2 = time.perf_counter()
+    skin.skin_gaussians(E, idx, w, rot, tr, sc.node_pos, sc.rot[:m], sc.scale[:m], sc.shs[:m])
+    t_skin = (time.perf_counter() - t2) * sc.n_gauss / m
+    ms = (t_gn * sc.iters + t_skin) * 1e3
+    return ms, t_setup, t_gn, t_skin
+
+
+def cpu_baseline(sc, samples=1):
+    ms, _, t_gn, t_skin = _oracle_frame_sample(sc)
+    return {"value": round(ms, 1), "unit": "ms/frame", "cores": 1, "kind": "port",
+            "sample": "oracle (numpy/scipy, float64): 1 Gauss-Newton iteration of the full %d-node solve "
+                      "(exact sparse solve) x %d iterations + skinning of 50k of %d Gaussians x %d; "
+                      "per-iteration %.2f s, skinning %.2f s" % (sc.n_nodes, sc.iters, sc.n_gauss,
+                                                                 sc.n_gauss // 50_000, t_gn, t_skin)}
+
+
+def run_reference(a):
+    ws, rank = _dist()
+    if rank != 0:
+        return
+    synth = importlib.import_module(PKG + ".synth")
+    sc = synth.make_scene(a.scene)
+    vals = []
+    for i in range(a.warmup + a.steps):
+        ms, _, _, _ = _oracle_frame_sample(sc)
+        if i >= a.warmup:
+            vals.append(ms)
+    import numpy as np
+    v = float(np.mean(vals))
+    line = {"metric": METRIC, "value": round(v, 1), "unit": "ms/frame", "n_gpus": ws, "steps": a.steps,
+            "warmup": a.warmup, "ms_per_step": round(v, 1), "higher_is_better": False, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
+            "config": {"workload": "%s (oracle port on host cores)" % sc.name},
+            "cpu_baseline": {"value": round(v, 1), "unit": "ms/frame", "cores": os.cpu_count(), "kind": "port",
+                             "sample": "1 GN iteration of the full solve + skinning of 50k Gaussians per step, "
+                                       "extrapolated to the frame"},
+            "e2e": {"value": round(v, 1), "unit": "ms/frame", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+if __name__ == "__main__":
+    a = _args()
+    if a.impl == "reference":
+        run_reference(a)
+    else:
+        run_ours(a)

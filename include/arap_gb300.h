@@ -1,0 +1,236 @@
+/*
+ * arap_gb300.h -- C ABI of the GB300 (sm_103a) embedded-deformation / ARAP
+ * hot path: kNN skinning weights, node graph, Gauss-Newton solve over node
+ * transforms, and skinning of Gaussians and density-grid samples.
+ *
+ * Conventions
+ *   - Every array argument is a DEVICE pointer owned by the caller unless the
+ *     parameter name ends in "_host".  Nothing is retained after a call except
+ *     inside an explicit handle (arap_solver).
+ *   - Every call takes the cudaStream_t it enqueues on (0 = legacy default).
+ *     Calls return after enqueueing; results are ready once the stream is.
+ *   - Every call returns an int status (ARAP_OK = 0).  Errors raised on the
+ *     device (non-finite values, timed-out barrier waits) are reported by the
+ *     calls that synchronise (arap_solver_solve, arap_get_device_status).
+ *   - Points are float32 xyz triples; quaternions are (w, x, y, z) float32;
+ *     node rotations are column-major 3x3 ("[0 3 6; 1 4 7; 2 5 8]"), exactly
+ *     DeformGraph::rot (Deform.hpp:29-38).
+ *   - "planes" layout: a per-item array with C components is stored as C
+ *     contiguous planes of length P (component c of item i at [c*P + i]).
+ */
+#ifndef ARAP_GB300_H
+#define ARAP_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct CUstream_st* arap_stream_t; /* == cudaStream_t */
+
+enum {
+  ARAP_OK = 0,
+  ARAP_NOT_CONVERGED = 1, /* iteration cap hit with early exit enabled (Deform.cpp:112-115 prints only) */
+  ARAP_ENONFINITE = 2,    /* NaN/Inf produced (e.g. zero kNN radius, singular block) */
+  ARAP_EBADINPUT = 3,     /* invalid sizes / indices / null pointers */
+  ARAP_ETIMEOUT = 4,      /* a bounded device-side wait gave up */
+  ARAP_ECUDA = 5,         /* a CUDA runtime call failed */
+  ARAP_ENOMEM = 6,        /* device allocation inside a handle failed */
+  ARAP_EUNSUPPORTED = 7   /* parameter outside the compiled range (e.g. k > 12) */
+};
+
+#define ARAP_KNN_MAX 12 /* KNN_MAX, helper.hpp:48 */
+
+/* ----------------------------------------------------------------- kNN --- */
+
+/* Node graph: for every node its k nearest OTHER nodes, ascending distance.
+ * Replaces DeformGraph::setupEdges / findNearestNodes (Deform.hpp:84-95,
+ * 153-185).  nodes_xyz [n*3]; neighbors_out [n*k] row-major (node-major).
+ * Requires 1 <= k <= ARAP_KNN_MAX and n >= k+1. */
+int arap_build_graph(const float* nodes_xyz, int n, int k, int32_t* neighbors_out,
+                     arap_stream_t stream);
+
+/* Skinning weights of P points against n nodes: the k nearest nodes and
+ * w_j = (1 - d_j/d_{k+1})^2 / sum (Deform.hpp:187-208, used by
+ * GaussianView::setupWeights* GaussianView.cpp:2818-2918).
+ * points_xyz [P*3]; idx_out, w_out in planes layout [k][P] (entry j of point i
+ * at [j*P + i]).  Distances are compared as float32 sqrt((dx*dx+dy*dy)+dz*dz);
+ * exact ties go to the lower node index. */
+int arap_compute_weights(const float* points_xyz, int P, const float* nodes_xyz, int n,
+                         int k, int32_t* idx_out, float* w_out, arap_stream_t stream);
+
+/* --------------------------------------------------------------- solver --- */
+
+enum { ARAP_PRECISION_PLAIN = 0, ARAP_PRECISION_MIXED = 1 };
+
+typedef struct {
+  float w_rot;            /* DeformGraph::w_rot (default 1),  Deform.hpp:56 */
+  float w_reg;            /* DeformGraph::w_reg (default 10), Deform.hpp:57 */
+  float w_con;            /* DeformGraph::w_con (default 100),Deform.hpp:58 */
+  float weighting_factor; /* GaussianView::_weighting_factor (default 1) */
+  int cons_on_center;     /* _constraints_on_center: one residual per block centre */
+  int max_iters;          /* Gauss-Newton iterations (reference MAX_ITERS = 30) */
+  int early_exit;         /* stop when |h| < (|x|+1e-6)*1e-6 (Deform.cpp:165) */
+  int precision;          /* ARAP_PRECISION_PLAIN or ARAP_PRECISION_MIXED */
+  float pcg_tol;          /* relative residual target of the inner PCG (<=0: default) */
+  int pcg_max_iters;      /* inner PCG iteration cap (<=0: default) */
+} arap_solve_config;
+
+typedef struct {
+  int status;             /* ARAP_* of the last solve */
+  int gn_iterations;      /* Gauss-Newton iterations executed */
+  int pcg_iterations;     /* total inner PCG iterations */
+  int halvings;           /* total line-search step halvings */
+  double initial_energy;  /* f.f at x = identity */
+  double final_energy;    /* f.f at the returned x */
+  int n_free, n_static, n_rows;
+} arap_solve_stats;
+
+typedef struct arap_solver arap_solver;
+
+/* Fill *cfg with the reference's defaults (Deform.hpp:54-58,
+ * GaussianView.hpp:429,459; MAX_ITERS Deform.cpp:3). */
+void arap_solve_config_default(arap_solve_config* cfg);
+
+/* Build a solve plan for one control-region configuration.  Replaces the
+ * bookkeeping of the Deform constructor (Deform.hpp:414-455: row counts,
+ * free/static sets from UpdateIndicies GaussianView.cpp:2010-2035,
+ * BelongsToSameBlock Deform.cpp:20-32, SelectKeyControls Deform.cpp:34-75).
+ *   neighbors   [n*k]  device, from arap_build_graph
+ *   anchor_idx  [k][n] device planes: kNN of each node's own vertex
+ *   anchor_w    [k][n] device planes  (cand_vertices[nodes[i].Vertex_index])
+ *   block_offsets_host [n_blocks+1], block_nodes_host [...]: node ids of each
+ *       block in block order (DeformGraph::indices_blocks)
+ *   block_type_host [n_blocks]: 1 active, 0 pinned, -1 excluded (blocks_type)
+ * The plan owns its device buffers; free with arap_solver_destroy. */
+int arap_solver_create(arap_solver** out, int n, int k, const int32_t* neighbors,
+                       const int32_t* anchor_idx, const float* anchor_w,
+                       const int32_t* block_offsets_host, const int32_t* block_nodes_host,
+                       const int32_t* block_type_host, int n_blocks,
+                       const arap_solve_config* cfg, arap_stream_t stream);
+
+/* One deformation solve (Deform::real_time_deform, Deform.cpp:77-169, then
+ * DeformGraph::putFreeInputs Deform.hpp:140-151).
+ *   node_pos [n*3]  current node positions (DeformGraph::nodes[i].Position)
+ *   aims     [n*3]  control targets (GaussianView::aim_positions)
+ *   rot_out  [n*9]  column-major R per node (identity for static nodes)
+ *   trans_out[n*3]  t per node (zero for static nodes)
+ *   stats_host      optional; when non-null the call synchronises the stream
+ *                   and fills it. */
+int arap_solver_solve(arap_solver* s, const float* node_pos, const float* aims,
+                      float* rot_out, float* trans_out, arap_solve_stats* stats_host,
+                      arap_stream_t stream);
+
+/* Gradient of 0.5*|f(x)|^2 as the reference's Jacobian states it (J^T f,
+ * Deform.cpp:120-122) at x [F*12] (free-node order, [R col-major | t]).
+ * grad_out [F*12]; energy_host (optional, synchronises) = f.f. */
+int arap_solver_energy_grad(arap_solver* s, const float* node_pos, const float* aims,
+                            const double* x, double* grad_out, double* energy_host,
+                            arap_stream_t stream);
+
+/* Number of free nodes (columns/12) and the free node ids ascending. */
+int arap_solver_free_count(const arap_solver* s);
+int arap_solver_free_ids(const arap_solver* s, int32_t* free_ids_host);
+
+void arap_solver_destroy(arap_solver* s);
+
+/* ------------------------------------------------------------ skinning --- */
+
+/* Per-node transform table used by every skinning call: for node j
+ * [R row-major 9 | g 3 | t+g 3 | 0] (16 floats).  Built from the solve
+ * output and the node positions the solve used. */
+int arap_node_table(int n, const float* rot, const float* trans, const float* node_pos,
+                    float* table_out, arap_stream_t stream);
+
+/* Six endpoints per Gaussian mu +/- (s_a + 1e-3) * 2 * R(q) e_a
+ * (GaussianView::GetEndPoints, GaussianView.cpp:4643-4668).
+ * ends_out in planes layout [18][N] (endpoint e, component c at plane 3e+c;
+ * e = 2a for +axis a, 2a+1 for -axis a).  ends_xyz_out (optional) receives the
+ * same points endpoint-major as xyz triples [(e*N + i)*3 + c], the input
+ * arap_compute_weights expects for the endpoint weights. */
+int arap_end_points(int N, const float* pos, const float* rot, const float* scale,
+                    float* ends_out, float* ends_xyz_out, arap_stream_t stream);
+
+/* One frame of Gaussian skinning, fused:
+ *   ED blend of the 6 endpoints (GaussianView::UpdatePosition,
+ *   GaussianView.cpp:3022-3040; DeformGraph::predict_mesh Deform.hpp:230-249)
+ *   then the per-Gaussian refit (UpdateAsSixPointsWithdrawBad,
+ *   GaussianView.cpp:3081-3166): centre, M = (P - c) Q^+, polar R/K,
+ *   quaternion, scale K_a/((s0_a+1e-3)*2)*s0_a, SH rotated by q q_old^-1.
+ *   ends      [18][N] in/out (deformed in place, every Gaussian)
+ *   ends_idx  [k][6][N], ends_w [k][6][N]: kNN of each endpoint, exactly what
+ *             arap_compute_weights returns for the 6N endpoint-major points
+ *             (neighbour j of endpoint e of Gaussian i at [(j*6 + e)*N + i])
+ *   node_table[n*16] from arap_node_table
+ *   scale0    [N*3]  scales at endpoint creation (scale_backup_vector)
+ *   static_mask [N] (uint8, optional): 1 = skip refit (static_gaussians)
+ *   pos_out [N*3], rot_inout [N*4] (in: q of the previous frame), scale_out [N*3]
+ *   shs_inout [N*48] optional, cov_out [N*6] optional (xx,xy,xz,yy,yz,zz of
+ *   R diag(s)^2 R^T). */
+int arap_skin_gaussians(int N, int k, float* ends, const int32_t* ends_idx,
+                        const float* ends_w, const float* node_table, const float* scale0,
+                        const uint8_t* static_mask, float* pos_out, float* rot_inout,
+                        float* scale_out, float* shs_inout, float* cov_out, int precision,
+                        arap_stream_t stream);
+
+/* Per-node unit quaternion of the Newton polar factor of R
+ * (FastUpdateSamplesSH, GaussianView.cpp:3172-3181; FastgetOthogonalMatrix
+ * helper.cpp:506-517).  quat_out [n*4] (w,x,y,z). */
+int arap_node_quaternions(int n, const float* rot, float* quat_out, int precision,
+                          arap_stream_t stream);
+
+/* One frame of sample skinning, fused: ED blend of the sample position
+ * (UpdatePositionforSamples GaussianView.cpp:3060-3077) and slerp-blended
+ * rotation of the sample's 48-float feature (RotateSHs cudakdtree.cu:201-222).
+ *   sample_pos [S*3] in/out, idx/w [k][S] planes, node_table, node_quat [n*4],
+ *   feature [S*48] in/out (optional), static_mask [S] uint8 optional. */
+int arap_skin_samples(int S, int k, float* sample_pos, const int32_t* idx, const float* w,
+                      const float* node_table, const float* node_quat, float* feature,
+                      const uint8_t* static_mask, arap_stream_t stream);
+
+/* New node positions: ED blend of each node's position with its anchor kNN
+ * (GaussianView.cpp:3042-3052).  node_pos_out must not alias node_table's
+ * source positions. */
+int arap_update_nodes(int n, int k, const float* node_pos, const int32_t* anchor_idx,
+                      const float* anchor_w, const float* node_table, float* node_pos_out,
+                      arap_stream_t stream);
+
+/* Items whose k neighbours are all static (CheckStaticSamples,
+ * GaussianView.cpp:2038-2070).  For Gaussians pass the 6 endpoint kNN as
+ * groups=6 (a Gaussian is static only if all 6*k neighbours are).
+ * node_is_static [n] uint8; mask_out [P] uint8. */
+int arap_static_mask(int P, int k, int groups, const int32_t* idx,
+                     const uint8_t* node_is_static, uint8_t* mask_out, arap_stream_t stream);
+
+/* ----------------------------------------------------- control targets --- */
+
+/* Control-target generators on the active blocks (type 1), in place on aims:
+ *   translate: aims += delta                (UpdateAimPosition GaussianView.cpp:2920-2933)
+ *   twist:     rotate about an axis through the active centroid by radian
+ *              (UpdateAimPositionTwist 2935-2959, PointRotateByAxis helper.cpp:1077-1100)
+ *   scale:     centre + s*(aim - centre)    (UpdateAimPositionScale 2961-2983)
+ * active_nodes [n_active] (device): node ids of the active blocks in block
+ * order; a node listed twice is moved twice, as the reference loops do.  The
+ * centroid is the mean of node_pos over the same list. */
+int arap_aims_translate(float* aims, const int32_t* active_nodes, int n_active, float dx,
+                        float dy, float dz, arap_stream_t stream);
+int arap_aims_twist(float* aims, const float* node_pos, const int32_t* active_nodes,
+                    int n_active, float ax, float ay, float az, float radian,
+                    arap_stream_t stream);
+int arap_aims_scale(float* aims, const float* node_pos, const int32_t* active_nodes,
+                    int n_active, float s, arap_stream_t stream);
+
+/* --------------------------------------------------------------- misc --- */
+
+/* Read and clear the library's sticky device error word (ARAP_* code). */
+int arap_get_device_status(arap_stream_t stream);
+
+/* Library version string. */
+const char* arap_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* ARAP_GB300_H */
