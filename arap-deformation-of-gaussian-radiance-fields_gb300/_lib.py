@@ -31,6 +31,12 @@ class SolveConfig(C.Structure):
                 ("pcg_tol", C.c_float), ("pcg_max_iters", C.c_int)]
 
 
+class GridInfo(C.Structure):
+    _fields_ = [("min_xyz", C.c_float * 3), ("max_xyz", C.c_float * 3), ("step", C.c_float),
+                ("interval", C.c_float), ("grid_num", C.c_int), ("n_valid", C.c_int),
+                ("n_pairs", C.c_longlong)]
+
+
 class SolveStats(C.Structure):
     _fields_ = [("status", C.c_int), ("gn_iterations", C.c_int), ("pcg_iterations", C.c_int),
                 ("halvings", C.c_int), ("initial_energy", C.c_double), ("final_energy", C.c_double),
@@ -66,6 +72,12 @@ SIGNATURES = {
     "arap_aims_translate": (I, [P, P, I, F, F, F, P]),
     "arap_aims_twist": (I, [P, P, P, I, F, F, F, F, P]),
     "arap_aims_scale": (I, [P, P, P, I, F, P]),
+    "arap_grid_build": (I, [C.POINTER(P), I, P, P, P, P, I, I, C.POINTER(GridInfo), P]),
+    "arap_grid_arrays": (I, [P, C.POINTER(P), C.POINTER(P), C.POINTER(P)]),
+    "arap_grid_samples": (I, [P, P, P]),
+    "arap_grid_ada_lpf": (I, [P, P, F, P, P]),
+    "arap_grid_density": (I, [P, P, P, P, P, P, P, P, F, P, P, P]),
+    "arap_grid_destroy": (None, [P]),
     "arap_get_device_status": (I, [P]),
     "arap_version": (C.c_char_p, []),
 }

@@ -1,0 +1,615 @@
+// Density grid (sm_103a): scene box, Gaussian -> cell CSR, grid samples,
+// adaptive low-pass filter and Gaussian-mixture density sampling.
+//
+// Reference: getOverallAABB (GaussianView.cpp:3601-3631), the per-Gaussian
+// boxes and cell binning of getGridSamples / UpdateContainingRelationship
+// (GaussianView.cpp:3634-3867, 3870-4149; GetBoxesGsGrid cudakdtree.cu:425-451),
+// the serial list fill (GaussianView.cpp:4077-4100) whose per-cell order --
+// ascending Gaussian index -- is reproduced by a per-cell sort after an
+// atomic fill, GetAdaLpfRatio (GaussianView.cpp:4670-4751) and the host
+// contract of CudaRasterizer::forward3d_grid (GaussianView.cpp:4222-4249).
+#include <climits>
+#include <new>
+
+#include "arap_common.cuh"
+
+namespace arap {
+
+struct GridParams {
+  float mn[3];
+  float mx[3];
+  float step;
+  float interval;
+  int g;
+  int padding;
+};
+
+__device__ __forceinline__ unsigned int f2ord(float f) {
+  const unsigned int u = __float_as_uint(f);
+  return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__device__ __forceinline__ float ord2f(unsigned int u) {
+  return __uint_as_float((u & 0x80000000u) ? (u & 0x7fffffffu) : ~u);
+}
+
+__global__ void minmax_kernel(int N, const float* __restrict__ pos, unsigned int* __restrict__ mm) {
+  unsigned int lo[3] = {0xffffffffu, 0xffffffffu, 0xffffffffu}, hi[3] = {0u, 0u, 0u};
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x) {
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const unsigned int o = f2ord(pos[3 * (size_t)i + c]);
+      lo[c] = min(lo[c], o);
+      hi[c] = max(hi[c], o);
+    }
+  }
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      lo[c] = min(lo[c], __shfl_xor_sync(0xffffffffu, lo[c], o));
+      hi[c] = max(hi[c], __shfl_xor_sync(0xffffffffu, hi[c], o));
+    }
+  }
+  if ((threadIdx.x & 31) == 0) {
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      atomicMin(mm + c, lo[c]);
+      atomicMax(mm + 3 + c, hi[c]);
+    }
+  }
+}
+
+// getOverallAABB in float32, then grid_step = max over axes of extent / g.
+__global__ void params_kernel(const unsigned int* __restrict__ mm, int g, int padding, GridParams* P) {
+  if (threadIdx.x != 0) return;
+  float mn[3], mx[3];
+  for (int c = 0; c < 3; ++c) {
+    const float a = ord2f(mm[c]), b = ord2f(mm[3 + c]);
+    const float mean = (b + a) / 2.0f;
+    const float lo = (a - mean) * 1.1f + mean;
+    const float hi = ((b - mean) * 1.1f + mean - lo) * 1.0078125f + lo;
+    mn[c] = fminf(lo, -0.75f);
+    mx[c] = fmaxf(hi, 0.75f);
+  }
+  float step = 0.f;
+  for (int c = 0; c < 3; ++c) {
+    P->mn[c] = mn[c];
+    P->mx[c] = mx[c];
+    step = fmaxf(step, (mx[c] - mn[c]) / (float)g);
+  }
+  P->step = step;
+  P->interval = step / 4.0f;
+  P->g = g;
+  P->padding = padding;
+}
+
+// Per-Gaussian cell range of its box (GaussianView.cpp:3961-4019, 4077-4085)
+// and the per-cell counts.
+__global__ void ranges_kernel(int N, const float* __restrict__ pos, const float* __restrict__ rot,
+                              const float* __restrict__ scale, const float* __restrict__ opacity,
+                              const GridParams* __restrict__ Pg, int* __restrict__ ranges,
+                              int* __restrict__ cell_count) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= N) return;
+  const GridParams P = *Pg;
+  const float a = opacity[i];
+  const float cut = 1.0f / 255.0f;
+  float f = 0.f;
+  if (!(a <= cut)) f = sqrtf(-2.0f * logf(cut / a));
+  float R[9];
+  quat_to_rowmajor(quat_normalize(__ldg(reinterpret_cast<const float4*>(rot) + i)), R);
+  const float p[3] = {pos[3 * (size_t)i], pos[3 * (size_t)i + 1], pos[3 * (size_t)i + 2]};
+  float lo[3] = {p[0], p[1], p[2]}, hi[3] = {p[0], p[1], p[2]};
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    const float s3 = f * scale[3 * (size_t)i + d];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const float e = R[c * 3 + d] * s3;
+      const float u = p[c] + e, v = p[c] - e;
+      lo[c] = fminf(lo[c], fminf(u, v));
+      hi[c] = fmaxf(hi[c], fmaxf(u, v));
+    }
+  }
+  int r[6];
+  int cnt = 1;
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    r[2 * c] = max((int)floorf((lo[c] - P.mn[c]) / P.step) - P.padding, 0);
+    r[2 * c + 1] = min((int)floorf((hi[c] - P.mn[c]) / P.step) + P.padding, P.g - 1);
+    cnt *= max(0, r[2 * c + 1] - r[2 * c] + 1);
+  }
+#pragma unroll
+  for (int t = 0; t < 6; ++t) ranges[6 * (size_t)i + t] = r[t];
+  if (cnt <= 0) return;
+  const int g = P.g;
+  for (int x = r[0]; x <= r[1]; ++x)
+    for (int y = r[2]; y <= r[3]; ++y)
+      for (int z = r[4]; z <= r[5]; ++z) atomicAdd(cell_count + ((size_t)x * g + y) * g + z, 1);
+}
+
+__global__ void fill_kernel(int N, const int* __restrict__ ranges, const GridParams* __restrict__ Pg,
+                            const int* __restrict__ off, int* __restrict__ cursor, int* __restrict__ lists) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= N) return;
+  const int g = Pg->g;
+  const int* r = ranges + 6 * (size_t)i;
+  for (int x = r[0]; x <= r[1]; ++x)
+    for (int y = r[2]; y <= r[3]; ++y)
+      for (int z = r[4]; z <= r[5]; ++z) {
+        const size_t c = ((size_t)x * g + y) * g + z;
+        const int slot = atomicAdd(cursor + c, 1);
+        lists[off[c] + slot] = i;
+      }
+}
+
+// ------------------------------------------------------------- scan -----
+constexpr int kScanThreads = 256;
+constexpr int kScanItems = 4;
+constexpr int kScanTile = kScanThreads * kScanItems;
+
+__global__ void scan_reduce_kernel(int n, const int* __restrict__ in, long long* __restrict__ sums) {
+  long long v[1] = {0};
+  const int base = blockIdx.x * kScanTile;
+  for (int t = threadIdx.x; t < kScanTile; t += kScanThreads) {
+    const int i = base + t;
+    if (i < n) v[0] += in[i];
+  }
+  double d[1] = {(double)v[0]};
+  block_sum<1>(d);
+  if (threadIdx.x == 0) sums[blockIdx.x] = (long long)llrint(d[0]);
+}
+
+// exclusive scan of the tile sums by one CTA; total at sums[nb]
+__global__ void scan_sums_kernel(int nb, long long* __restrict__ sums) {
+  __shared__ long long s_carry;
+  if (threadIdx.x == 0) s_carry = 0;
+  __syncthreads();
+  for (int base = 0; base < nb; base += blockDim.x) {
+    const int i = base + threadIdx.x;
+    long long v = i < nb ? sums[i] : 0;
+    // inclusive warp scan
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    long long x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const long long y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += y;
+    }
+    __shared__ long long s_w[32];
+    if (lane == 31) s_w[w] = x;
+    __syncthreads();
+    if (w == 0) {
+      long long t = lane < (int)(blockDim.x >> 5) ? s_w[lane] : 0;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const long long y = __shfl_up_sync(0xffffffffu, t, o);
+        if (lane >= o) t += y;
+      }
+      s_w[lane] = t;
+    }
+    __syncthreads();
+    const long long incl = x + (w > 0 ? s_w[w - 1] : 0) + s_carry;
+    if (i < nb) sums[i] = incl - v;
+    __syncthreads();
+    if (threadIdx.x == blockDim.x - 1) s_carry = incl;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) sums[nb] = s_carry;
+}
+
+__global__ void scan_apply_kernel(int n, const int* __restrict__ in, const long long* __restrict__ sums,
+                                  int* __restrict__ out) {
+  __shared__ long long s_w[kScanThreads / 32];
+  const int base = blockIdx.x * kScanTile + threadIdx.x * kScanItems;
+  long long loc[kScanItems];
+  long long t = 0;
+#pragma unroll
+  for (int j = 0; j < kScanItems; ++j) {
+    const int i = base + j;
+    loc[j] = t;
+    t += (i < n) ? in[i] : 0;
+  }
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  long long x = t;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const long long y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) s_w[w] = x;
+  __syncthreads();
+  long long wp = 0;
+  for (int q = 0; q < w; ++q) wp += s_w[q];
+  const long long excl = sums[blockIdx.x] + wp + x - t;
+#pragma unroll
+  for (int j = 0; j < kScanItems; ++j) {
+    const int i = base + j;
+    if (i < n) {
+      const long long v = excl + loc[j];
+      out[i] = v > INT_MAX ? INT_MAX : (int)v;
+    }
+  }
+  if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) out[n] = (int)min(sums[gridDim.x], (long long)INT_MAX);
+}
+
+// ------------------------------------------------------ per-cell sort ----
+__global__ void flags_kernel(int n, const int* __restrict__ count, int* __restrict__ flag) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) flag[i] = count[i] > 0 ? 1 : 0;
+}
+
+__global__ void compact_kernel(int n, const int* __restrict__ count, const int* __restrict__ pos,
+                               int* __restrict__ valid) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n && count[i] > 0) valid[pos[i]] = i;
+}
+
+constexpr int kSortMax = 16384;
+
+// Bitonic sort of each occupied cell's list in shared memory (one CTA per cell).
+__global__ void sort_cells_kernel(int nvalid, const int* __restrict__ valid, const int* __restrict__ off,
+                                  int* __restrict__ lists) {
+  extern __shared__ int s_keys[];
+  const int v = blockIdx.x;
+  if (v >= nvalid) return;
+  const int c = valid[v];
+  const int b = off[c], L = off[c + 1] - b;
+  if (L <= 1) return;
+  if (L > kSortMax) {
+    if (threadIdx.x == 0) raise_status(ARAP_EUNSUPPORTED);
+    return;
+  }
+  int P2 = 1;
+  while (P2 < L) P2 <<= 1;
+  for (int t = threadIdx.x; t < P2; t += blockDim.x) s_keys[t] = t < L ? lists[b + t] : INT_MAX;
+  __syncthreads();
+  for (int k = 2; k <= P2; k <<= 1) {
+    for (int j = k >> 1; j > 0; j >>= 1) {
+      for (int t = threadIdx.x; t < P2; t += blockDim.x) {
+        const int u = t ^ j;
+        if (u > t) {
+          const int a = s_keys[t], bb = s_keys[u];
+          const bool up = (t & k) == 0;
+          if ((a > bb) == up) {
+            s_keys[t] = bb;
+            s_keys[u] = a;
+          }
+        }
+      }
+      __syncthreads();
+    }
+  }
+  for (int t = threadIdx.x; t < L; t += blockDim.x) lists[b + t] = s_keys[t];
+}
+
+// 64 samples per occupied cell (GaussianView.cpp:4104-4133).
+__global__ void samples_kernel(int nvalid, const int* __restrict__ valid, const GridParams* __restrict__ Pg,
+                               float* __restrict__ out) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nvalid * 64) return;
+  const GridParams P = *Pg;
+  const int v = t >> 6, s = t & 63;
+  const int c = valid[v];
+  const int g = P.g;
+  const int ci[3] = {c / (g * g), (c % (g * g)) / g, c % g};
+  const int si[3] = {s / 16, (s % 16) / 4, s % 4};
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    const float base = (float)((double)(P.mn[d] + (float)ci[d] * P.step) + 0.5 * (double)P.interval);
+    out[3 * (size_t)t + d] = base + (float)si[d] * P.interval;
+  }
+}
+
+// GetAdaLpfRatio: M = P Q^T (Q Q^T)^-1 with Q the unit-cube corners and P
+// the corner samples' offsets / 3; out = lpf * M M^T (row-major 3x3).
+__global__ void ada_lpf_kernel(int nvalid, const float* __restrict__ samples, float lpf, float* __restrict__ out) {
+  const int v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= nvalid) return;
+  const float* S = samples + (size_t)v * 64 * 3;
+  float PQ[3][3] = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};  // [coord][axis]
+#pragma unroll
+  for (int cidx = 1; cidx < 8; ++cidx) {
+    const int bx = cidx & 1, by = (cidx >> 1) & 1, bz = (cidx >> 2) & 1;
+    const int idx = bx * 48 + by * 12 + bz * 3;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      const float pd = (S[3 * idx + d] - S[d]) / 3.0f;
+      if (bx) PQ[d][0] += pd;
+      if (by) PQ[d][1] += pd;
+      if (bz) PQ[d][2] += pd;
+    }
+  }
+  // (Q Q^T)^-1 = 0.5 I - 0.125 * ones
+  float M[3][3];
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    const float s = PQ[d][0] + PQ[d][1] + PQ[d][2];
+#pragma unroll
+    for (int j = 0; j < 3; ++j) M[d][j] = 0.5f * PQ[d][j] - 0.125f * s;
+  }
+#pragma unroll
+  for (int a = 0; a < 3; ++a)
+#pragma unroll
+    for (int b = 0; b < 3; ++b)
+      out[(size_t)v * 9 + a * 3 + b] = lpf * (M[a][0] * M[b][0] + M[a][1] * M[b][1] + M[a][2] * M[b][2]);
+}
+
+// Density sampling: one CTA of 64 threads per occupied cell, one thread per
+// sample; the cell's Gaussians are staged in shared memory in chunks with
+// their inverse filtered covariance (S_i + L)^-1.
+constexpr int kDensChunk = 64;
+
+__global__ void __launch_bounds__(64) density_kernel(
+    int nvalid, const int* __restrict__ valid, const int* __restrict__ off, const int* __restrict__ lists,
+    const float* __restrict__ pos, const float* __restrict__ rot, const float* __restrict__ scale,
+    const float* __restrict__ opacity, const float* __restrict__ shs, const float* __restrict__ samples,
+    const float* __restrict__ ada, float lpf, float* __restrict__ sigma, float* __restrict__ feat) {
+  __shared__ float s_mu[kDensChunk][3];
+  __shared__ float s_A[kDensChunk][6];
+  __shared__ float s_a[kDensChunk];
+  __shared__ float s_sh[kDensChunk][48];
+  const int v = blockIdx.x;
+  if (v >= nvalid) return;
+  const int c = valid[v];
+  const int b = off[c], L = off[c + 1] - b;
+  float Lm[6];
+  if (ada) {
+    const float* m = ada + (size_t)v * 9;
+    Lm[0] = m[0]; Lm[1] = m[1]; Lm[2] = m[2]; Lm[3] = m[4]; Lm[4] = m[5]; Lm[5] = m[8];
+  } else {
+    Lm[0] = lpf; Lm[1] = 0.f; Lm[2] = 0.f; Lm[3] = lpf; Lm[4] = 0.f; Lm[5] = lpf;
+  }
+  const int s = threadIdx.x;
+  const size_t sid = (size_t)v * 64 + s;
+  const float x = samples[3 * sid], y = samples[3 * sid + 1], z = samples[3 * sid + 2];
+  float acc = 0.f;
+  float F[48];
+#pragma unroll
+  for (int t = 0; t < 48; ++t) F[t] = 0.f;
+  for (int c0 = 0; c0 < L; c0 += kDensChunk) {
+    const int cnt = min(kDensChunk, L - c0);
+    __syncthreads();
+    if (s < cnt) {
+      const int gi = lists[b + c0 + s];
+      float R[9];
+      quat_to_rowmajor(quat_normalize(__ldg(reinterpret_cast<const float4*>(rot) + gi)), R);
+      const float s2[3] = {scale[3 * (size_t)gi] * scale[3 * (size_t)gi],
+                           scale[3 * (size_t)gi + 1] * scale[3 * (size_t)gi + 1],
+                           scale[3 * (size_t)gi + 2] * scale[3 * (size_t)gi + 2]};
+      float C6[6];
+      int o = 0;
+#pragma unroll
+      for (int r = 0; r < 3; ++r)
+#pragma unroll
+        for (int q = r; q < 3; ++q)
+          C6[o++] = R[r * 3] * s2[0] * R[q * 3] + R[r * 3 + 1] * s2[1] * R[q * 3 + 1] + R[r * 3 + 2] * s2[2] * R[q * 3 + 2];
+#pragma unroll
+      for (int t = 0; t < 6; ++t) C6[t] += Lm[t];
+      // inverse of the symmetric 3x3 (a b c; b d e; c e f)
+      const float a = C6[0], bb = C6[1], cc = C6[2], d = C6[3], e = C6[4], f = C6[5];
+      const float A0 = d * f - e * e, A1 = cc * e - bb * f, A2 = bb * e - cc * d;
+      const float det = a * A0 + bb * A1 + cc * A2;
+      const float id = 1.0f / det;
+      s_A[s][0] = A0 * id;
+      s_A[s][1] = A1 * id;
+      s_A[s][2] = A2 * id;
+      s_A[s][3] = (a * f - cc * cc) * id;
+      s_A[s][4] = (bb * cc - a * e) * id;
+      s_A[s][5] = (a * d - bb * bb) * id;
+      s_mu[s][0] = pos[3 * (size_t)gi];
+      s_mu[s][1] = pos[3 * (size_t)gi + 1];
+      s_mu[s][2] = pos[3 * (size_t)gi + 2];
+      s_a[s] = opacity[gi];
+    }
+    // stage SH cooperatively: cnt * 48 floats
+    for (int t = s; t < cnt * 12; t += 64) {
+      const int gq = t / 12, q4 = t % 12;
+      const int gi = lists[b + c0 + gq];
+      const float4 u = __ldg(reinterpret_cast<const float4*>(shs + 48 * (size_t)gi) + q4);
+      s_sh[gq][4 * q4] = u.x;
+      s_sh[gq][4 * q4 + 1] = u.y;
+      s_sh[gq][4 * q4 + 2] = u.z;
+      s_sh[gq][4 * q4 + 3] = u.w;
+    }
+    __syncthreads();
+    for (int q = 0; q < cnt; ++q) {
+      const float dx = x - s_mu[q][0], dy = y - s_mu[q][1], dz = z - s_mu[q][2];
+      const float* A = s_A[q];
+      const float m = A[0] * dx * dx + A[3] * dy * dy + A[5] * dz * dz +
+                      2.f * (A[1] * dx * dy + A[2] * dx * dz + A[4] * dy * dz);
+      const float gw = s_a[q] * __expf(-0.5f * m);
+      acc += gw;
+#pragma unroll
+      for (int t = 0; t < 48; ++t) F[t] = fmaf(gw, s_sh[q][t], F[t]);
+    }
+  }
+  sigma[sid] = acc;
+  float4* fo = reinterpret_cast<float4*>(feat + 48 * sid);
+#pragma unroll
+  for (int t = 0; t < 12; ++t) fo[t] = make_float4(F[4 * t], F[4 * t + 1], F[4 * t + 2], F[4 * t + 3]);
+}
+
+}  // namespace arap
+
+// ------------------------------------------------------------------ host --
+using namespace arap;
+
+struct arap_grid {
+  int N = 0, g = 0, padding = 1, nvalid = 0;
+  long long npairs = 0;
+  GridParams* params = nullptr;  // device
+  int* off = nullptr;            // [g^3 + 1]
+  int* lists = nullptr;          // [npairs]
+  int* valid = nullptr;          // [nvalid]
+  int* ranges = nullptr;         // [N*6]
+  GridParams host{};
+};
+
+static int scan_exclusive(const int* in, int* out, int n, long long* sums, cudaStream_t st) {
+  const int nb = (n + kScanTile - 1) / kScanTile;
+  scan_reduce_kernel<<<nb, kScanThreads, 0, st>>>(n, in, sums);
+  scan_sums_kernel<<<1, 1024, 0, st>>>(nb, sums);
+  scan_apply_kernel<<<nb, kScanThreads, 0, st>>>(n, in, sums, out);
+  ARAP_LAUNCH_CHECK();
+  return ARAP_OK;
+}
+
+extern "C" void arap_grid_destroy(arap_grid* G) {
+  if (!G) return;
+  cudaFree(G->params);
+  cudaFree(G->off);
+  cudaFree(G->lists);
+  cudaFree(G->valid);
+  cudaFree(G->ranges);
+  delete G;
+}
+
+extern "C" int arap_grid_build(arap_grid** out, int N, const float* pos, const float* rot, const float* scale,
+                               const float* opacity, int grid_num, int padding, arap_grid_info* info_host,
+                               arap_stream_t stream) {
+  if (!out) return ARAP_EBADINPUT;
+  *out = nullptr;
+  if (N < 1 || !pos || !rot || !scale || !opacity || grid_num < 1 || grid_num > 1024 || padding < 0)
+    return ARAP_EBADINPUT;
+  if (reinterpret_cast<uintptr_t>(rot) & 15) return ARAP_EBADINPUT;
+  cudaStream_t st = (cudaStream_t)stream;
+  const long long cells = (long long)grid_num * grid_num * grid_num;
+  if (cells >= INT_MAX) return ARAP_EUNSUPPORTED;
+  const int C = (int)cells;
+  auto* G = new (std::nothrow) arap_grid();
+  if (!G) return ARAP_ENOMEM;
+  G->N = N;
+  G->g = grid_num;
+  G->padding = padding;
+  int* count = nullptr;
+  int* cursor = nullptr;
+  int* flagpos = nullptr;
+  long long* sums = nullptr;
+  unsigned int* mm = nullptr;
+  int rc = ARAP_OK;
+  const int nbs = (C + 1 + kScanTile - 1) / kScanTile + 1;
+  auto fail = [&](int code) {
+    cudaFree(count);
+    cudaFree(cursor);
+    cudaFree(flagpos);
+    cudaFree(sums);
+    cudaFree(mm);
+    arap_grid_destroy(G);
+    return code;
+  };
+  if (cudaMalloc(&G->params, sizeof(GridParams)) || cudaMalloc(&G->off, sizeof(int) * ((size_t)C + 1)) ||
+      cudaMalloc(&G->ranges, sizeof(int) * 6 * (size_t)N) || cudaMalloc(&count, sizeof(int) * (size_t)C) ||
+      cudaMalloc(&cursor, sizeof(int) * (size_t)C) || cudaMalloc(&flagpos, sizeof(int) * ((size_t)C + 1)) ||
+      cudaMalloc(&sums, sizeof(long long) * (nbs + 1)) || cudaMalloc(&mm, sizeof(unsigned int) * 6)) {
+    (void)cudaGetLastError();
+    return fail(ARAP_ENOMEM);
+  }
+  const unsigned int init[6] = {0xffffffffu, 0xffffffffu, 0xffffffffu, 0u, 0u, 0u};
+  if (cudaMemcpyAsync(mm, init, sizeof(init), cudaMemcpyHostToDevice, st) ||
+      cudaMemsetAsync(count, 0, sizeof(int) * (size_t)C, st) || cudaMemsetAsync(cursor, 0, sizeof(int) * (size_t)C, st))
+    return fail(ARAP_ECUDA);
+  minmax_kernel<<<std::min(grid_for(N, 256), 1184), 256, 0, st>>>(N, pos, mm);
+  params_kernel<<<1, 32, 0, st>>>(mm, grid_num, padding, G->params);
+  ranges_kernel<<<grid_for(N, 128), 128, 0, st>>>(N, pos, rot, scale, opacity, G->params, G->ranges, count);
+  if (cudaPeekAtLastError() != cudaSuccess) {
+    (void)cudaGetLastError();
+    return fail(ARAP_ECUDA);
+  }
+  if ((rc = scan_exclusive(count, G->off, C, sums, st)) != ARAP_OK) return fail(rc);
+  long long total = 0;
+  if (cudaMemcpyAsync(&total, sums + (C + kScanTile - 1) / kScanTile, sizeof(long long), cudaMemcpyDeviceToHost, st) ||
+      cudaMemcpyAsync(&G->host, G->params, sizeof(GridParams), cudaMemcpyDeviceToHost, st) ||
+      cudaStreamSynchronize(st))
+    return fail(ARAP_ECUDA);
+  if (total >= INT_MAX) return fail(ARAP_EUNSUPPORTED);
+  G->npairs = total;
+  if (cudaMalloc(&G->lists, sizeof(int) * (size_t)std::max(total, 1ll))) {
+    (void)cudaGetLastError();
+    return fail(ARAP_ENOMEM);
+  }
+  fill_kernel<<<grid_for(N, 128), 128, 0, st>>>(N, G->ranges, G->params, G->off, cursor, G->lists);
+  flags_kernel<<<grid_for(C, 256), 256, 0, st>>>(C, count, cursor);
+  if ((rc = scan_exclusive(cursor, flagpos, C, sums, st)) != ARAP_OK) return fail(rc);
+  int nvalid = 0;
+  if (cudaMemcpyAsync(&nvalid, flagpos + C, sizeof(int), cudaMemcpyDeviceToHost, st) || cudaStreamSynchronize(st))
+    return fail(ARAP_ECUDA);
+  G->nvalid = nvalid;
+  if (cudaMalloc(&G->valid, sizeof(int) * (size_t)std::max(nvalid, 1))) {
+    (void)cudaGetLastError();
+    return fail(ARAP_ENOMEM);
+  }
+  compact_kernel<<<grid_for(C, 256), 256, 0, st>>>(C, count, flagpos, G->valid);
+  if (nvalid > 0) {
+    if (cudaFuncSetAttribute(sort_cells_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             kSortMax * (int)sizeof(int)))
+      return fail(ARAP_ECUDA);
+    sort_cells_kernel<<<nvalid, 256, kSortMax * sizeof(int), st>>>(nvalid, G->valid, G->off, G->lists);
+  }
+  if (cudaPeekAtLastError() != cudaSuccess) {
+    (void)cudaGetLastError();
+    return fail(ARAP_ECUDA);
+  }
+  if (cudaStreamSynchronize(st)) return fail(ARAP_ECUDA);
+  cudaFree(count);
+  cudaFree(cursor);
+  cudaFree(flagpos);
+  cudaFree(sums);
+  cudaFree(mm);
+  if (info_host) {
+    for (int c = 0; c < 3; ++c) {
+      info_host->min_xyz[c] = G->host.mn[c];
+      info_host->max_xyz[c] = G->host.mx[c];
+    }
+    info_host->step = G->host.step;
+    info_host->interval = G->host.interval;
+    info_host->grid_num = grid_num;
+    info_host->n_valid = nvalid;
+    info_host->n_pairs = total;
+  }
+  *out = G;
+  return arap_get_device_status(stream);
+}
+
+extern "C" int arap_grid_arrays(const arap_grid* G, const int32_t** cell_offsets, const int32_t** cell_lists,
+                                const int32_t** valid_cells) {
+  if (!G) return ARAP_EBADINPUT;
+  if (cell_offsets) *cell_offsets = G->off;
+  if (cell_lists) *cell_lists = G->lists;
+  if (valid_cells) *valid_cells = G->valid;
+  return ARAP_OK;
+}
+
+extern "C" int arap_grid_samples(const arap_grid* G, float* samples_out, arap_stream_t stream) {
+  if (!G || !samples_out) return ARAP_EBADINPUT;
+  if (G->nvalid == 0) return ARAP_OK;
+  samples_kernel<<<grid_for((long long)G->nvalid * 64, 256), 256, 0, (cudaStream_t)stream>>>(
+      G->nvalid, G->valid, G->params, samples_out);
+  ARAP_LAUNCH_CHECK();
+  return ARAP_OK;
+}
+
+extern "C" int arap_grid_ada_lpf(const arap_grid* G, const float* samples, float lpf, float* out,
+                                 arap_stream_t stream) {
+  if (!G || !samples || !out) return ARAP_EBADINPUT;
+  if (G->nvalid == 0) return ARAP_OK;
+  ada_lpf_kernel<<<grid_for(G->nvalid, 128), 128, 0, (cudaStream_t)stream>>>(G->nvalid, samples, lpf, out);
+  ARAP_LAUNCH_CHECK();
+  return ARAP_OK;
+}
+
+extern "C" int arap_grid_density(const arap_grid* G, const float* pos, const float* rot, const float* scale,
+                                 const float* opacity, const float* shs, const float* samples, const float* ada,
+                                 float lpf, float* sigma_out, float* feature_out, arap_stream_t stream) {
+  if (!G || !pos || !rot || !scale || !opacity || !shs || !samples || !sigma_out || !feature_out)
+    return ARAP_EBADINPUT;
+  if ((reinterpret_cast<uintptr_t>(rot) | reinterpret_cast<uintptr_t>(shs) |
+       reinterpret_cast<uintptr_t>(feature_out)) & 15)
+    return ARAP_EBADINPUT;
+  if (G->nvalid == 0) return ARAP_OK;
+  density_kernel<<<G->nvalid, 64, 0, (cudaStream_t)stream>>>(G->nvalid, G->valid, G->off, G->lists, pos, rot,
+                                                              scale, opacity, shs, samples, ada, lpf, sigma_out,
+                                                              feature_out);
+  ARAP_LAUNCH_CHECK();
+  return ARAP_OK;
+}

@@ -2,6 +2,7 @@
 // bookkeeping of the Deform constructor, Deform.hpp:414-455 and
 // Deform.cpp:6-75) and the C ABI.
 #include <algorithm>
+#include <cmath>
 #include <cstring>
 #include <new>
 #include <set>
@@ -244,6 +245,7 @@ extern "C" int arap_solver_create(arap_solver** out, int n, int k, const int32_t
     P.q = cv.take<float>((size_t)F * 12);
     P.g = cv.take<float>((size_t)F * 12);
     P.dinv = cv.take<float>((size_t)F * 144);
+    P.order = cv.take<int32_t>(F);
     P.partials = cv.take<double>((size_t)8 * grid);
     P.results = cv.take<double>(8);
     P.stats = cv.take<double>(8);
@@ -276,6 +278,26 @@ extern "C" int arap_solver_create(arap_solver** out, int n, int k, const int32_t
   e = e ? e : up(P.mem_rank, mem_rank.data(), mem_rank.size() * 4);
   e = e ? e : up(P.mem_node, mem_node.data(), mem_node.size() * 4);
   e = e ? e : up(P.mem_w, mem_w.data(), mem_w.size() * 4);
+  // cost-balanced processing order: heaviest nodes first, dealt to the warps
+  // in alternating direction so every warp gets a similar total
+  std::vector<int32_t> order(F);
+  {
+    std::vector<std::pair<long long, int>> cost(F);
+    for (int r = 0; r < F; ++r) {
+      long long c = 16;
+      for (int t = item_off[r]; t < item_off[r + 1]; ++t)
+        c += item_flat[t].x == ITEM_CON ? 1 + (grp_off[item_flat[t].z + 1] - grp_off[item_flat[t].z]) * k : 2;
+      cost[r] = {-c, r};
+    }
+    std::sort(cost.begin(), cost.end());
+    const int nw = grid * (kSolveThreads / 32);
+    for (int i = 0; i < F; ++i) {
+      const int rd = i / nw, w = i % nw;
+      const int src = rd * nw + ((rd & 1) ? std::min(nw, F - rd * nw) - 1 - w : w);
+      order[i] = cost[src].second;
+    }
+  }
+  e = e ? e : up(P.order, order.data(), order.size() * 4);
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   if (e != cudaSuccess) {
     cudaFree(s->block);
@@ -287,9 +309,9 @@ extern "C" int arap_solver_create(arap_solver** out, int n, int k, const int32_t
   P.F = F;
   P.G = G;
   P.U = U;
-  P.wr = sqrtf(cfg.w_rot);
-  P.wg = sqrtf(cfg.w_reg);
-  P.wc = sqrtf(cfg.w_con);
+  P.wr = std::sqrt((double)cfg.w_rot);
+  P.wg = std::sqrt((double)cfg.w_reg);
+  P.wc = std::sqrt((double)cfg.w_con);
   P.wf = wf;
   P.max_iters = cfg.max_iters;
   P.early_exit = cfg.early_exit;

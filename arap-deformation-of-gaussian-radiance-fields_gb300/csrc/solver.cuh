@@ -53,7 +53,9 @@ struct SolveParams {
   float* trans_out;          // [n*3]
   const double* x_in;        // grad-only mode: evaluation point
   double* grad_out;          // grad-only mode: J^T f
-  float wr, wg, wc, wf;      // square roots of w_rot, w_reg, w_con; weighting factor
+  double wr, wg, wc;         // square roots of w_rot, w_reg, w_con (Deform.hpp:452-454)
+  float wf;                  // weighting factor
+  const int32_t* order;      // [F] processing order of the free nodes (cost-balanced)
   int max_iters, early_exit, pcg_max;
   float pcg_tol;
   int mode;                  // 0 solve, 1 gradient/energy only

@@ -51,18 +51,24 @@ __device__ __forceinline__ void load_pt(const SolveParams& P, int rr, bool first
   }
 }
 
-// x + scale * h of free node rr (all 12, or the translation part).
+// Offset from the identity transform, dx = x + scale*h - [I | 0], of free
+// node rr.  Residuals are evaluated from dx so that float32 arithmetic does not
+// cancel O(1) terms ((R - I) d instead of R d - d, 2 dx_00 + |dx_0|^2 instead
+// of |c_0|^2 - 1); the formulas are algebraically those of Deform.cpp:378-581.
 template <typename RT>
 __device__ __forceinline__ void load_x(const SolveParams& P, int rr, RT scale, RT (&v)[12]) {
   const double* xp = P.x + 12 * (size_t)rr;
+  double d[12];
+#pragma unroll
+  for (int i = 0; i < 12; ++i) d[i] = __ldcg(xp + i) - ((i == 0 || i == 4 || i == 8) ? 1.0 : 0.0);
   if (scale != RT(0)) {
     float hv[12];
     ld12cg(P.h, rr, hv);
 #pragma unroll
-    for (int i = 0; i < 12; ++i) v[i] = RT(__ldcg(xp + i)) + scale * RT(hv[i]);
+    for (int i = 0; i < 12; ++i) v[i] = RT(d[i]) + scale * RT(hv[i]);
   } else {
 #pragma unroll
-    for (int i = 0; i < 12; ++i) v[i] = RT(__ldcg(xp + i));
+    for (int i = 0; i < 12; ++i) v[i] = RT(d[i]);
   }
 }
 
@@ -91,37 +97,41 @@ __device__ __forceinline__ void load_pos(const SolveParams& P, int node, RT (&v)
 // Constraint-group residual f_g (Deform.cpp:484-580) at x + scale*h:
 // wc * (sum_members sum_anchors a (R_l (v_c - g_l) + g_l + t_l)  [free l]
 //                                 a v_c                           [other l]
-//        - mult * target).
+//        - mult * target)
+// evaluated as wc * (sum_u [sum_free a ((R_l - I)(v_c - g_l) + t_l) + v_c sum a]
+//                    - mult * target).
 template <typename RT>
 __device__ void con_residual(const SolveParams& P, int g, RT scale, RT (&f)[3]) {
   f[0] = f[1] = f[2] = RT(0);
+  RT base[3] = {RT(0), RT(0), RT(0)};
   const int k = P.k;
   const int s0 = __ldg(P.grp_off + g), s1 = __ldg(P.grp_off + g + 1);
   for (int s = s0; s < s1; ++s) {
     RT v[3];
     load_pos<RT>(P, __ldg(P.grp_member + s), v);
+    RT wsum = RT(0);
     for (int t = 0; t < k; ++t) {
       const int slot = s * k + t;
       const RT a = RT(__ldg(P.mem_w + slot));
+      wsum += a;
       const int rk = __ldg(P.mem_rank + slot);
-      if (rk < 0) {
-#pragma unroll
-        for (int c = 0; c < 3; ++c) f[c] += a * v[c];
-      } else {
+      if (rk >= 0) {
         RT gl[3], X[12];
         load_pos<RT>(P, __ldg(P.mem_node + slot), gl);
         load_x<RT>(P, rk, scale, X);
         const RT d0 = v[0] - gl[0], d1 = v[1] - gl[1], d2 = v[2] - gl[2];
 #pragma unroll
-        for (int c = 0; c < 3; ++c) f[c] += a * (X[c] * d0 + X[3 + c] * d1 + X[6 + c] * d2 + gl[c] + X[9 + c]);
+        for (int c = 0; c < 3; ++c) f[c] += a * (X[c] * d0 + X[3 + c] * d1 + X[6 + c] * d2 + X[9 + c]);
       }
     }
+#pragma unroll
+    for (int c = 0; c < 3; ++c) base[c] += v[c] * wsum;
   }
   const float4 tg = P.grp_target[g];
   const RT wc = RT(P.wc);
-  f[0] = wc * (f[0] - RT(tg.w) * RT(tg.x));
-  f[1] = wc * (f[1] - RT(tg.w) * RT(tg.y));
-  f[2] = wc * (f[2] - RT(tg.w) * RT(tg.z));
+  f[0] = wc * (f[0] + (base[0] - RT(tg.w) * RT(tg.x)));
+  f[1] = wc * (f[1] + (base[1] - RT(tg.w) * RT(tg.y)));
+  f[2] = wc * (f[2] + (base[2] - RT(tg.w) * RT(tg.z)));
 }
 
 // J_g p of a constraint group (linear part only).
@@ -130,6 +140,7 @@ __device__ void con_jp(const SolveParams& P, int g, bool first, float beta, cons
   const int k = P.k;
   const int s0 = __ldg(P.grp_off + g), s1 = __ldg(P.grp_off + g + 1);
   for (int s = s0; s < s1; ++s) {
+#pragma unroll 4
     for (int t = 0; t < k; ++t) {
       const int slot = s * k + t;
       const int rk = __ldg(P.mem_rank + slot);
@@ -142,9 +153,10 @@ __device__ void con_jp(const SolveParams& P, int g, bool first, float beta, cons
         u[c] = fmaf(geo.x, fmaf(geo.y, pl[c], fmaf(geo.z, pl[3 + c], fmaf(geo.w, pl[6 + c], pl[9 + c]))), u[c]);
     }
   }
-  u[0] *= P.wc;
-  u[1] *= P.wc;
-  u[2] *= P.wc;
+  const float wcf = (float)P.wc;
+  u[0] *= wcf;
+  u[1] *= wcf;
+  u[2] *= wcf;
 }
 
 template <typename T>
@@ -204,7 +216,7 @@ __device__ void residual_node(const SolveParams& P, int r, RT scale, RT (&acc)[1
       if (m.y >= 0) load_xt<RT>(P, m.y, scale, tk);
       RT f[3];
 #pragma unroll
-      for (int c = 0; c < 3; ++c) f[c] = ws * (xj[c] * d[0] + xj[3 + c] * d[1] + xj[6 + c] * d[2] + xj[9 + c] - tk[c] - d[c]);
+      for (int c = 0; c < 3; ++c) f[c] = ws * (xj[c] * d[0] + xj[3 + c] * d[1] + xj[6 + c] * d[2] + (xj[9 + c] - tk[c]));
       e += double(f[0]) * double(f[0]) + double(f[1]) * double(f[1]) + double(f[2]) * double(f[2]);
       if (PASS == PASS_GRAD) {
         // Jacobian entries use the float difference (Deform.cpp:254-257) and
@@ -218,8 +230,9 @@ __device__ void residual_node(const SolveParams& P, int r, RT scale, RT (&acc)[1
           for (int rr = 0; rr < 3; ++rr) acc[3 * c + rr] += ws * RT(dJ[c]) * f[rr];
 #pragma unroll
         for (int rr = 0; rr < 3; ++rr) acc[9 + rr] += w * f[rr];
-        const float wsf = P.wg * s;
-        q_add(Q, wsf * dJ[0], wsf * dJ[1], wsf * dJ[2], P.wg);
+        const float wgf = (float)P.wg;
+        const float wsf = wgf * s;
+        q_add(Q, wsf * dJ[0], wsf * dJ[1], wsf * dJ[2], wgf);
       }
     } else if (m.x == ITEM_STATIC) {
       // f = -w t_j (Deform.cpp:458-482)
@@ -228,7 +241,7 @@ __device__ void residual_node(const SolveParams& P, int r, RT scale, RT (&acc)[1
       if (PASS == PASS_GRAD) {
 #pragma unroll
         for (int rr = 0; rr < 3; ++rr) acc[9 + rr] += -w * f[rr];
-        Q[9] += P.wg * P.wg;
+        Q[9] += (float)(P.wg * P.wg);
       }
     } else if (PASS == PASS_GRAD) {
       if (m.x == ITEM_IN) {
@@ -240,10 +253,10 @@ __device__ void residual_node(const SolveParams& P, int r, RT scale, RT (&acc)[1
         const RT d[3] = {gj[0] - gi[0], gj[1] - gi[1], gj[2] - gi[2]};
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
-          const RT f = ws * (xi[c] * d[0] + xi[3 + c] * d[1] + xi[6 + c] * d[2] + xi[9 + c] - xj[9 + c] - d[c]);
+          const RT f = ws * (xi[c] * d[0] + xi[3 + c] * d[1] + xi[6 + c] * d[2] + (xi[9 + c] - xj[9 + c]));
           acc[9 + c] += -ws * f;
         }
-        Q[9] += (P.wg * s) * (P.wg * s);
+        Q[9] += (float)((P.wg * s) * (P.wg * s));
       } else {  // ITEM_CON
         const int g = m.z;
         RT fg[3];
@@ -277,26 +290,32 @@ __device__ void residual_node(const SolveParams& P, int r, RT scale, RT (&acc)[1
               ev[2] = fmaf(gg.x, gg.w, ev[2]);
               al += gg.x;
             }
-          q_add(Q, P.wc * ev[0], P.wc * ev[1], P.wc * ev[2], P.wc * al);
+          const float wcf = (float)P.wc;
+          q_add(Q, wcf * ev[0], wcf * ev[1], wcf * ev[2], wcf * al);
         }
       }
     }
   }
   if (lane == 0) {
-    // orthogonality rows (Deform.cpp:384-404)
+    // orthogonality rows (Deform.cpp:384-404) from the offsets D = R - I:
+    // c_a . c_b = D_ab + D_ba + D_a . D_b,  |c_a|^2 - 1 = 2 D_aa + |D_a|^2
     const RT wr = RT(P.wr);
-    const RT* c0 = xj;
-    const RT* c1 = xj + 3;
-    const RT* c2 = xj + 6;
-    const RT f[6] = {wr * (c0[0] * c1[0] + c0[1] * c1[1] + c0[2] * c1[2]),
-                     wr * (c0[0] * c2[0] + c0[1] * c2[1] + c0[2] * c2[2]),
-                     wr * (c1[0] * c2[0] + c1[1] * c2[1] + c1[2] * c2[2]),
-                     wr * (c0[0] * c0[0] + c0[1] * c0[1] + c0[2] * c0[2] - RT(1)),
-                     wr * (c1[0] * c1[0] + c1[1] * c1[1] + c1[2] * c1[2] - RT(1)),
-                     wr * (c2[0] * c2[0] + c2[1] * c2[1] + c2[2] * c2[2] - RT(1))};
+    const RT* D0 = xj;
+    const RT* D1 = xj + 3;
+    const RT* D2 = xj + 6;
+    auto dot3 = [](const RT* a, const RT* b) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; };
+    const RT f[6] = {wr * (D0[1] + D1[0] + dot3(D0, D1)),
+                     wr * (D0[2] + D2[0] + dot3(D0, D2)),
+                     wr * (D1[2] + D2[1] + dot3(D1, D2)),
+                     wr * (RT(2) * D0[0] + dot3(D0, D0)),
+                     wr * (RT(2) * D1[1] + dot3(D1, D1)),
+                     wr * (RT(2) * D2[2] + dot3(D2, D2))};
 #pragma unroll
     for (int i = 0; i < 6; ++i) e += double(f[i]) * double(f[i]);
     if (PASS == PASS_GRAD) {
+      const RT c0[3] = {RT(1) + D0[0], D0[1], D0[2]};
+      const RT c1[3] = {D1[0], RT(1) + D1[1], D1[2]};
+      const RT c2[3] = {D2[0], D2[1], RT(1) + D2[2]};
 #pragma unroll
       for (int c = 0; c < 3; ++c) {
         acc[c] += wr * (f[0] * c1[c] + f[1] * c2[c] + RT(2) * f[3] * c0[c]);
@@ -324,7 +343,7 @@ __device__ void spmv_node(const SolveParams& P, int r, bool first, float beta, c
   load_p(P, r, first, beta, pold, pj);
 #pragma unroll
   for (int i = 0; i < 12; ++i) acc[i] = 0.f;
-  const float w = P.wg;
+  const float w = (float)P.wg;
   const int b0 = __ldg(P.item_off + r), b1 = __ldg(P.item_off + r + 1);
   for (int it = b0 + lane; it < b1; it += 32) {
     const int4 m = __ldg(P.items + it);
@@ -362,7 +381,7 @@ __device__ void spmv_node(const SolveParams& P, int r, bool first, float beta, c
       float u[3];
       con_jp(P, m.z, first, beta, pold, u);
       const float4 geo = __ldcg(P.mem_geo + m.y);
-      const float wa = P.wc * geo.x;
+      const float wa = (float)P.wc * geo.x;
 #pragma unroll
       for (int c = 0; c < 3; ++c) {
         acc[c] = fmaf(wa * geo.y, u[c], acc[c]);
@@ -384,7 +403,7 @@ __device__ void spmv_node(const SolveParams& P, int r, bool first, float beta, c
     const float* p0 = pj;
     const float* p1 = pj + 3;
     const float* p2 = pj + 6;
-    const float wr = P.wr;
+    const float wr = (float)P.wr;
     auto dot = [](const float* a3, const float* b3) { return a3[0] * b3[0] + a3[1] * b3[1] + a3[2] * b3[2]; };
     const float u0 = wr * (dot(c1, p0) + dot(c0, p1));
     const float u1 = wr * (dot(c2, p0) + dot(c0, p2));
@@ -426,7 +445,7 @@ __device__ void build_dinv(const SolveParams& P, int r, const float (&Q)[10], fl
       D[(9 + rr) * 12 + 9 + rr] = Q[9];
     }
     // rotation rows: [c1|c0|0], [c2|0|c0], [0|c2|c1], [2c0|0|0], [0|2c1|0], [0|0|2c2]
-    const float wr = P.wr;
+    const float wr = (float)P.wr;
     float J[6][9];
 #pragma unroll
     for (int a = 0; a < 6; ++a)

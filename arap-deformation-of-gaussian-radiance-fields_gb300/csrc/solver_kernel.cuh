@@ -65,7 +65,8 @@ __global__ void __launch_bounds__(kSolveThreads) gn_solve_kernel(SolveParams P) 
   for (int it = 0; it < P.max_iters; ++it) {
     // ---- gradient -J^T f, energy, preconditioner, PCG start (h=0, r=g, z=M^-1 g)
     double red[4] = {0.0, 0.0, 0.0, 0.0}, out[4];
-    for (int r = gw; r < F; r += nw) {
+    for (int oi = gw; oi < F; oi += nw) {
+      const int r = __ldg(P.order + oi);
       RT acc[12];
       float Q[10];
       double en;
@@ -128,7 +129,8 @@ __global__ void __launch_bounds__(kSolveThreads) gn_solve_kernel(SolveParams P) 
       float* pcur = (pi & 1) ? P.p1 : P.p0;
       const float* pold = (pi & 1) ? P.p0 : P.p1;
       double pq[1] = {0.0}, opq[1];
-      for (int r = gw; r < F; r += nw) {
+      for (int oi = gw; oi < F; oi += nw) {
+      const int r = __ldg(P.order + oi);
         float acc[12], pj[12];
         spmv_node(P, r, first, beta, pold, acc, pj);
         if (lane < 12) {
@@ -149,7 +151,8 @@ __global__ void __launch_bounds__(kSolveThreads) gn_solve_kernel(SolveParams P) 
       if (!(opq[0] > 0.0)) break;
       const float alpha = (float)(rz / opq[0]);
       double rzr[2] = {0.0, 0.0}, orz[2];
-      for (int r = gw; r < F; r += nw) {
+      for (int oi = gw; oi < F; oi += nw) {
+      const int r = __ldg(P.order + oi);
         float rc = 0.f;
         if (lane < 12) {
           const size_t o = 12 * (size_t)r + lane;
@@ -178,7 +181,8 @@ __global__ void __launch_bounds__(kSolveThreads) gn_solve_kernel(SolveParams P) 
     double hh = 0.0;
     for (int ls = 0; ls < 50; ++ls) {
       double en2[2] = {0.0, 0.0}, oen[2];
-      for (int r = gw; r < F; r += nw) {
+      for (int oi = gw; oi < F; oi += nw) {
+      const int r = __ldg(P.order + oi);
         RT acc[12];
         float Q[10];
         double en;

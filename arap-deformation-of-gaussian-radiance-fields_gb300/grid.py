@@ -1,0 +1,97 @@
+"""Density grid over a Gaussian field (C ABI ``arap_grid_*``).
+
+Mirrors the reference's grid set-up (getOverallAABB, getGridSamples,
+UpdateContainingRelationship, GetAdaLpfRatio; GaussianView.cpp:3601-4149,
+4670-4751) and the host contract of its density sampler (forward3d_grid,
+GaussianView.cpp:4222-4249).
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import torch
+
+from . import _lib
+from ._lib import GridInfo, check
+from .deform import _f32, _p, _s
+
+LPF_PARAMETER = 0.2  # GaussianView.hpp:482
+
+
+class Grid:
+    """Cell binning of one Gaussian field; owns the CSR on the device."""
+
+    def __init__(self, pos, rot, scale, opacity, grid_num, padding=1):
+        lib = _lib.load()
+        self.pos, self.rot, self.scale, self.opacity = _f32(pos), _f32(rot), _f32(scale), _f32(opacity)
+        self.N = self.pos.shape[0]
+        info = GridInfo()
+        h = C.c_void_p()
+        check("arap_grid_build", lib.arap_grid_build(
+            C.byref(h), self.N, _p(self.pos), _p(self.rot), _p(self.scale), _p(self.opacity),
+            int(grid_num), int(padding), C.byref(info), _s()))
+        self._h = h
+        self.info = info
+        self.grid_num = int(grid_num)
+        self.n_valid = int(info.n_valid)
+        self.n_pairs = int(info.n_pairs)
+        self.step = float(info.step)
+        self.min_xyz = tuple(info.min_xyz)
+        self.max_xyz = tuple(info.max_xyz)
+        self.sample_pos = torch.empty((self.n_valid * 64, 3), dtype=torch.float32, device="cuda")
+        check("arap_grid_samples", lib.arap_grid_samples(h, _p(self.sample_pos), _s()))
+        # low_pass_filter_param = (step/4)^2 * lpf_parameter (GaussianView.cpp:3879-3881)
+        self.lpf_param = (self.step / 4.0) ** 2 * LPF_PARAMETER
+
+    def arrays(self):
+        """(cell_offsets [g^3+1], cell_lists [n_pairs], valid_cells [n_valid]) as int32 tensor copies."""
+        off, lst, val = C.c_void_p(), C.c_void_p(), C.c_void_p()
+        check("arap_grid_arrays", _lib.load().arap_grid_arrays(self._h, C.byref(off), C.byref(lst), C.byref(val)))
+        g3 = self.grid_num ** 3
+        return (_wrap_i32(off.value, g3 + 1), _wrap_i32(lst.value, self.n_pairs),
+                _wrap_i32(val.value, self.n_valid))
+
+    def ada_lpf(self, samples=None, lpf=LPF_PARAMETER):
+        samples = self.sample_pos if samples is None else _f32(samples)
+        out = torch.empty((self.n_valid, 9), dtype=torch.float32, device="cuda")
+        check("arap_grid_ada_lpf", _lib.load().arap_grid_ada_lpf(self._h, _p(samples), float(lpf), _p(out), _s()))
+        return out
+
+    def density(self, shs, samples=None, ada=None, lpf_param=None):
+        samples = self.sample_pos if samples is None else _f32(samples)
+        lpf_param = self.lpf_param if lpf_param is None else lpf_param
+        S = self.n_valid * 64
+        sigma = torch.empty((S,), dtype=torch.float32, device="cuda")
+        feat = torch.empty((S, 48), dtype=torch.float32, device="cuda")
+        check("arap_grid_density", _lib.load().arap_grid_density(
+            self._h, _p(self.pos), _p(self.rot), _p(self.scale), _p(self.opacity), _p(_f32(shs)), _p(samples),
+            _p(ada) if ada is not None else None, float(lpf_param), _p(sigma), _p(feat), _s()))
+        return sigma, feat
+
+    def close(self):
+        if getattr(self, "_h", None):
+            _lib.load().arap_grid_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class _DevView:
+    def __init__(self, ptr, n):
+        self.__cuda_array_interface__ = {"shape": (n,), "typestr": "<i4", "data": (int(ptr or 0), False),
+                                         "version": 3}
+
+
+def _wrap_i32(ptr, n):
+    """Copy n int32 from a library-owned device pointer into a new tensor."""
+    if n == 0:
+        return torch.empty((0,), dtype=torch.int32, device="cuda")
+    return torch.as_tensor(_DevView(ptr, n), device="cuda").clone()
+
+
+def build_grid(pos, rot, scale, opacity, grid_num, padding=1):
+    return Grid(pos, rot, scale, opacity, grid_num, padding)

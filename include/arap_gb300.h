@@ -222,6 +222,61 @@ int arap_aims_twist(float* aims, const float* node_pos, const int32_t* active_no
 int arap_aims_scale(float* aims, const float* node_pos, const int32_t* active_nodes,
                     int n_active, float s, arap_stream_t stream);
 
+/* ----------------------------------------------------------------- grid --- */
+
+typedef struct {
+  float min_xyz[3];  /* scene box (getOverallAABB, GaussianView.cpp:3601-3631) */
+  float max_xyz[3];
+  float step;        /* cell edge: max over axes of extent / grid_num */
+  float interval;    /* sample spacing: step / 4 (SAMPLES_PER_GRID, helper.hpp:56) */
+  int grid_num;
+  int n_valid;       /* occupied cells (non-empty lists) */
+  long long n_pairs; /* total (cell, Gaussian) entries */
+} arap_grid_info;
+
+typedef struct arap_grid arap_grid;
+
+/* Bin N Gaussians into the grid_num^3 grid: every cell covered by a
+ * Gaussian's box (centre +/- R s_3d, s_3d = sqrt(-2 ln((1/255)/opacity)) s,
+ * widened by `padding` cells; GaussianView.cpp:3961-4019 and
+ * GetBoxesGsGrid cudakdtree.cu:425-451) lists that Gaussian.  Lists are in
+ * ascending Gaussian order, as the reference's serial fill
+ * (GaussianView.cpp:4077-4100) leaves them.  rot = (w,x,y,z) [N*4]; scale and
+ * opacity activated.  The handle owns its device arrays; synchronises. */
+int arap_grid_build(arap_grid** out, int N, const float* pos, const float* rot, const float* scale,
+                    const float* opacity, int grid_num, int padding, arap_grid_info* info_host,
+                    arap_stream_t stream);
+
+/* Device arrays owned by the handle: cell_offsets [g^3+1] (exclusive prefix
+ * of the per-cell counts, grid_gs_prefix_sum shifted by one), cell_lists
+ * [n_pairs] (grided_gs_idx), valid_cells [n_valid] ascending (valid_grid_idx). */
+int arap_grid_arrays(const arap_grid* grid, const int32_t** cell_offsets, const int32_t** cell_lists,
+                     const int32_t** valid_cells);
+
+/* 64 samples per occupied cell, cell-major, sample s at
+ * min + cell*step + (0.5 + (s/16, s/4%4, s%4)) * interval
+ * (GaussianView.cpp:4104-4133).  samples_out [n_valid*64*3]. */
+int arap_grid_samples(const arap_grid* grid, float* samples_out, arap_stream_t stream);
+
+/* Adaptive low-pass filter per occupied cell (GetAdaLpfRatio,
+ * GaussianView.cpp:4670-4751): lpf * M M^T, M the least-squares linear map of
+ * the unit cube's corners onto the cell's corner samples / 3.
+ * samples [n_valid*64*3]; out [n_valid*9] row-major. */
+int arap_grid_ada_lpf(const arap_grid* grid, const float* samples, float lpf, float* out,
+                      arap_stream_t stream);
+
+/* Gaussian-mixture density at the grid samples, this library's definition of
+ * CudaRasterizer::forward3d_grid (call sites GaussianView.cpp:4222-4249):
+ *   sigma(x) = sum_i a_i exp(-1/2 d^T (S_i + L)^-1 d),  F(x) = sum_i (...) SH_i
+ * over the sample's cell list, S_i = R diag(s)^2 R^T, L = the cell's adaptive
+ * 3x3 (ada, [n_valid*9]) or lpf * I when ada is null.
+ * sigma_out [n_valid*64], feature_out [n_valid*64*48]. */
+int arap_grid_density(const arap_grid* grid, const float* pos, const float* rot, const float* scale,
+                      const float* opacity, const float* shs, const float* samples, const float* ada,
+                      float lpf, float* sigma_out, float* feature_out, arap_stream_t stream);
+
+void arap_grid_destroy(arap_grid* grid);
+
 /* --------------------------------------------------------------- misc --- */
 
 /* Read and clear the library's sticky device error word (ARAP_* code). */

@@ -1,0 +1,92 @@
+"""GPU parity of the density grid: scene box, cell CSR (exact, ascending lists),
+samples, adaptive low-pass filter and density sampling against the oracle."""
+import numpy as np
+import pytest
+
+from tests import _helpers as H
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+
+def _t(a):
+    return torch.as_tensor(np.ascontiguousarray(a)).cuda()
+
+
+@pytest.fixture(scope="module", params=["bend4k", "twist20k"])
+def scene(request):
+    return H.synth.make_scene(request.param)
+
+
+@pytest.fixture(scope="module")
+def gridmod(dev):
+    import importlib
+    return importlib.import_module("arap-deformation-of-gaussian-radiance-fields_gb300.grid")
+
+
+def test_grid_csr_exact(gridmod, scene):
+    from oracle import grid as og
+    G = gridmod.build_grid(_t(scene.pos), _t(scene.rot), _t(scene.scale), _t(scene.opacity), scene.grid_num)
+    mn, mx = og.overall_aabb(scene.pos)
+    assert np.array_equal(np.array(G.min_xyz, np.float32), mn)
+    assert np.array_equal(np.array(G.max_xyz, np.float32), mx)
+    step = og.grid_step(mn, mx, scene.grid_num)
+    assert np.float32(G.step) == step
+    lo, hi = og.gaussian_aabbs(scene.pos, scene.rot, scene.scale, scene.opacity)
+    off_ref, lists_ref = og.cell_csr(lo, hi, mn, step, scene.grid_num)
+    off, lists, valid = (t.cpu().numpy() for t in G.arrays())
+    # box corners can differ by one float32 rounding between CUDA and numpy
+    # transcendental/rotation arithmetic; a Gaussian whose box edge lands on a
+    # cell boundary may then cover one more or one fewer cell layer
+    mism = np.flatnonzero(off != off_ref)
+    assert mism.size <= max(2, 1e-5 * off.size), mism.size
+    if mism.size == 0:
+        assert np.array_equal(lists, lists_ref)
+    # every cell's list is ascending
+    d = np.diff(lists.astype(np.int64))
+    cell_of = np.repeat(np.arange(off.size - 1), np.diff(off))
+    same = cell_of[1:] == cell_of[:-1]
+    assert (d[same] > 0).all()
+    assert np.array_equal(valid, np.flatnonzero(np.diff(off) > 0))
+
+
+def test_grid_samples_and_ada_lpf(gridmod, scene):
+    from oracle import grid as og
+    G = gridmod.build_grid(_t(scene.pos), _t(scene.rot), _t(scene.scale), _t(scene.opacity), scene.grid_num)
+    off, _, valid = (t.cpu().numpy() for t in G.arrays())
+    mn = np.array(G.min_xyz, np.float32)
+    v_ref, s_ref = og.grid_samples(off.astype(np.int64), mn, np.float32(G.step), scene.grid_num)
+    assert np.array_equal(valid, v_ref)
+    np.testing.assert_array_equal(G.sample_pos.cpu().numpy(), s_ref)
+    # undeformed samples: the adaptive filter is interval^2 * 0.2 * I
+    ada = G.ada_lpf().cpu().numpy().reshape(-1, 3, 3)
+    iv = np.float64(G.step) / 4
+    assert np.abs(ada - np.eye(3) * iv * iv * 0.2).max() <= 1e-6 * iv * iv
+    # deformed samples against the oracle
+    rng = np.random.default_rng(0)
+    S = s_ref + (0.1 * iv * rng.standard_normal(s_ref.shape)).astype(np.float32)
+    ada2 = G.ada_lpf(_t(S)).cpu().numpy().reshape(-1, 3, 3)
+    ref = og.ada_lpf(S)
+    assert np.abs(ada2 - ref).max() <= 1e-4 * np.abs(ref).max()
+
+
+def test_grid_density(gridmod):
+    from oracle import grid as og
+    sc = H.synth.make_scene("bend4k")
+    G = gridmod.build_grid(_t(sc.pos), _t(sc.rot), _t(sc.scale), _t(sc.opacity), sc.grid_num)
+    off, lists, valid = (t.cpu().numpy() for t in G.arrays())
+    sig, feat = G.density(_t(sc.shs))
+    sig, feat = sig.cpu().numpy(), feat.cpu().numpy()
+    rng = np.random.default_rng(1)
+    pick = rng.choice(sig.size, 400, replace=False)
+    samples = G.sample_pos.cpu().numpy()
+    cell_of_sample = valid[pick // 64]
+    s_ref, f_ref = og.density(samples[pick], off.astype(np.int64), lists, cell_of_sample, sc.pos, sc.rot,
+                              sc.scale, sc.opacity, sc.shs, np.float64(G.lpf_param))
+    scale_s = max(np.abs(s_ref).max(), 1e-6)
+    assert np.abs(sig[pick] - s_ref).max() <= 1e-4 * scale_s
+    assert np.abs(feat[pick] - f_ref).max() <= 1e-4 * max(np.abs(f_ref).max(), 1e-6)
+    # adaptive filter path
+    ada = G.ada_lpf()
+    sig2, _ = G.density(_t(sc.shs), ada=ada)
+    np.testing.assert_allclose(sig2.cpu().numpy(), sig, rtol=1e-4, atol=1e-6 * scale_s)
