@@ -28,7 +28,7 @@ class SolveConfig(C.Structure):
     _fields_ = [("w_rot", C.c_float), ("w_reg", C.c_float), ("w_con", C.c_float),
                 ("weighting_factor", C.c_float), ("cons_on_center", C.c_int),
                 ("max_iters", C.c_int), ("early_exit", C.c_int), ("precision", C.c_int),
-                ("pcg_tol", C.c_float), ("pcg_max_iters", C.c_int)]
+                ("pcg_tol", C.c_float), ("pcg_max_iters", C.c_int), ("coarse_nodes", C.c_int)]
 
 
 class GridInfo(C.Structure):

@@ -33,4 +33,5 @@ extern "C" void arap_solve_config_default(arap_solve_config* cfg) {
   cfg->precision = ARAP_PRECISION_PLAIN;
   cfg->pcg_tol = 0.0f;
   cfg->pcg_max_iters = 0;
+  cfg->coarse_nodes = 0;
 }

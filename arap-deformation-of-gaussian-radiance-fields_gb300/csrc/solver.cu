@@ -198,6 +198,77 @@ extern "C" int arap_solver_create(arap_solver** out, int n, int k, const int32_t
     item_off[r + 1] = (int32_t)item_flat.size();
   }
 
+  // aggregates of the coarse space: breadth-first growth over the node graph
+  // (both edge directions, free nodes only) up to coarse_nodes members; small
+  // leftovers join their neighbouring aggregate
+  std::vector<int32_t> agg(F, -1), pivot, agg_count;
+  if (cfg.coarse_nodes > 0 && F > cfg.coarse_nodes) {
+    std::vector<std::vector<int32_t>> adj(F);
+    for (int i = 0; i < n; ++i) {
+      if (rank[i] < 0) continue;
+      for (int t = 0; t < k; ++t) {
+        const int j = nb[(size_t)i * k + t];
+        if (rank[j] < 0) continue;
+        adj[rank[i]].push_back(rank[j]);
+        adj[rank[j]].push_back(rank[i]);
+      }
+    }
+    const int target = cfg.coarse_nodes;
+    std::vector<int32_t> queue;
+    for (int seed = 0; seed < F; ++seed) {
+      if (agg[seed] >= 0) continue;
+      const int a = (int)pivot.size();
+      pivot.push_back(free_ids[seed]);
+      agg_count.push_back(0);
+      queue.assign(1, seed);
+      agg[seed] = a;
+      agg_count[a] = 1;
+      for (size_t q = 0; q < queue.size() && agg_count[a] < target; ++q)
+        for (int v : adj[queue[q]]) {
+          if (agg[v] >= 0) continue;
+          agg[v] = a;
+          queue.push_back(v);
+          if (++agg_count[a] >= target) break;
+        }
+    }
+    // merge aggregates below a quarter of the target into a neighbour
+    const int NA0 = (int)pivot.size();
+    std::vector<int32_t> remap(NA0);
+    for (int a = 0; a < NA0; ++a) remap[a] = a;
+    for (int r = 0; r < F; ++r) {
+      const int a = agg[r];
+      if (agg_count[a] >= target / 4 || remap[a] != a) continue;
+      for (int v : adj[r]) {
+        const int b = remap[agg[v]];
+        if (b != a && agg_count[b] >= target / 4) {
+          remap[a] = b;
+          agg_count[b] += agg_count[a];
+          agg_count[a] = 0;
+          break;
+        }
+      }
+    }
+    std::vector<int32_t> newid(NA0, -1), piv2, cnt2;
+    for (int a = 0; a < NA0; ++a) {
+      int b = a;
+      while (remap[b] != b) b = remap[b];
+      if (newid[b] < 0) {
+        newid[b] = (int32_t)piv2.size();
+        piv2.push_back(pivot[b]);
+        cnt2.push_back(0);
+      }
+      newid[a] = newid[b];
+    }
+    for (int r = 0; r < F; ++r) {
+      agg[r] = newid[agg[r]];
+      cnt2[agg[r]] += 1;
+    }
+    pivot.swap(piv2);
+    agg_count.swap(cnt2);
+  }
+  const int NA = (int)pivot.size();
+  const int NC = 12 * NA;
+
   auto* s = new (std::nothrow) arap_solver();
   if (!s) return ARAP_ENOMEM;
   s->n = n;
@@ -246,6 +317,17 @@ extern "C" int arap_solver_create(arap_solver** out, int n, int k, const int32_t
     P.g = cv.take<float>((size_t)F * 12);
     P.dinv = cv.take<float>((size_t)F * 144);
     P.order = cv.take<int32_t>(F);
+    P.agg = cv.take<int32_t>(F);
+    P.pivot = cv.take<int32_t>(NA);
+    P.agg_count = cv.take<int32_t>(NA);
+    P.Qd = cv.take<double>((size_t)NA * NA * 16);
+    P.Cw = cv.take<float>((size_t)2 * NC * NC);
+    P.Wgj = cv.take<float>((size_t)NC * kGJBlock);
+    P.Pgj = cv.take<float>((size_t)kGJBlock * kGJBlock);
+    P.rotagg = cv.take<double>((size_t)2 * NA * 81);
+    P.Cinv = cv.take<float>((size_t)NC * NC);
+    P.rc = cv.take<double>((size_t)2 * NC);
+    P.zc = cv.take<float>(NC);
     P.partials = cv.take<double>((size_t)8 * grid);
     P.results = cv.take<double>(8);
     P.stats = cv.take<double>(8);
@@ -298,6 +380,11 @@ extern "C" int arap_solver_create(arap_solver** out, int n, int k, const int32_t
     }
   }
   e = e ? e : up(P.order, order.data(), order.size() * 4);
+  if (NA > 0) {
+    e = e ? e : up(P.agg, agg.data(), agg.size() * 4);
+    e = e ? e : up(P.pivot, pivot.data(), pivot.size() * 4);
+    e = e ? e : up(P.agg_count, agg_count.data(), agg_count.size() * 4);
+  }
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   if (e != cudaSuccess) {
     cudaFree(s->block);
@@ -319,6 +406,8 @@ extern "C" int arap_solver_create(arap_solver** out, int n, int k, const int32_t
   P.pcg_tol = s->cfg.pcg_tol;
   P.mode = 0;
   P.refine = 0;
+  P.NA = NA;
+  P.NC = NC;
   *out = s;
   return ARAP_OK;
 }

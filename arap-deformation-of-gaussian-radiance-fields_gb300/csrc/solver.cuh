@@ -5,6 +5,8 @@
 
 namespace arap {
 
+constexpr int kGJBlock = 48;  // pivot block of the coarse Gauss-Jordan inversion
+
 // Coupling items of one free node j (all rows of J that touch x_j besides its
 // own rotation rows).  int4 {kind, a, b, c}:
 //   ITEM_OUT    regularisation rows (j -> k), k = Neighbor[t] of j
@@ -60,6 +62,20 @@ struct SolveParams {
   float pcg_tol;
   int mode;                  // 0 solve, 1 gradient/energy only
   int refine;                // mixed precision: FP64 refinement sweeps per solve
+  // two-level preconditioner (coarse space: one affine ED transform per
+  // aggregate; node j of aggregate a gets dR_j = dR_a, dt_j = dR_a (g_j - g_pa) + dT_a)
+  int NA, NC;                // aggregates, coarse unknowns (12 NA); NA = 0 disables it
+  const int32_t* agg;        // [F] aggregate of each free node
+  const int32_t* pivot;      // [NA] node id of each aggregate's reference node
+  const int32_t* agg_count;  // [NA] free nodes per aggregate
+  double* Qd;                // [NA*NA*16] 4x4 kernels of the coarse blocks
+  float* Cw;                 // [2*NC*NC] coarse matrix / Gauss-Jordan ping-pong
+  float* Cinv;               // [NC*NC] inverse of the coarse matrix
+  float* Wgj;                // [NC*kGJBlock] Gauss-Jordan row multipliers
+  float* Pgj;                // [kGJBlock^2] inverse of the current pivot block
+  double* rotagg;            // [2*NA*81] per-aggregate sums of J_rot^T J_rot (GN-iteration parity)
+  double* rc;                // [2*NC] restricted residual, double-buffered
+  float* zc;                 // [NC] coarse correction
 };
 
 }  // namespace arap

@@ -27,11 +27,29 @@ __device__ __forceinline__ void ld3t_cg(const float* base, int r, float (&v)[3])
   v[0] = c.y; v[1] = c.z; v[2] = c.w;
 }
 
-// Search direction of free node rr for this PCG iteration, formed on the fly:
-// p = z + beta * p_old (p = z on the first iteration).
-__device__ __forceinline__ void load_p(const SolveParams& P, int rr, bool first, float beta,
+// Coarse correction of free node rr (node id `node`): z += P_j zc[a] with
+// dR_j = dR_a, dt_j = dR_a (g_j - g_pivot(a)) + dT_a.
+__device__ __forceinline__ void coarse_prolong(const SolveParams& P, int rr, int node, float (&v)[12]) {
+  const int a = __ldg(P.agg + rr);
+  const int pv = __ldg(P.pivot + a);
+  const float d0 = __ldg(P.node_pos + 3 * (size_t)node) - __ldg(P.node_pos + 3 * (size_t)pv);
+  const float d1 = __ldg(P.node_pos + 3 * (size_t)node + 1) - __ldg(P.node_pos + 3 * (size_t)pv + 1);
+  const float d2 = __ldg(P.node_pos + 3 * (size_t)node + 2) - __ldg(P.node_pos + 3 * (size_t)pv + 2);
+  float c[12];
+  ld12cg(P.zc, a, c);
+#pragma unroll
+  for (int i = 0; i < 9; ++i) v[i] += c[i];
+#pragma unroll
+  for (int r = 0; r < 3; ++r) v[9 + r] += c[9 + r] + d0 * c[r] + d1 * c[3 + r] + d2 * c[6 + r];
+}
+
+// Search direction of free node rr (node id `node`) for this PCG iteration,
+// formed on the fly: p = z + beta * p_old (p = z on the first iteration),
+// z = Dinv r (+ the coarse correction when the two-level preconditioner is on).
+__device__ __forceinline__ void load_p(const SolveParams& P, int rr, int node, bool first, float beta,
                                        const float* pold, float (&v)[12]) {
   ld12cg(P.z, rr, v);
+  if (P.NA) coarse_prolong(P, rr, node, v);
   if (!first) {
     float o[12];
     ld12cg(pold, rr, o);
@@ -40,8 +58,16 @@ __device__ __forceinline__ void load_p(const SolveParams& P, int rr, bool first,
   }
 }
 
-__device__ __forceinline__ void load_pt(const SolveParams& P, int rr, bool first, float beta,
+__device__ __forceinline__ void load_pt(const SolveParams& P, int rr, int node, bool first, float beta,
                                         const float* pold, float (&v)[3]) {
+  if (P.NA) {
+    float f[12];
+    load_p(P, rr, node, first, beta, pold, f);
+    v[0] = f[9];
+    v[1] = f[10];
+    v[2] = f[11];
+    return;
+  }
   ld3t_cg(P.z, rr, v);
   if (!first) {
     float o[3];
@@ -147,7 +173,7 @@ __device__ void con_jp(const SolveParams& P, int g, bool first, float beta, cons
       if (rk < 0) continue;
       const float4 geo = __ldcg(P.mem_geo + slot);
       float pl[12];
-      load_p(P, rk, first, beta, pold, pl);
+      load_p(P, rk, __ldg(P.mem_node + slot), first, beta, pold, pl);
 #pragma unroll
       for (int c = 0; c < 3; ++c)
         u[c] = fmaf(geo.x, fmaf(geo.y, pl[c], fmaf(geo.z, pl[3 + c], fmaf(geo.w, pl[6 + c], pl[9 + c]))), u[c]);
@@ -340,7 +366,7 @@ __device__ void spmv_node(const SolveParams& P, int r, bool first, float beta, c
   const int j = __ldg(P.free_ids + r);
   const float gj[3] = {__ldg(P.node_pos + 3 * (size_t)j), __ldg(P.node_pos + 3 * (size_t)j + 1),
                        __ldg(P.node_pos + 3 * (size_t)j + 2)};
-  load_p(P, r, first, beta, pold, pj);
+  load_p(P, r, j, first, beta, pold, pj);
 #pragma unroll
   for (int i = 0; i < 12; ++i) acc[i] = 0.f;
   const float w = (float)P.wg;
@@ -353,7 +379,7 @@ __device__ void spmv_node(const SolveParams& P, int r, bool first, float beta, c
                           __ldg(P.node_pos + 3 * (size_t)m.z + 1) - gj[1],
                           __ldg(P.node_pos + 3 * (size_t)m.z + 2) - gj[2]};
       float pk[3] = {0.f, 0.f, 0.f};
-      if (m.y >= 0) load_pt(P, m.y, first, beta, pold, pk);
+      if (m.y >= 0) load_pt(P, m.y, m.z, first, beta, pold, pk);
 #pragma unroll
       for (int c = 0; c < 3; ++c) {
         const float u = ws * fmaf(pj[c], d[0], fmaf(pj[3 + c], d[1], pj[6 + c] * d[2])) + w * pj[9 + c] - ws * pk[c];
@@ -368,7 +394,7 @@ __device__ void spmv_node(const SolveParams& P, int r, bool first, float beta, c
                           gj[1] - __ldg(P.node_pos + 3 * (size_t)m.z + 1),
                           gj[2] - __ldg(P.node_pos + 3 * (size_t)m.z + 2)};
       float pi[12];
-      load_p(P, m.y, first, beta, pold, pi);
+      load_p(P, m.y, m.z, first, beta, pold, pi);
 #pragma unroll
       for (int c = 0; c < 3; ++c) {
         const float u = ws * fmaf(pi[c], d[0], fmaf(pi[3 + c], d[1], pi[6 + c] * d[2])) + w * pi[9 + c] - ws * pj[9 + c];
@@ -539,6 +565,192 @@ __device__ __forceinline__ float apply_dinv(const SolveParams& P, int rr, float 
     zc = fmaf(__ldcg(row + i), ri, zc);
   }
   return lane < 12 ? zc : 0.f;
+}
+
+
+// ------------------------------------------------------ coarse level ----
+// 4x4 kernel index: unknowns (R[r][0], R[r][1], R[r][2], t[r]) of one row r;
+// coarse unknown u of an aggregate is R col-major (3c + r) for u < 9, t[u-9].
+__device__ __forceinline__ void coarse_add(const SolveParams& P, int a, int b, const float (&va)[4],
+                                           const float (&vb)[4]) {
+  double* q = P.Qd + ((size_t)a * P.NA + b) * 16;
+#pragma unroll
+  for (int x = 0; x < 4; ++x)
+#pragma unroll
+    for (int y = 0; y < 4; ++y) atomicAdd(q + 4 * x + y, (double)va[x] * (double)vb[y]);
+}
+
+// Coefficients of one regularisation / static / constraint row (all three r
+// share them) on the coarse unknowns of aggregate a: a J-row with R-part w_R
+// (per column c) and t-part w_t on node j maps to (w_R + w_t d_j, w_t).
+__device__ __forceinline__ void coarse_vec(const SolveParams& P, int rr, int node, float wr0, float wr1,
+                                           float wr2, float wt, float (&v)[4]) {
+  const int a = __ldg(P.agg + rr);
+  const int pv = __ldg(P.pivot + a);
+  v[0] = wr0 + wt * (__ldg(P.node_pos + 3 * (size_t)node) - __ldg(P.node_pos + 3 * (size_t)pv));
+  v[1] = wr1 + wt * (__ldg(P.node_pos + 3 * (size_t)node + 1) - __ldg(P.node_pos + 3 * (size_t)pv + 1));
+  v[2] = wr2 + wt * (__ldg(P.node_pos + 3 * (size_t)node + 2) - __ldg(P.node_pos + 3 * (size_t)pv + 2));
+  v[3] = wt;
+}
+
+// Coarse matrix kernels of the rows owned by free node r (its outgoing
+// regularisation rows and the static rows pointing at it).
+__device__ void coarse_rows_node(const SolveParams& P, int r) {
+  const int lane = threadIdx.x & 31;
+  const int j = __ldg(P.free_ids + r);
+  const int a = __ldg(P.agg + r);
+  const float w = (float)P.wg;
+  const float gj[3] = {__ldg(P.node_pos + 3 * (size_t)j), __ldg(P.node_pos + 3 * (size_t)j + 1),
+                       __ldg(P.node_pos + 3 * (size_t)j + 2)};
+  const int b0 = __ldg(P.item_off + r), b1 = __ldg(P.item_off + r + 1);
+  for (int it = b0 + lane; it < b1; it += 32) {
+    const int4 m = __ldg(P.items + it);
+    if (m.x == ITEM_OUT) {
+      const float ws = w * __int_as_float(m.w);
+      const float d[3] = {__ldg(P.node_pos + 3 * (size_t)m.z) - gj[0], __ldg(P.node_pos + 3 * (size_t)m.z + 1) - gj[1],
+                          __ldg(P.node_pos + 3 * (size_t)m.z + 2) - gj[2]};
+      float va[4], vb[4];
+      coarse_vec(P, r, j, ws * d[0], ws * d[1], ws * d[2], w, va);
+      if (m.y >= 0) {
+        coarse_vec(P, m.y, m.z, 0.f, 0.f, 0.f, -ws, vb);
+        const int b = __ldg(P.agg + m.y);
+        if (b == a) {
+          float v[4] = {va[0] + vb[0], va[1] + vb[1], va[2] + vb[2], va[3] + vb[3]};
+          coarse_add(P, a, a, v, v);
+        } else {
+          coarse_add(P, a, a, va, va);
+          coarse_add(P, a, b, va, vb);
+          coarse_add(P, b, a, vb, va);
+          coarse_add(P, b, b, vb, vb);
+        }
+      } else {
+        coarse_add(P, a, a, va, va);
+      }
+    } else if (m.x == ITEM_STATIC) {
+      float v[4];
+      coarse_vec(P, r, j, 0.f, 0.f, 0.f, -w, v);
+      coarse_add(P, a, a, v, v);
+    }
+  }
+}
+
+// Coarse kernels of constraint group g (one thread): J_g restricted to the
+// aggregates its free anchors belong to, then every pair.
+__device__ void coarse_rows_group(const SolveParams& P, int g) {
+  constexpr int kMaxAgg = 24;
+  int ids[kMaxAgg];
+  float vv[kMaxAgg][4];
+  int na = 0;
+  const float wc = (float)P.wc;
+  const int s0 = __ldg(P.grp_off + g), s1 = __ldg(P.grp_off + g + 1);
+  for (int s = s0; s < s1; ++s) {
+    const int c = __ldg(P.grp_member + s);
+    for (int t = 0; t < P.k; ++t) {
+      const int slot = s * P.k + t;
+      const int rk = __ldg(P.mem_rank + slot);
+      if (rk < 0) continue;
+      const int b = __ldg(P.agg + rk);
+      const int pv = __ldg(P.pivot + b);
+      const float a = wc * __ldg(P.mem_w + slot);
+      // R-part a (v_c - g_l) plus t-part a (g_l - g_pivot) = a (v_c - g_pivot)
+      float v[4];
+#pragma unroll
+      for (int q = 0; q < 3; ++q) {
+        const float dv = __ldg(P.node_pos + 3 * (size_t)c + q) - __ldg(P.node_pos + 3 * (size_t)__ldg(P.mem_node + slot) + q);
+        const float dl = __ldg(P.node_pos + 3 * (size_t)__ldg(P.mem_node + slot) + q) - __ldg(P.node_pos + 3 * (size_t)pv + q);
+        v[q] = a * (dv + dl);
+      }
+      v[3] = a;
+      int f = -1;
+      for (int q = 0; q < na; ++q)
+        if (ids[q] == b) f = q;
+      if (f < 0) {
+        if (na == kMaxAgg) {
+          raise_status(ARAP_EUNSUPPORTED);
+          continue;
+        }
+        f = na++;
+        ids[f] = b;
+        vv[f][0] = vv[f][1] = vv[f][2] = vv[f][3] = 0.f;
+      }
+#pragma unroll
+      for (int q = 0; q < 4; ++q) vv[f][q] += v[q];
+    }
+  }
+  for (int x = 0; x < na; ++x)
+    for (int y = 0; y < na; ++y) {
+      float vx[4] = {vv[x][0], vv[x][1], vv[x][2], vv[x][3]};
+      float vy[4] = {vv[y][0], vv[y][1], vv[y][2], vv[y][3]};
+      coarse_add(P, ids[x], ids[y], vx, vy);
+    }
+}
+
+// J_rot^T J_rot (9x9) of free node rr at the current x (float copy), added to
+// its aggregate's sum (all lanes of the warp call it).
+__device__ __forceinline__ void coarse_rot_node(const SolveParams& P, int rr, double* rotagg) {
+  const int lane = threadIdx.x & 31;
+  float X[9];
+#pragma unroll
+  for (int i = 0; i < 9; ++i) X[i] = __ldcg(P.xf + 12 * (size_t)rr + i);
+  const float wr = (float)P.wr;
+  float J[6][9];
+#pragma unroll
+  for (int a = 0; a < 6; ++a)
+#pragma unroll
+    for (int b = 0; b < 9; ++b) J[a][b] = 0.f;
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    J[0][c] = wr * X[3 + c]; J[0][3 + c] = wr * X[c];
+    J[1][c] = wr * X[6 + c]; J[1][6 + c] = wr * X[c];
+    J[2][3 + c] = wr * X[6 + c]; J[2][6 + c] = wr * X[3 + c];
+    J[3][c] = 2.f * wr * X[c];
+    J[4][3 + c] = 2.f * wr * X[3 + c];
+    J[5][6 + c] = 2.f * wr * X[6 + c];
+  }
+  double* dst = rotagg + 81 * (size_t)__ldg(P.agg + rr);
+  for (int e = lane; e < 81; e += 32) {
+    const int a = e / 9, b = e % 9;
+    float v = 0.f;
+#pragma unroll
+    for (int t = 0; t < 6; ++t) {
+      // select J[t][a] * J[t][b] without dynamic register indexing
+      float ja = 0.f, jb = 0.f;
+#pragma unroll
+      for (int q = 0; q < 9; ++q) {
+        ja = (q == a) ? J[t][q] : ja;
+        jb = (q == b) ? J[t][q] : jb;
+      }
+      v = fmaf(ja, jb, v);
+    }
+    atomicAdd(dst + e, (double)v);
+  }
+}
+
+// Dense coarse matrix entry (I, J): the 4x4 kernels expanded over the three
+// rows r, plus the aggregate's sum of orthogonality blocks at the current x.
+__device__ __forceinline__ float coarse_entry_x(const SolveParams& P, const double* rotagg, int I, int J) {
+  const int a = I / 12, iI = I % 12, b = J / 12, iJ = J % 12;
+  const int rI = iI < 9 ? iI % 3 : iI - 9, pI = iI < 9 ? iI / 3 : 3;
+  const int rJ = iJ < 9 ? iJ % 3 : iJ - 9, pJ = iJ < 9 ? iJ / 3 : 3;
+  double v = (rI == rJ) ? P.Qd[((size_t)a * P.NA + b) * 16 + 4 * pI + pJ] : 0.0;
+  if (a == b && iI < 9 && iJ < 9) v += __ldcg(rotagg + 81 * (size_t)a + 9 * iI + iJ);
+  return (float)v;
+}
+
+// Restriction of free node rr's residual (lane c < 12 holds r_c) into rc:
+// (P_j^T r_j)_{3c+r} = r_{3c+r} + d_c r_{9+r}, (P_j^T r_j)_{9+r} = r_{9+r}.
+__device__ __forceinline__ void coarse_restrict(const SolveParams& P, int rr, float rc_lane, double* rc) {
+  const int lane = threadIdx.x & 31;
+  const int a = __ldg(P.agg + rr);
+  const int node = __ldg(P.free_ids + rr);
+  const int pv = __ldg(P.pivot + a);
+  const int c = lane < 9 ? lane / 3 : 0, r = lane < 9 ? lane % 3 : 0;
+  const float rt = __shfl_sync(0xffffffffu, rc_lane, 9 + r);
+  if (lane < 12) {
+    float v = rc_lane;
+    if (lane < 9) v += (__ldg(P.node_pos + 3 * (size_t)node + c) - __ldg(P.node_pos + 3 * (size_t)pv + c)) * rt;
+    atomicAdd(rc + 12 * a + lane, (double)v);
+  }
 }
 
 }  // namespace arap

@@ -17,6 +17,124 @@ __device__ __forceinline__ bool reduce_all(const SolveParams& P, double (&v)[N],
   return grid_sync_reduce<N>(P.bar, P.partials, P.results, v, out);
 }
 
+// Inverse of the coarse matrix in Cw[0] by blocked Gauss-Jordan (float32, no
+// pivoting: the matrix is symmetric positive definite).  For each pivot block
+// K: CTA 0 inverts A_KK in shared memory; every CTA forms W = A_:K A_KK^-1;
+// then A_KK <- A_KK^-1, A_Kj <- A_KK^-1 A_Kj, A_iK <- -W_iK,
+// A_ij <- A_ij - W_iK A_Kj.  Three grid barriers per block.  Returns false on a
+// barrier failure; *ok = 0 when a pivot block was not positive definite.
+__device__ bool coarse_invert(const SolveParams& P, int* ok) {
+  __shared__ float s_piv[kGJBlock][kGJBlock + 1];
+  __shared__ float s_row[kGJBlock], s_col[kGJBlock];
+  __shared__ int s_bad;
+  const int NC = P.NC;
+  const size_t NC2 = (size_t)NC * NC;
+  const int gt = blockIdx.x * blockDim.x + threadIdx.x;
+  const int nt = gridDim.x * blockDim.x;
+  int src_i = 0;
+  *ok = 1;
+  for (int K0 = 0; K0 < NC; K0 += kGJBlock) {
+    const int kb = min(kGJBlock, NC - K0);
+    const float* src = P.Cw + src_i * NC2;
+    float* dst = P.Cw + (1 - src_i) * NC2;
+    const bool last = K0 + kb >= NC;
+    double bad[1] = {0.0}, obad[1];
+    if (blockIdx.x == 0) {
+      if (threadIdx.x == 0) s_bad = 0;
+      for (int t = threadIdx.x; t < kb * kb; t += blockDim.x)
+        s_piv[t / kb][t % kb] = __ldcg(src + (size_t)(K0 + t / kb) * NC + K0 + t % kb);
+      for (int m = 0; m < kb; ++m) {
+        __syncthreads();
+        if (threadIdx.x < kb) {
+          s_row[threadIdx.x] = s_piv[m][threadIdx.x];
+          s_col[threadIdx.x] = s_piv[threadIdx.x][m];
+        }
+        __syncthreads();
+        const float pv = s_row[m];
+        if (!(pv > 0.f)) {
+          if (threadIdx.x == 0) s_bad = 1;
+          continue;
+        }
+        const float ip = 1.f / pv;
+        for (int t = threadIdx.x; t < kb * kb; t += blockDim.x) {
+          const int i = t / kb, j = t % kb;
+          float v;
+          if (i == m && j == m)
+            v = ip;
+          else if (i == m)
+            v = s_row[j] * ip;
+          else if (j == m)
+            v = -s_col[i] * ip;
+          else
+            v = s_piv[i][j] - s_col[i] * s_row[j] * ip;
+          s_piv[i][j] = v;
+        }
+      }
+      __syncthreads();
+      for (int t = threadIdx.x; t < kb * kb; t += blockDim.x) P.Pgj[t] = s_piv[t / kb][t % kb];
+      bad[0] = s_bad;
+    }
+    if (!grid_sync_reduce<1>(P.bar, P.partials, P.results, bad, obad)) return false;
+    if (obad[0] != 0.0) *ok = 0;
+    for (size_t e = gt; e < (size_t)NC * kb; e += nt) {
+      const int i = (int)(e / kb), n = (int)(e % kb);
+      if (i >= K0 && i < K0 + kb) continue;
+      float w = 0.f;
+      for (int m = 0; m < kb; ++m) w = fmaf(__ldcg(src + (size_t)i * NC + K0 + m), __ldcg(P.Pgj + m * kb + n), w);
+      P.Wgj[(size_t)i * kb + n] = w;
+    }
+    double d0[1] = {0.0}, o0[1];
+    if (!grid_sync_reduce<1>(P.bar, P.partials, P.results, d0, o0)) return false;
+    for (size_t e = gt; e < NC2; e += nt) {
+      const int i = (int)(e / NC), j = (int)(e % NC);
+      const int iK = i - K0, jK = j - K0;
+      const bool inI = iK >= 0 && iK < kb, inJ = jK >= 0 && jK < kb;
+      float v;
+      if (inI && inJ) {
+        v = __ldcg(P.Pgj + iK * kb + jK);
+      } else if (inI) {
+        v = 0.f;
+        for (int m = 0; m < kb; ++m) v = fmaf(__ldcg(P.Pgj + iK * kb + m), __ldcg(src + (size_t)(K0 + m) * NC + j), v);
+      } else if (inJ) {
+        v = -__ldcg(P.Wgj + (size_t)i * kb + jK);
+      } else {
+        v = __ldcg(src + e);
+        for (int m = 0; m < kb; ++m) v = fmaf(-__ldcg(P.Wgj + (size_t)i * kb + m), __ldcg(src + (size_t)(K0 + m) * NC + j), v);
+      }
+      if (last)
+        P.Cinv[e] = v;
+      else
+        dst[e] = v;
+    }
+    if (!grid_sync_reduce<1>(P.bar, P.partials, P.results, d0, o0)) return false;
+    src_i ^= 1;
+  }
+  return true;
+}
+
+// zc = Cinv rc (one warp per row), zero the other restriction buffer, and
+// this thread's share of rc . zc.
+__device__ __forceinline__ bool coarse_solve(const SolveParams& P, const double* rc, double* rc_other,
+                                             double (&part)[1], int ok) {
+  const int lane = threadIdx.x & 31;
+  const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int nw = (gridDim.x * blockDim.x) >> 5;
+  const int NC = P.NC;
+  for (int i = gw; i < NC; i += nw) {
+    double acc = 0.0;
+    const float* row = P.Cinv + (size_t)i * NC;
+    if (ok)
+      for (int j = lane; j < NC; j += 32) acc += (double)__ldcg(row + j) * __ldcg(rc + j);
+    acc = warp_sum(acc);
+    if (lane == 0) {
+      P.zc[i] = (float)acc;
+      part[0] += __ldcg(rc + i) * acc;
+    }
+  }
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < NC; e += gridDim.x * blockDim.x) rc_other[e] = 0.0;
+  return true;
+}
+
 template <typename RT>
 __global__ void __launch_bounds__(kSolveThreads) gn_solve_kernel(SolveParams P) {
   __shared__ float s_D[kSolveWarps][144];
@@ -55,7 +173,20 @@ __global__ void __launch_bounds__(kSolveThreads) gn_solve_kernel(SolveParams P) 
     P.x[e] = v;
     P.xf[e] = (float)v;
   }
+  const bool coarse = P.NA > 0 && P.mode == 0;
+  if (coarse) {
+    for (int e = gt; e < P.NA * P.NA * 16; e += nt) P.Qd[e] = 0.0;
+    for (int e = gt; e < 2 * P.NC; e += nt) P.rc[e] = 0.0;
+    for (int e = gt; e < 2 * P.NA * 81; e += nt) P.rotagg[e] = 0.0;
+  }
   {
+    double d0[1] = {0.0}, o0[1];
+    if (!grid_sync_reduce<1>(P.bar, P.partials, P.results, d0, o0)) return;
+  }
+  if (coarse) {
+    // coarse matrix P^T (J^T J at x = I) P, fixed for this solve
+    for (int oi = gw; oi < F; oi += nw) coarse_rows_node(P, __ldg(P.order + oi));
+    for (int g = gt; g < P.G; g += nt) coarse_rows_group(P, g);
     double d0[1] = {0.0}, o0[1];
     if (!grid_sync_reduce<1>(P.bar, P.partials, P.results, d0, o0)) return;
   }
@@ -83,11 +214,13 @@ __global__ void __launch_bounds__(kSolveThreads) gn_solve_kernel(SolveParams P) 
         continue;
       }
       build_dinv(P, r, Q, s_D[wib]);
+      if (coarse) coarse_rot_node(P, r, P.rotagg + (it & 1) * 81 * P.NA);
       float gc = 0.f;
 #pragma unroll
       for (int i = 0; i < 12; ++i)
         if (i == lane) gc = -(float)acc[i];
       const float zc = apply_dinv(P, r, gc);
+      if (coarse) coarse_restrict(P, r, gc, P.rc);
       if (lane < 12) {
         const size_t o = 12 * (size_t)r + lane;
         P.g[o] = gc;
@@ -117,10 +250,30 @@ __global__ void __launch_bounds__(kSolveThreads) gn_solve_kernel(SolveParams P) 
       return;
     }
 
-    // ---- PCG on (J^T J) h = g, two barriers per iteration
+    // ---- PCG on (J^T J) h = g: two barriers per iteration, plus one for the
+    // coarse solve when the two-level preconditioner is on
     double rz = out[2];
     const double rr0 = out[3];
     double rr = rr0;
+    int coarse_ok = 0;
+    if (coarse) {
+      // coarse matrix at this x: fixed kernels + current orthogonality blocks
+      const double* rot_now = P.rotagg + (it & 1) * 81 * P.NA;
+      double* rot_next = P.rotagg + ((it + 1) & 1) * 81 * P.NA;
+      const size_t NC2 = (size_t)P.NC * P.NC;
+      for (size_t e = gt; e < NC2; e += nt) P.Cw[e] = coarse_entry_x(P, rot_now, (int)(e / P.NC), (int)(e % P.NC));
+      for (int e = gt; e < 81 * P.NA; e += nt) rot_next[e] = 0.0;
+      double d0[1] = {0.0}, o0[1];
+      if (!grid_sync_reduce<1>(P.bar, P.partials, P.results, d0, o0)) return;
+      if (!coarse_invert(P, &coarse_ok)) return;
+      if (!coarse_ok && gt == 0) raise_status(ARAP_ENONFINITE);
+    }
+    if (coarse) {
+      double rzc[1] = {0.0}, orc[1];
+      if (!coarse_solve(P, P.rc, P.rc + P.NC, rzc, coarse_ok)) return;
+      if (!reduce_all<1>(P, rzc, orc)) return;
+      rz += orc[0];
+    }
     const double tol2 = (double)P.pcg_tol * (double)P.pcg_tol * rr0;
     float beta = 0.f;
     int pi = 0;
@@ -130,7 +283,7 @@ __global__ void __launch_bounds__(kSolveThreads) gn_solve_kernel(SolveParams P) 
       const float* pold = (pi & 1) ? P.p0 : P.p1;
       double pq[1] = {0.0}, opq[1];
       for (int oi = gw; oi < F; oi += nw) {
-      const int r = __ldg(P.order + oi);
+        const int r = __ldg(P.order + oi);
         float acc[12], pj[12];
         spmv_node(P, r, first, beta, pold, acc, pj);
         if (lane < 12) {
@@ -150,9 +303,10 @@ __global__ void __launch_bounds__(kSolveThreads) gn_solve_kernel(SolveParams P) 
       if (!reduce_all<1>(P, pq, opq)) return;
       if (!(opq[0] > 0.0)) break;
       const float alpha = (float)(rz / opq[0]);
+      double* rc_next = P.rc + ((pi + 1) & 1) * P.NC;
       double rzr[2] = {0.0, 0.0}, orz[2];
       for (int oi = gw; oi < F; oi += nw) {
-      const int r = __ldg(P.order + oi);
+        const int r = __ldg(P.order + oi);
         float rc = 0.f;
         if (lane < 12) {
           const size_t o = 12 * (size_t)r + lane;
@@ -161,6 +315,7 @@ __global__ void __launch_bounds__(kSolveThreads) gn_solve_kernel(SolveParams P) 
           P.r[o] = rc;
         }
         const float zc = apply_dinv(P, r, rc);
+        if (coarse) coarse_restrict(P, r, rc, rc_next);
         if (lane < 12) {
           P.z[12 * (size_t)r + lane] = zc;
           rzr[0] += (double)rc * (double)zc;
@@ -168,10 +323,18 @@ __global__ void __launch_bounds__(kSolveThreads) gn_solve_kernel(SolveParams P) 
         }
       }
       if (!reduce_all<2>(P, rzr, orz)) return;
-      beta = (float)(orz[0] / rz);
-      rz = orz[0];
-      rr = orz[1];
       ++pi;
+      rr = orz[1];
+      if (rr <= tol2 || pi >= P.pcg_max) break;
+      double rz_new = orz[0];
+      if (coarse) {
+        double rzc[1] = {0.0}, orc[1];
+        if (!coarse_solve(P, rc_next, P.rc + (pi & 1 ? 0 : 1) * P.NC, rzc, coarse_ok)) return;
+        if (!reduce_all<1>(P, rzc, orc)) return;
+        rz_new += orc[0];
+      }
+      beta = (float)(rz_new / rz);
+      rz = rz_new;
     }
     pcg_total += pi;
 

@@ -76,6 +76,8 @@ typedef struct {
   int precision;          /* ARAP_PRECISION_PLAIN or ARAP_PRECISION_MIXED */
   float pcg_tol;          /* relative residual target of the inner PCG (<=0: default) */
   int pcg_max_iters;      /* inner PCG iteration cap (<=0: default) */
+  int coarse_nodes;       /* two-level PCG: target free nodes per aggregate of the coarse
+                             (per-aggregate affine) space; 0 = block-Jacobi only */
 } arap_solve_config;
 
 typedef struct {

@@ -101,8 +101,8 @@ def _problem(scene):
     return nb, aidx, aw, aims
 
 
-@pytest.mark.parametrize("precision", [0, 1])
-def test_solve_matches_oracle(dev, scene, precision):
+@pytest.mark.parametrize("precision,coarse", [(0, 0), (1, 0), (1, 32)])
+def test_solve_matches_oracle(dev, scene, precision, coarse):
     from oracle import ed
     nb, aidx, aw, aims = _problem(scene)
     pr = ed.EDProblem(scene.node_pos, nb, aidx, aw, scene.blocks, scene.block_type, aims)
@@ -110,7 +110,7 @@ def test_solve_matches_oracle(dev, scene, precision):
     rot_ref, tr_ref = ed.put_free_inputs(pr, x_ref)
     solver = dev.Solver(_t(nb.astype(np.int32)), _t(aidx.T.astype(np.int32)), _t(aw.T.astype(np.float32)),
                         scene.blocks, scene.block_type, max_iters=scene.iters, early_exit=0,
-                        precision=precision)
+                        precision=precision, coarse_nodes=coarse)
     rot, tr, st = solver.solve(_t(scene.node_pos), _t(aims))
     assert st["status"] == 0
     assert st["gn_iterations"] == scene.iters
@@ -118,7 +118,7 @@ def test_solve_matches_oracle(dev, scene, precision):
     X = np.concatenate([_np(rot), _np(tr)], axis=1)
     Xr = np.concatenate([rot_ref, tr_ref], axis=1)
     err = np.abs(X - Xr).max() / np.abs(Xr).max()
-    print("solve", scene.name, precision, "rel err", err, "pcg", st["pcg_iterations"],
+    print("solve", scene.name, precision, coarse, "rel err", err, "pcg", st["pcg_iterations"],
           "E", st["final_energy"], st_ref.final_energy)
     assert abs(st["initial_energy"] - st_ref.energies[0]) <= 1e-5 * st_ref.energies[0]
     assert err <= (1e-5 if precision == 1 else 5e-5)
