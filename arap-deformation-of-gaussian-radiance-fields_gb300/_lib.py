@@ -74,6 +74,7 @@ SIGNATURES = {
     "arap_aims_scale": (I, [P, P, P, I, F, P]),
     "arap_grid_build": (I, [C.POINTER(P), I, P, P, P, P, I, I, C.POINTER(GridInfo), P]),
     "arap_grid_arrays": (I, [P, C.POINTER(P), C.POINTER(P), C.POINTER(P)]),
+    "arap_grid_center_order": (I, [P, I, P, P, P]),
     "arap_grid_samples": (I, [P, P, P]),
     "arap_grid_ada_lpf": (I, [P, P, F, P, P]),
     "arap_grid_density": (I, [P, P, P, P, P, P, P, P, F, P, P, P]),

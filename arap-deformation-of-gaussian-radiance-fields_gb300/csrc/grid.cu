@@ -283,6 +283,29 @@ __global__ void sort_cells_kernel(int nvalid, const int* __restrict__ valid, con
   for (int t = threadIdx.x; t < L; t += blockDim.x) lists[b + t] = s_keys[t];
 }
 
+// Cell of each Gaussian centre (GaussianView.cpp:3918-3928) and per-cell counts.
+__global__ void center_cell_kernel(int N, const float* __restrict__ pos, const GridParams* __restrict__ Pg,
+                                   int* __restrict__ cell, int* __restrict__ count) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= N) return;
+  const GridParams P = *Pg;
+  int c3[3];
+#pragma unroll
+  for (int c = 0; c < 3; ++c)
+    c3[c] = min(max((int)floorf((pos[3 * (size_t)i + c] - P.mn[c]) / P.step), 0), P.g - 1);
+  const int id = (c3[0] * P.g + c3[1]) * P.g + c3[2];
+  cell[i] = id;
+  atomicAdd(count + id, 1);
+}
+
+__global__ void center_fill_kernel(int N, const int* __restrict__ cell, const int* __restrict__ off,
+                                   int* __restrict__ cursor, int* __restrict__ lists) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= N) return;
+  const int c = cell[i];
+  lists[off[c] + atomicAdd(cursor + c, 1)] = i;
+}
+
 // 64 samples per occupied cell (GaussianView.cpp:4104-4133).
 __global__ void samples_kernel(int nvalid, const int* __restrict__ valid, const GridParams* __restrict__ Pg,
                                float* __restrict__ out) {
@@ -296,8 +319,9 @@ __global__ void samples_kernel(int nvalid, const int* __restrict__ valid, const 
   const int si[3] = {s / 16, (s % 16) / 4, s % 4};
 #pragma unroll
   for (int d = 0; d < 3; ++d) {
-    const float base = (float)((double)(P.mn[d] + (float)ci[d] * P.step) + 0.5 * (double)P.interval);
-    out[3 * (size_t)t + d] = base + (float)si[d] * P.interval;
+    // float32 multiply and add kept separate, as the reference's host code
+    const float base = (float)((double)__fadd_rn(P.mn[d], __fmul_rn((float)ci[d], P.step)) + 0.5 * (double)P.interval);
+    out[3 * (size_t)t + d] = __fadd_rn(base, __fmul_rn((float)si[d], P.interval));
   }
 }
 
@@ -568,6 +592,55 @@ extern "C" int arap_grid_build(arap_grid** out, int N, const float* pos, const f
     info_host->n_pairs = total;
   }
   *out = G;
+  return arap_get_device_status(stream);
+}
+
+extern "C" int arap_grid_center_order(const arap_grid* G, int N, const float* pos, int32_t* order_out,
+                                      arap_stream_t stream) {
+  if (!G || !pos || !order_out || N < 1) return ARAP_EBADINPUT;
+  cudaStream_t st = (cudaStream_t)stream;
+  const long long cells = (long long)G->g * G->g * G->g;
+  const int C = (int)cells;
+  int *cell = nullptr, *count = nullptr, *cursor = nullptr, *off = nullptr, *flagpos = nullptr, *valid = nullptr;
+  long long* sums = nullptr;
+  const int nbs = (C + 1 + kScanTile - 1) / kScanTile + 1;
+  int rc = ARAP_OK;
+  auto done = [&](int code) {
+    cudaFree(cell); cudaFree(count); cudaFree(cursor); cudaFree(off); cudaFree(flagpos); cudaFree(valid);
+    cudaFree(sums);
+    return code;
+  };
+  if (cudaMalloc(&cell, sizeof(int) * (size_t)N) || cudaMalloc(&count, sizeof(int) * (size_t)C) ||
+      cudaMalloc(&cursor, sizeof(int) * (size_t)C) || cudaMalloc(&off, sizeof(int) * ((size_t)C + 1)) ||
+      cudaMalloc(&flagpos, sizeof(int) * ((size_t)C + 1)) || cudaMalloc(&sums, sizeof(long long) * (nbs + 1))) {
+    (void)cudaGetLastError();
+    return done(ARAP_ENOMEM);
+  }
+  if (cudaMemsetAsync(count, 0, sizeof(int) * (size_t)C, st) || cudaMemsetAsync(cursor, 0, sizeof(int) * (size_t)C, st))
+    return done(ARAP_ECUDA);
+  center_cell_kernel<<<grid_for(N, 256), 256, 0, st>>>(N, pos, G->params, cell, count);
+  if ((rc = scan_exclusive(count, off, C, sums, st)) != ARAP_OK) return done(rc);
+  center_fill_kernel<<<grid_for(N, 256), 256, 0, st>>>(N, cell, off, cursor, order_out);
+  flags_kernel<<<grid_for(C, 256), 256, 0, st>>>(C, count, cursor);
+  if ((rc = scan_exclusive(cursor, flagpos, C, sums, st)) != ARAP_OK) return done(rc);
+  int nvalid = 0;
+  if (cudaMemcpyAsync(&nvalid, flagpos + C, sizeof(int), cudaMemcpyDeviceToHost, st) || cudaStreamSynchronize(st))
+    return done(ARAP_ECUDA);
+  if (nvalid > 0) {
+    if (cudaMalloc(&valid, sizeof(int) * (size_t)nvalid)) {
+      (void)cudaGetLastError();
+      return done(ARAP_ENOMEM);
+    }
+    compact_kernel<<<grid_for(C, 256), 256, 0, st>>>(C, count, flagpos, valid);
+    if (cudaFuncSetAttribute(sort_cells_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSortMax * (int)sizeof(int)))
+      return done(ARAP_ECUDA);
+    sort_cells_kernel<<<nvalid, 256, kSortMax * sizeof(int), st>>>(nvalid, valid, off, order_out);
+  }
+  if (cudaPeekAtLastError() != cudaSuccess || cudaStreamSynchronize(st) != cudaSuccess) {
+    (void)cudaGetLastError();
+    return done(ARAP_ECUDA);
+  }
+  done(ARAP_OK);
   return arap_get_device_status(stream);
 }
 

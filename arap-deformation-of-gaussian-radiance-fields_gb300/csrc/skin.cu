@@ -13,7 +13,7 @@ namespace arap {
 
 constexpr int kSkinThreads = 128;
 
-// Node table entry: [R row-major 9 | g 3 | t+g 3 | 0] as four float4.
+// Node table entry: [R - I row-major 9 | g 3 | t 3 | 0] as four float4.
 struct NodeXf {
   float4 a, b, c, d;
 };
@@ -28,17 +28,24 @@ __device__ __forceinline__ NodeXf load_node(const float* __restrict__ table, int
   return x;
 }
 
-// w * (R (p - g) + t + g), the summand of DeformGraph::predict_mesh
-// (Deform.hpp:238-246).
+// w * ((R - I)(p - g) + t): the summand of DeformGraph::predict_mesh
+// (Deform.hpp:238-246) minus w p.  A blend is accumulated from these small
+// terms and added to (sum w) p once at the end (ed_finish), so the stored
+// position is rounded once instead of once per neighbour.
 __device__ __forceinline__ void ed_term(const NodeXf& x, float w, float px, float py, float pz,
                                         float& ox, float& oy, float& oz) {
   const float dx = px - x.c.y, dy = py - x.c.z, dz = pz - x.c.w;
-  const float mx = fmaf(x.a.x, dx, fmaf(x.a.y, dy, x.a.z * dz)) + x.d.x;
-  const float my = fmaf(x.a.w, dx, fmaf(x.b.x, dy, x.b.y * dz)) + x.d.y;
-  const float mz = fmaf(x.b.z, dx, fmaf(x.b.w, dy, x.c.x * dz)) + x.d.z;
+  const float mx = fmaf(x.a.x, dx, fmaf(x.a.y, dy, fmaf(x.a.z, dz, x.d.x)));
+  const float my = fmaf(x.a.w, dx, fmaf(x.b.x, dy, fmaf(x.b.y, dz, x.d.y)));
+  const float mz = fmaf(x.b.z, dx, fmaf(x.b.w, dy, fmaf(x.c.x, dz, x.d.z)));
   ox = fmaf(w, mx, ox);
   oy = fmaf(w, my, oy);
   oz = fmaf(w, mz, oz);
+}
+
+// p' = (sum w) p + sum w ((R - I)(p - g) + t) = p + [(sum w - 1) p + acc].
+__device__ __forceinline__ float ed_finish(float p, float wsum, float acc) {
+  return p + fmaf(wsum - 1.0f, p, acc);
 }
 
 __global__ void node_table_kernel(int n, const float* __restrict__ rot,
@@ -49,13 +56,10 @@ __global__ void node_table_kernel(int n, const float* __restrict__ rot,
   const float* r = rot + 9 * (size_t)j;  // column-major
   float4* t = reinterpret_cast<float4*>(table) + 4 * (size_t)j;
   const float gx = pos[3 * (size_t)j], gy = pos[3 * (size_t)j + 1], gz = pos[3 * (size_t)j + 2];
-  const double cx = (double)trans[3 * (size_t)j] + gx;
-  const double cy = (double)trans[3 * (size_t)j + 1] + gy;
-  const double cz = (double)trans[3 * (size_t)j + 2] + gz;
-  t[0] = make_float4(r[0], r[3], r[6], r[1]);
-  t[1] = make_float4(r[4], r[7], r[2], r[5]);
-  t[2] = make_float4(r[8], gx, gy, gz);
-  t[3] = make_float4((float)cx, (float)cy, (float)cz, 0.f);
+  t[0] = make_float4(r[0] - 1.0f, r[3], r[6], r[1]);
+  t[1] = make_float4(r[4] - 1.0f, r[7], r[2], r[5]);
+  t[2] = make_float4(r[8] - 1.0f, gx, gy, gz);
+  t[3] = make_float4(trans[3 * (size_t)j], trans[3 * (size_t)j + 1], trans[3 * (size_t)j + 2], 0.f);
 }
 
 // GetEndPoints (GaussianView.cpp:4643-4668).
@@ -87,6 +91,34 @@ __global__ void end_points_kernel(int N, const float* __restrict__ pos,
 
 // Fused UpdatePosition (endpoint part, GaussianView.cpp:3022-3040) and
 // UpdateAsSixPointsWithdrawBad (GaussianView.cpp:3081-3166).
+//
+// One CTA owns a tile of kSkinTile Gaussians.  Every input of the tile -- the
+// 18 endpoint planes, the 6k index and weight planes, scale0, the previous
+// quaternions and the 48-float SH records -- is first copied into shared
+// memory with cp.async (no registers held while the copies are in flight, so
+// the whole tile's traffic is outstanding at once); then each thread skins
+// its Gaussian from shared memory and the SH records go back with coalesced
+// 16-byte stores.
+constexpr int kSkinTile = kSkinThreads;  // Gaussians per CTA
+constexpr int kShStride = 52;            // floats per staged SH record (13 float4: conflict-free)
+
+__device__ __forceinline__ void cp_async4(void* smem, const void* gmem) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() {
+  asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;" ::: "memory");
+}
+
+template <int K>
+constexpr size_t skin_smem_bytes() {
+  return sizeof(float) * (size_t)kSkinTile * (18 + 12 * K + 3 + 4 + kShStride);
+}
+
 template <int K, bool MIXED>
 __global__ void __launch_bounds__(kSkinThreads)
     skin_gaussians_kernel(int N, float* __restrict__ ends, const int32_t* __restrict__ eidx,
@@ -95,125 +127,163 @@ __global__ void __launch_bounds__(kSkinThreads)
                           float* __restrict__ pos_out, float* __restrict__ rot_inout,
                           float* __restrict__ scale_out, float* __restrict__ shs,
                           float* __restrict__ cov_out) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= N) return;
-  float e[18];
+  extern __shared__ float4 s_raw4[];
+  float* s_raw = reinterpret_cast<float*>(s_raw4);
+  float* s_sh = s_raw;                                        // [T][52]
+  float4* s_q = reinterpret_cast<float4*>(s_sh + kSkinTile * kShStride);  // [T]
+  float* s_ends = reinterpret_cast<float*>(s_q + kSkinTile);  // [18][T]
+  float* s_w = s_ends + 18 * kSkinTile;                       // [6K][T]
+  int* s_idx = reinterpret_cast<int*>(s_w + 6 * K * kSkinTile);  // [6K][T]
+  float* s_s0 = reinterpret_cast<float*>(s_idx + 6 * K * kSkinTile);  // [T][3]
+  const int t = threadIdx.x;
+  const int tile0 = blockIdx.x * kSkinTile;
+  const int cnt = min(kSkinTile, N - tile0);
+  const int i = tile0 + t;
+  const bool active = t < cnt;
+  // ---- stage the tile
+  if (active) {
 #pragma unroll
-  for (int c = 0; c < 18; ++c) e[c] = __ldcs(ends + (size_t)c * N + i);
+    for (int c = 0; c < 18; ++c) cp_async4(s_ends + c * kSkinTile + t, ends + (size_t)c * N + i);
 #pragma unroll
-  for (int ep = 0; ep < 6; ++ep) {
-    float ox = 0.f, oy = 0.f, oz = 0.f;
-#pragma unroll
-    for (int j = 0; j < K; ++j) {
-      const size_t o = (size_t)(j * 6 + ep) * N + i;
-      const int nid = __ldcs(eidx + o);
-      const float w = __ldcs(ew + o);
-      const NodeXf x = load_node(table, nid);
-      ed_term(x, w, e[3 * ep], e[3 * ep + 1], e[3 * ep + 2], ox, oy, oz);
+    for (int c = 0; c < 6 * K; ++c) {
+      cp_async4(s_w + c * kSkinTile + t, ew + (size_t)c * N + i);
+      cp_async4(s_idx + c * kSkinTile + t, eidx + (size_t)c * N + i);
     }
-    e[3 * ep] = ox;
-    e[3 * ep + 1] = oy;
-    e[3 * ep + 2] = oz;
+    cp_async16(s_q + t, reinterpret_cast<const float4*>(rot_inout) + i);
   }
-#pragma unroll
-  for (int c = 0; c < 18; ++c) __stcs(ends + (size_t)c * N + i, e[c]);
-  if (static_mask && static_mask[i]) return;
-
-  float cx = 0.f, cy = 0.f, cz = 0.f;
-#pragma unroll
-  for (int ep = 0; ep < 6; ++ep) {
-    cx += e[3 * ep];
-    cy += e[3 * ep + 1];
-    cz += e[3 * ep + 2];
-  }
-  cx *= (1.0f / 6.0f);
-  cy *= (1.0f / 6.0f);
-  cz *= (1.0f / 6.0f);
-  // M = (P - c) Q^+ with Q = [e0 -e0 e1 -e1 e2 -e2], Q^+ = Q^T / 2:
-  // column a of M is (P_{2a} - P_{2a+1}) / 2.
-  float M[9];
-#pragma unroll
-  for (int a = 0; a < 3; ++a) {
-#pragma unroll
-    for (int r = 0; r < 3; ++r) M[r * 3 + a] = 0.5f * (e[3 * (2 * a) + r] - e[3 * (2 * a + 1) + r]);
-  }
-  float R[9];
-  bool ok;
-  if (MIXED) {
-    // FP64 polar factor when M is ill-conditioned (sigma_min/sigma_max < 1e-3)
-    float nx = 0.f, ny = 0.f, Y[9];
-    ok = inv_transpose3(M, Y);
-#pragma unroll
-    for (int t = 0; t < 9; ++t) {
-      nx += M[t] * M[t];
-      ny += Y[t] * Y[t];
-    }
-    if (!ok || nx * ny > 1e6f) {
-      double Md[9], Rd[9];
-#pragma unroll
-      for (int t = 0; t < 9; ++t) Md[t] = M[t];
-      ok = polar_factor<double>(Md, Rd, 40, 1e-15);
-#pragma unroll
-      for (int t = 0; t < 9; ++t) R[t] = (float)Rd[t];
-    } else {
-      ok = polar_factor<float>(M, R, 20, 2e-7f);
-    }
-  } else {
-    ok = polar_factor<float>(M, R, 20, 2e-7f);
-  }
-  if (!ok) raise_status(ARAP_ENONFINITE);
-  // K = diag(R^T M) = diag(V S V^T)
-  float Kd[3];
-#pragma unroll
-  for (int a = 0; a < 3; ++a) Kd[a] = R[a] * M[a] + R[3 + a] * M[3 + a] + R[6 + a] * M[6 + a];
-  const float4 q = quat_normalize(quat_from_rowmajor(R));
-  float s[3];
-#pragma unroll
-  for (int a = 0; a < 3; ++a) {
-    const float s0 = scale0[3 * (size_t)i + a];
-    s[a] = Kd[a] / ((s0 + 1e-3f) * 2.0f) * s0;
-  }
-  pos_out[3 * (size_t)i] = cx;
-  pos_out[3 * (size_t)i + 1] = cy;
-  pos_out[3 * (size_t)i + 2] = cz;
-  scale_out[3 * (size_t)i] = s[0];
-  scale_out[3 * (size_t)i + 1] = s[1];
-  scale_out[3 * (size_t)i + 2] = s[2];
-  float4* rq = reinterpret_cast<float4*>(rot_inout) + i;
-  const float4 q_old = *rq;
-  *rq = q;
+  for (int e = t; e < 3 * cnt; e += kSkinThreads) cp_async4(s_s0 + e, scale0 + 3 * (size_t)tile0 + e);
   if (shs) {
-    const float4 qr = quat_normalize(quat_mul(q, quat_inverse(q_old)));
-    float Rr[9];
-    quat_to_rowmajor(qr, Rr);
-    float4* sp = reinterpret_cast<float4*>(shs + 48 * (size_t)i);
-    float v[48];
-#pragma unroll
-    for (int t = 0; t < 12; ++t) {
-      const float4 u = __ldcs(sp + t);
-      v[4 * t] = u.x;
-      v[4 * t + 1] = u.y;
-      v[4 * t + 2] = u.z;
-      v[4 * t + 3] = u.w;
-    }
-    rotate_sh48<true>(Rr, v);
-#pragma unroll
-    for (int t = 0; t < 12; ++t) __stcs(sp + t, make_float4(v[4 * t], v[4 * t + 1], v[4 * t + 2], v[4 * t + 3]));
+    const float* src = shs + 48 * (size_t)tile0;
+    for (int q = t; q < 12 * cnt; q += kSkinThreads)
+      cp_async16(s_sh + (q / 12) * kShStride + (q % 12) * 4, src + 4 * (size_t)q);
   }
-  if (cov_out) {
-    float Rq[9];
-    quat_to_rowmajor(q, Rq);
-    const float s2[3] = {s[0] * s[0], s[1] * s[1], s[2] * s[2]};
-    float S[6];
-    int o = 0;
+  cp_async_wait_all();
+  __syncthreads();
+
+  if (active) {
+    float e[18];
 #pragma unroll
-    for (int r = 0; r < 3; ++r)
+    for (int c = 0; c < 18; ++c) e[c] = s_ends[c * kSkinTile + t];
 #pragma unroll
-      for (int c = r; c < 3; ++c)
-        S[o++] = Rq[r * 3] * s2[0] * Rq[c * 3] + Rq[r * 3 + 1] * s2[1] * Rq[c * 3 + 1] +
-                 Rq[r * 3 + 2] * s2[2] * Rq[c * 3 + 2];
+    for (int ep = 0; ep < 6; ++ep) {
+      float ox = 0.f, oy = 0.f, oz = 0.f, ws = 0.f;
 #pragma unroll
-    for (int t = 0; t < 6; ++t) cov_out[6 * (size_t)i + t] = S[t];
+      for (int j = 0; j < K; ++j) {
+        const int c = j * 6 + ep;
+        const NodeXf x = load_node(table, s_idx[c * kSkinTile + t]);
+        const float w = s_w[c * kSkinTile + t];
+        ws += w;
+        ed_term(x, w, e[3 * ep], e[3 * ep + 1], e[3 * ep + 2], ox, oy, oz);
+      }
+      e[3 * ep] = ed_finish(e[3 * ep], ws, ox);
+      e[3 * ep + 1] = ed_finish(e[3 * ep + 1], ws, oy);
+      e[3 * ep + 2] = ed_finish(e[3 * ep + 2], ws, oz);
+    }
+#pragma unroll
+    for (int c = 0; c < 18; ++c) __stcs(ends + (size_t)c * N + i, e[c]);
+    const bool is_static = static_mask && static_mask[i];
+    if (!is_static) {
+      float cx = 0.f, cy = 0.f, cz = 0.f;
+#pragma unroll
+      for (int ep = 0; ep < 6; ++ep) {
+        cx += e[3 * ep];
+        cy += e[3 * ep + 1];
+        cz += e[3 * ep + 2];
+      }
+      cx *= (1.0f / 6.0f);
+      cy *= (1.0f / 6.0f);
+      cz *= (1.0f / 6.0f);
+      // M = (P - c) Q^+ with Q = [e0 -e0 e1 -e1 e2 -e2], Q^+ = Q^T / 2:
+      // column a of M is (P_{2a} - P_{2a+1}) / 2.
+      float M[9];
+#pragma unroll
+      for (int a = 0; a < 3; ++a)
+#pragma unroll
+        for (int r = 0; r < 3; ++r) M[r * 3 + a] = 0.5f * (e[3 * (2 * a) + r] - e[3 * (2 * a + 1) + r]);
+      float R[9];
+      bool ok;
+      if (MIXED) {
+        // FP64 polar factor when M is ill-conditioned (sigma_min/sigma_max < 1e-3)
+        float nx = 0.f, ny = 0.f, Y[9];
+        ok = inv_transpose3(M, Y);
+#pragma unroll
+        for (int q = 0; q < 9; ++q) {
+          nx += M[q] * M[q];
+          ny += Y[q] * Y[q];
+        }
+        if (!ok || nx * ny > 1e6f) {
+          double Md[9], Rd[9];
+#pragma unroll
+          for (int q = 0; q < 9; ++q) Md[q] = M[q];
+          ok = polar_factor<double>(Md, Rd, 40, 1e-15);
+#pragma unroll
+          for (int q = 0; q < 9; ++q) R[q] = (float)Rd[q];
+        } else {
+          ok = polar_factor<float>(M, R, 20, 2e-7f);
+        }
+      } else {
+        ok = polar_factor<float>(M, R, 20, 2e-7f);
+      }
+      if (!ok) raise_status(ARAP_ENONFINITE);
+      // K = diag(R^T M) = diag(V S V^T)
+      float Kd[3];
+#pragma unroll
+      for (int a = 0; a < 3; ++a) Kd[a] = R[a] * M[a] + R[3 + a] * M[3 + a] + R[6 + a] * M[6 + a];
+      const float4 q = quat_normalize(quat_from_rowmajor(R));
+      float sc[3];
+#pragma unroll
+      for (int a = 0; a < 3; ++a) {
+        const float s0 = s_s0[3 * t + a];
+        sc[a] = Kd[a] / ((s0 + 1e-3f) * 2.0f) * s0;
+      }
+      pos_out[3 * (size_t)i] = cx;
+      pos_out[3 * (size_t)i + 1] = cy;
+      pos_out[3 * (size_t)i + 2] = cz;
+      scale_out[3 * (size_t)i] = sc[0];
+      scale_out[3 * (size_t)i + 1] = sc[1];
+      scale_out[3 * (size_t)i + 2] = sc[2];
+      const float4 q_old = s_q[t];
+      reinterpret_cast<float4*>(rot_inout)[i] = q;
+      if (cov_out) {
+        float Rq[9];
+        quat_to_rowmajor(q, Rq);
+        const float s2[3] = {sc[0] * sc[0], sc[1] * sc[1], sc[2] * sc[2]};
+        float S[6];
+        int o = 0;
+#pragma unroll
+        for (int r = 0; r < 3; ++r)
+#pragma unroll
+          for (int c = r; c < 3; ++c)
+            S[o++] = Rq[r * 3] * s2[0] * Rq[c * 3] + Rq[r * 3 + 1] * s2[1] * Rq[c * 3 + 1] +
+                     Rq[r * 3 + 2] * s2[2] * Rq[c * 3 + 2];
+#pragma unroll
+        for (int q6 = 0; q6 < 6; ++q6) cov_out[6 * (size_t)i + q6] = S[q6];
+      }
+      if (shs) {
+        const float4 qr = quat_normalize(quat_mul(q, quat_inverse(q_old)));
+        float Rr[9];
+        quat_to_rowmajor(qr, Rr);
+        float4* rec = reinterpret_cast<float4*>(s_sh + t * kShStride);
+        float v[48];
+#pragma unroll
+        for (int q4 = 0; q4 < 12; ++q4) {
+          const float4 u = rec[q4];
+          v[4 * q4] = u.x;
+          v[4 * q4 + 1] = u.y;
+          v[4 * q4 + 2] = u.z;
+          v[4 * q4 + 3] = u.w;
+        }
+        rotate_sh48<true>(Rr, v);
+#pragma unroll
+        for (int q4 = 0; q4 < 12; ++q4) rec[q4] = make_float4(v[4 * q4], v[4 * q4 + 1], v[4 * q4 + 2], v[4 * q4 + 3]);
+      }
+    }
+  }
+  if (shs) {
+    __syncthreads();
+    float4* dst = reinterpret_cast<float4*>(shs + 48 * (size_t)tile0);
+    for (int q = t; q < 12 * cnt; q += kSkinThreads)
+      __stcs(dst + q, *reinterpret_cast<const float4*>(s_sh + (q / 12) * kShStride + (q % 12) * 4));
   }
 }
 
@@ -285,7 +355,7 @@ __global__ void __launch_bounds__(kSkinThreads)
   if (i >= S) return;
   if (static_mask && static_mask[i]) return;
   const float px = spos[3 * (size_t)i], py = spos[3 * (size_t)i + 1], pz = spos[3 * (size_t)i + 2];
-  float ox = 0.f, oy = 0.f, oz = 0.f;
+  float ox = 0.f, oy = 0.f, oz = 0.f, ws = 0.f;
   float4 wq = make_float4(1.f, 0.f, 0.f, 0.f);
   float last = 0.f;
 #pragma unroll
@@ -293,6 +363,7 @@ __global__ void __launch_bounds__(kSkinThreads)
     const int nid = __ldcs(idx + (size_t)j * S + i);
     const float wj = __ldcs(w + (size_t)j * S + i);
     const NodeXf x = load_node(table, nid);
+    ws += wj;
     ed_term(x, wj, px, py, pz, ox, oy, oz);
     if (feature) {
       const float t = wj / (wj + last);
@@ -300,9 +371,9 @@ __global__ void __launch_bounds__(kSkinThreads)
       last += wj;
     }
   }
-  spos[3 * (size_t)i] = ox;
-  spos[3 * (size_t)i + 1] = oy;
-  spos[3 * (size_t)i + 2] = oz;
+  spos[3 * (size_t)i] = ed_finish(px, ws, ox);
+  spos[3 * (size_t)i + 1] = ed_finish(py, ws, oy);
+  spos[3 * (size_t)i + 2] = ed_finish(pz, ws, oz);
   if (feature) {
     float Rr[9];
     quat_to_rowmajor(quat_normalize(wq), Rr);
@@ -329,14 +400,16 @@ __global__ void update_nodes_kernel(int n, int k, const float* __restrict__ pos,
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const float px = pos[3 * (size_t)i], py = pos[3 * (size_t)i + 1], pz = pos[3 * (size_t)i + 2];
-  float ox = 0.f, oy = 0.f, oz = 0.f;
+  float ox = 0.f, oy = 0.f, oz = 0.f, ws = 0.f;
   for (int j = 0; j < k; ++j) {
     const NodeXf x = load_node(table, aidx[(size_t)j * n + i]);
-    ed_term(x, aw[(size_t)j * n + i], px, py, pz, ox, oy, oz);
+    const float w = aw[(size_t)j * n + i];
+    ws += w;
+    ed_term(x, w, px, py, pz, ox, oy, oz);
   }
-  out[3 * (size_t)i] = ox;
-  out[3 * (size_t)i + 1] = oy;
-  out[3 * (size_t)i + 2] = oz;
+  out[3 * (size_t)i] = ed_finish(px, ws, ox);
+  out[3 * (size_t)i + 1] = ed_finish(py, ws, oy);
+  out[3 * (size_t)i + 2] = ed_finish(pz, ws, oz);
 }
 
 __global__ void static_mask_kernel(int P, int planes, const int32_t* __restrict__ idx,
@@ -437,13 +510,17 @@ template <int K>
 static void launch_skin_g(bool mixed, int N, float* ends, const int32_t* eidx, const float* ew,
                           const float* table, const float* scale0, const uint8_t* st, float* pos,
                           float* rot, float* scale, float* shs, float* cov, cudaStream_t s) {
-  const int grid = grid_for(N, kSkinThreads);
-  if (mixed)
-    skin_gaussians_kernel<K, true><<<grid, kSkinThreads, 0, s>>>(N, ends, eidx, ew, table, scale0, st,
-                                                                  pos, rot, scale, shs, cov);
-  else
-    skin_gaussians_kernel<K, false><<<grid, kSkinThreads, 0, s>>>(N, ends, eidx, ew, table, scale0, st,
-                                                                   pos, rot, scale, shs, cov);
+  const int grid = grid_for(N, kSkinTile);
+  constexpr size_t smem = skin_smem_bytes<K>();
+  if (mixed) {
+    cudaFuncSetAttribute(skin_gaussians_kernel<K, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    skin_gaussians_kernel<K, true><<<grid, kSkinThreads, smem, s>>>(N, ends, eidx, ew, table, scale0, st,
+                                                                     pos, rot, scale, shs, cov);
+  } else {
+    cudaFuncSetAttribute(skin_gaussians_kernel<K, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    skin_gaussians_kernel<K, false><<<grid, kSkinThreads, smem, s>>>(N, ends, eidx, ew, table, scale0, st,
+                                                                      pos, rot, scale, shs, cov);
+  }
 }
 
 template <int K>

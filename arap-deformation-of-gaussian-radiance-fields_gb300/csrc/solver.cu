@@ -268,6 +268,19 @@ extern "C" int arap_solver_create(arap_solver** out, int n, int k, const int32_t
   }
   const int NA = (int)pivot.size();
   const int NC = 12 * NA;
+  // cost of each node for the processing order, from the unpatched kinds
+  std::vector<long long> node_cost(F, 16);
+  for (int r = 0; r < F; ++r)
+    for (int t = item_off[r]; t < item_off[r + 1]; ++t)
+      node_cost[r] += item_flat[t].x == ITEM_CON ? 1 + (grp_off[item_flat[t].z + 1] - grp_off[item_flat[t].z]) * k : 2;
+  // aggregate of the other node in each coupling item, and of each anchor
+  std::vector<int32_t> mem_agg((size_t)U * k, -1);
+  if (NA > 0) {
+    for (size_t q = 0; q < mem_agg.size(); ++q)
+      if (mem_rank[q] >= 0) mem_agg[q] = agg[mem_rank[q]];
+    for (auto& it4 : item_flat)
+      if ((it4.x == ITEM_OUT || it4.x == ITEM_IN) && it4.y >= 0) it4.x |= agg[it4.y] << 4;
+  }
 
   auto* s = new (std::nothrow) arap_solver();
   if (!s) return ARAP_ENOMEM;
@@ -328,6 +341,8 @@ extern "C" int arap_solver_create(arap_solver** out, int n, int k, const int32_t
     P.Cinv = cv.take<float>((size_t)NC * NC);
     P.rc = cv.take<double>((size_t)2 * NC);
     P.zc = cv.take<float>(NC);
+    P.mem_agg = cv.take<int32_t>((size_t)U * k);
+    P.dpiv = cv.take<float4>(NA ? F : 0);
     P.partials = cv.take<double>((size_t)8 * grid);
     P.results = cv.take<double>(8);
     P.stats = cv.take<double>(8);
@@ -366,10 +381,7 @@ extern "C" int arap_solver_create(arap_solver** out, int n, int k, const int32_t
   {
     std::vector<std::pair<long long, int>> cost(F);
     for (int r = 0; r < F; ++r) {
-      long long c = 16;
-      for (int t = item_off[r]; t < item_off[r + 1]; ++t)
-        c += item_flat[t].x == ITEM_CON ? 1 + (grp_off[item_flat[t].z + 1] - grp_off[item_flat[t].z]) * k : 2;
-      cost[r] = {-c, r};
+      cost[r] = {-node_cost[r], r};
     }
     std::sort(cost.begin(), cost.end());
     const int nw = grid * (kSolveThreads / 32);
@@ -381,6 +393,7 @@ extern "C" int arap_solver_create(arap_solver** out, int n, int k, const int32_t
   }
   e = e ? e : up(P.order, order.data(), order.size() * 4);
   if (NA > 0) {
+    e = e ? e : up(P.mem_agg, mem_agg.data(), mem_agg.size() * 4);
     e = e ? e : up(P.agg, agg.data(), agg.size() * 4);
     e = e ? e : up(P.pivot, pivot.data(), pivot.size() * 4);
     e = e ? e : up(P.agg_count, agg_count.data(), agg_count.size() * 4);

@@ -17,6 +17,9 @@ constexpr int kGJBlock = 48;  // pivot block of the coarse Gauss-Jordan inversio
 //               a = -1, b = node i, c = 0
 //   ITEM_CON    constraint group g whose member anchors contain j
 //               a = member-anchor slot (u*k + t), b = g, c = 0
+// The low 4 bits of the kind word hold the kind; the bits above hold the
+// coarse aggregate of node a's free rank (ITEM_OUT / ITEM_IN) when the
+// two-level preconditioner is on.
 enum { ITEM_OUT = 0, ITEM_IN = 1, ITEM_STATIC = 2, ITEM_CON = 3 };
 
 struct SolveParams {
@@ -76,6 +79,8 @@ struct SolveParams {
   double* rotagg;            // [2*NA*81] per-aggregate sums of J_rot^T J_rot (GN-iteration parity)
   double* rc;                // [2*NC] restricted residual, double-buffered
   float* zc;                 // [NC] coarse correction
+  const int32_t* mem_agg;    // [U*k] aggregate of each free anchor (-1 otherwise)
+  float4* dpiv;              // [F] per solve: g_j - g_pivot(agg(j))
 };
 
 }  // namespace arap

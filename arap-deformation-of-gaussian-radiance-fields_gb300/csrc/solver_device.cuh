@@ -27,14 +27,11 @@ __device__ __forceinline__ void ld3t_cg(const float* base, int r, float (&v)[3])
   v[0] = c.y; v[1] = c.z; v[2] = c.w;
 }
 
-// Coarse correction of free node rr (node id `node`): z += P_j zc[a] with
+// Coarse correction of free node rr in aggregate a: z += P_j zc[a] with
 // dR_j = dR_a, dt_j = dR_a (g_j - g_pivot(a)) + dT_a.
-__device__ __forceinline__ void coarse_prolong(const SolveParams& P, int rr, int node, float (&v)[12]) {
-  const int a = __ldg(P.agg + rr);
-  const int pv = __ldg(P.pivot + a);
-  const float d0 = __ldg(P.node_pos + 3 * (size_t)node) - __ldg(P.node_pos + 3 * (size_t)pv);
-  const float d1 = __ldg(P.node_pos + 3 * (size_t)node + 1) - __ldg(P.node_pos + 3 * (size_t)pv + 1);
-  const float d2 = __ldg(P.node_pos + 3 * (size_t)node + 2) - __ldg(P.node_pos + 3 * (size_t)pv + 2);
+__device__ __forceinline__ void coarse_prolong(const SolveParams& P, int rr, int a, float (&v)[12]) {
+  const float4 dp = __ldcg(P.dpiv + rr);
+  const float d0 = dp.x, d1 = dp.y, d2 = dp.z;
   float c[12];
   ld12cg(P.zc, a, c);
 #pragma unroll
@@ -46,10 +43,10 @@ __device__ __forceinline__ void coarse_prolong(const SolveParams& P, int rr, int
 // Search direction of free node rr (node id `node`) for this PCG iteration,
 // formed on the fly: p = z + beta * p_old (p = z on the first iteration),
 // z = Dinv r (+ the coarse correction when the two-level preconditioner is on).
-__device__ __forceinline__ void load_p(const SolveParams& P, int rr, int node, bool first, float beta,
+__device__ __forceinline__ void load_p(const SolveParams& P, int rr, int agg, bool first, float beta,
                                        const float* pold, float (&v)[12]) {
   ld12cg(P.z, rr, v);
-  if (P.NA) coarse_prolong(P, rr, node, v);
+  if (P.NA) coarse_prolong(P, rr, agg, v);
   if (!first) {
     float o[12];
     ld12cg(pold, rr, o);
@@ -58,11 +55,11 @@ __device__ __forceinline__ void load_p(const SolveParams& P, int rr, int node, b
   }
 }
 
-__device__ __forceinline__ void load_pt(const SolveParams& P, int rr, int node, bool first, float beta,
+__device__ __forceinline__ void load_pt(const SolveParams& P, int rr, int agg, bool first, float beta,
                                         const float* pold, float (&v)[3]) {
   if (P.NA) {
     float f[12];
-    load_p(P, rr, node, first, beta, pold, f);
+    load_p(P, rr, agg, first, beta, pold, f);
     v[0] = f[9];
     v[1] = f[10];
     v[2] = f[11];
@@ -173,7 +170,7 @@ __device__ void con_jp(const SolveParams& P, int g, bool first, float beta, cons
       if (rk < 0) continue;
       const float4 geo = __ldcg(P.mem_geo + slot);
       float pl[12];
-      load_p(P, rk, __ldg(P.mem_node + slot), first, beta, pold, pl);
+      load_p(P, rk, P.NA ? __ldg(P.mem_agg + slot) : 0, first, beta, pold, pl);
 #pragma unroll
       for (int c = 0; c < 3; ++c)
         u[c] = fmaf(geo.x, fmaf(geo.y, pl[c], fmaf(geo.z, pl[3 + c], fmaf(geo.w, pl[6 + c], pl[9 + c]))), u[c]);
@@ -231,7 +228,7 @@ __device__ void residual_node(const SolveParams& P, int r, RT scale, RT (&acc)[1
   const int b0 = __ldg(P.item_off + r), b1 = __ldg(P.item_off + r + 1);
   for (int it = b0 + lane; it < b1; it += 32) {
     const int4 m = __ldg(P.items + it);
-    if (m.x == ITEM_OUT) {
+    if ((m.x & 15) == ITEM_OUT) {
       // f = w s (R_j d + g_j + t_j - g_k - t_k), d = g_k - g_j (Deform.cpp:421-449)
       const float s = __int_as_float(m.w);
       const RT ws = w * RT(s);
@@ -260,7 +257,7 @@ __device__ void residual_node(const SolveParams& P, int r, RT scale, RT (&acc)[1
         const float wsf = wgf * s;
         q_add(Q, wsf * dJ[0], wsf * dJ[1], wsf * dJ[2], wgf);
       }
-    } else if (m.x == ITEM_STATIC) {
+    } else if ((m.x & 15) == ITEM_STATIC) {
       // f = -w t_j (Deform.cpp:458-482)
       RT f[3] = {-w * xj[9], -w * xj[10], -w * xj[11]};
       e += double(f[0]) * double(f[0]) + double(f[1]) * double(f[1]) + double(f[2]) * double(f[2]);
@@ -270,7 +267,7 @@ __device__ void residual_node(const SolveParams& P, int r, RT scale, RT (&acc)[1
         Q[9] += (float)(P.wg * P.wg);
       }
     } else if (PASS == PASS_GRAD) {
-      if (m.x == ITEM_IN) {
+      if ((m.x & 15) == ITEM_IN) {
         const float s = __int_as_float(m.w);
         const RT ws = w * RT(s);
         RT gi[3], xi[12];
@@ -301,7 +298,7 @@ __device__ void residual_node(const SolveParams& P, int r, RT scale, RT (&acc)[1
         bool first_of_run = true;
         if (it > b0) {
           const int4 pm = __ldg(P.items + it - 1);
-          first_of_run = !(pm.x == ITEM_CON && pm.z == g);
+          first_of_run = !((pm.x & 15) == ITEM_CON && pm.z == g);
         }
         if (first_of_run) {
           float ev[3] = {0.f, 0.f, 0.f}, al = 0.f;
@@ -366,20 +363,20 @@ __device__ void spmv_node(const SolveParams& P, int r, bool first, float beta, c
   const int j = __ldg(P.free_ids + r);
   const float gj[3] = {__ldg(P.node_pos + 3 * (size_t)j), __ldg(P.node_pos + 3 * (size_t)j + 1),
                        __ldg(P.node_pos + 3 * (size_t)j + 2)};
-  load_p(P, r, j, first, beta, pold, pj);
+  load_p(P, r, P.NA ? __ldg(P.agg + r) : 0, first, beta, pold, pj);
 #pragma unroll
   for (int i = 0; i < 12; ++i) acc[i] = 0.f;
   const float w = (float)P.wg;
   const int b0 = __ldg(P.item_off + r), b1 = __ldg(P.item_off + r + 1);
   for (int it = b0 + lane; it < b1; it += 32) {
     const int4 m = __ldg(P.items + it);
-    if (m.x == ITEM_OUT) {
+    if ((m.x & 15) == ITEM_OUT) {
       const float ws = w * __int_as_float(m.w);
       const float d[3] = {__ldg(P.node_pos + 3 * (size_t)m.z) - gj[0],
                           __ldg(P.node_pos + 3 * (size_t)m.z + 1) - gj[1],
                           __ldg(P.node_pos + 3 * (size_t)m.z + 2) - gj[2]};
       float pk[3] = {0.f, 0.f, 0.f};
-      if (m.y >= 0) load_pt(P, m.y, m.z, first, beta, pold, pk);
+      if (m.y >= 0) load_pt(P, m.y, m.x >> 4, first, beta, pold, pk);
 #pragma unroll
       for (int c = 0; c < 3; ++c) {
         const float u = ws * fmaf(pj[c], d[0], fmaf(pj[3 + c], d[1], pj[6 + c] * d[2])) + w * pj[9 + c] - ws * pk[c];
@@ -388,19 +385,19 @@ __device__ void spmv_node(const SolveParams& P, int r, bool first, float beta, c
         acc[6 + c] = fmaf(ws * d[2], u, acc[6 + c]);
         acc[9 + c] = fmaf(w, u, acc[9 + c]);
       }
-    } else if (m.x == ITEM_IN) {
+    } else if ((m.x & 15) == ITEM_IN) {
       const float ws = w * __int_as_float(m.w);
       const float d[3] = {gj[0] - __ldg(P.node_pos + 3 * (size_t)m.z),
                           gj[1] - __ldg(P.node_pos + 3 * (size_t)m.z + 1),
                           gj[2] - __ldg(P.node_pos + 3 * (size_t)m.z + 2)};
       float pi[12];
-      load_p(P, m.y, m.z, first, beta, pold, pi);
+      load_p(P, m.y, m.x >> 4, first, beta, pold, pi);
 #pragma unroll
       for (int c = 0; c < 3; ++c) {
         const float u = ws * fmaf(pi[c], d[0], fmaf(pi[3 + c], d[1], pi[6 + c] * d[2])) + w * pi[9 + c] - ws * pj[9 + c];
         acc[9 + c] = fmaf(-ws, u, acc[9 + c]);
       }
-    } else if (m.x == ITEM_STATIC) {
+    } else if ((m.x & 15) == ITEM_STATIC) {
 #pragma unroll
       for (int c = 0; c < 3; ++c) acc[9 + c] = fmaf(w * w, pj[9 + c], acc[9 + c]);
     } else {
@@ -605,7 +602,7 @@ __device__ void coarse_rows_node(const SolveParams& P, int r) {
   const int b0 = __ldg(P.item_off + r), b1 = __ldg(P.item_off + r + 1);
   for (int it = b0 + lane; it < b1; it += 32) {
     const int4 m = __ldg(P.items + it);
-    if (m.x == ITEM_OUT) {
+    if ((m.x & 15) == ITEM_OUT) {
       const float ws = w * __int_as_float(m.w);
       const float d[3] = {__ldg(P.node_pos + 3 * (size_t)m.z) - gj[0], __ldg(P.node_pos + 3 * (size_t)m.z + 1) - gj[1],
                           __ldg(P.node_pos + 3 * (size_t)m.z + 2) - gj[2]};
@@ -626,7 +623,7 @@ __device__ void coarse_rows_node(const SolveParams& P, int r) {
       } else {
         coarse_add(P, a, a, va, va);
       }
-    } else if (m.x == ITEM_STATIC) {
+    } else if ((m.x & 15) == ITEM_STATIC) {
       float v[4];
       coarse_vec(P, r, j, 0.f, 0.f, 0.f, -w, v);
       coarse_add(P, a, a, v, v);

@@ -175,6 +175,12 @@ __global__ void __launch_bounds__(kSolveThreads) gn_solve_kernel(SolveParams P) 
   }
   const bool coarse = P.NA > 0 && P.mode == 0;
   if (coarse) {
+    for (int r = gt; r < F; r += nt) {
+      const int j = P.free_ids[r];
+      const int pv = P.pivot[P.agg[r]];
+      P.dpiv[r] = make_float4(P.node_pos[3 * j] - P.node_pos[3 * pv], P.node_pos[3 * j + 1] - P.node_pos[3 * pv + 1],
+                              P.node_pos[3 * j + 2] - P.node_pos[3 * pv + 2], 0.f);
+    }
     for (int e = gt; e < P.NA * P.NA * 16; e += nt) P.Qd[e] = 0.0;
     for (int e = gt; e < 2 * P.NC; e += nt) P.rc[e] = 0.0;
     for (int e = gt; e < 2 * P.NA * 81; e += nt) P.rotagg[e] = 0.0;

@@ -51,6 +51,14 @@ class Grid:
         return (_wrap_i32(off.value, g3 + 1), _wrap_i32(lst.value, self.n_pairs),
                 _wrap_i32(val.value, self.n_valid))
 
+    def center_order(self, pos=None):
+        """Stable cell order of the Gaussian centres (int64 permutation)."""
+        pos = self.pos if pos is None else _f32(pos)
+        out = torch.empty((pos.shape[0],), dtype=torch.int32, device="cuda")
+        check("arap_grid_center_order", _lib.load().arap_grid_center_order(
+            self._h, pos.shape[0], _p(pos), _p(out), _s()))
+        return out.long()
+
     def ada_lpf(self, samples=None, lpf=LPF_PARAMETER):
         samples = self.sample_pos if samples is None else _f32(samples)
         out = torch.empty((self.n_valid, 9), dtype=torch.float32, device="cuda")

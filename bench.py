@@ -39,7 +39,9 @@ def _args():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--scene", default="twist300k")
-    ap.add_argument("--precision", default="mixed", choices=["plain", "mixed"])
+    ap.add_argument("--form", default="chosen", choices=["plain", "chosen"],
+                    help="chosen: FP64 residual/gradient + two-level PCG; plain: FP32 + block-Jacobi PCG")
+    ap.add_argument("--coarse-nodes", type=int, default=64)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-samples", action="store_true")
     return ap.parse_args()
@@ -106,22 +108,37 @@ def _dist():
 
 # ------------------------------------------------------------ workload ----
 
-def build_state(scene_name, precision, with_samples):
+def solve_config(dev, sc, form, coarse_nodes):
+    if form == "chosen":
+        return dev.default_config(max_iters=sc.iters, early_exit=0, precision=1, coarse_nodes=coarse_nodes)
+    return dev.default_config(max_iters=sc.iters, early_exit=0, precision=0, coarse_nodes=0)
+
+
+def build_state(scene_name, form, coarse_nodes, with_samples):
     import numpy as np
     import torch
     dev = importlib.import_module(PKG + ".deform")
     synth = importlib.import_module(PKG + ".synth")
+    grid = importlib.import_module(PKG + ".grid")
     sc = synth.make_scene(scene_name)
+    # the reference reorders the Gaussians by the grid cell of their centre
+    # before binning (GaussianView.cpp:3918-3953); node ids follow
+    g0 = grid.build_grid(torch.as_tensor(sc.pos).cuda(), torch.as_tensor(sc.rot).cuda(),
+                         torch.as_tensor(sc.scale).cuda(), torch.as_tensor(sc.opacity).cuda(), sc.grid_num)
+    order = g0.center_order().cpu().numpy()
+    g0.close()
+    inv = np.empty_like(order)
+    inv[order] = np.arange(order.size)
+    sc.pos, sc.rot, sc.scale, sc.opacity, sc.shs = (a[order] for a in (sc.pos, sc.rot, sc.scale, sc.opacity, sc.shs))
+    sc.node_vertex = inv[sc.node_vertex].astype(np.int32)
     sample_pos = feature = None
     if with_samples:
-        grid = importlib.import_module(PKG + ".grid")
         g = grid.build_grid(torch.as_tensor(sc.pos).cuda(), torch.as_tensor(sc.rot).cuda(),
                             torch.as_tensor(sc.scale).cuda(), torch.as_tensor(sc.opacity).cuda(), sc.grid_num)
         sample_pos = g.sample_pos
         rng = np.random.default_rng(5)
         feature = torch.as_tensor((0.2 * rng.standard_normal((sample_pos.shape[0], 48))).astype(np.float32)).cuda()
-    cfg = dev.default_config(max_iters=sc.iters, early_exit=0,
-                             precision=1 if precision == "mixed" else 0)
+    cfg = solve_config(dev, sc, form, coarse_nodes)
     st = dev.GaussianDeformer(torch.as_tensor(sc.pos), torch.as_tensor(sc.rot), torch.as_tensor(sc.scale),
                               torch.as_tensor(sc.shs), sc.node_vertex, sc.k, sc.blocks, sc.block_type,
                               sample_pos=sample_pos, feature=feature, config=cfg)
@@ -158,7 +175,7 @@ def run_ours(a):
         import torch.distributed as tdist
         tdist.init_process_group("nccl")
     dev = importlib.import_module(PKG + ".deform")
-    sc, st = build_state(a.scene, a.precision, not a.no_samples)
+    sc, st = build_state(a.scene, a.form, a.coarse_nodes, not a.no_samples)
     snap = snapshot(st)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
     s = torch.cuda.current_stream()
@@ -224,6 +241,28 @@ def run_ours(a):
     restore(st, snap)
     stats = st.frame(stats=True)
     torch.cuda.synchronize()
+    # the other form on the same state, same steps
+    other = "plain" if a.form == "chosen" else "chosen"
+    st.solver = dev.Solver(st.neighbors, st.anchor_idx, st.anchor_w, st.blocks, st.block_type,
+                           config=solve_config(dev, sc, other, a.coarse_nodes))
+    st.precision = st.solver.config.precision
+    for _ in range(2):
+        restore(st, snap)
+        st.frame(stats=False)
+    o_ms = []
+    for _ in range(max(2, a.steps // 2)):
+        restore(st, snap)
+        flush.fill_(1.0)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(s)
+        st.frame(stats=False)
+        e1.record(s)
+        torch.cuda.synchronize()
+        o_ms.append(e0.elapsed_time(e1))
+    restore(st, snap)
+    o_stats = st.frame(stats=True)
+    torch.cuda.synchronize()
 
     peak, peak_kind = _peaks()
     k = sc.k
@@ -241,11 +280,11 @@ def run_ours(a):
         "higher_is_better": False,
         "scaling": "weak",
         "vs_baseline": None,
-        "dtype": "f32+f64" if a.precision == "mixed" else "f32",
+        "dtype": "f32+f64" if a.form == "chosen" else "f32",
         "data": "synthetic (seeded two-bars-and-sphere field; reference datasets absent)",
         "config": {"workload": "%s: %d Gaussians, %d^3 grid, %d nodes, k=%d, %d GN iterations, "
-                               "twist 90 deg, precision=%s" % (sc.name, sc.n_gauss, sc.grid_num,
-                                                                sc.n_nodes, k, sc.iters, a.precision),
+                               "twist 90 deg, form=%s" % (sc.name, sc.n_gauss, sc.grid_num,
+                                                           sc.n_nodes, k, sc.iters, a.form),
                    "samples": int(st.sample_pos.shape[0]) if st.sample_pos is not None else 0,
                    "l2": "flushed between steps (256 MB write)",
                    "state": "restored to the rest pose inside each step",
@@ -258,6 +297,11 @@ def run_ours(a):
         "gpu_launches": launches_per_step * a.steps,
         "solve": {"pcg_iterations": stats["pcg_iterations"], "gn_iterations": stats["gn_iterations"],
                   "final_energy": stats["final_energy"]},
+        "forms": {a.form: {"ms_per_frame": round(ms_step, 3), "pcg_iterations": stats["pcg_iterations"]},
+                  other: {"ms_per_frame": round(float(np.mean(o_ms)), 3),
+                          "pcg_iterations": o_stats["pcg_iterations"]},
+                  "chosen_speedup_over_plain": round((float(np.mean(o_ms)) / ms_step) if a.form == "chosen"
+                                                     else (ms_step / float(np.mean(o_ms))), 3)},
         "status": status,
         "clocks": clk.summary(),
     }

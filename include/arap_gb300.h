@@ -141,8 +141,10 @@ void arap_solver_destroy(arap_solver* s);
 /* ------------------------------------------------------------ skinning --- */
 
 /* Per-node transform table used by every skinning call: for node j
- * [R row-major 9 | g 3 | t+g 3 | 0] (16 floats).  Built from the solve
- * output and the node positions the solve used. */
+ * [R - I row-major 9 | g 3 | t 3 | 0] (16 floats).  Built from the solve
+ * output and the node positions the solve used.  Blends evaluate
+ * p' = p + [(sum w - 1) p + sum w ((R - I)(p - g) + t)], algebraically
+ * DeformGraph::predict_mesh (Deform.hpp:230-249), rounded once. */
 int arap_node_table(int n, const float* rot, const float* trans, const float* node_pos,
                     float* table_out, arap_stream_t stream);
 
@@ -254,6 +256,14 @@ int arap_grid_build(arap_grid** out, int N, const float* pos, const float* rot, 
  * [n_pairs] (grided_gs_idx), valid_cells [n_valid] ascending (valid_grid_idx). */
 int arap_grid_arrays(const arap_grid* grid, const int32_t** cell_offsets, const int32_t** cell_lists,
                      const int32_t** valid_cells);
+
+/* Stable order of N Gaussians by the grid cell of their centre (cell index
+ * x*g^2 + y*g + z ascending, original order within a cell): the reorder the
+ * reference applies before binning (GaussianView.cpp:3918-3953).  order_out
+ * [N]: order_out[r] = original index of the Gaussian placed at rank r.
+ * Synchronises. */
+int arap_grid_center_order(const arap_grid* grid, int N, const float* pos, int32_t* order_out,
+                           arap_stream_t stream);
 
 /* 64 samples per occupied cell, cell-major, sample s at
  * min + cell*step + (0.5 + (s/16, s/4%4, s%4)) * interval

@@ -108,11 +108,12 @@ def grid_samples(off, mn, step, grid_num):
     out = np.empty((valid.size, 64, 3), F32)
     half = 0.5 * np.float64(interval)
     for d, ci in enumerate((x, y, z)):
-        base = (mn[d] + (ci * step).astype(F32)).astype(F32)
+        # float32 products and sums (int * float is float in the reference)
+        base = (mn[d] + (ci.astype(F32) * F32(step)).astype(F32)).astype(F32)
         base = (base.astype(np.float64) + half).astype(F32)
         for s in range(64):
             si = (s // 16, (s % 16) // 4, s % 4)[d]
-            out[:, s, d] = (base + F32(si) * interval).astype(F32)
+            out[:, s, d] = (base + (F32(si) * interval).astype(F32)).astype(F32)
     return valid, out.reshape(-1, 3)
 
 

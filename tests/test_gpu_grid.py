@@ -90,3 +90,13 @@ def test_grid_density(gridmod):
     ada = G.ada_lpf()
     sig2, _ = G.density(_t(sc.shs), ada=ada)
     np.testing.assert_allclose(sig2.cpu().numpy(), sig, rtol=1e-4, atol=1e-6 * scale_s)
+
+
+def test_grid_center_order(gridmod, scene):
+    from oracle import grid as og
+    G = gridmod.build_grid(_t(scene.pos), _t(scene.rot), _t(scene.scale), _t(scene.opacity), scene.grid_num)
+    order = G.center_order().cpu().numpy()
+    mn = np.array(G.min_xyz, np.float32)
+    cell, new_index = og.center_cells(scene.pos, mn, np.float32(G.step), scene.grid_num)
+    ref = np.argsort(cell, kind="stable")
+    assert np.array_equal(order, ref)
