@@ -287,6 +287,186 @@ __global__ void __launch_bounds__(kSkinThreads)
   }
 }
 
+// Adjoint of the Gaussian skinning map: given dL/dmu [N*3] and dL/dSigma
+// [N*6] (packed xx,xy,xz,yy,yz,zz; dL = sum_p g_p dSigma_p), accumulate dL/d
+// (R_j, t_j) into grad_node [n*12] ([dR column-major 9 | dt 3]).  Each thread
+// recomputes its Gaussian's blended endpoints and polar factor from the
+// pre-frame endpoints (nothing is stored by the forward), then
+//   Sigma = R D R^T, D_a = (c_a K_a)^2, K_a = (R^T M)_aa, c_a = s0_a/((s0_a+1e-3)*2)
+//   dL/dR += 2 G R D,  dL/dK_a = (R^T G R)_aa 2 c_a^2 K_a,
+//   dL/dM += R diag(dL/dK) ; dL/dR += M diag(dL/dK),
+//   polar: A = R^T dL/dR, w = (tr S I - S)^-1 skew(A), dL/dM += 2 R [w]x,
+//   M_a = (P_2a - P_2a+1)/2, mu = mean P, P_e = sum_j w_ej (R_j (p_e - g_j) + g_j + t_j).
+// Node gradients are summed per CTA in a shared-memory hash table of node ids
+// and flushed with one global atomic per (node, component).
+constexpr int kHashSlots = 512;
+
+__device__ __forceinline__ void hash_add(int* keys, float (*vals)[12], int nid, const float (&v)[12],
+                                         float* __restrict__ grad_node) {
+  unsigned h = ((unsigned)nid * 2654435761u) & (kHashSlots - 1);
+  for (int probe = 0; probe < kHashSlots; ++probe) {
+    const int k = atomicCAS(keys + h, -1, nid);
+    if (k == -1 || k == nid) {
+#pragma unroll
+      for (int c = 0; c < 12; ++c) atomicAdd(&vals[h][c], v[c]);
+      return;
+    }
+    h = (h + 1) & (kHashSlots - 1);
+  }
+#pragma unroll
+  for (int c = 0; c < 12; ++c) atomicAdd(grad_node + 12 * (size_t)nid + c, v[c]);
+}
+
+template <int K>
+__global__ void __launch_bounds__(kSkinThreads)
+    skin_gaussians_backward_kernel(int N, const float* __restrict__ ends_in, const int32_t* __restrict__ eidx,
+                                   const float* __restrict__ ew, const float* __restrict__ table,
+                                   const float* __restrict__ scale0, const uint8_t* __restrict__ static_mask,
+                                   const float* __restrict__ grad_pos, const float* __restrict__ grad_cov,
+                                   float* __restrict__ grad_node) {
+  __shared__ int s_keys[kHashSlots];
+  __shared__ float s_vals[kHashSlots][12];
+  for (int q = threadIdx.x; q < kHashSlots; q += blockDim.x) {
+    s_keys[q] = -1;
+#pragma unroll
+    for (int c = 0; c < 12; ++c) s_vals[q][c] = 0.f;
+  }
+  __syncthreads();
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < N && !(static_mask && static_mask[i])) {
+    float p0[18], e[18];
+#pragma unroll
+    for (int c = 0; c < 18; ++c) p0[c] = __ldg(ends_in + (size_t)c * N + i);
+#pragma unroll
+    for (int ep = 0; ep < 6; ++ep) {
+      float ox = 0.f, oy = 0.f, oz = 0.f, ws = 0.f;
+#pragma unroll
+      for (int j = 0; j < K; ++j) {
+        const size_t o = (size_t)(j * 6 + ep) * N + i;
+        const NodeXf x = load_node(table, __ldg(eidx + o));
+        const float w = __ldg(ew + o);
+        ws += w;
+        ed_term(x, w, p0[3 * ep], p0[3 * ep + 1], p0[3 * ep + 2], ox, oy, oz);
+      }
+      e[3 * ep] = ed_finish(p0[3 * ep], ws, ox);
+      e[3 * ep + 1] = ed_finish(p0[3 * ep + 1], ws, oy);
+      e[3 * ep + 2] = ed_finish(p0[3 * ep + 2], ws, oz);
+    }
+    float M[9];
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+      for (int r = 0; r < 3; ++r) M[r * 3 + a] = 0.5f * (e[3 * (2 * a) + r] - e[3 * (2 * a + 1) + r]);
+    float R[9];
+    if (!polar_factor<float>(M, R, 20, 2e-7f)) raise_status(ARAP_ENONFINITE);
+    float S[9];  // R^T M, symmetrised
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+      for (int b = 0; b < 3; ++b) S[a * 3 + b] = R[a] * M[b] + R[3 + a] * M[3 + b] + R[6 + a] * M[6 + b];
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+      for (int b = a + 1; b < 3; ++b) S[a * 3 + b] = S[b * 3 + a] = 0.5f * (S[a * 3 + b] + S[b * 3 + a]);
+    float cK[3], D[3], Kd[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      const float s0 = scale0[3 * (size_t)i + a];
+      cK[a] = s0 / ((s0 + 1e-3f) * 2.0f);
+      Kd[a] = R[a] * M[a] + R[3 + a] * M[3 + a] + R[6 + a] * M[6 + a];
+      D[a] = (cK[a] * Kd[a]) * (cK[a] * Kd[a]);
+    }
+    const float* gc = grad_cov + 6 * (size_t)i;
+    const float G[9] = {gc[0], 0.5f * gc[1], 0.5f * gc[2], 0.5f * gc[1], gc[3], 0.5f * gc[4],
+                        0.5f * gc[2], 0.5f * gc[4], gc[5]};
+    float GR[9];  // G R
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+#pragma unroll
+      for (int a = 0; a < 3; ++a) GR[r * 3 + a] = G[r * 3] * R[a] + G[r * 3 + 1] * R[3 + a] + G[r * 3 + 2] * R[6 + a];
+    float gK[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      const float gD = R[a] * GR[a] + R[3 + a] * GR[3 + a] + R[6 + a] * GR[6 + a];
+      gK[a] = gD * 2.f * cK[a] * cK[a] * Kd[a];
+    }
+    float gR[9], gM[9];
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+#pragma unroll
+      for (int a = 0; a < 3; ++a) {
+        gR[r * 3 + a] = 2.f * GR[r * 3 + a] * D[a] + M[r * 3 + a] * gK[a];
+        gM[r * 3 + a] = R[r * 3 + a] * gK[a];
+      }
+    float A[9];  // R^T gR
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+      for (int b = 0; b < 3; ++b) A[a * 3 + b] = R[a] * gR[b] + R[3 + a] * gR[3 + b] + R[6 + a] * gR[6 + b];
+    const float av[3] = {0.5f * (A[7] - A[5]), 0.5f * (A[2] - A[6]), 0.5f * (A[3] - A[1])};
+    const float tr = S[0] + S[4] + S[8];
+    float T[9], Ti[9];
+#pragma unroll
+    for (int q = 0; q < 9; ++q) T[q] = -S[q];
+    T[0] += tr;
+    T[4] += tr;
+    T[8] += tr;
+    float om[3] = {0.f, 0.f, 0.f};
+    if (inv_transpose3(T, Ti)) {  // T symmetric: inverse-transpose = inverse
+#pragma unroll
+      for (int r = 0; r < 3; ++r) om[r] = Ti[r * 3] * av[0] + Ti[r * 3 + 1] * av[1] + Ti[r * 3 + 2] * av[2];
+    }
+    const float Y[9] = {0.f, -om[2], om[1], om[2], 0.f, -om[0], -om[1], om[0], 0.f};
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+#pragma unroll
+      for (int a = 0; a < 3; ++a)
+        gM[r * 3 + a] += 2.f * (R[r * 3] * Y[a] + R[r * 3 + 1] * Y[3 + a] + R[r * 3 + 2] * Y[6 + a]);
+    float gP[18];
+    const float gm[3] = {grad_pos[3 * (size_t)i] * (1.f / 6.f), grad_pos[3 * (size_t)i + 1] * (1.f / 6.f),
+                         grad_pos[3 * (size_t)i + 2] * (1.f / 6.f)};
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+      for (int r = 0; r < 3; ++r) {
+        gP[3 * (2 * a) + r] = gm[r] + 0.5f * gM[r * 3 + a];
+        gP[3 * (2 * a + 1) + r] = gm[r] - 0.5f * gM[r * 3 + a];
+      }
+#pragma unroll 1
+    for (int ep = 0; ep < 6; ++ep) {
+      float gpe[3], pe[3];
+#pragma unroll
+      for (int r = 0; r < 3; ++r) {
+        gpe[r] = gP[3 * ep + r];
+        pe[r] = p0[3 * ep + r];
+      }
+#pragma unroll 2
+      for (int j = 0; j < K; ++j) {
+        const size_t o = (size_t)(j * 6 + ep) * N + i;
+        const int nid = __ldg(eidx + o);
+        const float w = __ldg(ew + o);
+        const float4 gg = __ldg(reinterpret_cast<const float4*>(table) + 4 * (size_t)nid + 2);
+        const float d[3] = {pe[0] - gg.y, pe[1] - gg.z, pe[2] - gg.w};
+        float v[12];
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
+#pragma unroll
+          for (int r = 0; r < 3; ++r) v[3 * c + r] = w * gpe[r] * d[c];
+#pragma unroll
+        for (int r = 0; r < 3; ++r) v[9 + r] = w * gpe[r];
+        hash_add(s_keys, s_vals, nid, v, grad_node);
+      }
+    }
+  }
+  __syncthreads();
+  for (int q = threadIdx.x; q < kHashSlots; q += blockDim.x) {
+    const int nid = s_keys[q];
+    if (nid < 0) continue;
+#pragma unroll
+    for (int c = 0; c < 12; ++c) atomicAdd(grad_node + 12 * (size_t)nid + c, s_vals[q][c]);
+  }
+}
+
 // Per-node quaternion of the polar factor (GaussianView.cpp:3172-3181).
 template <bool MIXED>
 __global__ void node_quat_kernel(int n, const float* __restrict__ rot, float* __restrict__ quat) {
@@ -577,6 +757,33 @@ extern "C" int arap_skin_gaussians(int N, int k, float* ends, const int32_t* end
     ARAP_SKG(1) ARAP_SKG(2) ARAP_SKG(3) ARAP_SKG(4) ARAP_SKG(5) ARAP_SKG(6)
     ARAP_SKG(7) ARAP_SKG(8) ARAP_SKG(9) ARAP_SKG(10) ARAP_SKG(11) ARAP_SKG(12)
 #undef ARAP_SKG
+    default:
+      return ARAP_EUNSUPPORTED;
+  }
+  ARAP_LAUNCH_CHECK();
+  return ARAP_OK;
+}
+
+extern "C" int arap_skin_gaussians_backward(int N, int k, const float* ends_in, const int32_t* ends_idx,
+                                            const float* ends_w, const float* node_table, const float* scale0,
+                                            const uint8_t* static_mask, const float* grad_pos,
+                                            const float* grad_cov, float* grad_node, arap_stream_t stream) {
+  if (N == 0) return ARAP_OK;
+  if (N < 0 || !ends_in || !ends_idx || !ends_w || !node_table || !scale0 || !grad_pos || !grad_cov || !grad_node)
+    return ARAP_EBADINPUT;
+  if (reinterpret_cast<uintptr_t>(node_table) & 15) return ARAP_EBADINPUT;
+  cudaStream_t s = (cudaStream_t)stream;
+  const int grid = grid_for(N, kSkinThreads);
+  switch (k) {
+#define ARAP_SKB(K)                                                                                         \
+  case K:                                                                                                   \
+    skin_gaussians_backward_kernel<K><<<grid, kSkinThreads, 0, s>>>(N, ends_in, ends_idx, ends_w, node_table, \
+                                                                    scale0, static_mask, grad_pos, grad_cov, \
+                                                                    grad_node);                              \
+    break;
+    ARAP_SKB(1) ARAP_SKB(2) ARAP_SKB(3) ARAP_SKB(4) ARAP_SKB(5) ARAP_SKB(6)
+    ARAP_SKB(7) ARAP_SKB(8) ARAP_SKB(9) ARAP_SKB(10) ARAP_SKB(11) ARAP_SKB(12)
+#undef ARAP_SKB
     default:
       return ARAP_EUNSUPPORTED;
   }

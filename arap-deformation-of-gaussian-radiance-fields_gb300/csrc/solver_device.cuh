@@ -9,7 +9,7 @@
 
 namespace arap {
 
-constexpr int kSolveThreads = 256;
+constexpr int kSolveThreads = 512;
 constexpr int kSolveWarps = kSolveThreads / 32;
 
 // Mutable per-node vectors are read through L2 (ld.global.cg): other CTAs
@@ -356,19 +356,25 @@ __device__ void residual_node(const SolveParams& P, int r, RT scale, RT (&acc)[1
   energy = warp_sum(e);
 }
 
-// q = (J^T J p)_r for free node r; also returns this node's p (all lanes).
-__device__ void spmv_node(const SolveParams& P, int r, bool first, float beta, const float* pold,
+// q = (J^T J p)_r for free node r, computed by one half-warp (16 lanes); also
+// returns this node's p in every lane of the half.  A half with valid == false
+// does no loads but takes part in the warp shuffles.
+__device__ void spmv_node(const SolveParams& P, int r, bool valid, bool first, float beta, const float* pold,
                           float (&acc)[12], float (&pj)[12]) {
-  const int lane = threadIdx.x & 31;
+  const int lane = threadIdx.x & 15;
+#pragma unroll
+  for (int i = 0; i < 12; ++i) {
+    acc[i] = 0.f;
+    pj[i] = 0.f;
+  }
+  if (valid) {
   const int j = __ldg(P.free_ids + r);
   const float gj[3] = {__ldg(P.node_pos + 3 * (size_t)j), __ldg(P.node_pos + 3 * (size_t)j + 1),
                        __ldg(P.node_pos + 3 * (size_t)j + 2)};
   load_p(P, r, P.NA ? __ldg(P.agg + r) : 0, first, beta, pold, pj);
-#pragma unroll
-  for (int i = 0; i < 12; ++i) acc[i] = 0.f;
   const float w = (float)P.wg;
   const int b0 = __ldg(P.item_off + r), b1 = __ldg(P.item_off + r + 1);
-  for (int it = b0 + lane; it < b1; it += 32) {
+  for (int it = b0 + lane; it < b1; it += 16) {
     const int4 m = __ldg(P.items + it);
     if ((m.x & 15) == ITEM_OUT) {
       const float ws = w * __int_as_float(m.w);
@@ -441,8 +447,12 @@ __device__ void spmv_node(const SolveParams& P, int r, bool first, float beta, c
       acc[6 + i] += wr * (u1 * c0[i] + u2 * c1[i] + 2.f * u5 * c2[i]);
     }
   }
+  }
 #pragma unroll
-  for (int i = 0; i < 12; ++i) acc[i] = warp_sum(acc[i]);
+  for (int i = 0; i < 12; ++i) {
+#pragma unroll
+    for (int o = 8; o > 0; o >>= 1) acc[i] += __shfl_xor_sync(0xffffffffu, acc[i], o);
+  }
 }
 
 // Diagonal 12x12 block of J^T J for free node r from Q and the rotation
@@ -549,6 +559,20 @@ __device__ void build_dinv(const SolveParams& P, int r, const float (&Q)[10], fl
     for (int i = 0; i < 12; ++i) out[i] = xs[i];
   }
   __syncwarp();
+}
+
+// Half-warp form: lane c < 12 of each 16-lane half holds r_c of its node rr.
+__device__ __forceinline__ float apply_dinv_h(const SolveParams& P, int rr, bool valid, float rc) {
+  const int lane = threadIdx.x & 31;
+  const int l16 = lane & 15, base = lane & 16;
+  float zc = 0.f;
+  const float* row = P.dinv + 144 * (size_t)(valid ? rr : 0) + 12 * (l16 < 12 ? l16 : 0);
+#pragma unroll
+  for (int i = 0; i < 12; ++i) {
+    const float ri = __shfl_sync(0xffffffffu, rc, base + i);
+    if (valid) zc = fmaf(__ldcg(row + i), ri, zc);
+  }
+  return (valid && l16 < 12) ? zc : 0.f;
 }
 
 // z = Dinv r for free node rr; lane c < 12 holds r_c and returns z_c.
@@ -732,6 +756,24 @@ __device__ __forceinline__ float coarse_entry_x(const SolveParams& P, const doub
   double v = (rI == rJ) ? P.Qd[((size_t)a * P.NA + b) * 16 + 4 * pI + pJ] : 0.0;
   if (a == b && iI < 9 && iJ < 9) v += __ldcg(rotagg + 81 * (size_t)a + 9 * iI + iJ);
   return (float)v;
+}
+
+// Half-warp form of coarse_restrict.
+__device__ __forceinline__ void coarse_restrict_h(const SolveParams& P, int rr, bool valid, float rc_lane,
+                                                  double* rc) {
+  const int lane = threadIdx.x & 31;
+  const int l16 = lane & 15, base = lane & 16;
+  const int c = l16 < 9 ? l16 / 3 : 0, r = l16 < 9 ? l16 % 3 : 0;
+  const float rt = __shfl_sync(0xffffffffu, rc_lane, base + 9 + r);
+  if (valid && l16 < 12) {
+    const int a = __ldg(P.agg + rr);
+    float v = rc_lane;
+    if (l16 < 9) {
+      const float4 dp = __ldcg(P.dpiv + rr);
+      v += (c == 0 ? dp.x : (c == 1 ? dp.y : dp.z)) * rt;
+    }
+    atomicAdd(rc + 12 * a + l16, (double)v);
+  }
 }
 
 // Restriction of free node rr's residual (lane c < 12 holds r_c) into rc:

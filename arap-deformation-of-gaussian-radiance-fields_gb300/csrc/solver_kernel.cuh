@@ -283,24 +283,28 @@ __global__ void __launch_bounds__(kSolveThreads) gn_solve_kernel(SolveParams P) 
     const double tol2 = (double)P.pcg_tol * (double)P.pcg_tol * rr0;
     float beta = 0.f;
     int pi = 0;
+    const int half = lane >> 4, l16 = lane & 15;
+    const int nhw = 2 * nw;
     while (rr > tol2 && pi < P.pcg_max && rz > 0.0) {
       const bool first = pi == 0;
       float* pcur = (pi & 1) ? P.p1 : P.p0;
       const float* pold = (pi & 1) ? P.p0 : P.p1;
       double pq[1] = {0.0}, opq[1];
-      for (int oi = gw; oi < F; oi += nw) {
-        const int r = __ldg(P.order + oi);
+      for (int base = 2 * gw; base < F; base += nhw) {
+        const int oi = base + half;
+        const bool valid = oi < F;
+        const int r = valid ? __ldg(P.order + oi) : 0;
         float acc[12], pj[12];
-        spmv_node(P, r, first, beta, pold, acc, pj);
-        if (lane < 12) {
+        spmv_node(P, r, valid, first, beta, pold, acc, pj);
+        if (valid && l16 < 12) {
           float pc = 0.f, qc = 0.f;
 #pragma unroll
           for (int i = 0; i < 12; ++i)
-            if (i == lane) {
+            if (i == l16) {
               pc = pj[i];
               qc = acc[i];
             }
-          const size_t o = 12 * (size_t)r + lane;
+          const size_t o = 12 * (size_t)r + l16;
           pcur[o] = pc;
           P.q[o] = qc;
           pq[0] += (double)pc * (double)qc;
@@ -311,19 +315,21 @@ __global__ void __launch_bounds__(kSolveThreads) gn_solve_kernel(SolveParams P) 
       const float alpha = (float)(rz / opq[0]);
       double* rc_next = P.rc + ((pi + 1) & 1) * P.NC;
       double rzr[2] = {0.0, 0.0}, orz[2];
-      for (int oi = gw; oi < F; oi += nw) {
-        const int r = __ldg(P.order + oi);
+      for (int base = 2 * gw; base < F; base += nhw) {
+        const int oi = base + half;
+        const bool valid = oi < F;
+        const int r = valid ? __ldg(P.order + oi) : 0;
         float rc = 0.f;
-        if (lane < 12) {
-          const size_t o = 12 * (size_t)r + lane;
+        if (valid && l16 < 12) {
+          const size_t o = 12 * (size_t)r + l16;
           P.h[o] = fmaf(alpha, __ldcg(pcur + o), __ldcg(P.h + o));
           rc = fmaf(-alpha, __ldcg(P.q + o), __ldcg(P.r + o));
           P.r[o] = rc;
         }
-        const float zc = apply_dinv(P, r, rc);
-        if (coarse) coarse_restrict(P, r, rc, rc_next);
-        if (lane < 12) {
-          P.z[12 * (size_t)r + lane] = zc;
+        const float zc = apply_dinv_h(P, r, valid, rc);
+        if (coarse) coarse_restrict_h(P, r, valid, rc, rc_next);
+        if (valid && l16 < 12) {
+          P.z[12 * (size_t)r + l16] = zc;
           rzr[0] += (double)rc * (double)zc;
           rzr[1] += (double)rc * (double)rc;
         }

@@ -26,7 +26,7 @@ from . import _lib
 from ._lib import ArapError, SolveConfig, SolveStats, check  # noqa: F401
 
 __all__ = ["build_graph", "compute_weights", "Solver", "node_table", "end_points",
-           "skin_gaussians", "node_quaternions", "skin_samples", "update_nodes",
+           "skin_gaussians", "skin_gaussians_backward", "node_quaternions", "skin_samples", "update_nodes",
            "static_mask", "aims_translate", "aims_twist", "aims_scale", "device_status",
            "default_config", "GaussianDeformer"]
 
@@ -204,6 +204,20 @@ def skin_gaussians(ends, ends_idx, ends_w, table, scale0, pos_out, rot_inout, sc
     check("arap_skin_gaussians", _lib_().arap_skin_gaussians(
         N, k, _p(ends), _p(ends_idx), _p(ends_w), _p(table), _p(scale0), _p(static), _p(pos_out),
         _p(rot_inout), _p(scale_out), _p(shs), _p(cov_out), int(precision), _s()))
+
+
+def skin_gaussians_backward(ends_in, ends_idx, ends_w, table, scale0, grad_pos, grad_cov, n, static=None,
+                            grad_node=None):
+    """Adjoint of skin_gaussians' (mu, Sigma) w.r.t. the node transforms:
+    returns grad_node [n,12] ([dR column-major 9 | dt 3])."""
+    N = grad_pos.shape[0]
+    k = ends_idx.shape[0]
+    if grad_node is None:
+        grad_node = torch.zeros((n, 12), dtype=torch.float32, device="cuda")
+    check("arap_skin_gaussians_backward", _lib_().arap_skin_gaussians_backward(
+        N, k, _p(ends_in), _p(ends_idx), _p(ends_w), _p(table), _p(scale0), _p(static), _p(grad_pos),
+        _p(grad_cov), _p(grad_node), _s()))
+    return grad_node
 
 
 def node_quaternions(rot, precision=_lib.PRECISION_PLAIN):

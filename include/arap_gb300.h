@@ -179,6 +179,19 @@ int arap_skin_gaussians(int N, int k, float* ends, const int32_t* ends_idx,
                         float* scale_out, float* shs_inout, float* cov_out, int precision,
                         arap_stream_t stream);
 
+/* Adjoint of arap_skin_gaussians' mu and Sigma with respect to the node
+ * transforms: given the upstream gradients grad_pos [N*3] and grad_cov [N*6]
+ * (packed xx,xy,xz,yy,yz,zz, dL = sum_p grad_cov_p dSigma_p), ADDS dL/dR_j and
+ * dL/dt_j into grad_node [n*12] ([dR column-major 9 | dt 3] per node; zero it
+ * first).  ends_in are the endpoints the forward started from (before it
+ * deformed them in place); node_table is the forward's table.  The blend and the
+ * per-Gaussian polar factor are recomputed, not stored.  No reference
+ * counterpart: the reference has no gradient of its skinning. */
+int arap_skin_gaussians_backward(int N, int k, const float* ends_in, const int32_t* ends_idx,
+                                 const float* ends_w, const float* node_table, const float* scale0,
+                                 const uint8_t* static_mask, const float* grad_pos, const float* grad_cov,
+                                 float* grad_node, arap_stream_t stream);
+
 /* Per-node unit quaternion of the Newton polar factor of R
  * (FastUpdateSamplesSH, GaussianView.cpp:3172-3181; FastgetOthogonalMatrix
  * helper.cpp:506-517).  quat_out [n*4] (w,x,y,z). */

@@ -394,17 +394,21 @@ def put_free_inputs(pr: EDProblem, x: np.ndarray):
 
 
 def ed_blend(points: np.ndarray, idx: np.ndarray, w: np.ndarray, rot: np.ndarray,
-             trans: np.ndarray, node_pos: np.ndarray) -> np.ndarray:
-    """predict_mesh (Deform.hpp:230-249): float32 output accumulating
-    w_j (R_j (p - g_j) + t_j + g_j) evaluated in float64."""
+             trans: np.ndarray, node_pos: np.ndarray, float_accumulate: bool = True) -> np.ndarray:
+    """predict_mesh (Deform.hpp:230-249): w_j (R_j (p - g_j) + t_j + g_j)
+    evaluated in float64.  With ``float_accumulate`` the sum is rounded to
+    float32 after every neighbour, as the reference's float ``output(c) +=``
+    does; without it the float64 sum is rounded once (the exact blend)."""
     p = np.asarray(points, F32)
     g = np.asarray(node_pos, F32)
-    out = np.zeros(p.shape, F32)
+    out = np.zeros(p.shape, F64)
     for j in range(idx.shape[1]):
         nj = idx[:, j]
         temp = (p - g[nj]).astype(F64)               # float32 difference
         R = rot[nj]
         moved = (R[:, 0:3] * temp[:, 0:1] + R[:, 3:6] * temp[:, 1:2]
                  + R[:, 6:9] * temp[:, 2:3]) + trans[nj] + g[nj].astype(F64)
-        out = (out.astype(F64) + w[:, j:j + 1] * moved).astype(F32)
-    return out
+        out = out + w[:, j:j + 1] * moved
+        if float_accumulate:
+            out = out.astype(F32).astype(F64)
+    return out.astype(F32)

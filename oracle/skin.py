@@ -262,13 +262,13 @@ def covariance6(rot, scale):
 
 
 def skin_gaussians(ends, ends_idx, ends_w, rot_node, trans_node, node_pos,
-                   rot_old, scale0, shs, static=None):
+                   rot_old, scale0, shs, static=None, float_accumulate=True):
     """One frame of Gaussian skinning: ED blend of the 6 endpoints
     (GaussianView.cpp:3022-3040) then the refit.  ``ends_idx``/``ends_w`` are
     [N*6,k] in endpoint order.  Returns (ends_new, pos, rot, scale, shs)."""
     N = ends.shape[0]
     e_new = _ed.ed_blend(ends.reshape(-1, 3), ends_idx, ends_w, rot_node,
-                         trans_node, node_pos).reshape(N, 6, 3)
+                         trans_node, node_pos, float_accumulate).reshape(N, 6, 3)
     pos, q, s, sh = refit_gaussians(e_new, rot_old, scale0, shs, static)
     return (e_new,) + (pos, q, s, sh)
 
@@ -336,10 +336,11 @@ def slerp_blend(idx, w, quats):
 
 
 def skin_samples(sample_pos, idx, w, rot_node, trans_node, node_pos, feature,
-                 static=None):
+                 static=None, float_accumulate=True):
     """UpdatePositionforSamples (GaussianView.cpp:3060-3077) and
     FastUpdateSamplesSH (GaussianView.cpp:3169-3186).  Returns (pos, feature)."""
-    pos = _ed.ed_blend(sample_pos, idx, np.asarray(w, F64), rot_node, trans_node, node_pos)
+    pos = _ed.ed_blend(sample_pos, idx, np.asarray(w, F64), rot_node, trans_node, node_pos,
+                       float_accumulate)
     q = node_quaternions(rot_node)
     qb = slerp_blend(idx, np.asarray(w, F32), q)
     feat = rotate_sh(feature, quat_to_matrix(quat_normalize(qb))).astype(F32)
@@ -356,3 +357,96 @@ def static_mask(idx, static_nodes, n_nodes):
     is_static = np.zeros(n_nodes, bool)
     is_static[np.asarray(static_nodes, np.int64)] = True
     return is_static[idx].all(axis=1)
+
+
+# ------------------------------------------------------------- adjoint ----
+
+def skin_forward_from_nodes(ends_in, idx, w, X, node_pos, scale0):
+    """(mu, Sigma [N,3,3]) of the skinned Gaussians as a function of the node
+    transforms X [n,12] ([R column-major | t]), float64 throughout; idx/w are
+    Gaussian-major [N*6, k]."""
+    n = X.shape[0]
+    N = ends_in.shape[0]
+    R = X[:, :9].reshape(n, 3, 3).transpose(0, 2, 1)
+    t = X[:, 9:]
+    g = np.asarray(node_pos, F64)
+    P = np.asarray(ends_in, F64).reshape(-1, 3)
+    out = np.zeros_like(P)
+    for j in range(idx.shape[1]):
+        nj = idx[:, j]
+        out += np.asarray(w, F64)[:, j:j + 1] * (np.einsum("nij,nj->ni", R[nj], P - g[nj]) + g[nj] + t[nj])
+    P2 = out.reshape(N, 6, 3)
+    mu = P2.mean(1)
+    M = np.stack([(P2[:, 2 * a] - P2[:, 2 * a + 1]) / 2 for a in range(3)], axis=2)
+    U, S, Vt = np.linalg.svd(M)
+    Rp = U @ Vt
+    K = np.einsum("nra,nra->na", Rp, M)
+    s0 = np.asarray(scale0, F64)
+    s = s0 / ((s0 + 1e-3) * 2) * K
+    Sig = np.einsum("nia,na,nja->nij", Rp, s * s, Rp)
+    return mu, Sig
+
+
+def skin_backward(ends_in, idx, w, X, node_pos, scale0, g_mu, g_sigma):
+    """dL/dX [n,12] for L = sum g_mu . mu + sum g_sigma : Sigma (g_sigma
+    symmetric [N,3,3]), float64, by the chain rule through the polar factor
+    (M = R S: dR = R [w]x, (tr S I - S) w = skew(R^T dM))."""
+    n = X.shape[0]
+    N = ends_in.shape[0]
+    g = np.asarray(node_pos, F64)
+    R = X[:, :9].reshape(n, 3, 3).transpose(0, 2, 1)
+    t = X[:, 9:]
+    P = np.asarray(ends_in, F64).reshape(-1, 3)
+    wf = np.asarray(w, F64)
+    out = np.zeros_like(P)
+    for j in range(idx.shape[1]):
+        nj = idx[:, j]
+        out += wf[:, j:j + 1] * (np.einsum("nij,nj->ni", R[nj], P - g[nj]) + g[nj] + t[nj])
+    P2 = out.reshape(N, 6, 3)
+    M = np.stack([(P2[:, 2 * a] - P2[:, 2 * a + 1]) / 2 for a in range(3)], axis=2)
+    U, _, Vt = np.linalg.svd(M)
+    Rp = U @ Vt
+    Sm = np.einsum("nra,nrb->nab", Rp, M)
+    Sm = 0.5 * (Sm + Sm.transpose(0, 2, 1))
+    K = np.einsum("naa->na", Sm)
+    s0 = np.asarray(scale0, F64)
+    c = s0 / ((s0 + 1e-3) * 2)
+    D = (c * K) ** 2
+    G = np.asarray(g_sigma, F64)
+    gR = 2 * np.einsum("nij,njk,nk->nik", G, Rp, D)
+    gK = np.einsum("nia,nij,nja->na", Rp, G, Rp) * 2 * c * c * K
+    gM = Rp * gK[:, None, :]
+    gR = gR + M * gK[:, None, :]
+    A = np.einsum("nri,nrj->nij", Rp, gR)
+    a = 0.5 * np.stack([A[:, 2, 1] - A[:, 1, 2], A[:, 0, 2] - A[:, 2, 0], A[:, 1, 0] - A[:, 0, 1]], 1)
+    T = np.einsum("nii->n", Sm)[:, None, None] * np.eye(3) - Sm
+    om = np.linalg.solve(T, a[..., None])[..., 0]
+    Y = np.zeros((N, 3, 3))
+    Y[:, 0, 1], Y[:, 0, 2], Y[:, 1, 2] = -om[:, 2], om[:, 1], -om[:, 0]
+    Y[:, 1, 0], Y[:, 2, 0], Y[:, 2, 1] = om[:, 2], -om[:, 1], om[:, 0]
+    gM = gM + 2 * np.einsum("nij,njk->nik", Rp, Y)
+    gP = np.repeat(np.asarray(g_mu, F64)[:, None, :] / 6, 6, 1)
+    for q in range(3):
+        gP[:, 2 * q] += gM[:, :, q] / 2
+        gP[:, 2 * q + 1] -= gM[:, :, q] / 2
+    gP = gP.reshape(-1, 3)
+    gX = np.zeros((n, 12))
+    for j in range(idx.shape[1]):
+        nj = idx[:, j]
+        d = P - g[nj]
+        contrib = wf[:, j:j + 1, None] * gP[:, :, None] * d[:, None, :]
+        np.add.at(gX, (nj, slice(0, 9)), contrib.transpose(0, 2, 1).reshape(-1, 9))
+        np.add.at(gX, (nj, slice(9, 12)), wf[:, j:j + 1] * gP)
+    return gX
+
+
+def packed_to_sym(g6):
+    """Upstream gradient of packed (xx,xy,xz,yy,yz,zz) as the symmetric G with
+    dL = sum G : dSigma."""
+    g6 = np.asarray(g6, F64)
+    G = np.empty((g6.shape[0], 3, 3))
+    G[:, 0, 0], G[:, 1, 1], G[:, 2, 2] = g6[:, 0], g6[:, 3], g6[:, 5]
+    G[:, 0, 1] = G[:, 1, 0] = 0.5 * g6[:, 1]
+    G[:, 0, 2] = G[:, 2, 0] = 0.5 * g6[:, 2]
+    G[:, 1, 2] = G[:, 2, 1] = 0.5 * g6[:, 4]
+    return G

@@ -6,7 +6,13 @@ Tolerances (float32 kernels against the float64 oracle):
   node transforms        max |dx| / max |x|   <= 1e-5 (mixed precision), 5e-5 (plain FP32)
   ED blend positions     max abs / scene extent <= 2e-6
   Gaussian mu            max abs / scene extent <= 2e-6
-  Gaussian Sigma         per-Gaussian |dS|_F / |S|_F <= 2e-5 (p99.9) and 1e-4 (max)
+  Gaussian Sigma         per-Gaussian |dS|_F / |S|_F <= 2e-5 (p99.9) and 1e-4 (max);
+                         flat Gaussians (stress scene, one axis ~1e-4 in a [0,4]^3 field)
+                         1e-4 / 5e-4: the float32 endpoints carry ~1e-4 relative on
+                         the flat axis, which also fixes the rotation to that level
+  The library rounds each ED blend once; the oracle comparisons below use the
+  oracle's exact (single-rounding) blend.  The reference rounds after every
+  neighbour (float accumulation), a difference of a few float32 ulps.
   quaternion             |1 - |<q, q_ref>|| <= 2e-6
   SH / features          max abs <= 5e-5 (coefficients ~N(0, 0.2))
 """
@@ -227,7 +233,8 @@ def test_skin_gaussians(dev, scene):
     w_o = _np(ew).reshape(scene.k, 6, N).transpose(2, 1, 0).reshape(6 * N, scene.k).astype(np.float64)
     rot64 = rot.astype(np.float64)
     e_ref, p_ref, q_ref, s_ref, sh_ref = skin.skin_gaussians(
-        e_in, idx_o, w_o, rot64, trans.astype(np.float64), scene.node_pos, scene.rot, scene.scale, scene.shs)
+        e_in, idx_o, w_o, rot64, trans.astype(np.float64), scene.node_pos, scene.rot, scene.scale, scene.shs,
+        float_accumulate=False)
     ext = float(np.ptp(scene.pos, axis=0).max())
     e_gpu = _np(ends).reshape(6, 3, N).transpose(2, 0, 1)
     assert np.abs(e_gpu - e_ref).max() / ext <= 2e-6
@@ -240,7 +247,8 @@ def test_skin_gaussians(dev, scene):
         return np.sqrt(v[:, 0] ** 2 + v[:, 3] ** 2 + v[:, 5] ** 2 + 2 * (v[:, 1] ** 2 + v[:, 2] ** 2 + v[:, 4] ** 2))
     rel = fro(c - c_ref) / fro(c_ref)
     print("cov rel p99.9", np.quantile(rel, 0.999), "max", rel.max())
-    assert np.quantile(rel, 0.999) <= 2e-5 and rel.max() <= 1e-4
+    flat = scene.name.startswith("stress")
+    assert np.quantile(rel, 0.999) <= (1e-4 if flat else 2e-5) and rel.max() <= (5e-4 if flat else 1e-4)
     assert np.abs(_np(shs) - sh_ref).max() <= 5e-5
 
 
@@ -290,7 +298,7 @@ def test_skin_samples(dev, scene):
     f = _t(feat)
     dev.skin_samples(p, idx, w, table, quat, f)
     p_ref, f_ref = skin.skin_samples(sp, _np(idx).T, _np(w).T, rot.astype(np.float64),
-                                     trans.astype(np.float64), scene.node_pos, feat)
+                                     trans.astype(np.float64), scene.node_pos, feat, float_accumulate=False)
     q_ref = skin.node_quaternions(rot.astype(np.float64))
     dq = np.abs(1 - np.abs((_np(quat).astype(np.float64) * q_ref).sum(1)))
     assert dq.max() <= 2e-6
@@ -306,7 +314,8 @@ def test_update_nodes_and_static(dev, scene):
     aidx, aw = ed.knn_weights(scene.pos[scene.node_vertex], scene.node_pos, scene.k)
     table = dev.node_table(_t(rot), _t(trans), _t(scene.node_pos))
     out = dev.update_nodes(_t(scene.node_pos), _t(aidx.T.astype(np.int32)), _t(aw.T.astype(np.float32)), table)
-    ref = ed.ed_blend(scene.node_pos, aidx, aw, rot.astype(np.float64), trans.astype(np.float64), scene.node_pos)
+    ref = ed.ed_blend(scene.node_pos, aidx, aw, rot.astype(np.float64), trans.astype(np.float64), scene.node_pos,
+                      float_accumulate=False)
     ext = float(np.ptp(scene.pos, axis=0).max())
     assert np.abs(_np(out) - ref).max() / ext <= 2e-6
     st_nodes = np.zeros(scene.n_nodes, np.uint8)
