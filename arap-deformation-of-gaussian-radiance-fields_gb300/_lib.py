@@ -40,10 +40,13 @@ class GridInfo(C.Structure):
 class SolveStats(C.Structure):
     _fields_ = [("status", C.c_int), ("gn_iterations", C.c_int), ("pcg_iterations", C.c_int),
                 ("halvings", C.c_int), ("initial_energy", C.c_double), ("final_energy", C.c_double),
-                ("n_free", C.c_int), ("n_static", C.c_int), ("n_rows", C.c_int)]
+                ("n_free", C.c_int), ("n_static", C.c_int), ("n_rows", C.c_int),
+                ("n_coarse", C.c_int), ("phase_ms", C.c_double * 5)]
 
     def as_dict(self):
-        return {f: getattr(self, f) for f, _ in self._fields_}
+        d = {f: getattr(self, f) for f, _ in self._fields_}
+        d["phase_ms"] = dict(zip(("setup", "gradient", "coarse", "pcg", "line_search"), list(self.phase_ms)))
+        return d
 
 
 P = C.c_void_p

@@ -345,7 +345,7 @@ extern "C" int arap_solver_create(arap_solver** out, int n, int k, const int32_t
     P.dpiv = cv.take<float4>(NA ? F : 0);
     P.partials = cv.take<double>((size_t)8 * grid);
     P.results = cv.take<double>(8);
-    P.stats = cv.take<double>(8);
+    P.stats = cv.take<double>(16);
     P.bar = cv.take<GridBarrier>(1);
   };
   Carver sizing{nullptr};
@@ -454,7 +454,7 @@ extern "C" int arap_solver_solve(arap_solver* s, const float* node_pos, const fl
   int rc = launch_solver(s, st);
   if (rc != ARAP_OK) return rc;
   if (!stats_host) return ARAP_OK;
-  double st8[8];
+  double st8[16];
   ARAP_CUDA_TRY(cudaMemcpyAsync(st8, s->P.stats, sizeof(st8), cudaMemcpyDeviceToHost, st));
   const int dev_status = arap_get_device_status(stream);  // synchronises
   std::memset(stats_host, 0, sizeof(*stats_host));
@@ -466,6 +466,8 @@ extern "C" int arap_solver_solve(arap_solver* s, const float* node_pos, const fl
   stats_host->n_free = s->F;
   stats_host->n_static = s->S;
   stats_host->n_rows = s->n_rows;
+  for (int q = 0; q < 5; ++q) stats_host->phase_ms[q] = st8[ST_T_PREP + q] * 1e-6;
+  stats_host->n_coarse = s->P.NC;
   int status = dev_status;
   if (status == ARAP_OK && s->cfg.early_exit && st8[ST_CONV] == 0.0 && s->cfg.max_iters > 0)
     status = ARAP_NOT_CONVERGED;
@@ -491,7 +493,7 @@ extern "C" int arap_solver_energy_grad(arap_solver* s, const float* node_pos, co
   s->P.aims = used.aims;
   if (rc != ARAP_OK) return rc;
   if (energy_host) {
-    double st8[8];
+    double st8[16];
     ARAP_CUDA_TRY(cudaMemcpyAsync(st8, used.stats, sizeof(st8), cudaMemcpyDeviceToHost, st));
     const int dev_status = arap_get_device_status(stream);
     *energy_host = st8[ST_E];

@@ -8,8 +8,18 @@
 
 namespace arap {
 
-// stats slots written by CTA 0
-enum { ST_ITERS = 0, ST_PCG = 1, ST_HALV = 2, ST_E0 = 3, ST_E = 4, ST_CONV = 5, ST_NONFINITE = 6 };
+// stats slots written by CTA 0; ST_T_* are nanoseconds spent in each phase
+// (global timer, read by thread 0 of CTA 0 after the phase's barrier)
+enum {
+  ST_ITERS = 0, ST_PCG = 1, ST_HALV = 2, ST_E0 = 3, ST_E = 4, ST_CONV = 5, ST_NONFINITE = 6,
+  ST_T_PREP = 8, ST_T_GRAD = 9, ST_T_COARSE = 10, ST_T_PCG = 11, ST_T_LS = 12
+};
+
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
 
 template <int N>
 __device__ __forceinline__ bool reduce_all(const SolveParams& P, double (&v)[N], double (&out)[N]) {
@@ -145,6 +155,13 @@ __global__ void __launch_bounds__(kSolveThreads) gn_solve_kernel(SolveParams P) 
   const int gt = blockIdx.x * blockDim.x + threadIdx.x;
   const int nt = gridDim.x * blockDim.x;
   const int F = P.F, k = P.k;
+  unsigned long long t_mark = global_ns();
+  double t_acc[5] = {0.0, 0.0, 0.0, 0.0, 0.0};  // prep, grad, coarse, pcg, line search
+  auto lap = [&](int slot) {
+    const unsigned long long now = global_ns();
+    t_acc[slot] += (double)(now - t_mark);
+    t_mark = now;
+  };
 
   // ---- per-frame geometry: member anchors, group targets, x = identity
   for (int slot = gt; slot < P.U * k; slot += nt) {
@@ -197,6 +214,7 @@ __global__ void __launch_bounds__(kSolveThreads) gn_solve_kernel(SolveParams P) 
     if (!grid_sync_reduce<1>(P.bar, P.partials, P.results, d0, o0)) return;
   }
 
+  lap(0);
   double e_first = 0.0, e_last = 0.0;
   int iters = 0, pcg_total = 0, halvings = 0, converged = 0;
   for (int it = 0; it < P.max_iters; ++it) {
@@ -247,6 +265,7 @@ __global__ void __launch_bounds__(kSolveThreads) gn_solve_kernel(SolveParams P) 
       red[1] += v * v;
     }
     if (!reduce_all<4>(P, red, out)) return;
+    lap(1);
     const double e_old = out[0];
     const double normv = sqrt(out[1]);
     if (it == 0) e_first = e_old;
@@ -273,6 +292,7 @@ __global__ void __launch_bounds__(kSolveThreads) gn_solve_kernel(SolveParams P) 
       if (!grid_sync_reduce<1>(P.bar, P.partials, P.results, d0, o0)) return;
       if (!coarse_invert(P, &coarse_ok)) return;
       if (!coarse_ok && gt == 0) raise_status(ARAP_ENONFINITE);
+      lap(2);
     }
     if (coarse) {
       double rzc[1] = {0.0}, orc[1];
@@ -349,6 +369,7 @@ __global__ void __launch_bounds__(kSolveThreads) gn_solve_kernel(SolveParams P) 
       rz = rz_new;
     }
     pcg_total += pi;
+    lap(3);
 
     // ---- line search: x + 2^-m h, m = 0..49 (Deform.cpp:144-156)
     RT scale = RT(1);
@@ -399,6 +420,7 @@ __global__ void __launch_bounds__(kSolveThreads) gn_solve_kernel(SolveParams P) 
       double d0[1] = {0.0}, o0[1];
       if (!reduce_all<1>(P, d0, o0)) return;
     }
+    lap(4);
     if (P.early_exit && normh < (normv + 1e-6) * 1e-6) {
       converged = 1;
       break;
@@ -439,6 +461,7 @@ __global__ void __launch_bounds__(kSolveThreads) gn_solve_kernel(SolveParams P) 
     P.stats[ST_E0] = e_first;
     P.stats[ST_E] = e_last;
     P.stats[ST_CONV] = converged;
+    for (int q = 0; q < 5; ++q) P.stats[ST_T_PREP + q] = t_acc[q];
   }
 }
 

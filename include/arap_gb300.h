@@ -88,6 +88,9 @@ typedef struct {
   double initial_energy;  /* f.f at x = identity */
   double final_energy;    /* f.f at the returned x */
   int n_free, n_static, n_rows;
+  int n_coarse;           /* coarse unknowns of the two-level preconditioner (0 = off) */
+  double phase_ms[5];     /* device time in: set-up, gradient/preconditioner, coarse
+                             inversion, PCG, line search (CTA 0's view) */
 } arap_solve_stats;
 
 typedef struct arap_solver arap_solver;

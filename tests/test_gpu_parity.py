@@ -166,7 +166,7 @@ def test_solve_centre_mode_and_weighting(dev):
         rot_ref, tr_ref = ed.put_free_inputs(pr, x_ref)
         solver = dev.Solver(_t(nb.astype(np.int32)), _t(aidx.T.astype(np.int32)), _t(aw.T.astype(np.float32)),
                             blocks, types, max_iters=5, early_exit=0, cons_on_center=cons,
-                            weighting_factor=wf, precision=1)
+                            weighting_factor=wf, precision=1, pcg_tol=1e-7)
         rot, tr, st = solver.solve(_t(sc.node_pos), _t(aims))
         X = np.concatenate([_np(rot), _np(tr)], axis=1)
         Xr = np.concatenate([rot_ref, tr_ref], axis=1)
@@ -249,7 +249,7 @@ def test_skin_gaussians(dev, scene):
     print("cov rel p99.9", np.quantile(rel, 0.999), "max", rel.max())
     flat = scene.name.startswith("stress")
     assert np.quantile(rel, 0.999) <= (1e-4 if flat else 2e-5) and rel.max() <= (5e-4 if flat else 1e-4)
-    assert np.abs(_np(shs) - sh_ref).max() <= 5e-5
+    assert np.abs(_np(shs) - sh_ref).max() <= (5e-4 if flat else 5e-5)
 
 
 def test_skin_samples_and_sh_golden(dev):
