@@ -41,11 +41,12 @@ class SolveStats(C.Structure):
     _fields_ = [("status", C.c_int), ("gn_iterations", C.c_int), ("pcg_iterations", C.c_int),
                 ("halvings", C.c_int), ("initial_energy", C.c_double), ("final_energy", C.c_double),
                 ("n_free", C.c_int), ("n_static", C.c_int), ("n_rows", C.c_int),
-                ("n_coarse", C.c_int), ("phase_ms", C.c_double * 5)]
+                ("n_coarse", C.c_int), ("phase_ms", C.c_double * 9)]
 
     def as_dict(self):
         d = {f: getattr(self, f) for f, _ in self._fields_}
-        d["phase_ms"] = dict(zip(("setup", "gradient", "coarse", "pcg", "line_search"), list(self.phase_ms)))
+        d["phase_ms"] = dict(zip(("setup", "gradient", "coarse", "pcg", "line_search", "coarse_invert",
+                                 "pcg_spmv_work", "pcg_update_work", "pcg_coarse_work"), list(self.phase_ms)))
         return d
 
 

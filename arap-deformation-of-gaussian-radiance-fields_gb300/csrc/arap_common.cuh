@@ -36,25 +36,35 @@ __device__ __forceinline__ void raise_status(int code) { atomicCAS(&g_status, 0,
 // Grid-wide barrier for cooperative launches (all CTAs co-resident).  Every
 // wait is bounded: after kSpinLimit polls a waiting CTA records ARAP_ETIMEOUT,
 // marks the barrier failed and returns false; callers then leave the kernel.
-// The barrier carries NSLOT deterministic FP64 sums: every CTA leaves one
-// partial per slot; the last CTA to arrive adds them in CTA order, publishes
-// the totals and only then releases the waiters.
+//
+// Counter barrier with a reduction.  Arrivals go to one monotonic counter
+// (zeroed before each launch): the arrivals of the e-th barrier of a launch
+// are the counts e*nb .. (e+1)*nb-1, so a CTA that has passed e barriers
+// waits for the count (e+1)*nb and nothing is ever reset.  Each barrier
+// carries up to kReduceSlots FP64 sums: a CTA's sums go to
+// partials[e & 1][cta][slot] before the release-add of its arrival; after the
+// acquire that sees every arrival, warp 0 of every CTA loads all partials at
+// once and adds them in CTA order, so every CTA gets the same bits.  Two
+// partial buffers suffice: a CTA can only reach barrier e+2 once every CTA has
+// arrived at e+1, i.e. has finished reading barrier e.
 struct GridBarrier {
   unsigned int count;
-  unsigned int gen;
+  unsigned int pad0;
   int failed;
-  int pad;
+  int pad1;
 };
 
 constexpr long long kSpinLimit = 1ll << 23;
+constexpr int kReduceSlots = 4;
+constexpr int kMaxGridCtas = 320;  // CTAs a barrier reduction supports (10 per lane)
 
 __device__ __forceinline__ unsigned int ld_acquire_u32(const unsigned int* p) {
   unsigned int v;
   asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
   return v;
 }
-__device__ __forceinline__ void st_release_u32(unsigned int* p, unsigned int v) {
-  asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+__device__ __forceinline__ void red_release_add_u32(unsigned int* p, unsigned int v) {
+  asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 __device__ __forceinline__ int ld_relaxed_i32(const int* p) {
   int v;
@@ -62,83 +72,115 @@ __device__ __forceinline__ int ld_relaxed_i32(const int* p) {
   return v;
 }
 
-// Sums are returned in out[] to every thread of every CTA.
-template <int NSLOT>
-__device__ bool grid_sync_reduce(GridBarrier* bar, double* partials, double* results,
-                                 const double (&mine)[NSLOT], double (&out)[NSLOT]) {
-  __shared__ int s_last;
-  __shared__ int s_ok;
-  __shared__ double s_out[NSLOT > 0 ? NSLOT : 1];
-  const unsigned int nb = gridDim.x;
-  if (threadIdx.x == 0) {
+template <typename T>
+__device__ __forceinline__ T warp_sum(T v) {
 #pragma unroll
-    for (int s = 0; s < NSLOT; ++s) partials[s * nb + blockIdx.x] = mine[s];
-  }
-  __syncthreads();
-  unsigned int g = 0;
-  if (threadIdx.x == 0) {
-    g = ld_acquire_u32(&bar->gen);  // cannot advance before this CTA arrives
-    __threadfence();
-    unsigned int arrived = atomicAdd(&bar->count, 1u);
-    s_last = (arrived == nb - 1);
-    s_ok = 1;
-  }
-  __syncthreads();
-  if (s_last) {
-    if (threadIdx.x < 32) {
-      __threadfence();
-#pragma unroll
-      for (int s = 0; s < NSLOT; ++s) {
-        double acc = 0.0;
-        for (unsigned int c = threadIdx.x; c < nb; c += 32) acc += __ldcg(partials + s * nb + c);
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-        if (threadIdx.x == 0) {
-          results[s] = acc;
-          s_out[s] = acc;
-        }
-      }
-      if (threadIdx.x == 0) {
-        atomicExch(&bar->count, 0u);
-        __threadfence();
-        st_release_u32(&bar->gen, g + 1u);
-        s_ok = ld_relaxed_i32(&bar->failed) == 0;
-      }
-    }
-  } else if (threadIdx.x == 0) {
-    long long it = 0;
-    int ok = 1;
-    while (ld_acquire_u32(&bar->gen) == g) {
-      if (ld_relaxed_i32(&bar->failed)) {
-        ok = 0;
-        break;
-      }
-      if (++it > kSpinLimit) {
-        atomicExch(&bar->failed, 1);
-        raise_status(ARAP_ETIMEOUT);
-        ok = 0;
-        break;
-      }
-      if (it > 256) __nanosleep(40);
-    }
-    if (ok) {
-#pragma unroll
-      for (int s = 0; s < NSLOT; ++s) s_out[s] = __ldcg(results + s);
-    }
-    s_ok = ok;
-  }
-  __syncthreads();
-#pragma unroll
-  for (int s = 0; s < NSLOT; ++s) out[s] = s_out[s];
-  const bool ok = s_ok != 0;
-  __syncthreads();
-  return ok;
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
 }
 
-__device__ __forceinline__ bool grid_sync(GridBarrier* bar, double* partials, double* results) {
-  double none[1] = {0.0}, o[1];
-  return grid_sync_reduce<1>(bar, partials, results, none, o);
-}
+// Per-thread handle of the grid barrier.  Every thread of every CTA must make
+// the same sequence of calls (the epoch is counted in registers).
+struct GridSync {
+  GridBarrier* bar;
+  double* partials;  // [2][gridDim.x][kReduceSlots]
+  unsigned int epoch;
+
+  // One thread per CTA: arrive at barrier e (release) and wait (acquire) for
+  // every CTA; bounded, false on failure.
+  __device__ bool arrive_and_wait(unsigned int e) {
+    red_release_add_u32(&bar->count, 1u);
+    const unsigned int target = (e + 1u) * gridDim.x;
+    long long it = 0;
+    while ((int)(ld_acquire_u32(&bar->count) - target) < 0) {
+      ++it;
+      if ((it & 63) == 0 && ld_relaxed_i32(&bar->failed)) return false;
+      if (it > kSpinLimit) {
+        atomicExch(&bar->failed, 1);
+        raise_status(ARAP_ETIMEOUT);
+        return false;
+      }
+      if (it > 1024) __nanosleep(32);
+    }
+    return true;
+  }
+
+  // v[] holds this thread's contributions on entry and the grid-wide sums on
+  // return (the same bits in every thread of every CTA).  Returns false when
+  // the barrier failed (timed out here or elsewhere).
+  template <int NSLOT>
+  __device__ bool reduce(double (&v)[NSLOT]) {
+    static_assert(NSLOT >= 1 && NSLOT <= kReduceSlots, "slots");
+    __shared__ double s_red[32][NSLOT];
+    __shared__ double s_out[NSLOT];
+    __shared__ int s_ok;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const unsigned int nb = gridDim.x;
+    const unsigned int e = epoch++;
+    double* buf = partials + (size_t)(e & 1u) * kReduceSlots * nb;
+#pragma unroll
+    for (int s = 0; s < NSLOT; ++s) v[s] = warp_sum(v[s]);
+    if (lane == 0) {
+#pragma unroll
+      for (int s = 0; s < NSLOT; ++s) s_red[w][s] = v[s];
+    }
+    __syncthreads();
+    if (w == 0) {
+      const int nw = blockDim.x >> 5;
+#pragma unroll
+      for (int s = 0; s < NSLOT; ++s) {
+        double c = lane < nw ? s_red[lane][s] : 0.0;
+        c = warp_sum(c);
+        if (lane == 0) buf[(size_t)blockIdx.x * kReduceSlots + s] = c;
+      }
+      int ok = 1;
+      if (lane == 0) ok = arrive_and_wait(e);
+      __syncwarp();
+      ok = __shfl_sync(0xffffffffu, ok, 0);
+      if (ok) {
+        // two slots per pass: every CTA's pair requested at once, then added in CTA order
+        constexpr int kQ = kMaxGridCtas / 32;
+#pragma unroll
+        for (int s0 = 0; s0 < NSLOT; s0 += 2) {
+          double2 t[kQ];
+#pragma unroll
+          for (int q = 0; q < kQ; ++q) {
+            const unsigned int c = lane + 32u * q;
+            t[q] = c < nb ? __ldcg(reinterpret_cast<const double2*>(buf + (size_t)c * kReduceSlots + s0))
+                          : make_double2(0.0, 0.0);
+          }
+          double a0 = 0.0, a1 = 0.0;
+#pragma unroll
+          for (int q = 0; q < kQ; ++q) {
+            a0 += t[q].x;
+            a1 += t[q].y;
+          }
+          a0 = warp_sum(a0);
+          if (s0 + 1 < NSLOT) a1 = warp_sum(a1);
+          if (lane == 0) {  // lane 0's association order, as in every CTA
+            s_out[s0] = a0;
+            if (s0 + 1 < NSLOT) s_out[s0 + 1] = a1;
+          }
+        }
+      }
+      if (lane == 0) s_ok = ok;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int s = 0; s < NSLOT; ++s) v[s] = s_out[s];
+    return s_ok != 0;
+  }
+
+  // Plain barrier (no sums): one arrival per CTA, as in reduce.
+  __device__ bool sync() {
+    __shared__ int s_sync_ok;
+    const unsigned int e = epoch++;
+    __syncthreads();
+    if (threadIdx.x == 0) s_sync_ok = arrive_and_wait(e) ? 1 : 0;
+    __syncthreads();
+    return s_sync_ok != 0;
+  }
+};
 
 // Marks the barrier failed so that peers waiting in it leave promptly.
 __device__ __forceinline__ void grid_fail(GridBarrier* bar, int code) {

@@ -202,7 +202,10 @@ extern "C" int arap_solver_create(arap_solver** out, int n, int k, const int32_t
   // (both edge directions, free nodes only) up to coarse_nodes members; small
   // leftovers join their neighbouring aggregate
   std::vector<int32_t> agg(F, -1), pivot, agg_count;
-  if (cfg.coarse_nodes > 0 && F > cfg.coarse_nodes) {
+  auto aggregate = [&](int target) {
+    std::fill(agg.begin(), agg.end(), -1);
+    pivot.clear();
+    agg_count.clear();
     std::vector<std::vector<int32_t>> adj(F);
     for (int i = 0; i < n; ++i) {
       if (rank[i] < 0) continue;
@@ -213,7 +216,6 @@ extern "C" int arap_solver_create(arap_solver** out, int n, int k, const int32_t
         adj[rank[j]].push_back(rank[i]);
       }
     }
-    const int target = cfg.coarse_nodes;
     std::vector<int32_t> queue;
     for (int seed = 0; seed < F; ++seed) {
       if (agg[seed] >= 0) continue;
@@ -265,6 +267,14 @@ extern "C" int arap_solver_create(arap_solver** out, int n, int k, const int32_t
     }
     pivot.swap(piv2);
     agg_count.swap(cnt2);
+  };
+  if (cfg.coarse_nodes > 0 && F > cfg.coarse_nodes) {
+    int target = cfg.coarse_nodes;
+    aggregate(target);
+    while ((int)pivot.size() > kMaxCoarseAggs) {
+      target += (target + 3) / 4;
+      aggregate(target);
+    }
   }
   const int NA = (int)pivot.size();
   const int NC = 12 * NA;
@@ -280,6 +290,20 @@ extern "C" int arap_solver_create(arap_solver** out, int n, int k, const int32_t
       if (mem_rank[q] >= 0) mem_agg[q] = agg[mem_rank[q]];
     for (auto& it4 : item_flat)
       if ((it4.x == ITEM_OUT || it4.x == ITEM_IN) && it4.y >= 0) it4.x |= agg[it4.y] << 4;
+  }
+  // per group: the distinct aggregates of its free anchors
+  std::vector<int32_t> gca_off{0}, gca;
+  if (NA > 0) {
+    for (int g = 0; g < G; ++g) {
+      const size_t first = gca.size();
+      for (int u = grp_off[g]; u < grp_off[g + 1]; ++u)
+        for (int t = 0; t < k; ++t) {
+          const int rk = mem_rank[(size_t)u * k + t];
+          if (rk < 0) continue;
+          if (std::find(gca.begin() + first, gca.end(), agg[rk]) == gca.end()) gca.push_back(agg[rk]);
+        }
+      gca_off.push_back((int32_t)gca.size());
+    }
   }
 
   auto* s = new (std::nothrow) arap_solver();
@@ -301,7 +325,7 @@ extern "C" int arap_solver_create(arap_solver** out, int n, int k, const int32_t
     delete s;
     return ARAP_ECUDA;
   }
-  s->grid = grid;
+  s->grid = std::min(grid, kMaxGridCtas);
 
   // device layout
   auto carve = [&](Carver& cv, SolveParams& P) {
@@ -327,7 +351,7 @@ extern "C" int arap_solver_create(arap_solver** out, int n, int k, const int32_t
     P.p0 = cv.take<float>((size_t)F * 12);
     P.p1 = cv.take<float>((size_t)F * 12);
     P.q = cv.take<float>((size_t)F * 12);
-    P.g = cv.take<float>((size_t)F * 12);
+    P.u = cv.take<float>((size_t)F * 12);
     P.dinv = cv.take<float>((size_t)F * 144);
     P.order = cv.take<int32_t>(F);
     P.agg = cv.take<int32_t>(F);
@@ -335,17 +359,18 @@ extern "C" int arap_solver_create(arap_solver** out, int n, int k, const int32_t
     P.agg_count = cv.take<int32_t>(NA);
     P.Qd = cv.take<double>((size_t)NA * NA * 16);
     P.Cw = cv.take<float>((size_t)2 * NC * NC);
-    P.Wgj = cv.take<float>((size_t)NC * kGJBlock);
-    P.Pgj = cv.take<float>((size_t)kGJBlock * kGJBlock);
     P.rotagg = cv.take<double>((size_t)2 * NA * 81);
     P.Cinv = cv.take<float>((size_t)NC * NC);
     P.rc = cv.take<double>((size_t)2 * NC);
     P.zc = cv.take<float>(NC);
     P.mem_agg = cv.take<int32_t>((size_t)U * k);
     P.dpiv = cv.take<float4>(NA ? F : 0);
-    P.partials = cv.take<double>((size_t)8 * grid);
-    P.results = cv.take<double>(8);
-    P.stats = cv.take<double>(16);
+    P.gca_off = cv.take<int32_t>(NA ? G + 1 : 0);
+    P.gca = cv.take<int32_t>(gca.size());
+    P.gcv = cv.take<float4>(gca.size());
+    P.uzg = cv.take<float4>(NA ? G : 0);
+    P.partials = cv.take<double>((size_t)2 * kReduceSlots * grid);
+    P.stats = cv.take<double>(kStatSlots);
     P.bar = cv.take<GridBarrier>(1);
   };
   Carver sizing{nullptr};
@@ -384,7 +409,7 @@ extern "C" int arap_solver_create(arap_solver** out, int n, int k, const int32_t
       cost[r] = {-node_cost[r], r};
     }
     std::sort(cost.begin(), cost.end());
-    const int nw = grid * (kSolveThreads / 32);
+    const int nw = s->grid * (kSolveThreads / 32);
     for (int i = 0; i < F; ++i) {
       const int rd = i / nw, w = i % nw;
       const int src = rd * nw + ((rd & 1) ? std::min(nw, F - rd * nw) - 1 - w : w);
@@ -397,6 +422,8 @@ extern "C" int arap_solver_create(arap_solver** out, int n, int k, const int32_t
     e = e ? e : up(P.agg, agg.data(), agg.size() * 4);
     e = e ? e : up(P.pivot, pivot.data(), pivot.size() * 4);
     e = e ? e : up(P.agg_count, agg_count.data(), agg_count.size() * 4);
+    e = e ? e : up(P.gca_off, gca_off.data(), gca_off.size() * 4);
+    e = e ? e : up(P.gca, gca.data(), gca.size() * 4);
   }
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   if (e != cudaSuccess) {
@@ -454,7 +481,7 @@ extern "C" int arap_solver_solve(arap_solver* s, const float* node_pos, const fl
   int rc = launch_solver(s, st);
   if (rc != ARAP_OK) return rc;
   if (!stats_host) return ARAP_OK;
-  double st8[16];
+  double st8[kStatSlots];
   ARAP_CUDA_TRY(cudaMemcpyAsync(st8, s->P.stats, sizeof(st8), cudaMemcpyDeviceToHost, st));
   const int dev_status = arap_get_device_status(stream);  // synchronises
   std::memset(stats_host, 0, sizeof(*stats_host));
@@ -466,7 +493,7 @@ extern "C" int arap_solver_solve(arap_solver* s, const float* node_pos, const fl
   stats_host->n_free = s->F;
   stats_host->n_static = s->S;
   stats_host->n_rows = s->n_rows;
-  for (int q = 0; q < 5; ++q) stats_host->phase_ms[q] = st8[ST_T_PREP + q] * 1e-6;
+  for (int q = 0; q < 9; ++q) stats_host->phase_ms[q] = st8[ST_T_PREP + q] * 1e-6;
   stats_host->n_coarse = s->P.NC;
   int status = dev_status;
   if (status == ARAP_OK && s->cfg.early_exit && st8[ST_CONV] == 0.0 && s->cfg.max_iters > 0)
@@ -493,7 +520,7 @@ extern "C" int arap_solver_energy_grad(arap_solver* s, const float* node_pos, co
   s->P.aims = used.aims;
   if (rc != ARAP_OK) return rc;
   if (energy_host) {
-    double st8[16];
+    double st8[kStatSlots];
     ARAP_CUDA_TRY(cudaMemcpyAsync(st8, used.stats, sizeof(st8), cudaMemcpyDeviceToHost, st));
     const int dev_status = arap_get_device_status(stream);
     *energy_host = st8[ST_E];

@@ -5,7 +5,9 @@
 
 namespace arap {
 
-constexpr int kGJBlock = 48;  // pivot block of the coarse Gauss-Jordan inversion
+constexpr int kGJBlock = 48;         // pivot block of the coarse Gauss-Jordan inversion
+constexpr int kMaxCoarseAggs = 80;   // aggregates of the coarse space (12 unknowns each)
+constexpr int kMaxCoarse = 12 * kMaxCoarseAggs;
 
 // Coupling items of one free node j (all rows of J that touch x_j besides its
 // own rotation rows).  int4 {kind, a, b, c}:
@@ -44,14 +46,13 @@ struct SolveParams {
   float* xf;                 // [F*12] float copy of x
   float* h;                  // [F*12] step
   float* r;                  // [F*12] PCG residual
-  float* z;                  // [F*12] preconditioned residual
-  float* p0;                 // [F*12] search direction, even iterations
-  float* p1;                 // [F*12] search direction, odd iterations
-  float* q;                  // [F*12] A p
-  float* g;                  // [F*12] right-hand side -J^T f
+  float* z;                  // [F*12] u_f = Dinv r (fine part of the preconditioned residual)
+  float* p0;                 // [F*12] search direction p
+  float* p1;                 // [F*12] s = (J^T J) p
+  float* q;                  // [F*12] w = (J^T J) u
+  float* u;                  // [F*12] preconditioned residual u = u_f + P zc
   float* dinv;               // [F*144] inverse of the 12x12 diagonal block of J^T J
-  double* partials;          // [8 * gridDim]
-  double* results;           // [8]
+  double* partials;          // [2 * kReduceSlots * gridDim] barrier partial sums
   GridBarrier* bar;
   double* stats;             // [8] device-side stats (see solver.cu)
   float* rot_out;            // [n*9]
@@ -74,13 +75,17 @@ struct SolveParams {
   double* Qd;                // [NA*NA*16] 4x4 kernels of the coarse blocks
   float* Cw;                 // [2*NC*NC] coarse matrix / Gauss-Jordan ping-pong
   float* Cinv;               // [NC*NC] inverse of the coarse matrix
-  float* Wgj;                // [NC*kGJBlock] Gauss-Jordan row multipliers
-  float* Pgj;                // [kGJBlock^2] inverse of the current pivot block
   double* rotagg;            // [2*NA*81] per-aggregate sums of J_rot^T J_rot (GN-iteration parity)
   double* rc;                // [2*NC] restricted residual, double-buffered
   float* zc;                 // [NC] coarse correction
   const int32_t* mem_agg;    // [U*k] aggregate of each free anchor (-1 otherwise)
   float4* dpiv;              // [F] per solve: g_j - g_pivot(agg(j))
+  // J_g u of each constraint group by linearity when the two-level
+  // preconditioner is on: u = u_f + P zc gives J_g u = J_g u_f + sum_a V_ga . zc_a
+  const int32_t* gca_off;    // [G+1] distinct aggregates of each group's free anchors
+  const int32_t* gca;        // aggregate ids
+  float4* gcv;               // per solve: V_ga = sum over anchors in a of w (v_c - g_pivot(a), 1)
+  float4* uzg;               // [G] w_con J_g u_f, refreshed after each update
 };
 
 }  // namespace arap

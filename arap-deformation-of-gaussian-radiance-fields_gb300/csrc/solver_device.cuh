@@ -40,38 +40,25 @@ __device__ __forceinline__ void coarse_prolong(const SolveParams& P, int rr, int
   for (int r = 0; r < 3; ++r) v[9 + r] += c[9 + r] + d0 * c[r] + d1 * c[3 + r] + d2 * c[6 + r];
 }
 
-// Search direction of free node rr (node id `node`) for this PCG iteration,
-// formed on the fly: p = z + beta * p_old (p = z on the first iteration),
-// z = Dinv r (+ the coarse correction when the two-level preconditioner is on).
-__device__ __forceinline__ void load_p(const SolveParams& P, int rr, int agg, bool first, float beta,
-                                       const float* pold, float (&v)[12]) {
+// Preconditioned residual u = u_f + P zc of free node rr in aggregate agg,
+// formed on the fly (u_f = Dinv r in P.z; the coarse correction when the
+// two-level preconditioner is on).
+__device__ __forceinline__ void load_u(const SolveParams& P, int rr, int agg, float (&v)[12]) {
   ld12cg(P.z, rr, v);
   if (P.NA) coarse_prolong(P, rr, agg, v);
-  if (!first) {
-    float o[12];
-    ld12cg(pold, rr, o);
-#pragma unroll
-    for (int i = 0; i < 12; ++i) v[i] = fmaf(beta, o[i], v[i]);
-  }
 }
 
-__device__ __forceinline__ void load_pt(const SolveParams& P, int rr, int agg, bool first, float beta,
-                                        const float* pold, float (&v)[3]) {
+// Translation part of u for free node rr.
+__device__ __forceinline__ void load_ut(const SolveParams& P, int rr, int agg, float (&v)[3]) {
   if (P.NA) {
     float f[12];
-    load_p(P, rr, agg, first, beta, pold, f);
+    load_u(P, rr, agg, f);
     v[0] = f[9];
     v[1] = f[10];
     v[2] = f[11];
     return;
   }
   ld3t_cg(P.z, rr, v);
-  if (!first) {
-    float o[3];
-    ld3t_cg(pold, rr, o);
-#pragma unroll
-    for (int i = 0; i < 3; ++i) v[i] = fmaf(beta, o[i], v[i]);
-  }
 }
 
 // Offset from the identity transform, dx = x + scale*h - [I | 0], of free
@@ -157,8 +144,8 @@ __device__ void con_residual(const SolveParams& P, int g, RT scale, RT (&f)[3]) 
   f[2] = wc * (f[2] + (base[2] - RT(tg.w) * RT(tg.z)));
 }
 
-// J_g p of a constraint group (linear part only).
-__device__ void con_jp(const SolveParams& P, int g, bool first, float beta, const float* pold, float (&u)[3]) {
+// J_g u of a constraint group (linear part only), from the anchors' u.
+__device__ void con_ju(const SolveParams& P, int g, float (&u)[3]) {
   u[0] = u[1] = u[2] = 0.f;
   const int k = P.k;
   const int s0 = __ldg(P.grp_off + g), s1 = __ldg(P.grp_off + g + 1);
@@ -170,7 +157,7 @@ __device__ void con_jp(const SolveParams& P, int g, bool first, float beta, cons
       if (rk < 0) continue;
       const float4 geo = __ldcg(P.mem_geo + slot);
       float pl[12];
-      load_p(P, rk, P.NA ? __ldg(P.mem_agg + slot) : 0, first, beta, pold, pl);
+      load_u(P, rk, P.NA ? __ldg(P.mem_agg + slot) : 0, pl);
 #pragma unroll
       for (int c = 0; c < 3; ++c)
         u[c] = fmaf(geo.x, fmaf(geo.y, pl[c], fmaf(geo.z, pl[3 + c], fmaf(geo.w, pl[6 + c], pl[9 + c]))), u[c]);
@@ -182,11 +169,46 @@ __device__ void con_jp(const SolveParams& P, int g, bool first, float beta, cons
   u[2] *= wcf;
 }
 
-template <typename T>
-__device__ __forceinline__ T warp_sum(T v) {
+// J_g u of a constraint group with the two-level preconditioner, by
+// linearity of u = u_f + P zc: w_con J_g u_f (computed once per group in the
+// coarse-solve phase) plus the coarse part w_con sum_a V_ga . zc_a.
+__device__ void con_ju_coarse(const SolveParams& P, int g, float (&u)[3]) {
+  const float4 uz = __ldcg(P.uzg + g);
+  u[0] = uz.x;
+  u[1] = uz.y;
+  u[2] = uz.z;
+  const float wcf = (float)P.wc;
+  const int f0 = __ldg(P.gca_off + g), f1 = __ldg(P.gca_off + g + 1);
+  for (int f = f0; f < f1; ++f) {
+    const float4 V = __ldcg(P.gcv + f);
+    float C[12];
+    ld12cg(P.zc, __ldg(P.gca + f), C);
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-  return v;
+    for (int c = 0; c < 3; ++c)
+      u[c] = fmaf(wcf, fmaf(V.x, C[c], fmaf(V.y, C[3 + c], fmaf(V.z, C[6 + c], V.w * C[9 + c]))), u[c]);
+  }
+}
+
+// w_con J_g u_f of group g (u_f = Dinv r in P.z); one warp, lane 0 stores it.
+__device__ __forceinline__ void con_jz_group(const SolveParams& P, int g) {
+  const int lane = threadIdx.x & 31;
+  const int k = P.k;
+  const int s0 = __ldg(P.grp_off + g) * k, s1 = __ldg(P.grp_off + g + 1) * k;
+  float u[3] = {0.f, 0.f, 0.f};
+  for (int slot = s0 + lane; slot < s1; slot += 32) {
+    const int rk = __ldg(P.mem_rank + slot);
+    if (rk < 0) continue;
+    const float4 geo = __ldcg(P.mem_geo + slot);
+    float zl[12];
+    ld12cg(P.z, rk, zl);
+#pragma unroll
+    for (int c = 0; c < 3; ++c)
+      u[c] = fmaf(geo.x, fmaf(geo.y, zl[c], fmaf(geo.z, zl[3 + c], fmaf(geo.w, zl[6 + c], zl[9 + c]))), u[c]);
+  }
+  const float wcf = (float)P.wc;
+#pragma unroll
+  for (int c = 0; c < 3; ++c) u[c] = wcf * warp_sum(u[c]);
+  if (lane == 0) P.uzg[g] = make_float4(u[0], u[1], u[2], 0.f);
 }
 
 // 4x4 symmetric accumulator index (a <= b).
@@ -356,11 +378,11 @@ __device__ void residual_node(const SolveParams& P, int r, RT scale, RT (&acc)[1
   energy = warp_sum(e);
 }
 
-// q = (J^T J p)_r for free node r, computed by one half-warp (16 lanes); also
-// returns this node's p in every lane of the half.  A half with valid == false
-// does no loads but takes part in the warp shuffles.
-__device__ void spmv_node(const SolveParams& P, int r, bool valid, bool first, float beta, const float* pold,
-                          float (&acc)[12], float (&pj)[12]) {
+// w = (J^T J u)_r for free node r, computed by one half-warp (16 lanes), with
+// u formed on the fly for every node it touches; also returns this node's u in
+// every lane of the half.  A half with valid == false does no loads but takes
+// part in the warp shuffles.
+__device__ void spmv_node(const SolveParams& P, int r, bool valid, float (&acc)[12], float (&pj)[12]) {
   const int lane = threadIdx.x & 15;
 #pragma unroll
   for (int i = 0; i < 12; ++i) {
@@ -371,7 +393,7 @@ __device__ void spmv_node(const SolveParams& P, int r, bool valid, bool first, f
   const int j = __ldg(P.free_ids + r);
   const float gj[3] = {__ldg(P.node_pos + 3 * (size_t)j), __ldg(P.node_pos + 3 * (size_t)j + 1),
                        __ldg(P.node_pos + 3 * (size_t)j + 2)};
-  load_p(P, r, P.NA ? __ldg(P.agg + r) : 0, first, beta, pold, pj);
+  load_u(P, r, P.NA ? __ldg(P.agg + r) : 0, pj);
   const float w = (float)P.wg;
   const int b0 = __ldg(P.item_off + r), b1 = __ldg(P.item_off + r + 1);
   for (int it = b0 + lane; it < b1; it += 16) {
@@ -382,7 +404,7 @@ __device__ void spmv_node(const SolveParams& P, int r, bool valid, bool first, f
                           __ldg(P.node_pos + 3 * (size_t)m.z + 1) - gj[1],
                           __ldg(P.node_pos + 3 * (size_t)m.z + 2) - gj[2]};
       float pk[3] = {0.f, 0.f, 0.f};
-      if (m.y >= 0) load_pt(P, m.y, m.x >> 4, first, beta, pold, pk);
+      if (m.y >= 0) load_ut(P, m.y, m.x >> 4, pk);
 #pragma unroll
       for (int c = 0; c < 3; ++c) {
         const float u = ws * fmaf(pj[c], d[0], fmaf(pj[3 + c], d[1], pj[6 + c] * d[2])) + w * pj[9 + c] - ws * pk[c];
@@ -397,7 +419,7 @@ __device__ void spmv_node(const SolveParams& P, int r, bool valid, bool first, f
                           gj[1] - __ldg(P.node_pos + 3 * (size_t)m.z + 1),
                           gj[2] - __ldg(P.node_pos + 3 * (size_t)m.z + 2)};
       float pi[12];
-      load_p(P, m.y, m.x >> 4, first, beta, pold, pi);
+      load_u(P, m.y, m.x >> 4, pi);
 #pragma unroll
       for (int c = 0; c < 3; ++c) {
         const float u = ws * fmaf(pi[c], d[0], fmaf(pi[3 + c], d[1], pi[6 + c] * d[2])) + w * pi[9 + c] - ws * pj[9 + c];
@@ -408,7 +430,10 @@ __device__ void spmv_node(const SolveParams& P, int r, bool valid, bool first, f
       for (int c = 0; c < 3; ++c) acc[9 + c] = fmaf(w * w, pj[9 + c], acc[9 + c]);
     } else {
       float u[3];
-      con_jp(P, m.z, first, beta, pold, u);
+      if (P.NA)
+        con_ju_coarse(P, m.z, u);
+      else
+        con_ju(P, m.z, u);
       const float4 geo = __ldcg(P.mem_geo + m.y);
       const float wa = (float)P.wc * geo.x;
 #pragma unroll

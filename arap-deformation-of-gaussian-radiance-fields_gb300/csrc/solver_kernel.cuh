@@ -8,12 +8,17 @@
 
 namespace arap {
 
-// stats slots written by CTA 0; ST_T_* are nanoseconds spent in each phase
-// (global timer, read by thread 0 of CTA 0 after the phase's barrier)
+// stats slots written by CTA 0; ST_T_PREP..ST_T_CINV are nanoseconds spent in
+// each phase (global timer, read by thread 0 of CTA 0 after the phase's
+// barrier); ST_T_W_* are the largest per-CTA sums of work time inside PCG
+// (from leaving one barrier to entering the next), combined with atomicMax
+// on the bit patterns of non-negative doubles.
 enum {
   ST_ITERS = 0, ST_PCG = 1, ST_HALV = 2, ST_E0 = 3, ST_E = 4, ST_CONV = 5, ST_NONFINITE = 6,
-  ST_T_PREP = 8, ST_T_GRAD = 9, ST_T_COARSE = 10, ST_T_PCG = 11, ST_T_LS = 12
+  ST_T_PREP = 8, ST_T_GRAD = 9, ST_T_COARSE = 10, ST_T_PCG = 11, ST_T_LS = 12, ST_T_CINV = 13,
+  ST_T_W_SPMV = 14, ST_T_W_UPD = 15, ST_T_W_CSOLVE = 16
 };
+constexpr int kStatSlots = 24;
 
 __device__ __forceinline__ unsigned long long global_ns() {
   unsigned long long t;
@@ -21,133 +26,183 @@ __device__ __forceinline__ unsigned long long global_ns() {
   return t;
 }
 
-template <int N>
-__device__ __forceinline__ bool reduce_all(const SolveParams& P, double (&v)[N], double (&out)[N]) {
-  block_sum<N>(v);
-  return grid_sync_reduce<N>(P.bar, P.partials, P.results, v, out);
-}
+// Shared scratch of the persistent kernel, reused phase by phase (phases are
+// separated by grid barriers, which include __syncthreads).
+constexpr int kGJRows = 8;  // rows of a CTA's strip handled together
+constexpr int kScratchFloats = 2 * kGJBlock * (kGJBlock + 1) + kGJRows * (kGJBlock + 1) + kGJRows * kGJBlock;
+static_assert(kScratchFloats >= kSolveWarps * 144, "scratch holds the 12x12 blocks");
+static_assert(kScratchFloats >= kMaxCoarse, "scratch holds the restricted residual");
 
 // Inverse of the coarse matrix in Cw[0] by blocked Gauss-Jordan (float32, no
 // pivoting: the matrix is symmetric positive definite).  For each pivot block
-// K: CTA 0 inverts A_KK in shared memory; every CTA forms W = A_:K A_KK^-1;
-// then A_KK <- A_KK^-1, A_Kj <- A_KK^-1 A_Kj, A_iK <- -W_iK,
-// A_ij <- A_ij - W_iK A_Kj.  Three grid barriers per block.  Returns false on a
-// barrier failure; *ok = 0 when a pivot block was not positive definite.
-__device__ bool coarse_invert(const SolveParams& P, int* ok) {
-  __shared__ float s_piv[kGJBlock][kGJBlock + 1];
-  __shared__ float s_row[kGJBlock], s_col[kGJBlock];
-  __shared__ int s_bad;
+// K (kGJBlock wide, the last one padded with the identity), every CTA inverts
+// A_KK in its own shared memory (ping-pong copies, one __syncthreads per step;
+// the same arithmetic in every CTA, so the same bits), then updates its own
+// strip of rows:
+//   A_KK <- A_KK^-1, A_Kj <- A_KK^-1 A_Kj, A_iK <- -W_iK,
+//   A_ij <- A_ij - W_iK A_Kj,  W = A_iK A_KK^-1,
+// with W of the strip in shared memory and the column A_Kj streamed from L2 in
+// one batch per column.  Reads Cw[src] and writes Cw[1-src] (Cinv for the
+// last block), so one grid barrier per block suffices.  Returns false on a
+// barrier failure; *ok = 0 when a pivot was not positive.
+__device__ bool coarse_invert(const SolveParams& P, GridSync& gs, int* ok, float* sm) {
+  constexpr int KB = kGJBlock, KP = kGJBlock + 1;
+  float(*pv0)[KP] = reinterpret_cast<float(*)[KP]>(sm);
+  float(*pv1)[KP] = reinterpret_cast<float(*)[KP]>(sm + KB * KP);
+  float(*wrow)[KP] = reinterpret_cast<float(*)[KP]>(sm + 2 * KB * KP);
+  // per strip row: -W_iK, or the row of A_KK^-1 for rows inside K (16-byte rows)
+  float(*wsel)[KB] = reinterpret_cast<float(*)[KB]>(sm + 2 * KB * KP + kGJRows * KP);
+  static_assert((2 * kGJBlock * (kGJBlock + 1) + kGJRows * (kGJBlock + 1)) % 4 == 0 && kGJBlock % 4 == 0,
+                "float4 rows");
   const int NC = P.NC;
   const size_t NC2 = (size_t)NC * NC;
-  const int gt = blockIdx.x * blockDim.x + threadIdx.x;
-  const int nt = gridDim.x * blockDim.x;
+  const int tid = threadIdx.x, bd = blockDim.x;
+  const int R = (NC + gridDim.x - 1) / gridDim.x;
+  const int r_begin = min(NC, (int)blockIdx.x * R), r_end = min(NC, r_begin + R);
   int src_i = 0;
   *ok = 1;
-  for (int K0 = 0; K0 < NC; K0 += kGJBlock) {
-    const int kb = min(kGJBlock, NC - K0);
+  for (int K0 = 0; K0 < NC; K0 += KB) {
+    const int kb = min(KB, NC - K0);
     const float* src = P.Cw + src_i * NC2;
-    float* dst = P.Cw + (1 - src_i) * NC2;
-    const bool last = K0 + kb >= NC;
-    double bad[1] = {0.0}, obad[1];
-    if (blockIdx.x == 0) {
-      if (threadIdx.x == 0) s_bad = 0;
-      for (int t = threadIdx.x; t < kb * kb; t += blockDim.x)
-        s_piv[t / kb][t % kb] = __ldcg(src + (size_t)(K0 + t / kb) * NC + K0 + t % kb);
-      for (int m = 0; m < kb; ++m) {
-        __syncthreads();
-        if (threadIdx.x < kb) {
-          s_row[threadIdx.x] = s_piv[m][threadIdx.x];
-          s_col[threadIdx.x] = s_piv[threadIdx.x][m];
-        }
-        __syncthreads();
-        const float pv = s_row[m];
-        if (!(pv > 0.f)) {
-          if (threadIdx.x == 0) s_bad = 1;
-          continue;
-        }
-        const float ip = 1.f / pv;
-        for (int t = threadIdx.x; t < kb * kb; t += blockDim.x) {
-          const int i = t / kb, j = t % kb;
+    float* dst = (K0 + kb >= NC) ? P.Cinv : P.Cw + (1 - src_i) * NC2;
+    for (int t = tid; t < KB * KB; t += bd) {
+      const int i = t / KB, j = t % KB;
+      pv0[i][j] = (i < kb && j < kb) ? __ldcg(src + (size_t)(K0 + i) * NC + K0 + j) : (i == j ? 1.f : 0.f);
+    }
+    __syncthreads();
+    int bad = 0;
+    for (int m = 0; m < KB; ++m) {
+      float(*cur)[KP] = (m & 1) ? pv1 : pv0;
+      float(*nxt)[KP] = (m & 1) ? pv0 : pv1;
+      const float pvt = cur[m][m];
+      bad |= !(pvt > 0.f);
+      const float ip = 1.f / pvt;
+#pragma unroll
+      for (int q = 0; q < (KB * KB + kSolveThreads - 1) / kSolveThreads; ++q) {
+        const int t = tid + q * kSolveThreads;
+        if (t < KB * KB) {
+          const int i = t / KB, j = t % KB;
+          const float cim = cur[i][m], cmj = cur[m][j];
           float v;
-          if (i == m && j == m)
-            v = ip;
-          else if (i == m)
-            v = s_row[j] * ip;
+          if (i == m)
+            v = (j == m) ? ip : cmj * ip;
           else if (j == m)
-            v = -s_col[i] * ip;
+            v = -cim * ip;
           else
-            v = s_piv[i][j] - s_col[i] * s_row[j] * ip;
-          s_piv[i][j] = v;
+            v = fmaf(-cim * ip, cmj, cur[i][j]);
+          nxt[i][j] = v;
         }
       }
       __syncthreads();
-      for (int t = threadIdx.x; t < kb * kb; t += blockDim.x) P.Pgj[t] = s_piv[t / kb][t % kb];
-      bad[0] = s_bad;
     }
-    if (!grid_sync_reduce<1>(P.bar, P.partials, P.results, bad, obad)) return false;
-    if (obad[0] != 0.0) *ok = 0;
-    for (size_t e = gt; e < (size_t)NC * kb; e += nt) {
-      const int i = (int)(e / kb), n = (int)(e % kb);
-      if (i >= K0 && i < K0 + kb) continue;
-      float w = 0.f;
-      for (int m = 0; m < kb; ++m) w = fmaf(__ldcg(src + (size_t)i * NC + K0 + m), __ldcg(P.Pgj + m * kb + n), w);
-      P.Wgj[(size_t)i * kb + n] = w;
-    }
-    double d0[1] = {0.0}, o0[1];
-    if (!grid_sync_reduce<1>(P.bar, P.partials, P.results, d0, o0)) return false;
-    for (size_t e = gt; e < NC2; e += nt) {
-      const int i = (int)(e / NC), j = (int)(e % NC);
-      const int iK = i - K0, jK = j - K0;
-      const bool inI = iK >= 0 && iK < kb, inJ = jK >= 0 && jK < kb;
-      float v;
-      if (inI && inJ) {
-        v = __ldcg(P.Pgj + iK * kb + jK);
-      } else if (inI) {
-        v = 0.f;
-        for (int m = 0; m < kb; ++m) v = fmaf(__ldcg(P.Pgj + iK * kb + m), __ldcg(src + (size_t)(K0 + m) * NC + j), v);
-      } else if (inJ) {
-        v = -__ldcg(P.Wgj + (size_t)i * kb + jK);
-      } else {
-        v = __ldcg(src + e);
-        for (int m = 0; m < kb; ++m) v = fmaf(-__ldcg(P.Wgj + (size_t)i * kb + m), __ldcg(src + (size_t)(K0 + m) * NC + j), v);
+    static_assert(kGJBlock % 2 == 0, "the inverse ends in pv0");
+    if (__syncthreads_or(bad)) *ok = 0;
+    for (int r0 = r_begin; r0 < r_end; r0 += kGJRows) {
+      const int nr = min(kGJRows, r_end - r0);
+      for (int t = tid; t < kGJRows * KB; t += bd) {
+        const int rr = t / KB, m = t % KB;
+        wrow[rr][m] = (rr < nr && m < kb) ? __ldcg(src + (size_t)(r0 + rr) * NC + K0 + m) : 0.f;
       }
-      if (last)
-        P.Cinv[e] = v;
-      else
-        dst[e] = v;
+      __syncthreads();
+      float wv = 0.f;
+      if (tid < kGJRows * KB) {
+        const int rr = tid / KB, n = tid % KB;
+#pragma unroll 16
+        for (int m = 0; m < KB; ++m) wv = fmaf(wrow[rr][m], pv0[m][n], wv);
+      }
+      if (tid < kGJRows * KB) {
+        const int rr = tid / KB, n = tid % KB;
+        const int iK = r0 + rr - K0;
+        wsel[rr][n] = (iK >= 0 && iK < kb) ? pv0[iK][n] : -wv;
+      }
+      __syncthreads();
+      for (int j = tid; j < NC; j += bd) {
+        const int jK = j - K0;
+        const bool inJ = jK >= 0 && jK < kb;
+        float out[kGJRows];
+        if (inJ) {
+          // A_KK^-1 inside the pivot block, -W_iK elsewhere: both are in wsel
+#pragma unroll
+          for (int rr = 0; rr < kGJRows; ++rr) out[rr] = wsel[rr][jK];
+        } else {
+          float akj[KB];
+#pragma unroll
+          for (int m = 0; m < KB; ++m) akj[m] = m < kb ? __ldcg(src + (size_t)(K0 + m) * NC + j) : 0.f;
+#pragma unroll
+          for (int rr = 0; rr < kGJRows; ++rr) {
+            const int iK = r0 + rr - K0;
+            const bool inI = iK >= 0 && iK < kb;
+            float v = (inI || rr >= nr) ? 0.f : __ldcg(src + (size_t)(r0 + rr) * NC + j);
+            const float4* w4 = reinterpret_cast<const float4*>(&wsel[rr][0]);
+#pragma unroll
+            for (int m4 = 0; m4 < KB / 4; ++m4) {
+              const float4 ww = w4[m4];
+              v = fmaf(ww.x, akj[4 * m4], v);
+              v = fmaf(ww.y, akj[4 * m4 + 1], v);
+              v = fmaf(ww.z, akj[4 * m4 + 2], v);
+              v = fmaf(ww.w, akj[4 * m4 + 3], v);
+            }
+            out[rr] = v;
+          }
+        }
+#pragma unroll
+        for (int rr = 0; rr < kGJRows; ++rr)
+          if (rr < nr) dst[(size_t)(r0 + rr) * NC + j] = out[rr];
+      }
+      __syncthreads();
     }
-    if (!grid_sync_reduce<1>(P.bar, P.partials, P.results, d0, o0)) return false;
+    if (!gs.sync()) return false;
     src_i ^= 1;
   }
   return true;
 }
 
-// zc = Cinv rc (one warp per row), zero the other restriction buffer, and
-// this thread's share of rc . zc.
-__device__ __forceinline__ bool coarse_solve(const SolveParams& P, const double* rc, double* rc_other,
-                                             double (&part)[1], int ok) {
+// zc = Cinv rc (one warp per row, the row loaded as float4s in one batch, rc
+// staged in shared memory), zero the other restriction buffer, and the group
+// products w_con J_g u_f.  Every thread of the CTA calls it.
+constexpr int kRowVec = (kMaxCoarse / 4 + 31) / 32;  // float4 loads per lane of a row
+__device__ __forceinline__ void coarse_solve(const SolveParams& P, const double* rc, double* rc_other, int ok,
+                                             float* s_rc) {
   const int lane = threadIdx.x & 31;
   const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int nw = (gridDim.x * blockDim.x) >> 5;
-  const int NC = P.NC;
+  const int NC = P.NC, n4 = NC / 4;
+  for (int e = threadIdx.x; e < NC; e += blockDim.x) s_rc[e] = (float)__ldcg(rc + e);
+  __syncthreads();
+  const float4* s4 = reinterpret_cast<const float4*>(s_rc);
   for (int i = gw; i < NC; i += nw) {
     double acc = 0.0;
-    const float* row = P.Cinv + (size_t)i * NC;
-    if (ok)
-      for (int j = lane; j < NC; j += 32) acc += (double)__ldcg(row + j) * __ldcg(rc + j);
-    acc = warp_sum(acc);
-    if (lane == 0) {
-      P.zc[i] = (float)acc;
-      part[0] += __ldcg(rc + i) * acc;
+    if (ok) {
+      const float4* row = reinterpret_cast<const float4*>(P.Cinv + (size_t)i * NC);
+      float4 v[kRowVec];
+#pragma unroll
+      for (int q = 0; q < kRowVec; ++q) {
+        const int c = lane + 32 * q;
+        v[q] = c < n4 ? __ldcg(row + c) : make_float4(0.f, 0.f, 0.f, 0.f);
+      }
+      float a = 0.f;
+#pragma unroll
+      for (int q = 0; q < kRowVec; ++q) {
+        const int c = lane + 32 * q;
+        if (c < n4) {
+          const float4 r4 = s4[c];
+          a = fmaf(v[q].x, r4.x, fmaf(v[q].y, r4.y, fmaf(v[q].z, r4.z, fmaf(v[q].w, r4.w, a))));
+        }
+      }
+      acc = (double)a;
     }
+    acc = warp_sum(acc);
+    if (lane == 0) P.zc[i] = (float)acc;
   }
   for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < NC; e += gridDim.x * blockDim.x) rc_other[e] = 0.0;
-  return true;
+  // w_con J_g u_f for the next products, on the warps the rows leave idle
+  for (int g = nw - 1 - gw; g < P.G; g += nw) con_jz_group(P, g);
 }
 
 template <typename RT>
 __global__ void __launch_bounds__(kSolveThreads) gn_solve_kernel(SolveParams P) {
-  __shared__ float s_D[kSolveWarps][144];
+  __shared__ __align__(16) float s_scratch[kScratchFloats];
+  float* const s_D = s_scratch;  // [kSolveWarps][144] during the gradient pass
   const int lane = threadIdx.x & 31;
   const int wib = threadIdx.x >> 5;
   const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -155,8 +210,31 @@ __global__ void __launch_bounds__(kSolveThreads) gn_solve_kernel(SolveParams P) 
   const int gt = blockIdx.x * blockDim.x + threadIdx.x;
   const int nt = gridDim.x * blockDim.x;
   const int F = P.F, k = P.k;
+  GridSync gs{P.bar, P.partials, 0u};
   unsigned long long t_mark = global_ns();
-  double t_acc[5] = {0.0, 0.0, 0.0, 0.0, 0.0};  // prep, grad, coarse, pcg, line search
+  double t_acc[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};  // prep, grad, coarse, pcg, line search, inversion
+  // PCG work of this CTA per phase kind (products, update, coarse solve): from
+  // leaving a barrier to the last warp of the CTA finishing its share (each
+  // warp posts its finish time; thread 0 reads the latest after the barrier)
+  __shared__ unsigned long long s_wend;
+  unsigned long long t_work[3] = {0ull, 0ull, 0ull};
+  unsigned long long t_w0 = 0ull;
+  int w_pend = -1;
+  if (threadIdx.x == 0) s_wend = 0ull;
+  auto work_flush = [&]() {
+    if (threadIdx.x == 0 && w_pend >= 0) {
+      t_work[w_pend] += s_wend - t_w0;
+      w_pend = -1;
+    }
+  };
+  auto work_begin = [&]() {
+    work_flush();
+    if (threadIdx.x == 0) t_w0 = global_ns();
+  };
+  auto work_end = [&](int slot) {
+    if (lane == 0) atomicMax(&s_wend, global_ns());
+    if (threadIdx.x == 0) w_pend = slot;
+  };
   auto lap = [&](int slot) {
     const unsigned long long now = global_ns();
     t_acc[slot] += (double)(now - t_mark);
@@ -201,17 +279,38 @@ __global__ void __launch_bounds__(kSolveThreads) gn_solve_kernel(SolveParams P) 
     for (int e = gt; e < P.NA * P.NA * 16; e += nt) P.Qd[e] = 0.0;
     for (int e = gt; e < 2 * P.NC; e += nt) P.rc[e] = 0.0;
     for (int e = gt; e < 2 * P.NA * 81; e += nt) P.rotagg[e] = 0.0;
+    // V_ga of every group and aggregate of its free anchors
+    for (int g = gt; g < P.G; g += nt) {
+      const int s0 = P.grp_off[g], s1 = P.grp_off[g + 1];
+      for (int f = P.gca_off[g]; f < P.gca_off[g + 1]; ++f) {
+        const int a = P.gca[f];
+        const int pv = P.pivot[a];
+        float4 V = make_float4(0.f, 0.f, 0.f, 0.f);
+        for (int u = s0; u < s1; ++u) {
+          const int c = P.grp_member[u];
+          for (int t = 0; t < k; ++t) {
+            const int slot = u * k + t;
+            const int rk = P.mem_rank[slot];
+            if (rk < 0 || P.agg[rk] != a) continue;
+            const float w = P.mem_w[slot];
+            V.x = fmaf(w, P.node_pos[3 * c] - P.node_pos[3 * pv], V.x);
+            V.y = fmaf(w, P.node_pos[3 * c + 1] - P.node_pos[3 * pv + 1], V.y);
+            V.z = fmaf(w, P.node_pos[3 * c + 2] - P.node_pos[3 * pv + 2], V.z);
+            V.w += w;
+          }
+        }
+        P.gcv[f] = V;
+      }
+    }
   }
-  {
-    double d0[1] = {0.0}, o0[1];
-    if (!grid_sync_reduce<1>(P.bar, P.partials, P.results, d0, o0)) return;
-  }
+  if (gt == 0)
+    for (int q = ST_T_W_SPMV; q <= ST_T_W_CSOLVE; ++q) P.stats[q] = 0.0;
+  if (!gs.sync()) return;
   if (coarse) {
     // coarse matrix P^T (J^T J at x = I) P, fixed for this solve
     for (int oi = gw; oi < F; oi += nw) coarse_rows_node(P, __ldg(P.order + oi));
     for (int g = gt; g < P.G; g += nt) coarse_rows_group(P, g);
-    double d0[1] = {0.0}, o0[1];
-    if (!grid_sync_reduce<1>(P.bar, P.partials, P.results, d0, o0)) return;
+    if (!gs.sync()) return;
   }
 
   lap(0);
@@ -219,7 +318,7 @@ __global__ void __launch_bounds__(kSolveThreads) gn_solve_kernel(SolveParams P) 
   int iters = 0, pcg_total = 0, halvings = 0, converged = 0;
   for (int it = 0; it < P.max_iters; ++it) {
     // ---- gradient -J^T f, energy, preconditioner, PCG start (h=0, r=g, z=M^-1 g)
-    double red[4] = {0.0, 0.0, 0.0, 0.0}, out[4];
+    double red[3] = {0.0, 0.0, 0.0};
     for (int oi = gw; oi < F; oi += nw) {
       const int r = __ldg(P.order + oi);
       RT acc[12];
@@ -237,7 +336,7 @@ __global__ void __launch_bounds__(kSolveThreads) gn_solve_kernel(SolveParams P) 
         }
         continue;
       }
-      build_dinv(P, r, Q, s_D[wib]);
+      build_dinv(P, r, Q, s_D + 144 * wib);
       if (coarse) coarse_rot_node(P, r, P.rotagg + (it & 1) * 81 * P.NA);
       float gc = 0.f;
 #pragma unroll
@@ -247,12 +346,10 @@ __global__ void __launch_bounds__(kSolveThreads) gn_solve_kernel(SolveParams P) 
       if (coarse) coarse_restrict(P, r, gc, P.rc);
       if (lane < 12) {
         const size_t o = 12 * (size_t)r + lane;
-        P.g[o] = gc;
         P.r[o] = gc;
         P.z[o] = zc;
         P.h[o] = 0.f;
-        red[2] += (double)gc * (double)zc;
-        red[3] += (double)gc * (double)gc;
+        red[2] += (double)gc * (double)gc;
       }
     }
     for (int g = gt; g < P.G; g += nt) {
@@ -264,10 +361,10 @@ __global__ void __launch_bounds__(kSolveThreads) gn_solve_kernel(SolveParams P) 
       const double v = __ldcg(P.x + e);
       red[1] += v * v;
     }
-    if (!reduce_all<4>(P, red, out)) return;
+    if (!gs.reduce<3>(red)) return;
     lap(1);
-    const double e_old = out[0];
-    const double normv = sqrt(out[1]);
+    const double e_old = red[0];
+    const double normv = sqrt(red[1]);
     if (it == 0) e_first = e_old;
     e_last = e_old;
     if (P.mode == 1) {
@@ -275,10 +372,14 @@ __global__ void __launch_bounds__(kSolveThreads) gn_solve_kernel(SolveParams P) 
       return;
     }
 
-    // ---- PCG on (J^T J) h = g: two barriers per iteration, plus one for the
-    // coarse solve when the two-level preconditioner is on
-    double rz = out[2];
-    const double rr0 = out[3];
+    // ---- PCG on (J^T J) h = g in the Chronopoulos-Gear form, one reduction
+    // per iteration:
+    //   (1) p = u + beta p, s = w + beta s, h += alpha p, r -= alpha s,
+    //       u_f = Dinv r and its restriction P^T r; plain barrier
+    //   (2) two-level only: zc = Cinv P^T r and w_con J_g u_f; plain barrier
+    //   (3) u = u_f + P zc, w = (J^T J) u; gamma = r.u, delta = w.u, r.r
+    //   beta = gamma / gamma_old, alpha = gamma / (delta - beta gamma / alpha_old)
+    const double rr0 = red[2];
     double rr = rr0;
     int coarse_ok = 0;
     if (coarse) {
@@ -288,87 +389,116 @@ __global__ void __launch_bounds__(kSolveThreads) gn_solve_kernel(SolveParams P) 
       const size_t NC2 = (size_t)P.NC * P.NC;
       for (size_t e = gt; e < NC2; e += nt) P.Cw[e] = coarse_entry_x(P, rot_now, (int)(e / P.NC), (int)(e % P.NC));
       for (int e = gt; e < 81 * P.NA; e += nt) rot_next[e] = 0.0;
-      double d0[1] = {0.0}, o0[1];
-      if (!grid_sync_reduce<1>(P.bar, P.partials, P.results, d0, o0)) return;
-      if (!coarse_invert(P, &coarse_ok)) return;
+      if (!gs.sync()) return;
+      const unsigned long long t_inv = global_ns();
+      if (!coarse_invert(P, gs, &coarse_ok, s_scratch)) return;
+      t_acc[5] += (double)(global_ns() - t_inv);
       if (!coarse_ok && gt == 0) raise_status(ARAP_ENONFINITE);
       lap(2);
     }
-    if (coarse) {
-      double rzc[1] = {0.0}, orc[1];
-      if (!coarse_solve(P, P.rc, P.rc + P.NC, rzc, coarse_ok)) return;
-      if (!reduce_all<1>(P, rzc, orc)) return;
-      rz += orc[0];
-    }
     const double tol2 = (double)P.pcg_tol * (double)P.pcg_tol * rr0;
-    float beta = 0.f;
-    int pi = 0;
     const int half = lane >> 4, l16 = lane & 15;
     const int nhw = 2 * nw;
-    while (rr > tol2 && pi < P.pcg_max && rz > 0.0) {
-      const bool first = pi == 0;
-      float* pcur = (pi & 1) ? P.p1 : P.p0;
-      const float* pold = (pi & 1) ? P.p0 : P.p1;
-      double pq[1] = {0.0}, opq[1];
+    // products: u = u_f + P zc (formed on the fly for every node a product
+    // touches), w = (J^T J) u, and gamma = r.u, delta = w.u, r.r in one
+    // reduction
+    auto products = [&](double (&s3)[3]) -> bool {
+      s3[0] = s3[1] = s3[2] = 0.0;
+      work_begin();
       for (int base = 2 * gw; base < F; base += nhw) {
         const int oi = base + half;
         const bool valid = oi < F;
         const int r = valid ? __ldg(P.order + oi) : 0;
-        float acc[12], pj[12];
-        spmv_node(P, r, valid, first, beta, pold, acc, pj);
+        float acc[12], uj[12];
+        spmv_node(P, r, valid, acc, uj);
         if (valid && l16 < 12) {
-          float pc = 0.f, qc = 0.f;
+          float uc = 0.f, wv = 0.f;
 #pragma unroll
           for (int i = 0; i < 12; ++i)
             if (i == l16) {
-              pc = pj[i];
-              qc = acc[i];
+              uc = uj[i];
+              wv = acc[i];
             }
           const size_t o = 12 * (size_t)r + l16;
-          pcur[o] = pc;
-          P.q[o] = qc;
-          pq[0] += (double)pc * (double)qc;
+          const float rv = __ldcg(P.r + o);
+          P.u[o] = uc;
+          P.q[o] = wv;
+          s3[0] += (double)rv * (double)uc;
+          s3[1] += (double)wv * (double)uc;
+          s3[2] += (double)rv * (double)rv;
         }
       }
-      if (!reduce_all<1>(P, pq, opq)) return;
-      if (!(opq[0] > 0.0)) break;
-      const float alpha = (float)(rz / opq[0]);
-      double* rc_next = P.rc + ((pi + 1) & 1) * P.NC;
-      double rzr[2] = {0.0, 0.0}, orz[2];
+      work_end(0);
+      return gs.reduce<3>(s3);
+    };
+    int cur = 0;  // rc buffer holding P^T r of the current residual
+    if (coarse) {
+      work_begin();
+      coarse_solve(P, P.rc, P.rc + P.NC, coarse_ok, s_scratch);
+      work_end(2);
+      if (!gs.sync()) return;
+    }
+    double s3[3];
+    if (!products(s3)) return;
+    double gam = s3[0];
+    rr = s3[2];
+    double alpha_d = s3[1] > 0.0 ? gam / s3[1] : 0.0;
+    float beta = 0.f;
+    int pi = 0;
+    bool go = rr > tol2 && gam > 0.0 && s3[1] > 0.0;
+    while (go && pi < P.pcg_max) {
+      // p = u + beta p, s = w + beta s (s = (J^T J) p), h += alpha p,
+      // r -= alpha s, u_f = Dinv r and its restriction
+      const float alpha = (float)alpha_d;
+      const bool first = pi == 0;
+      double* rc_next = P.rc + (cur ^ 1) * P.NC;
+      work_begin();
       for (int base = 2 * gw; base < F; base += nhw) {
         const int oi = base + half;
         const bool valid = oi < F;
         const int r = valid ? __ldg(P.order + oi) : 0;
-        float rc = 0.f;
+        float rv = 0.f;
         if (valid && l16 < 12) {
           const size_t o = 12 * (size_t)r + l16;
-          P.h[o] = fmaf(alpha, __ldcg(pcur + o), __ldcg(P.h + o));
-          rc = fmaf(-alpha, __ldcg(P.q + o), __ldcg(P.r + o));
-          P.r[o] = rc;
+          const float uo = __ldcg(P.u + o), wo = __ldcg(P.q + o);
+          const float pn = first ? uo : fmaf(beta, __ldcg(P.p0 + o), uo);
+          const float sn = first ? wo : fmaf(beta, __ldcg(P.p1 + o), wo);
+          P.p0[o] = pn;
+          P.p1[o] = sn;
+          P.h[o] = fmaf(alpha, pn, __ldcg(P.h + o));
+          rv = fmaf(-alpha, sn, __ldcg(P.r + o));
+          P.r[o] = rv;
         }
-        const float zc = apply_dinv_h(P, r, valid, rc);
-        if (coarse) coarse_restrict_h(P, r, valid, rc, rc_next);
-        if (valid && l16 < 12) {
-          P.z[12 * (size_t)r + l16] = zc;
-          rzr[0] += (double)rc * (double)zc;
-          rzr[1] += (double)rc * (double)rc;
-        }
+        const float zv = apply_dinv_h(P, r, valid, rv);
+        if (coarse) coarse_restrict_h(P, r, valid, rv, rc_next);
+        if (valid && l16 < 12) P.z[12 * (size_t)r + l16] = zv;
       }
-      if (!reduce_all<2>(P, rzr, orz)) return;
+      work_end(1);
+      if (!gs.sync()) return;
       ++pi;
-      rr = orz[1];
-      if (rr <= tol2 || pi >= P.pcg_max) break;
-      double rz_new = orz[0];
+      cur ^= 1;
       if (coarse) {
-        double rzc[1] = {0.0}, orc[1];
-        if (!coarse_solve(P, rc_next, P.rc + (pi & 1 ? 0 : 1) * P.NC, rzc, coarse_ok)) return;
-        if (!reduce_all<1>(P, rzc, orc)) return;
-        rz_new += orc[0];
+        work_begin();
+        coarse_solve(P, P.rc + cur * P.NC, P.rc + (cur ^ 1) * P.NC, coarse_ok, s_scratch);
+        work_end(2);
+        if (!gs.sync()) return;
       }
-      beta = (float)(rz_new / rz);
-      rz = rz_new;
+      if (!products(s3)) return;
+      rr = s3[2];
+      if (rr <= tol2 || pi >= P.pcg_max) break;
+      const double gam_new = s3[0];
+      const double bd = gam_new / gam;
+      const double den = s3[1] - bd * gam_new / alpha_d;
+      if (!(gam_new > 0.0) || !(den > 0.0)) break;
+      beta = (float)bd;
+      alpha_d = gam_new / den;
+      gam = gam_new;
     }
+    // both restriction buffers start the next gradient pass at zero
+    if (coarse)
+      for (int e = gt; e < 2 * P.NC; e += nt) P.rc[e] = 0.0;
     pcg_total += pi;
+    work_flush();
     lap(3);
 
     // ---- line search: x + 2^-m h, m = 0..49 (Deform.cpp:144-156)
@@ -376,7 +506,7 @@ __global__ void __launch_bounds__(kSolveThreads) gn_solve_kernel(SolveParams P) 
     bool accepted = false;
     double hh = 0.0;
     for (int ls = 0; ls < 50; ++ls) {
-      double en2[2] = {0.0, 0.0}, oen[2];
+      double en2[2] = {0.0, 0.0};
       for (int oi = gw; oi < F; oi += nw) {
       const int r = __ldg(P.order + oi);
         RT acc[12];
@@ -396,14 +526,14 @@ __global__ void __launch_bounds__(kSolveThreads) gn_solve_kernel(SolveParams P) 
           en2[1] += v * v;
         }
       }
-      if (!reduce_all<2>(P, en2, oen)) return;
-      if (ls == 0) hh = oen[1];
-      if (oen[0] > e_old) {
+      if (!gs.reduce<2>(en2)) return;
+      if (ls == 0) hh = en2[1];
+      if (en2[0] > e_old) {
         scale *= RT(0.5);
         ++halvings;
       } else {
         accepted = true;
-        e_last = oen[0];
+        e_last = en2[0];
         break;
       }
     }
@@ -416,10 +546,7 @@ __global__ void __launch_bounds__(kSolveThreads) gn_solve_kernel(SolveParams P) 
     }
     const double normh = (double)scale * sqrt(hh);
     iters = it + 1;
-    {
-      double d0[1] = {0.0}, o0[1];
-      if (!reduce_all<1>(P, d0, o0)) return;
-    }
+    if (!gs.sync()) return;
     lap(4);
     if (P.early_exit && normh < (normv + 1e-6) * 1e-6) {
       converged = 1;
@@ -461,8 +588,12 @@ __global__ void __launch_bounds__(kSolveThreads) gn_solve_kernel(SolveParams P) 
     P.stats[ST_E0] = e_first;
     P.stats[ST_E] = e_last;
     P.stats[ST_CONV] = converged;
-    for (int q = 0; q < 5; ++q) P.stats[ST_T_PREP + q] = t_acc[q];
+    for (int q = 0; q < 6; ++q) P.stats[ST_T_PREP + q] = t_acc[q];
   }
+  if (threadIdx.x == 0)
+    for (int q = 0; q < 3; ++q)
+      atomicMax(reinterpret_cast<unsigned long long*>(P.stats + ST_T_W_SPMV + q),
+                (unsigned long long)__double_as_longlong((double)t_work[q]));
 }
 
 }  // namespace arap

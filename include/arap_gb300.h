@@ -77,7 +77,9 @@ typedef struct {
   float pcg_tol;          /* relative residual target of the inner PCG (<=0: default) */
   int pcg_max_iters;      /* inner PCG iteration cap (<=0: default) */
   int coarse_nodes;       /* two-level PCG: target free nodes per aggregate of the coarse
-                             (per-aggregate affine) space; 0 = block-Jacobi only */
+                             (per-aggregate affine) space; 0 = block-Jacobi only.  The
+                             target is raised (by a quarter at a time) until there are
+                             at most 80 aggregates (960 coarse unknowns). */
 } arap_solve_config;
 
 typedef struct {
@@ -89,8 +91,12 @@ typedef struct {
   double final_energy;    /* f.f at the returned x */
   int n_free, n_static, n_rows;
   int n_coarse;           /* coarse unknowns of the two-level preconditioner (0 = off) */
-  double phase_ms[5];     /* device time in: set-up, gradient/preconditioner, coarse
-                             inversion, PCG, line search (CTA 0's view) */
+  double phase_ms[9];     /* device time in: [0] set-up, [1] gradient/preconditioner,
+                             [2] coarse matrix build + inversion, [3] PCG, [4] line search
+                             (CTA 0's view); [5] of which the coarse inversion; the
+                             slowest CTA's own work (barrier waits excluded) inside
+                             PCG: [6] products (J^T J) p, [7] vector update and
+                             preconditioner, [8] coarse solves */
 } arap_solve_stats;
 
 typedef struct arap_solver arap_solver;
