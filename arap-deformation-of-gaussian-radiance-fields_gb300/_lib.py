@@ -16,6 +16,7 @@ STATUS_NAMES = {0: "OK", 1: "NOT_CONVERGED", 2: "ENONFINITE", 3: "EBADINPUT",
                 4: "ETIMEOUT", 5: "ECUDA", 6: "ENOMEM", 7: "EUNSUPPORTED"}
 PRECISION_PLAIN, PRECISION_MIXED = 0, 1
 KNN_MAX = 12
+CENTER_SCRATCH_BYTES = 8 << 20  # ARAP_CENTER_SCRATCH_BYTES
 
 
 class ArapError(RuntimeError):
@@ -80,6 +81,7 @@ SIGNATURES = {
     "arap_grid_build": (I, [C.POINTER(P), I, P, P, P, P, I, I, C.POINTER(GridInfo), P]),
     "arap_grid_arrays": (I, [P, C.POINTER(P), C.POINTER(P), C.POINTER(P)]),
     "arap_grid_center_order": (I, [P, I, P, P, P]),
+    "arap_grid_center_order_noalloc": (I, [P, I, P, P, P]),
     "arap_grid_samples": (I, [P, P, P]),
     "arap_grid_ada_lpf": (I, [P, P, F, P, P]),
     "arap_grid_density": (I, [P, P, P, P, P, P, P, P, F, P, P, P]),

@@ -8,6 +8,7 @@
 // ascending Gaussian index -- is reproduced by a per-cell sort after an
 // atomic fill, GetAdaLpfRatio (GaussianView.cpp:4670-4751) and the host
 // contract of CudaRasterizer::forward3d_grid (GaussianView.cpp:4222-4249).
+#include <atomic>
 #include <climits>
 #include <new>
 
@@ -685,4 +686,91 @@ extern "C" int arap_grid_density(const arap_grid* G, const float* pos, const flo
                                                               feature_out);
   ARAP_LAUNCH_CHECK();
   return ARAP_OK;
+}
+
+// ------------------------------------------- allocation-free centre order ----
+// arap_grid_center_order_noalloc: the same kernel sequence as
+// arap_grid_center_order with its scratch carved from one static device array
+// of ARAP_CENTER_SCRATCH_BYTES instead of cudaMalloc/cudaFree.  The array's
+// address is resolved once per device, with that device current, by the first
+// call on it.  Calls that overlap on the GPU share the array and race.
+static __device__ __align__(256) unsigned char g_center_scratch[ARAP_CENTER_SCRATCH_BYTES];
+
+namespace {
+constexpr int kMaxScratchDevices = 64;
+std::atomic<unsigned char*> g_center_scratch_ptr[kMaxScratchDevices];
+
+int center_scratch_base(unsigned char** out) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) {
+    (void)cudaGetLastError();
+    return ARAP_ECUDA;
+  }
+  if (dev < 0 || dev >= kMaxScratchDevices) return ARAP_EUNSUPPORTED;
+  unsigned char* p = g_center_scratch_ptr[dev].load(std::memory_order_acquire);
+  if (!p) {
+    unsigned char* ptr = nullptr;
+    if (cudaGetSymbolAddress((void**)&ptr, g_center_scratch) != cudaSuccess || !ptr) {
+      (void)cudaGetLastError();
+      return ARAP_ECUDA;
+    }
+    g_center_scratch_ptr[dev].store(ptr, std::memory_order_release);
+    p = ptr;
+  }
+  *out = p;
+  return ARAP_OK;
+}
+
+size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
+}  // namespace
+
+extern "C" int arap_grid_center_order_noalloc(const arap_grid* G, int N, const float* pos, int32_t* order_out,
+                                              arap_stream_t stream) {
+  if (!G || !pos || !order_out || N < 1) return ARAP_EBADINPUT;
+  cudaStream_t st = (cudaStream_t)stream;
+  const int C = G->g * G->g * G->g;
+  const int nbs = (C + 1 + kScanTile - 1) / kScanTile + 1;
+  // scratch: cell [N], count [C], cursor [C], off [C+1], flagpos [C+1],
+  // valid [C], sums [nbs+1] (long long), each 256-byte aligned
+  const size_t b_cell = align256(sizeof(int) * (size_t)N), b_cnt = align256(sizeof(int) * (size_t)C),
+               b_off = align256(sizeof(int) * ((size_t)C + 1)), b_sums = align256(sizeof(long long) * (nbs + 1));
+  const size_t need = b_cell + 3 * b_cnt + 2 * b_off + b_sums;
+  if (need > (size_t)ARAP_CENTER_SCRATCH_BYTES) return ARAP_EUNSUPPORTED;
+  unsigned char* base = nullptr;
+  int rc = center_scratch_base(&base);
+  if (rc != ARAP_OK) return rc;
+  int* cell = reinterpret_cast<int*>(base);
+  int* count = reinterpret_cast<int*>(base + b_cell);
+  int* cursor = reinterpret_cast<int*>(base + b_cell + b_cnt);
+  int* valid = reinterpret_cast<int*>(base + b_cell + 2 * b_cnt);
+  int* off = reinterpret_cast<int*>(base + b_cell + 3 * b_cnt);
+  int* flagpos = reinterpret_cast<int*>(base + b_cell + 3 * b_cnt + b_off);
+  long long* sums = reinterpret_cast<long long*>(base + b_cell + 3 * b_cnt + 2 * b_off);
+  // the per-cell counters start at zero; every other region is written
+  // before it is read
+  if (cudaMemsetAsync(count, 0, sizeof(int) * (size_t)C, st) || cudaMemsetAsync(cursor, 0, sizeof(int) * (size_t)C, st)) {
+    (void)cudaGetLastError();
+    return ARAP_ECUDA;
+  }
+  center_cell_kernel<<<grid_for(N, 256), 256, 0, st>>>(N, pos, G->params, cell, count);
+  if ((rc = scan_exclusive(count, off, C, sums, st)) != ARAP_OK) return rc;
+  center_fill_kernel<<<grid_for(N, 256), 256, 0, st>>>(N, cell, off, cursor, order_out);
+  flags_kernel<<<grid_for(C, 256), 256, 0, st>>>(C, count, cursor);
+  if ((rc = scan_exclusive(cursor, flagpos, C, sums, st)) != ARAP_OK) return rc;
+  int nvalid = 0;
+  if (cudaMemcpyAsync(&nvalid, flagpos + C, sizeof(int), cudaMemcpyDeviceToHost, st) || cudaStreamSynchronize(st)) {
+    (void)cudaGetLastError();
+    return ARAP_ECUDA;
+  }
+  if (nvalid > 0) {
+    compact_kernel<<<grid_for(C, 256), 256, 0, st>>>(C, count, flagpos, valid);
+    if (cudaFuncSetAttribute(sort_cells_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSortMax * (int)sizeof(int)))
+      return ARAP_ECUDA;
+    sort_cells_kernel<<<nvalid, 256, kSortMax * sizeof(int), st>>>(nvalid, valid, off, order_out);
+  }
+  if (cudaPeekAtLastError() != cudaSuccess || cudaStreamSynchronize(st) != cudaSuccess) {
+    (void)cudaGetLastError();
+    return ARAP_ECUDA;
+  }
+  return arap_get_device_status(stream);
 }

@@ -287,6 +287,25 @@ int arap_grid_arrays(const arap_grid* grid, const int32_t** cell_offsets, const 
 int arap_grid_center_order(const arap_grid* grid, int N, const float* pos, int32_t* order_out,
                            arap_stream_t stream);
 
+/* Size of the static device scratch array of arap_grid_center_order_noalloc. */
+#define ARAP_CENTER_SCRATCH_BYTES (8u << 20)
+
+/* No counterpart in the reference: an addition of this library for callers
+ * that may not allocate device memory while they run (a frame loop where the
+ * device-wide synchronisation of cudaMalloc/cudaFree would stall rendering, or
+ * a process whose device memory is fully reserved by its own allocator).
+ * Same arguments and result as arap_grid_center_order, but no allocation: the
+ * scratch (cell [N], per-cell counters, offsets and flags [4 g^3 + 2], occupied
+ * cells [g^3], scan sums) is carved from one static device array of
+ * ARAP_CENTER_SCRATCH_BYTES, about 4 N + 20 g^3 bytes in all; larger requests
+ * return ARAP_EUNSUPPORTED before any device work.  The first call on each
+ * device resolves the array's address (cudaGetSymbolAddress) with that device
+ * current; make that first call before any stream capture.  Calls that
+ * overlap on the GPU (other streams, other host threads) share the array and
+ * race: serialise them.  Synchronises. */
+int arap_grid_center_order_noalloc(const arap_grid* grid, int N, const float* pos, int32_t* order_out,
+                                   arap_stream_t stream);
+
 /* 64 samples per occupied cell, cell-major, sample s at
  * min + cell*step + (0.5 + (s/16, s/4%4, s%4)) * interval
  * (GaussianView.cpp:4104-4133).  samples_out [n_valid*64*3]. */
