@@ -92,35 +92,24 @@ __global__ void end_points_kernel(int N, const float* __restrict__ pos,
 // Fused UpdatePosition (endpoint part, GaussianView.cpp:3022-3040) and
 // UpdateAsSixPointsWithdrawBad (GaussianView.cpp:3081-3166).
 //
-// One CTA owns a tile of kSkinTile Gaussians.  Every input of the tile -- the
-// 18 endpoint planes, the 6k index and weight planes, scale0, the previous
-// quaternions and the 48-float SH records -- is first copied into shared
-// memory with cp.async (no registers held while the copies are in flight, so
-// the whole tile's traffic is outstanding at once); then each thread skins
-// its Gaussian from shared memory and the SH records go back with coalesced
-// 16-byte stores.
+// One thread per Gaussian, kSkinTile per CTA.  The tile's 48-float SH records
+// and previous quaternions are copied into shared memory with cp.async (16-byte
+// copies of contiguous records) while each thread blends its six endpoints from
+// coalesced loads of the endpoint, index and weight planes; the SH records go
+// back with coalesced 16-byte stores.  Shared memory (28.6 KB) and registers
+// (launch bound of four CTAs per SM) keep 16 warps per SM resident.
 constexpr int kSkinTile = kSkinThreads;  // Gaussians per CTA
 constexpr int kShStride = 52;            // floats per staged SH record (13 float4: conflict-free)
 
-__device__ __forceinline__ void cp_async4(void* smem, const void* gmem) {
-  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
-  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(s), "l"(gmem) : "memory");
-}
 __device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
   const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
   asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(s), "l"(gmem) : "memory");
 }
-__device__ __forceinline__ void cp_async_wait_all() {
-  asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;" ::: "memory");
-}
 
-template <int K>
-constexpr size_t skin_smem_bytes() {
-  return sizeof(float) * (size_t)kSkinTile * (18 + 12 * K + 3 + 4 + kShStride);
-}
+constexpr size_t skin_smem_bytes() { return sizeof(float) * (size_t)kSkinTile * (4 + kShStride); }
 
 template <int K, bool MIXED>
-__global__ void __launch_bounds__(kSkinThreads)
+__global__ void __launch_bounds__(kSkinThreads, 4)
     skin_gaussians_kernel(int N, float* __restrict__ ends, const int32_t* __restrict__ eidx,
                           const float* __restrict__ ew, const float* __restrict__ table,
                           const float* __restrict__ scale0, const uint8_t* __restrict__ static_mask,
@@ -131,47 +120,38 @@ __global__ void __launch_bounds__(kSkinThreads)
   float* s_raw = reinterpret_cast<float*>(s_raw4);
   float* s_sh = s_raw;                                        // [T][52]
   float4* s_q = reinterpret_cast<float4*>(s_sh + kSkinTile * kShStride);  // [T]
-  float* s_ends = reinterpret_cast<float*>(s_q + kSkinTile);  // [18][T]
-  float* s_w = s_ends + 18 * kSkinTile;                       // [6K][T]
-  int* s_idx = reinterpret_cast<int*>(s_w + 6 * K * kSkinTile);  // [6K][T]
-  float* s_s0 = reinterpret_cast<float*>(s_idx + 6 * K * kSkinTile);  // [T][3]
   const int t = threadIdx.x;
   const int tile0 = blockIdx.x * kSkinTile;
   const int cnt = min(kSkinTile, N - tile0);
   const int i = tile0 + t;
   const bool active = t < cnt;
-  // ---- stage the tile
-  if (active) {
-#pragma unroll
-    for (int c = 0; c < 18; ++c) cp_async4(s_ends + c * kSkinTile + t, ends + (size_t)c * N + i);
-#pragma unroll
-    for (int c = 0; c < 6 * K; ++c) {
-      cp_async4(s_w + c * kSkinTile + t, ew + (size_t)c * N + i);
-      cp_async4(s_idx + c * kSkinTile + t, eidx + (size_t)c * N + i);
-    }
-    cp_async16(s_q + t, reinterpret_cast<const float4*>(rot_inout) + i);
-  }
-  for (int e = t; e < 3 * cnt; e += kSkinThreads) cp_async4(s_s0 + e, scale0 + 3 * (size_t)tile0 + e);
+  // ---- stage the SH records and previous quaternions of the tile
+  if (active) cp_async16(s_q + t, reinterpret_cast<const float4*>(rot_inout) + i);
   if (shs) {
     const float* src = shs + 48 * (size_t)tile0;
     for (int q = t; q < 12 * cnt; q += kSkinThreads)
       cp_async16(s_sh + (q / 12) * kShStride + (q % 12) * 4, src + 4 * (size_t)q);
   }
-  cp_async_wait_all();
-  __syncthreads();
+  asm volatile("cp.async.commit_group;" ::: "memory");
 
+  float e[18];
   if (active) {
-    float e[18];
 #pragma unroll
-    for (int c = 0; c < 18; ++c) e[c] = s_ends[c * kSkinTile + t];
+    for (int c = 0; c < 18; ++c) e[c] = __ldcs(ends + (size_t)c * N + i);
 #pragma unroll
     for (int ep = 0; ep < 6; ++ep) {
       float ox = 0.f, oy = 0.f, oz = 0.f, ws = 0.f;
+      int id[K];
+      float wv[K];
 #pragma unroll
       for (int j = 0; j < K; ++j) {
-        const int c = j * 6 + ep;
-        const NodeXf x = load_node(table, s_idx[c * kSkinTile + t]);
-        const float w = s_w[c * kSkinTile + t];
+        id[j] = __ldcs(eidx + (size_t)(j * 6 + ep) * N + i);
+        wv[j] = __ldcs(ew + (size_t)(j * 6 + ep) * N + i);
+      }
+#pragma unroll
+      for (int j = 0; j < K; ++j) {
+        const NodeXf x = load_node(table, id[j]);
+        const float w = wv[j];
         ws += w;
         ed_term(x, w, e[3 * ep], e[3 * ep + 1], e[3 * ep + 2], ox, oy, oz);
       }
@@ -181,6 +161,10 @@ __global__ void __launch_bounds__(kSkinThreads)
     }
 #pragma unroll
     for (int c = 0; c < 18; ++c) __stcs(ends + (size_t)c * N + i, e[c]);
+  }
+  asm volatile("cp.async.wait_group 0;" ::: "memory");
+  __syncthreads();
+  if (active) {
     const bool is_static = static_mask && static_mask[i];
     if (!is_static) {
       float cx = 0.f, cy = 0.f, cz = 0.f;
@@ -233,7 +217,7 @@ __global__ void __launch_bounds__(kSkinThreads)
       float sc[3];
 #pragma unroll
       for (int a = 0; a < 3; ++a) {
-        const float s0 = s_s0[3 * t + a];
+        const float s0 = __ldg(scale0 + 3 * (size_t)i + a);
         sc[a] = Kd[a] / ((s0 + 1e-3f) * 2.0f) * s0;
       }
       pos_out[3 * (size_t)i] = cx;
@@ -691,16 +675,13 @@ static void launch_skin_g(bool mixed, int N, float* ends, const int32_t* eidx, c
                           const float* table, const float* scale0, const uint8_t* st, float* pos,
                           float* rot, float* scale, float* shs, float* cov, cudaStream_t s) {
   const int grid = grid_for(N, kSkinTile);
-  constexpr size_t smem = skin_smem_bytes<K>();
-  if (mixed) {
-    cudaFuncSetAttribute(skin_gaussians_kernel<K, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    skin_gaussians_kernel<K, true><<<grid, kSkinThreads, smem, s>>>(N, ends, eidx, ew, table, scale0, st,
-                                                                     pos, rot, scale, shs, cov);
-  } else {
-    cudaFuncSetAttribute(skin_gaussians_kernel<K, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    skin_gaussians_kernel<K, false><<<grid, kSkinThreads, smem, s>>>(N, ends, eidx, ew, table, scale0, st,
-                                                                      pos, rot, scale, shs, cov);
-  }
+  constexpr size_t smem = skin_smem_bytes();
+  if (mixed)
+    skin_gaussians_kernel<K, true><<<grid, kSkinThreads, smem, s>>>(N, ends, eidx, ew, table, scale0, st, pos, rot,
+                                                                     scale, shs, cov);
+  else
+    skin_gaussians_kernel<K, false><<<grid, kSkinThreads, smem, s>>>(N, ends, eidx, ew, table, scale0, st, pos, rot,
+                                                                      scale, shs, cov);
 }
 
 template <int K>
