@@ -343,6 +343,8 @@ extern "C" int arap_solver_create(arap_solver** out, int n, int k, const int32_t
     P.mem_w = cv.take<float>((size_t)U * k);
     P.mem_geo = cv.take<float4>((size_t)U * k);
     P.grp_target = cv.take<float4>(G);
+    P.grp_f = cv.take<double>((size_t)3 * G);
+    P.item_cq = cv.take<float4>(item_flat.size());
     P.x = cv.take<double>((size_t)F * 12);
     P.xf = cv.take<float>((size_t)F * 12);
     P.h = cv.take<float>((size_t)F * 12);
@@ -436,6 +438,7 @@ extern "C" int arap_solver_create(arap_solver** out, int n, int k, const int32_t
   P.F = F;
   P.G = G;
   P.U = U;
+  P.n_items = (int)item_flat.size();
   P.wr = std::sqrt((double)cfg.w_rot);
   P.wg = std::sqrt((double)cfg.w_reg);
   P.wc = std::sqrt((double)cfg.w_con);

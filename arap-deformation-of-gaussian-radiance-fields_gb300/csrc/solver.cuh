@@ -25,7 +25,7 @@ constexpr int kMaxCoarse = 12 * kMaxCoarseAggs;
 enum { ITEM_OUT = 0, ITEM_IN = 1, ITEM_STATIC = 2, ITEM_CON = 3 };
 
 struct SolveParams {
-  int n, k, F, G, U;
+  int n, k, F, G, U, n_items;
   const int32_t* free_ids;   // [F]
   const int32_t* rank;       // [n]
   const int32_t* item_off;   // [F+1]
@@ -40,6 +40,9 @@ struct SolveParams {
   const float* mem_w;        // [U*k] anchor weight a_cl
   float4* mem_geo;           // [U*k] per frame {a, v_c - g_l}
   float4* grp_target;        // [G] per frame {target xyz, mult}
+  double* grp_f;             // [G*3] constraint residual of each group at the current x
+  float4* item_cq;           // [n_items] per solve, ITEM_CON only: {sum a (v_c - g_j), sum a} over
+                             // the group's anchors equal to the item's node (first item of a run)
   const float* node_pos;     // [n*3]
   const float* aims;         // [n*3]
   double* x;                 // [F*12] Gauss-Newton iterate

@@ -110,38 +110,39 @@ __device__ __forceinline__ void load_pos(const SolveParams& P, int node, RT (&v)
 //        - mult * target)
 // evaluated as wc * (sum_u [sum_free a ((R_l - I)(v_c - g_l) + t_l) + v_c sum a]
 //                    - mult * target).
+// One warp, lanes over the group's (member, anchor) slots; every lane returns f.
 template <typename RT>
-__device__ void con_residual(const SolveParams& P, int g, RT scale, RT (&f)[3]) {
-  f[0] = f[1] = f[2] = RT(0);
-  RT base[3] = {RT(0), RT(0), RT(0)};
+__device__ void con_residual_warp(const SolveParams& P, int g, RT scale, RT (&f)[3]) {
+  const int lane = threadIdx.x & 31;
   const int k = P.k;
-  const int s0 = __ldg(P.grp_off + g), s1 = __ldg(P.grp_off + g + 1);
-  for (int s = s0; s < s1; ++s) {
+  const int s0 = __ldg(P.grp_off + g) * k, s1 = __ldg(P.grp_off + g + 1) * k;
+  RT acc[3] = {RT(0), RT(0), RT(0)}, base[3] = {RT(0), RT(0), RT(0)};
+  for (int slot = s0 + lane; slot < s1; slot += 32) {
     RT v[3];
-    load_pos<RT>(P, __ldg(P.grp_member + s), v);
-    RT wsum = RT(0);
-    for (int t = 0; t < k; ++t) {
-      const int slot = s * k + t;
-      const RT a = RT(__ldg(P.mem_w + slot));
-      wsum += a;
-      const int rk = __ldg(P.mem_rank + slot);
-      if (rk >= 0) {
-        RT gl[3], X[12];
-        load_pos<RT>(P, __ldg(P.mem_node + slot), gl);
-        load_x<RT>(P, rk, scale, X);
-        const RT d0 = v[0] - gl[0], d1 = v[1] - gl[1], d2 = v[2] - gl[2];
+    load_pos<RT>(P, __ldg(P.grp_member + slot / k), v);
+    const RT a = RT(__ldg(P.mem_w + slot));
 #pragma unroll
-        for (int c = 0; c < 3; ++c) f[c] += a * (X[c] * d0 + X[3 + c] * d1 + X[6 + c] * d2 + X[9 + c]);
-      }
+    for (int c = 0; c < 3; ++c) base[c] += a * v[c];
+    const int rk = __ldg(P.mem_rank + slot);
+    if (rk >= 0) {
+      RT gl[3], X[12];
+      load_pos<RT>(P, __ldg(P.mem_node + slot), gl);
+      load_x<RT>(P, rk, scale, X);
+      const RT d0 = v[0] - gl[0], d1 = v[1] - gl[1], d2 = v[2] - gl[2];
+#pragma unroll
+      for (int c = 0; c < 3; ++c) acc[c] += a * (X[c] * d0 + X[3 + c] * d1 + X[6 + c] * d2 + X[9 + c]);
     }
+  }
 #pragma unroll
-    for (int c = 0; c < 3; ++c) base[c] += v[c] * wsum;
+  for (int c = 0; c < 3; ++c) {
+    acc[c] = warp_sum(acc[c]);
+    base[c] = warp_sum(base[c]);
   }
   const float4 tg = P.grp_target[g];
   const RT wc = RT(P.wc);
-  f[0] = wc * (f[0] + (base[0] - RT(tg.w) * RT(tg.x)));
-  f[1] = wc * (f[1] + (base[1] - RT(tg.w) * RT(tg.y)));
-  f[2] = wc * (f[2] + (base[2] - RT(tg.w) * RT(tg.z)));
+  f[0] = wc * (acc[0] + (base[0] - RT(tg.w) * RT(tg.x)));
+  f[1] = wc * (acc[1] + (base[1] - RT(tg.w) * RT(tg.y)));
+  f[2] = wc * (acc[2] + (base[2] - RT(tg.w) * RT(tg.z)));
 }
 
 // J_g u of a constraint group (linear part only), from the anchors' u.
@@ -302,10 +303,10 @@ __device__ void residual_node(const SolveParams& P, int r, RT scale, RT (&acc)[1
           acc[9 + c] += -ws * f;
         }
         Q[9] += (float)((P.wg * s) * (P.wg * s));
-      } else {  // ITEM_CON
+      } else {  // ITEM_CON: the group's residual from the group pass
         const int g = m.z;
-        RT fg[3];
-        con_residual<RT>(P, g, scale, fg);
+        const RT fg[3] = {RT(__ldcg(P.grp_f + 3 * (size_t)g)), RT(__ldcg(P.grp_f + 3 * (size_t)g + 1)),
+                          RT(__ldcg(P.grp_f + 3 * (size_t)g + 2))};
         const float4 geo = __ldcg(P.mem_geo + m.y);
         const RT wa = RT(P.wc) * RT(geo.x);
         const float dv[3] = {geo.y, geo.z, geo.w};
@@ -315,28 +316,12 @@ __device__ void residual_node(const SolveParams& P, int r, RT scale, RT (&acc)[1
           for (int rr = 0; rr < 3; ++rr) acc[3 * c + rr] += wa * RT(dv[c]) * fg[rr];
 #pragma unroll
         for (int rr = 0; rr < 3; ++rr) acc[9 + rr] += wa * fg[rr];
-        // diagonal block: aggregate all anchors of this group equal to j, once
-        // per (group, node) run (items are sorted by group)
-        bool first_of_run = true;
-        if (it > b0) {
-          const int4 pm = __ldg(P.items + it - 1);
-          first_of_run = !((pm.x & 15) == ITEM_CON && pm.z == g);
-        }
-        if (first_of_run) {
-          float ev[3] = {0.f, 0.f, 0.f}, al = 0.f;
-          const int s0 = __ldg(P.grp_off + g), s1 = __ldg(P.grp_off + g + 1);
-          for (int s = s0; s < s1; ++s)
-            for (int t = 0; t < P.k; ++t) {
-              const int slot = s * P.k + t;
-              if (__ldg(P.mem_node + slot) != j) continue;
-              const float4 gg = __ldcg(P.mem_geo + slot);
-              ev[0] = fmaf(gg.x, gg.y, ev[0]);
-              ev[1] = fmaf(gg.x, gg.z, ev[1]);
-              ev[2] = fmaf(gg.x, gg.w, ev[2]);
-              al += gg.x;
-            }
+        // diagonal block: this item's share, summed once per solve over the
+        // group's anchors equal to j (zero for all but the first item of a run)
+        const float4 cq = __ldcg(P.item_cq + it);
+        if (cq.w != 0.f) {
           const float wcf = (float)P.wc;
-          q_add(Q, wcf * ev[0], wcf * ev[1], wcf * ev[2], wcf * al);
+          q_add(Q, wcf * cq.x, wcf * cq.y, wcf * cq.z, wcf * cq.w);
         }
       }
     }
@@ -480,108 +465,90 @@ __device__ void spmv_node(const SolveParams& P, int r, bool valid, float (&acc)[
   }
 }
 
-// Diagonal 12x12 block of J^T J for free node r from Q and the rotation
-// rows at x (float copy), Cholesky-factored by lane 0 and inverted column by
-// column by lanes 0..11 into P.dinv (row-major, symmetric).
-__device__ void build_dinv(const SolveParams& P, int r, const float (&Q)[10], float* D) {
+// Diagonal 12x12 block of J^T J for free node r from Q and the rotation rows
+// at x (float copy), inverted by Gauss-Jordan without pivoting (the block is
+// symmetric positive definite) across 24 lanes: lane j < 12 holds column j of
+// the block, lane 12 + j column j of the identity, and every step takes the
+// pivot column from its lane by shuffle.  Lanes 12..23 end with the columns of
+// the inverse (= its rows) and store them into P.dinv (row-major).  A block
+// that is not positive definite falls back to the inverse of its diagonal.
+__device__ void build_dinv(const SolveParams& P, int r, const float (&Q)[10]) {
   const int lane = threadIdx.x & 31;
-  if (lane == 0) {
-    float X[9];
+  float X[9];
 #pragma unroll
-    for (int i = 0; i < 9; ++i) X[i] = __ldcg(P.xf + 12 * (size_t)r + i);
+  for (int i = 0; i < 9; ++i) X[i] = __ldcg(P.xf + 12 * (size_t)r + i);
+  // rotation rows: [c1|c0|0], [c2|0|c0], [0|c2|c1], [2c0|0|0], [0|2c1|0], [0|0|2c2]
+  const float wr = (float)P.wr;
+  float J[6][9];
 #pragma unroll
-    for (int i = 0; i < 144; ++i) D[i] = 0.f;
+  for (int a = 0; a < 6; ++a)
 #pragma unroll
-    for (int rr = 0; rr < 3; ++rr) {
+    for (int b = 0; b < 9; ++b) J[a][b] = 0.f;
 #pragma unroll
-      for (int a = 0; a < 3; ++a) {
-#pragma unroll
-        for (int b = 0; b < 3; ++b) D[(3 * a + rr) * 12 + 3 * b + rr] = Q[a <= b ? qi(a, b) : qi(b, a)];
-        D[(3 * a + rr) * 12 + 9 + rr] = Q[qi(a, 3)];
-        D[(9 + rr) * 12 + 3 * a + rr] = Q[qi(a, 3)];
-      }
-      D[(9 + rr) * 12 + 9 + rr] = Q[9];
-    }
-    // rotation rows: [c1|c0|0], [c2|0|c0], [0|c2|c1], [2c0|0|0], [0|2c1|0], [0|0|2c2]
-    const float wr = (float)P.wr;
-    float J[6][9];
-#pragma unroll
-    for (int a = 0; a < 6; ++a)
-#pragma unroll
-      for (int b = 0; b < 9; ++b) J[a][b] = 0.f;
-#pragma unroll
-    for (int c = 0; c < 3; ++c) {
-      J[0][c] = wr * X[3 + c]; J[0][3 + c] = wr * X[c];
-      J[1][c] = wr * X[6 + c]; J[1][6 + c] = wr * X[c];
-      J[2][3 + c] = wr * X[6 + c]; J[2][6 + c] = wr * X[3 + c];
-      J[3][c] = 2.f * wr * X[c];
-      J[4][3 + c] = 2.f * wr * X[3 + c];
-      J[5][6 + c] = 2.f * wr * X[6 + c];
-    }
-#pragma unroll
-    for (int a = 0; a < 9; ++a)
-#pragma unroll
-      for (int b = 0; b < 9; ++b) {
-        float s = 0.f;
-#pragma unroll
-        for (int t = 0; t < 6; ++t) s = fmaf(J[t][a], J[t][b], s);
-        D[a * 12 + b] += s;
-      }
-    // Cholesky, lower triangle in place
-    bool ok = true;
-    for (int c = 0; c < 12 && ok; ++c) {
-      float s = D[c * 12 + c];
-      for (int t = 0; t < c; ++t) s -= D[c * 12 + t] * D[c * 12 + t];
-      if (!(s > 0.f)) {
-        ok = false;
-        break;
-      }
-      const float l = sqrtf(s);
-      D[c * 12 + c] = l;
-      const float il = 1.f / l;
-      for (int i = c + 1; i < 12; ++i) {
-        float v = D[i * 12 + c];
-        for (int t = 0; t < c; ++t) v -= D[i * 12 + t] * D[c * 12 + t];
-        D[i * 12 + c] = v * il;
-      }
-    }
-    if (!ok) {
-      // Jacobi fallback: diagonal of the block
-      for (int a = 0; a < 12; ++a) {
-        float dg = 0.f;
-        if (a < 9) {
-          float s = 0.f;
-          for (int t = 0; t < 6; ++t) s += J[t][a] * J[t][a];
-          dg = s;
-        }
-        const int rr = a < 9 ? a % 3 : a - 9;
-        dg += (a < 9) ? Q[qi(a / 3, a / 3)] : Q[9];
-        (void)rr;
-        for (int b = 0; b < 12; ++b) D[a * 12 + b] = 0.f;
-        D[a * 12 + a] = sqrtf(fmaxf(dg, 1e-20f));
-      }
-    }
+  for (int c = 0; c < 3; ++c) {
+    J[0][c] = wr * X[3 + c]; J[0][3 + c] = wr * X[c];
+    J[1][c] = wr * X[6 + c]; J[1][6 + c] = wr * X[c];
+    J[2][3 + c] = wr * X[6 + c]; J[2][6 + c] = wr * X[3 + c];
+    J[3][c] = 2.f * wr * X[c];
+    J[4][3 + c] = 2.f * wr * X[3 + c];
+    J[5][6 + c] = 2.f * wr * X[6 + c];
   }
-  __syncwarp();
-  if (lane < 12) {
-    float y[12], xs[12];
+  // column `lane` (= row, the block is symmetric); unknown u is R[u % 3][u / 3]
+  // for u < 9 and t[u - 9] otherwise
+  float col[12];
+  const int L = lane < 12 ? lane : 0;
+  const int aL = L < 9 ? L / 3 : 3, rL = L < 9 ? L % 3 : L - 9;
 #pragma unroll
-    for (int i = 0; i < 12; ++i) {
-      float s = (i == lane) ? 1.f : 0.f;
+  for (int b = 0; b < 12; ++b) {
+    const int ab = b < 9 ? b / 3 : 3, rb = b < 9 ? b % 3 : b - 9;
+    float v = 0.f;
+    if (rL == rb) {
+      const int lo = aL < ab ? aL : ab, hi = aL < ab ? ab : aL;
+      float qv = 0.f;
 #pragma unroll
-      for (int t = 0; t < i; ++t) s -= D[i * 12 + t] * y[t];
-      y[i] = s / D[i * 12 + i];
+      for (int x = 0; x < 4; ++x)
+#pragma unroll
+        for (int y = x; y < 4; ++y)
+          if (x == lo && y == hi) qv = Q[qi(x, y)];
+      v = qv;
     }
+    if (b < 9 && L < 9) {
+      float jj = 0.f;
 #pragma unroll
-    for (int i = 11; i >= 0; --i) {
-      float s = y[i];
+      for (int t = 0; t < 6; ++t) {
+        float jl = 0.f;
 #pragma unroll
-      for (int t = i + 1; t < 12; ++t) s -= D[t * 12 + i] * xs[t];
-      xs[i] = s / D[i * 12 + i];
+        for (int q = 0; q < 9; ++q) jl = (q == L) ? J[t][q] : jl;
+        jj = fmaf(jl, J[t][b], jj);
+      }
+      v += jj;
     }
-    float* out = P.dinv + 144 * (size_t)r + 12 * lane;
+    col[b] = lane < 12 ? v : ((lane == 12 + b) ? 1.f : 0.f);
+  }
+  float dg = 0.f;  // this lane's diagonal entry, for the fallback
 #pragma unroll
-    for (int i = 0; i < 12; ++i) out[i] = xs[i];
+  for (int b = 0; b < 12; ++b)
+    if (b == L) dg = col[b];
+  bool ok = true;
+#pragma unroll
+  for (int k = 0; k < 12; ++k) {
+    float ck[12];
+#pragma unroll
+    for (int i = 0; i < 12; ++i) ck[i] = __shfl_sync(0xffffffffu, col[i], k);
+    const float piv = ck[k];
+    ok = ok && piv > 0.f;
+    const float akj = col[k] / piv;
+#pragma unroll
+    for (int i = 0; i < 12; ++i)
+      if (i != k) col[i] = fmaf(-ck[i], akj, col[i]);
+    col[k] = akj;
+  }
+  const float dgj = __shfl_sync(0xffffffffu, dg, lane >= 12 && lane < 24 ? lane - 12 : 0);
+  if (lane >= 12 && lane < 24) {
+    const int j = lane - 12;
+    float* out = P.dinv + 144 * (size_t)r + 12 * j;
+#pragma unroll
+    for (int i = 0; i < 12; ++i) out[i] = ok ? col[i] : ((i == j) ? 1.f / fmaxf(dgj, 1e-20f) : 0.f);
   }
   __syncwarp();
 }

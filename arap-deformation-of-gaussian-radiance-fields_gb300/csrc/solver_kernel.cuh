@@ -30,7 +30,6 @@ __device__ __forceinline__ unsigned long long global_ns() {
 // separated by grid barriers, which include __syncthreads).
 constexpr int kGJRows = 8;  // rows of a CTA's strip handled together
 constexpr int kScratchFloats = 2 * kGJBlock * (kGJBlock + 1) + kGJRows * (kGJBlock + 1) + kGJRows * kGJBlock;
-static_assert(kScratchFloats >= kSolveWarps * 144, "scratch holds the 12x12 blocks");
 static_assert(kScratchFloats >= kMaxCoarse, "scratch holds the restricted residual");
 
 // Inverse of the coarse matrix in Cw[0] by blocked Gauss-Jordan (float32, no
@@ -202,9 +201,7 @@ __device__ __forceinline__ void coarse_solve(const SolveParams& P, const double*
 template <typename RT>
 __global__ void __launch_bounds__(kSolveThreads) gn_solve_kernel(SolveParams P) {
   __shared__ __align__(16) float s_scratch[kScratchFloats];
-  float* const s_D = s_scratch;  // [kSolveWarps][144] during the gradient pass
   const int lane = threadIdx.x & 31;
-  const int wib = threadIdx.x >> 5;
   const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int nw = (gridDim.x * blockDim.x) >> 5;
   const int gt = blockIdx.x * blockDim.x + threadIdx.x;
@@ -306,6 +303,37 @@ __global__ void __launch_bounds__(kSolveThreads) gn_solve_kernel(SolveParams P) 
   if (gt == 0)
     for (int q = ST_T_W_SPMV; q <= ST_T_W_CSOLVE; ++q) P.stats[q] = 0.0;
   if (!gs.sync()) return;
+  // diagonal-block share of every constraint item (fixed for this solve): the
+  // group's anchors equal to the item's node, summed into the first item of
+  // the node's run of that group
+  for (int e = gt; e < P.n_items; e += nt) {
+    const int4 m = P.items[e];
+    if ((m.x & 15) != ITEM_CON) continue;
+    const int g = m.z;
+    const int j = P.mem_node[m.y];
+    const int b0 = P.item_off[P.rank[j]];
+    bool first = true;
+    if (e > b0) {
+      const int4 pm = P.items[e - 1];
+      first = !((pm.x & 15) == ITEM_CON && pm.z == g);
+    }
+    float4 cq = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (first) {
+      const int s0 = P.grp_off[g], s1 = P.grp_off[g + 1];
+      for (int u = s0; u < s1; ++u)
+        for (int t = 0; t < k; ++t) {
+          const int slot = u * k + t;
+          if (P.mem_node[slot] != j) continue;
+          const float4 gg = P.mem_geo[slot];
+          cq.x = fmaf(gg.x, gg.y, cq.x);
+          cq.y = fmaf(gg.x, gg.z, cq.y);
+          cq.z = fmaf(gg.x, gg.w, cq.z);
+          cq.w += gg.x;
+        }
+    }
+    P.item_cq[e] = cq;
+  }
+  if (!coarse && !gs.sync()) return;
   if (coarse) {
     // coarse matrix P^T (J^T J at x = I) P, fixed for this solve
     for (int oi = gw; oi < F; oi += nw) coarse_rows_node(P, __ldg(P.order + oi));
@@ -319,6 +347,18 @@ __global__ void __launch_bounds__(kSolveThreads) gn_solve_kernel(SolveParams P) 
   for (int it = 0; it < P.max_iters; ++it) {
     // ---- gradient -J^T f, energy, preconditioner, PCG start (h=0, r=g, z=M^-1 g)
     double red[3] = {0.0, 0.0, 0.0};
+    // constraint residuals, one warp per group, for the nodes' products
+    for (int g = gw; g < P.G; g += nw) {
+      RT f[3];
+      con_residual_warp<RT>(P, g, RT(0), f);
+      if (lane == 0) {
+        P.grp_f[3 * (size_t)g] = double(f[0]);
+        P.grp_f[3 * (size_t)g + 1] = double(f[1]);
+        P.grp_f[3 * (size_t)g + 2] = double(f[2]);
+        red[0] += double(f[0]) * double(f[0]) + double(f[1]) * double(f[1]) + double(f[2]) * double(f[2]);
+      }
+    }
+    if (!gs.sync()) return;
     for (int oi = gw; oi < F; oi += nw) {
       const int r = __ldg(P.order + oi);
       RT acc[12];
@@ -336,7 +376,7 @@ __global__ void __launch_bounds__(kSolveThreads) gn_solve_kernel(SolveParams P) 
         }
         continue;
       }
-      build_dinv(P, r, Q, s_D + 144 * wib);
+      build_dinv(P, r, Q);
       if (coarse) coarse_rot_node(P, r, P.rotagg + (it & 1) * 81 * P.NA);
       float gc = 0.f;
 #pragma unroll
@@ -351,11 +391,6 @@ __global__ void __launch_bounds__(kSolveThreads) gn_solve_kernel(SolveParams P) 
         P.h[o] = 0.f;
         red[2] += (double)gc * (double)gc;
       }
-    }
-    for (int g = gt; g < P.G; g += nt) {
-      RT f[3];
-      con_residual<RT>(P, g, RT(0), f);
-      red[0] += double(f[0]) * double(f[0]) + double(f[1]) * double(f[1]) + double(f[2]) * double(f[2]);
     }
     for (int e = gt; e < F * 12; e += nt) {
       const double v = __ldcg(P.x + e);
@@ -515,10 +550,11 @@ __global__ void __launch_bounds__(kSolveThreads) gn_solve_kernel(SolveParams P) 
         residual_node<RT, PASS_ENERGY>(P, r, scale, acc, Q, en);
         if (lane == 0) en2[0] += en;
       }
-      for (int g = gt; g < P.G; g += nt) {
+      for (int g = gw; g < P.G; g += nw) {
         RT f[3];
-        con_residual<RT>(P, g, scale, f);
-        en2[0] += double(f[0]) * double(f[0]) + double(f[1]) * double(f[1]) + double(f[2]) * double(f[2]);
+        con_residual_warp<RT>(P, g, scale, f);
+        if (lane == 0)
+          en2[0] += double(f[0]) * double(f[0]) + double(f[1]) * double(f[1]) + double(f[2]) * double(f[2]);
       }
       if (ls == 0) {
         for (int e = gt; e < F * 12; e += nt) {
