@@ -56,7 +56,7 @@ struct GridBarrier {
 
 constexpr long long kSpinLimit = 1ll << 23;
 constexpr int kReduceSlots = 4;
-constexpr int kMaxGridCtas = 320;  // CTAs a barrier reduction supports (10 per lane)
+constexpr int kMaxGridCtas = 160;  // CTAs a barrier reduction supports (5 per lane)
 
 __device__ __forceinline__ unsigned int ld_acquire_u32(const unsigned int* p) {
   unsigned int v;
@@ -138,29 +138,22 @@ struct GridSync {
       __syncwarp();
       ok = __shfl_sync(0xffffffffu, ok, 0);
       if (ok) {
-        // two slots per pass: every CTA's pair requested at once, then added in CTA order
+        // every slot of every CTA requested at once, then added in CTA order
         constexpr int kQ = kMaxGridCtas / 32;
+        double t[kQ][NSLOT];
 #pragma unroll
-        for (int s0 = 0; s0 < NSLOT; s0 += 2) {
-          double2 t[kQ];
+        for (int q = 0; q < kQ; ++q) {
+          const unsigned int c = lane + 32u * q;
 #pragma unroll
-          for (int q = 0; q < kQ; ++q) {
-            const unsigned int c = lane + 32u * q;
-            t[q] = c < nb ? __ldcg(reinterpret_cast<const double2*>(buf + (size_t)c * kReduceSlots + s0))
-                          : make_double2(0.0, 0.0);
-          }
-          double a0 = 0.0, a1 = 0.0;
+          for (int s = 0; s < NSLOT; ++s) t[q][s] = c < nb ? __ldcg(buf + (size_t)c * kReduceSlots + s) : 0.0;
+        }
 #pragma unroll
-          for (int q = 0; q < kQ; ++q) {
-            a0 += t[q].x;
-            a1 += t[q].y;
-          }
-          a0 = warp_sum(a0);
-          if (s0 + 1 < NSLOT) a1 = warp_sum(a1);
-          if (lane == 0) {  // lane 0's association order, as in every CTA
-            s_out[s0] = a0;
-            if (s0 + 1 < NSLOT) s_out[s0 + 1] = a1;
-          }
+        for (int s = 0; s < NSLOT; ++s) {
+          double a = 0.0;
+#pragma unroll
+          for (int q = 0; q < kQ; ++q) a += t[q][s];
+          a = warp_sum(a);
+          if (lane == 0) s_out[s] = a;  // lane 0's association order, as in every CTA
         }
       }
       if (lane == 0) s_ok = ok;

@@ -5,7 +5,7 @@
 
 namespace arap {
 
-constexpr int kGJBlock = 48;         // pivot block of the coarse Gauss-Jordan inversion
+constexpr int kGJBlock = 32;         // pivot block of the coarse Gauss-Jordan inversion (one warp)
 constexpr int kMaxCoarseAggs = 80;   // aggregates of the coarse space (12 unknowns each)
 constexpr int kMaxCoarse = 12 * kMaxCoarseAggs;
 

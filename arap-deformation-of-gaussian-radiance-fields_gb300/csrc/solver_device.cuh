@@ -363,6 +363,85 @@ __device__ void residual_node(const SolveParams& P, int r, RT scale, RT (&acc)[1
   energy = warp_sum(e);
 }
 
+// One coupling item of a product, fetched: the item, its geometry (d, ws for
+// regularisation rows, mem_geo for constraint items) and the other node's
+// vector (u_k translation for ITEM_OUT, u_i for ITEM_IN, J_g u for ITEM_CON).
+struct CouplingData {
+  int kind;
+  float4 aux;
+  float v[12];
+};
+
+__device__ __forceinline__ void fetch_item(const SolveParams& P, int it, const float (&gj)[3], float w,
+                                           CouplingData& D) {
+  const int4 m = __ldg(P.items + it);
+  D.kind = m.x & 15;
+#pragma unroll
+  for (int i = 0; i < 12; ++i) D.v[i] = 0.f;
+  if (D.kind == ITEM_OUT || D.kind == ITEM_IN) {
+    const float sgn = D.kind == ITEM_OUT ? 1.f : -1.f;
+    D.aux = make_float4(sgn * (__ldg(P.node_pos + 3 * (size_t)m.z) - gj[0]),
+                        sgn * (__ldg(P.node_pos + 3 * (size_t)m.z + 1) - gj[1]),
+                        sgn * (__ldg(P.node_pos + 3 * (size_t)m.z + 2) - gj[2]), w * __int_as_float(m.w));
+    if (D.kind == ITEM_IN) {
+      load_u(P, m.y, m.x >> 4, D.v);
+    } else if (m.y >= 0) {
+      float t3[3];
+      load_ut(P, m.y, m.x >> 4, t3);
+      D.v[0] = t3[0];
+      D.v[1] = t3[1];
+      D.v[2] = t3[2];
+    }
+  } else if (D.kind == ITEM_CON) {
+    float u[3];
+    if (P.NA)
+      con_ju_coarse(P, m.z, u);
+    else
+      con_ju(P, m.z, u);
+    D.v[0] = u[0];
+    D.v[1] = u[1];
+    D.v[2] = u[2];
+    D.aux = __ldcg(P.mem_geo + m.y);
+  }
+}
+
+__device__ __forceinline__ void apply_item(const SolveParams& P, const CouplingData& D, float w,
+                                           const float (&pj)[12], float (&acc)[12]) {
+  if (D.kind == ITEM_OUT) {
+    const float ws = D.aux.w;
+    const float d[3] = {D.aux.x, D.aux.y, D.aux.z};
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const float u = ws * fmaf(pj[c], d[0], fmaf(pj[3 + c], d[1], pj[6 + c] * d[2])) + w * pj[9 + c] - ws * D.v[c];
+      acc[c] = fmaf(ws * d[0], u, acc[c]);
+      acc[3 + c] = fmaf(ws * d[1], u, acc[3 + c]);
+      acc[6 + c] = fmaf(ws * d[2], u, acc[6 + c]);
+      acc[9 + c] = fmaf(w, u, acc[9 + c]);
+    }
+  } else if (D.kind == ITEM_IN) {
+    const float ws = D.aux.w;
+    const float d[3] = {D.aux.x, D.aux.y, D.aux.z};
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const float u = ws * fmaf(D.v[c], d[0], fmaf(D.v[3 + c], d[1], D.v[6 + c] * d[2])) + w * D.v[9 + c] -
+                      ws * pj[9 + c];
+      acc[9 + c] = fmaf(-ws, u, acc[9 + c]);
+    }
+  } else if (D.kind == ITEM_STATIC) {
+#pragma unroll
+    for (int c = 0; c < 3; ++c) acc[9 + c] = fmaf(w * w, pj[9 + c], acc[9 + c]);
+  } else {
+    const float wa = (float)P.wc * D.aux.x;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      acc[c] = fmaf(wa * D.aux.y, D.v[c], acc[c]);
+      acc[3 + c] = fmaf(wa * D.aux.z, D.v[c], acc[3 + c]);
+      acc[6 + c] = fmaf(wa * D.aux.w, D.v[c], acc[6 + c]);
+      acc[9 + c] = fmaf(wa, D.v[c], acc[9 + c]);
+    }
+  }
+}
+
 // w = (J^T J u)_r for free node r, computed by one half-warp (16 lanes), with
 // u formed on the fly for every node it touches; also returns this node's u in
 // every lane of the half.  A half with valid == false does no loads but takes
@@ -381,54 +460,15 @@ __device__ void spmv_node(const SolveParams& P, int r, bool valid, float (&acc)[
   load_u(P, r, P.NA ? __ldg(P.agg + r) : 0, pj);
   const float w = (float)P.wg;
   const int b0 = __ldg(P.item_off + r), b1 = __ldg(P.item_off + r + 1);
-  for (int it = b0 + lane; it < b1; it += 16) {
-    const int4 m = __ldg(P.items + it);
-    if ((m.x & 15) == ITEM_OUT) {
-      const float ws = w * __int_as_float(m.w);
-      const float d[3] = {__ldg(P.node_pos + 3 * (size_t)m.z) - gj[0],
-                          __ldg(P.node_pos + 3 * (size_t)m.z + 1) - gj[1],
-                          __ldg(P.node_pos + 3 * (size_t)m.z + 2) - gj[2]};
-      float pk[3] = {0.f, 0.f, 0.f};
-      if (m.y >= 0) load_ut(P, m.y, m.x >> 4, pk);
-#pragma unroll
-      for (int c = 0; c < 3; ++c) {
-        const float u = ws * fmaf(pj[c], d[0], fmaf(pj[3 + c], d[1], pj[6 + c] * d[2])) + w * pj[9 + c] - ws * pk[c];
-        acc[c] = fmaf(ws * d[0], u, acc[c]);
-        acc[3 + c] = fmaf(ws * d[1], u, acc[3 + c]);
-        acc[6 + c] = fmaf(ws * d[2], u, acc[6 + c]);
-        acc[9 + c] = fmaf(w, u, acc[9 + c]);
-      }
-    } else if ((m.x & 15) == ITEM_IN) {
-      const float ws = w * __int_as_float(m.w);
-      const float d[3] = {gj[0] - __ldg(P.node_pos + 3 * (size_t)m.z),
-                          gj[1] - __ldg(P.node_pos + 3 * (size_t)m.z + 1),
-                          gj[2] - __ldg(P.node_pos + 3 * (size_t)m.z + 2)};
-      float pi[12];
-      load_u(P, m.y, m.x >> 4, pi);
-#pragma unroll
-      for (int c = 0; c < 3; ++c) {
-        const float u = ws * fmaf(pi[c], d[0], fmaf(pi[3 + c], d[1], pi[6 + c] * d[2])) + w * pi[9 + c] - ws * pj[9 + c];
-        acc[9 + c] = fmaf(-ws, u, acc[9 + c]);
-      }
-    } else if ((m.x & 15) == ITEM_STATIC) {
-#pragma unroll
-      for (int c = 0; c < 3; ++c) acc[9 + c] = fmaf(w * w, pj[9 + c], acc[9 + c]);
-    } else {
-      float u[3];
-      if (P.NA)
-        con_ju_coarse(P, m.z, u);
-      else
-        con_ju(P, m.z, u);
-      const float4 geo = __ldcg(P.mem_geo + m.y);
-      const float wa = (float)P.wc * geo.x;
-#pragma unroll
-      for (int c = 0; c < 3; ++c) {
-        acc[c] = fmaf(wa * geo.y, u[c], acc[c]);
-        acc[3 + c] = fmaf(wa * geo.z, u[c], acc[3 + c]);
-        acc[6 + c] = fmaf(wa * geo.w, u[c], acc[6 + c]);
-        acc[9 + c] = fmaf(wa, u[c], acc[9 + c]);
-      }
-    }
+  // two items per lane per round: both items' loads are issued before either
+  // is used, so a round costs one round trip
+  for (int it = b0 + lane; it < b1; it += 32) {
+    const bool hasB = it + 16 < b1;
+    CouplingData A, B;
+    fetch_item(P, it, gj, w, A);
+    if (hasB) fetch_item(P, it + 16, gj, w, B);
+    apply_item(P, A, w, pj, acc);
+    if (hasB) apply_item(P, B, w, pj, acc);
   }
   if (lane == 0) {
     // J_rot^T J_rot p with J_rot at the current x (float copy)

@@ -29,15 +29,16 @@ __device__ __forceinline__ unsigned long long global_ns() {
 // Shared scratch of the persistent kernel, reused phase by phase (phases are
 // separated by grid barriers, which include __syncthreads).
 constexpr int kGJRows = 8;  // rows of a CTA's strip handled together
-constexpr int kScratchFloats = 2 * kGJBlock * (kGJBlock + 1) + kGJRows * (kGJBlock + 1) + kGJRows * kGJBlock;
+constexpr int kScratchFloats = kGJBlock * (kGJBlock + 1) + kGJRows * (kGJBlock + 1) + kGJRows * kGJBlock;
 static_assert(kScratchFloats >= kMaxCoarse, "scratch holds the restricted residual");
 
 // Inverse of the coarse matrix in Cw[0] by blocked Gauss-Jordan (float32, no
 // pivoting: the matrix is symmetric positive definite).  For each pivot block
-// K (kGJBlock wide, the last one padded with the identity), every CTA inverts
-// A_KK in its own shared memory (ping-pong copies, one __syncthreads per step;
-// the same arithmetic in every CTA, so the same bits), then updates its own
-// strip of rows:
+// K (kGJBlock = 32 wide, the last one padded with the identity), warp 0 of
+// every CTA inverts A_KK in registers -- lane j holds column j, each step takes
+// the pivot column from its lane by shuffle, so the 32 sequential steps need
+// neither shared memory nor block barriers (and every CTA computes the same
+// bits) -- then every CTA updates its own strip of rows:
 //   A_KK <- A_KK^-1, A_Kj <- A_KK^-1 A_Kj, A_iK <- -W_iK,
 //   A_ij <- A_ij - W_iK A_Kj,  W = A_iK A_KK^-1,
 // with W of the strip in shared memory and the column A_Kj streamed from L2 in
@@ -46,56 +47,52 @@ static_assert(kScratchFloats >= kMaxCoarse, "scratch holds the restricted residu
 // barrier failure; *ok = 0 when a pivot was not positive.
 __device__ bool coarse_invert(const SolveParams& P, GridSync& gs, int* ok, float* sm) {
   constexpr int KB = kGJBlock, KP = kGJBlock + 1;
+  static_assert(KB == 32, "one lane per pivot column");
   float(*pv0)[KP] = reinterpret_cast<float(*)[KP]>(sm);
-  float(*pv1)[KP] = reinterpret_cast<float(*)[KP]>(sm + KB * KP);
-  float(*wrow)[KP] = reinterpret_cast<float(*)[KP]>(sm + 2 * KB * KP);
+  float(*wrow)[KP] = reinterpret_cast<float(*)[KP]>(sm + KB * KP);
   // per strip row: -W_iK, or the row of A_KK^-1 for rows inside K (16-byte rows)
-  float(*wsel)[KB] = reinterpret_cast<float(*)[KB]>(sm + 2 * KB * KP + kGJRows * KP);
-  static_assert((2 * kGJBlock * (kGJBlock + 1) + kGJRows * (kGJBlock + 1)) % 4 == 0 && kGJBlock % 4 == 0,
-                "float4 rows");
+  float(*wsel)[KB] = reinterpret_cast<float(*)[KB]>(sm + KB * KP + kGJRows * KP);
+  static_assert((KB * KP + kGJRows * KP) % 4 == 0, "float4 rows");
   const int NC = P.NC;
   const size_t NC2 = (size_t)NC * NC;
-  const int tid = threadIdx.x, bd = blockDim.x;
+  const int tid = threadIdx.x, bd = blockDim.x, lane = tid & 31;
   const int R = (NC + gridDim.x - 1) / gridDim.x;
   const int r_begin = min(NC, (int)blockIdx.x * R), r_end = min(NC, r_begin + R);
   int src_i = 0;
   *ok = 1;
+  __shared__ int s_bad;
   for (int K0 = 0; K0 < NC; K0 += KB) {
     const int kb = min(KB, NC - K0);
     const float* src = P.Cw + src_i * NC2;
     float* dst = (K0 + kb >= NC) ? P.Cinv : P.Cw + (1 - src_i) * NC2;
-    for (int t = tid; t < KB * KB; t += bd) {
-      const int i = t / KB, j = t % KB;
-      pv0[i][j] = (i < kb && j < kb) ? __ldcg(src + (size_t)(K0 + i) * NC + K0 + j) : (i == j ? 1.f : 0.f);
-    }
-    __syncthreads();
-    int bad = 0;
-    for (int m = 0; m < KB; ++m) {
-      float(*cur)[KP] = (m & 1) ? pv1 : pv0;
-      float(*nxt)[KP] = (m & 1) ? pv0 : pv1;
-      const float pvt = cur[m][m];
-      bad |= !(pvt > 0.f);
-      const float ip = 1.f / pvt;
+    if (tid < 32) {
+      // column `lane` of the pivot block, padded with the identity
+      float col[KB];
 #pragma unroll
-      for (int q = 0; q < (KB * KB + kSolveThreads - 1) / kSolveThreads; ++q) {
-        const int t = tid + q * kSolveThreads;
-        if (t < KB * KB) {
-          const int i = t / KB, j = t % KB;
-          const float cim = cur[i][m], cmj = cur[m][j];
-          float v;
+      for (int i = 0; i < KB; ++i)
+        col[i] = (i < kb && lane < kb) ? __ldcg(src + (size_t)(K0 + i) * NC + K0 + lane) : (i == lane ? 1.f : 0.f);
+      int bad = 0;
+#pragma unroll
+      for (int m = 0; m < KB; ++m) {
+        const float pvt = __shfl_sync(0xffffffffu, col[m], m);
+        bad |= !(pvt > 0.f);
+        const float ip = 1.f / pvt;
+        const float cmj = col[m];
+#pragma unroll
+        for (int i = 0; i < KB; ++i) {
+          const float cim = __shfl_sync(0xffffffffu, col[i], m);
           if (i == m)
-            v = (j == m) ? ip : cmj * ip;
-          else if (j == m)
-            v = -cim * ip;
+            col[i] = (lane == m) ? ip : cmj * ip;
           else
-            v = fmaf(-cim * ip, cmj, cur[i][j]);
-          nxt[i][j] = v;
+            col[i] = (lane == m) ? -cim * ip : fmaf(-cim * ip, cmj, col[i]);
         }
       }
-      __syncthreads();
+#pragma unroll
+      for (int i = 0; i < KB; ++i) pv0[i][lane] = col[i];
+      if (lane == 0) s_bad = bad;
     }
-    static_assert(kGJBlock % 2 == 0, "the inverse ends in pv0");
-    if (__syncthreads_or(bad)) *ok = 0;
+    __syncthreads();
+    if (s_bad) *ok = 0;
     for (int r0 = r_begin; r0 < r_end; r0 += kGJRows) {
       const int nr = min(kGJRows, r_end - r0);
       for (int t = tid; t < kGJRows * KB; t += bd) {
@@ -444,6 +441,7 @@ __global__ void __launch_bounds__(kSolveThreads) gn_solve_kernel(SolveParams P) 
         const int oi = base + half;
         const bool valid = oi < F;
         const int r = valid ? __ldg(P.order + oi) : 0;
+        const float rv = (valid && l16 < 12) ? __ldcg(P.r + 12 * (size_t)r + l16) : 0.f;
         float acc[12], uj[12];
         spmv_node(P, r, valid, acc, uj);
         if (valid && l16 < 12) {
@@ -455,7 +453,6 @@ __global__ void __launch_bounds__(kSolveThreads) gn_solve_kernel(SolveParams P) 
               wv = acc[i];
             }
           const size_t o = 12 * (size_t)r + l16;
-          const float rv = __ldcg(P.r + o);
           P.u[o] = uc;
           P.q[o] = wv;
           s3[0] += (double)rv * (double)uc;
