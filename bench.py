@@ -295,7 +295,10 @@ def run_ours(a):
                      "peak": peak, "peak_kind": peak_kind, "unit": "GB/s", "frac": round(achieved / peak, 4),
                      "traffic": None, "bytes_per_launch": bytes_launch, "ms_per_launch": round(skin_ms, 5)},
         "gpu_launches": launches_per_step * a.steps,
-        "solve": {"pcg_iterations": stats["pcg_iterations"], "gn_iterations": stats["gn_iterations"],
+        "solve": {"bound": "latency (L2-resident persistent kernel; reported per PCG iteration)",
+                  "pcg_iterations": stats["pcg_iterations"], "gn_iterations": stats["gn_iterations"],
+                  "us_per_pcg_iteration": round(1000.0 * stats["phase_ms"]["pcg"] / max(1, stats["pcg_iterations"]), 2),
+                  "phase_ms": {k: round(v, 3) for k, v in stats["phase_ms"].items()},
                   "final_energy": stats["final_energy"]},
         "forms": {a.form: {"ms_per_frame": round(ms_step, 3), "pcg_iterations": stats["pcg_iterations"]},
                   other: {"ms_per_frame": round(float(np.mean(o_ms)), 3),
