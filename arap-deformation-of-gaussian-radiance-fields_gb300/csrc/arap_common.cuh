@@ -110,6 +110,23 @@ struct GridSync {
   // the barrier failed (timed out here or elsewhere).
   template <int NSLOT>
   __device__ bool reduce(double (&v)[NSLOT]) {
+#pragma unroll
+    for (int s = 0; s < NSLOT; ++s) v[s] = warp_sum(v[s]);
+    return reduce_warp_sums<NSLOT>(v);
+  }
+
+  // As reduce, for float contributions: the warp sums are taken in float
+  // (a warp holds a few dozen terms), everything above the warp in FP64.
+  template <int NSLOT>
+  __device__ bool reduce_f(const float (&vf)[NSLOT], double (&out)[NSLOT]) {
+#pragma unroll
+    for (int s = 0; s < NSLOT; ++s) out[s] = (double)warp_sum(vf[s]);
+    return reduce_warp_sums<NSLOT>(out);
+  }
+
+  // v[] holds the warp's sums (valid in lane 0) on entry.
+  template <int NSLOT>
+  __device__ bool reduce_warp_sums(double (&v)[NSLOT]) {
     static_assert(NSLOT >= 1 && NSLOT <= kReduceSlots, "slots");
     __shared__ double s_red[32][NSLOT];
     __shared__ double s_out[NSLOT];
@@ -118,8 +135,6 @@ struct GridSync {
     const unsigned int nb = gridDim.x;
     const unsigned int e = epoch++;
     double* buf = partials + (size_t)(e & 1u) * kReduceSlots * nb;
-#pragma unroll
-    for (int s = 0; s < NSLOT; ++s) v[s] = warp_sum(v[s]);
     if (lane == 0) {
 #pragma unroll
       for (int s = 0; s < NSLOT; ++s) s_red[w][s] = v[s];

@@ -167,7 +167,7 @@ __device__ __forceinline__ void coarse_solve(const SolveParams& P, const double*
   __syncthreads();
   const float4* s4 = reinterpret_cast<const float4*>(s_rc);
   for (int i = gw; i < NC; i += nw) {
-    double acc = 0.0;
+    float a = 0.f;
     if (ok) {
       const float4* row = reinterpret_cast<const float4*>(P.Cinv + (size_t)i * NC);
       float4 v[kRowVec];
@@ -176,7 +176,6 @@ __device__ __forceinline__ void coarse_solve(const SolveParams& P, const double*
         const int c = lane + 32 * q;
         v[q] = c < n4 ? __ldcg(row + c) : make_float4(0.f, 0.f, 0.f, 0.f);
       }
-      float a = 0.f;
 #pragma unroll
       for (int q = 0; q < kRowVec; ++q) {
         const int c = lane + 32 * q;
@@ -185,10 +184,9 @@ __device__ __forceinline__ void coarse_solve(const SolveParams& P, const double*
           a = fmaf(v[q].x, r4.x, fmaf(v[q].y, r4.y, fmaf(v[q].z, r4.z, fmaf(v[q].w, r4.w, a))));
         }
       }
-      acc = (double)a;
     }
-    acc = warp_sum(acc);
-    if (lane == 0) P.zc[i] = (float)acc;
+    a = warp_sum(a);
+    if (lane == 0) P.zc[i] = a;
   }
   for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < NC; e += gridDim.x * blockDim.x) rc_other[e] = 0.0;
   // w_con J_g u_f for the next products, on the warps the rows leave idle
@@ -435,7 +433,7 @@ __global__ void __launch_bounds__(kSolveThreads) gn_solve_kernel(SolveParams P) 
     // touches), w = (J^T J) u, and gamma = r.u, delta = w.u, r.r in one
     // reduction
     auto products = [&](double (&s3)[3]) -> bool {
-      s3[0] = s3[1] = s3[2] = 0.0;
+      float f3[3] = {0.f, 0.f, 0.f};
       work_begin();
       for (int base = 2 * gw; base < F; base += nhw) {
         const int oi = base + half;
@@ -455,13 +453,13 @@ __global__ void __launch_bounds__(kSolveThreads) gn_solve_kernel(SolveParams P) 
           const size_t o = 12 * (size_t)r + l16;
           P.u[o] = uc;
           P.q[o] = wv;
-          s3[0] += (double)rv * (double)uc;
-          s3[1] += (double)wv * (double)uc;
-          s3[2] += (double)rv * (double)rv;
+          f3[0] = fmaf(rv, uc, f3[0]);
+          f3[1] = fmaf(wv, uc, f3[1]);
+          f3[2] = fmaf(rv, rv, f3[2]);
         }
       }
       work_end(0);
-      return gs.reduce<3>(s3);
+      return gs.reduce_f<3>(f3, s3);
     };
     int cur = 0;  // rc buffer holding P^T r of the current residual
     if (coarse) {
