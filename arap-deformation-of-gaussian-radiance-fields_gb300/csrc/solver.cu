@@ -402,21 +402,14 @@ extern "C" int arap_solver_create(arap_solver** out, int n, int k, const int32_t
   e = e ? e : up(P.mem_rank, mem_rank.data(), mem_rank.size() * 4);
   e = e ? e : up(P.mem_node, mem_node.data(), mem_node.size() * 4);
   e = e ? e : up(P.mem_w, mem_w.data(), mem_w.size() * 4);
-  // cost-balanced processing order: heaviest nodes first, dealt to the warps
-  // in alternating direction so every warp gets a similar total
+  // processing order: costliest nodes first; the kernel deals order position
+  // p to CTA p % grid, so every SM gets its share of the expensive nodes
   std::vector<int32_t> order(F);
   {
     std::vector<std::pair<long long, int>> cost(F);
-    for (int r = 0; r < F; ++r) {
-      cost[r] = {-node_cost[r], r};
-    }
+    for (int r = 0; r < F; ++r) cost[r] = {-node_cost[r], r};
     std::sort(cost.begin(), cost.end());
-    const int nw = s->grid * (kSolveThreads / 32);
-    for (int i = 0; i < F; ++i) {
-      const int rd = i / nw, w = i % nw;
-      const int src = rd * nw + ((rd & 1) ? std::min(nw, F - rd * nw) - 1 - w : w);
-      order[i] = cost[src].second;
-    }
+    for (int i = 0; i < F; ++i) order[i] = cost[i].second;
   }
   e = e ? e : up(P.order, order.data(), order.size() * 4);
   if (NA > 0) {

@@ -202,6 +202,9 @@ __global__ void __launch_bounds__(kSolveThreads) gn_solve_kernel(SolveParams P) 
   const int gt = blockIdx.x * blockDim.x + threadIdx.x;
   const int nt = gridDim.x * blockDim.x;
   const int F = P.F, k = P.k;
+  // node order position p belongs to CTA p % gridDim.x: the costliest nodes
+  // (the order is by cost, descending) are spread over all SMs
+  const int wib = threadIdx.x >> 5, nbk = gridDim.x;
   GridSync gs{P.bar, P.partials, 0u};
   unsigned long long t_mark = global_ns();
   double t_acc[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};  // prep, grad, coarse, pcg, line search, inversion
@@ -354,8 +357,8 @@ __global__ void __launch_bounds__(kSolveThreads) gn_solve_kernel(SolveParams P) 
       }
     }
     if (!gs.sync()) return;
-    for (int oi = gw; oi < F; oi += nw) {
-      const int r = __ldg(P.order + oi);
+    for (int ws = wib; ws * nbk + (int)blockIdx.x < F; ws += kSolveWarps) {
+      const int r = __ldg(P.order + ws * nbk + blockIdx.x);
       RT acc[12];
       float Q[10];
       double en;
@@ -428,15 +431,14 @@ __global__ void __launch_bounds__(kSolveThreads) gn_solve_kernel(SolveParams P) 
     }
     const double tol2 = (double)P.pcg_tol * (double)P.pcg_tol * rr0;
     const int half = lane >> 4, l16 = lane & 15;
-    const int nhw = 2 * nw;
     // products: u = u_f + P zc (formed on the fly for every node a product
     // touches), w = (J^T J) u, and gamma = r.u, delta = w.u, r.r in one
     // reduction
     auto products = [&](double (&s3)[3]) -> bool {
       float f3[3] = {0.f, 0.f, 0.f};
       work_begin();
-      for (int base = 2 * gw; base < F; base += nhw) {
-        const int oi = base + half;
+      for (int hs0 = 2 * wib; hs0 * nbk + (int)blockIdx.x < F; hs0 += 2 * kSolveWarps) {
+        const int oi = (hs0 + half) * nbk + blockIdx.x;
         const bool valid = oi < F;
         const int r = valid ? __ldg(P.order + oi) : 0;
         const float rv = (valid && l16 < 12) ? __ldcg(P.r + 12 * (size_t)r + l16) : 0.f;
@@ -483,8 +485,8 @@ __global__ void __launch_bounds__(kSolveThreads) gn_solve_kernel(SolveParams P) 
       const bool first = pi == 0;
       double* rc_next = P.rc + (cur ^ 1) * P.NC;
       work_begin();
-      for (int base = 2 * gw; base < F; base += nhw) {
-        const int oi = base + half;
+      for (int hs0 = 2 * wib; hs0 * nbk + (int)blockIdx.x < F; hs0 += 2 * kSolveWarps) {
+        const int oi = (hs0 + half) * nbk + blockIdx.x;
         const bool valid = oi < F;
         const int r = valid ? __ldg(P.order + oi) : 0;
         float rv = 0.f;
@@ -537,8 +539,8 @@ __global__ void __launch_bounds__(kSolveThreads) gn_solve_kernel(SolveParams P) 
     double hh = 0.0;
     for (int ls = 0; ls < 50; ++ls) {
       double en2[2] = {0.0, 0.0};
-      for (int oi = gw; oi < F; oi += nw) {
-      const int r = __ldg(P.order + oi);
+      for (int ws = wib; ws * nbk + (int)blockIdx.x < F; ws += kSolveWarps) {
+        const int r = __ldg(P.order + ws * nbk + blockIdx.x);
         RT acc[12];
         float Q[10];
         double en;
