@@ -206,34 +206,45 @@ __global__ void __launch_bounds__(kSolveThreads) gn_solve_kernel(SolveParams P) 
   // (the order is by cost, descending) are spread over all SMs
   const int wib = threadIdx.x >> 5, nbk = gridDim.x;
   GridSync gs{P.bar, P.partials, 0u};
-  unsigned long long t_mark = global_ns();
-  double t_acc[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};  // prep, grad, coarse, pcg, line search, inversion
-  // PCG work of this CTA per phase kind (products, update, coarse solve): from
-  // leaving a barrier to the last warp of the CTA finishing its share (each
-  // warp posts its finish time; thread 0 reads the latest after the barrier)
-  __shared__ unsigned long long s_wend;
-  unsigned long long t_work[3] = {0ull, 0ull, 0ull};
-  unsigned long long t_w0 = 0ull;
-  int w_pend = -1;
-  if (threadIdx.x == 0) s_wend = 0ull;
+  // phase timers, thread 0's only, kept in shared memory rather than registers
+  // that would stay live through the whole kernel.  acc: prep, grad, coarse,
+  // pcg, line search, inversion (ns).  work: PCG work of this CTA per phase
+  // kind (products, update, coarse solve), from leaving a barrier to the last
+  // warp of the CTA finishing its share (each warp posts its finish time to
+  // wend; thread 0 reads the latest after the barrier).
+  __shared__ struct {
+    unsigned long long mark, w0, wend, inv0;
+    double acc[6];
+    unsigned long long work[3];
+    int pend;
+  } s_clk;
+  if (threadIdx.x == 0) {
+    s_clk.mark = global_ns();
+    s_clk.wend = 0ull;
+    s_clk.pend = -1;
+    for (int q = 0; q < 6; ++q) s_clk.acc[q] = 0.0;
+    for (int q = 0; q < 3; ++q) s_clk.work[q] = 0ull;
+  }
   auto work_flush = [&]() {
-    if (threadIdx.x == 0 && w_pend >= 0) {
-      t_work[w_pend] += s_wend - t_w0;
-      w_pend = -1;
+    if (threadIdx.x == 0 && s_clk.pend >= 0) {
+      s_clk.work[s_clk.pend] += s_clk.wend - s_clk.w0;
+      s_clk.pend = -1;
     }
   };
   auto work_begin = [&]() {
     work_flush();
-    if (threadIdx.x == 0) t_w0 = global_ns();
+    if (threadIdx.x == 0) s_clk.w0 = global_ns();
   };
   auto work_end = [&](int slot) {
-    if (lane == 0) atomicMax(&s_wend, global_ns());
-    if (threadIdx.x == 0) w_pend = slot;
+    if (lane == 0) atomicMax(&s_clk.wend, global_ns());
+    if (threadIdx.x == 0) s_clk.pend = slot;
   };
   auto lap = [&](int slot) {
-    const unsigned long long now = global_ns();
-    t_acc[slot] += (double)(now - t_mark);
-    t_mark = now;
+    if (threadIdx.x == 0) {
+      const unsigned long long now = global_ns();
+      s_clk.acc[slot] += (double)(now - s_clk.mark);
+      s_clk.mark = now;
+    }
   };
 
   // ---- per-frame geometry: member anchors, group targets, x = identity
@@ -423,9 +434,9 @@ __global__ void __launch_bounds__(kSolveThreads) gn_solve_kernel(SolveParams P) 
       for (size_t e = gt; e < NC2; e += nt) P.Cw[e] = coarse_entry_x(P, rot_now, (int)(e / P.NC), (int)(e % P.NC));
       for (int e = gt; e < 81 * P.NA; e += nt) rot_next[e] = 0.0;
       if (!gs.sync()) return;
-      const unsigned long long t_inv = global_ns();
+      if (threadIdx.x == 0) s_clk.inv0 = global_ns();
       if (!coarse_invert(P, gs, &coarse_ok, s_scratch)) return;
-      t_acc[5] += (double)(global_ns() - t_inv);
+      if (threadIdx.x == 0) s_clk.acc[5] += (double)(global_ns() - s_clk.inv0);
       if (!coarse_ok && gt == 0) raise_status(ARAP_ENONFINITE);
       lap(2);
     }
@@ -621,12 +632,12 @@ __global__ void __launch_bounds__(kSolveThreads) gn_solve_kernel(SolveParams P) 
     P.stats[ST_E0] = e_first;
     P.stats[ST_E] = e_last;
     P.stats[ST_CONV] = converged;
-    for (int q = 0; q < 6; ++q) P.stats[ST_T_PREP + q] = t_acc[q];
+    for (int q = 0; q < 6; ++q) P.stats[ST_T_PREP + q] = s_clk.acc[q];
   }
   if (threadIdx.x == 0)
     for (int q = 0; q < 3; ++q)
       atomicMax(reinterpret_cast<unsigned long long*>(P.stats + ST_T_W_SPMV + q),
-                (unsigned long long)__double_as_longlong((double)t_work[q]));
+                (unsigned long long)__double_as_longlong((double)s_clk.work[q]));
 }
 
 }  // namespace arap
