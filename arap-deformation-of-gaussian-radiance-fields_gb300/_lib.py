@@ -67,6 +67,11 @@ SIGNATURES = {
     "arap_solver_free_count": (I, [P]),
     "arap_solver_free_ids": (I, [P, P]),
     "arap_solver_destroy": (None, [P]),
+    "arap_solver_batch_create": (I, [P, P, I, F, P]),
+    "arap_solver_batch_solve": (I, [P, P, P, P, P, P, P]),
+    "arap_solver_batch_autotune": (I, [P, P, P, P, P, P, P]),
+    "arap_solver_batch_ctas": (I, [P, P]),
+    "arap_solver_batch_destroy": (None, [P]),
     "arap_node_table": (I, [I, P, P, P, P, P]),
     "arap_end_points": (I, [I, P, P, P, P, P, P]),
     "arap_skin_gaussians": (I, [I, I, P, P, P, P, P, P, P, P, P, P, P, I, P]),

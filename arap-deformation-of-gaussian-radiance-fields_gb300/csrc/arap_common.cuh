@@ -79,18 +79,22 @@ __device__ __forceinline__ T warp_sum(T v) {
   return v;
 }
 
-// Per-thread handle of the grid barrier.  Every thread of every CTA must make
+// Per-thread handle of the grid barrier over a group of nb co-resident CTAs
+// (the whole grid, or one instance's share of a batched launch); bid is this
+// CTA's index in the group.  Every thread of every CTA of the group must make
 // the same sequence of calls (the epoch is counted in registers).
 struct GridSync {
   GridBarrier* bar;
-  double* partials;  // [2][gridDim.x][kReduceSlots]
+  double* partials;  // [2][nb][kReduceSlots]
   unsigned int epoch;
+  unsigned int nb;
+  unsigned int bid;
 
   // One thread per CTA: arrive at barrier e (release) and wait (acquire) for
   // every CTA; bounded, false on failure.
   __device__ bool arrive_and_wait(unsigned int e) {
     red_release_add_u32(&bar->count, 1u);
-    const unsigned int target = (e + 1u) * gridDim.x;
+    const unsigned int target = (e + 1u) * nb;
     long long it = 0;
     while ((int)(ld_acquire_u32(&bar->count) - target) < 0) {
       ++it;
@@ -132,7 +136,6 @@ struct GridSync {
     __shared__ double s_out[NSLOT];
     __shared__ int s_ok;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    const unsigned int nb = gridDim.x;
     const unsigned int e = epoch++;
     double* buf = partials + (size_t)(e & 1u) * kReduceSlots * nb;
     if (lane == 0) {
@@ -146,7 +149,7 @@ struct GridSync {
       for (int s = 0; s < NSLOT; ++s) {
         double c = lane < nw ? s_red[lane][s] : 0.0;
         c = warp_sum(c);
-        if (lane == 0) buf[(size_t)blockIdx.x * kReduceSlots + s] = c;
+        if (lane == 0) buf[(size_t)bid * kReduceSlots + s] = c;
       }
       int ok = 1;
       if (lane == 0) ok = arrive_and_wait(e);

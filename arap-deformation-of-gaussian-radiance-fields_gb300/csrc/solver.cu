@@ -448,6 +448,27 @@ extern "C" int arap_solver_create(arap_solver** out, int n, int k, const int32_t
   return ARAP_OK;
 }
 
+// Host stats of one solve from its device slots; returns the call's status
+// (ARAP_NOT_CONVERGED is reported in the stats only).
+static int fill_stats(const arap_solver* s, const double* st8, int dev_status, arap_solve_stats* stats_host) {
+  std::memset(stats_host, 0, sizeof(*stats_host));
+  stats_host->gn_iterations = (int)st8[ST_ITERS];
+  stats_host->pcg_iterations = (int)st8[ST_PCG];
+  stats_host->halvings = (int)st8[ST_HALV];
+  stats_host->initial_energy = st8[ST_E0];
+  stats_host->final_energy = st8[ST_E];
+  stats_host->n_free = s->F;
+  stats_host->n_static = s->S;
+  stats_host->n_rows = s->n_rows;
+  for (int q = 0; q < 9; ++q) stats_host->phase_ms[q] = st8[ST_T_PREP + q] * 1e-6;
+  stats_host->n_coarse = s->P.NC;
+  int status = dev_status;
+  if (status == ARAP_OK && s->cfg.early_exit && st8[ST_CONV] == 0.0 && s->cfg.max_iters > 0)
+    status = ARAP_NOT_CONVERGED;
+  stats_host->status = status;
+  return status == ARAP_NOT_CONVERGED ? ARAP_OK : status;
+}
+
 static int launch_solver(arap_solver* s, cudaStream_t st) {
   if (cudaMemsetAsync(s->P.bar, 0, sizeof(GridBarrier), st) != cudaSuccess) return ARAP_ECUDA;
   void* args[] = {&s->P};
@@ -480,22 +501,7 @@ extern "C" int arap_solver_solve(arap_solver* s, const float* node_pos, const fl
   double st8[kStatSlots];
   ARAP_CUDA_TRY(cudaMemcpyAsync(st8, s->P.stats, sizeof(st8), cudaMemcpyDeviceToHost, st));
   const int dev_status = arap_get_device_status(stream);  // synchronises
-  std::memset(stats_host, 0, sizeof(*stats_host));
-  stats_host->gn_iterations = (int)st8[ST_ITERS];
-  stats_host->pcg_iterations = (int)st8[ST_PCG];
-  stats_host->halvings = (int)st8[ST_HALV];
-  stats_host->initial_energy = st8[ST_E0];
-  stats_host->final_energy = st8[ST_E];
-  stats_host->n_free = s->F;
-  stats_host->n_static = s->S;
-  stats_host->n_rows = s->n_rows;
-  for (int q = 0; q < 9; ++q) stats_host->phase_ms[q] = st8[ST_T_PREP + q] * 1e-6;
-  stats_host->n_coarse = s->P.NC;
-  int status = dev_status;
-  if (status == ARAP_OK && s->cfg.early_exit && st8[ST_CONV] == 0.0 && s->cfg.max_iters > 0)
-    status = ARAP_NOT_CONVERGED;
-  stats_host->status = status;
-  return status == ARAP_NOT_CONVERGED ? ARAP_OK : status;
+  return fill_stats(s, st8, dev_status, stats_host);
 }
 
 extern "C" int arap_solver_energy_grad(arap_solver* s, const float* node_pos, const float* aims, const double* x,
@@ -537,4 +543,241 @@ extern "C" void arap_solver_destroy(arap_solver* s) {
   if (!s) return;
   if (s->block) cudaFree(s->block);
   delete s;
+}
+
+// ------------------------------------------------------------ batches ----
+struct arap_solver_batch {
+  std::vector<arap_solver*> solvers;
+  int precision = 0;
+  int grid = 0;                 // co-resident CTAs of the batched kernel
+  float exponent = 1.f;         // CTA share ~ (coupling items + free nodes)^exponent
+  std::vector<int> cta_first;   // [count+1]
+  void* block = nullptr;        // device: params, cta_first, barriers, partials
+  SolveParams* d_params = nullptr;
+  int* d_cta_first = nullptr;
+  GridBarrier* d_bars = nullptr;
+  double* d_partials = nullptr;
+  SolveParams* h_params = nullptr;  // pinned staging of the parameter array
+  cudaEvent_t staged{};             // the last upload of h_params has been read
+  bool staged_valid = false;
+};
+
+namespace {
+
+// CTA ranges of a batch: every instance gets at least one CTA, the rest in
+// proportion to its work estimate raised to the exponent (largest remainders).
+void split_ctas(arap_solver_batch* b) {
+  const int count = (int)b->solvers.size();
+  std::vector<double> w(count);
+  double sum = 0.0;
+  for (int i = 0; i < count; ++i) {
+    const arap_solver* s = b->solvers[i];
+    w[i] = std::pow((double)(s->n_items + s->F) + 1.0, (double)b->exponent);
+    sum += w[i];
+  }
+  const int spare = b->grid - count;
+  std::vector<int> n(count, 1);
+  std::vector<std::pair<double, int>> rem(count);
+  int given = 0;
+  for (int i = 0; i < count; ++i) {
+    const double share = spare * w[i] / sum;
+    const int whole = (int)std::floor(share);
+    n[i] += whole;
+    given += whole;
+    rem[i] = {-(share - whole), i};
+  }
+  std::sort(rem.begin(), rem.end());
+  for (int q = 0; q < spare - given; ++q) n[rem[q % count].second] += 1;
+  b->cta_first.assign(count + 1, 0);
+  for (int i = 0; i < count; ++i) b->cta_first[i + 1] = b->cta_first[i] + n[i];
+}
+
+// The CTA ranges go to the device when they change (creation, autotuning),
+// never inside a solve, so a solve can be captured in a CUDA graph.
+int upload_ctas(arap_solver_batch* b) {
+  if (cudaMemcpy(b->d_cta_first, b->cta_first.data(), sizeof(int) * b->cta_first.size(), cudaMemcpyHostToDevice) !=
+      cudaSuccess) {
+    (void)cudaGetLastError();
+    return ARAP_ECUDA;
+  }
+  return ARAP_OK;
+}
+
+template <typename RT>
+int batch_grid() {
+  int dev = 0, sms = 0, per_sm = 0, coop = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return -1;
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return -1;
+  if (cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev) != cudaSuccess || !coop) return -1;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, gn_solve_batch_kernel<RT>, kSolveThreads, 0) !=
+      cudaSuccess || per_sm < 1)
+    return -1;
+  return std::min(sms * std::min(per_sm, 2), kMaxGridCtas);
+}
+
+}  // namespace
+
+extern "C" int arap_solver_batch_create(arap_solver_batch** out, arap_solver* const* solvers, int count,
+                                        float balance_exponent, arap_stream_t stream) {
+  (void)stream;
+  if (!out || !solvers || count < 1) return ARAP_EBADINPUT;
+  *out = nullptr;
+  for (int i = 0; i < count; ++i)
+    if (!solvers[i] || solvers[i]->cfg.precision != solvers[0]->cfg.precision) return ARAP_EBADINPUT;
+  auto* b = new (std::nothrow) arap_solver_batch();
+  if (!b) return ARAP_ENOMEM;
+  b->solvers.assign(solvers, solvers + count);
+  b->precision = solvers[0]->cfg.precision;
+  b->grid = b->precision == ARAP_PRECISION_MIXED ? batch_grid<double>() : batch_grid<float>();
+  if (b->grid <= 0) {
+    delete b;
+    return ARAP_ECUDA;
+  }
+  if (count > b->grid) {
+    delete b;
+    return ARAP_EUNSUPPORTED;
+  }
+  b->exponent = balance_exponent > 0.f ? balance_exponent : 1.f;
+  split_ctas(b);
+  Carver sizing{nullptr};
+  auto carve = [&](Carver& cv) {
+    b->d_params = cv.take<SolveParams>(count);
+    b->d_cta_first = cv.take<int>(count + 1);
+    b->d_bars = cv.take<GridBarrier>(count);
+    b->d_partials = cv.take<double>((size_t)2 * kReduceSlots * b->grid);
+  };
+  carve(sizing);
+  if (cudaMalloc(&b->block, sizing.off + 256) != cudaSuccess ||
+      cudaMallocHost(reinterpret_cast<void**>(&b->h_params), sizeof(SolveParams) * count) != cudaSuccess ||
+      cudaEventCreateWithFlags(&b->staged, cudaEventDisableTiming) != cudaSuccess) {
+    (void)cudaGetLastError();
+    arap_solver_batch_destroy(b);
+    return ARAP_ENOMEM;
+  }
+  Carver cv{static_cast<char*>(b->block)};
+  carve(cv);
+  if (upload_ctas(b) != ARAP_OK) {
+    arap_solver_batch_destroy(b);
+    return ARAP_ECUDA;
+  }
+  *out = b;
+  return ARAP_OK;
+}
+
+extern "C" int arap_solver_batch_solve(arap_solver_batch* b, const float* const* node_pos, const float* const* aims,
+                                       float* const* rot_out, float* const* trans_out, arap_solve_stats* stats_host,
+                                       arap_stream_t stream) {
+  if (!b || !node_pos || !aims || !rot_out || !trans_out) return ARAP_EBADINPUT;
+  const int count = (int)b->solvers.size();
+  for (int i = 0; i < count; ++i)
+    if (!node_pos[i] || !aims[i] || !rot_out[i] || !trans_out[i]) return ARAP_EBADINPUT;
+  cudaStream_t st = (cudaStream_t)stream;
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  ARAP_CUDA_TRY(cudaStreamIsCapturing(st, &cap));
+  // the previous upload of the staging array must have been read before it is rewritten
+  if (b->staged_valid && cap == cudaStreamCaptureStatusNone) ARAP_CUDA_TRY(cudaEventSynchronize(b->staged));
+  for (int i = 0; i < count; ++i) {
+    SolveParams P = b->solvers[i]->P;
+    P.node_pos = node_pos[i];
+    P.aims = aims[i];
+    P.rot_out = rot_out[i];
+    P.trans_out = trans_out[i];
+    P.mode = 0;
+    P.x_in = nullptr;
+    P.grad_out = nullptr;
+    P.bar = b->d_bars + i;
+    P.partials = b->d_partials + (size_t)2 * kReduceSlots * b->cta_first[i];
+    b->h_params[i] = P;
+  }
+  ARAP_CUDA_TRY(cudaMemcpyAsync(b->d_params, b->h_params, sizeof(SolveParams) * count, cudaMemcpyHostToDevice, st));
+  if (cap == cudaStreamCaptureStatusNone) {
+    ARAP_CUDA_TRY(cudaEventRecord(b->staged, st));
+    b->staged_valid = true;
+  }
+  ARAP_CUDA_TRY(cudaMemsetAsync(b->d_bars, 0, sizeof(GridBarrier) * count, st));
+  void* args[] = {&b->d_params, &b->d_cta_first, const_cast<int*>(&count)};
+  cudaError_t e;
+  if (b->precision == ARAP_PRECISION_MIXED)
+    e = cudaLaunchCooperativeKernel((const void*)gn_solve_batch_kernel<double>, b->grid, kSolveThreads, args, 0, st);
+  else
+    e = cudaLaunchCooperativeKernel((const void*)gn_solve_batch_kernel<float>, b->grid, kSolveThreads, args, 0, st);
+  if (e != cudaSuccess) {
+    (void)cudaGetLastError();
+    return ARAP_ECUDA;
+  }
+  if (!stats_host) return ARAP_OK;
+  std::vector<double> st8((size_t)kStatSlots * count);
+  for (int i = 0; i < count; ++i)
+    ARAP_CUDA_TRY(cudaMemcpyAsync(st8.data() + (size_t)kStatSlots * i, b->solvers[i]->P.stats,
+                                  sizeof(double) * kStatSlots, cudaMemcpyDeviceToHost, st));
+  const int dev_status = arap_get_device_status(stream);  // synchronises
+  int status = ARAP_OK;
+  for (int i = 0; i < count; ++i) {
+    const int si = fill_stats(b->solvers[i], st8.data() + (size_t)kStatSlots * i, dev_status, stats_host + i);
+    if (status == ARAP_OK) status = si;
+  }
+  return status;
+}
+
+extern "C" int arap_solver_batch_autotune(arap_solver_batch* b, const float* const* node_pos,
+                                          const float* const* aims, float* const* rot_out, float* const* trans_out,
+                                          float* best_exponent, arap_stream_t stream) {
+  if (!b) return ARAP_EBADINPUT;
+  cudaStream_t st = (cudaStream_t)stream;
+  const float candidates[] = {0.5f, 0.75f, 1.0f, 1.25f};
+  float best = b->exponent, best_ms = 1e30f;
+  cudaEvent_t e0, e1;
+  ARAP_CUDA_TRY(cudaEventCreate(&e0));
+  if (cudaEventCreate(&e1) != cudaSuccess) {
+    cudaEventDestroy(e0);
+    return ARAP_ECUDA;
+  }
+  int rc = ARAP_OK;
+  for (float c : candidates) {
+    b->exponent = c;
+    split_ctas(b);
+    if ((rc = upload_ctas(b)) != ARAP_OK) break;
+    // one untimed solve, then the timed one
+    rc = arap_solver_batch_solve(b, node_pos, aims, rot_out, trans_out, nullptr, stream);
+    if (rc != ARAP_OK) break;
+    if (cudaEventRecord(e0, st) != cudaSuccess) {
+      rc = ARAP_ECUDA;
+      break;
+    }
+    rc = arap_solver_batch_solve(b, node_pos, aims, rot_out, trans_out, nullptr, stream);
+    if (rc != ARAP_OK) break;
+    float ms = 0.f;
+    if (cudaEventRecord(e1, st) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess ||
+        cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess) {
+      rc = ARAP_ECUDA;
+      break;
+    }
+    if (ms < best_ms) {
+      best_ms = ms;
+      best = c;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  b->exponent = best;
+  split_ctas(b);
+  if (rc == ARAP_OK) rc = upload_ctas(b);
+  if (best_exponent) *best_exponent = best;
+  if (rc != ARAP_OK) return rc;
+  return arap_get_device_status(stream);
+}
+
+extern "C" int arap_solver_batch_ctas(const arap_solver_batch* b, int32_t* cta_first_host) {
+  if (!b || !cta_first_host) return ARAP_EBADINPUT;
+  std::copy(b->cta_first.begin(), b->cta_first.end(), cta_first_host);
+  return ARAP_OK;
+}
+
+extern "C" void arap_solver_batch_destroy(arap_solver_batch* b) {
+  if (!b) return;
+  if (b->staged_valid) cudaEventSynchronize(b->staged);
+  if (b->staged) cudaEventDestroy(b->staged);
+  if (b->h_params) cudaFreeHost(b->h_params);
+  if (b->block) cudaFree(b->block);
+  delete b;
 }

@@ -56,8 +56,8 @@ __device__ bool coarse_invert(const SolveParams& P, GridSync& gs, int* ok, float
   const int NC = P.NC;
   const size_t NC2 = (size_t)NC * NC;
   const int tid = threadIdx.x, bd = blockDim.x, lane = tid & 31;
-  const int R = (NC + gridDim.x - 1) / gridDim.x;
-  const int r_begin = min(NC, (int)blockIdx.x * R), r_end = min(NC, r_begin + R);
+  const int R = (NC + (int)gs.nb - 1) / (int)gs.nb;
+  const int r_begin = min(NC, (int)gs.bid * R), r_end = min(NC, r_begin + R);
   int src_i = 0;
   *ok = 1;
   __shared__ int s_bad;
@@ -157,11 +157,11 @@ __device__ bool coarse_invert(const SolveParams& P, GridSync& gs, int* ok, float
 // staged in shared memory), zero the other restriction buffer, and the group
 // products w_con J_g u_f.  Every thread of the CTA calls it.
 constexpr int kRowVec = (kMaxCoarse / 4 + 31) / 32;  // float4 loads per lane of a row
-__device__ __forceinline__ void coarse_solve(const SolveParams& P, const double* rc, double* rc_other, int ok,
-                                             float* s_rc) {
+__device__ __forceinline__ void coarse_solve(const SolveParams& P, const GridSync& gs, const double* rc,
+                                             double* rc_other, int ok, float* s_rc) {
   const int lane = threadIdx.x & 31;
-  const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int nw = (gridDim.x * blockDim.x) >> 5;
+  const int gw = (int)(gs.bid * blockDim.x + threadIdx.x) >> 5;
+  const int nw = (int)(gs.nb * blockDim.x) >> 5;
   const int NC = P.NC, n4 = NC / 4;
   for (int e = threadIdx.x; e < NC; e += blockDim.x) s_rc[e] = (float)__ldcg(rc + e);
   __syncthreads();
@@ -188,24 +188,26 @@ __device__ __forceinline__ void coarse_solve(const SolveParams& P, const double*
     a = warp_sum(a);
     if (lane == 0) P.zc[i] = a;
   }
-  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < NC; e += gridDim.x * blockDim.x) rc_other[e] = 0.0;
+  for (int e = gs.bid * blockDim.x + threadIdx.x; e < NC; e += gs.nb * blockDim.x) rc_other[e] = 0.0;
   // w_con J_g u_f for the next products, on the warps the rows leave idle
   for (int g = nw - 1 - gw; g < P.G; g += nw) con_jz_group(P, g);
 }
 
+// The whole solve on a group of nbk co-resident CTAs; bid is this CTA's index
+// in the group.
 template <typename RT>
-__global__ void __launch_bounds__(kSolveThreads) gn_solve_kernel(SolveParams P) {
+__device__ __forceinline__ void solve_body(const SolveParams& P, int bid, int nbk) {
   __shared__ __align__(16) float s_scratch[kScratchFloats];
   const int lane = threadIdx.x & 31;
-  const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int nw = (gridDim.x * blockDim.x) >> 5;
-  const int gt = blockIdx.x * blockDim.x + threadIdx.x;
-  const int nt = gridDim.x * blockDim.x;
+  const int gw = (bid * (int)blockDim.x + (int)threadIdx.x) >> 5;
+  const int nw = (nbk * (int)blockDim.x) >> 5;
+  const int gt = bid * (int)blockDim.x + (int)threadIdx.x;
+  const int nt = nbk * (int)blockDim.x;
   const int F = P.F, k = P.k;
-  // node order position p belongs to CTA p % gridDim.x: the costliest nodes
-  // (the order is by cost, descending) are spread over all SMs
-  const int wib = threadIdx.x >> 5, nbk = gridDim.x;
-  GridSync gs{P.bar, P.partials, 0u};
+  // node order position p belongs to CTA p % nbk: the costliest nodes (the
+  // order is by cost, descending) are spread over all SMs
+  const int wib = threadIdx.x >> 5;
+  GridSync gs{P.bar, P.partials, 0u, (unsigned int)nbk, (unsigned int)bid};
   // phase timers, thread 0's only, kept in shared memory rather than registers
   // that would stay live through the whole kernel.  acc: prep, grad, coarse,
   // pcg, line search, inversion (ns).  work: PCG work of this CTA per phase
@@ -368,8 +370,8 @@ __global__ void __launch_bounds__(kSolveThreads) gn_solve_kernel(SolveParams P) 
       }
     }
     if (!gs.sync()) return;
-    for (int ws = wib; ws * nbk + (int)blockIdx.x < F; ws += kSolveWarps) {
-      const int r = __ldg(P.order + ws * nbk + blockIdx.x);
+    for (int ws = wib; ws * nbk + bid < F; ws += kSolveWarps) {
+      const int r = __ldg(P.order + ws * nbk + bid);
       RT acc[12];
       float Q[10];
       double en;
@@ -448,8 +450,8 @@ __global__ void __launch_bounds__(kSolveThreads) gn_solve_kernel(SolveParams P) 
     auto products = [&](double (&s3)[3]) -> bool {
       float f3[3] = {0.f, 0.f, 0.f};
       work_begin();
-      for (int hs0 = 2 * wib; hs0 * nbk + (int)blockIdx.x < F; hs0 += 2 * kSolveWarps) {
-        const int oi = (hs0 + half) * nbk + blockIdx.x;
+      for (int hs0 = 2 * wib; hs0 * nbk + bid < F; hs0 += 2 * kSolveWarps) {
+        const int oi = (hs0 + half) * nbk + bid;
         const bool valid = oi < F;
         const int r = valid ? __ldg(P.order + oi) : 0;
         const float rv = (valid && l16 < 12) ? __ldcg(P.r + 12 * (size_t)r + l16) : 0.f;
@@ -477,7 +479,7 @@ __global__ void __launch_bounds__(kSolveThreads) gn_solve_kernel(SolveParams P) 
     int cur = 0;  // rc buffer holding P^T r of the current residual
     if (coarse) {
       work_begin();
-      coarse_solve(P, P.rc, P.rc + P.NC, coarse_ok, s_scratch);
+      coarse_solve(P, gs, P.rc, P.rc + P.NC, coarse_ok, s_scratch);
       work_end(2);
       if (!gs.sync()) return;
     }
@@ -496,8 +498,8 @@ __global__ void __launch_bounds__(kSolveThreads) gn_solve_kernel(SolveParams P) 
       const bool first = pi == 0;
       double* rc_next = P.rc + (cur ^ 1) * P.NC;
       work_begin();
-      for (int hs0 = 2 * wib; hs0 * nbk + (int)blockIdx.x < F; hs0 += 2 * kSolveWarps) {
-        const int oi = (hs0 + half) * nbk + blockIdx.x;
+      for (int hs0 = 2 * wib; hs0 * nbk + bid < F; hs0 += 2 * kSolveWarps) {
+        const int oi = (hs0 + half) * nbk + bid;
         const bool valid = oi < F;
         const int r = valid ? __ldg(P.order + oi) : 0;
         float rv = 0.f;
@@ -522,7 +524,7 @@ __global__ void __launch_bounds__(kSolveThreads) gn_solve_kernel(SolveParams P) 
       cur ^= 1;
       if (coarse) {
         work_begin();
-        coarse_solve(P, P.rc + cur * P.NC, P.rc + (cur ^ 1) * P.NC, coarse_ok, s_scratch);
+        coarse_solve(P, gs, P.rc + cur * P.NC, P.rc + (cur ^ 1) * P.NC, coarse_ok, s_scratch);
         work_end(2);
         if (!gs.sync()) return;
       }
@@ -550,8 +552,8 @@ __global__ void __launch_bounds__(kSolveThreads) gn_solve_kernel(SolveParams P) 
     double hh = 0.0;
     for (int ls = 0; ls < 50; ++ls) {
       double en2[2] = {0.0, 0.0};
-      for (int ws = wib; ws * nbk + (int)blockIdx.x < F; ws += kSolveWarps) {
-        const int r = __ldg(P.order + ws * nbk + blockIdx.x);
+      for (int ws = wib; ws * nbk + bid < F; ws += kSolveWarps) {
+        const int r = __ldg(P.order + ws * nbk + bid);
         RT acc[12];
         float Q[10];
         double en;
@@ -638,6 +640,35 @@ __global__ void __launch_bounds__(kSolveThreads) gn_solve_kernel(SolveParams P) 
     for (int q = 0; q < 3; ++q)
       atomicMax(reinterpret_cast<unsigned long long*>(P.stats + ST_T_W_SPMV + q),
                 (unsigned long long)__double_as_longlong((double)s_clk.work[q]));
+}
+
+template <typename RT>
+__global__ void __launch_bounds__(kSolveThreads) gn_solve_kernel(SolveParams P) {
+  solve_body<RT>(P, blockIdx.x, gridDim.x);
+}
+
+// Batched solves: CTAs cta_first[i] .. cta_first[i+1]-1 of the cooperative
+// grid run instance i with their own barrier; the instance's parameters are
+// copied into shared memory.
+template <typename RT>
+__global__ void __launch_bounds__(kSolveThreads)
+    gn_solve_batch_kernel(const SolveParams* __restrict__ params, const int* __restrict__ cta_first, int count) {
+  __shared__ SolveParams s_P;
+  __shared__ int s_inst;
+  if (threadIdx.x == 0) {
+    int i = 0;
+    while (i + 1 < count && cta_first[i + 1] <= (int)blockIdx.x) ++i;
+    s_inst = i;
+  }
+  __syncthreads();
+  const int i = s_inst;
+  {
+    const int* src = reinterpret_cast<const int*>(params + i);
+    int* dst = reinterpret_cast<int*>(&s_P);
+    for (int q = threadIdx.x; q < (int)(sizeof(SolveParams) / sizeof(int)); q += blockDim.x) dst[q] = src[q];
+  }
+  __syncthreads();
+  solve_body<RT>(s_P, (int)blockIdx.x - cta_first[i], cta_first[i + 1] - cta_first[i]);
 }
 
 }  // namespace arap

@@ -180,6 +180,72 @@ class Solver:
 
 # ------------------------------------------------------------ skinning ----
 
+class SolverBatch:
+    """Several Solvers (one precision) solved in one cooperative launch
+    (arap_solver_batch_*): the grid's CTAs are split among the instances."""
+
+    def __init__(self, solvers, balance_exponent=1.0):
+        self.solvers = list(solvers)
+        n = len(self.solvers)
+        hs = (C.c_void_p * n)(*[s._h.value for s in self.solvers])
+        h = C.c_void_p()
+        check("arap_solver_batch_create", _lib_().arap_solver_batch_create(
+            C.byref(h), C.cast(hs, C.c_void_p), n, float(balance_exponent), _s()))
+        self._h = h
+
+    def _ptrs(self, tensors):
+        return (C.c_void_p * len(tensors))(*[t.data_ptr() for t in tensors])
+
+    def _outputs(self, rot_out, trans_out):
+        if rot_out is None:
+            rot_out = [torch.empty((s.n, 9), dtype=torch.float32, device="cuda") for s in self.solvers]
+        if trans_out is None:
+            trans_out = [torch.empty((s.n, 3), dtype=torch.float32, device="cuda") for s in self.solvers]
+        return rot_out, trans_out
+
+    def solve(self, node_pos, aims, rot_out=None, trans_out=None, stats=True):
+        """Lists of per-instance inputs and outputs; with ``stats`` the stream is
+        synchronised and the per-instance statistics are returned."""
+        node_pos = [_f32(x) for x in node_pos]
+        aims = [_f32(x) for x in aims]
+        rot_out, trans_out = self._outputs(rot_out, trans_out)
+        self._keep = (node_pos, aims, rot_out, trans_out)  # pointers stay valid while queued
+        n = len(self.solvers)
+        st = (SolveStats * n)() if stats else None
+        code = _lib_().arap_solver_batch_solve(
+            self._h, C.cast(self._ptrs(node_pos), C.c_void_p), C.cast(self._ptrs(aims), C.c_void_p),
+            C.cast(self._ptrs(rot_out), C.c_void_p), C.cast(self._ptrs(trans_out), C.c_void_p),
+            C.cast(st, C.c_void_p) if st is not None else None, _s())
+        check("arap_solver_batch_solve", code)
+        return rot_out, trans_out, ([x.as_dict() for x in st] if st is not None else None)
+
+    def autotune(self, node_pos, aims):
+        node_pos = [_f32(x) for x in node_pos]
+        aims = [_f32(x) for x in aims]
+        rot_out, trans_out = self._outputs(None, None)
+        best = C.c_float()
+        check("arap_solver_batch_autotune", _lib_().arap_solver_batch_autotune(
+            self._h, C.cast(self._ptrs(node_pos), C.c_void_p), C.cast(self._ptrs(aims), C.c_void_p),
+            C.cast(self._ptrs(rot_out), C.c_void_p), C.cast(self._ptrs(trans_out), C.c_void_p), C.byref(best), _s()))
+        return best.value
+
+    def ctas(self):
+        out = (C.c_int32 * (len(self.solvers) + 1))()
+        check("arap_solver_batch_ctas", _lib_().arap_solver_batch_ctas(self._h, C.cast(out, C.c_void_p)))
+        return list(out)
+
+    def close(self):
+        if getattr(self, "_h", None) is not None and self._h.value:
+            _lib_().arap_solver_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def node_table(rot, trans, node_pos):
     n = rot.shape[0]
     out = torch.empty((n, 16), dtype=torch.float32, device="cuda")

@@ -157,6 +157,11 @@ def restore(st, snap):
         getattr(st, n).copy_(t)
 
 
+# DRAM bytes per launch of skin_gaussians_kernel measured by ncu on the named
+# workload (dram__bytes_read.sum + dram__bytes_write.sum of one launch).
+SKIN_DRAM_BYTES = {("twist300k", 8): 252_920_320}
+
+
 def skin_bytes_per_gaussian(k, with_shs=True, with_cov=True):
     """Algorithmic bytes of arap_skin_gaussians per Gaussian: read 6 endpoints
     (72), 6k indices + 6k weights (48k), scale0 (12), previous q (16), SH (192);
@@ -293,7 +298,9 @@ def run_ours(a):
                 "h2d_bytes_per_step": int(st.n * 12), "d2h_bytes_per_step": int(st.n * 48)},
         "roofline": {"kernel": "arap_skin_gaussians", "bound": "hbm", "achieved": round(achieved, 1),
                      "peak": peak, "peak_kind": peak_kind, "unit": "GB/s", "frac": round(achieved / peak, 4),
-                     "traffic": None, "bytes_per_launch": bytes_launch, "ms_per_launch": round(skin_ms, 5)},
+                     "traffic": SKIN_DRAM_BYTES.get((sc.name, k)), "traffic_source": "ncu dram__bytes_read.sum + "
+                     "dram__bytes_write.sum, one launch (profiles/skin_gaussians_twist300k.md)",
+                     "bytes_per_launch": bytes_launch, "ms_per_launch": round(skin_ms, 5)},
         "gpu_launches": launches_per_step * a.steps,
         "solve": {"bound": "latency (L2-resident persistent kernel; reported per PCG iteration)",
                   "pcg_iterations": stats["pcg_iterations"], "gn_iterations": stats["gn_iterations"],

@@ -147,6 +147,42 @@ int arap_solver_free_ids(const arap_solver* s, int32_t* free_ids_host);
 
 void arap_solver_destroy(arap_solver* s);
 
+/* No counterpart in the reference, whose viewer deforms one field at a time:
+ * several independent solves in one cooperative persistent launch.
+ * - The co-resident grid (one CTA per SM) is split among the instances: each
+ *   gets at least one CTA, the rest go in proportion to (coupling items + free
+ *   nodes)^balance_exponent (<= 0: 1).
+ * - Each instance runs the same Gauss-Newton/PCG iteration as
+ *   arap_solver_solve on its own CTAs, with its own grid barrier and its own
+ *   solver's buffers. Results equal separate solves to rounding (reduction
+ *   order).
+ * - All solvers must share one precision, and count may not exceed the grid
+ *   (ARAP_EUNSUPPORTED).
+ * - A solver may belong to several batches but must not run in two launches
+ *   at once. */
+typedef struct arap_solver_batch arap_solver_batch;
+int arap_solver_batch_create(arap_solver_batch** out, arap_solver* const* solvers, int count,
+                             float balance_exponent, arap_stream_t stream);
+/* node_pos, aims, rot_out, trans_out: host arrays of count device pointers,
+ * with the meaning of arap_solver_solve's arguments. stats_host: NULL (no
+ * synchronisation) or count entries (synchronises).
+ * Without stats the call queues two copies (a pinned upload of the instances'
+ * parameters, a barrier reset) and one cooperative launch, all on `stream`.
+ * It can therefore be captured in a CUDA graph. A replay reads the parameter
+ * staging as left by the most recent call on this batch. */
+int arap_solver_batch_solve(arap_solver_batch* batch, const float* const* node_pos, const float* const* aims,
+                            float* const* rot_out, float* const* trans_out, arap_solve_stats* stats_host,
+                            arap_stream_t stream);
+/* Autotuner of the CTA split: times one batch solve for each balance exponent
+ * in {0.5, 0.75, 1, 1.25} (after an untimed one) and keeps the fastest.
+ * Outputs are written by the trial solves. Synchronises. */
+int arap_solver_batch_autotune(arap_solver_batch* batch, const float* const* node_pos, const float* const* aims,
+                               float* const* rot_out, float* const* trans_out, float* best_exponent,
+                               arap_stream_t stream);
+/* cta_first_host [count+1]: instance i runs on CTAs cta_first[i] .. cta_first[i+1]-1. */
+int arap_solver_batch_ctas(const arap_solver_batch* batch, int32_t* cta_first_host);
+void arap_solver_batch_destroy(arap_solver_batch* batch);
+
 /* ------------------------------------------------------------ skinning --- */
 
 /* Per-node transform table used by every skinning call: for node j
