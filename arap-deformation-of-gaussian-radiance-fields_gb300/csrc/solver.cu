@@ -724,7 +724,7 @@ extern "C" int arap_solver_batch_autotune(arap_solver_batch* b, const float* con
                                           float* best_exponent, arap_stream_t stream) {
   if (!b) return ARAP_EBADINPUT;
   cudaStream_t st = (cudaStream_t)stream;
-  const float candidates[] = {0.5f, 0.75f, 1.0f, 1.25f};
+  const float candidates[] = {0.75f, 1.0f, 1.25f, 1.5f, 2.0f};
   float best = b->exponent, best_ms = 1e30f;
   cudaEvent_t e0, e1;
   ARAP_CUDA_TRY(cudaEventCreate(&e0));

@@ -33,7 +33,7 @@ import math
 
 import numpy as np
 
-__all__ = ["Scene", "make_scene", "build_scene", "SCENES"]
+__all__ = ["Scene", "Instance", "make_scene", "build_scene", "batch_instances", "SCENES"]
 
 
 @dataclasses.dataclass
@@ -196,6 +196,64 @@ def _stress(n, seed, n_nodes=30000, grid_num=128, k=12, iters=30):
     return build_scene("stress%dk" % (n // 1000), pos, (-9.0, -4.0, -4.0),
                        (0.3, 0.5, 0.5), grid_num, n_nodes, k, reg,
                        ("scale", 1.5), iters, seed)
+
+
+@dataclasses.dataclass
+class Instance:
+    """One deformation instance of a batch: nodes, graph degree, control
+    regions and operation (the Gaussians are not needed by the solve)."""
+    node_pos: np.ndarray     # float32 [n,3]
+    k: int
+    blocks: list
+    block_type: np.ndarray
+    op: tuple
+    iters: int
+
+
+def batch_instances(count: int = 64, seed: int = 0, nodes=(300, 8000), k: int = 8, iters: int = 20):
+    """``count`` instances with node counts log-uniform in ``nodes``: random
+    unions of bars and balls under a random scale and rotation, pinned below
+    10% and active above 90% of a random axis, and an operation drawn from
+    bend (translate), twist (90 degrees about the axis) and scale x U[0.5, 2]."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(count):
+        n_nodes = int(round(math.exp(rng.uniform(math.log(nodes[0]), math.log(nodes[1])))))
+        npts = 12 * n_nodes
+        parts = []
+        for _ in range(int(rng.integers(1, 4))):
+            if rng.random() < 0.5:
+                lo = rng.uniform(0.0, 0.5, 3)
+                parts.append(_sample_bar(rng, npts, lo, lo + rng.uniform(0.15, 0.5, 3)))
+            else:
+                parts.append(_sample_ball(rng, npts, rng.uniform(0.3, 0.7, 3), rng.uniform(0.1, 0.3)))
+        pts = np.concatenate(parts)[rng.permutation(npts * len(parts))[:npts]]
+        q = _unit_quats(rng, 1)[0].astype(np.float64)
+        w, x, y, z = q
+        R = np.array([[1 - 2 * (y * y + z * z), 2 * (x * y - w * z), 2 * (x * z + w * y)],
+                      [2 * (x * y + w * z), 1 - 2 * (x * x + z * z), 2 * (y * z - w * x)],
+                      [2 * (x * z - w * y), 2 * (y * z + w * x), 1 - 2 * (x * x + y * y)]])
+        pts = (pts @ R.T) * rng.uniform(0.5, 2.0)
+        node_pos = pts[voxel_nodes(pts, n_nodes)].astype(np.float32)
+        axis = int(rng.integers(0, 3))
+        c = node_pos[:, axis]
+        lo, hi = np.quantile(c, 0.1), np.quantile(c, 0.9)
+        blocks = [np.flatnonzero(c < lo).astype(np.int32), np.flatnonzero(c > hi).astype(np.int32)]
+        kind = int(rng.integers(0, 3))
+        ext = float(np.ptp(node_pos, axis=0).max())
+        if kind == 0:
+            d = np.zeros(3)
+            d[(axis + 1) % 3] = 0.3 * ext
+            op = ("translate", tuple(float(v) for v in d))
+        elif kind == 1:
+            a = np.zeros(3)
+            a[axis] = 1.0
+            op = ("twist", tuple(float(v) for v in a), math.pi / 2)
+        else:
+            op = ("scale", float(rng.uniform(0.5, 2.0)))
+        out.append(Instance(node_pos=node_pos, k=k, blocks=blocks, block_type=np.array([0, 1], np.int32),
+                            op=op, iters=iters))
+    return out
 
 
 SCENES = {

@@ -44,6 +44,8 @@ def _args():
     ap.add_argument("--coarse-nodes", type=int, default=64)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-samples", action="store_true")
+    ap.add_argument("--batch", type=int, default=64,
+                    help="instances of the batched-solve leg (0: skip it)")
     return ap.parse_args()
 
 
@@ -169,6 +171,72 @@ def skin_bytes_per_gaussian(k, with_shs=True, with_cov=True):
     rd = 72 + 48 * k + 12 + 16 + (192 if with_shs else 0)
     wr = 72 + 12 + 16 + 12 + (192 if with_shs else 0) + (24 if with_cov else 0)
     return rd + wr
+
+
+def batch_leg(count):
+    """Batched solves: ``count`` instances (node counts log-uniform in
+    [300, 8000], random shapes and operations, 20 Gauss-Newton iterations,
+    chosen form) in one cooperative launch, against the same instances solved
+    one after another."""
+    import numpy as np
+    import torch
+    dev = importlib.import_module(PKG + ".deform")
+    synth = importlib.import_module(PKG + ".synth")
+    inst = synth.batch_instances(count)
+    solvers, pos, aims = [], [], []
+    for it in inst:
+        p = torch.as_tensor(it.node_pos).cuda()
+        nb = dev.build_graph(p, it.k)
+        aidx, aw = dev.compute_weights(p, p, it.k)
+        act = torch.as_tensor(it.blocks[1].astype(np.int32)).cuda()
+        a = p.clone()
+        if it.op[0] == "translate":
+            dev.aims_translate(a, act, it.op[1])
+        elif it.op[0] == "twist":
+            dev.aims_twist(a, p, act, it.op[1], it.op[2])
+        else:
+            dev.aims_scale(a, p, act, it.op[1])
+        solvers.append(dev.Solver(nb, aidx, aw, it.blocks, it.block_type, max_iters=it.iters, early_exit=0,
+                                  precision=1, coarse_nodes=64))
+        pos.append(p)
+        aims.append(a)
+    batch = dev.SolverBatch(solvers)
+    best = batch.autotune(pos, aims)
+    rot = [torch.empty((s.n, 9), device="cuda") for s in solvers]
+    tr = [torch.empty((s.n, 3), device="cuda") for s in solvers]
+
+    def timed(fn, reps):
+        out = []
+        for _ in range(reps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            e0.record()
+            fn()
+            e1.record()
+            torch.cuda.synchronize()
+            out.append(e0.elapsed_time(e1))
+        return float(np.median(out))
+
+    batch.solve(pos, aims, rot, tr, stats=False)
+    ms_b = timed(lambda: batch.solve(pos, aims, rot, tr, stats=False), 3)
+    _, _, st_b = batch.solve(pos, aims, rot, tr, stats=True)
+
+    def seq():
+        for s_, p_, a_, r_, t_ in zip(solvers, pos, aims, rot, tr):
+            s_.solve(p_, a_, r_, t_, stats=False)
+    seq()
+    ms_s = timed(seq, 1)
+    out = {"instances": count, "nodes_total": int(sum(s_.n for s_ in solvers)),
+           "nodes_range": [int(min(s_.n for s_ in solvers)), int(max(s_.n for s_ in solvers))],
+           "gn_iterations": inst[0].iters, "form": "chosen (mixed, coarse 64)",
+           "ms_batched": round(ms_b, 3), "ms_sequential": round(ms_s, 3),
+           "instances_per_s_batched": round(1000.0 * count / ms_b, 1),
+           "batched_speedup_over_sequential": round(ms_s / ms_b, 3),
+           "balance_exponent": best, "status": max(x["status"] for x in st_b)}
+    batch.close()
+    for s_ in solvers:
+        s_.close()
+    return out
 
 
 def run_ours(a):
@@ -315,6 +383,8 @@ def run_ours(a):
         "status": status,
         "clocks": clk.summary(),
     }
+    if rank == 0 and a.batch > 0:
+        line["batch"] = batch_leg(a.batch)
     if rank == 0 and not a.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(sc, samples=1)
     if rank == 0:

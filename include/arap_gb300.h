@@ -174,7 +174,7 @@ int arap_solver_batch_solve(arap_solver_batch* batch, const float* const* node_p
                             float* const* rot_out, float* const* trans_out, arap_solve_stats* stats_host,
                             arap_stream_t stream);
 /* Autotuner of the CTA split: times one batch solve for each balance exponent
- * in {0.5, 0.75, 1, 1.25} (after an untimed one) and keeps the fastest.
+ * in {0.75, 1, 1.25, 1.5, 2} (after an untimed one) and keeps the fastest.
  * Outputs are written by the trial solves. Synchronises. */
 int arap_solver_batch_autotune(arap_solver_batch* batch, const float* const* node_pos, const float* const* aims,
                                float* const* rot_out, float* const* trans_out, float* best_exponent,
