@@ -75,6 +75,10 @@ SIGNATURES = {
     "arap_node_table": (I, [I, P, P, P, P, P]),
     "arap_end_points": (I, [I, P, P, P, P, P, P]),
     "arap_skin_gaussians": (I, [I, I, P, P, P, P, P, P, P, P, P, P, P, I, P]),
+    "arap_skin_plan_create": (I, [P, I, I, P, P, P]),
+    "arap_skin_plan_info": (I, [P, P, P, P]),
+    "arap_skin_plan_destroy": (None, [P]),
+    "arap_skin_gaussians_planned": (I, [P, P, P, P, P, P, P, P, P, P, P, P, I, P]),
     "arap_skin_gaussians_backward": (I, [I, I, P, P, P, P, P, P, P, P, P, P]),
     "arap_node_quaternions": (I, [I, P, P, I, P]),
     "arap_skin_samples": (I, [I, I, P, P, P, P, P, P, P, P]),

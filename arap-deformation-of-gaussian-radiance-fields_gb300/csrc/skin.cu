@@ -7,6 +7,10 @@
 // [C][P] so that every warp load is one 128-byte line; per-item outputs that
 // the rasteriser consumes keep the reference's AoS records (pos float3,
 // rot float4 (w,x,y,z), scale float3, SH 48 floats [coef*3 + rgb]).
+#include <algorithm>
+#include <new>
+#include <vector>
+
 #include "arap_common.cuh"
 
 namespace arap {
@@ -108,23 +112,52 @@ __device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
 
 constexpr size_t skin_smem_bytes() { return sizeof(float) * (size_t)kSkinTile * (4 + kShStride); }
 
-template <int K, bool MIXED>
+// Skinning plan (set-up time, arap_skin_plan_create): per tile of kSkinTile
+// Gaussians the distinct nodes its endpoints blend (at most kPlanNodes), each
+// endpoint neighbour as an 8-bit index into that list, and the weights, both
+// per Gaussian endpoint-major ([6][K], contiguous).  A frame then copies the
+// tile's node records into shared memory once and gathers from there.
+constexpr int kPlanNodes = 256;
+constexpr int kPlanRec = 20;  // floats per staged node record (16 used; 80-byte stride spreads banks)
+struct SkinPlanDev {
+  const int32_t* tile_count;  // [tiles] distinct nodes of the tile (> kPlanNodes: no local list)
+  const int32_t* tile_nodes;  // [tiles][kPlanNodes]
+  const uint8_t* lidx;        // [N][6][kp] local node index, kp = K rounded up to 4
+  const float* wts;           // [N][6][K]
+  int kp;
+};
+constexpr size_t skin_plan_smem_bytes() { return skin_smem_bytes() + sizeof(float) * kPlanNodes * kPlanRec; }
+
+template <int K, bool MIXED, bool PLANNED>
 __global__ void __launch_bounds__(kSkinThreads, 4)
     skin_gaussians_kernel(int N, float* __restrict__ ends, const int32_t* __restrict__ eidx,
                           const float* __restrict__ ew, const float* __restrict__ table,
                           const float* __restrict__ scale0, const uint8_t* __restrict__ static_mask,
                           float* __restrict__ pos_out, float* __restrict__ rot_inout,
                           float* __restrict__ scale_out, float* __restrict__ shs,
-                          float* __restrict__ cov_out) {
+                          float* __restrict__ cov_out, SkinPlanDev plan) {
   extern __shared__ float4 s_raw4[];
   float* s_raw = reinterpret_cast<float*>(s_raw4);
   float* s_sh = s_raw;                                        // [T][52]
   float4* s_q = reinterpret_cast<float4*>(s_sh + kSkinTile * kShStride);  // [T]
+  float* s_nodes = reinterpret_cast<float*>(s_q + kSkinTile);  // PLANNED: [kPlanNodes][kPlanRec]
   const int t = threadIdx.x;
   const int tile0 = blockIdx.x * kSkinTile;
   const int cnt = min(kSkinTile, N - tile0);
   const int i = tile0 + t;
   const bool active = t < cnt;
+  // ---- planned: the tile's node records into shared memory (first copy group)
+  int n_local = kPlanNodes + 1;
+  if (PLANNED) {
+    n_local = __ldg(plan.tile_count + blockIdx.x);
+    if (n_local <= kPlanNodes) {
+      const int32_t* list = plan.tile_nodes + (size_t)blockIdx.x * kPlanNodes;
+      for (int e = t; e < 4 * n_local; e += kSkinThreads)
+        cp_async16(s_nodes + (e >> 2) * kPlanRec + (e & 3) * 4, table + 16 * (size_t)__ldg(list + (e >> 2)) + (e & 3) * 4);
+    }
+    asm volatile("cp.async.commit_group;" ::: "memory");
+  }
+  const bool local = PLANNED && n_local <= kPlanNodes;
   // ---- stage the SH records and previous quaternions of the tile
   if (active) cp_async16(s_q + t, reinterpret_cast<const float4*>(rot_inout) + i);
   if (shs) {
@@ -133,6 +166,11 @@ __global__ void __launch_bounds__(kSkinThreads, 4)
       cp_async16(s_sh + (q / 12) * kShStride + (q % 12) * 4, src + 4 * (size_t)q);
   }
   asm volatile("cp.async.commit_group;" ::: "memory");
+  if (PLANNED) {
+    // the node records (first group) are needed now, the SH records later
+    asm volatile("cp.async.wait_group 1;" ::: "memory");
+    __syncthreads();
+  }
 
   float e[18];
   if (active) {
@@ -143,14 +181,48 @@ __global__ void __launch_bounds__(kSkinThreads, 4)
       float ox = 0.f, oy = 0.f, oz = 0.f, ws = 0.f;
       int id[K];
       float wv[K];
+      if (local) {
+        const uint32_t* lw = reinterpret_cast<const uint32_t*>(plan.lidx + ((size_t)i * 6 + ep) * plan.kp);
+        const float* wp = plan.wts + ((size_t)i * 6 + ep) * K;
 #pragma unroll
-      for (int j = 0; j < K; ++j) {
-        id[j] = __ldcs(eidx + (size_t)(j * 6 + ep) * N + i);
-        wv[j] = __ldcs(ew + (size_t)(j * 6 + ep) * N + i);
+        for (int q = 0; q < (K + 3) / 4; ++q) {
+          const uint32_t b4 = __ldcs(lw + q);
+#pragma unroll
+          for (int r = 0; r < 4; ++r)
+            if (4 * q + r < K) id[4 * q + r] = (b4 >> (8 * r)) & 0xffu;
+        }
+        if (K % 4 == 0) {
+#pragma unroll
+          for (int q = 0; q < K / 4; ++q) {
+            const float4 w4 = __ldcs(reinterpret_cast<const float4*>(wp) + q);
+            wv[4 * q] = w4.x;
+            wv[4 * q + 1] = w4.y;
+            wv[4 * q + 2] = w4.z;
+            wv[4 * q + 3] = w4.w;
+          }
+        } else {
+#pragma unroll
+          for (int j = 0; j < K; ++j) wv[j] = __ldcs(wp + j);
+        }
+      } else {
+#pragma unroll
+        for (int j = 0; j < K; ++j) {
+          id[j] = __ldcs(eidx + (size_t)(j * 6 + ep) * N + i);
+          wv[j] = __ldcs(ew + (size_t)(j * 6 + ep) * N + i);
+        }
       }
 #pragma unroll
       for (int j = 0; j < K; ++j) {
-        const NodeXf x = load_node(table, id[j]);
+        NodeXf x;
+        if (local) {
+          const float4* r4 = reinterpret_cast<const float4*>(s_nodes + id[j] * kPlanRec);
+          x.a = r4[0];
+          x.b = r4[1];
+          x.c = r4[2];
+          x.d = r4[3];
+        } else {
+          x = load_node(table, id[j]);
+        }
         const float w = wv[j];
         ws += w;
         ed_term(x, w, e[3 * ep], e[3 * ep + 1], e[3 * ep + 2], ox, oy, oz);
@@ -670,19 +742,95 @@ __global__ void aims_kernel(int op, float* __restrict__ aims, const float* __res
   }
 }
 
-template <int K>
-static void launch_skin_g(bool mixed, int N, float* ends, const int32_t* eidx, const float* ew,
-                          const float* table, const float* scale0, const uint8_t* st, float* pos,
-                          float* rot, float* scale, float* shs, float* cov, cudaStream_t s) {
+template <int K, bool PLANNED>
+static int launch_skin_g(bool mixed, int N, float* ends, const int32_t* eidx, const float* ew,
+                         const float* table, const float* scale0, const uint8_t* st, float* pos,
+                         float* rot, float* scale, float* shs, float* cov, const SkinPlanDev& plan, cudaStream_t s) {
   const int grid = grid_for(N, kSkinTile);
-  constexpr size_t smem = skin_smem_bytes();
-  if (mixed)
-    skin_gaussians_kernel<K, true><<<grid, kSkinThreads, smem, s>>>(N, ends, eidx, ew, table, scale0, st, pos, rot,
-                                                                     scale, shs, cov);
-  else
-    skin_gaussians_kernel<K, false><<<grid, kSkinThreads, smem, s>>>(N, ends, eidx, ew, table, scale0, st, pos, rot,
-                                                                      scale, shs, cov);
+  constexpr size_t smem = PLANNED ? skin_plan_smem_bytes() : skin_smem_bytes();
+  if (mixed) {
+    if (PLANNED && cudaFuncSetAttribute(skin_gaussians_kernel<K, true, PLANNED>,
+                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+      return ARAP_ECUDA;
+    skin_gaussians_kernel<K, true, PLANNED><<<grid, kSkinThreads, smem, s>>>(N, ends, eidx, ew, table, scale0, st,
+                                                                              pos, rot, scale, shs, cov, plan);
+  } else {
+    if (PLANNED && cudaFuncSetAttribute(skin_gaussians_kernel<K, false, PLANNED>,
+                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+      return ARAP_ECUDA;
+    skin_gaussians_kernel<K, false, PLANNED><<<grid, kSkinThreads, smem, s>>>(N, ends, eidx, ew, table, scale0, st,
+                                                                               pos, rot, scale, shs, cov, plan);
+  }
+  return ARAP_OK;
 }
+
+// ---- skinning plan (set-up time)
+// One CTA per tile: the distinct node ids of the tile's endpoint neighbours
+// (shared-memory hash, then ascending order), their count, and each
+// neighbour's 8-bit index into the list, written endpoint-major per Gaussian
+// with the weights.  A tile with more than kPlanNodes distinct nodes keeps
+// only its count; frames then gather its nodes from the global table.
+constexpr int kPlanHash = 2048;
+constexpr int kPlanThreads = 256;
+__global__ void __launch_bounds__(kPlanThreads)
+    skin_plan_kernel(int N, int K, const int32_t* __restrict__ eidx, const float* __restrict__ ew, int kp,
+                     int32_t* __restrict__ tile_count, int32_t* __restrict__ tile_nodes, uint8_t* __restrict__ lidx,
+                     float* __restrict__ wts) {
+  __shared__ int s_key[kPlanHash];
+  __shared__ int s_list[kPlanNodes];
+  __shared__ int s_n, s_over;
+  const int t = threadIdx.x;
+  const int tile0 = blockIdx.x * kSkinTile;
+  const int cnt = min(kSkinTile, N - tile0);
+  for (int q = t; q < kPlanHash; q += kPlanThreads) s_key[q] = -1;
+  if (t == 0) {
+    s_n = 0;
+    s_over = 0;
+  }
+  __syncthreads();
+  const int total = cnt * 6 * K;
+  for (int e = t; e < total; e += kPlanThreads) {
+    const int g = e / (6 * K), c = e % (6 * K);  // plane c = j * 6 + ep
+    const int id = eidx[(size_t)c * N + tile0 + g];
+    unsigned h = ((unsigned)id * 2654435761u) & (kPlanHash - 1);
+    for (int probe = 0; probe < kPlanHash; ++probe) {
+      const int prev = atomicCAS(&s_key[h], -1, id);
+      if (prev == -1) {
+        const int slot = atomicAdd(&s_n, 1);
+        if (slot < kPlanNodes)
+          s_list[slot] = id;
+        else
+          s_over = 1;
+        break;
+      }
+      if (prev == id) break;
+      h = (h + 1) & (kPlanHash - 1);
+    }
+  }
+  __syncthreads();
+  const int n = s_n;
+  if (t == 0) tile_count[blockIdx.x] = (n > kPlanNodes || s_over) ? kPlanNodes + 1 : n;
+  if (n > kPlanNodes || s_over) return;
+  // ascending order of the list (rank by counting), written to the plan
+  for (int a = t; a < n; a += kPlanThreads) {
+    const int v = s_list[a];
+    int rank = 0;
+    for (int b = 0; b < n; ++b) rank += s_list[b] < v;
+    tile_nodes[(size_t)blockIdx.x * kPlanNodes + rank] = v;
+  }
+  __syncthreads();
+  for (int e = t; e < total; e += kPlanThreads) {
+    const int g = e / (6 * K), c = e % (6 * K);
+    const int j = c / 6, ep = c % 6;
+    const int id = eidx[(size_t)c * N + tile0 + g];
+    int rank = 0;
+    for (int b = 0; b < n; ++b) rank += s_list[b] < id;
+    const size_t o = ((size_t)(tile0 + g) * 6 + ep);
+    lidx[o * kp + j] = (uint8_t)rank;
+    wts[o * K + j] = ew[(size_t)c * N + tile0 + g];
+  }
+}
+
 
 template <int K>
 static void launch_skin_s(int S, float* spos, const int32_t* idx, const float* w, const float* table,
@@ -729,11 +877,12 @@ extern "C" int arap_skin_gaussians(int N, int k, float* ends, const int32_t* end
     return ARAP_EBADINPUT;
   const bool mixed = precision == ARAP_PRECISION_MIXED;
   cudaStream_t s = (cudaStream_t)stream;
+  int rc = ARAP_OK;
   switch (k) {
 #define ARAP_SKG(K)                                                                                   \
   case K:                                                                                             \
-    launch_skin_g<K>(mixed, N, ends, ends_idx, ends_w, node_table, scale0, static_mask, pos_out,      \
-                     rot_inout, scale_out, shs_inout, cov_out, s);                                    \
+    rc = launch_skin_g<K, false>(mixed, N, ends, ends_idx, ends_w, node_table, scale0, static_mask, pos_out, \
+                                 rot_inout, scale_out, shs_inout, cov_out, SkinPlanDev{}, s);            \
     break;
     ARAP_SKG(1) ARAP_SKG(2) ARAP_SKG(3) ARAP_SKG(4) ARAP_SKG(5) ARAP_SKG(6)
     ARAP_SKG(7) ARAP_SKG(8) ARAP_SKG(9) ARAP_SKG(10) ARAP_SKG(11) ARAP_SKG(12)
@@ -741,6 +890,106 @@ extern "C" int arap_skin_gaussians(int N, int k, float* ends, const int32_t* end
     default:
       return ARAP_EUNSUPPORTED;
   }
+  if (rc != ARAP_OK) return rc;
+  ARAP_LAUNCH_CHECK();
+  return ARAP_OK;
+}
+
+struct arap_skin_plan {
+  int N = 0, k = 0, tiles = 0, kp = 0, overflow = 0, max_nodes = 0;
+  void* block = nullptr;
+  SkinPlanDev dev{};
+};
+
+extern "C" int arap_skin_plan_create(arap_skin_plan** out, int N, int k, const int32_t* ends_idx,
+                                     const float* ends_w, arap_stream_t stream) {
+  if (!out) return ARAP_EBADINPUT;
+  *out = nullptr;
+  if (N < 1 || k < 1 || k > ARAP_KNN_MAX || !ends_idx || !ends_w) return ARAP_EBADINPUT;
+  cudaStream_t st = (cudaStream_t)stream;
+  auto* p = new (std::nothrow) arap_skin_plan();
+  if (!p) return ARAP_ENOMEM;
+  p->N = N;
+  p->k = k;
+  p->tiles = (N + kSkinTile - 1) / kSkinTile;
+  p->kp = (k + 3) & ~3;
+  const size_t b_count = ((sizeof(int32_t) * p->tiles) + 255) & ~size_t(255);
+  const size_t b_nodes = ((sizeof(int32_t) * (size_t)p->tiles * kPlanNodes) + 255) & ~size_t(255);
+  const size_t b_lidx = (((size_t)N * 6 * p->kp) + 255) & ~size_t(255);
+  const size_t b_wts = sizeof(float) * (size_t)N * 6 * k;
+  if (cudaMalloc(&p->block, b_count + b_nodes + b_lidx + b_wts) != cudaSuccess) {
+    (void)cudaGetLastError();
+    delete p;
+    return ARAP_ENOMEM;
+  }
+  char* base = static_cast<char*>(p->block);
+  int32_t* count = reinterpret_cast<int32_t*>(base);
+  int32_t* nodes = reinterpret_cast<int32_t*>(base + b_count);
+  uint8_t* lidx = reinterpret_cast<uint8_t*>(base + b_count + b_nodes);
+  float* wts = reinterpret_cast<float*>(base + b_count + b_nodes + b_lidx);
+  p->dev = SkinPlanDev{count, nodes, lidx, wts, p->kp};
+  if (cudaMemsetAsync(lidx, 0, b_lidx, st) != cudaSuccess) {
+    arap_skin_plan_destroy(p);
+    return ARAP_ECUDA;
+  }
+  skin_plan_kernel<<<p->tiles, kPlanThreads, 0, st>>>(N, k, ends_idx, ends_w, p->kp, count, nodes, lidx, wts);
+  std::vector<int32_t> h(p->tiles);
+  if (cudaPeekAtLastError() != cudaSuccess ||
+      cudaMemcpyAsync(h.data(), count, sizeof(int32_t) * p->tiles, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+      cudaStreamSynchronize(st) != cudaSuccess) {
+    (void)cudaGetLastError();
+    arap_skin_plan_destroy(p);
+    return ARAP_ECUDA;
+  }
+  for (int v : h) {
+    if (v > kPlanNodes) ++p->overflow;
+    else p->max_nodes = std::max(p->max_nodes, v);
+  }
+  *out = p;
+  return ARAP_OK;
+}
+
+extern "C" int arap_skin_plan_info(const arap_skin_plan* p, int* tiles, int* overflow_tiles, int* max_nodes) {
+  if (!p) return ARAP_EBADINPUT;
+  if (tiles) *tiles = p->tiles;
+  if (overflow_tiles) *overflow_tiles = p->overflow;
+  if (max_nodes) *max_nodes = p->max_nodes;
+  return ARAP_OK;
+}
+
+extern "C" void arap_skin_plan_destroy(arap_skin_plan* p) {
+  if (!p) return;
+  if (p->block) cudaFree(p->block);
+  delete p;
+}
+
+extern "C" int arap_skin_gaussians_planned(const arap_skin_plan* plan, float* ends, const int32_t* ends_idx,
+                                           const float* ends_w, const float* node_table, const float* scale0,
+                                           const uint8_t* static_mask, float* pos_out, float* rot_inout,
+                                           float* scale_out, float* shs_inout, float* cov_out, int precision,
+                                           arap_stream_t stream) {
+  if (!plan || !ends || !ends_idx || !ends_w || !node_table || !scale0 || !pos_out || !rot_inout || !scale_out)
+    return ARAP_EBADINPUT;
+  if ((reinterpret_cast<uintptr_t>(node_table) | reinterpret_cast<uintptr_t>(rot_inout) |
+       reinterpret_cast<uintptr_t>(shs_inout)) & 15)
+    return ARAP_EBADINPUT;
+  const int N = plan->N;
+  const bool mixed = precision == ARAP_PRECISION_MIXED;
+  cudaStream_t s = (cudaStream_t)stream;
+  int rc = ARAP_OK;
+  switch (plan->k) {
+#define ARAP_SKP(K)                                                                                       \
+  case K:                                                                                                 \
+    rc = launch_skin_g<K, true>(mixed, N, ends, ends_idx, ends_w, node_table, scale0, static_mask, pos_out, \
+                                rot_inout, scale_out, shs_inout, cov_out, plan->dev, s);                  \
+    break;
+    ARAP_SKP(1) ARAP_SKP(2) ARAP_SKP(3) ARAP_SKP(4) ARAP_SKP(5) ARAP_SKP(6)
+    ARAP_SKP(7) ARAP_SKP(8) ARAP_SKP(9) ARAP_SKP(10) ARAP_SKP(11) ARAP_SKP(12)
+#undef ARAP_SKP
+    default:
+      return ARAP_EUNSUPPORTED;
+  }
+  if (rc != ARAP_OK) return rc;
   ARAP_LAUNCH_CHECK();
   return ARAP_OK;
 }

@@ -272,6 +272,43 @@ def skin_gaussians(ends, ends_idx, ends_w, table, scale0, pos_out, rot_inout, sc
         _p(rot_inout), _p(scale_out), _p(shs), _p(cov_out), int(precision), _s()))
 
 
+class SkinPlan:
+    """Set-up-time layout of the endpoint kNN for skin_gaussians_planned
+    (arap_skin_plan_*): per tile of 128 Gaussians its distinct nodes and
+    8-bit local indices, weights contiguous per Gaussian."""
+
+    def __init__(self, ends_idx, ends_w):
+        self.k, self.N = int(ends_idx.shape[0]), int(ends_idx.shape[1]) // 6
+        self.ends_idx, self.ends_w = ends_idx, ends_w
+        h = C.c_void_p()
+        check("arap_skin_plan_create", _lib_().arap_skin_plan_create(
+            C.byref(h), self.N, self.k, _p(ends_idx), _p(ends_w), _s()))
+        self._h = h
+
+    def info(self):
+        t, o, m = C.c_int(), C.c_int(), C.c_int()
+        check("arap_skin_plan_info", _lib_().arap_skin_plan_info(self._h, C.byref(t), C.byref(o), C.byref(m)))
+        return {"tiles": t.value, "overflow_tiles": o.value, "max_nodes": m.value}
+
+    def close(self):
+        if getattr(self, "_h", None) is not None and self._h.value:
+            _lib_().arap_skin_plan_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def skin_gaussians_planned(plan, ends, table, scale0, pos_out, rot_inout, scale_out, shs=None, cov_out=None,
+                           static=None, precision=_lib.PRECISION_PLAIN):
+    check("arap_skin_gaussians_planned", _lib_().arap_skin_gaussians_planned(
+        plan._h, _p(ends), _p(plan.ends_idx), _p(plan.ends_w), _p(table), _p(scale0), _p(static), _p(pos_out),
+        _p(rot_inout), _p(scale_out), _p(shs), _p(cov_out), int(precision), _s()))
+
+
 def skin_gaussians_backward(ends_in, ends_idx, ends_w, table, scale0, grad_pos, grad_cov, n, static=None,
                             grad_node=None):
     """Adjoint of skin_gaussians' (mu, Sigma) w.r.t. the node transforms:
@@ -346,7 +383,7 @@ class GaussianDeformer:
     re-anchored to the nodes."""
 
     def __init__(self, pos, rot, scale, shs, node_vertex, k, blocks, block_type,
-                 sample_pos=None, feature=None, config=None, **cfg_kw):
+                 sample_pos=None, feature=None, config=None, use_plan=True, **cfg_kw):
         dev = "cuda"
         self.k = int(k)
         self.pos = _f32(pos)
@@ -366,6 +403,7 @@ class GaussianDeformer:
         self.ends, ends_xyz = end_points(self.pos, self.rot, self.scale)
         self.ends_idx, self.ends_w = compute_weights(ends_xyz, self.node_pos, self.k)
         del ends_xyz
+        self.skin_plan = SkinPlan(self.ends_idx, self.ends_w) if use_plan else None
         self.sample_pos = _f32(sample_pos) if sample_pos is not None else None
         self.feature = _f32(feature) if feature is not None else None
         if self.sample_pos is not None:
@@ -413,8 +451,12 @@ class GaussianDeformer:
             skin_samples(self.sample_pos, self.sample_idx, self.sample_w, table, quat, self.feature, self.s_static)
         if skin_events is not None:
             skin_events[0].record()
-        skin_gaussians(self.ends, self.ends_idx, self.ends_w, table, self.scale0, self.pos, self.rot,
-                       self.scale, self.shs, self.cov if with_cov else None, self.g_static, self.precision)
+        if self.skin_plan is not None:
+            skin_gaussians_planned(self.skin_plan, self.ends, table, self.scale0, self.pos, self.rot, self.scale,
+                                   self.shs, self.cov if with_cov else None, self.g_static, self.precision)
+        else:
+            skin_gaussians(self.ends, self.ends_idx, self.ends_w, table, self.scale0, self.pos, self.rot,
+                           self.scale, self.shs, self.cov if with_cov else None, self.g_static, self.precision)
         if skin_events is not None:
             skin_events[1].record()
         update_nodes(self.node_pos, self.anchor_idx, self.anchor_w, table, self.node_pos_next)

@@ -160,15 +160,18 @@ def restore(st, snap):
 
 
 # DRAM bytes per launch of skin_gaussians_kernel measured by ncu on the named
-# workload (dram__bytes_read.sum + dram__bytes_write.sum of one launch).
-SKIN_DRAM_BYTES = {("twist300k", 8): 252_920_320}
+# workload (dram__bytes_read.sum + dram__bytes_write.sum of one launch), keyed
+# by (scene, k, planned).
+SKIN_DRAM_BYTES = {}
 
 
-def skin_bytes_per_gaussian(k, with_shs=True, with_cov=True):
-    """Algorithmic bytes of arap_skin_gaussians per Gaussian: read 6 endpoints
-    (72), 6k indices + 6k weights (48k), scale0 (12), previous q (16), SH (192);
-    write endpoints (72), mu (12), q (16), scale (12), SH (192), Sigma (24)."""
-    rd = 72 + 48 * k + 12 + 16 + (192 if with_shs else 0)
+def skin_bytes_per_gaussian(k, with_shs=True, with_cov=True, planned=True):
+    """Algorithmic bytes of Gaussian skinning per Gaussian: read 6 endpoints
+    (72), 6k neighbour indices (1 byte each with the skinning plan, else 4) and
+    6k weights (24k), scale0 (12), previous q (16), SH (192); write endpoints
+    (72), mu (12), q (16), scale (12), SH (192), Sigma (24).  The plan's node
+    lists (a few hundred bytes per 128-Gaussian tile) are not counted."""
+    rd = 72 + 6 * k * (1 if planned else 4) + 24 * k + 12 + 16 + (192 if with_shs else 0)
     wr = 72 + 12 + 16 + 12 + (192 if with_shs else 0) + (24 if with_cov else 0)
     return rd + wr
 
@@ -339,7 +342,7 @@ def run_ours(a):
 
     peak, peak_kind = _peaks()
     k = sc.k
-    bytes_launch = skin_bytes_per_gaussian(k) * sc.n_gauss
+    bytes_launch = skin_bytes_per_gaussian(k, planned=st.skin_plan is not None) * sc.n_gauss
     achieved = bytes_launch / (skin_ms * 1e-3) / 1e9
     launches_per_step = 5 + (1 if st.sample_pos is not None else 0) + (1 if st.feature is not None else 0)
     line = {
@@ -364,9 +367,11 @@ def run_ours(a):
                    "wall_s_timed_region": round(wall, 3)},
         "e2e": {"value": round(float(np.mean(e2e_ms)), 4), "unit": "ms/frame",
                 "h2d_bytes_per_step": int(st.n * 12), "d2h_bytes_per_step": int(st.n * 48)},
-        "roofline": {"kernel": "arap_skin_gaussians", "bound": "hbm", "achieved": round(achieved, 1),
+        "roofline": {"kernel": "arap_skin_gaussians_planned" if st.skin_plan is not None else "arap_skin_gaussians",
+                     "bound": "hbm", "achieved": round(achieved, 1),
                      "peak": peak, "peak_kind": peak_kind, "unit": "GB/s", "frac": round(achieved / peak, 4),
-                     "traffic": SKIN_DRAM_BYTES.get((sc.name, k)), "traffic_source": "ncu dram__bytes_read.sum + "
+                     "traffic": SKIN_DRAM_BYTES.get((sc.name, k, st.skin_plan is not None)),
+                     "traffic_source": "ncu dram__bytes_read.sum + "
                      "dram__bytes_write.sum, one launch (profiles/skin_gaussians_twist300k.md)",
                      "bytes_per_launch": bytes_launch, "ms_per_launch": round(skin_ms, 5)},
         "gpu_launches": launches_per_step * a.steps,

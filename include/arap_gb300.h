@@ -224,6 +224,33 @@ int arap_skin_gaussians(int N, int k, float* ends, const int32_t* ends_idx,
                         float* scale_out, float* shs_inout, float* cov_out, int precision,
                         arap_stream_t stream);
 
+/* Skinning plan: no counterpart in the reference; a set-up-time layout of
+ * the endpoint kNN for arap_skin_gaussians_planned.
+ * - Per tile of 128 Gaussians it keeps the distinct nodes the tile's endpoints
+ *   blend (at most 256) and each neighbour as an 8-bit index into that list.
+ * - The weights are copied per Gaussian, endpoint-major.
+ * Build it once after arap_compute_weights of the endpoints, and again
+ * whenever ends_idx/ends_w or the Gaussian order change. Synchronises. */
+typedef struct arap_skin_plan arap_skin_plan;
+int arap_skin_plan_create(arap_skin_plan** out, int N, int k, const int32_t* ends_idx,
+                          const float* ends_w, arap_stream_t stream);
+/* tiles; tiles with more than 256 distinct nodes (skinned from the global table);
+ * the largest distinct-node count of the other tiles. */
+int arap_skin_plan_info(const arap_skin_plan* plan, int* tiles, int* overflow_tiles, int* max_nodes);
+void arap_skin_plan_destroy(arap_skin_plan* plan);
+/* arap_skin_gaussians with the plan's layout and the same results (the same
+ * arithmetic in the same order).
+ * - A CTA copies its tile's node records into shared memory once.
+ * - Each Gaussian reads 8-bit node indices and contiguous weights, not the
+ *   int32 and float planes.
+ * - ends_idx/ends_w are read only for tiles over 256 nodes. N and k are the
+ *   plan's. */
+int arap_skin_gaussians_planned(const arap_skin_plan* plan, float* ends, const int32_t* ends_idx,
+                                const float* ends_w, const float* node_table, const float* scale0,
+                                const uint8_t* static_mask, float* pos_out, float* rot_inout,
+                                float* scale_out, float* shs_inout, float* cov_out, int precision,
+                                arap_stream_t stream);
+
 /* Adjoint of arap_skin_gaussians' mu and Sigma with respect to the node
  * transforms: given the upstream gradients grad_pos [N*3] and grad_cov [N*6]
  * (packed xx,xy,xz,yy,yz,zz, dL = sum_p grad_cov_p dSigma_p), ADDS dL/dR_j and
