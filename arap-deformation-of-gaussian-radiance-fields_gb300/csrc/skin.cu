@@ -173,37 +173,58 @@ __global__ void __launch_bounds__(kSkinThreads, 4)
   }
 
   float e[18];
+  // loads the refit needs later, issued now so that they overlap the blend
+  const bool is_static = active && static_mask && __ldg(static_mask + i);
+  float s0v[3] = {0.f, 0.f, 0.f};
+  if (active) {
+#pragma unroll
+    for (int a = 0; a < 3; ++a) s0v[a] = __ldg(scale0 + 3 * (size_t)i + a);
+  }
   if (active) {
 #pragma unroll
     for (int c = 0; c < 18; ++c) e[c] = __ldcs(ends + (size_t)c * N + i);
+    // planned: endpoint ep+1's indices and weights are requested before
+    // endpoint ep is blended
+    constexpr int KW = (K + 3) / 4;
+    uint32_t lw_next[KW];
+    float w_next[K];
+    auto fetch_plan = [&](int ep, uint32_t(&lw)[KW], float(&wv)[K]) {
+      const uint32_t* lp = reinterpret_cast<const uint32_t*>(plan.lidx + ((size_t)i * 6 + ep) * plan.kp);
+      const float* wp = plan.wts + ((size_t)i * 6 + ep) * K;
+#pragma unroll
+      for (int q = 0; q < KW; ++q) lw[q] = __ldcs(lp + q);
+      if (K % 4 == 0) {
+#pragma unroll
+        for (int q = 0; q < K / 4; ++q) {
+          const float4 w4 = __ldcs(reinterpret_cast<const float4*>(wp) + q);
+          wv[4 * q] = w4.x;
+          wv[4 * q + 1] = w4.y;
+          wv[4 * q + 2] = w4.z;
+          wv[4 * q + 3] = w4.w;
+        }
+      } else {
+#pragma unroll
+        for (int j = 0; j < K; ++j) wv[j] = __ldcs(wp + j);
+      }
+    };
+    if (local) fetch_plan(0, lw_next, w_next);
 #pragma unroll
     for (int ep = 0; ep < 6; ++ep) {
       float ox = 0.f, oy = 0.f, oz = 0.f, ws = 0.f;
       int id[K];
       float wv[K];
       if (local) {
-        const uint32_t* lw = reinterpret_cast<const uint32_t*>(plan.lidx + ((size_t)i * 6 + ep) * plan.kp);
-        const float* wp = plan.wts + ((size_t)i * 6 + ep) * K;
+        uint32_t lw[KW];
 #pragma unroll
-        for (int q = 0; q < (K + 3) / 4; ++q) {
-          const uint32_t b4 = __ldcs(lw + q);
+        for (int q = 0; q < KW; ++q) lw[q] = lw_next[q];
+#pragma unroll
+        for (int j = 0; j < K; ++j) wv[j] = w_next[j];
+        if (ep + 1 < 6) fetch_plan(ep + 1, lw_next, w_next);
+#pragma unroll
+        for (int q = 0; q < KW; ++q)
 #pragma unroll
           for (int r = 0; r < 4; ++r)
-            if (4 * q + r < K) id[4 * q + r] = (b4 >> (8 * r)) & 0xffu;
-        }
-        if (K % 4 == 0) {
-#pragma unroll
-          for (int q = 0; q < K / 4; ++q) {
-            const float4 w4 = __ldcs(reinterpret_cast<const float4*>(wp) + q);
-            wv[4 * q] = w4.x;
-            wv[4 * q + 1] = w4.y;
-            wv[4 * q + 2] = w4.z;
-            wv[4 * q + 3] = w4.w;
-          }
-        } else {
-#pragma unroll
-          for (int j = 0; j < K; ++j) wv[j] = __ldcs(wp + j);
-        }
+            if (4 * q + r < K) id[4 * q + r] = (lw[q] >> (8 * r)) & 0xffu;
       } else {
 #pragma unroll
         for (int j = 0; j < K; ++j) {
@@ -237,7 +258,6 @@ __global__ void __launch_bounds__(kSkinThreads, 4)
   asm volatile("cp.async.wait_group 0;" ::: "memory");
   __syncthreads();
   if (active) {
-    const bool is_static = static_mask && static_mask[i];
     if (!is_static) {
       float cx = 0.f, cy = 0.f, cz = 0.f;
 #pragma unroll
@@ -289,7 +309,7 @@ __global__ void __launch_bounds__(kSkinThreads, 4)
       float sc[3];
 #pragma unroll
       for (int a = 0; a < 3; ++a) {
-        const float s0 = __ldg(scale0 + 3 * (size_t)i + a);
+        const float s0 = s0v[a];
         sc[a] = Kd[a] / ((s0 + 1e-3f) * 2.0f) * s0;
       }
       pos_out[3 * (size_t)i] = cx;
