@@ -27,13 +27,19 @@ __device__ __forceinline__ void ld3t_cg(const float* base, int r, float (&v)[3])
   v[0] = c.y; v[1] = c.z; v[2] = c.w;
 }
 
+// The CTA's shared-memory copy of the coarse correction zc, staged at the
+// start of the products phase (12 floats per aggregate, read by its ~64
+// nodes and by the constraint items touching it).
+__shared__ __align__(16) float s_zc[kMaxCoarse];
+
 // Coarse correction of free node rr in aggregate a: z += P_j zc[a] with
-// dR_j = dR_a, dt_j = dR_a (g_j - g_pivot(a)) + dT_a.
+// dR_j = dR_a, dt_j = dR_a (g_j - g_pivot(a)) + dT_a, zc from s_zc.
 __device__ __forceinline__ void coarse_prolong(const SolveParams& P, int rr, int a, float (&v)[12]) {
   const float4 dp = __ldcg(P.dpiv + rr);
   const float d0 = dp.x, d1 = dp.y, d2 = dp.z;
-  float c[12];
-  ld12cg(P.zc, a, c);
+  const float4* c4 = reinterpret_cast<const float4*>(s_zc + 12 * a);
+  const float4 ca = c4[0], cb = c4[1], cc = c4[2];
+  const float c[12] = {ca.x, ca.y, ca.z, ca.w, cb.x, cb.y, cb.z, cb.w, cc.x, cc.y, cc.z, cc.w};
 #pragma unroll
   for (int i = 0; i < 9; ++i) v[i] += c[i];
 #pragma unroll
@@ -41,8 +47,8 @@ __device__ __forceinline__ void coarse_prolong(const SolveParams& P, int rr, int
 }
 
 // Preconditioned residual u = u_f + P zc of free node rr in aggregate agg,
-// formed on the fly (u_f = Dinv r in P.z; the coarse correction when the
-// two-level preconditioner is on).
+// formed on the fly (u_f = Dinv r in P.z; the coarse correction, from s_zc,
+// when the two-level preconditioner is on).
 __device__ __forceinline__ void load_u(const SolveParams& P, int rr, int agg, float (&v)[12]) {
   ld12cg(P.z, rr, v);
   if (P.NA) coarse_prolong(P, rr, agg, v);
@@ -182,8 +188,9 @@ __device__ void con_ju_coarse(const SolveParams& P, int g, float (&u)[3]) {
   const int f0 = __ldg(P.gca_off + g), f1 = __ldg(P.gca_off + g + 1);
   for (int f = f0; f < f1; ++f) {
     const float4 V = __ldcg(P.gcv + f);
-    float C[12];
-    ld12cg(P.zc, __ldg(P.gca + f), C);
+    const float4* c4 = reinterpret_cast<const float4*>(s_zc + 12 * __ldg(P.gca + f));
+    const float4 ca = c4[0], cb = c4[1], cc = c4[2];
+    const float C[12] = {ca.x, ca.y, ca.z, ca.w, cb.x, cb.y, cb.z, cb.w, cc.x, cc.y, cc.z, cc.w};
 #pragma unroll
     for (int c = 0; c < 3; ++c)
       u[c] = fmaf(wcf, fmaf(V.x, C[c], fmaf(V.y, C[3 + c], fmaf(V.z, C[6 + c], V.w * C[9 + c]))), u[c]);

@@ -450,6 +450,12 @@ __device__ __forceinline__ void solve_body(const SolveParams& P, int bid, int nb
     auto products = [&](double (&s3)[3]) -> bool {
       float f3[3] = {0.f, 0.f, 0.f};
       work_begin();
+      // the coarse correction zc (12 floats per aggregate, shared by its
+      // ~64 nodes) is read from a shared-memory copy
+      if (coarse) {
+        for (int e = threadIdx.x; e < P.NC; e += blockDim.x) s_zc[e] = __ldcg(P.zc + e);
+        __syncthreads();
+      }
       for (int hs0 = 2 * wib; hs0 * nbk + bid < F; hs0 += 2 * kSolveWarps) {
         const int oi = (hs0 + half) * nbk + bid;
         const bool valid = oi < F;
