@@ -19,6 +19,9 @@ struct arap_solver {
   void* block = nullptr;  // one device allocation holding everything below
   SolveParams P{};
   std::vector<int32_t> free_host;
+  std::vector<int32_t> order_host;  // processing order (free ranks)
+  std::vector<int32_t> stage_cost;  // shared-memory bytes of each free node's tables
+  std::vector<int32_t> res_cost;    // the same in resident mode (two-level PCG only; empty otherwise)
 };
 
 namespace {
@@ -52,6 +55,61 @@ int occupancy_grid(int per_sm_cap) {
     return -1;
   if (per_sm < 1) return -1;
   return sms * std::min(per_sm, per_sm_cap);
+}
+
+// Largest dynamic shared memory a CTA of kernel fn may take for its resident
+// node tables: the device's per-block opt-in limit less the kernel's static
+// shared memory and a reserve, and at most kStageMaxBytes so that L1 keeps
+// room for the kernel's local memory.  The kernel's attribute is raised to it.
+constexpr int kStageMaxBytes = 160 * 1024;
+int stage_limit(const void* fn) {
+  int dev = 0, optin = 0;
+  cudaFuncAttributes fa{};
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess ||
+      cudaFuncGetAttributes(&fa, fn) != cudaSuccess) {
+    (void)cudaGetLastError();
+    return 0;
+  }
+  const int lim = std::min(optin - (int)fa.sharedSizeBytes - 1024, kStageMaxBytes) & ~15;
+  if (lim <= 0) return 0;
+  if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, lim) != cudaSuccess) {
+    (void)cudaGetLastError();
+    return 0;
+  }
+  return lim;
+}
+
+// Shared memory the tables of a solve need when its free nodes are dealt
+// round-robin over nbk CTAs (the largest CTA share), uncapped.
+long long stage_need(const std::vector<int32_t>& order, const std::vector<int32_t>& cost, int nbk) {
+  if (nbk <= 0) return 0;
+  std::vector<long long> per(nbk, 0);
+  for (size_t p = 0; p < order.size(); ++p) per[p % nbk] += cost[order[p]];
+  long long need = 0;
+  for (long long v : per) need = std::max(need, v);
+  return (need + 15) & ~15ll;
+}
+
+// Staging of a solve on nbk CTAs under limit bytes: resident mode when every
+// CTA's nodes fit with their PCG vectors, else as many nodes as fit.
+struct StagePlan {
+  int bytes = 0;
+  int resident = 0;
+};
+StagePlan plan_stage(const arap_solver* s, int nbk, int limit) {
+  StagePlan p;
+  if (limit <= 0 || nbk <= 0) return p;
+  if (!s->res_cost.empty()) {
+    const long long need = stage_need(s->order_host, s->res_cost, nbk);
+    if (need <= limit) {
+      p.bytes = (int)need;
+      p.resident = 1;
+      return p;
+    }
+  }
+  p.bytes = (int)std::min<long long>(stage_need(s->order_host, s->stage_cost, nbk), limit);
+  return p;
 }
 
 }  // namespace
@@ -305,6 +363,21 @@ extern "C" int arap_solver_create(arap_solver** out, int n, int k, const int32_t
       gca_off.push_back((int32_t)gca.size());
     }
   }
+  // coarse-list entries and constraint items of each node, and the shared
+  // memory of its tables
+  std::vector<int2> con_info(F, make_int2(0, 0));
+  std::vector<int32_t> stage_cost(F, 0), res_cost;
+  if (NA > 0) res_cost.assign(F, 0);
+  for (int r = 0; r < F; ++r) {
+    const int items_r = item_off[r + 1] - item_off[r];
+    for (int t = item_off[r]; t < item_off[r + 1]; ++t)
+      if (NA > 0 && (item_flat[t].x & 15) == ITEM_CON) {
+        con_info[r].x += gca_off[item_flat[t].z + 1] - gca_off[item_flat[t].z];
+        con_info[r].y += 1;
+      }
+    stage_cost[r] = stage_node_bytes(items_r, con_info[r].x, con_info[r].y, false);
+    if (NA > 0) res_cost[r] = stage_node_bytes(items_r, con_info[r].x, con_info[r].y, true);
+  }
 
   auto* s = new (std::nothrow) arap_solver();
   if (!s) return ARAP_ENOMEM;
@@ -371,6 +444,7 @@ extern "C" int arap_solver_create(arap_solver** out, int n, int k, const int32_t
     P.gca = cv.take<int32_t>(gca.size());
     P.gcv = cv.take<float4>(gca.size());
     P.uzg = cv.take<float4>(NA ? G : 0);
+    P.con_info = cv.take<int2>(F);
     P.partials = cv.take<double>((size_t)2 * kReduceSlots * grid);
     P.stats = cv.take<double>(kStatSlots);
     P.bar = cv.take<GridBarrier>(1);
@@ -412,6 +486,7 @@ extern "C" int arap_solver_create(arap_solver** out, int n, int k, const int32_t
     for (int i = 0; i < F; ++i) order[i] = cost[i].second;
   }
   e = e ? e : up(P.order, order.data(), order.size() * 4);
+  e = e ? e : up(P.con_info, con_info.data(), con_info.size() * sizeof(int2));
   if (NA > 0) {
     e = e ? e : up(P.mem_agg, mem_agg.data(), mem_agg.size() * 4);
     e = e ? e : up(P.agg, agg.data(), agg.size() * 4);
@@ -444,6 +519,16 @@ extern "C" int arap_solver_create(arap_solver** out, int n, int k, const int32_t
   P.refine = 0;
   P.NA = NA;
   P.NC = NC;
+  s->order_host = order;
+  s->stage_cost = stage_cost;
+  s->res_cost = res_cost;
+  {
+    const void* fn = cfg.precision == ARAP_PRECISION_MIXED ? (const void*)gn_solve_kernel<double>
+                                                           : (const void*)gn_solve_kernel<float>;
+    const StagePlan sp = plan_stage(s, s->grid, stage_limit(fn));
+    P.stage_cap = sp.bytes;
+    P.resident = sp.resident;
+  }
   *out = s;
   return ARAP_OK;
 }
@@ -474,9 +559,11 @@ static int launch_solver(arap_solver* s, cudaStream_t st) {
   void* args[] = {&s->P};
   cudaError_t e;
   if (s->cfg.precision == ARAP_PRECISION_MIXED)
-    e = cudaLaunchCooperativeKernel((const void*)gn_solve_kernel<double>, s->grid, kSolveThreads, args, 0, st);
+    e = cudaLaunchCooperativeKernel((const void*)gn_solve_kernel<double>, s->grid, kSolveThreads, args,
+                                    (size_t)s->P.stage_cap, st);
   else
-    e = cudaLaunchCooperativeKernel((const void*)gn_solve_kernel<float>, s->grid, kSolveThreads, args, 0, st);
+    e = cudaLaunchCooperativeKernel((const void*)gn_solve_kernel<float>, s->grid, kSolveThreads, args,
+                                    (size_t)s->P.stage_cap, st);
   if (e != cudaSuccess) {
     (void)cudaGetLastError();
     return ARAP_ECUDA;
@@ -552,6 +639,9 @@ struct arap_solver_batch {
   int grid = 0;                 // co-resident CTAs of the batched kernel
   float exponent = 1.f;         // CTA share ~ (coupling items + free nodes)^exponent
   std::vector<int> cta_first;   // [count+1]
+  int stage_limit = 0;          // shared-memory limit of the batched kernel's resident tables
+  int stage_cap = 0;            // dynamic shared memory of a batched launch
+  std::vector<int> resident;    // per instance: resident mode (see plan_stage)
   void* block = nullptr;        // device: params, cta_first, barriers, partials
   SolveParams* d_params = nullptr;
   int* d_cta_first = nullptr;
@@ -590,6 +680,13 @@ void split_ctas(arap_solver_batch* b) {
   for (int q = 0; q < spare - given; ++q) n[rem[q % count].second] += 1;
   b->cta_first.assign(count + 1, 0);
   for (int i = 0; i < count; ++i) b->cta_first[i + 1] = b->cta_first[i] + n[i];
+  b->stage_cap = 0;
+  b->resident.assign(count, 0);
+  for (int i = 0; i < count; ++i) {
+    const StagePlan sp = plan_stage(b->solvers[i], n[i], b->stage_limit);
+    b->stage_cap = std::max(b->stage_cap, sp.bytes);
+    b->resident[i] = sp.resident;
+  }
 }
 
 // The CTA ranges go to the device when they change (creation, autotuning),
@@ -638,6 +735,8 @@ extern "C" int arap_solver_batch_create(arap_solver_batch** out, arap_solver* co
     return ARAP_EUNSUPPORTED;
   }
   b->exponent = balance_exponent > 0.f ? balance_exponent : 1.f;
+  b->stage_limit = stage_limit(b->precision == ARAP_PRECISION_MIXED ? (const void*)gn_solve_batch_kernel<double>
+                                                                    : (const void*)gn_solve_batch_kernel<float>);
   split_ctas(b);
   Carver sizing{nullptr};
   auto carve = [&](Carver& cv) {
@@ -687,6 +786,8 @@ extern "C" int arap_solver_batch_solve(arap_solver_batch* b, const float* const*
     P.grad_out = nullptr;
     P.bar = b->d_bars + i;
     P.partials = b->d_partials + (size_t)2 * kReduceSlots * b->cta_first[i];
+    P.stage_cap = b->stage_cap;
+    P.resident = b->resident[i];
     b->h_params[i] = P;
   }
   ARAP_CUDA_TRY(cudaMemcpyAsync(b->d_params, b->h_params, sizeof(SolveParams) * count, cudaMemcpyHostToDevice, st));
@@ -698,9 +799,11 @@ extern "C" int arap_solver_batch_solve(arap_solver_batch* b, const float* const*
   void* args[] = {&b->d_params, &b->d_cta_first, const_cast<int*>(&count)};
   cudaError_t e;
   if (b->precision == ARAP_PRECISION_MIXED)
-    e = cudaLaunchCooperativeKernel((const void*)gn_solve_batch_kernel<double>, b->grid, kSolveThreads, args, 0, st);
+    e = cudaLaunchCooperativeKernel((const void*)gn_solve_batch_kernel<double>, b->grid, kSolveThreads, args,
+                                    (size_t)b->stage_cap, st);
   else
-    e = cudaLaunchCooperativeKernel((const void*)gn_solve_batch_kernel<float>, b->grid, kSolveThreads, args, 0, st);
+    e = cudaLaunchCooperativeKernel((const void*)gn_solve_batch_kernel<float>, b->grid, kSolveThreads, args,
+                                    (size_t)b->stage_cap, st);
   if (e != cudaSuccess) {
     (void)cudaGetLastError();
     return ARAP_ECUDA;

@@ -89,6 +89,27 @@ struct SolveParams {
   const int32_t* gca;        // aggregate ids
   float4* gcv;               // per solve: V_ga = sum over anchors in a of w (v_c - g_pivot(a), 1)
   float4* uzg;               // [G] w_con J_g u_f, refreshed after each update
+  // CTA-resident node tables: each CTA keeps the fixed data of the free nodes
+  // it processes (coupling items with their geometry, diagonal-block
+  // inverses, aggregate offsets) in dynamic shared memory, for as many of its
+  // nodes as stage_cap bytes hold; the rest are read from the global tables
+  const int2* con_info;      // [F] {coarse-list entries, constraint items} of each node (0 without a coarse level)
+  int stage_cap;             // dynamic shared memory of the launch, bytes (0: nothing staged)
+  int resident;              // every CTA holds all of its nodes, with their PCG vectors (two-level PCG only)
 };
+
+// Shared-memory bytes of one staged node: its 12x12 inverse block (576), two
+// node records (32) and its aggregate offset (16), plus 32 per coupling item
+// (item + geometry) and 20 per coarse-list entry of its constraint items.
+constexpr int kStageNodeBytes = 576 + 32 + 16;
+constexpr int kStageItemBytes = 32;
+constexpr int kStageListBytes = 20;
+// Resident mode adds per node its PCG vectors (8 x 12 floats) and the float
+// copy of x (12), per coupling item the other node's aggregate offset (16),
+// and per constraint item its group id and the group's w_con J_g u_f (20).
+constexpr int kResVecs = 8;
+constexpr int kResNodeBytes = kResVecs * 48 + 48;
+constexpr int kResItemBytes = 16;
+constexpr int kResConBytes = 20;
 
 }  // namespace arap

@@ -32,10 +32,51 @@ __device__ __forceinline__ void ld3t_cg(const float* base, int r, float (&v)[3])
 // nodes and by the constraint items touching it).
 __shared__ __align__(16) float s_zc[kMaxCoarse];
 
-// Coarse correction of free node rr in aggregate a: z += P_j zc[a] with
-// dR_j = dR_a, dt_j = dR_a (g_j - g_pivot(a)) + dT_a, zc from s_zc.
-__device__ __forceinline__ void coarse_prolong(const SolveParams& P, int rr, int a, float (&v)[12]) {
-  const float4 dp = __ldcg(P.dpiv + rr);
+// CTA-resident node tables in dynamic shared memory.  Slot s of a CTA is the
+// s-th free node it processes (order position s * nbk + bid).  For n staged
+// slots, ni coupling items, nl coarse-list entries and nc constraint items the
+// layout is
+//   [inverse blocks: n x 144 floats][nodes: n int4 {r, item base, items, aggregate}]
+//   [bases: n int4 {list base, constraint-item base}][offsets: n float4 g_j - g_pivot]
+//   [items: ni int4][geometry: ni float4][list V_ga: nl float4]
+//   resident mode only: [PCG vectors: n x 8 x 12 floats][x: n x 12 floats]
+//                       [other node's offset: ni float4][w_con J_g u_f: nc float4]
+//   [list aggregate: nl int] resident mode only: [constraint group: nc int]
+// Staged constraint items carry {kind | constraint-item index << 4, list base,
+// g, list length} and, for every item, the geometry a product needs
+// ({sgn (g_k - g_j), w scale} for regularisation items, {a, v_c - g_l} for
+// constraint items).
+extern __shared__ __align__(16) unsigned char s_dyn[];
+struct StageLayout {
+  int n;                                   // staged slots (even unless all of the CTA's nodes are staged)
+  int nd, nx, dp, it, ax, gv, vec, xf, yd, cu, ga, cg;  // byte offsets after the inverse blocks
+  int ncon;                                // constraint items of the staged slots
+};
+__shared__ StageLayout s_stg;
+
+__device__ __forceinline__ float* stg_dinv(int s) { return reinterpret_cast<float*>(s_dyn) + 144 * s; }
+__device__ __forceinline__ int4* stg_node() { return reinterpret_cast<int4*>(s_dyn + s_stg.nd); }
+__device__ __forceinline__ int4* stg_base() { return reinterpret_cast<int4*>(s_dyn + s_stg.nx); }
+__device__ __forceinline__ float4* stg_dpiv() { return reinterpret_cast<float4*>(s_dyn + s_stg.dp); }
+__device__ __forceinline__ int4* stg_item() { return reinterpret_cast<int4*>(s_dyn + s_stg.it); }
+__device__ __forceinline__ float4* stg_geo() { return reinterpret_cast<float4*>(s_dyn + s_stg.ax); }
+__device__ __forceinline__ float4* stg_lv() { return reinterpret_cast<float4*>(s_dyn + s_stg.gv); }
+__device__ __forceinline__ int* stg_la() { return reinterpret_cast<int*>(s_dyn + s_stg.ga); }
+// resident mode: PCG vector k of slot s (12 floats), x of slot s, the other
+// node's offset of item i, w_con J_g u_f and group of constraint item c
+enum { RV_UF = 0, RV_R, RV_P, RV_S, RV_H, RV_U, RV_W, RV_WF };
+__device__ __forceinline__ float* stg_vec(int s, int k) {
+  return reinterpret_cast<float*>(s_dyn + s_stg.vec) + 12 * (kResVecs * s + k);
+}
+__device__ __forceinline__ float* stg_xf(int s) { return reinterpret_cast<float*>(s_dyn + s_stg.xf) + 12 * s; }
+__device__ __forceinline__ float4* stg_ydp() { return reinterpret_cast<float4*>(s_dyn + s_stg.yd); }
+__device__ __forceinline__ float4* stg_cuz() { return reinterpret_cast<float4*>(s_dyn + s_stg.cu); }
+__device__ __forceinline__ int* stg_cg() { return reinterpret_cast<int*>(s_dyn + s_stg.cg); }
+
+// Coarse correction of a free node with offset dp = g_j - g_pivot(a) in
+// aggregate a: z += P_j zc[a] with dR_j = dR_a, dt_j = dR_a dp + dT_a, zc
+// from s_zc.
+__device__ __forceinline__ void coarse_prolong_dp(const float4 dp, int a, float (&v)[12]) {
   const float d0 = dp.x, d1 = dp.y, d2 = dp.z;
   const float4* c4 = reinterpret_cast<const float4*>(s_zc + 12 * a);
   const float4 ca = c4[0], cb = c4[1], cc = c4[2];
@@ -44,6 +85,10 @@ __device__ __forceinline__ void coarse_prolong(const SolveParams& P, int rr, int
   for (int i = 0; i < 9; ++i) v[i] += c[i];
 #pragma unroll
   for (int r = 0; r < 3; ++r) v[9 + r] += c[9 + r] + d0 * c[r] + d1 * c[3 + r] + d2 * c[6 + r];
+}
+
+__device__ __forceinline__ void coarse_prolong(const SolveParams& P, int rr, int a, float (&v)[12]) {
+  coarse_prolong_dp(__ldcg(P.dpiv + rr), a, v);
 }
 
 // Preconditioned residual u = u_f + P zc of free node rr in aggregate agg,
@@ -189,6 +234,25 @@ __device__ void con_ju_coarse(const SolveParams& P, int g, float (&u)[3]) {
   for (int f = f0; f < f1; ++f) {
     const float4 V = __ldcg(P.gcv + f);
     const float4* c4 = reinterpret_cast<const float4*>(s_zc + 12 * __ldg(P.gca + f));
+    const float4 ca = c4[0], cb = c4[1], cc = c4[2];
+    const float C[12] = {ca.x, ca.y, ca.z, ca.w, cb.x, cb.y, cb.z, cb.w, cc.x, cc.y, cc.z, cc.w};
+#pragma unroll
+    for (int c = 0; c < 3; ++c)
+      u[c] = fmaf(wcf, fmaf(V.x, C[c], fmaf(V.y, C[3 + c], fmaf(V.z, C[6 + c], V.w * C[9 + c]))), u[c]);
+  }
+}
+
+// con_ju_coarse of a staged constraint item: the group's aggregates and
+// V_ga are the len entries of the CTA's coarse list from off.
+__device__ __forceinline__ void con_ju_list(const SolveParams& P, int g, int off, int len, float (&u)[3]) {
+  const float4 uz = __ldcg(P.uzg + g);
+  u[0] = uz.x;
+  u[1] = uz.y;
+  u[2] = uz.z;
+  const float wcf = (float)P.wc;
+  for (int f = off; f < off + len; ++f) {
+    const float4 V = stg_lv()[f];
+    const float4* c4 = reinterpret_cast<const float4*>(s_zc + 12 * stg_la()[f]);
     const float4 ca = c4[0], cb = c4[1], cc = c4[2];
     const float C[12] = {ca.x, ca.y, ca.z, ca.w, cb.x, cb.y, cb.z, cb.w, cc.x, cc.y, cc.z, cc.w};
 #pragma unroll
@@ -453,7 +517,7 @@ __device__ __forceinline__ void apply_item(const SolveParams& P, const CouplingD
 // u formed on the fly for every node it touches; also returns this node's u in
 // every lane of the half.  A half with valid == false does no loads but takes
 // part in the warp shuffles.
-__device__ void spmv_node(const SolveParams& P, int r, bool valid, float (&acc)[12], float (&pj)[12]) {
+static __device__ __noinline__ void spmv_node(const SolveParams& P, int r, bool valid, float (&acc)[12], float (&pj)[12]) {
   const int lane = threadIdx.x & 15;
 #pragma unroll
   for (int i = 0; i < 12; ++i) {
@@ -512,6 +576,172 @@ __device__ void spmv_node(const SolveParams& P, int r, bool valid, float (&acc)[
   }
 }
 
+// Translation part of coarse_prolong_dp (the same expression for v[9..11]).
+__device__ __forceinline__ void coarse_prolong_t(const float4 dp, int a, float (&t)[3]) {
+  const float d0 = dp.x, d1 = dp.y, d2 = dp.z;
+  const float4* c4 = reinterpret_cast<const float4*>(s_zc + 12 * a);
+  const float4 ca = c4[0], cb = c4[1], cc = c4[2];
+  const float c[12] = {ca.x, ca.y, ca.z, ca.w, cb.x, cb.y, cb.z, cb.w, cc.x, cc.y, cc.z, cc.w};
+#pragma unroll
+  for (int r = 0; r < 3; ++r) t[r] += c[9 + r] + d0 * c[r] + d1 * c[3 + r] + d2 * c[6 + r];
+}
+
+// A staged coupling item in two steps: issue() starts every global load the
+// item needs (the other node's u_f and offset, or the group's w_con J_g u_f)
+// without using any of them, so that the loads of all items of a round are in
+// flight together; finish() adds the coarse parts from shared memory.  The
+// result equals fetch_item's.
+struct StagedItem {
+  CouplingData d;
+  float4 dp;     // offset of the other node (ITEM_IN / ITEM_OUT, coarse level on)
+  int a;         // its aggregate; for ITEM_CON the list base
+  int len;       // ITEM_CON: coarse-list length
+};
+
+__device__ __forceinline__ void item_issue(const SolveParams& P, int i, StagedItem& S) {
+  const int4 m = stg_item()[i];
+  CouplingData& D = S.d;
+  D.kind = m.x & 15;
+  D.aux = stg_geo()[i];
+  S.a = m.x >> 4;
+  S.len = 0;
+  S.dp = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+  for (int q = 0; q < 12; ++q) D.v[q] = 0.f;
+  if (D.kind == ITEM_IN) {
+    ld12cg(P.z, m.y, D.v);
+    if (P.NA) S.dp = __ldcg(P.dpiv + m.y);
+  } else if (D.kind == ITEM_OUT) {
+    if (m.y >= 0) {
+      float t3[3];
+      ld3t_cg(P.z, m.y, t3);
+      D.v[0] = t3[0];
+      D.v[1] = t3[1];
+      D.v[2] = t3[2];
+      if (P.NA) S.dp = __ldcg(P.dpiv + m.y);
+    } else {
+      D.kind = ITEM_OUT | 16;  // static neighbour: no vector
+    }
+  } else if (D.kind == ITEM_CON) {
+    if (P.NA) {
+      const float4 uz = __ldcg(P.uzg + m.z);
+      D.v[0] = uz.x;
+      D.v[1] = uz.y;
+      D.v[2] = uz.z;
+      S.a = m.y;
+      S.len = m.w;
+    } else {
+      float u[3];
+      con_ju(P, m.z, u);
+      D.v[0] = u[0];
+      D.v[1] = u[1];
+      D.v[2] = u[2];
+    }
+  }
+}
+
+__device__ __forceinline__ void item_finish(const SolveParams& P, StagedItem& S) {
+  CouplingData& D = S.d;
+  if (D.kind == (ITEM_OUT | 16)) {
+    D.kind = ITEM_OUT;
+    return;
+  }
+  if (!P.NA) return;
+  if (D.kind == ITEM_IN) {
+    coarse_prolong_dp(S.dp, S.a, D.v);
+  } else if (D.kind == ITEM_OUT) {
+    float t3[3] = {D.v[0], D.v[1], D.v[2]};
+    coarse_prolong_t(S.dp, S.a, t3);
+    D.v[0] = t3[0];
+    D.v[1] = t3[1];
+    D.v[2] = t3[2];
+  } else if (D.kind == ITEM_CON) {
+    const float wcf = (float)P.wc;
+    for (int f = S.a; f < S.a + S.len; ++f) {
+      const float4 V = stg_lv()[f];
+      const float4* c4 = reinterpret_cast<const float4*>(s_zc + 12 * stg_la()[f]);
+      const float4 ca = c4[0], cb = c4[1], cc = c4[2];
+      const float C[12] = {ca.x, ca.y, ca.z, ca.w, cb.x, cb.y, cb.z, cb.w, cc.x, cc.y, cc.z, cc.w};
+#pragma unroll
+      for (int c = 0; c < 3; ++c)
+        D.v[c] = fmaf(wcf, fmaf(V.x, C[c], fmaf(V.y, C[3 + c], fmaf(V.z, C[6 + c], V.w * C[9 + c]))), D.v[c]);
+    }
+  }
+}
+
+// spmv_node for staged slot s (free node r): the same arithmetic in the same
+// order, with the node's items, geometry and aggregate offset in shared
+// memory.  All global loads of a round (the node's own u_f, x and the other
+// nodes' vectors) are issued before any is used, so a product costs one
+// round trip to L2 instead of a chain of dependent global loads.  The
+// rotation term's x comes from lanes 0..8 of the half.
+__device__ __forceinline__ void spmv_node_stg(const SolveParams& P, int s, int r, bool valid, float (&acc)[12],
+                                              float (&pj)[12]) {
+  const int lane = threadIdx.x & 15;
+  const int base = threadIdx.x & 16;
+#pragma unroll
+  for (int i = 0; i < 12; ++i) {
+    acc[i] = 0.f;
+    pj[i] = 0.f;
+  }
+  float xr = 0.f;
+  if (valid) {
+    const int4 nd = stg_node()[s];
+    if (lane < 9) xr = __ldcg(P.xf + 12 * (size_t)r + lane);
+    ld12cg(P.z, r, pj);
+    bool own = !P.NA;  // own coarse part added
+    const float w = (float)P.wg;
+    for (int q = lane; q < nd.z; q += 32) {
+      const bool hasB = q + 16 < nd.z;
+      StagedItem A, B;
+      item_issue(P, nd.y + q, A);
+      if (hasB) item_issue(P, nd.y + q + 16, B);
+      if (!own) {
+        coarse_prolong_dp(stg_dpiv()[s], nd.w, pj);
+        own = true;
+      }
+      item_finish(P, A);
+      apply_item(P, A.d, w, pj, acc);
+      if (hasB) {
+        item_finish(P, B);
+        apply_item(P, B.d, w, pj, acc);
+      }
+    }
+    if (!own) coarse_prolong_dp(stg_dpiv()[s], nd.w, pj);
+  }
+  float X[9];
+#pragma unroll
+  for (int i = 0; i < 9; ++i) X[i] = __shfl_sync(0xffffffffu, xr, base + i);
+  if (valid && lane == 0) {
+    // J_rot^T J_rot p with J_rot at the current x (float copy)
+    const float* c0 = X;
+    const float* c1 = X + 3;
+    const float* c2 = X + 6;
+    const float* p0 = pj;
+    const float* p1 = pj + 3;
+    const float* p2 = pj + 6;
+    const float wr = (float)P.wr;
+    auto dot = [](const float* a3, const float* b3) { return a3[0] * b3[0] + a3[1] * b3[1] + a3[2] * b3[2]; };
+    const float u0 = wr * (dot(c1, p0) + dot(c0, p1));
+    const float u1 = wr * (dot(c2, p0) + dot(c0, p2));
+    const float u2 = wr * (dot(c2, p1) + dot(c1, p2));
+    const float u3 = 2.f * wr * dot(c0, p0);
+    const float u4 = 2.f * wr * dot(c1, p1);
+    const float u5 = 2.f * wr * dot(c2, p2);
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      acc[i] += wr * (u0 * c1[i] + u1 * c2[i] + 2.f * u3 * c0[i]);
+      acc[3 + i] += wr * (u0 * c0[i] + u2 * c2[i] + 2.f * u4 * c1[i]);
+      acc[6 + i] += wr * (u1 * c0[i] + u2 * c1[i] + 2.f * u5 * c2[i]);
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < 12; ++i) {
+#pragma unroll
+    for (int o = 8; o > 0; o >>= 1) acc[i] += __shfl_xor_sync(0xffffffffu, acc[i], o);
+  }
+}
+
 // Diagonal 12x12 block of J^T J for free node r from Q and the rotation rows
 // at x (float copy), inverted by Gauss-Jordan without pivoting (the block is
 // symmetric positive definite) across 24 lanes: lane j < 12 holds column j of
@@ -519,7 +749,8 @@ __device__ void spmv_node(const SolveParams& P, int r, bool valid, float (&acc)[
 // pivot column from its lane by shuffle.  Lanes 12..23 end with the columns of
 // the inverse (= its rows) and store them into P.dinv (row-major).  A block
 // that is not positive definite falls back to the inverse of its diagonal.
-__device__ void build_dinv(const SolveParams& P, int r, const float (&Q)[10]) {
+template <bool STG>
+__device__ void build_dinv(const SolveParams& P, int r, int slot, const float (&Q)[10]) {
   const int lane = threadIdx.x & 31;
   float X[9];
 #pragma unroll
@@ -593,7 +824,11 @@ __device__ void build_dinv(const SolveParams& P, int r, const float (&Q)[10]) {
   const float dgj = __shfl_sync(0xffffffffu, dg, lane >= 12 && lane < 24 ? lane - 12 : 0);
   if (lane >= 12 && lane < 24) {
     const int j = lane - 12;
-    float* out = P.dinv + 144 * (size_t)r + 12 * j;
+    float* out;
+    if constexpr (STG)
+      out = stg_dinv(slot) + 12 * j;
+    else
+      out = P.dinv + 144 * (size_t)r + 12 * j;
 #pragma unroll
     for (int i = 0; i < 12; ++i) out[i] = ok ? col[i] : ((i == j) ? 1.f / fmaxf(dgj, 1e-20f) : 0.f);
   }
@@ -614,15 +849,36 @@ __device__ __forceinline__ float apply_dinv_h(const SolveParams& P, int rr, bool
   return (valid && l16 < 12) ? zc : 0.f;
 }
 
-// z = Dinv r for free node rr; lane c < 12 holds r_c and returns z_c.
-__device__ __forceinline__ float apply_dinv(const SolveParams& P, int rr, float rc) {
+// apply_dinv_h with the inverse block of staged slot s.
+__device__ __forceinline__ float apply_dinv_h_stg(int s, bool valid, float rc) {
+  const int lane = threadIdx.x & 31;
+  const int l16 = lane & 15, base = lane & 16;
+  float zc = 0.f;
+  const float* row = stg_dinv(valid ? s : 0) + 12 * (l16 < 12 ? l16 : 0);
+#pragma unroll
+  for (int i = 0; i < 12; ++i) {
+    const float ri = __shfl_sync(0xffffffffu, rc, base + i);
+    if (valid) zc = fmaf(row[i], ri, zc);
+  }
+  return (valid && l16 < 12) ? zc : 0.f;
+}
+
+// z = Dinv r for free node rr (staged: slot's inverse block in shared
+// memory); lane c < 12 holds r_c and returns z_c.
+template <bool STG>
+__device__ __forceinline__ float apply_dinv(const SolveParams& P, int rr, int slot, float rc) {
   const int lane = threadIdx.x & 31;
   float zc = 0.f;
-  const float* row = P.dinv + 144 * (size_t)rr + 12 * (lane < 12 ? lane : 0);
+  const int L = lane < 12 ? lane : 0;
 #pragma unroll
   for (int i = 0; i < 12; ++i) {
     const float ri = __shfl_sync(0xffffffffu, rc, i);
-    zc = fmaf(__ldcg(row + i), ri, zc);
+    float d;
+    if constexpr (STG)
+      d = stg_dinv(slot)[12 * L + i];
+    else
+      d = __ldcg(P.dinv + 144 * (size_t)rr + 12 * L + i);
+    zc = fmaf(d, ri, zc);
   }
   return lane < 12 ? zc : 0.f;
 }
@@ -815,6 +1071,23 @@ __device__ __forceinline__ void coarse_restrict_h(const SolveParams& P, int rr, 
   }
 }
 
+// coarse_restrict_h of staged slot s (aggregate and offset from shared memory).
+__device__ __forceinline__ void coarse_restrict_h_stg(int s, bool valid, float rc_lane, double* rc) {
+  const int lane = threadIdx.x & 31;
+  const int l16 = lane & 15, base = lane & 16;
+  const int c = l16 < 9 ? l16 / 3 : 0, r = l16 < 9 ? l16 % 3 : 0;
+  const float rt = __shfl_sync(0xffffffffu, rc_lane, base + 9 + r);
+  if (valid && l16 < 12) {
+    const int a = stg_node()[s].w;
+    float v = rc_lane;
+    if (l16 < 9) {
+      const float4 dp = stg_dpiv()[s];
+      v += (c == 0 ? dp.x : (c == 1 ? dp.y : dp.z)) * rt;
+    }
+    atomicAdd(rc + 12 * a + l16, (double)v);
+  }
+}
+
 // Restriction of free node rr's residual (lane c < 12 holds r_c) into rc:
 // (P_j^T r_j)_{3c+r} = r_{3c+r} + d_c r_{9+r}, (P_j^T r_j)_{9+r} = r_{9+r}.
 __device__ __forceinline__ void coarse_restrict(const SolveParams& P, int rr, float rc_lane, double* rc) {
@@ -829,6 +1102,382 @@ __device__ __forceinline__ void coarse_restrict(const SolveParams& P, int rr, fl
     if (lane < 9) v += (__ldg(P.node_pos + 3 * (size_t)node + c) - __ldg(P.node_pos + 3 * (size_t)pv + c)) * rt;
     atomicAdd(rc + 12 * a + lane, (double)v);
   }
+}
+
+// ---------------------------------------------------- resident PCG ----
+// With every node of a CTA resident, (J^T J) u with u = u_f + P zc is taken
+// in two parts by linearity: w_f = (J^T J)_reg u_f (regularisation and
+// static-node rows, the neighbours' u_f from L2) in the coarse-solve phase,
+// and the rest in the products phase from shared memory only: the
+// regularisation rows on y = P zc (every node's y from zc and its offset),
+// the constraint rows on J_g u = w_con J_g u_f + sum_a V_ga zc_a, and the
+// rotation rows on u.  The vector update touches only the CTA's own nodes.
+
+// PCG vector update of resident slot s (half-warp; lane c < 12 owns entry c):
+// p = u + beta p, s = w + beta s, h += alpha p, r -= alpha s, u_f = Dinv r,
+// and the restriction of r into rc.  u_f and h also go to global memory
+// (neighbours' products, line search).
+static __device__ __noinline__ void res_update(const SolveParams& P, int s, bool valid, float alpha, float beta,
+                                           bool first, double* rc) {
+  const int l16 = threadIdx.x & 15;
+  const bool own = valid && l16 < 12;
+  float rv = 0.f, hv = 0.f;
+  int r = 0;
+  if (own) {
+    r = stg_node()[s].x;
+    const float uo = stg_vec(s, RV_U)[l16], wo = stg_vec(s, RV_W)[l16];
+    const float pn = first ? uo : fmaf(beta, stg_vec(s, RV_P)[l16], uo);
+    const float sn = first ? wo : fmaf(beta, stg_vec(s, RV_S)[l16], wo);
+    stg_vec(s, RV_P)[l16] = pn;
+    stg_vec(s, RV_S)[l16] = sn;
+    hv = fmaf(alpha, pn, stg_vec(s, RV_H)[l16]);
+    stg_vec(s, RV_H)[l16] = hv;
+    rv = fmaf(-alpha, sn, stg_vec(s, RV_R)[l16]);
+    stg_vec(s, RV_R)[l16] = rv;
+  }
+  const float zv = apply_dinv_h_stg(s, valid, rv);
+  coarse_restrict_h_stg(s, valid, rv, rc);
+  if (own) {
+    stg_vec(s, RV_UF)[l16] = zv;
+    P.z[12 * (size_t)r + l16] = zv;
+    P.h[12 * (size_t)r + l16] = hv;
+  }
+}
+
+// w_f = (J^T J)_reg u_f of resident slot s (regularisation and static-node
+// items; constraint items are left to res_products).  Lane c < 12 of the
+// half stores entry c.
+static __device__ __noinline__ void res_products_f(const SolveParams& P, int s, bool valid) {
+  const int lane = threadIdx.x & 15;
+  float acc[12], pj[12];
+#pragma unroll
+  for (int i = 0; i < 12; ++i) {
+    acc[i] = 0.f;
+    pj[i] = 0.f;
+  }
+  if (valid) {
+    const int4 nd = stg_node()[s];
+    const float4* u4 = reinterpret_cast<const float4*>(stg_vec(s, RV_UF));
+    const float4 a = u4[0], b = u4[1], c = u4[2];
+    pj[0] = a.x; pj[1] = a.y; pj[2] = a.z; pj[3] = a.w; pj[4] = b.x; pj[5] = b.y;
+    pj[6] = b.z; pj[7] = b.w; pj[8] = c.x; pj[9] = c.y; pj[10] = c.z; pj[11] = c.w;
+    const float w = (float)P.wg;
+    for (int q = lane; q < nd.z; q += 32) {
+      const bool hasB = q + 16 < nd.z;
+      CouplingData A, B;
+      auto fetch = [&](int i, CouplingData& D) {
+        const int4 m = stg_item()[i];
+        D.kind = m.x & 15;
+        D.aux = stg_geo()[i];
+#pragma unroll
+        for (int t = 0; t < 12; ++t) D.v[t] = 0.f;
+        if (D.kind == ITEM_IN) {
+          ld12cg(P.z, m.y, D.v);
+        } else if (D.kind == ITEM_OUT && m.y >= 0) {
+          float t3[3];
+          ld3t_cg(P.z, m.y, t3);
+          D.v[0] = t3[0];
+          D.v[1] = t3[1];
+          D.v[2] = t3[2];
+        }
+      };
+      fetch(nd.y + q, A);
+      if (hasB) fetch(nd.y + q + 16, B);
+      if (A.kind != ITEM_CON) apply_item(P, A, w, pj, acc);
+      if (hasB && B.kind != ITEM_CON) apply_item(P, B, w, pj, acc);
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < 12; ++i) {
+#pragma unroll
+    for (int o = 8; o > 0; o >>= 1) acc[i] += __shfl_xor_sync(0xffffffffu, acc[i], o);
+  }
+  if (valid && lane < 12) {
+    float v = 0.f;
+#pragma unroll
+    for (int i = 0; i < 12; ++i)
+      if (i == lane) v = acc[i];
+    stg_vec(s, RV_WF)[lane] = v;
+  }
+}
+
+// The rest of w = (J^T J) u for resident slot s, from shared memory only
+// (s_zc and the staged w_con J_g u_f of the CTA's constraint items must be in
+// place): u = u_f + y, w = w_f + (J^T J)_reg y + constraint rows on J_g u +
+// rotation rows on u.  Stores u and w and adds r.u, w.u and r.r into f3
+// (lane c < 12 of the half owns entry c).
+static __device__ __noinline__ void res_products(const SolveParams& P, int s, bool valid, float (&f3)[3]) {
+  const int lane = threadIdx.x & 15;
+  const int base = threadIdx.x & 16;
+  float acc[12], y[12];
+#pragma unroll
+  for (int i = 0; i < 12; ++i) {
+    acc[i] = 0.f;
+    y[i] = 0.f;
+  }
+  float xr = 0.f;
+  if (valid) {
+    const int4 nd = stg_node()[s];
+    if (lane < 9) xr = stg_xf(s)[lane];
+    coarse_prolong_dp(stg_dpiv()[s], nd.w, y);
+    const float w = (float)P.wg;
+    const float wcf = (float)P.wc;
+    for (int q = lane; q < nd.z; q += 16) {
+      const int i = nd.y + q;
+      CouplingData D;
+      const int4 m = stg_item()[i];
+      D.kind = m.x & 15;
+      D.aux = stg_geo()[i];
+#pragma unroll
+      for (int t = 0; t < 12; ++t) D.v[t] = 0.f;
+      if (D.kind == ITEM_IN) {
+        coarse_prolong_dp(stg_ydp()[i], m.x >> 4, D.v);
+      } else if (D.kind == ITEM_OUT) {
+        if (m.y >= 0) {
+          float t3[3] = {0.f, 0.f, 0.f};
+          coarse_prolong_t(stg_ydp()[i], m.x >> 4, t3);
+          D.v[0] = t3[0];
+          D.v[1] = t3[1];
+          D.v[2] = t3[2];
+        }
+      } else if (D.kind == ITEM_CON) {
+        const float4 uz = stg_cuz()[m.x >> 4];
+        D.v[0] = uz.x;
+        D.v[1] = uz.y;
+        D.v[2] = uz.z;
+        for (int f = m.y; f < m.y + m.w; ++f) {
+          const float4 V = stg_lv()[f];
+          const float4* c4 = reinterpret_cast<const float4*>(s_zc + 12 * stg_la()[f]);
+          const float4 ca = c4[0], cb = c4[1], cc = c4[2];
+          const float C[12] = {ca.x, ca.y, ca.z, ca.w, cb.x, cb.y, cb.z, cb.w, cc.x, cc.y, cc.z, cc.w};
+#pragma unroll
+          for (int c = 0; c < 3; ++c)
+            D.v[c] = fmaf(wcf, fmaf(V.x, C[c], fmaf(V.y, C[3 + c], fmaf(V.z, C[6 + c], V.w * C[9 + c]))), D.v[c]);
+        }
+      }
+      apply_item(P, D, w, y, acc);
+    }
+  }
+  // u = u_f + y for the rotation rows
+  float uj[12];
+  {
+    const float4* u4 = reinterpret_cast<const float4*>(stg_vec(valid ? s : 0, RV_UF));
+    const float4 a = u4[0], b = u4[1], c = u4[2];
+    const float uf[12] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w, c.x, c.y, c.z, c.w};
+#pragma unroll
+    for (int i = 0; i < 12; ++i) uj[i] = uf[i] + y[i];
+  }
+  float X[9];
+#pragma unroll
+  for (int i = 0; i < 9; ++i) X[i] = __shfl_sync(0xffffffffu, xr, base + i);
+  if (valid && lane == 0) {
+    const float* c0 = X;
+    const float* c1 = X + 3;
+    const float* c2 = X + 6;
+    const float* p0 = uj;
+    const float* p1 = uj + 3;
+    const float* p2 = uj + 6;
+    const float wr = (float)P.wr;
+    auto dot = [](const float* a3, const float* b3) { return a3[0] * b3[0] + a3[1] * b3[1] + a3[2] * b3[2]; };
+    const float u0 = wr * (dot(c1, p0) + dot(c0, p1));
+    const float u1 = wr * (dot(c2, p0) + dot(c0, p2));
+    const float u2 = wr * (dot(c2, p1) + dot(c1, p2));
+    const float u3 = 2.f * wr * dot(c0, p0);
+    const float u4 = 2.f * wr * dot(c1, p1);
+    const float u5 = 2.f * wr * dot(c2, p2);
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      acc[i] += wr * (u0 * c1[i] + u1 * c2[i] + 2.f * u3 * c0[i]);
+      acc[3 + i] += wr * (u0 * c0[i] + u2 * c2[i] + 2.f * u4 * c1[i]);
+      acc[6 + i] += wr * (u1 * c0[i] + u2 * c1[i] + 2.f * u5 * c2[i]);
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < 12; ++i) {
+#pragma unroll
+    for (int o = 8; o > 0; o >>= 1) acc[i] += __shfl_xor_sync(0xffffffffu, acc[i], o);
+  }
+  if (valid && lane < 12) {
+    float uc = 0.f, wv = 0.f;
+#pragma unroll
+    for (int i = 0; i < 12; ++i)
+      if (i == lane) {
+        uc = uj[i];
+        wv = acc[i];
+      }
+    wv += stg_vec(s, RV_WF)[lane];
+    const float rv = stg_vec(s, RV_R)[lane];
+    stg_vec(s, RV_U)[lane] = uc;
+    stg_vec(s, RV_W)[lane] = wv;
+    f3[0] = fmaf(rv, uc, f3[0]);
+    f3[1] = fmaf(wv, uc, f3[1]);
+    f3[2] = fmaf(rv, rv, f3[2]);
+  }
+}
+
+// Shared-memory bytes of one node's tables (host and device use the same sum).
+__host__ __device__ __forceinline__ int stage_node_bytes(int items, int lists, int cons, bool resident) {
+  int b = kStageNodeBytes + kStageItemBytes * items + kStageListBytes * lists;
+  if (resident) b += kResNodeBytes + kResItemBytes * items + kResConBytes * cons;
+  return b;
+}
+
+// Fills the CTA's resident node tables for this solve (after the per-solve
+// geometry: member offsets, aggregate offsets and V_ga).  Warp 0 finds how
+// many of the CTA's nodes fit in stage_cap bytes and lays the regions out;
+// then one warp per staged node copies its items with their geometry and
+// coarse lists.  Nothing is staged in gradient-only mode.  In resident mode
+// every node of the CTA must fit (the host sizes stage_cap so).
+__device__ void stage_build(const SolveParams& P, int bid, int nbk) {
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  const int F = P.F;
+  const bool res = P.resident != 0 && P.mode == 0 && P.NA > 0;
+  const int cnt = bid < F ? (F - bid + nbk - 1) / nbk : 0;
+  auto node_counts = [&](int s, int& r, int& a, int& l, int& c) {
+    r = 0;
+    a = 0;
+    l = 0;
+    c = 0;
+    if (s < cnt) {
+      r = __ldg(P.order + s * nbk + bid);
+      a = __ldg(P.item_off + r + 1) - __ldg(P.item_off + r);
+      const int2 ci = __ldg(P.con_info + r);
+      l = ci.x;
+      c = ci.y;
+    }
+  };
+  auto scan = [&](int v) {
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int t = __shfl_up_sync(0xffffffffu, v, o);
+      if (lane >= o) v += t;
+    }
+    return v;
+  };
+  if (wib == 0) {
+    int used = 0, n = 0, ni = 0, nl = 0, nc = 0;
+    bool more = P.stage_cap > 0 && P.mode == 0;
+    for (int c0 = 0; c0 < cnt && more; c0 += 32) {
+      int r, a, l, c;
+      node_counts(c0 + lane, r, a, l, c);
+      const int bytes = c0 + lane < cnt ? stage_node_bytes(a, l, c, res) : 0;
+      const int ib = scan(bytes), ia = scan(a), il = scan(l), ic = scan(c);
+      // inclusive byte sums grow with the lane, so the slots that fit are a prefix
+      const unsigned fit = __ballot_sync(0xffffffffu, c0 + lane < cnt && used + ib <= P.stage_cap);
+      const int kf = __popc(fit);
+      if (kf > 0) {
+        used += __shfl_sync(0xffffffffu, ib, kf - 1);
+        ni += __shfl_sync(0xffffffffu, ia, kf - 1);
+        nl += __shfl_sync(0xffffffffu, il, kf - 1);
+        nc += __shfl_sync(0xffffffffu, ic, kf - 1);
+        n += kf;
+      }
+      more = kf == 32;
+    }
+    // the two halves of a warp are staged together: an even count unless all fit
+    if (n < cnt) {
+      n &= ~1;
+      if (res && lane == 0) raise_status(ARAP_EUNSUPPORTED);
+    }
+    if (lane == 0) {
+      StageLayout L;
+      L.n = n;
+      L.ncon = res ? nc : 0;
+      L.nd = 576 * n;
+      L.nx = L.nd + 16 * n;
+      L.dp = L.nx + 16 * n;
+      L.it = L.dp + 16 * n;
+      L.ax = L.it + 16 * ni;
+      L.gv = L.ax + 16 * ni;
+      L.vec = L.gv + 16 * nl;
+      L.xf = L.vec + (res ? kResVecs * 48 * n : 0);
+      L.yd = L.xf + (res ? 48 * n : 0);
+      L.cu = L.yd + (res ? 16 * ni : 0);
+      L.ga = L.cu + (res ? 16 * nc : 0);
+      L.cg = L.ga + 4 * nl;
+      s_stg = L;
+    }
+  }
+  __syncthreads();
+  const int n = s_stg.n;
+  if (n == 0) return;
+  if (wib == 0) {
+    // node records, list and constraint-item bases
+    int ib = 0, lb = 0, cb = 0;
+    for (int c0 = 0; c0 < n; c0 += 32) {
+      const int sl = c0 + lane;
+      int r, a, l, c;
+      node_counts(sl < n ? sl : cnt, r, a, l, c);
+      const int ia = scan(a), il = scan(l), ic = scan(c);
+      if (sl < n) {
+        stg_node()[sl] = make_int4(r, ib + ia - a, a, P.NA ? __ldg(P.agg + r) : 0);
+        stg_base()[sl] = make_int4(lb + il - l, cb + ic - c, 0, 0);
+        stg_dpiv()[sl] = P.NA ? __ldcg(P.dpiv + r) : make_float4(0.f, 0.f, 0.f, 0.f);
+      }
+      ib += __shfl_sync(0xffffffffu, ia, 31);
+      lb += __shfl_sync(0xffffffffu, il, 31);
+      cb += __shfl_sync(0xffffffffu, ic, 31);
+    }
+  }
+  __syncthreads();
+  const float w = (float)P.wg;
+  for (int sl = wib; sl < n; sl += kSolveWarps) {
+    const int4 nd = stg_node()[sl];
+    const int r = nd.x;
+    const int b0 = __ldg(P.item_off + r);
+    const int j = __ldg(P.free_ids + r);
+    const float gj[3] = {__ldg(P.node_pos + 3 * (size_t)j), __ldg(P.node_pos + 3 * (size_t)j + 1),
+                         __ldg(P.node_pos + 3 * (size_t)j + 2)};
+    const int4 bs = stg_base()[sl];
+    int lb = bs.x, cb = bs.y;
+    for (int q0 = 0; q0 < nd.z; q0 += 32) {
+      const int q = q0 + lane;
+      const bool has = q < nd.z;
+      int4 m = has ? __ldg(P.items + b0 + q) : make_int4(ITEM_STATIC, -1, 0, 0);
+      const int kind = m.x & 15;
+      float4 ax = make_float4(0.f, 0.f, 0.f, 0.f);
+      float4 yd = make_float4(0.f, 0.f, 0.f, 0.f);
+      int f0 = 0, len = 0;
+      if (kind == ITEM_OUT || kind == ITEM_IN) {
+        // the geometry fetch_item forms: sgn (g_k - g_j), w * scale
+        const float sgn = kind == ITEM_OUT ? 1.f : -1.f;
+        ax = make_float4(sgn * (__ldg(P.node_pos + 3 * (size_t)m.z) - gj[0]),
+                         sgn * (__ldg(P.node_pos + 3 * (size_t)m.z + 1) - gj[1]),
+                         sgn * (__ldg(P.node_pos + 3 * (size_t)m.z + 2) - gj[2]), w * __int_as_float(m.w));
+        if (res && P.NA && m.y >= 0) yd = __ldcg(P.dpiv + m.y);
+      } else if (kind == ITEM_CON) {
+        ax = __ldcg(P.mem_geo + m.y);
+        if (P.NA) {
+          f0 = __ldg(P.gca_off + m.z);
+          len = __ldg(P.gca_off + m.z + 1) - f0;
+        }
+      }
+      const int il = scan(len);
+      const int ic = scan(kind == ITEM_CON && P.NA ? 1 : 0);
+      if (kind == ITEM_CON && P.NA) {
+        const int off = lb + il - len;
+        for (int e = 0; e < len; ++e) {
+          stg_lv()[off + e] = __ldcg(P.gcv + f0 + e);
+          stg_la()[off + e] = __ldg(P.gca + f0 + e);
+        }
+        if (res) {
+          const int ci = cb + ic - 1;
+          stg_cg()[ci] = m.z;
+          m.x = ITEM_CON | (ci << 4);
+        }
+        m.y = off;
+        m.w = len;
+      }
+      if (has) {
+        stg_item()[nd.y + q] = m;
+        stg_geo()[nd.y + q] = ax;
+        if (res) stg_ydp()[nd.y + q] = yd;
+      }
+      lb += __shfl_sync(0xffffffffu, il, 31);
+      cb += __shfl_sync(0xffffffffu, ic, 31);
+    }
+  }
+  __syncthreads();
 }
 
 }  // namespace arap

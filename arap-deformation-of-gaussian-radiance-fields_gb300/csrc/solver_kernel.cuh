@@ -277,6 +277,7 @@ __device__ __forceinline__ void solve_body(const SolveParams& P, int bid, int nb
     P.xf[e] = (float)v;
   }
   const bool coarse = P.NA > 0 && P.mode == 0;
+  const bool resident = coarse && P.resident != 0;
   if (coarse) {
     for (int r = gt; r < F; r += nt) {
       const int j = P.free_ids[r];
@@ -314,6 +315,7 @@ __device__ __forceinline__ void solve_body(const SolveParams& P, int bid, int nb
   if (gt == 0)
     for (int q = ST_T_W_SPMV; q <= ST_T_W_CSOLVE; ++q) P.stats[q] = 0.0;
   if (!gs.sync()) return;
+  stage_build(P, bid, nbk);
   // diagonal-block share of every constraint item (fixed for this solve): the
   // group's anchors equal to the item's node, summed into the first item of
   // the node's run of that group
@@ -371,7 +373,8 @@ __device__ __forceinline__ void solve_body(const SolveParams& P, int bid, int nb
     }
     if (!gs.sync()) return;
     for (int ws = wib; ws * nbk + bid < F; ws += kSolveWarps) {
-      const int r = __ldg(P.order + ws * nbk + bid);
+      const bool stg = ws < s_stg.n;
+      const int r = stg ? stg_node()[ws].x : __ldg(P.order + ws * nbk + bid);
       RT acc[12];
       float Q[10];
       double en;
@@ -387,13 +390,16 @@ __device__ __forceinline__ void solve_body(const SolveParams& P, int bid, int nb
         }
         continue;
       }
-      build_dinv(P, r, Q);
+      if (stg)
+        build_dinv<true>(P, r, ws, Q);
+      else
+        build_dinv<false>(P, r, 0, Q);
       if (coarse) coarse_rot_node(P, r, P.rotagg + (it & 1) * 81 * P.NA);
       float gc = 0.f;
 #pragma unroll
       for (int i = 0; i < 12; ++i)
         if (i == lane) gc = -(float)acc[i];
-      const float zc = apply_dinv(P, r, gc);
+      const float zc = stg ? apply_dinv<true>(P, r, ws, gc) : apply_dinv<false>(P, r, 0, gc);
       if (coarse) coarse_restrict(P, r, gc, P.rc);
       if (lane < 12) {
         const size_t o = 12 * (size_t)r + lane;
@@ -401,6 +407,12 @@ __device__ __forceinline__ void solve_body(const SolveParams& P, int bid, int nb
         P.z[o] = zc;
         P.h[o] = 0.f;
         red[2] += (double)gc * (double)gc;
+        if (resident && stg) {
+          stg_vec(ws, RV_R)[lane] = gc;
+          stg_vec(ws, RV_UF)[lane] = zc;
+          stg_vec(ws, RV_H)[lane] = 0.f;
+          stg_xf(ws)[lane] = __ldcg(P.xf + o);
+        }
       }
     }
     for (int e = gt; e < F * 12; e += nt) {
@@ -459,10 +471,15 @@ __device__ __forceinline__ void solve_body(const SolveParams& P, int bid, int nb
       for (int hs0 = 2 * wib; hs0 * nbk + bid < F; hs0 += 2 * kSolveWarps) {
         const int oi = (hs0 + half) * nbk + bid;
         const bool valid = oi < F;
-        const int r = valid ? __ldg(P.order + oi) : 0;
+        // staged or not, for both halves of the warp alike
+        const bool stg = hs0 < s_stg.n;
+        const int r = valid ? (stg ? stg_node()[hs0 + half].x : __ldg(P.order + oi)) : 0;
         const float rv = (valid && l16 < 12) ? __ldcg(P.r + 12 * (size_t)r + l16) : 0.f;
         float acc[12], uj[12];
-        spmv_node(P, r, valid, acc, uj);
+        if (stg)
+          spmv_node_stg(P, hs0 + half, r, valid, acc, uj);
+        else
+          spmv_node(P, r, valid, acc, uj);
         if (valid && l16 < 12) {
           float uc = 0.f, wv = 0.f;
 #pragma unroll
@@ -483,6 +500,62 @@ __device__ __forceinline__ void solve_body(const SolveParams& P, int bid, int nb
       return gs.reduce_f<3>(f3, s3);
     };
     int cur = 0;  // rc buffer holding P^T r of the current residual
+    int pi = 0;
+    if (resident) {
+      // ---- two-level PCG with the CTA's nodes resident in shared memory:
+      //   (1) vector update of own nodes (no global loads); plain barrier
+      //   (2) zc = Cinv P^T r, w_con J_g u_f, w_f = (J^T J)_reg u_f; plain barrier
+      //   (3) the rest of w from shared memory; gamma, delta, r.r in one reduction
+      const int ns = s_stg.n;
+      auto phase2 = [&]() -> bool {
+        work_begin();
+        for (int hs0 = 2 * wib; hs0 < ns; hs0 += 2 * kSolveWarps) res_products_f(P, hs0 + half, hs0 + half < ns);
+        coarse_solve(P, gs, P.rc + cur * P.NC, P.rc + (cur ^ 1) * P.NC, coarse_ok, s_scratch);
+        work_end(2);
+        return gs.sync();
+      };
+      auto phase3 = [&](double (&s3)[3]) -> bool {
+        float f3[3] = {0.f, 0.f, 0.f};
+        work_begin();
+        for (int e = threadIdx.x; e < P.NC; e += blockDim.x) s_zc[e] = __ldcg(P.zc + e);
+        for (int e = threadIdx.x; e < s_stg.ncon; e += blockDim.x) stg_cuz()[e] = __ldcg(P.uzg + stg_cg()[e]);
+        __syncthreads();
+        for (int hs0 = 2 * wib; hs0 < ns; hs0 += 2 * kSolveWarps) res_products(P, hs0 + half, hs0 + half < ns, f3);
+        work_end(0);
+        return gs.reduce_f<3>(f3, s3);
+      };
+      if (!phase2()) return;
+      double s3[3];
+      if (!phase3(s3)) return;
+      double gam = s3[0];
+      rr = s3[2];
+      double alpha_d = s3[1] > 0.0 ? gam / s3[1] : 0.0;
+      float beta = 0.f;
+      bool go = rr > tol2 && gam > 0.0 && s3[1] > 0.0;
+      while (go && pi < P.pcg_max) {
+        const float alpha = (float)alpha_d;
+        const bool first = pi == 0;
+        double* rc_next = P.rc + (cur ^ 1) * P.NC;
+        work_begin();
+        for (int hs0 = 2 * wib; hs0 < ns; hs0 += 2 * kSolveWarps)
+          res_update(P, hs0 + half, hs0 + half < ns, alpha, beta, first, rc_next);
+        work_end(1);
+        if (!gs.sync()) return;
+        ++pi;
+        cur ^= 1;
+        if (!phase2()) return;
+        if (!phase3(s3)) return;
+        rr = s3[2];
+        if (rr <= tol2 || pi >= P.pcg_max) break;
+        const double gam_new = s3[0];
+        const double bd = gam_new / gam;
+        const double den = s3[1] - bd * gam_new / alpha_d;
+        if (!(gam_new > 0.0) || !(den > 0.0)) break;
+        beta = (float)bd;
+        alpha_d = gam_new / den;
+        gam = gam_new;
+      }
+    } else {
     if (coarse) {
       work_begin();
       coarse_solve(P, gs, P.rc, P.rc + P.NC, coarse_ok, s_scratch);
@@ -495,7 +568,6 @@ __device__ __forceinline__ void solve_body(const SolveParams& P, int bid, int nb
     rr = s3[2];
     double alpha_d = s3[1] > 0.0 ? gam / s3[1] : 0.0;
     float beta = 0.f;
-    int pi = 0;
     bool go = rr > tol2 && gam > 0.0 && s3[1] > 0.0;
     while (go && pi < P.pcg_max) {
       // p = u + beta p, s = w + beta s (s = (J^T J) p), h += alpha p,
@@ -507,7 +579,8 @@ __device__ __forceinline__ void solve_body(const SolveParams& P, int bid, int nb
       for (int hs0 = 2 * wib; hs0 * nbk + bid < F; hs0 += 2 * kSolveWarps) {
         const int oi = (hs0 + half) * nbk + bid;
         const bool valid = oi < F;
-        const int r = valid ? __ldg(P.order + oi) : 0;
+        const bool stg = hs0 < s_stg.n;
+        const int r = valid ? (stg ? stg_node()[hs0 + half].x : __ldg(P.order + oi)) : 0;
         float rv = 0.f;
         if (valid && l16 < 12) {
           const size_t o = 12 * (size_t)r + l16;
@@ -520,8 +593,13 @@ __device__ __forceinline__ void solve_body(const SolveParams& P, int bid, int nb
           rv = fmaf(-alpha, sn, __ldcg(P.r + o));
           P.r[o] = rv;
         }
-        const float zv = apply_dinv_h(P, r, valid, rv);
-        if (coarse) coarse_restrict_h(P, r, valid, rv, rc_next);
+        const float zv = stg ? apply_dinv_h_stg(hs0 + half, valid, rv) : apply_dinv_h(P, r, valid, rv);
+        if (coarse) {
+          if (stg)
+            coarse_restrict_h_stg(hs0 + half, valid, rv, rc_next);
+          else
+            coarse_restrict_h(P, r, valid, rv, rc_next);
+        }
         if (valid && l16 < 12) P.z[12 * (size_t)r + l16] = zv;
       }
       work_end(1);
@@ -544,6 +622,7 @@ __device__ __forceinline__ void solve_body(const SolveParams& P, int bid, int nb
       beta = (float)bd;
       alpha_d = gam_new / den;
       gam = gam_new;
+    }
     }
     // both restriction buffers start the next gradient pass at zero
     if (coarse)
