@@ -79,6 +79,51 @@ __device__ __forceinline__ T warp_sum(T v) {
   return v;
 }
 
+// Float-float addition (hi, lo) += (bh, bl): TwoSum of the high parts
+// (Knuth, TAOCP vol. 2, 4.2.2) plus the low parts, renormalised.  No
+// multiplications, so no contraction into FMA can change it.
+__device__ __forceinline__ void dd_add(float& hi, float& lo, float bh, float bl) {
+  const float s = hi + bh;
+  const float bb = s - hi;
+  float err = (hi - (s - bb)) + (bh - bb);
+  err += lo + bl;
+  hi = s + err;
+  lo = err - (hi - s);
+}
+
+// Float-float products and quotients (Dekker's method with an FMA for the
+// exact product error), for the few scalars that must not lose the precision
+// the float-float sums keep.
+__device__ __forceinline__ float2 dd_mul(float2 a, float2 b) {
+  const float p = a.x * b.x;
+  float e = fmaf(a.x, b.x, -p);
+  e = fmaf(a.x, b.y, fmaf(a.y, b.x, e));
+  const float hi = p + e;
+  return make_float2(hi, e - (hi - p));
+}
+__device__ __forceinline__ float2 dd_sub(float2 a, float2 b) {
+  float hi = a.x, lo = a.y;
+  dd_add(hi, lo, -b.x, -b.y);
+  return make_float2(hi, lo);
+}
+__device__ __forceinline__ float2 dd_div(float2 a, float2 b) {
+  const float q1 = a.x / b.x;
+  const float2 r = dd_sub(a, dd_mul(b, make_float2(q1, 0.f)));
+  const float q2 = r.x / b.x;
+  const float hi = q1 + q2;
+  return make_float2(hi, q2 - (hi - q1));
+}
+
+// Butterfly float-float sum over the warp; lane 0's result is the one used.
+__device__ __forceinline__ void dd_warp_sum(float& hi, float& lo) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const float h2 = __shfl_xor_sync(0xffffffffu, hi, o);
+    const float l2 = __shfl_xor_sync(0xffffffffu, lo, o);
+    dd_add(hi, lo, h2, l2);
+  }
+}
+
 // Per-thread handle of the grid barrier over a group of nb co-resident CTAs
 // (the whole grid, or one instance's share of a batched launch); bid is this
 // CTA's index in the group.  Every thread of every CTA of the group must make
@@ -119,13 +164,63 @@ struct GridSync {
     return reduce_warp_sums<NSLOT>(v);
   }
 
-  // As reduce, for float contributions: the warp sums are taken in float
-  // (a warp holds a few dozen terms), everything above the warp in FP64.
+  // As reduce, for float contributions, in FP32 only (FP64 arithmetic has
+  // ~64-cycle latency on this part): float warp sums, then float-float
+  // (hi, lo) sums above the warp (Knuth's TwoSum), so the grid-wide sum keeps
+  // about twice float's precision; returned as float-float pairs.  Every CTA
+  // adds the same terms in the same order, so all get the same bits.
   template <int NSLOT>
-  __device__ bool reduce_f(const float (&vf)[NSLOT], double (&out)[NSLOT]) {
+  __device__ bool reduce_f(const float (&vf)[NSLOT], float2 (&out)[NSLOT]) {
+    static_assert(NSLOT >= 1 && NSLOT <= kReduceSlots, "slots");
+    __shared__ float s_redf[32][NSLOT];
+    __shared__ float2 s_outf[NSLOT];
+    __shared__ int s_okf;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const unsigned int e = epoch++;
+    float2* buf = reinterpret_cast<float2*>(partials + (size_t)(e & 1u) * kReduceSlots * nb);
 #pragma unroll
-    for (int s = 0; s < NSLOT; ++s) out[s] = (double)warp_sum(vf[s]);
-    return reduce_warp_sums<NSLOT>(out);
+    for (int s = 0; s < NSLOT; ++s) {
+      const float ws = warp_sum(vf[s]);
+      if (lane == 0) s_redf[w][s] = ws;
+    }
+    __syncthreads();
+    if (w == 0) {
+      const int nw = blockDim.x >> 5;
+#pragma unroll
+      for (int s = 0; s < NSLOT; ++s) {
+        float hi = lane < nw ? s_redf[lane][s] : 0.f, lo = 0.f;
+        dd_warp_sum(hi, lo);
+        if (lane == 0) buf[(size_t)bid * kReduceSlots + s] = make_float2(hi, lo);
+      }
+      int ok = 1;
+      if (lane == 0) ok = arrive_and_wait(e);
+      __syncwarp();
+      ok = __shfl_sync(0xffffffffu, ok, 0);
+      if (ok) {
+        constexpr int kQ = kMaxGridCtas / 32;
+        float2 t[kQ][NSLOT];
+#pragma unroll
+        for (int q = 0; q < kQ; ++q) {
+          const unsigned int c = lane + 32u * q;
+#pragma unroll
+          for (int s = 0; s < NSLOT; ++s)
+            t[q][s] = c < nb ? __ldcg(buf + (size_t)c * kReduceSlots + s) : make_float2(0.f, 0.f);
+        }
+#pragma unroll
+        for (int s = 0; s < NSLOT; ++s) {
+          float hi = 0.f, lo = 0.f;
+#pragma unroll
+          for (int q = 0; q < kQ; ++q) dd_add(hi, lo, t[q][s].x, t[q][s].y);
+          dd_warp_sum(hi, lo);
+          if (lane == 0) s_outf[s] = make_float2(hi, lo);  // lane 0's association order, as in every CTA
+        }
+      }
+      if (lane == 0) s_okf = ok;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int s = 0; s < NSLOT; ++s) out[s] = s_outf[s];
+    return s_okf != 0;
   }
 
   // v[] holds the warp's sums (valid in lane 0) on entry.

@@ -510,6 +510,9 @@ extern "C" int arap_solver_create(arap_solver** out, int n, int k, const int32_t
   P.wr = std::sqrt((double)cfg.w_rot);
   P.wg = std::sqrt((double)cfg.w_reg);
   P.wc = std::sqrt((double)cfg.w_con);
+  P.wrf = (float)P.wr;
+  P.wgf = (float)P.wg;
+  P.wcf = (float)P.wc;
   P.wf = wf;
   P.max_iters = cfg.max_iters;
   P.early_exit = cfg.early_exit;

@@ -63,6 +63,7 @@ struct SolveParams {
   const double* x_in;        // grad-only mode: evaluation point
   double* grad_out;          // grad-only mode: J^T f
   double wr, wg, wc;         // square roots of w_rot, w_reg, w_con (Deform.hpp:452-454)
+  float wrf, wgf, wcf;       // the same rounded to float (FP64 conversions are slow on this part)
   float wf;                  // weighting factor
   const int32_t* order;      // [F] processing order of the free nodes (cost-balanced)
   int max_iters, early_exit, pcg_max;

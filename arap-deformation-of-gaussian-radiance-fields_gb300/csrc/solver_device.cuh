@@ -215,7 +215,7 @@ __device__ void con_ju(const SolveParams& P, int g, float (&u)[3]) {
         u[c] = fmaf(geo.x, fmaf(geo.y, pl[c], fmaf(geo.z, pl[3 + c], fmaf(geo.w, pl[6 + c], pl[9 + c]))), u[c]);
     }
   }
-  const float wcf = (float)P.wc;
+  const float wcf = P.wcf;
   u[0] *= wcf;
   u[1] *= wcf;
   u[2] *= wcf;
@@ -229,7 +229,7 @@ __device__ void con_ju_coarse(const SolveParams& P, int g, float (&u)[3]) {
   u[0] = uz.x;
   u[1] = uz.y;
   u[2] = uz.z;
-  const float wcf = (float)P.wc;
+  const float wcf = P.wcf;
   const int f0 = __ldg(P.gca_off + g), f1 = __ldg(P.gca_off + g + 1);
   for (int f = f0; f < f1; ++f) {
     const float4 V = __ldcg(P.gcv + f);
@@ -249,7 +249,7 @@ __device__ __forceinline__ void con_ju_list(const SolveParams& P, int g, int off
   u[0] = uz.x;
   u[1] = uz.y;
   u[2] = uz.z;
-  const float wcf = (float)P.wc;
+  const float wcf = P.wcf;
   for (int f = off; f < off + len; ++f) {
     const float4 V = stg_lv()[f];
     const float4* c4 = reinterpret_cast<const float4*>(s_zc + 12 * stg_la()[f]);
@@ -277,7 +277,7 @@ __device__ __forceinline__ void con_jz_group(const SolveParams& P, int g) {
     for (int c = 0; c < 3; ++c)
       u[c] = fmaf(geo.x, fmaf(geo.y, zl[c], fmaf(geo.z, zl[3 + c], fmaf(geo.w, zl[6 + c], zl[9 + c]))), u[c]);
   }
-  const float wcf = (float)P.wc;
+  const float wcf = P.wcf;
 #pragma unroll
   for (int c = 0; c < 3; ++c) u[c] = wcf * warp_sum(u[c]);
   if (lane == 0) P.uzg[g] = make_float4(u[0], u[1], u[2], 0.f);
@@ -347,7 +347,7 @@ __device__ void residual_node(const SolveParams& P, int r, RT scale, RT (&acc)[1
           for (int rr = 0; rr < 3; ++rr) acc[3 * c + rr] += ws * RT(dJ[c]) * f[rr];
 #pragma unroll
         for (int rr = 0; rr < 3; ++rr) acc[9 + rr] += w * f[rr];
-        const float wgf = (float)P.wg;
+        const float wgf = P.wgf;
         const float wsf = wgf * s;
         q_add(Q, wsf * dJ[0], wsf * dJ[1], wsf * dJ[2], wgf);
       }
@@ -391,7 +391,7 @@ __device__ void residual_node(const SolveParams& P, int r, RT scale, RT (&acc)[1
         // group's anchors equal to j (zero for all but the first item of a run)
         const float4 cq = __ldcg(P.item_cq + it);
         if (cq.w != 0.f) {
-          const float wcf = (float)P.wc;
+          const float wcf = P.wcf;
           q_add(Q, wcf * cq.x, wcf * cq.y, wcf * cq.z, wcf * cq.w);
         }
       }
@@ -502,7 +502,7 @@ __device__ __forceinline__ void apply_item(const SolveParams& P, const CouplingD
 #pragma unroll
     for (int c = 0; c < 3; ++c) acc[9 + c] = fmaf(w * w, pj[9 + c], acc[9 + c]);
   } else {
-    const float wa = (float)P.wc * D.aux.x;
+    const float wa = P.wcf * D.aux.x;
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
       acc[c] = fmaf(wa * D.aux.y, D.v[c], acc[c]);
@@ -529,7 +529,7 @@ static __device__ __noinline__ void spmv_node(const SolveParams& P, int r, bool 
   const float gj[3] = {__ldg(P.node_pos + 3 * (size_t)j), __ldg(P.node_pos + 3 * (size_t)j + 1),
                        __ldg(P.node_pos + 3 * (size_t)j + 2)};
   load_u(P, r, P.NA ? __ldg(P.agg + r) : 0, pj);
-  const float w = (float)P.wg;
+  const float w = P.wgf;
   const int b0 = __ldg(P.item_off + r), b1 = __ldg(P.item_off + r + 1);
   // two items per lane per round: both items' loads are issued before either
   // is used, so a round costs one round trip
@@ -553,7 +553,7 @@ static __device__ __noinline__ void spmv_node(const SolveParams& P, int r, bool 
     const float* p0 = pj;
     const float* p1 = pj + 3;
     const float* p2 = pj + 6;
-    const float wr = (float)P.wr;
+    const float wr = P.wrf;
     auto dot = [](const float* a3, const float* b3) { return a3[0] * b3[0] + a3[1] * b3[1] + a3[2] * b3[2]; };
     const float u0 = wr * (dot(c1, p0) + dot(c0, p1));
     const float u1 = wr * (dot(c2, p0) + dot(c0, p2));
@@ -656,7 +656,7 @@ __device__ __forceinline__ void item_finish(const SolveParams& P, StagedItem& S)
     D.v[1] = t3[1];
     D.v[2] = t3[2];
   } else if (D.kind == ITEM_CON) {
-    const float wcf = (float)P.wc;
+    const float wcf = P.wcf;
     for (int f = S.a; f < S.a + S.len; ++f) {
       const float4 V = stg_lv()[f];
       const float4* c4 = reinterpret_cast<const float4*>(s_zc + 12 * stg_la()[f]);
@@ -690,7 +690,7 @@ __device__ __forceinline__ void spmv_node_stg(const SolveParams& P, int s, int r
     if (lane < 9) xr = __ldcg(P.xf + 12 * (size_t)r + lane);
     ld12cg(P.z, r, pj);
     bool own = !P.NA;  // own coarse part added
-    const float w = (float)P.wg;
+    const float w = P.wgf;
     for (int q = lane; q < nd.z; q += 32) {
       const bool hasB = q + 16 < nd.z;
       StagedItem A, B;
@@ -720,7 +720,7 @@ __device__ __forceinline__ void spmv_node_stg(const SolveParams& P, int s, int r
     const float* p0 = pj;
     const float* p1 = pj + 3;
     const float* p2 = pj + 6;
-    const float wr = (float)P.wr;
+    const float wr = P.wrf;
     auto dot = [](const float* a3, const float* b3) { return a3[0] * b3[0] + a3[1] * b3[1] + a3[2] * b3[2]; };
     const float u0 = wr * (dot(c1, p0) + dot(c0, p1));
     const float u1 = wr * (dot(c2, p0) + dot(c0, p2));
@@ -756,7 +756,7 @@ __device__ void build_dinv(const SolveParams& P, int r, int slot, const float (&
 #pragma unroll
   for (int i = 0; i < 9; ++i) X[i] = __ldcg(P.xf + 12 * (size_t)r + i);
   // rotation rows: [c1|c0|0], [c2|0|c0], [0|c2|c1], [2c0|0|0], [0|2c1|0], [0|0|2c2]
-  const float wr = (float)P.wr;
+  const float wr = P.wrf;
   float J[6][9];
 #pragma unroll
   for (int a = 0; a < 6; ++a)
@@ -915,7 +915,7 @@ __device__ void coarse_rows_node(const SolveParams& P, int r) {
   const int lane = threadIdx.x & 31;
   const int j = __ldg(P.free_ids + r);
   const int a = __ldg(P.agg + r);
-  const float w = (float)P.wg;
+  const float w = P.wgf;
   const float gj[3] = {__ldg(P.node_pos + 3 * (size_t)j), __ldg(P.node_pos + 3 * (size_t)j + 1),
                        __ldg(P.node_pos + 3 * (size_t)j + 2)};
   const int b0 = __ldg(P.item_off + r), b1 = __ldg(P.item_off + r + 1);
@@ -957,7 +957,7 @@ __device__ void coarse_rows_group(const SolveParams& P, int g) {
   int ids[kMaxAgg];
   float vv[kMaxAgg][4];
   int na = 0;
-  const float wc = (float)P.wc;
+  const float wc = P.wcf;
   const int s0 = __ldg(P.grp_off + g), s1 = __ldg(P.grp_off + g + 1);
   for (int s = s0; s < s1; ++s) {
     const int c = __ldg(P.grp_member + s);
@@ -1008,7 +1008,7 @@ __device__ __forceinline__ void coarse_rot_node(const SolveParams& P, int rr, do
   float X[9];
 #pragma unroll
   for (int i = 0; i < 9; ++i) X[i] = __ldcg(P.xf + 12 * (size_t)rr + i);
-  const float wr = (float)P.wr;
+  const float wr = P.wrf;
   float J[6][9];
 #pragma unroll
   for (int a = 0; a < 6; ++a)
@@ -1161,7 +1161,7 @@ static __device__ __noinline__ void res_products_f(const SolveParams& P, int s, 
     const float4 a = u4[0], b = u4[1], c = u4[2];
     pj[0] = a.x; pj[1] = a.y; pj[2] = a.z; pj[3] = a.w; pj[4] = b.x; pj[5] = b.y;
     pj[6] = b.z; pj[7] = b.w; pj[8] = c.x; pj[9] = c.y; pj[10] = c.z; pj[11] = c.w;
-    const float w = (float)P.wg;
+    const float w = P.wgf;
     for (int q = lane; q < nd.z; q += 32) {
       const bool hasB = q + 16 < nd.z;
       CouplingData A, B;
@@ -1220,8 +1220,8 @@ static __device__ __noinline__ void res_products(const SolveParams& P, int s, bo
     const int4 nd = stg_node()[s];
     if (lane < 9) xr = stg_xf(s)[lane];
     coarse_prolong_dp(stg_dpiv()[s], nd.w, y);
-    const float w = (float)P.wg;
-    const float wcf = (float)P.wc;
+    const float w = P.wgf;
+    const float wcf = P.wcf;
     for (int q = lane; q < nd.z; q += 16) {
       const int i = nd.y + q;
       CouplingData D;
@@ -1277,7 +1277,7 @@ static __device__ __noinline__ void res_products(const SolveParams& P, int s, bo
     const float* p0 = uj;
     const float* p1 = uj + 3;
     const float* p2 = uj + 6;
-    const float wr = (float)P.wr;
+    const float wr = P.wrf;
     auto dot = [](const float* a3, const float* b3) { return a3[0] * b3[0] + a3[1] * b3[1] + a3[2] * b3[2]; };
     const float u0 = wr * (dot(c1, p0) + dot(c0, p1));
     const float u1 = wr * (dot(c2, p0) + dot(c0, p2));
@@ -1420,7 +1420,7 @@ __device__ void stage_build(const SolveParams& P, int bid, int nbk) {
     }
   }
   __syncthreads();
-  const float w = (float)P.wg;
+  const float w = P.wgf;
   for (int sl = wib; sl < n; sl += kSolveWarps) {
     const int4 nd = stg_node()[sl];
     const int r = nd.x;

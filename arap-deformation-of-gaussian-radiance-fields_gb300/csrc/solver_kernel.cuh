@@ -438,7 +438,12 @@ __device__ __forceinline__ void solve_body(const SolveParams& P, int bid, int nb
     //   (3) u = u_f + P zc, w = (J^T J) u; gamma = r.u, delta = w.u, r.r
     //   beta = gamma / gamma_old, alpha = gamma / (delta - beta gamma / alpha_old)
     const double rr0 = red[2];
-    double rr = rr0;
+    // the PCG scalars are float-float (hi, lo) pairs: its sums are
+    // float-float reductions of float terms, and FP64 arithmetic (~64-cycle
+    // latency, divisions many times that) would sit on every iteration's
+    // critical path.  The recurrence den = delta - beta gamma / alpha cancels
+    // near convergence, which plain float does not survive.
+    float rr = (float)rr0;
     int coarse_ok = 0;
     if (coarse) {
       // coarse matrix at this x: fixed kernels + current orthogonality blocks
@@ -454,12 +459,12 @@ __device__ __forceinline__ void solve_body(const SolveParams& P, int bid, int nb
       if (!coarse_ok && gt == 0) raise_status(ARAP_ENONFINITE);
       lap(2);
     }
-    const double tol2 = (double)P.pcg_tol * (double)P.pcg_tol * rr0;
+    const float tol2 = (float)((double)P.pcg_tol * (double)P.pcg_tol * rr0);
     const int half = lane >> 4, l16 = lane & 15;
     // products: u = u_f + P zc (formed on the fly for every node a product
     // touches), w = (J^T J) u, and gamma = r.u, delta = w.u, r.r in one
     // reduction
-    auto products = [&](double (&s3)[3]) -> bool {
+    auto products = [&](float2 (&s3)[3]) -> bool {
       float f3[3] = {0.f, 0.f, 0.f};
       work_begin();
       // the coarse correction zc (12 floats per aggregate, shared by its
@@ -514,7 +519,7 @@ __device__ __forceinline__ void solve_body(const SolveParams& P, int bid, int nb
         work_end(2);
         return gs.sync();
       };
-      auto phase3 = [&](double (&s3)[3]) -> bool {
+      auto phase3 = [&](float2 (&s3)[3]) -> bool {
         float f3[3] = {0.f, 0.f, 0.f};
         work_begin();
         for (int e = threadIdx.x; e < P.NC; e += blockDim.x) s_zc[e] = __ldcg(P.zc + e);
@@ -525,15 +530,15 @@ __device__ __forceinline__ void solve_body(const SolveParams& P, int bid, int nb
         return gs.reduce_f<3>(f3, s3);
       };
       if (!phase2()) return;
-      double s3[3];
+      float2 s3[3];
       if (!phase3(s3)) return;
-      double gam = s3[0];
-      rr = s3[2];
-      double alpha_d = s3[1] > 0.0 ? gam / s3[1] : 0.0;
+      float2 gam = s3[0];
+      rr = s3[2].x;
+      bool go = rr > tol2 && gam.x > 0.f && s3[1].x > 0.f;
+      float2 alpha_d = go ? dd_div(gam, s3[1]) : make_float2(0.f, 0.f);
       float beta = 0.f;
-      bool go = rr > tol2 && gam > 0.0 && s3[1] > 0.0;
       while (go && pi < P.pcg_max) {
-        const float alpha = (float)alpha_d;
+        const float alpha = alpha_d.x;
         const bool first = pi == 0;
         double* rc_next = P.rc + (cur ^ 1) * P.NC;
         work_begin();
@@ -545,14 +550,15 @@ __device__ __forceinline__ void solve_body(const SolveParams& P, int bid, int nb
         cur ^= 1;
         if (!phase2()) return;
         if (!phase3(s3)) return;
-        rr = s3[2];
+        rr = s3[2].x;
         if (rr <= tol2 || pi >= P.pcg_max) break;
-        const double gam_new = s3[0];
-        const double bd = gam_new / gam;
-        const double den = s3[1] - bd * gam_new / alpha_d;
-        if (!(gam_new > 0.0) || !(den > 0.0)) break;
-        beta = (float)bd;
-        alpha_d = gam_new / den;
+        const float2 gam_new = s3[0];
+        if (!(gam_new.x > 0.f)) break;
+        const float2 bd = dd_div(gam_new, gam);
+        const float2 den = dd_sub(s3[1], dd_div(dd_mul(bd, gam_new), alpha_d));
+        if (!(den.x > 0.f)) break;
+        beta = bd.x;
+        alpha_d = dd_div(gam_new, den);
         gam = gam_new;
       }
     } else {
@@ -562,17 +568,17 @@ __device__ __forceinline__ void solve_body(const SolveParams& P, int bid, int nb
       work_end(2);
       if (!gs.sync()) return;
     }
-    double s3[3];
+    float2 s3[3];
     if (!products(s3)) return;
-    double gam = s3[0];
-    rr = s3[2];
-    double alpha_d = s3[1] > 0.0 ? gam / s3[1] : 0.0;
+    float2 gam = s3[0];
+    rr = s3[2].x;
+    bool go = rr > tol2 && gam.x > 0.f && s3[1].x > 0.f;
+    float2 alpha_d = go ? dd_div(gam, s3[1]) : make_float2(0.f, 0.f);
     float beta = 0.f;
-    bool go = rr > tol2 && gam > 0.0 && s3[1] > 0.0;
     while (go && pi < P.pcg_max) {
+      const float alpha = alpha_d.x;
       // p = u + beta p, s = w + beta s (s = (J^T J) p), h += alpha p,
       // r -= alpha s, u_f = Dinv r and its restriction
-      const float alpha = (float)alpha_d;
       const bool first = pi == 0;
       double* rc_next = P.rc + (cur ^ 1) * P.NC;
       work_begin();
@@ -613,14 +619,15 @@ __device__ __forceinline__ void solve_body(const SolveParams& P, int bid, int nb
         if (!gs.sync()) return;
       }
       if (!products(s3)) return;
-      rr = s3[2];
+      rr = s3[2].x;
       if (rr <= tol2 || pi >= P.pcg_max) break;
-      const double gam_new = s3[0];
-      const double bd = gam_new / gam;
-      const double den = s3[1] - bd * gam_new / alpha_d;
-      if (!(gam_new > 0.0) || !(den > 0.0)) break;
-      beta = (float)bd;
-      alpha_d = gam_new / den;
+      const float2 gam_new = s3[0];
+      if (!(gam_new.x > 0.f)) break;
+      const float2 bd = dd_div(gam_new, gam);
+      const float2 den = dd_sub(s3[1], dd_div(dd_mul(bd, gam_new), alpha_d));
+      if (!(den.x > 0.f)) break;
+      beta = bd.x;
+      alpha_d = dd_div(gam_new, den);
       gam = gam_new;
     }
     }
