@@ -81,10 +81,12 @@ int stage_limit(const void* fn) {
 }
 
 // Shared memory the tables of a solve need when its free nodes are dealt
-// round-robin over nbk CTAs (the largest CTA share), uncapped.
-long long stage_need(const std::vector<int32_t>& order, const std::vector<int32_t>& cost, int nbk) {
+// round-robin over nbk CTAs (the largest CTA share), uncapped; with NC > 0
+// each CTA also holds its rows of the coarse inverse.
+long long stage_need(const std::vector<int32_t>& order, const std::vector<int32_t>& cost, int nbk, int NC) {
   if (nbk <= 0) return 0;
   std::vector<long long> per(nbk, 0);
+  for (int b = 0; b < nbk && NC > 0; ++b) per[b] = 4ll * NC * stage_coarse_rows(NC, b, nbk);
   for (size_t p = 0; p < order.size(); ++p) per[p % nbk] += cost[order[p]];
   long long need = 0;
   for (long long v : per) need = std::max(need, v);
@@ -101,14 +103,14 @@ StagePlan plan_stage(const arap_solver* s, int nbk, int limit) {
   StagePlan p;
   if (limit <= 0 || nbk <= 0) return p;
   if (!s->res_cost.empty()) {
-    const long long need = stage_need(s->order_host, s->res_cost, nbk);
+    const long long need = stage_need(s->order_host, s->res_cost, nbk, s->P.NC);
     if (need <= limit) {
       p.bytes = (int)need;
       p.resident = 1;
       return p;
     }
   }
-  p.bytes = (int)std::min<long long>(stage_need(s->order_host, s->stage_cost, nbk), limit);
+  p.bytes = (int)std::min<long long>(stage_need(s->order_host, s->stage_cost, nbk, 0), limit);
   return p;
 }
 
@@ -365,18 +367,31 @@ extern "C" int arap_solver_create(arap_solver** out, int n, int k, const int32_t
   }
   // coarse-list entries and constraint items of each node, and the shared
   // memory of its tables
-  std::vector<int2> con_info(F, make_int2(0, 0));
+  // and, with a coarse level, the distinct aggregates coupled to it (its own,
+  // its regularisation neighbours', its constraint groups')
+  std::vector<int4> con_info(F, make_int4(0, 0, 0, 0));
   std::vector<int32_t> stage_cost(F, 0), res_cost;
   if (NA > 0) res_cost.assign(F, 0);
+  std::vector<int32_t> coupled;
   for (int r = 0; r < F; ++r) {
     const int items_r = item_off[r + 1] - item_off[r];
-    for (int t = item_off[r]; t < item_off[r + 1]; ++t)
-      if (NA > 0 && (item_flat[t].x & 15) == ITEM_CON) {
-        con_info[r].x += gca_off[item_flat[t].z + 1] - gca_off[item_flat[t].z];
+    coupled.clear();
+    if (NA > 0) coupled.push_back(agg[r]);
+    for (int t = item_off[r]; t < item_off[r + 1]; ++t) {
+      if (NA == 0) continue;
+      const int4 m = item_flat[t];
+      const int kind = m.x & 15;
+      if ((kind == ITEM_OUT || kind == ITEM_IN) && m.y >= 0) coupled.push_back(agg[m.y]);
+      if (kind == ITEM_CON) {
+        con_info[r].x += gca_off[m.z + 1] - gca_off[m.z];
         con_info[r].y += 1;
+        for (int f = gca_off[m.z]; f < gca_off[m.z + 1]; ++f) coupled.push_back(gca[f]);
       }
-    stage_cost[r] = stage_node_bytes(items_r, con_info[r].x, con_info[r].y, false);
-    if (NA > 0) res_cost[r] = stage_node_bytes(items_r, con_info[r].x, con_info[r].y, true);
+    }
+    std::sort(coupled.begin(), coupled.end());
+    con_info[r].z = (int)(std::unique(coupled.begin(), coupled.end()) - coupled.begin());
+    stage_cost[r] = stage_node_bytes(items_r, con_info[r].x, con_info[r].y, con_info[r].z, false);
+    if (NA > 0) res_cost[r] = stage_node_bytes(items_r, con_info[r].x, con_info[r].y, con_info[r].z, true);
   }
 
   auto* s = new (std::nothrow) arap_solver();
@@ -444,7 +459,7 @@ extern "C" int arap_solver_create(arap_solver** out, int n, int k, const int32_t
     P.gca = cv.take<int32_t>(gca.size());
     P.gcv = cv.take<float4>(gca.size());
     P.uzg = cv.take<float4>(NA ? G : 0);
-    P.con_info = cv.take<int2>(F);
+    P.con_info = cv.take<int4>(F);
     P.partials = cv.take<double>((size_t)2 * kReduceSlots * grid);
     P.stats = cv.take<double>(kStatSlots);
     P.bar = cv.take<GridBarrier>(1);
@@ -486,7 +501,7 @@ extern "C" int arap_solver_create(arap_solver** out, int n, int k, const int32_t
     for (int i = 0; i < F; ++i) order[i] = cost[i].second;
   }
   e = e ? e : up(P.order, order.data(), order.size() * 4);
-  e = e ? e : up(P.con_info, con_info.data(), con_info.size() * sizeof(int2));
+  e = e ? e : up(P.con_info, con_info.data(), con_info.size() * sizeof(int4));
   if (NA > 0) {
     e = e ? e : up(P.mem_agg, mem_agg.data(), mem_agg.size() * 4);
     e = e ? e : up(P.agg, agg.data(), agg.size() * 4);

@@ -11,6 +11,7 @@ namespace arap {
 
 constexpr int kSolveThreads = 512;
 constexpr int kSolveWarps = kSolveThreads / 32;
+constexpr int kRcPerThread = (kMaxCoarse + kSolveThreads - 1) / kSolveThreads;
 
 // Mutable per-node vectors are read through L2 (ld.global.cg): other CTAs
 // write them between grid barriers, and L1 is not coherent across SMs.
@@ -41,7 +42,11 @@ __shared__ __align__(16) float s_zc[kMaxCoarse];
 //   [items: ni int4][geometry: ni float4][list V_ga: nl float4]
 //   resident mode only: [PCG vectors: n x 8 x 12 floats][x: n x 12 floats]
 //                       [other node's offset: ni float4][w_con J_g u_f: nc float4]
+//                       [rotation blocks: n x 9 x 12 floats][coarse blocks: na x 144 floats]
+//                       [zc of each coupled aggregate: na x 12 floats]
+//                       [coarse-inverse rows of the CTA: nrows x NC floats]
 //   [list aggregate: nl int] resident mode only: [constraint group: nc int]
+//                                                [coupled aggregate: na int]
 // Staged constraint items carry {kind | constraint-item index << 4, list base,
 // g, list length} and, for every item, the geometry a product needs
 // ({sgn (g_k - g_j), w scale} for regularisation items, {a, v_c - g_l} for
@@ -49,8 +54,10 @@ __shared__ __align__(16) float s_zc[kMaxCoarse];
 extern __shared__ __align__(16) unsigned char s_dyn[];
 struct StageLayout {
   int n;                                   // staged slots (even unless all of the CTA's nodes are staged)
-  int nd, nx, dp, it, ax, gv, vec, xf, yd, cu, ga, cg;  // byte offsets after the inverse blocks
+  int nd, nx, dp, it, ax, gv, vec, xf, yd, cu, rot, mm, zz, crow, ga, cg, mag;  // byte offsets
   int ncon;                                // constraint items of the staged slots
+  int nent;                                // coupled-aggregate entries of the staged slots
+  int nrows;                               // coarse-inverse rows held (resident mode)
 };
 __shared__ StageLayout s_stg;
 
@@ -70,6 +77,13 @@ __device__ __forceinline__ float* stg_vec(int s, int k) {
 }
 __device__ __forceinline__ float* stg_xf(int s) { return reinterpret_cast<float*>(s_dyn + s_stg.xf) + 12 * s; }
 __device__ __forceinline__ float4* stg_ydp() { return reinterpret_cast<float4*>(s_dyn + s_stg.yd); }
+__device__ __forceinline__ float* stg_rot(int s) { return reinterpret_cast<float*>(s_dyn + s_stg.rot) + 108 * s; }
+__device__ __forceinline__ float* stg_mm(int e) { return reinterpret_cast<float*>(s_dyn + s_stg.mm) + 144 * e; }
+__device__ __forceinline__ float* stg_crow(int j, int NC) {
+  return reinterpret_cast<float*>(s_dyn + s_stg.crow) + (size_t)j * NC;
+}
+__device__ __forceinline__ int* stg_mag() { return reinterpret_cast<int*>(s_dyn + s_stg.mag); }
+__device__ __forceinline__ float* stg_zz(int e) { return reinterpret_cast<float*>(s_dyn + s_stg.zz) + 12 * e; }
 __device__ __forceinline__ float4* stg_cuz() { return reinterpret_cast<float4*>(s_dyn + s_stg.cu); }
 __device__ __forceinline__ int* stg_cg() { return reinterpret_cast<int*>(s_dyn + s_stg.cg); }
 
@@ -849,18 +863,22 @@ __device__ __forceinline__ float apply_dinv_h(const SolveParams& P, int rr, bool
   return (valid && l16 < 12) ? zc : 0.f;
 }
 
-// apply_dinv_h with the inverse block of staged slot s.
+// apply_dinv_h with the inverse block of staged slot s (three accumulators,
+// the row read as float4s).
 __device__ __forceinline__ float apply_dinv_h_stg(int s, bool valid, float rc) {
   const int lane = threadIdx.x & 31;
   const int l16 = lane & 15, base = lane & 16;
-  float zc = 0.f;
-  const float* row = stg_dinv(valid ? s : 0) + 12 * (l16 < 12 ? l16 : 0);
+  const float4* row = reinterpret_cast<const float4*>(stg_dinv(valid ? s : 0) + 12 * (l16 < 12 ? l16 : 0));
+  float ri[12];
 #pragma unroll
-  for (int i = 0; i < 12; ++i) {
-    const float ri = __shfl_sync(0xffffffffu, rc, base + i);
-    if (valid) zc = fmaf(row[i], ri, zc);
+  for (int i = 0; i < 12; ++i) ri[i] = __shfl_sync(0xffffffffu, rc, base + i);
+  float z[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+  for (int q = 0; q < 3; ++q) {
+    const float4 d = row[q];
+    z[q] = fmaf(d.x, ri[4 * q], fmaf(d.y, ri[4 * q + 1], fmaf(d.z, ri[4 * q + 2], d.w * ri[4 * q + 3])));
   }
-  return (valid && l16 < 12) ? zc : 0.f;
+  return (valid && l16 < 12) ? (z[0] + z[1]) + z[2] : 0.f;
 }
 
 // z = Dinv r for free node rr (staged: slot's inverse block in shared
@@ -1315,11 +1333,251 @@ static __device__ __noinline__ void res_products(const SolveParams& P, int s, bo
   }
 }
 
+// P_k e_i: the prolongation of coarse unknown i of node k's own aggregate
+// (coarse_prolong_dp with zc = e_i): identity on the rotation part, and
+// dt = e_t + dR dp on the translation part.
+__device__ __forceinline__ void prolong_unit(const float4 dp, int i, float (&v)[12]) {
+#pragma unroll
+  for (int q = 0; q < 9; ++q) v[q] = q == i ? 1.f : 0.f;
+#pragma unroll
+  for (int r = 0; r < 3; ++r)
+    v[9 + r] = (9 + r == i ? 1.f : 0.f) + (i == r ? dp.x : 0.f) + (i == 3 + r ? dp.y : 0.f) + (i == 6 + r ? dp.z : 0.f);
+}
+
+// Coarse blocks of resident slot s (one warp): the aggregates a coupled to the
+// node (its own, its regularisation neighbours', its constraint groups') and,
+// for each, M_a = the node's rows of (J^T J)_{reg,static,con} P restricted to
+// aggregate a, column by column: column i is the product with zc = e_i on a
+// (apply_item over the node's items, the constraint items with their coarse
+// parts V_ga only).  Stored row-major so that lane c reads row c.
+static __device__ __noinline__ void build_coarse_blocks(const SolveParams& P, int s) {
+  const int lane = threadIdx.x & 31;
+  const int4 nd = stg_node()[s];
+  const int4 bs = stg_base()[s];
+  const int na = bs.z >> 16, mb = bs.w;
+  int cnt = 0;
+  if (lane == 0) {
+    auto add = [&](int a) {
+      for (int t = 0; t < cnt; ++t)
+        if (stg_mag()[mb + t] == a) return;
+      if (cnt < na) stg_mag()[mb + cnt++] = a;
+    };
+    add(nd.w);
+    for (int q = 0; q < nd.z; ++q) {
+      const int4 m = stg_item()[nd.y + q];
+      const int kind = m.x & 15;
+      if ((kind == ITEM_IN || kind == ITEM_OUT) && m.y >= 0) add(m.x >> 4);
+      if (kind == ITEM_CON)
+        for (int f = m.y; f < m.y + m.w; ++f) add(stg_la()[f]);
+    }
+    // (the host counts the same set; any spare entry gets a zero block)
+    for (int t = cnt; t < na; ++t) stg_mag()[mb + t] = nd.w;
+  }
+  cnt = __shfl_sync(0xffffffffu, cnt, 0);
+  __syncwarp();
+  const float4 dpj = stg_dpiv()[s];
+  const float w = P.wgf, wcf = P.wcf;
+  for (int t = 0; t < na; ++t) {
+    const int a = t < cnt ? stg_mag()[mb + t] : -1;
+    for (int i = 0; i < 12; ++i) {
+      float acc[12], yj[12];
+#pragma unroll
+      for (int q = 0; q < 12; ++q) acc[q] = 0.f;
+      if (a == nd.w) {
+        prolong_unit(dpj, i, yj);
+      } else {
+#pragma unroll
+        for (int q = 0; q < 12; ++q) yj[q] = 0.f;
+      }
+      for (int q = lane; q < nd.z; q += 32) {
+        const int it = nd.y + q;
+        const int4 m = stg_item()[it];
+        CouplingData D;
+        D.kind = m.x & 15;
+        D.aux = stg_geo()[it];
+#pragma unroll
+        for (int c = 0; c < 12; ++c) D.v[c] = 0.f;
+        if ((D.kind == ITEM_IN || D.kind == ITEM_OUT) && m.y >= 0 && (m.x >> 4) == a) {
+          float v[12];
+          prolong_unit(stg_ydp()[it], i, v);
+          if (D.kind == ITEM_IN) {
+#pragma unroll
+            for (int c = 0; c < 12; ++c) D.v[c] = v[c];
+          } else {
+            D.v[0] = v[9];
+            D.v[1] = v[10];
+            D.v[2] = v[11];
+          }
+        } else if (D.kind == ITEM_CON) {
+          for (int f = m.y; f < m.y + m.w; ++f) {
+            if (stg_la()[f] != a) continue;
+            const float4 V = stg_lv()[f];
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+              const float vc = i == c ? V.x : (i == 3 + c ? V.y : (i == 6 + c ? V.z : (i == 9 + c ? V.w : 0.f)));
+              D.v[c] = fmaf(wcf, vc, D.v[c]);
+            }
+          }
+        }
+        apply_item(P, D, w, yj, acc);
+      }
+#pragma unroll
+      for (int c = 0; c < 12; ++c) acc[c] = warp_sum(acc[c]);
+      if (lane < 12) {
+        float v = 0.f;
+#pragma unroll
+        for (int c = 0; c < 12; ++c)
+          if (c == lane) v = acc[c];
+        stg_mm(mb + t)[12 * lane + i] = v;
+      }
+    }
+  }
+  __syncwarp();
+}
+
+// The rotation block J_rot^T J_rot (9x9) of resident slot s at the staged x
+// (one warp; lane c < 9 writes row c, padded to 12).
+__device__ __forceinline__ void rot_block(const SolveParams& P, int s) {
+  const int lane = threadIdx.x & 31;
+  if (lane >= 9) return;
+  const float* X = stg_xf(s);
+  const float wr = P.wrf;
+  // rows of J_rot (Deform.cpp:186-214 as products): [c1|c0|0], [c2|0|c0],
+  // [0|c2|c1], 2[c0|0|0], 2[0|c1|0], 2[0|0|c2]
+  auto jrow = [&](int t, int b) -> float {
+    const int blk = b / 3, e = b % 3;
+    switch (t) {
+      case 0: return blk == 0 ? wr * X[3 + e] : (blk == 1 ? wr * X[e] : 0.f);
+      case 1: return blk == 0 ? wr * X[6 + e] : (blk == 2 ? wr * X[e] : 0.f);
+      case 2: return blk == 1 ? wr * X[6 + e] : (blk == 2 ? wr * X[3 + e] : 0.f);
+      case 3: return blk == 0 ? 2.f * wr * X[e] : 0.f;
+      case 4: return blk == 1 ? 2.f * wr * X[3 + e] : 0.f;
+      default: return blk == 2 ? 2.f * wr * X[6 + e] : 0.f;
+    }
+  };
+  float* row = stg_rot(s) + 12 * lane;
+  for (int b = 0; b < 9; ++b) {
+    float v = 0.f;
+    for (int t = 0; t < 6; ++t) v = fmaf(jrow(t, lane), jrow(t, b), v);
+    row[b] = v;
+  }
+  row[9] = row[10] = row[11] = 0.f;
+}
+
+// The rest of w = (J^T J) u for resident slot s from the coarse blocks (lane
+// c < 12 of the half computes entry c; the zc of every coupled aggregate and
+// the w_con J_g u_f of every constraint item must be staged): w = w_f +
+// sum_a M_a zc_a + constraint rows on w_con J_g u_f + rotation block on u,
+// with u = u_f + P_j zc (the node's own aggregate is its first entry).
+// Every shared-memory address follows from the two node records, so a call
+// costs two dependent shared-memory round trips plus its FMA chains.
+__device__ __forceinline__ void res_products_m(const SolveParams& P, int s, bool valid, float (&f3)[3]) {
+  const int c = threadIdx.x & 15;
+  if (!valid || c >= 12) return;
+  const int4 nd = stg_node()[s];
+  const int4 bs = stg_base()[s];
+  const int ncon = bs.z & 0xffff, na = bs.z >> 16;
+  float wv = stg_vec(s, RV_WF)[c];
+  // three accumulators (one per float4 of a row) keep the FMA chains short
+  float wq[3] = {0.f, 0.f, 0.f};
+#pragma unroll 4
+  for (int t = 0; t < na; ++t) {
+    const float4* m4 = reinterpret_cast<const float4*>(stg_mm(bs.w + t) + 12 * c);
+    const float4* z4 = reinterpret_cast<const float4*>(stg_zz(bs.w + t));
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+      const float4 mq = m4[q], zq = z4[q];
+      wq[q] = fmaf(mq.x, zq.x, fmaf(mq.y, zq.y, fmaf(mq.z, zq.z, fmaf(mq.w, zq.w, wq[q]))));
+    }
+  }
+  wv += (wq[0] + wq[1]) + wq[2];
+  // constraint rows on w_con J_g u_f (apply_item's ITEM_CON with D.v = the
+  // staged value); the node's constraint items are its last ncon items and
+  // consecutive in the CTA's constraint list
+  const int g3 = c / 3, cc = c - 3 * g3;
+  const int c0 = nd.y + nd.z - ncon;
+#pragma unroll 2
+  for (int q = 0; q < ncon; ++q) {
+    const float4 ax = stg_geo()[c0 + q];
+    const float4 uz = stg_cuz()[bs.y + q];
+    const float wa = P.wcf * ax.x;
+    const float coef = g3 == 0 ? ax.y : (g3 == 1 ? ax.z : (g3 == 2 ? ax.w : 1.f));
+    const float uzc = cc == 0 ? uz.x : (cc == 1 ? uz.y : uz.z);
+    wv = fmaf(wa * coef, uzc, wv);
+  }
+  // u = u_f + P_j zc of the node's own aggregate
+  const float4* uf4 = reinterpret_cast<const float4*>(stg_vec(s, RV_UF));
+  const float4* zj4 = reinterpret_cast<const float4*>(stg_zz(bs.w));
+  const float4 ua = uf4[0], ub = uf4[1], uc4 = uf4[2];
+  const float4 za = zj4[0], zb = zj4[1], zc4 = zj4[2];
+  const float uf[12] = {ua.x, ua.y, ua.z, ua.w, ub.x, ub.y, ub.z, ub.w, uc4.x, uc4.y, uc4.z, uc4.w};
+  const float zj[12] = {za.x, za.y, za.z, za.w, zb.x, zb.y, zb.z, zb.w, zc4.x, zc4.y, zc4.z, zc4.w};
+  float ucv = 0.f, ufc = 0.f;
+#pragma unroll
+  for (int i = 0; i < 12; ++i)
+    if (i == c) ufc = uf[i];
+  if (c < 9) {
+#pragma unroll
+    for (int i = 0; i < 9; ++i)
+      if (i == c) ucv = ufc + zj[i];
+    const float4* R4 = reinterpret_cast<const float4*>(stg_rot(s) + 12 * c);
+    const float4 ra = R4[0], rb = R4[1], rc = R4[2];
+    const float R[9] = {ra.x, ra.y, ra.z, ra.w, rb.x, rb.y, rb.z, rb.w, rc.x};
+    float rot = 0.f;
+#pragma unroll
+    for (int i = 0; i < 9; ++i) rot = fmaf(R[i], uf[i] + zj[i], rot);
+    wv += rot;
+  } else {
+    const float4 dp = stg_dpiv()[s];
+    const int r = c - 9;
+    float z9 = 0.f, z0 = 0.f, z3 = 0.f, z6 = 0.f;
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+      if (i == r) {
+        z9 = zj[9 + i];
+        z0 = zj[i];
+        z3 = zj[3 + i];
+        z6 = zj[6 + i];
+      }
+    ucv = ufc + (z9 + dp.x * z0 + dp.y * z3 + dp.z * z6);
+  }
+  const float rv = stg_vec(s, RV_R)[c];
+  stg_vec(s, RV_U)[c] = ucv;
+  stg_vec(s, RV_W)[c] = wv;
+  f3[0] = fmaf(rv, ucv, f3[0]);
+  f3[1] = fmaf(wv, ucv, f3[1]);
+  f3[2] = fmaf(rv, rv, f3[2]);
+}
+
+// zc for the CTA's rows of the coarse inverse (resident mode): row j of the
+// CTA is row bid + j nbk, held in shared memory; rc (float) in s_rc.
+__device__ __forceinline__ void coarse_rows_res(const SolveParams& P, int bid, int nbk, int ok, const float* s_rc) {
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  const int NC = P.NC, n4 = NC / 4;
+  const float4* s4 = reinterpret_cast<const float4*>(s_rc);
+  for (int j = wib; j < s_stg.nrows; j += kSolveWarps) {
+    const float4* row = reinterpret_cast<const float4*>(stg_crow(j, NC));
+    float a0 = 0.f, a1 = 0.f;
+    for (int q = lane; q < n4; q += 32) {
+      const float4 v = row[q], r4 = s4[q];
+      a0 = fmaf(v.x, r4.x, fmaf(v.y, r4.y, a0));
+      a1 = fmaf(v.z, r4.z, fmaf(v.w, r4.w, a1));
+    }
+    const float a = warp_sum(a0 + a1);
+    if (lane == 0) P.zc[bid + j * nbk] = ok ? a : 0.f;
+  }
+}
+
 // Shared-memory bytes of one node's tables (host and device use the same sum).
-__host__ __device__ __forceinline__ int stage_node_bytes(int items, int lists, int cons, bool resident) {
+__host__ __device__ __forceinline__ int stage_node_bytes(int items, int lists, int cons, int aggs, bool resident) {
   int b = kStageNodeBytes + kStageItemBytes * items + kStageListBytes * lists;
-  if (resident) b += kResNodeBytes + kResItemBytes * items + kResConBytes * cons;
+  if (resident) b += kResNodeBytes + kResItemBytes * items + kResConBytes * cons + kResAggBytes * aggs;
   return b;
+}
+
+// Coarse-inverse rows CTA bid of nbk holds in resident mode (rows bid, bid + nbk, ...).
+__host__ __device__ __forceinline__ int stage_coarse_rows(int NC, int bid, int nbk) {
+  return bid < NC ? (NC - bid + nbk - 1) / nbk : 0;
 }
 
 // Fills the CTA's resident node tables for this solve (after the per-solve
@@ -1333,17 +1591,19 @@ __device__ void stage_build(const SolveParams& P, int bid, int nbk) {
   const int F = P.F;
   const bool res = P.resident != 0 && P.mode == 0 && P.NA > 0;
   const int cnt = bid < F ? (F - bid + nbk - 1) / nbk : 0;
-  auto node_counts = [&](int s, int& r, int& a, int& l, int& c) {
+  auto node_counts = [&](int s, int& r, int& a, int& l, int& c, int& g) {
     r = 0;
     a = 0;
     l = 0;
     c = 0;
+    g = 0;
     if (s < cnt) {
       r = __ldg(P.order + s * nbk + bid);
       a = __ldg(P.item_off + r + 1) - __ldg(P.item_off + r);
-      const int2 ci = __ldg(P.con_info + r);
+      const int4 ci = __ldg(P.con_info + r);
       l = ci.x;
       c = ci.y;
+      g = ci.z;
     }
   };
   auto scan = [&](int v) {
@@ -1355,13 +1615,14 @@ __device__ void stage_build(const SolveParams& P, int bid, int nbk) {
     return v;
   };
   if (wib == 0) {
-    int used = 0, n = 0, ni = 0, nl = 0, nc = 0;
+    const int nrows = res ? stage_coarse_rows(P.NC, bid, nbk) : 0;
+    int used = nrows * P.NC * 4, n = 0, ni = 0, nl = 0, nc = 0, na = 0;
     bool more = P.stage_cap > 0 && P.mode == 0;
     for (int c0 = 0; c0 < cnt && more; c0 += 32) {
-      int r, a, l, c;
-      node_counts(c0 + lane, r, a, l, c);
-      const int bytes = c0 + lane < cnt ? stage_node_bytes(a, l, c, res) : 0;
-      const int ib = scan(bytes), ia = scan(a), il = scan(l), ic = scan(c);
+      int r, a, l, c, g;
+      node_counts(c0 + lane, r, a, l, c, g);
+      const int bytes = c0 + lane < cnt ? stage_node_bytes(a, l, c, g, res) : 0;
+      const int ib = scan(bytes), ia = scan(a), il = scan(l), ic = scan(c), ig = scan(g);
       // inclusive byte sums grow with the lane, so the slots that fit are a prefix
       const unsigned fit = __ballot_sync(0xffffffffu, c0 + lane < cnt && used + ib <= P.stage_cap);
       const int kf = __popc(fit);
@@ -1370,6 +1631,7 @@ __device__ void stage_build(const SolveParams& P, int bid, int nbk) {
         ni += __shfl_sync(0xffffffffu, ia, kf - 1);
         nl += __shfl_sync(0xffffffffu, il, kf - 1);
         nc += __shfl_sync(0xffffffffu, ic, kf - 1);
+        na += __shfl_sync(0xffffffffu, ig, kf - 1);
         n += kf;
       }
       more = kf == 32;
@@ -1383,6 +1645,8 @@ __device__ void stage_build(const SolveParams& P, int bid, int nbk) {
       StageLayout L;
       L.n = n;
       L.ncon = res ? nc : 0;
+      L.nrows = nrows;
+      if (!res) na = 0;
       L.nd = 576 * n;
       L.nx = L.nd + 16 * n;
       L.dp = L.nx + 16 * n;
@@ -1393,8 +1657,14 @@ __device__ void stage_build(const SolveParams& P, int bid, int nbk) {
       L.xf = L.vec + (res ? kResVecs * 48 * n : 0);
       L.yd = L.xf + (res ? 48 * n : 0);
       L.cu = L.yd + (res ? 16 * ni : 0);
-      L.ga = L.cu + (res ? 16 * nc : 0);
+      L.rot = L.cu + (res ? 16 * nc : 0);
+      L.mm = L.rot + (res ? 432 * n : 0);
+      L.zz = L.mm + 576 * na;
+      L.crow = L.zz + 48 * na;
+      L.nent = na;
+      L.ga = L.crow + 4 * nrows * P.NC;
       L.cg = L.ga + 4 * nl;
+      L.mag = L.cg + (res ? 4 * nc : 0);
       s_stg = L;
     }
   }
@@ -1402,21 +1672,22 @@ __device__ void stage_build(const SolveParams& P, int bid, int nbk) {
   const int n = s_stg.n;
   if (n == 0) return;
   if (wib == 0) {
-    // node records, list and constraint-item bases
-    int ib = 0, lb = 0, cb = 0;
+    // node records, list, constraint-item and coupled-aggregate bases
+    int ib = 0, lb = 0, cb = 0, gb = 0;
     for (int c0 = 0; c0 < n; c0 += 32) {
       const int sl = c0 + lane;
-      int r, a, l, c;
-      node_counts(sl < n ? sl : cnt, r, a, l, c);
-      const int ia = scan(a), il = scan(l), ic = scan(c);
+      int r, a, l, c, g;
+      node_counts(sl < n ? sl : cnt, r, a, l, c, g);
+      const int ia = scan(a), il = scan(l), ic = scan(c), ig = scan(g);
       if (sl < n) {
         stg_node()[sl] = make_int4(r, ib + ia - a, a, P.NA ? __ldg(P.agg + r) : 0);
-        stg_base()[sl] = make_int4(lb + il - l, cb + ic - c, 0, 0);
+        stg_base()[sl] = make_int4(lb + il - l, cb + ic - c, c | (g << 16), gb + ig - g);
         stg_dpiv()[sl] = P.NA ? __ldcg(P.dpiv + r) : make_float4(0.f, 0.f, 0.f, 0.f);
       }
       ib += __shfl_sync(0xffffffffu, ia, 31);
       lb += __shfl_sync(0xffffffffu, il, 31);
       cb += __shfl_sync(0xffffffffu, ic, 31);
+      gb += __shfl_sync(0xffffffffu, ig, 31);
     }
   }
   __syncthreads();
@@ -1478,6 +1749,10 @@ __device__ void stage_build(const SolveParams& P, int bid, int nbk) {
     }
   }
   __syncthreads();
+  if (res) {
+    for (int sl = wib; sl < n; sl += kSolveWarps) build_coarse_blocks(P, sl);
+    __syncthreads();
+  }
 }
 
 }  // namespace arap

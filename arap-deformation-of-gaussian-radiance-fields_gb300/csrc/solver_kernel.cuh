@@ -414,6 +414,10 @@ __device__ __forceinline__ void solve_body(const SolveParams& P, int bid, int nb
           stg_xf(ws)[lane] = __ldcg(P.xf + o);
         }
       }
+      if (resident && stg) {
+        __syncwarp();
+        rot_block(P, ws);
+      }
     }
     for (int e = gt; e < F * 12; e += nt) {
       const double v = __ldcg(P.x + e);
@@ -457,6 +461,16 @@ __device__ __forceinline__ void solve_body(const SolveParams& P, int bid, int nb
       if (!coarse_invert(P, gs, &coarse_ok, s_scratch)) return;
       if (threadIdx.x == 0) s_clk.acc[5] += (double)(global_ns() - s_clk.inv0);
       if (!coarse_ok && gt == 0) raise_status(ARAP_ENONFINITE);
+      if (resident) {
+        // this CTA's rows of the coarse inverse (rows bid, bid + nbk, ...)
+        const int NC = P.NC, n4 = NC / 4;
+        for (int e = threadIdx.x; e < s_stg.nrows * n4; e += blockDim.x) {
+          const int j = e / n4, q = e - j * n4;
+          reinterpret_cast<float4*>(stg_crow(j, NC))[q] =
+              __ldcg(reinterpret_cast<const float4*>(P.Cinv + (size_t)(bid + j * nbk) * NC) + q);
+        }
+        __syncthreads();
+      }
       lap(2);
     }
     const float tol2 = (float)((double)P.pcg_tol * (double)P.pcg_tol * rr0);
@@ -514,18 +528,41 @@ __device__ __forceinline__ void solve_body(const SolveParams& P, int bid, int nb
       const int ns = s_stg.n;
       auto phase2 = [&]() -> bool {
         work_begin();
+        // the restricted residual is requested first, so that its round trip
+        // overlaps the products'
+        const double* rcb = P.rc + cur * P.NC;
+        double rcv[kRcPerThread];
+#pragma unroll
+        for (int q = 0; q < kRcPerThread; ++q) {
+          const int e = threadIdx.x + q * kSolveThreads;
+          rcv[q] = e < P.NC ? __ldcg(rcb + e) : 0.0;
+        }
         for (int hs0 = 2 * wib; hs0 < ns; hs0 += 2 * kSolveWarps) res_products_f(P, hs0 + half, hs0 + half < ns);
-        coarse_solve(P, gs, P.rc + cur * P.NC, P.rc + (cur ^ 1) * P.NC, coarse_ok, s_scratch);
+#pragma unroll
+        for (int q = 0; q < kRcPerThread; ++q) {
+          const int e = threadIdx.x + q * kSolveThreads;
+          if (e < P.NC) s_scratch[e] = (float)rcv[q];
+        }
+        __syncthreads();
+        coarse_rows_res(P, bid, nbk, coarse_ok, s_scratch);
+        double* rco = P.rc + (cur ^ 1) * P.NC;
+        for (int e = gt; e < P.NC; e += nt) rco[e] = 0.0;
+        for (int g = nw - 1 - gw; g < P.G; g += nw) con_jz_group(P, g);
         work_end(2);
         return gs.sync();
       };
       auto phase3 = [&](float2 (&s3)[3]) -> bool {
         float f3[3] = {0.f, 0.f, 0.f};
         work_begin();
-        for (int e = threadIdx.x; e < P.NC; e += blockDim.x) s_zc[e] = __ldcg(P.zc + e);
+        // zc of every coupled aggregate of the CTA's nodes, w_con J_g u_f of
+        // every constraint item
+        for (int e = threadIdx.x; e < 12 * s_stg.nent; e += blockDim.x) {
+          const int en = e / 12, i = e - 12 * en;
+          stg_zz(en)[i] = __ldcg(P.zc + 12 * stg_mag()[en] + i);
+        }
         for (int e = threadIdx.x; e < s_stg.ncon; e += blockDim.x) stg_cuz()[e] = __ldcg(P.uzg + stg_cg()[e]);
         __syncthreads();
-        for (int hs0 = 2 * wib; hs0 < ns; hs0 += 2 * kSolveWarps) res_products(P, hs0 + half, hs0 + half < ns, f3);
+        for (int hs0 = 2 * wib; hs0 < ns; hs0 += 2 * kSolveWarps) res_products_m(P, hs0 + half, hs0 + half < ns, f3);
         work_end(0);
         return gs.reduce_f<3>(f3, s3);
       };
