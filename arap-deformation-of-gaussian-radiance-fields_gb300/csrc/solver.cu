@@ -385,13 +385,15 @@ extern "C" int arap_solver_create(arap_solver** out, int n, int k, const int32_t
       if (kind == ITEM_CON) {
         con_info[r].x += gca_off[m.z + 1] - gca_off[m.z];
         con_info[r].y += 1;
+        con_info[r].w += (grp_off[m.z + 1] - grp_off[m.z]) * k;
         for (int f = gca_off[m.z]; f < gca_off[m.z + 1]; ++f) coupled.push_back(gca[f]);
       }
     }
     std::sort(coupled.begin(), coupled.end());
     con_info[r].z = (int)(std::unique(coupled.begin(), coupled.end()) - coupled.begin());
-    stage_cost[r] = stage_node_bytes(items_r, con_info[r].x, con_info[r].y, con_info[r].z, false);
-    if (NA > 0) res_cost[r] = stage_node_bytes(items_r, con_info[r].x, con_info[r].y, con_info[r].z, true);
+    stage_cost[r] = stage_node_bytes(items_r, con_info[r].x, con_info[r].y, con_info[r].z, con_info[r].w, false);
+    if (NA > 0)
+      res_cost[r] = stage_node_bytes(items_r, con_info[r].x, con_info[r].y, con_info[r].z, con_info[r].w, true);
   }
 
   auto* s = new (std::nothrow) arap_solver();

@@ -94,8 +94,8 @@ struct SolveParams {
   // it processes (coupling items with their geometry, diagonal-block
   // inverses, aggregate offsets) in dynamic shared memory, for as many of its
   // nodes as stage_cap bytes hold; the rest are read from the global tables
-  const int4* con_info;      // [F] {coarse-list entries, constraint items, aggregates coupled to the node, 0}
-                             // (0 without a coarse level)
+  const int4* con_info;      // [F] {coarse-list entries, constraint items, aggregates coupled to the node,
+                             // member-anchor slots of its constraint items' groups} (0 without a coarse level)
   int stage_cap;             // dynamic shared memory of the launch, bytes (0: nothing staged)
   int resident;              // every CTA holds all of its nodes, with their PCG vectors (two-level PCG only)
 };
@@ -109,13 +109,16 @@ constexpr int kStageListBytes = 20;
 // Resident mode adds per node its PCG vectors (8 x 12 floats), the float copy
 // of x (12) and its 9x9 rotation block (rows padded to 12), per coupling item
 // the other node's aggregate offset (16), per constraint item its group id
-// and the group's w_con J_g u_f (20), per aggregate coupled to the node its id
+// and the group's w_con J_g v with the range of its member-anchor slots (28),
+// per such slot its anchor's free rank and geometry (20), per aggregate
+// coupled to the node its id
 // and the node's 12x12 block of (J^T J)_{reg,con} P on it (580), and per CTA
 // its rows of the coarse inverse.
 constexpr int kResVecs = 8;
 constexpr int kResNodeBytes = kResVecs * 48 + 48 + 9 * 48;
 constexpr int kResItemBytes = 16;
-constexpr int kResConBytes = 20;
+constexpr int kResConBytes = 28;  // group id, w_con J_g v, slot range of the group
+constexpr int kResSlotBytes = 20; // member-anchor slot of a constraint item's group: free rank, geometry
 constexpr int kResAggBytes = 576 + 48 + 4;  // block, the aggregate's zc (staged per iteration), id
 
 }  // namespace arap

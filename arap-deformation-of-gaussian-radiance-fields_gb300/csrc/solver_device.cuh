@@ -45,8 +45,9 @@ __shared__ __align__(16) float s_zc[kMaxCoarse];
 //                       [rotation blocks: n x 9 x 12 floats][coarse blocks: na x 144 floats]
 //                       [zc of each coupled aggregate: na x 12 floats]
 //                       [coarse-inverse rows of the CTA: nrows x NC floats]
+//                       [member-anchor slot geometry: nsl float4][slot range per constraint item: nc int2]
 //   [list aggregate: nl int] resident mode only: [constraint group: nc int]
-//                                                [coupled aggregate: na int]
+//                                                [coupled aggregate: na int][slot free rank: nsl int]
 // Staged constraint items carry {kind | constraint-item index << 4, list base,
 // g, list length} and, for every item, the geometry a product needs
 // ({sgn (g_k - g_j), w scale} for regularisation items, {a, v_c - g_l} for
@@ -54,7 +55,7 @@ __shared__ __align__(16) float s_zc[kMaxCoarse];
 extern __shared__ __align__(16) unsigned char s_dyn[];
 struct StageLayout {
   int n;                                   // staged slots (even unless all of the CTA's nodes are staged)
-  int nd, nx, dp, it, ax, gv, vec, xf, yd, cu, rot, mm, zz, crow, ga, cg, mag;  // byte offsets
+  int nd, nx, dp, it, ax, gv, vec, xf, yd, cu, rot, mm, zz, crow, gsg, cgs, ga, cg, mag, gsr;  // byte offsets
   int ncon;                                // constraint items of the staged slots
   int nent;                                // coupled-aggregate entries of the staged slots
   int nrows;                               // coarse-inverse rows held (resident mode)
@@ -84,6 +85,9 @@ __device__ __forceinline__ float* stg_crow(int j, int NC) {
 }
 __device__ __forceinline__ int* stg_mag() { return reinterpret_cast<int*>(s_dyn + s_stg.mag); }
 __device__ __forceinline__ float* stg_zz(int e) { return reinterpret_cast<float*>(s_dyn + s_stg.zz) + 12 * e; }
+__device__ __forceinline__ float4* stg_gsg() { return reinterpret_cast<float4*>(s_dyn + s_stg.gsg); }
+__device__ __forceinline__ int2* stg_cgs() { return reinterpret_cast<int2*>(s_dyn + s_stg.cgs); }
+__device__ __forceinline__ int* stg_gsr() { return reinterpret_cast<int*>(s_dyn + s_stg.gsr); }
 __device__ __forceinline__ float4* stg_cuz() { return reinterpret_cast<float4*>(s_dyn + s_stg.cu); }
 __device__ __forceinline__ int* stg_cg() { return reinterpret_cast<int*>(s_dyn + s_stg.cg); }
 
@@ -275,12 +279,13 @@ __device__ __forceinline__ void con_ju_list(const SolveParams& P, int g, int off
   }
 }
 
-// w_con J_g u_f of group g (u_f = Dinv r in P.z); one warp, lane 0 stores it.
-__device__ __forceinline__ void con_jz_group(const SolveParams& P, int g) {
+// w_con J_g u_f of group g (u_f = Dinv r in P.z); one warp, lane 0 stores it,
+// every lane returns it in u.
+__device__ __forceinline__ void con_jz_group(const SolveParams& P, int g, float (&u)[3]) {
   const int lane = threadIdx.x & 31;
   const int k = P.k;
   const int s0 = __ldg(P.grp_off + g) * k, s1 = __ldg(P.grp_off + g + 1) * k;
-  float u[3] = {0.f, 0.f, 0.f};
+  u[0] = u[1] = u[2] = 0.f;
   for (int slot = s0 + lane; slot < s1; slot += 32) {
     const int rk = __ldg(P.mem_rank + slot);
     if (rk < 0) continue;
@@ -295,6 +300,10 @@ __device__ __forceinline__ void con_jz_group(const SolveParams& P, int g) {
 #pragma unroll
   for (int c = 0; c < 3; ++c) u[c] = wcf * warp_sum(u[c]);
   if (lane == 0) P.uzg[g] = make_float4(u[0], u[1], u[2], 0.f);
+}
+__device__ __forceinline__ void con_jz_group(const SolveParams& P, int g) {
+  float u[3];
+  con_jz_group(P, g, u);
 }
 
 // 4x4 symmetric accumulator index (a <= b).
@@ -1549,6 +1558,275 @@ __device__ __forceinline__ void res_products_m(const SolveParams& P, int s, bool
   f3[2] = fmaf(rv, rv, f3[2]);
 }
 
+// ------------------------------------------- V-cycle preconditioner ----
+// The resident two-level PCG applies the symmetric two-grid cycle
+//   z1 = D^-1 r,  zc = C^-1 P^T (r - A z1),  z2 = z1 + P zc,
+//   u = z2 + D^-1 (r - A z2),  w = A u = A z2 + A z3 (z3 = D^-1 (r - A z2))
+// with the block-Jacobi smoother D before and after the coarse correction.
+// It needs about half the iterations of the additive form D^-1 + P C^-1 P^T
+// on these problems, for two more barriers per iteration.  A z1 and A z3 take
+// the neighbours' vectors from L2; A P zc comes from the coarse blocks.
+
+// Rotation block of slot s applied to the first nine entries of v (lane c < 9).
+__device__ __forceinline__ float rot_apply(int s, int c, const float (&v)[12]) {
+  const float4* R4 = reinterpret_cast<const float4*>(stg_rot(s) + 12 * c);
+  const float4 ra = R4[0], rb = R4[1], rc = R4[2];
+  const float R[9] = {ra.x, ra.y, ra.z, ra.w, rb.x, rb.y, rb.z, rb.w, rc.x};
+  float a0 = 0.f, a1 = 0.f, a2 = 0.f;
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    a0 = fmaf(R[i], v[i], a0);
+    a1 = fmaf(R[3 + i], v[3 + i], a1);
+    a2 = fmaf(R[6 + i], v[6 + i], a2);
+  }
+  return (a0 + a1) + a2;
+}
+
+// Constraint rows of slot s on the staged w_con J_g v of its constraint
+// items (apply_item's ITEM_CON; the node's constraint items are its last ncon
+// items and consecutive in the CTA's constraint list); entry c.
+__device__ __forceinline__ float con_apply(const SolveParams& P, const int4& nd, const int4& bs, int c) {
+  const int ncon = bs.z & 0xffff;
+  const int g3 = c / 3, cc = c - 3 * g3;
+  const int c0 = nd.y + nd.z - ncon;
+  float v = 0.f;
+  for (int q = 0; q < ncon; ++q) {
+    const float4 ax = stg_geo()[c0 + q];
+    const float4 uz = stg_cuz()[bs.y + q];
+    const float wa = P.wcf * ax.x;
+    const float coef = g3 == 0 ? ax.y : (g3 == 1 ? ax.z : (g3 == 2 ? ax.w : 1.f));
+    const float uzc = cc == 0 ? uz.x : (cc == 1 ? uz.y : uz.z);
+    v = fmaf(wa * coef, uzc, v);
+  }
+  return v;
+}
+
+__device__ __forceinline__ void ld12s(const float* p, float (&v)[12]) {
+  const float4* p4 = reinterpret_cast<const float4*>(p);
+  const float4 a = p4[0], b = p4[1], c = p4[2];
+  v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w; v[4] = b.x; v[5] = b.y;
+  v[6] = b.z; v[7] = b.w; v[8] = c.x; v[9] = c.y; v[10] = c.z; v[11] = c.w;
+}
+
+// (J^T J)_{reg,static} v of resident slot s (regularisation and static-node
+// items; the node's own v is slot vector k, the neighbours' v come from P.z),
+// reduced over the half-warp: every lane of the half holds the 12 entries.
+__device__ __forceinline__ void reg_product(const SolveParams& P, int s, bool valid, int k, float (&acc)[12]) {
+  const int lane = threadIdx.x & 15;
+  float pj[12];
+#pragma unroll
+  for (int i = 0; i < 12; ++i) {
+    acc[i] = 0.f;
+    pj[i] = 0.f;
+  }
+  if (valid) {
+    const int4 nd = stg_node()[s];
+    ld12s(stg_vec(s, k), pj);
+    const float w = P.wgf;
+    for (int q = lane; q < nd.z; q += 32) {
+      const bool hasB = q + 16 < nd.z;
+      CouplingData A, B;
+      auto fetch = [&](int i, CouplingData& D) {
+        const int4 m = stg_item()[i];
+        D.kind = m.x & 15;
+        D.aux = stg_geo()[i];
+#pragma unroll
+        for (int t = 0; t < 12; ++t) D.v[t] = 0.f;
+        if (D.kind == ITEM_IN) {
+          ld12cg(P.z, m.y, D.v);
+        } else if (D.kind == ITEM_OUT && m.y >= 0) {
+          float t3[3];
+          ld3t_cg(P.z, m.y, t3);
+          D.v[0] = t3[0];
+          D.v[1] = t3[1];
+          D.v[2] = t3[2];
+        }
+      };
+      fetch(nd.y + q, A);
+      if (hasB) fetch(nd.y + q + 16, B);
+      if (A.kind != ITEM_CON) apply_item(P, A, w, pj, acc);
+      if (hasB && B.kind != ITEM_CON) apply_item(P, B, w, pj, acc);
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < 12; ++i) {
+#pragma unroll
+    for (int o = 8; o > 0; o >>= 1) acc[i] += __shfl_xor_sync(0xffffffffu, acc[i], o);
+  }
+}
+
+__device__ __forceinline__ float pick12(const float (&v)[12], int c) {
+  float x = 0.f;
+#pragma unroll
+  for (int i = 0; i < 12; ++i)
+    if (i == c) x = v[i];
+  return x;
+}
+
+// Phase 1: p = u + beta p, s = w + beta s, h += alpha p, r -= alpha s,
+// z1 = D^-1 r for resident slot s; z1 and h also to global memory.
+static __device__ __noinline__ void vc_update(const SolveParams& P, int s, bool valid, float alpha, float beta,
+                                              bool first) {
+  const int l16 = threadIdx.x & 15;
+  const bool own = valid && l16 < 12;
+  float rv = 0.f, hv = 0.f;
+  int r = 0;
+  if (own) {
+    r = stg_node()[s].x;
+    const float uo = stg_vec(s, RV_U)[l16], wo = stg_vec(s, RV_W)[l16];
+    const float pn = first ? uo : fmaf(beta, stg_vec(s, RV_P)[l16], uo);
+    const float sn = first ? wo : fmaf(beta, stg_vec(s, RV_S)[l16], wo);
+    stg_vec(s, RV_P)[l16] = pn;
+    stg_vec(s, RV_S)[l16] = sn;
+    hv = fmaf(alpha, pn, stg_vec(s, RV_H)[l16]);
+    stg_vec(s, RV_H)[l16] = hv;
+    rv = fmaf(-alpha, sn, stg_vec(s, RV_R)[l16]);
+    stg_vec(s, RV_R)[l16] = rv;
+  }
+  const float zv = apply_dinv_h_stg(s, valid, rv);
+  if (own) {
+    stg_vec(s, RV_UF)[l16] = zv;
+    P.z[12 * (size_t)r + l16] = zv;
+    P.h[12 * (size_t)r + l16] = hv;
+  }
+}
+
+// Phase 2, nodes: a1 = (J^T J)_{reg,static,rot} z1 of resident slot s (kept
+// in RV_WF) and the restriction of r - a1 into rc (the constraint rows are
+// restricted per group, vc_group_restrict).
+static __device__ __noinline__ void vc_products_z1(const SolveParams& P, int s, bool valid, double* rc) {
+  const int c = threadIdx.x & 15;
+  float acc[12];
+  reg_product(P, s, valid, RV_UF, acc);
+  float t = 0.f;
+  if (valid && c < 12) {
+    float z1[12];
+    ld12s(stg_vec(s, RV_UF), z1);
+    float a1 = pick12(acc, c);
+    if (c < 9) a1 += rot_apply(s, c, z1);
+    stg_vec(s, RV_WF)[c] = a1;
+    t = stg_vec(s, RV_R)[c] - a1;
+  }
+  coarse_restrict_h_stg(s, valid, t, rc);
+}
+
+// Phase 2, groups: w_con J_g z1 of group g (one warp; to P.uzg) and the
+// restriction of its constraint rows, rc_a -= (J_g P_a)^T (w_con J_g z1).
+__device__ __forceinline__ void vc_group_restrict(const SolveParams& P, int g, double* rc) {
+  const int lane = threadIdx.x & 31;
+  float uz[3];
+  con_jz_group(P, g, uz);
+  if (lane >= 12) return;
+  const int blk = lane / 3, cc = lane - 3 * blk;
+  const float u = cc == 0 ? uz[0] : (cc == 1 ? uz[1] : uz[2]);
+  const int f0 = __ldg(P.gca_off + g), f1 = __ldg(P.gca_off + g + 1);
+  for (int f = f0; f < f1; ++f) {
+    const float4 V = __ldcg(P.gcv + f);
+    const float vb = blk == 0 ? V.x : (blk == 1 ? V.y : (blk == 2 ? V.z : V.w));
+    atomicAdd(rc + 12 * __ldg(P.gca + f) + lane, -(double)(P.wcf * vb * u));
+  }
+}
+
+// Phase 4: z2 = z1 + P zc, A z2 = a1 + constraint rows on w_con J_g z1 +
+// A P zc (coarse blocks, rotation block on P_j zc), z3 = D^-1 (r - A z2),
+// u = z2 + z3 for resident slot s.  Keeps u, A z2 (RV_WF) and z3 (RV_UF, also
+// to P.z for the neighbours).  zc entries and w_con J_g z1 must be staged.
+static __device__ __noinline__ void vc_precond(const SolveParams& P, int s, bool valid) {
+  const int c = threadIdx.x & 15;
+  float t = 0.f, z2 = 0.f, az2 = 0.f;
+  int r = 0;
+  if (valid && c < 12) {
+    const int4 nd = stg_node()[s];
+    const int4 bs = stg_base()[s];
+    const int na = bs.z >> 16;
+    r = nd.x;
+    float wq[3] = {0.f, 0.f, 0.f};
+#pragma unroll 4
+    for (int e = 0; e < na; ++e) {
+      const float4* m4 = reinterpret_cast<const float4*>(stg_mm(bs.w + e) + 12 * c);
+      const float4* z4 = reinterpret_cast<const float4*>(stg_zz(bs.w + e));
+#pragma unroll
+      for (int q = 0; q < 3; ++q) {
+        const float4 mq = m4[q], zq = z4[q];
+        wq[q] = fmaf(mq.x, zq.x, fmaf(mq.y, zq.y, fmaf(mq.z, zq.z, fmaf(mq.w, zq.w, wq[q]))));
+      }
+    }
+    float zj[12];
+    ld12s(stg_zz(bs.w), zj);  // the node's own aggregate is its first entry
+    float pz;
+    if (c < 9) {
+      pz = pick12(zj, c);
+    } else {
+      const float4 dp = stg_dpiv()[s];
+      const int rr = c - 9;
+      pz = pick12(zj, 9 + rr) + dp.x * pick12(zj, rr) + dp.y * pick12(zj, 3 + rr) + dp.z * pick12(zj, 6 + rr);
+    }
+    float apz = (wq[0] + wq[1]) + wq[2];
+    if (c < 9) apz += rot_apply(s, c, zj);
+    z2 = stg_vec(s, RV_UF)[c] + pz;
+    az2 = stg_vec(s, RV_WF)[c] + con_apply(P, nd, bs, c) + apz;
+    t = stg_vec(s, RV_R)[c] - az2;
+  }
+  const float z3 = apply_dinv_h_stg(s, valid, t);
+  if (valid && c < 12) {
+    stg_vec(s, RV_U)[c] = z2 + z3;
+    stg_vec(s, RV_WF)[c] = az2;
+    stg_vec(s, RV_UF)[c] = z3;
+    P.z[12 * (size_t)r + c] = z3;
+  }
+}
+
+// Phase 5, groups: w_con J_g z3 for constraint item ci of the CTA (eight
+// lanes; the group's member-anchor slots are staged), into the staged slot.
+__device__ __forceinline__ void vc_group_z3(const SolveParams& P, int ci, bool valid) {
+  const int q8 = threadIdx.x & 7;
+  const unsigned mask = 0xffu << (threadIdx.x & 24);
+  float u[3] = {0.f, 0.f, 0.f};
+  if (valid) {
+    const int2 sr = stg_cgs()[ci];
+    for (int e = q8; e < sr.y; e += 8) {
+      const int rk = stg_gsr()[sr.x + e];
+      if (rk < 0) continue;
+      const float4 geo = stg_gsg()[sr.x + e];
+      float zl[12];
+      ld12cg(P.z, rk, zl);
+#pragma unroll
+      for (int c = 0; c < 3; ++c)
+        u[c] = fmaf(geo.x, fmaf(geo.y, zl[c], fmaf(geo.z, zl[3 + c], fmaf(geo.w, zl[6 + c], zl[9 + c]))), u[c]);
+    }
+  }
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+#pragma unroll
+    for (int o = 4; o > 0; o >>= 1) u[c] += __shfl_xor_sync(mask, u[c], o);
+  }
+  if (valid && q8 == 0) stg_cuz()[ci] = make_float4(P.wcf * u[0], P.wcf * u[1], P.wcf * u[2], 0.f);
+}
+
+// Phase 5, nodes: A z3 = (J^T J)_{reg,static} z3 + constraint rows on
+// w_con J_g z3 + rotation block on z3; w = A z2 + A z3; adds r.u, w.u, r.r
+// into f3.
+static __device__ __noinline__ void vc_products(const SolveParams& P, int s, bool valid, float (&f3)[3]) {
+  const int c = threadIdx.x & 15;
+  float acc[12];
+  reg_product(P, s, valid, RV_UF, acc);
+  if (valid && c < 12) {
+    const int4 nd = stg_node()[s];
+    const int4 bs = stg_base()[s];
+    float z3[12];
+    ld12s(stg_vec(s, RV_UF), z3);
+    float az3 = pick12(acc, c) + con_apply(P, nd, bs, c);
+    if (c < 9) az3 += rot_apply(s, c, z3);
+    const float wv = stg_vec(s, RV_WF)[c] + az3;
+    const float uc = stg_vec(s, RV_U)[c];
+    const float rv = stg_vec(s, RV_R)[c];
+    stg_vec(s, RV_W)[c] = wv;
+    f3[0] = fmaf(rv, uc, f3[0]);
+    f3[1] = fmaf(wv, uc, f3[1]);
+    f3[2] = fmaf(rv, rv, f3[2]);
+  }
+}
+
 // zc for the CTA's rows of the coarse inverse (resident mode): row j of the
 // CTA is row bid + j nbk, held in shared memory; rc (float) in s_rc.
 __device__ __forceinline__ void coarse_rows_res(const SolveParams& P, int bid, int nbk, int ok, const float* s_rc) {
@@ -1569,9 +1847,11 @@ __device__ __forceinline__ void coarse_rows_res(const SolveParams& P, int bid, i
 }
 
 // Shared-memory bytes of one node's tables (host and device use the same sum).
-__host__ __device__ __forceinline__ int stage_node_bytes(int items, int lists, int cons, int aggs, bool resident) {
+__host__ __device__ __forceinline__ int stage_node_bytes(int items, int lists, int cons, int aggs, int slots,
+                                                         bool resident) {
   int b = kStageNodeBytes + kStageItemBytes * items + kStageListBytes * lists;
-  if (resident) b += kResNodeBytes + kResItemBytes * items + kResConBytes * cons + kResAggBytes * aggs;
+  if (resident)
+    b += kResNodeBytes + kResItemBytes * items + kResConBytes * cons + kResAggBytes * aggs + kResSlotBytes * slots;
   return b;
 }
 
@@ -1591,12 +1871,13 @@ __device__ void stage_build(const SolveParams& P, int bid, int nbk) {
   const int F = P.F;
   const bool res = P.resident != 0 && P.mode == 0 && P.NA > 0;
   const int cnt = bid < F ? (F - bid + nbk - 1) / nbk : 0;
-  auto node_counts = [&](int s, int& r, int& a, int& l, int& c, int& g) {
+  auto node_counts = [&](int s, int& r, int& a, int& l, int& c, int& g, int& z) {
     r = 0;
     a = 0;
     l = 0;
     c = 0;
     g = 0;
+    z = 0;
     if (s < cnt) {
       r = __ldg(P.order + s * nbk + bid);
       a = __ldg(P.item_off + r + 1) - __ldg(P.item_off + r);
@@ -1604,6 +1885,7 @@ __device__ void stage_build(const SolveParams& P, int bid, int nbk) {
       l = ci.x;
       c = ci.y;
       g = ci.z;
+      z = ci.w;
     }
   };
   auto scan = [&](int v) {
@@ -1616,13 +1898,13 @@ __device__ void stage_build(const SolveParams& P, int bid, int nbk) {
   };
   if (wib == 0) {
     const int nrows = res ? stage_coarse_rows(P.NC, bid, nbk) : 0;
-    int used = nrows * P.NC * 4, n = 0, ni = 0, nl = 0, nc = 0, na = 0;
+    int used = nrows * P.NC * 4, n = 0, ni = 0, nl = 0, nc = 0, na = 0, nz = 0;
     bool more = P.stage_cap > 0 && P.mode == 0;
     for (int c0 = 0; c0 < cnt && more; c0 += 32) {
-      int r, a, l, c, g;
-      node_counts(c0 + lane, r, a, l, c, g);
-      const int bytes = c0 + lane < cnt ? stage_node_bytes(a, l, c, g, res) : 0;
-      const int ib = scan(bytes), ia = scan(a), il = scan(l), ic = scan(c), ig = scan(g);
+      int r, a, l, c, g, z;
+      node_counts(c0 + lane, r, a, l, c, g, z);
+      const int bytes = c0 + lane < cnt ? stage_node_bytes(a, l, c, g, z, res) : 0;
+      const int ib = scan(bytes), ia = scan(a), il = scan(l), ic = scan(c), ig = scan(g), iz = scan(z);
       // inclusive byte sums grow with the lane, so the slots that fit are a prefix
       const unsigned fit = __ballot_sync(0xffffffffu, c0 + lane < cnt && used + ib <= P.stage_cap);
       const int kf = __popc(fit);
@@ -1632,6 +1914,7 @@ __device__ void stage_build(const SolveParams& P, int bid, int nbk) {
         nl += __shfl_sync(0xffffffffu, il, kf - 1);
         nc += __shfl_sync(0xffffffffu, ic, kf - 1);
         na += __shfl_sync(0xffffffffu, ig, kf - 1);
+        nz += __shfl_sync(0xffffffffu, iz, kf - 1);
         n += kf;
       }
       more = kf == 32;
@@ -1646,7 +1929,10 @@ __device__ void stage_build(const SolveParams& P, int bid, int nbk) {
       L.n = n;
       L.ncon = res ? nc : 0;
       L.nrows = nrows;
-      if (!res) na = 0;
+      if (!res) {
+        na = 0;
+        nz = 0;
+      }
       L.nd = 576 * n;
       L.nx = L.nd + 16 * n;
       L.dp = L.nx + 16 * n;
@@ -1662,9 +1948,12 @@ __device__ void stage_build(const SolveParams& P, int bid, int nbk) {
       L.zz = L.mm + 576 * na;
       L.crow = L.zz + 48 * na;
       L.nent = na;
-      L.ga = L.crow + 4 * nrows * P.NC;
+      L.gsg = L.crow + 4 * nrows * P.NC;
+      L.cgs = L.gsg + 16 * nz;
+      L.ga = L.cgs + (res ? 8 * nc : 0);
       L.cg = L.ga + 4 * nl;
       L.mag = L.cg + (res ? 4 * nc : 0);
+      L.gsr = L.mag + 4 * na;
       s_stg = L;
     }
   }
@@ -1673,21 +1962,24 @@ __device__ void stage_build(const SolveParams& P, int bid, int nbk) {
   if (n == 0) return;
   if (wib == 0) {
     // node records, list, constraint-item and coupled-aggregate bases
-    int ib = 0, lb = 0, cb = 0, gb = 0;
+    int ib = 0, lb = 0, cb = 0, gb = 0, zb = 0;
     for (int c0 = 0; c0 < n; c0 += 32) {
       const int sl = c0 + lane;
-      int r, a, l, c, g;
-      node_counts(sl < n ? sl : cnt, r, a, l, c, g);
-      const int ia = scan(a), il = scan(l), ic = scan(c), ig = scan(g);
+      int r, a, l, c, g, z;
+      node_counts(sl < n ? sl : cnt, r, a, l, c, g, z);
+      const int ia = scan(a), il = scan(l), ic = scan(c), ig = scan(g), iz = scan(z);
       if (sl < n) {
         stg_node()[sl] = make_int4(r, ib + ia - a, a, P.NA ? __ldg(P.agg + r) : 0);
         stg_base()[sl] = make_int4(lb + il - l, cb + ic - c, c | (g << 16), gb + ig - g);
-        stg_dpiv()[sl] = P.NA ? __ldcg(P.dpiv + r) : make_float4(0.f, 0.f, 0.f, 0.f);
+        // the offset's fourth word holds the slot base of the node's member-anchor slots
+        const float4 dp = P.NA ? __ldcg(P.dpiv + r) : make_float4(0.f, 0.f, 0.f, 0.f);
+        stg_dpiv()[sl] = make_float4(dp.x, dp.y, dp.z, __int_as_float(zb + iz - z));
       }
       ib += __shfl_sync(0xffffffffu, ia, 31);
       lb += __shfl_sync(0xffffffffu, il, 31);
       cb += __shfl_sync(0xffffffffu, ic, 31);
       gb += __shfl_sync(0xffffffffu, ig, 31);
+      zb += __shfl_sync(0xffffffffu, iz, 31);
     }
   }
   __syncthreads();
@@ -1700,7 +1992,7 @@ __device__ void stage_build(const SolveParams& P, int bid, int nbk) {
     const float gj[3] = {__ldg(P.node_pos + 3 * (size_t)j), __ldg(P.node_pos + 3 * (size_t)j + 1),
                          __ldg(P.node_pos + 3 * (size_t)j + 2)};
     const int4 bs = stg_base()[sl];
-    int lb = bs.x, cb = bs.y;
+    int lb = bs.x, cb = bs.y, zb = __float_as_int(stg_dpiv()[sl].w);
     for (int q0 = 0; q0 < nd.z; q0 += 32) {
       const int q = q0 + lane;
       const bool has = q < nd.z;
@@ -1725,18 +2017,35 @@ __device__ void stage_build(const SolveParams& P, int bid, int nbk) {
       }
       const int il = scan(len);
       const int ic = scan(kind == ITEM_CON && P.NA ? 1 : 0);
+      const int loff = lb + il - len;
       if (kind == ITEM_CON && P.NA) {
-        const int off = lb + il - len;
         for (int e = 0; e < len; ++e) {
-          stg_lv()[off + e] = __ldcg(P.gcv + f0 + e);
-          stg_la()[off + e] = __ldg(P.gca + f0 + e);
+          stg_lv()[loff + e] = __ldcg(P.gcv + f0 + e);
+          stg_la()[loff + e] = __ldg(P.gca + f0 + e);
         }
         if (res) {
           const int ci = cb + ic - 1;
           stg_cg()[ci] = m.z;
           m.x = ITEM_CON | (ci << 4);
         }
-        m.y = off;
+      }
+      // member-anchor slots of the constraint item's group (resident mode)
+      int zs = 0, z0 = 0;
+      if (res && kind == ITEM_CON) {
+        z0 = __ldg(P.grp_off + m.z) * P.k;
+        zs = __ldg(P.grp_off + m.z + 1) * P.k - z0;
+      }
+      const int iz = scan(zs);
+      if (res && kind == ITEM_CON) {
+        const int off = zb + iz - zs;
+        stg_cgs()[cb + ic - 1] = make_int2(off, zs);
+        for (int e = 0; e < zs; ++e) {
+          stg_gsr()[off + e] = __ldg(P.mem_rank + z0 + e);
+          stg_gsg()[off + e] = __ldcg(P.mem_geo + z0 + e);
+        }
+      }
+      if (kind == ITEM_CON && P.NA) {
+        m.y = loff;
         m.w = len;
       }
       if (has) {
@@ -1746,6 +2055,7 @@ __device__ void stage_build(const SolveParams& P, int bid, int nbk) {
       }
       lb += __shfl_sync(0xffffffffu, il, 31);
       cb += __shfl_sync(0xffffffffu, ic, 31);
+      zb += __shfl_sync(0xffffffffu, iz, 31);
     }
   }
   __syncthreads();

@@ -400,7 +400,8 @@ __device__ __forceinline__ void solve_body(const SolveParams& P, int bid, int nb
       for (int i = 0; i < 12; ++i)
         if (i == lane) gc = -(float)acc[i];
       const float zc = stg ? apply_dinv<true>(P, r, ws, gc) : apply_dinv<false>(P, r, 0, gc);
-      if (coarse) coarse_restrict(P, r, gc, P.rc);
+      // (the resident PCG restricts r - A z1 itself)
+      if (coarse && !resident) coarse_restrict(P, r, gc, P.rc);
       if (lane < 12) {
         const size_t o = 12 * (size_t)r + lane;
         P.r[o] = gc;
@@ -521,40 +522,36 @@ __device__ __forceinline__ void solve_body(const SolveParams& P, int bid, int nb
     int cur = 0;  // rc buffer holding P^T r of the current residual
     int pi = 0;
     if (resident) {
-      // ---- two-level PCG with the CTA's nodes resident in shared memory:
-      //   (1) vector update of own nodes (no global loads); plain barrier
-      //   (2) zc = Cinv P^T r, w_con J_g u_f, w_f = (J^T J)_reg u_f; plain barrier
-      //   (3) the rest of w from shared memory; gamma, delta, r.r in one reduction
+      // ---- two-level PCG with the CTA's nodes resident in shared memory and
+      // the symmetric two-grid preconditioner (vc_* in solver_device.cuh):
+      //   (1) update of own nodes, z1 = D^-1 r; plain barrier
+      //   (2) A z1 but its constraint rows, the restriction of r - A z1 (nodes,
+      //       and per group for the constraint rows); plain barrier
+      //   (3) zc = C^-1 P^T (r - A z1) over the CTA's rows of C^-1; plain barrier
+      //   (4) z2 = z1 + P zc, A z2, z3 = D^-1 (r - A z2), u = z2 + z3; plain barrier
+      //   (5) A z3, w = A z2 + A z3; gamma, delta, r.r in one reduction
       const int ns = s_stg.n;
-      auto phase2 = [&]() -> bool {
+      auto apply_m = [&](float2 (&s3)[3]) -> bool {
+        double* rcw = P.rc + cur * P.NC;
         work_begin();
-        // the restricted residual is requested first, so that its round trip
-        // overlaps the products'
-        const double* rcb = P.rc + cur * P.NC;
-        double rcv[kRcPerThread];
+        for (int hs0 = 2 * wib; hs0 < ns; hs0 += 2 * kSolveWarps) vc_products_z1(P, hs0 + half, hs0 + half < ns, rcw);
+        for (int g = nw - 1 - gw; g < P.G; g += nw) vc_group_restrict(P, g, rcw);
+        work_end(2);
+        if (!gs.sync()) return false;
+        work_begin();
 #pragma unroll
         for (int q = 0; q < kRcPerThread; ++q) {
           const int e = threadIdx.x + q * kSolveThreads;
-          rcv[q] = e < P.NC ? __ldcg(rcb + e) : 0.0;
-        }
-        for (int hs0 = 2 * wib; hs0 < ns; hs0 += 2 * kSolveWarps) res_products_f(P, hs0 + half, hs0 + half < ns);
-#pragma unroll
-        for (int q = 0; q < kRcPerThread; ++q) {
-          const int e = threadIdx.x + q * kSolveThreads;
-          if (e < P.NC) s_scratch[e] = (float)rcv[q];
+          if (e < P.NC) s_scratch[e] = (float)__ldcg(rcw + e);
         }
         __syncthreads();
         coarse_rows_res(P, bid, nbk, coarse_ok, s_scratch);
         double* rco = P.rc + (cur ^ 1) * P.NC;
         for (int e = gt; e < P.NC; e += nt) rco[e] = 0.0;
-        for (int g = nw - 1 - gw; g < P.G; g += nw) con_jz_group(P, g);
         work_end(2);
-        return gs.sync();
-      };
-      auto phase3 = [&](float2 (&s3)[3]) -> bool {
-        float f3[3] = {0.f, 0.f, 0.f};
+        if (!gs.sync()) return false;
         work_begin();
-        // zc of every coupled aggregate of the CTA's nodes, w_con J_g u_f of
+        // zc of every coupled aggregate of the CTA's nodes, w_con J_g z1 of
         // every constraint item
         for (int e = threadIdx.x; e < 12 * s_stg.nent; e += blockDim.x) {
           const int en = e / 12, i = e - 12 * en;
@@ -562,13 +559,24 @@ __device__ __forceinline__ void solve_body(const SolveParams& P, int bid, int nb
         }
         for (int e = threadIdx.x; e < s_stg.ncon; e += blockDim.x) stg_cuz()[e] = __ldcg(P.uzg + stg_cg()[e]);
         __syncthreads();
-        for (int hs0 = 2 * wib; hs0 < ns; hs0 += 2 * kSolveWarps) res_products_m(P, hs0 + half, hs0 + half < ns, f3);
+        for (int hs0 = 2 * wib; hs0 < ns; hs0 += 2 * kSolveWarps) vc_precond(P, hs0 + half, hs0 + half < ns);
+        work_end(1);
+        if (!gs.sync()) return false;
+        work_begin();
+        // w_con J_g z3 of the CTA's constraint items, eight lanes each
+        for (int c0 = 0; c0 < s_stg.ncon; c0 += kSolveThreads / 8) {
+          const int ci = c0 + (int)(threadIdx.x >> 3);
+          vc_group_z3(P, ci, ci < s_stg.ncon);
+        }
+        __syncthreads();
+        float f3[3] = {0.f, 0.f, 0.f};
+        for (int hs0 = 2 * wib; hs0 < ns; hs0 += 2 * kSolveWarps) vc_products(P, hs0 + half, hs0 + half < ns, f3);
         work_end(0);
+        cur ^= 1;
         return gs.reduce_f<3>(f3, s3);
       };
-      if (!phase2()) return;
       float2 s3[3];
-      if (!phase3(s3)) return;
+      if (!apply_m(s3)) return;
       float2 gam = s3[0];
       rr = s3[2].x;
       bool go = rr > tol2 && gam.x > 0.f && s3[1].x > 0.f;
@@ -577,16 +585,13 @@ __device__ __forceinline__ void solve_body(const SolveParams& P, int bid, int nb
       while (go && pi < P.pcg_max) {
         const float alpha = alpha_d.x;
         const bool first = pi == 0;
-        double* rc_next = P.rc + (cur ^ 1) * P.NC;
         work_begin();
         for (int hs0 = 2 * wib; hs0 < ns; hs0 += 2 * kSolveWarps)
-          res_update(P, hs0 + half, hs0 + half < ns, alpha, beta, first, rc_next);
+          vc_update(P, hs0 + half, hs0 + half < ns, alpha, beta, first);
         work_end(1);
         if (!gs.sync()) return;
         ++pi;
-        cur ^= 1;
-        if (!phase2()) return;
-        if (!phase3(s3)) return;
+        if (!apply_m(s3)) return;
         rr = s3[2].x;
         if (rr <= tol2 || pi >= P.pcg_max) break;
         const float2 gam_new = s3[0];
