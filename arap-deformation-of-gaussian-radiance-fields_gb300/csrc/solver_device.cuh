@@ -1663,6 +1663,81 @@ __device__ __forceinline__ float pick12(const float (&v)[12], int c) {
   return x;
 }
 
+// w_con J_g v of constraint item ci of the CTA, in two steps so that its
+// global loads overlap the node products: group_issue loads the anchor row of
+// slot q8 of the group's member-anchor slots (eight lanes per item),
+// group_finish adds the remaining slots, reduces over the eight lanes and
+// stores the staged value.
+struct GroupLoad {
+  float v[12];
+  float4 geo;
+  bool has;
+};
+__device__ __forceinline__ void group_issue(const SolveParams& P, int ci, bool valid, GroupLoad& G) {
+  const int q8 = threadIdx.x & 7;
+  G.has = false;
+  G.geo = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+  for (int i = 0; i < 12; ++i) G.v[i] = 0.f;
+  if (!valid) return;
+  const int2 sr = stg_cgs()[ci];
+  if (q8 >= sr.y) return;
+  const int rk = stg_gsr()[sr.x + q8];
+  if (rk < 0) return;
+  G.geo = stg_gsg()[sr.x + q8];
+  ld12cg(P.z, rk, G.v);
+  G.has = true;
+}
+__device__ __forceinline__ void group_finish(const SolveParams& P, int ci, bool valid, const GroupLoad& G) {
+  const int q8 = threadIdx.x & 7;
+  const unsigned mask = 0xffu << (threadIdx.x & 24);
+  float u[3] = {0.f, 0.f, 0.f};
+  auto add = [&](const float4 geo, const float (&zl)[12]) {
+#pragma unroll
+    for (int c = 0; c < 3; ++c)
+      u[c] = fmaf(geo.x, fmaf(geo.y, zl[c], fmaf(geo.z, zl[3 + c], fmaf(geo.w, zl[6 + c], zl[9 + c]))), u[c]);
+  };
+  if (G.has) add(G.geo, G.v);
+  if (valid) {
+    const int2 sr = stg_cgs()[ci];
+    for (int e = q8 + 8; e < sr.y; e += 8) {
+      const int rk = stg_gsr()[sr.x + e];
+      if (rk < 0) continue;
+      float zl[12];
+      ld12cg(P.z, rk, zl);
+      add(stg_gsg()[sr.x + e], zl);
+    }
+  }
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+#pragma unroll
+    for (int o = 4; o > 0; o >>= 1) u[c] += __shfl_xor_sync(mask, u[c], o);
+  }
+  if (valid && q8 == 0) stg_cuz()[ci] = make_float4(P.wcf * u[0], P.wcf * u[1], P.wcf * u[2], 0.f);
+}
+
+// (J^T J)_{reg,static} v of resident slot s into slot vector RV_W (the
+// constraint and rotation rows are added by full_product_finish).
+static __device__ __noinline__ void reg_product_store(const SolveParams& P, int s, bool valid, int k) {
+  const int c = threadIdx.x & 15;
+  float acc[12];
+  reg_product(P, s, valid, k, acc);
+  if (valid && c < 12) stg_vec(s, RV_W)[c] = pick12(acc, c);
+}
+
+// Entry c of the full (J^T J) v of resident slot s: the stored
+// regularisation part, the constraint rows on the staged w_con J_g v, the
+// rotation block on v (slot vector k).
+__device__ __forceinline__ float full_product_finish(const SolveParams& P, int s, int k, int c) {
+  const int4 nd = stg_node()[s];
+  const int4 bs = stg_base()[s];
+  float v[12];
+  ld12s(stg_vec(s, k), v);
+  float a = stg_vec(s, RV_W)[c] + con_apply(P, nd, bs, c);
+  if (c < 9) a += rot_apply(s, c, v);
+  return a;
+}
+
 // Phase 1: p = u + beta p, s = w + beta s, h += alpha p, r -= alpha s,
 // z1 = D^-1 r for resident slot s; z1 and h also to global memory.
 static __device__ __noinline__ void vc_update(const SolveParams& P, int s, bool valid, float alpha, float beta,
@@ -1691,46 +1766,23 @@ static __device__ __noinline__ void vc_update(const SolveParams& P, int s, bool 
   }
 }
 
-// Phase 2, nodes: a1 = (J^T J)_{reg,static,rot} z1 of resident slot s (kept
-// in RV_WF) and the restriction of r - a1 into rc (the constraint rows are
-// restricted per group, vc_group_restrict).
-static __device__ __noinline__ void vc_products_z1(const SolveParams& P, int s, bool valid, double* rc) {
+// Phase 2, after the products: a1 = (J^T J) z1 of resident slot s (kept in
+// RV_WF) and the restriction of r - a1 into rc.
+static __device__ __noinline__ void vc_restrict(const SolveParams& P, int s, bool valid, double* rc) {
   const int c = threadIdx.x & 15;
-  float acc[12];
-  reg_product(P, s, valid, RV_UF, acc);
   float t = 0.f;
   if (valid && c < 12) {
-    float z1[12];
-    ld12s(stg_vec(s, RV_UF), z1);
-    float a1 = pick12(acc, c);
-    if (c < 9) a1 += rot_apply(s, c, z1);
+    const float a1 = full_product_finish(P, s, RV_UF, c);
     stg_vec(s, RV_WF)[c] = a1;
     t = stg_vec(s, RV_R)[c] - a1;
   }
   coarse_restrict_h_stg(s, valid, t, rc);
 }
 
-// Phase 2, groups: w_con J_g z1 of group g (one warp; to P.uzg) and the
-// restriction of its constraint rows, rc_a -= (J_g P_a)^T (w_con J_g z1).
-__device__ __forceinline__ void vc_group_restrict(const SolveParams& P, int g, double* rc) {
-  const int lane = threadIdx.x & 31;
-  float uz[3];
-  con_jz_group(P, g, uz);
-  if (lane >= 12) return;
-  const int blk = lane / 3, cc = lane - 3 * blk;
-  const float u = cc == 0 ? uz[0] : (cc == 1 ? uz[1] : uz[2]);
-  const int f0 = __ldg(P.gca_off + g), f1 = __ldg(P.gca_off + g + 1);
-  for (int f = f0; f < f1; ++f) {
-    const float4 V = __ldcg(P.gcv + f);
-    const float vb = blk == 0 ? V.x : (blk == 1 ? V.y : (blk == 2 ? V.z : V.w));
-    atomicAdd(rc + 12 * __ldg(P.gca + f) + lane, -(double)(P.wcf * vb * u));
-  }
-}
-
-// Phase 4: z2 = z1 + P zc, A z2 = a1 + constraint rows on w_con J_g z1 +
-// A P zc (coarse blocks, rotation block on P_j zc), z3 = D^-1 (r - A z2),
-// u = z2 + z3 for resident slot s.  Keeps u, A z2 (RV_WF) and z3 (RV_UF, also
-// to P.z for the neighbours).  zc entries and w_con J_g z1 must be staged.
+// Phase 4: z2 = z1 + P zc, A z2 = a1 + A P zc (coarse blocks, rotation block
+// on P_j zc), z3 = D^-1 (r - A z2), u = z2 + z3 for resident slot s.  Keeps
+// u, A z2 (RV_WF) and z3 (RV_UF, also to P.z for the neighbours).  The zc
+// entries must be staged.
 static __device__ __noinline__ void vc_precond(const SolveParams& P, int s, bool valid) {
   const int c = threadIdx.x & 15;
   float t = 0.f, z2 = 0.f, az2 = 0.f;
@@ -1764,7 +1816,7 @@ static __device__ __noinline__ void vc_precond(const SolveParams& P, int s, bool
     float apz = (wq[0] + wq[1]) + wq[2];
     if (c < 9) apz += rot_apply(s, c, zj);
     z2 = stg_vec(s, RV_UF)[c] + pz;
-    az2 = stg_vec(s, RV_WF)[c] + con_apply(P, nd, bs, c) + apz;
+    az2 = stg_vec(s, RV_WF)[c] + apz;
     t = stg_vec(s, RV_R)[c] - az2;
   }
   const float z3 = apply_dinv_h_stg(s, valid, t);
@@ -1776,55 +1828,18 @@ static __device__ __noinline__ void vc_precond(const SolveParams& P, int s, bool
   }
 }
 
-// Phase 5, groups: w_con J_g z3 for constraint item ci of the CTA (eight
-// lanes; the group's member-anchor slots are staged), into the staged slot.
-__device__ __forceinline__ void vc_group_z3(const SolveParams& P, int ci, bool valid) {
-  const int q8 = threadIdx.x & 7;
-  const unsigned mask = 0xffu << (threadIdx.x & 24);
-  float u[3] = {0.f, 0.f, 0.f};
-  if (valid) {
-    const int2 sr = stg_cgs()[ci];
-    for (int e = q8; e < sr.y; e += 8) {
-      const int rk = stg_gsr()[sr.x + e];
-      if (rk < 0) continue;
-      const float4 geo = stg_gsg()[sr.x + e];
-      float zl[12];
-      ld12cg(P.z, rk, zl);
-#pragma unroll
-      for (int c = 0; c < 3; ++c)
-        u[c] = fmaf(geo.x, fmaf(geo.y, zl[c], fmaf(geo.z, zl[3 + c], fmaf(geo.w, zl[6 + c], zl[9 + c]))), u[c]);
-    }
-  }
-#pragma unroll
-  for (int c = 0; c < 3; ++c) {
-#pragma unroll
-    for (int o = 4; o > 0; o >>= 1) u[c] += __shfl_xor_sync(mask, u[c], o);
-  }
-  if (valid && q8 == 0) stg_cuz()[ci] = make_float4(P.wcf * u[0], P.wcf * u[1], P.wcf * u[2], 0.f);
-}
-
-// Phase 5, nodes: A z3 = (J^T J)_{reg,static} z3 + constraint rows on
-// w_con J_g z3 + rotation block on z3; w = A z2 + A z3; adds r.u, w.u, r.r
-// into f3.
-static __device__ __noinline__ void vc_products(const SolveParams& P, int s, bool valid, float (&f3)[3]) {
+// Phase 5, after the products: w = A z2 + A z3 for resident slot s; adds
+// r.u, w.u and r.r into f3.
+static __device__ __noinline__ void vc_finish(const SolveParams& P, int s, bool valid, float (&f3)[3]) {
   const int c = threadIdx.x & 15;
-  float acc[12];
-  reg_product(P, s, valid, RV_UF, acc);
-  if (valid && c < 12) {
-    const int4 nd = stg_node()[s];
-    const int4 bs = stg_base()[s];
-    float z3[12];
-    ld12s(stg_vec(s, RV_UF), z3);
-    float az3 = pick12(acc, c) + con_apply(P, nd, bs, c);
-    if (c < 9) az3 += rot_apply(s, c, z3);
-    const float wv = stg_vec(s, RV_WF)[c] + az3;
-    const float uc = stg_vec(s, RV_U)[c];
-    const float rv = stg_vec(s, RV_R)[c];
-    stg_vec(s, RV_W)[c] = wv;
-    f3[0] = fmaf(rv, uc, f3[0]);
-    f3[1] = fmaf(wv, uc, f3[1]);
-    f3[2] = fmaf(rv, rv, f3[2]);
-  }
+  if (!valid || c >= 12) return;
+  const float wv = stg_vec(s, RV_WF)[c] + full_product_finish(P, s, RV_UF, c);
+  const float uc = stg_vec(s, RV_U)[c];
+  const float rv = stg_vec(s, RV_R)[c];
+  stg_vec(s, RV_W)[c] = wv;
+  f3[0] = fmaf(rv, uc, f3[0]);
+  f3[1] = fmaf(wv, uc, f3[1]);
+  f3[2] = fmaf(rv, rv, f3[2]);
 }
 
 // zc for the CTA's rows of the coarse inverse (resident mode): row j of the

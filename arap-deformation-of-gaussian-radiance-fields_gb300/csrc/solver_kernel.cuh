@@ -525,17 +525,35 @@ __device__ __forceinline__ void solve_body(const SolveParams& P, int bid, int nb
       // ---- two-level PCG with the CTA's nodes resident in shared memory and
       // the symmetric two-grid preconditioner (vc_* in solver_device.cuh):
       //   (1) update of own nodes, z1 = D^-1 r; plain barrier
-      //   (2) A z1 but its constraint rows, the restriction of r - A z1 (nodes,
-      //       and per group for the constraint rows); plain barrier
+      //   (2) A z1 and the restriction of r - A z1; plain barrier
       //   (3) zc = C^-1 P^T (r - A z1) over the CTA's rows of C^-1; plain barrier
       //   (4) z2 = z1 + P zc, A z2, z3 = D^-1 (r - A z2), u = z2 + z3; plain barrier
       //   (5) A z3, w = A z2 + A z3; gamma, delta, r.r in one reduction
       const int ns = s_stg.n;
+      // (J^T J) v of the CTA's nodes (v = slot vector RV_UF here and in P.z):
+      // the regularisation rows into RV_W, w_con J_g v of the CTA's constraint
+      // items into their staged slots; the first 64 items' loads are issued
+      // before the node products so that both take one round trip
+      auto full_products = [&]() {
+        const int qw = (int)(threadIdx.x >> 3);
+        const int ncon = s_stg.ncon;
+        GroupLoad G;
+        group_issue(P, qw, qw < ncon, G);
+        for (int hs0 = 2 * wib; hs0 < ns; hs0 += 2 * kSolveWarps) reg_product_store(P, hs0 + half, hs0 + half < ns, RV_UF);
+        group_finish(P, qw, qw < ncon, G);
+        for (int c0 = kSolveThreads / 8; c0 < ncon; c0 += kSolveThreads / 8) {
+          const int ci = c0 + qw;
+          GroupLoad G2;
+          group_issue(P, ci, ci < ncon, G2);
+          group_finish(P, ci, ci < ncon, G2);
+        }
+        __syncthreads();
+      };
       auto apply_m = [&](float2 (&s3)[3]) -> bool {
         double* rcw = P.rc + cur * P.NC;
         work_begin();
-        for (int hs0 = 2 * wib; hs0 < ns; hs0 += 2 * kSolveWarps) vc_products_z1(P, hs0 + half, hs0 + half < ns, rcw);
-        for (int g = nw - 1 - gw; g < P.G; g += nw) vc_group_restrict(P, g, rcw);
+        full_products();
+        for (int hs0 = 2 * wib; hs0 < ns; hs0 += 2 * kSolveWarps) vc_restrict(P, hs0 + half, hs0 + half < ns, rcw);
         work_end(2);
         if (!gs.sync()) return false;
         work_begin();
@@ -551,26 +569,19 @@ __device__ __forceinline__ void solve_body(const SolveParams& P, int bid, int nb
         work_end(2);
         if (!gs.sync()) return false;
         work_begin();
-        // zc of every coupled aggregate of the CTA's nodes, w_con J_g z1 of
-        // every constraint item
+        // zc of every coupled aggregate of the CTA's nodes
         for (int e = threadIdx.x; e < 12 * s_stg.nent; e += blockDim.x) {
           const int en = e / 12, i = e - 12 * en;
           stg_zz(en)[i] = __ldcg(P.zc + 12 * stg_mag()[en] + i);
         }
-        for (int e = threadIdx.x; e < s_stg.ncon; e += blockDim.x) stg_cuz()[e] = __ldcg(P.uzg + stg_cg()[e]);
         __syncthreads();
         for (int hs0 = 2 * wib; hs0 < ns; hs0 += 2 * kSolveWarps) vc_precond(P, hs0 + half, hs0 + half < ns);
         work_end(1);
         if (!gs.sync()) return false;
         work_begin();
-        // w_con J_g z3 of the CTA's constraint items, eight lanes each
-        for (int c0 = 0; c0 < s_stg.ncon; c0 += kSolveThreads / 8) {
-          const int ci = c0 + (int)(threadIdx.x >> 3);
-          vc_group_z3(P, ci, ci < s_stg.ncon);
-        }
-        __syncthreads();
+        full_products();
         float f3[3] = {0.f, 0.f, 0.f};
-        for (int hs0 = 2 * wib; hs0 < ns; hs0 += 2 * kSolveWarps) vc_products(P, hs0 + half, hs0 + half < ns, f3);
+        for (int hs0 = 2 * wib; hs0 < ns; hs0 += 2 * kSolveWarps) vc_finish(P, hs0 + half, hs0 + half < ns, f3);
         work_end(0);
         cur ^= 1;
         return gs.reduce_f<3>(f3, s3);
