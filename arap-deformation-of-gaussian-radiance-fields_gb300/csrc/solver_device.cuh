@@ -1132,215 +1132,12 @@ __device__ __forceinline__ void coarse_restrict(const SolveParams& P, int rr, fl
 }
 
 // ---------------------------------------------------- resident PCG ----
-// With every node of a CTA resident, (J^T J) u with u = u_f + P zc is taken
-// in two parts by linearity: w_f = (J^T J)_reg u_f (regularisation and
-// static-node rows, the neighbours' u_f from L2) in the coarse-solve phase,
-// and the rest in the products phase from shared memory only: the
-// regularisation rows on y = P zc (every node's y from zc and its offset),
-// the constraint rows on J_g u = w_con J_g u_f + sum_a V_ga zc_a, and the
-// rotation rows on u.  The vector update touches only the CTA's own nodes.
-
-// PCG vector update of resident slot s (half-warp; lane c < 12 owns entry c):
-// p = u + beta p, s = w + beta s, h += alpha p, r -= alpha s, u_f = Dinv r,
-// and the restriction of r into rc.  u_f and h also go to global memory
-// (neighbours' products, line search).
-static __device__ __noinline__ void res_update(const SolveParams& P, int s, bool valid, float alpha, float beta,
-                                           bool first, double* rc) {
-  const int l16 = threadIdx.x & 15;
-  const bool own = valid && l16 < 12;
-  float rv = 0.f, hv = 0.f;
-  int r = 0;
-  if (own) {
-    r = stg_node()[s].x;
-    const float uo = stg_vec(s, RV_U)[l16], wo = stg_vec(s, RV_W)[l16];
-    const float pn = first ? uo : fmaf(beta, stg_vec(s, RV_P)[l16], uo);
-    const float sn = first ? wo : fmaf(beta, stg_vec(s, RV_S)[l16], wo);
-    stg_vec(s, RV_P)[l16] = pn;
-    stg_vec(s, RV_S)[l16] = sn;
-    hv = fmaf(alpha, pn, stg_vec(s, RV_H)[l16]);
-    stg_vec(s, RV_H)[l16] = hv;
-    rv = fmaf(-alpha, sn, stg_vec(s, RV_R)[l16]);
-    stg_vec(s, RV_R)[l16] = rv;
-  }
-  const float zv = apply_dinv_h_stg(s, valid, rv);
-  coarse_restrict_h_stg(s, valid, rv, rc);
-  if (own) {
-    stg_vec(s, RV_UF)[l16] = zv;
-    P.z[12 * (size_t)r + l16] = zv;
-    P.h[12 * (size_t)r + l16] = hv;
-  }
-}
-
-// w_f = (J^T J)_reg u_f of resident slot s (regularisation and static-node
-// items; constraint items are left to res_products).  Lane c < 12 of the
-// half stores entry c.
-static __device__ __noinline__ void res_products_f(const SolveParams& P, int s, bool valid) {
-  const int lane = threadIdx.x & 15;
-  float acc[12], pj[12];
-#pragma unroll
-  for (int i = 0; i < 12; ++i) {
-    acc[i] = 0.f;
-    pj[i] = 0.f;
-  }
-  if (valid) {
-    const int4 nd = stg_node()[s];
-    const float4* u4 = reinterpret_cast<const float4*>(stg_vec(s, RV_UF));
-    const float4 a = u4[0], b = u4[1], c = u4[2];
-    pj[0] = a.x; pj[1] = a.y; pj[2] = a.z; pj[3] = a.w; pj[4] = b.x; pj[5] = b.y;
-    pj[6] = b.z; pj[7] = b.w; pj[8] = c.x; pj[9] = c.y; pj[10] = c.z; pj[11] = c.w;
-    const float w = P.wgf;
-    for (int q = lane; q < nd.z; q += 32) {
-      const bool hasB = q + 16 < nd.z;
-      CouplingData A, B;
-      auto fetch = [&](int i, CouplingData& D) {
-        const int4 m = stg_item()[i];
-        D.kind = m.x & 15;
-        D.aux = stg_geo()[i];
-#pragma unroll
-        for (int t = 0; t < 12; ++t) D.v[t] = 0.f;
-        if (D.kind == ITEM_IN) {
-          ld12cg(P.z, m.y, D.v);
-        } else if (D.kind == ITEM_OUT && m.y >= 0) {
-          float t3[3];
-          ld3t_cg(P.z, m.y, t3);
-          D.v[0] = t3[0];
-          D.v[1] = t3[1];
-          D.v[2] = t3[2];
-        }
-      };
-      fetch(nd.y + q, A);
-      if (hasB) fetch(nd.y + q + 16, B);
-      if (A.kind != ITEM_CON) apply_item(P, A, w, pj, acc);
-      if (hasB && B.kind != ITEM_CON) apply_item(P, B, w, pj, acc);
-    }
-  }
-#pragma unroll
-  for (int i = 0; i < 12; ++i) {
-#pragma unroll
-    for (int o = 8; o > 0; o >>= 1) acc[i] += __shfl_xor_sync(0xffffffffu, acc[i], o);
-  }
-  if (valid && lane < 12) {
-    float v = 0.f;
-#pragma unroll
-    for (int i = 0; i < 12; ++i)
-      if (i == lane) v = acc[i];
-    stg_vec(s, RV_WF)[lane] = v;
-  }
-}
-
-// The rest of w = (J^T J) u for resident slot s, from shared memory only
-// (s_zc and the staged w_con J_g u_f of the CTA's constraint items must be in
-// place): u = u_f + y, w = w_f + (J^T J)_reg y + constraint rows on J_g u +
-// rotation rows on u.  Stores u and w and adds r.u, w.u and r.r into f3
-// (lane c < 12 of the half owns entry c).
-static __device__ __noinline__ void res_products(const SolveParams& P, int s, bool valid, float (&f3)[3]) {
-  const int lane = threadIdx.x & 15;
-  const int base = threadIdx.x & 16;
-  float acc[12], y[12];
-#pragma unroll
-  for (int i = 0; i < 12; ++i) {
-    acc[i] = 0.f;
-    y[i] = 0.f;
-  }
-  float xr = 0.f;
-  if (valid) {
-    const int4 nd = stg_node()[s];
-    if (lane < 9) xr = stg_xf(s)[lane];
-    coarse_prolong_dp(stg_dpiv()[s], nd.w, y);
-    const float w = P.wgf;
-    const float wcf = P.wcf;
-    for (int q = lane; q < nd.z; q += 16) {
-      const int i = nd.y + q;
-      CouplingData D;
-      const int4 m = stg_item()[i];
-      D.kind = m.x & 15;
-      D.aux = stg_geo()[i];
-#pragma unroll
-      for (int t = 0; t < 12; ++t) D.v[t] = 0.f;
-      if (D.kind == ITEM_IN) {
-        coarse_prolong_dp(stg_ydp()[i], m.x >> 4, D.v);
-      } else if (D.kind == ITEM_OUT) {
-        if (m.y >= 0) {
-          float t3[3] = {0.f, 0.f, 0.f};
-          coarse_prolong_t(stg_ydp()[i], m.x >> 4, t3);
-          D.v[0] = t3[0];
-          D.v[1] = t3[1];
-          D.v[2] = t3[2];
-        }
-      } else if (D.kind == ITEM_CON) {
-        const float4 uz = stg_cuz()[m.x >> 4];
-        D.v[0] = uz.x;
-        D.v[1] = uz.y;
-        D.v[2] = uz.z;
-        for (int f = m.y; f < m.y + m.w; ++f) {
-          const float4 V = stg_lv()[f];
-          const float4* c4 = reinterpret_cast<const float4*>(s_zc + 12 * stg_la()[f]);
-          const float4 ca = c4[0], cb = c4[1], cc = c4[2];
-          const float C[12] = {ca.x, ca.y, ca.z, ca.w, cb.x, cb.y, cb.z, cb.w, cc.x, cc.y, cc.z, cc.w};
-#pragma unroll
-          for (int c = 0; c < 3; ++c)
-            D.v[c] = fmaf(wcf, fmaf(V.x, C[c], fmaf(V.y, C[3 + c], fmaf(V.z, C[6 + c], V.w * C[9 + c]))), D.v[c]);
-        }
-      }
-      apply_item(P, D, w, y, acc);
-    }
-  }
-  // u = u_f + y for the rotation rows
-  float uj[12];
-  {
-    const float4* u4 = reinterpret_cast<const float4*>(stg_vec(valid ? s : 0, RV_UF));
-    const float4 a = u4[0], b = u4[1], c = u4[2];
-    const float uf[12] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w, c.x, c.y, c.z, c.w};
-#pragma unroll
-    for (int i = 0; i < 12; ++i) uj[i] = uf[i] + y[i];
-  }
-  float X[9];
-#pragma unroll
-  for (int i = 0; i < 9; ++i) X[i] = __shfl_sync(0xffffffffu, xr, base + i);
-  if (valid && lane == 0) {
-    const float* c0 = X;
-    const float* c1 = X + 3;
-    const float* c2 = X + 6;
-    const float* p0 = uj;
-    const float* p1 = uj + 3;
-    const float* p2 = uj + 6;
-    const float wr = P.wrf;
-    auto dot = [](const float* a3, const float* b3) { return a3[0] * b3[0] + a3[1] * b3[1] + a3[2] * b3[2]; };
-    const float u0 = wr * (dot(c1, p0) + dot(c0, p1));
-    const float u1 = wr * (dot(c2, p0) + dot(c0, p2));
-    const float u2 = wr * (dot(c2, p1) + dot(c1, p2));
-    const float u3 = 2.f * wr * dot(c0, p0);
-    const float u4 = 2.f * wr * dot(c1, p1);
-    const float u5 = 2.f * wr * dot(c2, p2);
-#pragma unroll
-    for (int i = 0; i < 3; ++i) {
-      acc[i] += wr * (u0 * c1[i] + u1 * c2[i] + 2.f * u3 * c0[i]);
-      acc[3 + i] += wr * (u0 * c0[i] + u2 * c2[i] + 2.f * u4 * c1[i]);
-      acc[6 + i] += wr * (u1 * c0[i] + u2 * c1[i] + 2.f * u5 * c2[i]);
-    }
-  }
-#pragma unroll
-  for (int i = 0; i < 12; ++i) {
-#pragma unroll
-    for (int o = 8; o > 0; o >>= 1) acc[i] += __shfl_xor_sync(0xffffffffu, acc[i], o);
-  }
-  if (valid && lane < 12) {
-    float uc = 0.f, wv = 0.f;
-#pragma unroll
-    for (int i = 0; i < 12; ++i)
-      if (i == lane) {
-        uc = uj[i];
-        wv = acc[i];
-      }
-    wv += stg_vec(s, RV_WF)[lane];
-    const float rv = stg_vec(s, RV_R)[lane];
-    stg_vec(s, RV_U)[lane] = uc;
-    stg_vec(s, RV_W)[lane] = wv;
-    f3[0] = fmaf(rv, uc, f3[0]);
-    f3[1] = fmaf(wv, uc, f3[1]);
-    f3[2] = fmaf(rv, rv, f3[2]);
-  }
-}
+// With every node of a CTA resident, the CTA's nodes keep their PCG vectors
+// in shared memory, and A P zc of a node comes from its coarse blocks: per
+// aggregate coupled to it, the 12x12 block of (J^T J)_{reg,static,con} P
+// restricted to that aggregate (built once per solve), plus its rotation
+// block on P_j zc.  The products of fine vectors (A z1, A z3 of the V-cycle
+// below) read the neighbours' vectors from L2.
 
 // P_k e_i: the prolongation of coarse unknown i of node k's own aggregate
 // (coarse_prolong_dp with zc = e_i): identity on the rotation part, and
@@ -1471,91 +1268,6 @@ __device__ __forceinline__ void rot_block(const SolveParams& P, int s) {
     row[b] = v;
   }
   row[9] = row[10] = row[11] = 0.f;
-}
-
-// The rest of w = (J^T J) u for resident slot s from the coarse blocks (lane
-// c < 12 of the half computes entry c; the zc of every coupled aggregate and
-// the w_con J_g u_f of every constraint item must be staged): w = w_f +
-// sum_a M_a zc_a + constraint rows on w_con J_g u_f + rotation block on u,
-// with u = u_f + P_j zc (the node's own aggregate is its first entry).
-// Every shared-memory address follows from the two node records, so a call
-// costs two dependent shared-memory round trips plus its FMA chains.
-__device__ __forceinline__ void res_products_m(const SolveParams& P, int s, bool valid, float (&f3)[3]) {
-  const int c = threadIdx.x & 15;
-  if (!valid || c >= 12) return;
-  const int4 nd = stg_node()[s];
-  const int4 bs = stg_base()[s];
-  const int ncon = bs.z & 0xffff, na = bs.z >> 16;
-  float wv = stg_vec(s, RV_WF)[c];
-  // three accumulators (one per float4 of a row) keep the FMA chains short
-  float wq[3] = {0.f, 0.f, 0.f};
-#pragma unroll 4
-  for (int t = 0; t < na; ++t) {
-    const float4* m4 = reinterpret_cast<const float4*>(stg_mm(bs.w + t) + 12 * c);
-    const float4* z4 = reinterpret_cast<const float4*>(stg_zz(bs.w + t));
-#pragma unroll
-    for (int q = 0; q < 3; ++q) {
-      const float4 mq = m4[q], zq = z4[q];
-      wq[q] = fmaf(mq.x, zq.x, fmaf(mq.y, zq.y, fmaf(mq.z, zq.z, fmaf(mq.w, zq.w, wq[q]))));
-    }
-  }
-  wv += (wq[0] + wq[1]) + wq[2];
-  // constraint rows on w_con J_g u_f (apply_item's ITEM_CON with D.v = the
-  // staged value); the node's constraint items are its last ncon items and
-  // consecutive in the CTA's constraint list
-  const int g3 = c / 3, cc = c - 3 * g3;
-  const int c0 = nd.y + nd.z - ncon;
-#pragma unroll 2
-  for (int q = 0; q < ncon; ++q) {
-    const float4 ax = stg_geo()[c0 + q];
-    const float4 uz = stg_cuz()[bs.y + q];
-    const float wa = P.wcf * ax.x;
-    const float coef = g3 == 0 ? ax.y : (g3 == 1 ? ax.z : (g3 == 2 ? ax.w : 1.f));
-    const float uzc = cc == 0 ? uz.x : (cc == 1 ? uz.y : uz.z);
-    wv = fmaf(wa * coef, uzc, wv);
-  }
-  // u = u_f + P_j zc of the node's own aggregate
-  const float4* uf4 = reinterpret_cast<const float4*>(stg_vec(s, RV_UF));
-  const float4* zj4 = reinterpret_cast<const float4*>(stg_zz(bs.w));
-  const float4 ua = uf4[0], ub = uf4[1], uc4 = uf4[2];
-  const float4 za = zj4[0], zb = zj4[1], zc4 = zj4[2];
-  const float uf[12] = {ua.x, ua.y, ua.z, ua.w, ub.x, ub.y, ub.z, ub.w, uc4.x, uc4.y, uc4.z, uc4.w};
-  const float zj[12] = {za.x, za.y, za.z, za.w, zb.x, zb.y, zb.z, zb.w, zc4.x, zc4.y, zc4.z, zc4.w};
-  float ucv = 0.f, ufc = 0.f;
-#pragma unroll
-  for (int i = 0; i < 12; ++i)
-    if (i == c) ufc = uf[i];
-  if (c < 9) {
-#pragma unroll
-    for (int i = 0; i < 9; ++i)
-      if (i == c) ucv = ufc + zj[i];
-    const float4* R4 = reinterpret_cast<const float4*>(stg_rot(s) + 12 * c);
-    const float4 ra = R4[0], rb = R4[1], rc = R4[2];
-    const float R[9] = {ra.x, ra.y, ra.z, ra.w, rb.x, rb.y, rb.z, rb.w, rc.x};
-    float rot = 0.f;
-#pragma unroll
-    for (int i = 0; i < 9; ++i) rot = fmaf(R[i], uf[i] + zj[i], rot);
-    wv += rot;
-  } else {
-    const float4 dp = stg_dpiv()[s];
-    const int r = c - 9;
-    float z9 = 0.f, z0 = 0.f, z3 = 0.f, z6 = 0.f;
-#pragma unroll
-    for (int i = 0; i < 3; ++i)
-      if (i == r) {
-        z9 = zj[9 + i];
-        z0 = zj[i];
-        z3 = zj[3 + i];
-        z6 = zj[6 + i];
-      }
-    ucv = ufc + (z9 + dp.x * z0 + dp.y * z3 + dp.z * z6);
-  }
-  const float rv = stg_vec(s, RV_R)[c];
-  stg_vec(s, RV_U)[c] = ucv;
-  stg_vec(s, RV_W)[c] = wv;
-  f3[0] = fmaf(rv, ucv, f3[0]);
-  f3[1] = fmaf(wv, ucv, f3[1]);
-  f3[2] = fmaf(rv, rv, f3[2]);
 }
 
 // ------------------------------------------- V-cycle preconditioner ----
