@@ -173,7 +173,7 @@ def restore(st, snap):
 # DRAM bytes per launch of skin_gaussians_kernel measured by ncu on the named
 # workload (dram__bytes_read.sum + dram__bytes_write.sum of one launch), keyed
 # by (scene, k, planned).
-SKIN_DRAM_BYTES = {}
+SKIN_DRAM_BYTES = {("twist300k", 8, True): 165792000 + 42921728}
 
 
 def skin_bytes_per_gaussian(k, with_shs=True, with_cov=True, planned=True):
