@@ -658,9 +658,17 @@ struct arap_solver_batch {
   int precision = 0;
   int grid = 0;                 // co-resident CTAs of the batched kernel
   float exponent = 1.f;         // CTA share ~ (coupling items + free nodes)^exponent
-  std::vector<int> cta_first;   // [count+1]
+  // Waves: launches that each run a group of instances on the whole grid.
+  // Instances whose nodes fit in shared memory on some number of CTAs (the
+  // resident two-level PCG) are packed into waves by that minimum, largest
+  // first; the others share one wave.  Position p of the parameter array is
+  // instance order[p]; wave w covers positions wave_first[w] ..
+  // wave_first[w+1]-1, and its CTA ranges are cta_local[wave_first[w] + w ..]
+  // (n_w + 1 entries).
+  std::vector<int> order, wave_first, cta_local, wave_cap;
+  std::vector<int> ctas;        // per instance: its CTAs
+  std::vector<size_t> part_off; // per instance: offset of its barrier partials
   int stage_limit = 0;          // shared-memory limit of the batched kernel's resident tables
-  int stage_cap = 0;            // dynamic shared memory of a batched launch
   std::vector<int> resident;    // per instance: resident mode (see plan_stage)
   void* block = nullptr;        // device: params, cta_first, barriers, partials
   SolveParams* d_params = nullptr;
@@ -674,45 +682,112 @@ struct arap_solver_batch {
 
 namespace {
 
-// CTA ranges of a batch: every instance gets at least one CTA, the rest in
-// proportion to its work estimate raised to the exponent (largest remainders).
-void split_ctas(arap_solver_batch* b) {
-  const int count = (int)b->solvers.size();
-  std::vector<double> w(count);
-  double sum = 0.0;
-  for (int i = 0; i < count; ++i) {
-    const arap_solver* s = b->solvers[i];
-    w[i] = std::pow((double)(s->n_items + s->F) + 1.0, (double)b->exponent);
-    sum += w[i];
+// Fewest CTAs on which solver s runs resident (all its nodes, with their PCG
+// vectors, in shared memory), or -1 when no share of the grid suffices.
+int resident_min_ctas(const arap_solver* s, int grid, int limit) {
+  if (s->res_cost.empty() || !plan_stage(s, grid, limit).resident) return -1;
+  int lo = 1, hi = grid;  // resident at hi; more CTAs never hurt
+  while (lo < hi) {
+    const int mid = (lo + hi) / 2;
+    if (plan_stage(s, mid, limit).resident)
+      hi = mid;
+    else
+      lo = mid + 1;
   }
-  const int spare = b->grid - count;
-  std::vector<int> n(count, 1);
-  std::vector<std::pair<double, int>> rem(count);
+  return lo;
+}
+
+// Adds the grid's spare CTAs to the instances of one wave in proportion to
+// their work estimate raised to the exponent (largest remainders).
+void share_spare(const arap_solver_batch* b, const std::vector<int>& inst, std::vector<int>& n, int spare) {
+  const int m = (int)inst.size();
+  if (m == 0 || spare <= 0) return;
+  std::vector<double> w(m);
+  double sum = 0.0;
+  for (int q = 0; q < m; ++q) {
+    const arap_solver* s = b->solvers[inst[q]];
+    w[q] = std::pow((double)(s->n_items + s->F) + 1.0, (double)b->exponent);
+    sum += w[q];
+  }
+  std::vector<std::pair<double, int>> rem(m);
   int given = 0;
-  for (int i = 0; i < count; ++i) {
-    const double share = spare * w[i] / sum;
+  for (int q = 0; q < m; ++q) {
+    const double share = spare * w[q] / sum;
     const int whole = (int)std::floor(share);
-    n[i] += whole;
+    n[q] += whole;
     given += whole;
-    rem[i] = {-(share - whole), i};
+    rem[q] = {-(share - whole), q};
   }
   std::sort(rem.begin(), rem.end());
-  for (int q = 0; q < spare - given; ++q) n[rem[q % count].second] += 1;
-  b->cta_first.assign(count + 1, 0);
-  for (int i = 0; i < count; ++i) b->cta_first[i + 1] = b->cta_first[i] + n[i];
-  b->stage_cap = 0;
-  b->resident.assign(count, 0);
+  for (int q = 0; q < spare - given; ++q) n[rem[q % m].second] += 1;
+}
+
+// Waves and CTA ranges of a batch (see arap_solver_batch).
+void split_ctas(arap_solver_batch* b) {
+  const int count = (int)b->solvers.size();
+  std::vector<int> need(count);
+  std::vector<int> res_inst, other;
   for (int i = 0; i < count; ++i) {
-    const StagePlan sp = plan_stage(b->solvers[i], n[i], b->stage_limit);
-    b->stage_cap = std::max(b->stage_cap, sp.bytes);
-    b->resident[i] = sp.resident;
+    need[i] = resident_min_ctas(b->solvers[i], b->grid, b->stage_limit);
+    (need[i] > 0 ? res_inst : other).push_back(i);
+  }
+  std::stable_sort(res_inst.begin(), res_inst.end(), [&](int x, int y) { return need[x] > need[y]; });
+  // first fit, largest first
+  std::vector<std::vector<int>> waves;
+  std::vector<int> used;
+  for (int i : res_inst) {
+    size_t w = 0;
+    while (w < waves.size() && used[w] + need[i] > b->grid) ++w;
+    if (w == waves.size()) {
+      waves.emplace_back();
+      used.push_back(0);
+    }
+    waves[w].push_back(i);
+    used[w] += need[i];
+  }
+  if (!other.empty()) {
+    waves.push_back(other);
+    used.push_back(0);
+  }
+  b->order.clear();
+  b->wave_first.assign(1, 0);
+  b->cta_local.clear();
+  b->wave_cap.clear();
+  b->ctas.assign(count, 0);
+  b->resident.assign(count, 0);
+  b->part_off.assign(count, 0);
+  size_t poff = 0;
+  for (auto& wv : waves) {
+    std::vector<int> n(wv.size());
+    int base = 0;
+    for (size_t q = 0; q < wv.size(); ++q) {
+      n[q] = need[wv[q]] > 0 ? need[wv[q]] : 1;
+      base += n[q];
+    }
+    share_spare(b, wv, n, b->grid - base);
+    int cap = 0, first = 0;
+    b->cta_local.push_back(0);
+    for (size_t q = 0; q < wv.size(); ++q) {
+      const int i = wv[q];
+      const StagePlan sp = plan_stage(b->solvers[i], n[q], b->stage_limit);
+      cap = std::max(cap, sp.bytes);
+      b->resident[i] = sp.resident;
+      b->ctas[i] = n[q];
+      b->part_off[i] = poff;
+      poff += (size_t)2 * kReduceSlots * n[q];
+      b->order.push_back(i);
+      first += n[q];
+      b->cta_local.push_back(first);
+    }
+    b->wave_cap.push_back(cap);
+    b->wave_first.push_back((int)b->order.size());
   }
 }
 
 // The CTA ranges go to the device when they change (creation, autotuning),
 // never inside a solve, so a solve can be captured in a CUDA graph.
 int upload_ctas(arap_solver_batch* b) {
-  if (cudaMemcpy(b->d_cta_first, b->cta_first.data(), sizeof(int) * b->cta_first.size(), cudaMemcpyHostToDevice) !=
+  if (cudaMemcpy(b->d_cta_first, b->cta_local.data(), sizeof(int) * b->cta_local.size(), cudaMemcpyHostToDevice) !=
       cudaSuccess) {
     (void)cudaGetLastError();
     return ARAP_ECUDA;
@@ -761,9 +836,9 @@ extern "C" int arap_solver_batch_create(arap_solver_batch** out, arap_solver* co
   Carver sizing{nullptr};
   auto carve = [&](Carver& cv) {
     b->d_params = cv.take<SolveParams>(count);
-    b->d_cta_first = cv.take<int>(count + 1);
+    b->d_cta_first = cv.take<int>(2 * count);
     b->d_bars = cv.take<GridBarrier>(count);
-    b->d_partials = cv.take<double>((size_t)2 * kReduceSlots * b->grid);
+    b->d_partials = cv.take<double>((size_t)2 * kReduceSlots * b->grid * count);
   };
   carve(sizing);
   if (cudaMalloc(&b->block, sizing.off + 256) != cudaSuccess ||
@@ -795,7 +870,11 @@ extern "C" int arap_solver_batch_solve(arap_solver_batch* b, const float* const*
   ARAP_CUDA_TRY(cudaStreamIsCapturing(st, &cap));
   // the previous upload of the staging array must have been read before it is rewritten
   if (b->staged_valid && cap == cudaStreamCaptureStatusNone) ARAP_CUDA_TRY(cudaEventSynchronize(b->staged));
-  for (int i = 0; i < count; ++i) {
+  std::vector<int> wave_of(count, 0);
+  for (size_t w = 0; w + 1 < b->wave_first.size(); ++w)
+    for (int p = b->wave_first[w]; p < b->wave_first[w + 1]; ++p) wave_of[b->order[p]] = (int)w;
+  for (int p = 0; p < count; ++p) {
+    const int i = b->order[p];
     SolveParams P = b->solvers[i]->P;
     P.node_pos = node_pos[i];
     P.aims = aims[i];
@@ -805,10 +884,10 @@ extern "C" int arap_solver_batch_solve(arap_solver_batch* b, const float* const*
     P.x_in = nullptr;
     P.grad_out = nullptr;
     P.bar = b->d_bars + i;
-    P.partials = b->d_partials + (size_t)2 * kReduceSlots * b->cta_first[i];
-    P.stage_cap = b->stage_cap;
+    P.partials = b->d_partials + b->part_off[i];
+    P.stage_cap = b->wave_cap[wave_of[i]];
     P.resident = b->resident[i];
-    b->h_params[i] = P;
+    b->h_params[p] = P;
   }
   ARAP_CUDA_TRY(cudaMemcpyAsync(b->d_params, b->h_params, sizeof(SolveParams) * count, cudaMemcpyHostToDevice, st));
   if (cap == cudaStreamCaptureStatusNone) {
@@ -816,17 +895,19 @@ extern "C" int arap_solver_batch_solve(arap_solver_batch* b, const float* const*
     b->staged_valid = true;
   }
   ARAP_CUDA_TRY(cudaMemsetAsync(b->d_bars, 0, sizeof(GridBarrier) * count, st));
-  void* args[] = {&b->d_params, &b->d_cta_first, const_cast<int*>(&count)};
-  cudaError_t e;
-  if (b->precision == ARAP_PRECISION_MIXED)
-    e = cudaLaunchCooperativeKernel((const void*)gn_solve_batch_kernel<double>, b->grid, kSolveThreads, args,
-                                    (size_t)b->stage_cap, st);
-  else
-    e = cudaLaunchCooperativeKernel((const void*)gn_solve_batch_kernel<float>, b->grid, kSolveThreads, args,
-                                    (size_t)b->stage_cap, st);
-  if (e != cudaSuccess) {
-    (void)cudaGetLastError();
-    return ARAP_ECUDA;
+  const void* fn = b->precision == ARAP_PRECISION_MIXED ? (const void*)gn_solve_batch_kernel<double>
+                                                        : (const void*)gn_solve_batch_kernel<float>;
+  for (size_t w = 0; w + 1 < b->wave_first.size(); ++w) {
+    const int p0 = b->wave_first[w];
+    int nw = b->wave_first[w + 1] - p0;
+    const SolveParams* prm = b->d_params + p0;
+    const int* cf = b->d_cta_first + p0 + (int)w;
+    const int grid = b->cta_local[p0 + (int)w + nw];
+    void* args[] = {&prm, &cf, &nw};
+    if (cudaLaunchCooperativeKernel(fn, grid, kSolveThreads, args, (size_t)b->wave_cap[w], st) != cudaSuccess) {
+      (void)cudaGetLastError();
+      return ARAP_ECUDA;
+    }
   }
   if (!stats_host) return ARAP_OK;
   std::vector<double> st8((size_t)kStatSlots * count);
@@ -892,7 +973,9 @@ extern "C" int arap_solver_batch_autotune(arap_solver_batch* b, const float* con
 
 extern "C" int arap_solver_batch_ctas(const arap_solver_batch* b, int32_t* cta_first_host) {
   if (!b || !cta_first_host) return ARAP_EBADINPUT;
-  std::copy(b->cta_first.begin(), b->cta_first.end(), cta_first_host);
+  // prefix sums of the CTAs each instance gets in its wave
+  cta_first_host[0] = 0;
+  for (size_t i = 0; i < b->ctas.size(); ++i) cta_first_host[i + 1] = cta_first_host[i] + b->ctas[i];
   return ARAP_OK;
 }
 

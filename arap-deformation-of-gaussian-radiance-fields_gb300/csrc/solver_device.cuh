@@ -1479,23 +1479,45 @@ static __device__ __noinline__ void vc_update(const SolveParams& P, int s, bool 
 }
 
 // Phase 2, after the products: a1 = (J^T J) z1 of resident slot s (kept in
-// RV_WF) and the restriction of r - a1 into rc.
-static __device__ __noinline__ void vc_restrict(const SolveParams& P, int s, bool valid, double* rc) {
+// RV_WF) and the restriction of r - a1 into rc (of r in the additive form,
+// vc = false).
+static __device__ __noinline__ void vc_restrict(const SolveParams& P, int s, bool valid, double* rc, bool vc) {
   const int c = threadIdx.x & 15;
   float t = 0.f;
   if (valid && c < 12) {
     const float a1 = full_product_finish(P, s, RV_UF, c);
     stg_vec(s, RV_WF)[c] = a1;
-    t = stg_vec(s, RV_R)[c] - a1;
+    t = stg_vec(s, RV_R)[c] - (vc ? a1 : 0.f);
   }
   coarse_restrict_h_stg(s, valid, t, rc);
+}
+
+// Restart of the resident PCG (after a V-cycle breakdown): r from the
+// gradient pass (P.r), h = 0, z1 = D^-1 r, for resident slot s.
+static __device__ __noinline__ void vc_restart(const SolveParams& P, int s, bool valid) {
+  const int c = threadIdx.x & 15;
+  const bool own = valid && c < 12;
+  float rv = 0.f;
+  int r = 0;
+  if (own) {
+    r = stg_node()[s].x;
+    rv = __ldcg(P.r + 12 * (size_t)r + c);
+    stg_vec(s, RV_R)[c] = rv;
+    stg_vec(s, RV_H)[c] = 0.f;
+  }
+  const float zv = apply_dinv_h_stg(s, valid, rv);
+  if (own) {
+    stg_vec(s, RV_UF)[c] = zv;
+    P.z[12 * (size_t)r + c] = zv;
+    P.h[12 * (size_t)r + c] = 0.f;
+  }
 }
 
 // Phase 4: z2 = z1 + P zc, A z2 = a1 + A P zc (coarse blocks, rotation block
 // on P_j zc), z3 = D^-1 (r - A z2), u = z2 + z3 for resident slot s.  Keeps
 // u, A z2 (RV_WF) and z3 (RV_UF, also to P.z for the neighbours).  The zc
 // entries must be staged.
-static __device__ __noinline__ void vc_precond(const SolveParams& P, int s, bool valid) {
+static __device__ __noinline__ void vc_precond(const SolveParams& P, int s, bool valid, bool vc) {
   const int c = threadIdx.x & 15;
   float t = 0.f, z2 = 0.f, az2 = 0.f;
   int r = 0;
@@ -1529,7 +1551,7 @@ static __device__ __noinline__ void vc_precond(const SolveParams& P, int s, bool
     if (c < 9) apz += rot_apply(s, c, zj);
     z2 = stg_vec(s, RV_UF)[c] + pz;
     az2 = stg_vec(s, RV_WF)[c] + apz;
-    t = stg_vec(s, RV_R)[c] - az2;
+    t = vc ? stg_vec(s, RV_R)[c] - az2 : 0.f;
   }
   const float z3 = apply_dinv_h_stg(s, valid, t);
   if (valid && c < 12) {
@@ -1538,6 +1560,20 @@ static __device__ __noinline__ void vc_precond(const SolveParams& P, int s, bool
     stg_vec(s, RV_UF)[c] = z3;
     P.z[12 * (size_t)r + c] = z3;
   }
+}
+
+// The additive form's last step (no post-smoothing, z3 = 0): w = A z2 for
+// resident slot s; adds r.u, w.u and r.r into f3.
+static __device__ __noinline__ void vc_finish_additive(const SolveParams& P, int s, bool valid, float (&f3)[3]) {
+  const int c = threadIdx.x & 15;
+  if (!valid || c >= 12) return;
+  const float wv = stg_vec(s, RV_WF)[c];
+  const float uc = stg_vec(s, RV_U)[c];
+  const float rv = stg_vec(s, RV_R)[c];
+  stg_vec(s, RV_W)[c] = wv;
+  f3[0] = fmaf(rv, uc, f3[0]);
+  f3[1] = fmaf(wv, uc, f3[1]);
+  f3[2] = fmaf(rv, rv, f3[2]);
 }
 
 // Phase 5, after the products: w = A z2 + A z3 for resident slot s; adds

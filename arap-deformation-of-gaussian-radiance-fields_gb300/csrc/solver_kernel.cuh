@@ -549,11 +549,13 @@ __device__ __forceinline__ void solve_body(const SolveParams& P, int bid, int nb
         }
         __syncthreads();
       };
-      auto apply_m = [&](float2 (&s3)[3]) -> bool {
+      // vc: the V-cycle; otherwise the additive form D^-1 + P C^-1 P^T on the
+      // same phases (restriction of r, no post-smoothing, no phase 5)
+      auto apply_m = [&](float2 (&s3)[3], bool vc) -> bool {
         double* rcw = P.rc + cur * P.NC;
         work_begin();
         full_products();
-        for (int hs0 = 2 * wib; hs0 < ns; hs0 += 2 * kSolveWarps) vc_restrict(P, hs0 + half, hs0 + half < ns, rcw);
+        for (int hs0 = 2 * wib; hs0 < ns; hs0 += 2 * kSolveWarps) vc_restrict(P, hs0 + half, hs0 + half < ns, rcw, vc);
         work_end(2);
         if (!gs.sync()) return false;
         work_begin();
@@ -575,44 +577,67 @@ __device__ __forceinline__ void solve_body(const SolveParams& P, int bid, int nb
           stg_zz(en)[i] = __ldcg(P.zc + 12 * stg_mag()[en] + i);
         }
         __syncthreads();
-        for (int hs0 = 2 * wib; hs0 < ns; hs0 += 2 * kSolveWarps) vc_precond(P, hs0 + half, hs0 + half < ns);
-        work_end(1);
-        if (!gs.sync()) return false;
-        work_begin();
-        full_products();
+        for (int hs0 = 2 * wib; hs0 < ns; hs0 += 2 * kSolveWarps) vc_precond(P, hs0 + half, hs0 + half < ns, vc);
         float f3[3] = {0.f, 0.f, 0.f};
-        for (int hs0 = 2 * wib; hs0 < ns; hs0 += 2 * kSolveWarps) vc_finish(P, hs0 + half, hs0 + half < ns, f3);
-        work_end(0);
+        if (vc) {
+          work_end(1);
+          if (!gs.sync()) return false;
+          work_begin();
+          full_products();
+          for (int hs0 = 2 * wib; hs0 < ns; hs0 += 2 * kSolveWarps) vc_finish(P, hs0 + half, hs0 + half < ns, f3);
+          work_end(0);
+        } else {
+          for (int hs0 = 2 * wib; hs0 < ns; hs0 += 2 * kSolveWarps)
+            vc_finish_additive(P, hs0 + half, hs0 + half < ns, f3);
+          work_end(1);
+        }
         cur ^= 1;
         return gs.reduce_f<3>(f3, s3);
       };
-      float2 s3[3];
-      if (!apply_m(s3)) return;
-      float2 gam = s3[0];
-      rr = s3[2].x;
-      bool go = rr > tol2 && gam.x > 0.f && s3[1].x > 0.f;
-      float2 alpha_d = go ? dd_div(gam, s3[1]) : make_float2(0.f, 0.f);
-      float beta = 0.f;
-      while (go && pi < P.pcg_max) {
-        const float alpha = alpha_d.x;
-        const bool first = pi == 0;
-        work_begin();
-        for (int hs0 = 2 * wib; hs0 < ns; hs0 += 2 * kSolveWarps)
-          vc_update(P, hs0 + half, hs0 + half < ns, alpha, beta, first);
-        work_end(1);
-        if (!gs.sync()) return;
-        ++pi;
-        if (!apply_m(s3)) return;
+      // The V-cycle is positive definite only while the block-Jacobi smoother
+      // converges (rho(D^-1 A) < 2; about 6 on some constraint-centre
+      // problems).  A breakdown (gamma or the C-G denominator not positive
+      // before convergence; the same bits in every CTA) restarts this step's
+      // PCG with the additive form, which is always positive definite.
+      for (int vc = 1; vc >= 0; --vc) {
+        bool broke = false;
+        float2 s3[3];
+        if (!apply_m(s3, vc != 0)) return;
+        float2 gam = s3[0];
         rr = s3[2].x;
-        if (rr <= tol2 || pi >= P.pcg_max) break;
-        const float2 gam_new = s3[0];
-        if (!(gam_new.x > 0.f)) break;
-        const float2 bd = dd_div(gam_new, gam);
-        const float2 den = dd_sub(s3[1], dd_div(dd_mul(bd, gam_new), alpha_d));
-        if (!(den.x > 0.f)) break;
-        beta = bd.x;
-        alpha_d = dd_div(gam_new, den);
-        gam = gam_new;
+        bool go = rr > tol2 && gam.x > 0.f && s3[1].x > 0.f;
+        broke = !go && rr > tol2;
+        float2 alpha_d = go ? dd_div(gam, s3[1]) : make_float2(0.f, 0.f);
+        float beta = 0.f;
+        for (int kk = 0; go && pi < P.pcg_max; ++kk) {
+          const float alpha = alpha_d.x;
+          work_begin();
+          for (int hs0 = 2 * wib; hs0 < ns; hs0 += 2 * kSolveWarps)
+            vc_update(P, hs0 + half, hs0 + half < ns, alpha, beta, kk == 0);
+          work_end(1);
+          if (!gs.sync()) return;
+          ++pi;
+          if (!apply_m(s3, vc != 0)) return;
+          rr = s3[2].x;
+          if (rr <= tol2 || pi >= P.pcg_max) break;
+          const float2 gam_new = s3[0];
+          if (!(gam_new.x > 0.f)) {
+            broke = true;
+            break;
+          }
+          const float2 bd = dd_div(gam_new, gam);
+          const float2 den = dd_sub(s3[1], dd_div(dd_mul(bd, gam_new), alpha_d));
+          if (!(den.x > 0.f)) {
+            broke = true;
+            break;
+          }
+          beta = bd.x;
+          alpha_d = dd_div(gam_new, den);
+          gam = gam_new;
+        }
+        if (!broke || !vc) break;
+        for (int hs0 = 2 * wib; hs0 < ns; hs0 += 2 * kSolveWarps) vc_restart(P, hs0 + half, hs0 + half < ns);
+        if (!gs.sync()) return;
       }
     } else {
     if (coarse) {

@@ -148,10 +148,14 @@ def test_energy_grad(dev, scene, precision, centre):
     assert H.rel_err(_np(g), gr) <= tol
 
 
-def test_solve_centre_mode_and_weighting(dev):
+@pytest.mark.parametrize("coarse", [0, 32])
+def test_solve_centre_mode_and_weighting(dev, coarse):
     # centre mode needs non-collinear block centroids: with two blocks the
     # rotation about the line through both centroids is free and J^T J is
-    # singular (for the reference's Cholesky as for any solver)
+    # singular (for the reference's Cholesky as for any solver).  The
+    # two-level solve runs at its default PCG tolerance: on this
+    # ill-conditioned system a 1e-7 target is below what the FP32 PCG vectors
+    # resolve (measured: 8.6e-7 at 1e-6, 1.2e-5 at 1e-7)
     from oracle import ed
     sc = H.synth.make_scene("bend4k")
     nb, aidx, aw, aims = _problem(sc)
@@ -166,12 +170,13 @@ def test_solve_centre_mode_and_weighting(dev):
         rot_ref, tr_ref = ed.put_free_inputs(pr, x_ref)
         solver = dev.Solver(_t(nb.astype(np.int32)), _t(aidx.T.astype(np.int32)), _t(aw.T.astype(np.float32)),
                             blocks, types, max_iters=5, early_exit=0, cons_on_center=cons,
-                            weighting_factor=wf, precision=1, pcg_tol=1e-7)
+                            weighting_factor=wf, precision=1, pcg_tol=1e-7 if coarse == 0 else 1e-6,
+                            coarse_nodes=coarse)
         rot, tr, st = solver.solve(_t(sc.node_pos), _t(aims))
         X = np.concatenate([_np(rot), _np(tr)], axis=1)
         Xr = np.concatenate([rot_ref, tr_ref], axis=1)
         assert st["n_rows"] == pr.n_rows
-        assert np.abs(X - Xr).max() / np.abs(Xr).max() <= 1e-5, (cons, wf)
+        assert np.abs(X - Xr).max() / np.abs(Xr).max() <= 1e-5, (cons, wf, coarse)
 
 
 def test_solve_early_exit(dev):
