@@ -181,8 +181,9 @@ class Solver:
 # ------------------------------------------------------------ skinning ----
 
 class SolverBatch:
-    """Several Solvers (one precision) solved in one cooperative launch
-    (arap_solver_batch_*): the grid's CTAs are split among the instances."""
+    """Several Solvers (one precision) solved together (arap_solver_batch_*):
+    one cooperative launch per wave of instances, the grid's CTAs split among
+    each wave's instances."""
 
     def __init__(self, solvers, balance_exponent=1.0):
         self.solvers = list(solvers)

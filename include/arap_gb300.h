@@ -148,10 +148,13 @@ int arap_solver_free_ids(const arap_solver* s, int32_t* free_ids_host);
 void arap_solver_destroy(arap_solver* s);
 
 /* No counterpart in the reference, whose viewer deforms one field at a time:
- * several independent solves in one cooperative persistent launch.
- * - The co-resident grid (one CTA per SM) is split among the instances: each
- *   gets at least one CTA, the rest go in proportion to (coupling items + free
- *   nodes)^balance_exponent (<= 0: 1).
+ * several independent solves in a few cooperative persistent launches (waves).
+ * - Instances whose nodes fit in shared memory on some share of the grid (the
+ *   resident two-level PCG) are packed into waves by that minimum share,
+ *   largest first; the other instances share one wave. In each wave the
+ *   co-resident grid (one CTA per SM) is split among its instances: each gets
+ *   its minimum (at least one CTA), the rest go in proportion to (coupling
+ *   items + free nodes)^balance_exponent (<= 0: 1).
  * - Each instance runs the same Gauss-Newton/PCG iteration as
  *   arap_solver_solve on its own CTAs, with its own grid barrier and its own
  *   solver's buffers. Results equal separate solves to rounding (reduction
@@ -167,7 +170,7 @@ int arap_solver_batch_create(arap_solver_batch** out, arap_solver* const* solver
  * with the meaning of arap_solver_solve's arguments. stats_host: NULL (no
  * synchronisation) or count entries (synchronises).
  * Without stats the call queues two copies (a pinned upload of the instances'
- * parameters, a barrier reset) and one cooperative launch, all on `stream`.
+ * parameters, a barrier reset) and one cooperative launch per wave, all on `stream`.
  * It can therefore be captured in a CUDA graph. A replay reads the parameter
  * staging as left by the most recent call on this batch. */
 int arap_solver_batch_solve(arap_solver_batch* batch, const float* const* node_pos, const float* const* aims,
@@ -179,7 +182,8 @@ int arap_solver_batch_solve(arap_solver_batch* batch, const float* const* node_p
 int arap_solver_batch_autotune(arap_solver_batch* batch, const float* const* node_pos, const float* const* aims,
                                float* const* rot_out, float* const* trans_out, float* best_exponent,
                                arap_stream_t stream);
-/* cta_first_host [count+1]: instance i runs on CTAs cta_first[i] .. cta_first[i+1]-1. */
+/* cta_first_host [count+1]: prefix sums of the CTAs each instance gets in its
+ * wave (instance i runs on cta_first[i+1] - cta_first[i] CTAs). */
 int arap_solver_batch_ctas(const arap_solver_batch* batch, int32_t* cta_first_host);
 void arap_solver_batch_destroy(arap_solver_batch* batch);
 

@@ -1,5 +1,5 @@
 """Batched solves (arap_solver_batch_*): several instances of uneven node
-counts in one cooperative launch must give each instance's separate-solve
+counts in batched launches (waves) must give each instance's separate-solve
 result (to reduction-order rounding), also when the batched solve is captured
 in a CUDA graph and replayed, and with the autotuned CTA split."""
 import numpy as np
