@@ -91,6 +91,9 @@ SIGNATURES = {
     "arap_grid_arrays": (I, [P, C.POINTER(P), C.POINTER(P), C.POINTER(P)]),
     "arap_grid_center_order": (I, [P, I, P, P, P]),
     "arap_grid_center_order_noalloc": (I, [P, I, P, P, P]),
+    "arap_ply_info": (I, [C.c_char_p, C.POINTER(C.c_int64), C.POINTER(I), C.POINTER(I)]),
+    "arap_ply_load": (I, [C.c_char_p, C.c_int64, I, P, P, P, P, P, P, P, P]),
+    "arap_ply_save": (I, [C.c_char_p, C.c_int64, P, P, P, P, P, P, P, P, C.POINTER(C.c_int64)]),
     "arap_grid_samples": (I, [P, P, P]),
     "arap_grid_ada_lpf": (I, [P, P, F, P, P]),
     "arap_grid_density": (I, [P, P, P, P, P, P, P, P, F, P, P, P]),

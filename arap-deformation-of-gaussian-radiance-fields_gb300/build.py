@@ -17,7 +17,7 @@ CSRC = os.path.join(HERE, "csrc")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 LIB = os.path.join(HERE, "libarap_gb300.so")
 OBJ = os.path.join(HERE, "_build")
-SOURCES = ["api.cu", "knn.cu", "skin.cu", "solver.cu", "grid.cu"]
+SOURCES = ["api.cu", "knn.cu", "skin.cu", "solver.cu", "grid.cu", "ply.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-rdc=true", "-Xcompiler", "-fPIC",
          "-Xcompiler", "-O2", "-I", INCLUDE]
@@ -52,7 +52,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
     srcs = [s for s in SOURCES if os.path.exists(os.path.join(CSRC, s))]
 
     def compile_one(src):
-        obj = os.path.join(OBJ, src.replace(".cu", ".o"))
+        obj = os.path.join(OBJ, os.path.splitext(src)[0] + ".o")
         cmd = [cc, *ARCH, *FLAGS, "-c", os.path.join(CSRC, src), "-o", obj]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:

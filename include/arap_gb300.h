@@ -397,6 +397,35 @@ int arap_grid_density(const arap_grid* grid, const float* pos, const float* rot,
 
 void arap_grid_destroy(arap_grid* grid);
 
+/* -------------------------------------------------------------- PLY IO --- */
+
+/* 3D Gaussian splatting binary PLY files, host memory only (no device call;
+ * usable without a GPU). Replaces the viewer's loadPly / loadPly_Origin /
+ * savePly (GaussianView.cpp:43-339). A file is accepted when it is binary
+ * little-endian with one `vertex` element of float properties holding x y z,
+ * f_dc_0..2, f_rest_* for SH degree 0..3, opacity, scale_0..2, rot_0..3 and
+ * optionally `index`; anything else is ARAP_EBADINPUT (the viewer aborts). */
+int arap_ply_info(const char* path, int64_t* count, int* sh_degree, int* has_index);
+
+/* Loads count splats (as reported by arap_ply_info) into activated SoA arrays:
+ * pos [count*3], shs [count*48] (rgb per coefficient, bands above the file's
+ * degree zero), opacity [count] (logistic of the stored logit), scale
+ * [count*3] (exp of the stored log), rot [count*4] (normalised, w x y z as
+ * stored). morton_order != 0 reorders the splats by the viewer's 21-bit-per-axis
+ * Morton code over the bounding box (ties in file order), as loadPly does.
+ * box_min/box_max [3] (nullable): the bounding box. index [count] (nullable;
+ * requires the property): the rounded `index` property. */
+int arap_ply_load(const char* path, int64_t count, int morton_order, float* pos, float* shs, float* opacity,
+                  float* scale, float* rot, float* box_min, float* box_max, int32_t* index);
+
+/* Saves the splats inside [box_min, box_max] (bounds included) that are not
+ * flagged in too_small [count] (nullable), as savePly does: SH degree 3,
+ * normals zero, scale stored as log, opacity as logit, rot as given.
+ * written (nullable): the number of splats written. */
+int arap_ply_save(const char* path, int64_t count, const float* pos, const float* shs, const float* opacity,
+                  const float* scale, const float* rot, const float* box_min, const float* box_max,
+                  const uint8_t* too_small, int64_t* written);
+
 /* --------------------------------------------------------------- misc --- */
 
 /* Read and clear the library's sticky device error word (ARAP_* code). */
