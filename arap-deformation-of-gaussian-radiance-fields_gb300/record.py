@@ -134,7 +134,7 @@ def replay_steps(h: DeformHistory):
     active block index) and its parameter: ``translation`` (x, y, z) for
     moves, ``axis`` (x, y, z, w) and ``angle_step`` for twists,
     ``scale_step`` for scales.  A delete with no block left is skipped; the
-    viewer does not advance its history there and stops replaying."""
+    viewer stalls on such a step (its history never advances past it)."""
     blocks, types, steps = [], [], []
     active = 0
     add_idx = move_idx = 0
