@@ -397,12 +397,38 @@ def run_ours(a):
     }
     if rank == 0 and a.batch > 0:
         line["batch"] = batch_leg(a.batch)
+    if rank == 0:
+        line["ply_io"] = ply_leg(sc)
     if rank == 0 and not a.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(sc, samples=1)
     if rank == 0:
         print(json.dumps(line))
     if ws > 1:
         torch.distributed.destroy_process_group()
+
+
+def ply_leg(sc, reps=3):
+    """Host time of the 3DGS PLY round trip of the workload's Gaussians
+    (arap_ply_save, then arap_ply_load with the viewer's Morton reorder),
+    best of reps, through a temporary file."""
+    import tempfile
+    import numpy as np
+    ply = importlib.import_module(PKG + ".ply")
+    big = np.float32(3e38)
+    with tempfile.TemporaryDirectory() as d:
+        path = os.path.join(d, "scene.ply")
+        t_save = t_load = float("inf")
+        for _ in range(reps):
+            t0 = time.perf_counter()
+            ply.save_ply(path, sc.pos, sc.shs, sc.opacity, sc.scale, sc.rot, [-big] * 3, [big] * 3)
+            t_save = min(t_save, time.perf_counter() - t0)
+            t0 = time.perf_counter()
+            out = ply.load_ply(path)
+            t_load = min(t_load, time.perf_counter() - t0)
+        mb = os.path.getsize(path) / 1e6
+    assert out["pos"].shape[0] == sc.pos.shape[0]
+    return {"splats": int(sc.pos.shape[0]), "file_mb": round(mb, 1), "save_ms": round(1e3 * t_save, 1),
+            "load_ms": round(1e3 * t_load, 1), "load_mb_per_s": round(mb / t_load, 1), "threads": 1}
 
 
 # ------------------------------------------------------- CPU baseline ----
