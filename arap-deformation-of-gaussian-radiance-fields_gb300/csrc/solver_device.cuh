@@ -72,6 +72,10 @@ __device__ __forceinline__ float4* stg_lv() { return reinterpret_cast<float4*>(s
 __device__ __forceinline__ int* stg_la() { return reinterpret_cast<int*>(s_dyn + s_stg.ga); }
 // resident mode: PCG vector k of slot s (12 floats), x of slot s, the other
 // node's offset of item i, w_con J_g u_f and group of constraint item c
+// In the V-cycle iteration: RV_UF holds z1 = D^-1 r (phases 1-4), then z3
+// (phases 4-5); RV_WF holds A z1 (phases 2-4), then A z2 (phases 4-5); RV_W
+// holds the regularisation part of a product while it is formed, then w;
+// RV_R, RV_P, RV_S, RV_H, RV_U are the PCG's r, p, s = A p, h and u.
 enum { RV_UF = 0, RV_R, RV_P, RV_S, RV_H, RV_U, RV_W, RV_WF };
 __device__ __forceinline__ float* stg_vec(int s, int k) {
   return reinterpret_cast<float*>(s_dyn + s_stg.vec) + 12 * (kResVecs * s + k);
