@@ -421,6 +421,7 @@ class GaussianDeformer:
             if (self.sample_pos is not None and bool(node_static.any())) else None
         self.solver = Solver(self.neighbors, self.anchor_idx, self.anchor_w, self.blocks,
                              self.block_type, config=config, **cfg_kw)
+        self._cfg = (config, dict(cfg_kw))
         self.precision = self.solver.config.precision
         act = [int(v) for b, t in zip(self.blocks, self.block_type) if t == 1 for v in b]
         self.active = torch.tensor(act, dtype=torch.int32, device=dev)
@@ -429,6 +430,47 @@ class GaussianDeformer:
         self.trans_nodes = torch.empty((self.n, 3), dtype=torch.float32, device=dev)
         self.node_pos_next = torch.empty_like(self.node_pos)
         self.cov = torch.empty((N, 6), dtype=torch.float32, device=dev)
+
+    def _controls_key(self):
+        return (tuple(tuple(int(v) for v in b.tolist()) for b in self.blocks),
+                tuple(self.block_type), bool(self.solver.config.cons_on_center))
+
+    def set_controls(self, blocks, block_type, constraints_on_center=None):
+        """Replace the control blocks between frames, and optionally the
+        constraint mode, as the viewer's UpdateIndicies and fresh ``Deform``
+        do before a frame (GaussianView.cpp:1996-2021, 1822, 1855).  The solver
+        of each configuration is created once and kept."""
+        centre = bool(self.solver.config.cons_on_center) if constraints_on_center is None \
+            else bool(constraints_on_center)
+        key = (tuple(tuple(int(v) for v in b) for b in blocks), tuple(int(t) for t in block_type), centre)
+        if len(key[0]) != len(key[1]):
+            raise ValueError("set_controls: %d blocks, %d block types" % (len(key[0]), len(key[1])))
+        current = self._controls_key()
+        if key == current:
+            return
+        cache = self.__dict__.setdefault("_solvers", {})
+        cache.setdefault(current, self.solver)
+        solver = cache.get(key)
+        if solver is None:
+            config, cfg_kw = self._cfg
+            cfg = SolveConfig.from_buffer_copy(config) if config is not None else default_config(**cfg_kw)
+            cfg.cons_on_center = int(centre)
+            solver = Solver(self.neighbors, self.anchor_idx, self.anchor_w, key[0], key[1], config=cfg)
+            cache[key] = solver
+        self.solver = solver
+        self.blocks = [torch.as_tensor(b, dtype=torch.int64) for b in key[0]]
+        self.block_type = list(key[1])
+        node_static = torch.zeros(self.n, dtype=torch.uint8, device="cuda")
+        for b, t in zip(self.blocks, self.block_type):
+            if t < 0 and b.numel():
+                node_static[b.to("cuda")] = 1
+        self.node_static = node_static
+        any_static = bool(node_static.any())
+        self.g_static = static_mask(self.ends_idx, node_static, self.N) if any_static else None
+        self.s_static = static_mask(self.sample_idx, node_static, self.sample_pos.shape[0]) \
+            if (self.sample_pos is not None and any_static) else None
+        act = [v for b, t in zip(key[0], key[1]) if t == 1 for v in b]
+        self.active = torch.tensor(act, dtype=torch.int32, device="cuda")
 
     def apply_op(self, op):
         """Move the active targets (UpdateAimPosition / Twist / Scale)."""
