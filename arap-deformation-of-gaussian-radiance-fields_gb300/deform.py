@@ -18,7 +18,6 @@ non-OK status; nothing falls back to a CPU path.
 from __future__ import annotations
 
 import ctypes as C
-import math
 
 import torch
 
@@ -49,9 +48,8 @@ def _s():
     return C.c_void_p(torch.cuda.current_stream().cuda_stream)
 
 
-def _f32(t, shape_tail=None):
-    t = t.to(device="cuda", dtype=torch.float32).contiguous()
-    return t
+def _f32(t):
+    return t.to(device="cuda", dtype=torch.float32).contiguous()
 
 
 def _i32(t):
