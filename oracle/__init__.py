@@ -22,4 +22,10 @@ Modules:
   grid   -- scene AABB, cell binning CSR, grid samples, adaptive low-pass,
             density sampling (GaussianView.cpp, cudakdtree.cu)
   targets-- control-target generators (GaussianView.cpp, helper.cpp)
+  ply    -- 3DGS PLY load/save (GaussianView.cpp)
+  stage2 -- the project's definition of the Stage-II alignment step (the
+            external kernels' source is absent) and the visible host
+            routines JudgeEmptyGrid / ExpandOpRange (GaussianView.cpp)
+  raster -- the published 3D Gaussian splatting forward, standing in for
+            the un-vendored rasteriser the viewer draws with
 """
