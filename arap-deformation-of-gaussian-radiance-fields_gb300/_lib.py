@@ -97,6 +97,8 @@ SIGNATURES = {
     "arap_grid_samples": (I, [P, P, P]),
     "arap_grid_ada_lpf": (I, [P, P, F, P, P]),
     "arap_grid_density": (I, [P, P, P, P, P, P, P, P, F, P, P, P]),
+    "arap_stage2_loss_grad": (I, [P, P, P, P, P, P, P, P, F, P, P, P, F, P, P, P, P, P, C.POINTER(D), P]),
+    "arap_stage2_adam": (I, [I, I, P, P, P, P, P, P, P, P, P, P, P, P, P, P, P]),
     "arap_grid_destroy": (None, [P]),
     "arap_get_device_status": (I, [P]),
     "arap_version": (C.c_char_p, []),

@@ -7,10 +7,15 @@
 // the serial list fill (GaussianView.cpp:4077-4100) whose per-cell order --
 // ascending Gaussian index -- is reproduced by a per-cell sort after an
 // atomic fill, GetAdaLpfRatio (GaussianView.cpp:4670-4751) and the host
-// contract of CudaRasterizer::forward3d_grid (GaussianView.cpp:4222-4249).
+// contract of CudaRasterizer::forward3d_grid (GaussianView.cpp:4222-4249),
+// and the library's definition of the Stage-II alignment step
+// (GaussianView.cpp:4363-4486: L1loss3d, backward3d_grid, update3d, whose
+// source is not in the reference tree).
 #include <atomic>
 #include <climits>
+#include <cmath>
 #include <new>
+#include <vector>
 
 #include "arap_common.cuh"
 
@@ -455,6 +460,328 @@ __global__ void __launch_bounds__(64) density_kernel(
   for (int t = 0; t < 12; ++t) fo[t] = make_float4(F[4 * t], F[4 * t + 1], F[4 * t + 2], F[4 * t + 3]);
 }
 
+// ------------------------------------------------- Stage-II alignment ----
+// The library's definition of the step the viewer runs through the
+// un-vendored rasteriser (L1loss3d + backward3d_grid + update3d): an L1 loss
+// between the field of the current Gaussians and the target field at the
+// grid samples, its gradient to the raw attributes (mean, quaternion,
+// log-scale, logit opacity, SH) and an Adam step.
+//
+// stage2_pair_kernel: one CTA of 64 threads per occupied cell.  Pass 1: one
+// thread per sample forms sigma and F as density_kernel does (from the raw
+// attributes) and the sample's dL/dsigma and dL/dF.  Pass 2: one thread per
+// Gaussian of the cell's list walks the 64 samples and sums that pair's
+// contribution, so no reduction across threads is needed; it writes 58
+// floats per pair (dL/dSH 48 | dL/dalpha | dL/dmu 3 | dL/dSigma 6, the upper
+// triangle of the symmetric matrix) into planes [58][npairs] at the pair's
+// CSR position.  stage2_gather_kernel then sums each Gaussian's pairs in
+// ascending cell order (deterministic) and applies the chain rule.
+constexpr int kS2Floats = 58;
+constexpr int kS2Params = 59;  // per Gaussian: opacity 1 | SH 48 | mean 3 | quaternion 4 | log-scale 3
+
+__device__ __forceinline__ float sign0(float v) { return (v > 0.f) ? 1.f : ((v < 0.f) ? -1.f : 0.f); }
+
+__device__ __forceinline__ void stage2_stage(int cnt, int base, const int* __restrict__ lists,
+                                             const float* __restrict__ pos, const float* __restrict__ rot,
+                                             const float* __restrict__ log_scale, const float* __restrict__ logit_op,
+                                             const float* __restrict__ shs, const float* Lm,
+                                             float (*s_mu)[3], float (*s_A)[6], float* s_a, float (*s_sh)[48]) {
+  const int s = threadIdx.x;
+  if (s < cnt) {
+    const int gi = lists[base + s];
+    float R[9];
+    quat_to_rowmajor(quat_normalize(__ldg(reinterpret_cast<const float4*>(rot) + gi)), R);
+    float s2[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      const float sc = __expf(log_scale[3 * (size_t)gi + d]);
+      s2[d] = sc * sc;
+    }
+    float C6[6];
+    int o = 0;
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+#pragma unroll
+      for (int q = r; q < 3; ++q)
+        C6[o++] = R[r * 3] * s2[0] * R[q * 3] + R[r * 3 + 1] * s2[1] * R[q * 3 + 1] + R[r * 3 + 2] * s2[2] * R[q * 3 + 2];
+#pragma unroll
+    for (int t = 0; t < 6; ++t) C6[t] += Lm[t];
+    const float a = C6[0], bb = C6[1], cc = C6[2], d = C6[3], e = C6[4], f = C6[5];
+    const float A0 = d * f - e * e, A1 = cc * e - bb * f, A2 = bb * e - cc * d;
+    const float id = 1.0f / (a * A0 + bb * A1 + cc * A2);
+    s_A[s][0] = A0 * id;
+    s_A[s][1] = A1 * id;
+    s_A[s][2] = A2 * id;
+    s_A[s][3] = (a * f - cc * cc) * id;
+    s_A[s][4] = (bb * cc - a * e) * id;
+    s_A[s][5] = (a * d - bb * bb) * id;
+    s_mu[s][0] = pos[3 * (size_t)gi];
+    s_mu[s][1] = pos[3 * (size_t)gi + 1];
+    s_mu[s][2] = pos[3 * (size_t)gi + 2];
+    s_a[s] = 1.0f / (1.0f + __expf(-logit_op[gi]));
+  }
+  for (int t = s; t < cnt * 12; t += 64) {
+    const int gq = t / 12, q4 = t % 12;
+    const int gi = lists[base + gq];
+    const float4 u = __ldg(reinterpret_cast<const float4*>(shs + 48 * (size_t)gi) + q4);
+    s_sh[gq][4 * q4] = u.x;
+    s_sh[gq][4 * q4 + 1] = u.y;
+    s_sh[gq][4 * q4 + 2] = u.z;
+    s_sh[gq][4 * q4 + 3] = u.w;
+  }
+}
+
+__global__ void __launch_bounds__(64) stage2_pair_kernel(
+    int nvalid, const int* __restrict__ valid, const int* __restrict__ off, const int* __restrict__ lists,
+    long long npairs, const float* __restrict__ pos, const float* __restrict__ rot,
+    const float* __restrict__ log_scale, const float* __restrict__ logit_op, const float* __restrict__ shs,
+    const float* __restrict__ samples, const float* __restrict__ ada, float lpf,
+    const float* __restrict__ aim_sigma, const float* __restrict__ aim_feat,
+    const uint8_t* __restrict__ cell_active, float wf, float* __restrict__ part, float* __restrict__ loss_cta) {
+  __shared__ float s_mu[kDensChunk][3];
+  __shared__ float s_A[kDensChunk][6];
+  __shared__ float s_a[kDensChunk];
+  __shared__ float s_sh[kDensChunk][48];
+  __shared__ float s_x[64][3];
+  __shared__ float s_ds[64];
+  __shared__ float s_df[64][48];
+  __shared__ float s_red[2][2];
+  const int v = blockIdx.x;
+  if (v >= nvalid) return;
+  const int c = valid[v];
+  const int b = off[c], L = off[c + 1] - b;
+  const bool act = cell_active == nullptr || cell_active[v] != 0;
+  float Lm[6];
+  if (ada) {
+    const float* m = ada + (size_t)v * 9;
+    Lm[0] = m[0]; Lm[1] = m[1]; Lm[2] = m[2]; Lm[3] = m[4]; Lm[4] = m[5]; Lm[5] = m[8];
+  } else {
+    Lm[0] = lpf; Lm[1] = 0.f; Lm[2] = 0.f; Lm[3] = lpf; Lm[4] = 0.f; Lm[5] = lpf;
+  }
+  const int s = threadIdx.x;
+  const size_t sid = (size_t)v * 64 + s;
+  const float x = samples[3 * sid], y = samples[3 * sid + 1], z = samples[3 * sid + 2];
+  s_x[s][0] = x;
+  s_x[s][1] = y;
+  s_x[s][2] = z;
+  // pass 1: the sample's sigma and F
+  float acc = 0.f;
+  float F[48];
+#pragma unroll
+  for (int t = 0; t < 48; ++t) F[t] = 0.f;
+  for (int c0 = 0; c0 < L; c0 += kDensChunk) {
+    const int cnt = min(kDensChunk, L - c0);
+    __syncthreads();
+    stage2_stage(cnt, b + c0, lists, pos, rot, log_scale, logit_op, shs, Lm, s_mu, s_A, s_a, s_sh);
+    __syncthreads();
+    for (int q = 0; q < cnt; ++q) {
+      const float dx = x - s_mu[q][0], dy = y - s_mu[q][1], dz = z - s_mu[q][2];
+      const float* A = s_A[q];
+      const float m = A[0] * dx * dx + A[3] * dy * dy + A[5] * dz * dz +
+                      2.f * (A[1] * dx * dy + A[2] * dx * dz + A[4] * dy * dz);
+      const float gw = s_a[q] * __expf(-0.5f * m);
+      acc += gw;
+#pragma unroll
+      for (int t = 0; t < 48; ++t) F[t] = fmaf(gw, s_sh[q][t], F[t]);
+    }
+  }
+  // dL/dsigma and dL/dF of the sample, and its loss terms
+  float ls = 0.f, lf = 0.f;
+  {
+    const float ts = aim_sigma[sid];
+    ls = act ? fabsf(acc - ts) : 0.f;
+    s_ds[s] = act ? sign0(acc - ts) : 0.f;
+    const float4* tf = reinterpret_cast<const float4*>(aim_feat + 48 * sid);
+#pragma unroll
+    for (int t = 0; t < 12; ++t) {
+      const float4 u = tf[t];
+      const float tv[4] = {u.x, u.y, u.z, u.w};
+#pragma unroll
+      for (int h = 0; h < 4; ++h) {
+        const float dv = F[4 * t + h] - tv[h];
+        lf += act ? fabsf(dv) : 0.f;
+        s_df[s][4 * t + h] = act ? wf * sign0(dv) : 0.f;
+      }
+    }
+    lf *= wf;
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    ls += __shfl_xor_sync(0xffffffffu, ls, o);
+    lf += __shfl_xor_sync(0xffffffffu, lf, o);
+  }
+  if ((s & 31) == 0) {
+    s_red[s >> 5][0] = ls;
+    s_red[s >> 5][1] = lf;
+  }
+  // pass 2: one thread per Gaussian of the chunk over the cell's 64 samples
+  for (int c0 = 0; c0 < L; c0 += kDensChunk) {
+    const int cnt = min(kDensChunk, L - c0);
+    __syncthreads();
+    stage2_stage(cnt, b + c0, lists, pos, rot, log_scale, logit_op, shs, Lm, s_mu, s_A, s_a, s_sh);
+    __syncthreads();
+    if (s < cnt) {
+      const float mx = s_mu[s][0], my = s_mu[s][1], mz = s_mu[s][2];
+      float A[6];
+#pragma unroll
+      for (int t = 0; t < 6; ++t) A[t] = s_A[s][t];
+      const float al = s_a[s];
+      float sh[48];
+#pragma unroll
+      for (int h = 0; h < 48; ++h) sh[h] = s_sh[s][h];
+      float gsh[48];
+#pragma unroll
+      for (int t = 0; t < 48; ++t) gsh[t] = 0.f;
+      float ga = 0.f, gm[3] = {0.f, 0.f, 0.f}, gS[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+      if (act) {
+        for (int t = 0; t < 64; ++t) {
+          const float dx = s_x[t][0] - mx, dy = s_x[t][1] - my, dz = s_x[t][2] - mz;
+          const float ax = A[0] * dx + A[1] * dy + A[2] * dz;
+          const float ay = A[1] * dx + A[3] * dy + A[4] * dz;
+          const float az = A[2] * dx + A[4] * dy + A[5] * dz;
+          const float G = __expf(-0.5f * (dx * ax + dy * ay + dz * az));
+          const float gw = al * G;
+          float cc = s_ds[t];
+#pragma unroll
+          for (int h = 0; h < 48; ++h) {
+            const float dfv = s_df[t][h];
+            cc = fmaf(dfv, sh[h], cc);
+            gsh[h] = fmaf(gw, dfv, gsh[h]);
+          }
+          ga = fmaf(cc, G, ga);
+          const float de = cc * gw;
+          gm[0] = fmaf(de, ax, gm[0]);
+          gm[1] = fmaf(de, ay, gm[1]);
+          gm[2] = fmaf(de, az, gm[2]);
+          const float hd = 0.5f * de;
+          gS[0] = fmaf(hd * ax, ax, gS[0]);
+          gS[1] = fmaf(hd * ax, ay, gS[1]);
+          gS[2] = fmaf(hd * ax, az, gS[2]);
+          gS[3] = fmaf(hd * ay, ay, gS[3]);
+          gS[4] = fmaf(hd * ay, az, gS[4]);
+          gS[5] = fmaf(hd * az, az, gS[5]);
+        }
+      }
+      const size_t p = (size_t)b + c0 + s;
+      const size_t np = (size_t)npairs;
+#pragma unroll
+      for (int h = 0; h < 48; ++h) part[h * np + p] = gsh[h];
+      part[48 * np + p] = ga;
+#pragma unroll
+      for (int h = 0; h < 3; ++h) part[(49 + h) * np + p] = gm[h];
+#pragma unroll
+      for (int h = 0; h < 6; ++h) part[(52 + h) * np + p] = gS[h];
+    }
+  }
+  __syncthreads();
+  if (s == 0) {
+    loss_cta[2 * (size_t)v] = s_red[0][0] + s_red[1][0];
+    loss_cta[2 * (size_t)v + 1] = s_red[0][1] + s_red[1][1];
+  }
+}
+
+__global__ void stage2_gather_kernel(int N, int g, const int* __restrict__ ranges, const int* __restrict__ off,
+                                     const int* __restrict__ lists, long long npairs,
+                                     const float* __restrict__ part, const float* __restrict__ rot,
+                                     const float* __restrict__ log_scale, const float* __restrict__ logit_op,
+                                     float* __restrict__ g_pos, float* __restrict__ g_rot,
+                                     float* __restrict__ g_ls, float* __restrict__ g_lo,
+                                     float* __restrict__ g_shs) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= N) return;
+  float acc[kS2Floats];
+#pragma unroll
+  for (int h = 0; h < kS2Floats; ++h) acc[h] = 0.f;
+  const int* r = ranges + 6 * (size_t)i;
+  const size_t np = (size_t)npairs;
+  for (int x = r[0]; x <= r[1]; ++x)
+    for (int y = r[2]; y <= r[3]; ++y)
+      for (int z = r[4]; z <= r[5]; ++z) {
+        const size_t c = ((size_t)x * g + y) * g + z;
+        int lo = off[c], hi = off[c + 1];
+        const int end = hi;
+        while (lo < hi) {
+          const int mid = (lo + hi) >> 1;
+          if (lists[mid] < i) lo = mid + 1; else hi = mid;
+        }
+        if (lo < end && lists[lo] == i) {
+#pragma unroll
+          for (int h = 0; h < kS2Floats; ++h) acc[h] += part[h * np + lo];
+        }
+      }
+  float4* gs = reinterpret_cast<float4*>(g_shs + 48 * (size_t)i);
+#pragma unroll
+  for (int t = 0; t < 12; ++t) gs[t] = make_float4(acc[4 * t], acc[4 * t + 1], acc[4 * t + 2], acc[4 * t + 3]);
+  const float al = 1.0f / (1.0f + __expf(-logit_op[i]));
+  g_lo[i] = acc[48] * al * (1.0f - al);
+#pragma unroll
+  for (int h = 0; h < 3; ++h) g_pos[3 * (size_t)i + h] = acc[49 + h];
+  // dL/dSigma as the full symmetric matrix
+  const float G[9] = {acc[52], acc[53], acc[54], acc[53], acc[55], acc[56], acc[54], acc[56], acc[57]};
+  const float4 q = __ldg(reinterpret_cast<const float4*>(rot) + i);
+  const float nq = sqrtf(q.x * q.x + q.y * q.y + q.z * q.z + q.w * q.w);
+  const float4 qn = make_float4(q.x / nq, q.y / nq, q.z / nq, q.w / nq);
+  float R[9];
+  quat_to_rowmajor(qn, R);
+  float sc[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) sc[k] = __expf(log_scale[3 * (size_t)i + k]);
+  float M[9];  // G R
+#pragma unroll
+  for (int a = 0; a < 3; ++a)
+#pragma unroll
+    for (int k = 0; k < 3; ++k) M[a * 3 + k] = G[a * 3] * R[k] + G[a * 3 + 1] * R[3 + k] + G[a * 3 + 2] * R[6 + k];
+  float dR[9];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const float rtgr = R[k] * M[k] + R[3 + k] * M[3 + k] + R[6 + k] * M[6 + k];
+    g_ls[3 * (size_t)i + k] = 2.0f * sc[k] * rtgr * sc[k];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) dR[a * 3 + k] = 2.0f * M[a * 3 + k] * sc[k] * sc[k];
+  }
+  const float w = qn.x, x = qn.y, y = qn.z, z = qn.w;
+  const float dw = 2.f * (-z * dR[1] + y * dR[2] + z * dR[3] - x * dR[5] - y * dR[6] + x * dR[7]);
+  const float dx = 2.f * (y * dR[1] + z * dR[2] + y * dR[3] - 2.f * x * dR[4] - w * dR[5] + z * dR[6] +
+                          w * dR[7] - 2.f * x * dR[8]);
+  const float dy = 2.f * (-2.f * y * dR[0] + x * dR[1] + w * dR[2] + x * dR[3] + z * dR[5] - w * dR[6] +
+                          z * dR[7] - 2.f * y * dR[8]);
+  const float dz = 2.f * (-2.f * z * dR[0] - w * dR[1] + x * dR[2] + w * dR[3] - 2.f * z * dR[4] + y * dR[5] +
+                          x * dR[6] + y * dR[7]);
+  const float dot = w * dw + x * dx + y * dy + z * dz;
+  reinterpret_cast<float4*>(g_rot)[i] =
+      make_float4((dw - w * dot) / nq, (dx - x * dot) / nq, (dy - y * dot) / nq, (dz - z * dot) / nq);
+}
+
+// Adam over the 59 attributes of each moved Gaussian; m and v are [N][59] in
+// the order opacity | SH | mean | quaternion | log-scale.
+struct Stage2Adam {
+  float* p[5];
+  const float* g[5];
+  float lr[5];
+};
+
+__global__ void stage2_adam_kernel(int N, Stage2Adam A, const uint8_t* __restrict__ moved, float* __restrict__ m,
+                                   float* __restrict__ v, float b1, float b2, float eps, float bc1, float bc2) {
+  const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= (long long)N * kS2Params) return;
+  const int i = (int)(e / kS2Params);
+  const int r = (int)(e % kS2Params);
+  if (moved && !moved[i]) return;
+  int a, k, width;
+  if (r < 1) { a = 0; k = r; width = 1; }
+  else if (r < 49) { a = 1; k = r - 1; width = 48; }
+  else if (r < 52) { a = 2; k = r - 49; width = 3; }
+  else if (r < 56) { a = 3; k = r - 52; width = 4; }
+  else { a = 4; k = r - 56; width = 3; }
+  const size_t idx = (size_t)i * width + k;
+  const float gv = A.g[a][idx];
+  const float mm = b1 * m[e] + (1.0f - b1) * gv;
+  const float vv = b2 * v[e] + (1.0f - b2) * gv * gv;
+  m[e] = mm;
+  v[e] = vv;
+  A.p[a][idx] -= A.lr[a] * (mm / bc1) / (sqrtf(vv / bc2) + eps);
+}
+
 }  // namespace arap
 
 // ------------------------------------------------------------------ host --
@@ -469,6 +796,10 @@ struct arap_grid {
   int* valid = nullptr;          // [nvalid]
   int* ranges = nullptr;         // [N*6]
   GridParams host{};
+  // Stage-II scratch: pair partials [58][npairs] then the per-cell losses
+  // [nvalid][2]; allocated by the first arap_stage2_loss_grad call
+  mutable float* stage2_scratch = nullptr;
+  mutable size_t stage2_floats = 0;
 };
 
 static int scan_exclusive(const int* in, int* out, int n, long long* sums, cudaStream_t st) {
@@ -487,6 +818,7 @@ extern "C" void arap_grid_destroy(arap_grid* G) {
   cudaFree(G->lists);
   cudaFree(G->valid);
   cudaFree(G->ranges);
+  cudaFree(G->stage2_scratch);
   delete G;
 }
 
@@ -684,6 +1016,73 @@ extern "C" int arap_grid_density(const arap_grid* G, const float* pos, const flo
   density_kernel<<<G->nvalid, 64, 0, (cudaStream_t)stream>>>(G->nvalid, G->valid, G->off, G->lists, pos, rot,
                                                               scale, opacity, shs, samples, ada, lpf, sigma_out,
                                                               feature_out);
+  ARAP_LAUNCH_CHECK();
+  return ARAP_OK;
+}
+
+extern "C" int arap_stage2_loss_grad(const arap_grid* G, const float* pos, const float* rot, const float* log_scale,
+                                     const float* logit_opacity, const float* shs, const float* samples,
+                                     const float* ada, float lpf, const float* aim_sigma, const float* aim_feature,
+                                     const uint8_t* cell_active, float feature_weight, float* grad_pos,
+                                     float* grad_rot, float* grad_log_scale, float* grad_logit_opacity,
+                                     float* grad_shs, double* loss_host, arap_stream_t stream) {
+  if (!G || !pos || !rot || !log_scale || !logit_opacity || !shs || !samples || !aim_sigma || !aim_feature ||
+      !grad_pos || !grad_rot || !grad_log_scale || !grad_logit_opacity || !grad_shs)
+    return ARAP_EBADINPUT;
+  if ((reinterpret_cast<uintptr_t>(rot) | reinterpret_cast<uintptr_t>(shs) |
+       reinterpret_cast<uintptr_t>(aim_feature) | reinterpret_cast<uintptr_t>(grad_rot) |
+       reinterpret_cast<uintptr_t>(grad_shs)) & 15)
+    return ARAP_EBADINPUT;
+  cudaStream_t st = (cudaStream_t)stream;
+  if (loss_host) loss_host[0] = loss_host[1] = 0.0;
+  if (G->N == 0) return ARAP_OK;
+  const size_t need = (size_t)kS2Floats * (size_t)G->npairs + 2 * (size_t)G->nvalid;
+  if (need > G->stage2_floats) {
+    cudaFree(G->stage2_scratch);
+    G->stage2_scratch = nullptr;
+    G->stage2_floats = 0;
+    ARAP_CUDA_TRY(cudaMalloc(&G->stage2_scratch, need * sizeof(float)));
+    G->stage2_floats = need;
+  }
+  float* part = G->stage2_scratch;
+  float* loss_cta = part + (size_t)kS2Floats * (size_t)G->npairs;
+  if (G->nvalid > 0)
+    stage2_pair_kernel<<<G->nvalid, 64, 0, st>>>(G->nvalid, G->valid, G->off, G->lists, G->npairs, pos, rot,
+                                                 log_scale, logit_opacity, shs, samples, ada, lpf, aim_sigma,
+                                                 aim_feature, cell_active, feature_weight, part, loss_cta);
+  stage2_gather_kernel<<<grid_for(G->N, 128), 128, 0, st>>>(G->N, G->g, G->ranges, G->off, G->lists, G->npairs,
+                                                            part, rot, log_scale, logit_opacity, grad_pos, grad_rot,
+                                                            grad_log_scale, grad_logit_opacity, grad_shs);
+  ARAP_LAUNCH_CHECK();
+  if (loss_host && G->nvalid > 0) {
+    std::vector<float> h(2 * (size_t)G->nvalid);
+    ARAP_CUDA_TRY(cudaMemcpyAsync(h.data(), loss_cta, h.size() * sizeof(float), cudaMemcpyDeviceToHost, st));
+    ARAP_CUDA_TRY(cudaStreamSynchronize(st));
+    for (int v = 0; v < G->nvalid; ++v) {
+      loss_host[0] += h[2 * (size_t)v];
+      loss_host[1] += h[2 * (size_t)v + 1];
+    }
+  }
+  return ARAP_OK;
+}
+
+extern "C" int arap_stage2_adam(int N, int step, const float* lr_host, const uint8_t* moved, float* logit_opacity,
+                                float* shs, float* pos, float* rot, float* log_scale, const float* g_opacity,
+                                const float* g_shs, const float* g_pos, const float* g_rot,
+                                const float* g_log_scale, float* m, float* v, arap_stream_t stream) {
+  if (N < 0 || step < 1 || !lr_host || !logit_opacity || !shs || !pos || !rot || !log_scale || !g_opacity ||
+      !g_shs || !g_pos || !g_rot || !g_log_scale || !m || !v)
+    return ARAP_EBADINPUT;
+  if (N == 0) return ARAP_OK;
+  Stage2Adam A;
+  A.p[0] = logit_opacity; A.p[1] = shs; A.p[2] = pos; A.p[3] = rot; A.p[4] = log_scale;
+  A.g[0] = g_opacity; A.g[1] = g_shs; A.g[2] = g_pos; A.g[3] = g_rot; A.g[4] = g_log_scale;
+  for (int a = 0; a < 5; ++a) A.lr[a] = lr_host[a];
+  const double b1 = 0.9, b2 = 0.999;
+  const float bc1 = (float)(1.0 - std::pow(b1, step)), bc2 = (float)(1.0 - std::pow(b2, step));
+  const long long total = (long long)N * kS2Params;
+  stage2_adam_kernel<<<grid_for(total, 256), 256, 0, (cudaStream_t)stream>>>(N, A, moved, m, v, (float)b1, (float)b2,
+                                                                               1e-8f, bc1, bc2);
   ARAP_LAUNCH_CHECK();
   return ARAP_OK;
 }

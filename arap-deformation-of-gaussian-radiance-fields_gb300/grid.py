@@ -76,6 +76,30 @@ class Grid:
             _p(ada) if ada is not None else None, float(lpf_param), _p(sigma), _p(feat), _s()))
         return sigma, feat
 
+    def stage2_loss_grad(self, params, aim_sigma, aim_feature, samples=None, ada=None, lpf_param=None,
+                         cell_active=None, feature_weight=1.0, with_loss=True):
+        """The Stage-II L1 loss and its gradient (arap_stage2_loss_grad).
+
+        ``params``: dict of raw attributes ``pos`` [N,3], ``rot`` [N,4],
+        ``log_scale`` [N,3], ``logit_opacity`` [N], ``shs`` [N,48] of the
+        Gaussians this grid was built over.  Returns ((shape loss, feature
+        loss) or None, dict of gradients shaped as ``params``)."""
+        samples = self.sample_pos if samples is None else _f32(samples)
+        lpf_param = self.lpf_param if lpf_param is None else lpf_param
+        p = {k: _f32(params[k]) for k in ("pos", "rot", "log_scale", "logit_opacity", "shs")}
+        grads = {k: torch.empty_like(v) for k, v in p.items()}
+        act = None
+        if cell_active is not None:
+            act = torch.as_tensor(cell_active, device="cuda").to(torch.uint8).contiguous()
+        loss = (C.c_double * 2)() if with_loss else None
+        check("arap_stage2_loss_grad", _lib.load().arap_stage2_loss_grad(
+            self._h, _p(p["pos"]), _p(p["rot"]), _p(p["log_scale"]), _p(p["logit_opacity"]), _p(p["shs"]),
+            _p(samples), _p(ada) if ada is not None else None, float(lpf_param), _p(_f32(aim_sigma)),
+            _p(_f32(aim_feature)), _p(act) if act is not None else None, float(feature_weight),
+            _p(grads["pos"]), _p(grads["rot"]), _p(grads["log_scale"]), _p(grads["logit_opacity"]),
+            _p(grads["shs"]), C.cast(loss, C.POINTER(C.c_double)) if loss is not None else None, _s()))
+        return ((loss[0], loss[1]) if loss is not None else None), grads
+
     def close(self):
         if getattr(self, "_h", None):
             _lib.load().arap_grid_destroy(self._h)
@@ -103,3 +127,34 @@ def _wrap_i32(ptr, n):
 
 def build_grid(pos, rot, scale, opacity, grid_num, padding=1):
     return Grid(pos, rot, scale, opacity, grid_num, padding)
+
+
+# Learning rates for opacity, SH, mean, quaternion, log-scale (GaussianView.hpp:418).
+STAGE2_LEARNING_RATES = (0.0, 0.002, 0.005, 0.1, 0.0001)
+
+
+class Stage2Adam:
+    """Adam moments of the raw attributes of N Gaussians (arap_stage2_adam)."""
+
+    def __init__(self, N, lr=STAGE2_LEARNING_RATES):
+        self.N = int(N)
+        self.lr = (C.c_float * 5)(*[float(v) for v in lr])
+        self.m = torch.zeros((self.N, 59), dtype=torch.float32, device="cuda")
+        self.v = torch.zeros((self.N, 59), dtype=torch.float32, device="cuda")
+        self.step = 0
+
+    def update(self, params, grads, moved=None):
+        """One step; ``params`` (float32 CUDA tensors, contiguous) is updated in place."""
+        self.step += 1
+        mv = None
+        if moved is not None:
+            mv = torch.as_tensor(moved, device="cuda").to(torch.uint8).contiguous()
+        for k in ("pos", "rot", "log_scale", "logit_opacity", "shs"):
+            t = params[k]
+            if t.dtype != torch.float32 or not t.is_cuda or not t.is_contiguous():
+                raise ValueError("Stage2Adam.update: %s must be a contiguous float32 CUDA tensor" % k)
+        check("arap_stage2_adam", _lib.load().arap_stage2_adam(
+            self.N, self.step, C.cast(self.lr, C.c_void_p), _p(mv) if mv is not None else None,
+            _p(params["logit_opacity"]), _p(params["shs"]), _p(params["pos"]), _p(params["rot"]),
+            _p(params["log_scale"]), _p(grads["logit_opacity"]), _p(grads["shs"]), _p(grads["pos"]),
+            _p(grads["rot"]), _p(grads["log_scale"]), _p(self.m), _p(self.v), _s()))

@@ -395,6 +395,39 @@ int arap_grid_density(const arap_grid* grid, const float* pos, const float* rot,
                       const float* opacity, const float* shs, const float* samples, const float* ada,
                       float lpf, float* sigma_out, float* feature_out, arap_stream_t stream);
 
+/* Stage-II alignment, the library's definition of the step the viewer runs
+ * through the un-vendored rasteriser (L1loss3d + backward3d_grid,
+ * GaussianView.cpp:4398-4448).  Attributes are raw: pos [N*3], rot [N*4]
+ * (w x y z, normalised when used), log_scale [N*3], logit_opacity [N],
+ * shs [N*48], for the N Gaussians the grid was built over (its cell lists are
+ * used as built).  At each sample of the occupied cells (samples as
+ * arap_grid_samples), with the filter ada / lpf as arap_grid_density:
+ *   loss = sum |sigma - aim_sigma| + feature_weight * sum |F - aim_feature|_1
+ * over the samples of cells with cell_active[v] != 0 (all when null), sign(0)
+ * = 0.  Writes the gradient to the raw attributes (grad_* shaped as the
+ * attributes; each Gaussian's pairs summed in ascending cell order, so the
+ * result is deterministic).  loss_host (nullable, synchronises): [2] = shape
+ * and feature loss.  The first call allocates 58 floats per (cell, Gaussian)
+ * pair plus 2 per occupied cell, kept with the grid. */
+int arap_stage2_loss_grad(const arap_grid* grid, const float* pos, const float* rot, const float* log_scale,
+                          const float* logit_opacity, const float* shs, const float* samples, const float* ada,
+                          float lpf, const float* aim_sigma, const float* aim_feature,
+                          const uint8_t* cell_active, float feature_weight, float* grad_pos, float* grad_rot,
+                          float* grad_log_scale, float* grad_logit_opacity, float* grad_shs, double* loss_host,
+                          arap_stream_t stream);
+
+/* One Adam step (update3d's role, GaussianView.cpp:4451-4476) of the raw
+ * attributes of the Gaussians with moved[i] != 0 (all when null), step >= 1
+ * counting from 1, beta1 0.9, beta2 0.999, eps 1e-8.  lr_host [5]: rates for
+ * opacity, SH, mean, quaternion, log-scale (the viewer's defaults are
+ * 0, 0.002, 0.005, 0.1, 0.0001, GaussianView.hpp:418).  m, v [N*59]: moments
+ * per Gaussian in the order opacity | SH 48 | mean 3 | quaternion 4 |
+ * log-scale 3, zero before the first step. */
+int arap_stage2_adam(int N, int step, const float* lr_host, const uint8_t* moved, float* logit_opacity,
+                     float* shs, float* pos, float* rot, float* log_scale, const float* grad_logit_opacity,
+                     const float* grad_shs, const float* grad_pos, const float* grad_rot,
+                     const float* grad_log_scale, float* m, float* v, arap_stream_t stream);
+
 void arap_grid_destroy(arap_grid* grid);
 
 /* -------------------------------------------------------------- PLY IO --- */
