@@ -15,17 +15,27 @@
 //   through the logistic function; SH coefficients are interleaved per
 //   coefficient (rgb) into 48 floats, the bands above D left zero;
 // - the file's `index` property, when present, is rounded to an integer.
+// The file read, the Morton codes and the per-splat decode run on up to 16
+// host threads over fixed contiguous ranges, and the Morton order is a
+// stable radix sort, so the result does not depend on the thread count.
 // Saving (GaussianView.cpp:264-339): splats outside the box [box_min,
 // box_max] or flagged too small are dropped; scales are stored as logs,
 // opacities as logits, quaternions as given, normals as zero, SH degree 3.
+#include <fcntl.h>
+#include <unistd.h>
+
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdint>
 #include <cstdio>
 #include <cstring>
 #include <fstream>
+#include <memory>
+#include <new>
 #include <sstream>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/arap_gb300.h"
@@ -131,6 +141,73 @@ uint64_t morton_code(const float* p, const float* lo, const float* hi) {
   return code;
 }
 
+// Host threads for the per-splat loops: up to 16, one per 16k splats.
+int worker_count(size_t n) {
+  const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+  const size_t by_size = n / 16384 + 1;
+  return (int)std::min<size_t>(std::min<size_t>(hw, 16), by_size);
+}
+
+// Runs f(thread, begin, end) over nt contiguous chunks of [0, n); chunk t
+// always covers the same range, so per-thread partial results are
+// deterministic.
+template <class F>
+void parallel_chunks(size_t n, int nt, F f) {
+  if (nt <= 1) {
+    f(0, 0, n);
+    return;
+  }
+  std::vector<std::thread> pool;
+  pool.reserve(nt - 1);
+  for (int t = 1; t < nt; ++t)
+    pool.emplace_back([&f, t, n, nt] { f(t, n * t / nt, n * (t + 1) / nt); });
+  f(0, 0, n / nt);
+  for (auto& th : pool) th.join();
+}
+
+// Stable LSD radix sort of `order` by `key` (both permuted together), 16-bit
+// digits; digits that are equal for every key are skipped.
+void radix_sort_stable(std::vector<uint64_t>& key, std::vector<uint32_t>& order) {
+  const size_t n = key.size();
+  std::vector<uint64_t> k2(n);
+  std::vector<uint32_t> o2(n);
+  std::vector<size_t> count(65537);
+  for (int shift = 0; shift < 64; shift += 16) {
+    std::fill(count.begin(), count.end(), 0);
+    for (size_t i = 0; i < n; ++i) ++count[((key[i] >> shift) & 0xffffu) + 1];
+    if (count[((key[0] >> shift) & 0xffffu) + 1] == n) continue;
+    for (size_t d = 1; d < count.size(); ++d) count[d] += count[d - 1];
+    for (size_t i = 0; i < n; ++i) {
+      const size_t dst = count[(key[i] >> shift) & 0xffffu]++;
+      k2[dst] = key[i];
+      o2[dst] = order[i];
+    }
+    key.swap(k2);
+    order.swap(o2);
+  }
+}
+
+// Reads [offset, offset + bytes) of the file into dst with nt threads, each
+// issuing pread on its own contiguous range.  False on any short read.
+bool read_parallel(const char* path, size_t offset, char* dst, size_t bytes, int nt) {
+  const int fd = ::open(path, O_RDONLY);
+  if (fd < 0) return false;
+  std::atomic<bool> ok{true};
+  parallel_chunks(bytes, nt, [&](int, size_t b, size_t e) {
+    size_t done = b;
+    while (done < e) {
+      const ssize_t r = ::pread(fd, dst + done, e - done, (off_t)(offset + done));
+      if (r <= 0) {
+        ok = false;
+        return;
+      }
+      done += (size_t)r;
+    }
+  });
+  ::close(fd);
+  return ok.load();
+}
+
 }  // namespace
 
 extern "C" int arap_ply_info(const char* path, int64_t* count, int* sh_degree, int* has_index) {
@@ -156,9 +233,15 @@ extern "C" int arap_ply_load(const char* path, int64_t count, int morton_order, 
   if (rc != ARAP_OK) return rc;
   if (count != (int64_t)L.count || (index && !L.has_index)) return ARAP_EBADINPUT;
   const size_t P = L.props.size(), N = (size_t)L.count;
-  std::vector<float> rec(P * N);
-  in.seekg(L.data_start);
-  if (N > 0 && !in.read(reinterpret_cast<char*>(rec.data()), (std::streamsize)(rec.size() * sizeof(float))))
+  if (N > (size_t)UINT32_MAX) return ARAP_EUNSUPPORTED;
+  // the records, read by several threads at once (uninitialised buffer: every
+  // byte is read or the call fails)
+  std::unique_ptr<float[]> rec_buf(new (std::nothrow) float[std::max<size_t>(P * N, 1)]);
+  if (!rec_buf) return ARAP_ENOMEM;
+  const float* const rec = rec_buf.get();
+  in.close();
+  if (N > 0 && !read_parallel(path, (size_t)L.data_start, reinterpret_cast<char*>(rec_buf.get()),
+                              P * N * sizeof(float), worker_count(N)))
     return ARAP_EBADINPUT;
   const int ix = L.at("x"), iop = L.at("opacity"), isc = L.at("scale_0"), irot = L.at("rot_0");
   const int isx = L.at("scale_1"), isy = L.at("scale_2");
@@ -170,44 +253,59 @@ extern "C" int arap_ply_load(const char* path, int64_t count, int morton_order, 
   for (int i = 0; i < 3 * (K - 1); ++i) irest[i] = L.at("f_rest_" + std::to_string(i));
   const int iidx = L.at("index");
 
-  // bounding box and the processing order
-  float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+  // bounding box: per-thread partial min/max, combined (order-independent)
+  const int nt = worker_count(N);
+  std::vector<float> part_lo((size_t)nt * 3, INFINITY), part_hi((size_t)nt * 3, -INFINITY);
   const int ipos[3] = {ix, iy, iz};
-  for (size_t i = 0; i < N; ++i)
+  parallel_chunks(N, nt, [&](int t, size_t b, size_t e) {
+    float* l = part_lo.data() + 3 * t;
+    float* h = part_hi.data() + 3 * t;
+    for (size_t i = b; i < e; ++i)
+      for (int a = 0; a < 3; ++a) {
+        const float v = rec[i * P + ipos[a]];
+        l[a] = std::min(l[a], v);
+        h[a] = std::max(h[a], v);
+      }
+  });
+  float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+  for (int t = 0; t < nt; ++t)
     for (int a = 0; a < 3; ++a) {
-      const float v = rec[i * P + ipos[a]];
-      lo[a] = std::min(lo[a], v);
-      hi[a] = std::max(hi[a], v);
+      lo[a] = std::min(lo[a], part_lo[3 * t + a]);
+      hi[a] = std::max(hi[a], part_hi[3 * t + a]);
     }
-  std::vector<size_t> order(N);
-  for (size_t i = 0; i < N; ++i) order[i] = i;
+  // the processing order: a stable sort by Morton code keeps ties in file order
+  std::vector<uint32_t> order(N);
+  for (size_t i = 0; i < N; ++i) order[i] = (uint32_t)i;
   if (morton_order && N > 1) {
-    std::vector<std::pair<uint64_t, size_t>> key(N);
-    for (size_t i = 0; i < N; ++i) {
-      const float p3[3] = {rec[i * P + ix], rec[i * P + iy], rec[i * P + iz]};
-      key[i] = {morton_code(p3, lo, hi), i};
-    }
-    std::sort(key.begin(), key.end());  // (code, file position): ties stay in file order
-    for (size_t i = 0; i < N; ++i) order[i] = key[i].second;
+    std::vector<uint64_t> code(N);
+    parallel_chunks(N, nt, [&](int, size_t b, size_t e) {
+      for (size_t i = b; i < e; ++i) {
+        const float p3[3] = {rec[i * P + ix], rec[i * P + iy], rec[i * P + iz]};
+        code[i] = morton_code(p3, lo, hi);
+      }
+    });
+    radix_sort_stable(code, order);
   }
-  for (size_t k = 0; k < N; ++k) {
-    const float* r = rec.data() + order[k] * P;
-    for (int a = 0; a < 3; ++a) pos[3 * k + a] = r[ipos[a]];
-    const float q[4] = {r[irot], r[ir1], r[ir2], r[ir3]};
-    float len2 = 0.f;
-    for (int j = 0; j < 4; ++j) len2 += q[j] * q[j];
-    const float len = std::sqrt(len2);
-    for (int j = 0; j < 4; ++j) rot[4 * k + j] = q[j] / len;
+  parallel_chunks(N, nt, [&](int, size_t kb, size_t ke) {
     const int is3[3] = {isc, isx, isy};
-    for (int a = 0; a < 3; ++a) scale[3 * k + a] = std::exp(r[is3[a]]);
-    opacity[k] = 1.0f / (1.0f + std::exp(-r[iop]));
-    float* sh = shs + (size_t)kShFloats * k;
-    for (int e = 0; e < kShFloats; ++e) sh[e] = 0.f;
-    for (int c = 0; c < 3; ++c) sh[c] = r[idc[c]];
-    for (int j = 1; j < K; ++j)
-      for (int c = 0; c < 3; ++c) sh[3 * j + c] = r[irest[(size_t)c * (K - 1) + (j - 1)]];
-    if (index) index[k] = (int32_t)std::lround(r[iidx]);
-  }
+    for (size_t k = kb; k < ke; ++k) {
+      const float* r = rec + (size_t)order[k] * P;
+      for (int a = 0; a < 3; ++a) pos[3 * k + a] = r[ipos[a]];
+      const float q[4] = {r[irot], r[ir1], r[ir2], r[ir3]};
+      float len2 = 0.f;
+      for (int j = 0; j < 4; ++j) len2 += q[j] * q[j];
+      const float len = std::sqrt(len2);
+      for (int j = 0; j < 4; ++j) rot[4 * k + j] = q[j] / len;
+      for (int a = 0; a < 3; ++a) scale[3 * k + a] = std::exp(r[is3[a]]);
+      opacity[k] = 1.0f / (1.0f + std::exp(-r[iop]));
+      float* sh = shs + (size_t)kShFloats * k;
+      for (int e = 0; e < kShFloats; ++e) sh[e] = 0.f;
+      for (int c = 0; c < 3; ++c) sh[c] = r[idc[c]];
+      for (int j = 1; j < K; ++j)
+        for (int c = 0; c < 3; ++c) sh[3 * j + c] = r[irest[(size_t)c * (K - 1) + (j - 1)]];
+      if (index) index[k] = (int32_t)std::lround(r[iidx]);
+    }
+  });
   if (box_min)
     for (int a = 0; a < 3; ++a) box_min[a] = lo[a];
   if (box_max)
