@@ -324,8 +324,17 @@ extern "C" int arap_ply_save(const char* path, int64_t count, const float* pos, 
       if (pos[3 * i + a] < box_min[a] || pos[3 * i + a] > box_max[a]) return false;
     return !(too_small && too_small[i]);
   };
-  int64_t n = 0;
-  for (int64_t i = 0; i < count; ++i) n += kept(i) ? 1 : 0;
+  // kept splats per fixed chunk, then each chunk encodes into its own range
+  const size_t total = (size_t)count;
+  const int nt = worker_count(total);
+  std::vector<int64_t> chunk_kept((size_t)nt + 1, 0);
+  parallel_chunks(total, nt, [&](int t, size_t b, size_t e) {
+    int64_t c = 0;
+    for (size_t i = b; i < e; ++i) c += kept((int64_t)i) ? 1 : 0;
+    chunk_kept[(size_t)t + 1] = c;
+  });
+  for (int t = 0; t < nt; ++t) chunk_kept[(size_t)t + 1] += chunk_kept[(size_t)t];
+  const int64_t n = chunk_kept[(size_t)nt];
   std::ofstream out(path, std::ios_base::binary);
   if (!out.good()) return ARAP_EBADINPUT;
   out << "ply\nformat binary_little_endian 1.0\nelement vertex " << n << "\n";
@@ -336,22 +345,26 @@ extern "C" int arap_ply_save(const char* path, int64_t count, const float* pos, 
   for (const char* t : tail) out << "property float " << t << "\n";
   out << "end_header\n";
   constexpr int R = 62;
-  std::vector<float> rec((size_t)R * (size_t)n, 0.f);
-  int64_t k = 0;
-  for (int64_t i = 0; i < count; ++i) {
-    if (!kept(i)) continue;
-    float* r = rec.data() + (size_t)R * k;
-    for (int a = 0; a < 3; ++a) r[a] = pos[3 * i + a];  // normals (3..5) stay zero
-    const float* sh = shs + (size_t)kShFloats * i;
-    for (int c = 0; c < 3; ++c) r[6 + c] = sh[c];
-    for (int j = 1; j < 16; ++j)
-      for (int c = 0; c < 3; ++c) r[9 + c * 15 + (j - 1)] = sh[3 * j + c];
-    const float o = opacity[i];
-    r[54] = std::log(o / (1.0f - o));
-    for (int a = 0; a < 3; ++a) r[55 + a] = std::log(scale[3 * i + a]);
-    for (int j = 0; j < 4; ++j) r[58 + j] = rot[4 * i + j];
-    ++k;
-  }
+  std::vector<float> rec((size_t)R * (size_t)n);
+  parallel_chunks(total, nt, [&](int t, size_t b, size_t e) {
+    int64_t k = chunk_kept[(size_t)t];
+    for (size_t ii = b; ii < e; ++ii) {
+      const int64_t i = (int64_t)ii;
+      if (!kept(i)) continue;
+      float* r = rec.data() + (size_t)R * (size_t)k;
+      for (int a = 0; a < 3; ++a) r[a] = pos[3 * i + a];
+      r[3] = r[4] = r[5] = 0.f;  // normals
+      const float* sh = shs + (size_t)kShFloats * i;
+      for (int c = 0; c < 3; ++c) r[6 + c] = sh[c];
+      for (int j = 1; j < 16; ++j)
+        for (int c = 0; c < 3; ++c) r[9 + c * 15 + (j - 1)] = sh[3 * j + c];
+      const float o = opacity[i];
+      r[54] = std::log(o / (1.0f - o));
+      for (int a = 0; a < 3; ++a) r[55 + a] = std::log(scale[3 * i + a]);
+      for (int j = 0; j < 4; ++j) r[58 + j] = rot[4 * i + j];
+      ++k;
+    }
+  });
   if (n > 0) out.write(reinterpret_cast<const char*>(rec.data()), (std::streamsize)(rec.size() * sizeof(float)));
   if (!out.good()) return ARAP_EBADINPUT;
   if (written) *written = n;

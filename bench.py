@@ -428,11 +428,10 @@ def ply_leg(sc, reps=3):
         mb = os.path.getsize(path) / 1e6
     assert out["pos"].shape[0] == sc.pos.shape[0]
     n = int(sc.pos.shape[0])
-    # the loader's host threads: up to 16, one per 16k splats; the save is one thread
-    load_threads = min(os.cpu_count() or 1, 16, n // 16384 + 1)
+    # host threads of the load and the save encode: up to 16, one per 16k splats
+    threads = min(os.cpu_count() or 1, 16, n // 16384 + 1)
     return {"splats": n, "file_mb": round(mb, 1), "save_ms": round(1e3 * t_save, 1),
-            "load_ms": round(1e3 * t_load, 1), "load_mb_per_s": round(mb / t_load, 1),
-            "load_threads": load_threads, "save_threads": 1}
+            "load_ms": round(1e3 * t_load, 1), "load_mb_per_s": round(mb / t_load, 1), "threads": threads}
 
 
 # ------------------------------------------------------- CPU baseline ----
