@@ -37,7 +37,8 @@ enum {
   ARAP_EBADINPUT = 3,     /* invalid sizes / indices / null pointers */
   ARAP_ETIMEOUT = 4,      /* a bounded device-side wait gave up */
   ARAP_ECUDA = 5,         /* a CUDA runtime call failed */
-  ARAP_ENOMEM = 6,        /* device allocation inside a handle failed */
+  ARAP_ENOMEM = 6,        /* an allocation failed: device memory inside a handle, or the PLY
+                             loader's host buffer */
   ARAP_EUNSUPPORTED = 7   /* parameter outside the compiled range (e.g. k > 12) */
 };
 
@@ -447,7 +448,8 @@ int arap_ply_info(const char* path, int64_t* count, int* sh_degree, int* has_ind
  * stored). morton_order != 0 reorders the splats by the viewer's 21-bit-per-axis
  * Morton code over the bounding box (ties in file order), as loadPly does.
  * box_min/box_max [3] (nullable): the bounding box. index [count] (nullable;
- * requires the property): the rounded `index` property. */
+ * requires the property): the rounded `index` property.  Runs on up to 16
+ * host threads; the result does not depend on their number. */
 int arap_ply_load(const char* path, int64_t count, int morton_order, float* pos, float* shs, float* opacity,
                   float* scale, float* rot, float* box_min, float* box_max, int32_t* index);
 
