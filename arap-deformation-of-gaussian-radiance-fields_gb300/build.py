@@ -20,7 +20,7 @@ OBJ = os.path.join(HERE, "_build")
 SOURCES = ["api.cu", "knn.cu", "skin.cu", "solver.cu", "grid.cu", "ply.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-rdc=true", "-Xcompiler", "-fPIC",
-         "-Xcompiler", "-O2", "-I", INCLUDE]
+         "-Xcompiler", "-O2", "-Xcompiler", "-pthread", "-I", INCLUDE]
 
 
 def nvcc() -> str:
@@ -64,7 +64,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
     with cf.ThreadPoolExecutor(max_workers=min(8, len(srcs))) as ex:
         objs = list(ex.map(compile_one, srcs))
     tmp = LIB + ".tmp"
-    cmd = [cc, *ARCH, "-shared", "-Xcompiler", "-fPIC", *objs, "-o", tmp]
+    cmd = [cc, *ARCH, "-shared", "-Xcompiler", "-fPIC", *objs, "-lpthread", "-o", tmp]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("link failed:\n%s\n%s" % (r.stdout, r.stderr))
