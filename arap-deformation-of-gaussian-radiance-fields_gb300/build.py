@@ -17,7 +17,7 @@ CSRC = os.path.join(HERE, "csrc")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 LIB = os.path.join(HERE, "libarap_gb300.so")
 OBJ = os.path.join(HERE, "_build")
-SOURCES = ["api.cu", "knn.cu", "skin.cu", "solver.cu", "grid.cu", "ply.cpp"]
+SOURCES = ["api.cu", "knn.cu", "skin.cu", "solver.cu", "grid.cu", "raster.cu", "ply.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-rdc=true", "-Xcompiler", "-fPIC",
          "-Xcompiler", "-O2", "-Xcompiler", "-pthread", "-I", INCLUDE]

@@ -431,6 +431,27 @@ int arap_stage2_adam(int N, int step, const float* lr_host, const uint8_t* moved
 
 void arap_grid_destroy(arap_grid* grid);
 
+/* ------------------------------------------------------------ render --- */
+
+/* Headless rasteriser of N Gaussians into a device image, the published 3D
+ * Gaussian splatting forward standing in for the un-vendored
+ * CudaRasterizer::forward the viewer draws the deformed field with
+ * (GaussianView.cpp:1066-1127); no window or GL interop.  Activated
+ * attributes as the skinning writes them: pos [N*3], shs [N*48] (interleaved
+ * rgb per coefficient, the first (sh_degree+1)^2 used), opacity [N], scale
+ * [N*3], rot [N*4] (w x y z, 16-byte aligned).  view_host, proj_host [16]:
+ * row-major world->camera and world->clip matrices (camera looks along +z);
+ * campos_host [3]; background_host [3].  image_out [3*height*width] planes;
+ * final_t_out [height*width] (nullable): the transmittance left;
+ * n_contrib_out (nullable): the Gaussians composited per pixel.  A 16x16
+ * tile may list at most 16384 Gaussians (else ARAP_EUNSUPPORTED).
+ * Allocates stream-ordered scratch and synchronises. */
+int arap_render(int N, const float* pos, const float* shs, const float* opacity, const float* scale,
+                const float* rot, float scale_modifier, int sh_degree, const float* view_host,
+                const float* proj_host, const float* campos_host, float tan_fovx, float tan_fovy, int width,
+                int height, const float* background_host, float* image_out, float* final_t_out,
+                int32_t* n_contrib_out, arap_stream_t stream);
+
 /* -------------------------------------------------------------- PLY IO --- */
 
 /* 3D Gaussian splatting binary PLY files, host memory only (no device call;
