@@ -99,6 +99,7 @@ SIGNATURES = {
     "arap_grid_density": (I, [P, P, P, P, P, P, P, P, F, P, P, P]),
     "arap_stage2_loss_grad": (I, [P, P, P, P, P, P, P, P, F, P, P, P, F, P, P, P, P, P, C.POINTER(D), P]),
     "arap_stage2_adam": (I, [I, I, P, P, P, P, P, P, P, P, P, P, P, P, P, P, P]),
+    "arap_stage2_cell_flags": (I, [P, P, P, P, P]),
     "arap_grid_destroy": (None, [P]),
     "arap_render": (I, [I, P, P, P, P, P, F, I, P, P, P, F, F, I, I, P, P, P, P, P]),
     "arap_get_device_status": (I, [P]),

@@ -782,6 +782,49 @@ __global__ void stage2_adam_kernel(int N, Stage2Adam A, const uint8_t* __restric
   A.p[a][idx] -= A.lr[a] * (mm / bc1) / (sqrtf(vv / bc2) + eps);
 }
 
+// JudgeEmptyGrid (GaussianView.cpp:4272-4316) and ExpandOpRange
+// (GaussianView.cpp:4319-4360) over the occupied cells: a cell marks itself
+// and its six face neighbours (clamped to the grid) in a g^3 byte map.
+__device__ __forceinline__ void mark_with_neighbours(int c, int g, uint8_t* __restrict__ map) {
+  const int x = c / (g * g), y = (c / g) % g, z = c % g;
+  map[c] = 1;
+  map[(size_t)max(x - 1, 0) * g * g + y * g + z] = 1;
+  map[(size_t)min(x + 1, g - 1) * g * g + y * g + z] = 1;
+  map[(size_t)x * g * g + max(y - 1, 0) * g + z] = 1;
+  map[(size_t)x * g * g + min(y + 1, g - 1) * g + z] = 1;
+  map[(size_t)x * g * g + y * g + max(z - 1, 0)] = 1;
+  map[(size_t)x * g * g + y * g + min(z + 1, g - 1)] = 1;
+}
+
+// mode 0: cells whose 64 aim opacities, summed in order in float, exceed 1e-6
+// mark; mode 1: cells not converged mark.
+__global__ void cell_mark_kernel(int nvalid, const int* __restrict__ valid, int g, int mode,
+                                 const float* __restrict__ aim_opacity, const uint8_t* __restrict__ converged,
+                                 uint8_t* __restrict__ map) {
+  const int v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= nvalid) return;
+  bool mark;
+  if (mode == 0) {
+    float tot = 0.f;
+    for (int j = 0; j < 64; ++j) tot = __fadd_rn(tot, aim_opacity[(size_t)v * 64 + j]);
+    mark = (double)tot > 1e-6;
+  } else {
+    mark = converged[v] == 0;
+  }
+  if (mark) mark_with_neighbours(valid[v], g, map);
+}
+
+// mode 0: empty_out[v] = 1 for an unmarked cell; mode 1: converged_io[v] = 0
+// for a marked cell.
+__global__ void cell_flag_kernel(int nvalid, const int* __restrict__ valid, int mode,
+                                 const uint8_t* __restrict__ map, uint8_t* __restrict__ out) {
+  const int v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= nvalid) return;
+  const bool m = map[valid[v]] != 0;
+  if (mode == 0) out[v] = m ? 0 : 1;
+  else if (m) out[v] = 0;
+}
+
 }  // namespace arap
 
 // ------------------------------------------------------------------ host --
@@ -1085,6 +1128,31 @@ extern "C" int arap_stage2_adam(int N, int step, const float* lr_host, const uin
                                                                                1e-8f, bc1, bc2);
   ARAP_LAUNCH_CHECK();
   return ARAP_OK;
+}
+
+extern "C" int arap_stage2_cell_flags(const arap_grid* G, const float* aim_opacity, uint8_t* empty_out,
+                                      uint8_t* converged_io, arap_stream_t stream) {
+  if (!G || (!empty_out && !converged_io) || (empty_out && !aim_opacity)) return ARAP_EBADINPUT;
+  if (G->nvalid == 0) return ARAP_OK;
+  cudaStream_t st = (cudaStream_t)stream;
+  const size_t cells = (size_t)G->g * G->g * G->g;
+  uint8_t* map = nullptr;
+  ARAP_CUDA_TRY(cudaMallocAsync(&map, cells, st));
+  int rc = ARAP_OK;
+  for (int mode = 0; mode < 2 && rc == ARAP_OK; ++mode) {
+    uint8_t* out = mode == 0 ? empty_out : converged_io;
+    if (!out) continue;
+    if (cudaMemsetAsync(map, 0, cells, st) != cudaSuccess) {
+      rc = ARAP_ECUDA;
+      break;
+    }
+    cell_mark_kernel<<<grid_for(G->nvalid, 256), 256, 0, st>>>(G->nvalid, G->valid, G->g, mode, aim_opacity,
+                                                                 converged_io, map);
+    cell_flag_kernel<<<grid_for(G->nvalid, 256), 256, 0, st>>>(G->nvalid, G->valid, mode, map, out);
+    if (cudaPeekAtLastError() != cudaSuccess) rc = ARAP_ECUDA;
+  }
+  cudaFreeAsync(map, st);
+  return rc;
 }
 
 // ------------------------------------------- allocation-free centre order ----

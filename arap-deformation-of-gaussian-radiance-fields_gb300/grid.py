@@ -100,6 +100,22 @@ class Grid:
             _p(grads["shs"]), C.cast(loss, C.POINTER(C.c_double)) if loss is not None else None, _s()))
         return ((loss[0], loss[1]) if loss is not None else None), grads
 
+    def stage2_cell_flags(self, aim_opacity=None, converged=None):
+        """(empty [n_valid] uint8 or None, converged [n_valid] uint8 or None):
+        JudgeEmptyGrid from the samples' aim opacities and ExpandOpRange of
+        ``converged`` (arap_stage2_cell_flags)."""
+        empty = None
+        if aim_opacity is not None:
+            aim_opacity = _f32(aim_opacity)
+            empty = torch.empty((self.n_valid,), dtype=torch.uint8, device="cuda")
+        conv = None
+        if converged is not None:
+            conv = torch.as_tensor(converged, device="cuda").to(torch.uint8).contiguous().clone()
+        check("arap_stage2_cell_flags", _lib.load().arap_stage2_cell_flags(
+            self._h, _p(aim_opacity) if aim_opacity is not None else None,
+            _p(empty) if empty is not None else None, _p(conv) if conv is not None else None, _s()))
+        return empty, conv
+
     def close(self):
         if getattr(self, "_h", None):
             _lib.load().arap_grid_destroy(self._h)

@@ -429,6 +429,18 @@ int arap_stage2_adam(int N, int step, const float* lr_host, const uint8_t* moved
                      const float* grad_shs, const float* grad_pos, const float* grad_rot,
                      const float* grad_log_scale, float* m, float* v, arap_stream_t stream);
 
+/* Cell flags of the Stage-II loop over the grid's occupied cells, both
+ * nullable (at least one given):
+ * - empty_out [n_valid] (JudgeEmptyGrid, GaussianView.cpp:4272-4316): 1 for a
+ *   cell that neither holds target density (its 64 aim_opacity values, summed
+ *   in order in float, exceed 1e-6) nor is a face neighbour of such a cell;
+ * - converged_io [n_valid] (ExpandOpRange, GaussianView.cpp:4319-4360): every
+ *   cell that is a face neighbour of a cell not converged becomes not
+ *   converged (0); flags are bytes, nonzero = converged.
+ * aim_opacity [n_valid*64] is needed for empty_out. */
+int arap_stage2_cell_flags(const arap_grid* grid, const float* aim_opacity, uint8_t* empty_out,
+                           uint8_t* converged_io, arap_stream_t stream);
+
 void arap_grid_destroy(arap_grid* grid);
 
 /* ------------------------------------------------------------ render --- */

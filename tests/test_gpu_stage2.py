@@ -85,3 +85,22 @@ def test_adam_matches_the_oracle():
         np.testing.assert_allclose(a, getattr(P, k), atol=1e-6, err_msg=k)
         assert torch.equal(dev[k][torch.from_numpy(~moved).cuda()], before[k][torch.from_numpy(~moved).cuda()])
     g.close()
+
+
+def test_cell_flags_match_the_oracle():
+    import torch
+    from oracle import stage2 as s2
+    grid_mod = importlib.import_module(PKG + ".grid")
+    p, _ = _scene(seed=3, N=400)
+    dev = {k: torch.from_numpy(v).cuda() for k, v in p.items()}
+    g = grid_mod.Grid(dev["pos"], dev["rot"], torch.exp(dev["log_scale"]), torch.sigmoid(dev["logit_opacity"]), 8)
+    _, _, valid = (a.cpu().numpy() for a in g.arrays())
+    rng = np.random.default_rng(4)
+    aim_op = np.zeros((g.n_valid, 64), np.float32)
+    dense = rng.random(g.n_valid) < 0.2
+    aim_op[dense] = rng.uniform(0, 1e-3, (int(dense.sum()), 64)).astype(np.float32)
+    conv = (rng.random(g.n_valid) < 0.8).astype(np.uint8)
+    empty, conv2 = g.stage2_cell_flags(torch.from_numpy(aim_op.reshape(-1)).cuda(), torch.from_numpy(conv).cuda())
+    np.testing.assert_array_equal(empty.cpu().numpy(), s2.judge_empty_cells(valid, aim_op.reshape(-1), 8))
+    np.testing.assert_array_equal(conv2.cpu().numpy().astype(bool), s2.expand_converged(valid, conv.astype(bool), 8))
+    g.close()
