@@ -174,3 +174,19 @@ class Stage2Adam:
             _p(params["logit_opacity"]), _p(params["shs"]), _p(params["pos"]), _p(params["rot"]),
             _p(params["log_scale"]), _p(grads["logit_opacity"]), _p(grads["shs"]), _p(grads["pos"]),
             _p(grads["rot"]), _p(grads["log_scale"]), _p(self.m), _p(self.v), _s()))
+
+
+def stage2_align(grid, params, aim_sigma, aim_feature, steps=101, moved=None, lr=STAGE2_LEARNING_RATES,
+                 feature_weight=1.0, ada=None, lpf_param=None, cell_active=None):
+    """The Stage-II loop (GPUOptimize, GaussianView.cpp:4363-4486, run
+    ``_optimize_steps`` = 101 times, GaussianView.hpp:420): loss and gradient,
+    then an Adam step of the moved Gaussians, ``steps`` times.  ``params`` is
+    updated in place; returns the (shape, feature) loss before each step."""
+    opt = Stage2Adam(params["pos"].shape[0], lr)
+    losses = []
+    for _ in range(int(steps)):
+        loss, grads = grid.stage2_loss_grad(params, aim_sigma, aim_feature, ada=ada, lpf_param=lpf_param,
+                                            cell_active=cell_active, feature_weight=feature_weight)
+        losses.append(loss)
+        opt.update(params, grads, moved=moved)
+    return losses

@@ -104,3 +104,26 @@ def test_cell_flags_match_the_oracle():
     np.testing.assert_array_equal(empty.cpu().numpy(), s2.judge_empty_cells(valid, aim_op.reshape(-1), 8))
     np.testing.assert_array_equal(conv2.cpu().numpy().astype(bool), s2.expand_converged(valid, conv.astype(bool), 8))
     g.close()
+
+
+def test_align_loop_follows_the_oracle():
+    import torch
+    grid_mod = importlib.import_module(PKG + ".grid")
+    p, t = _scene(seed=5)
+    dev = {k: torch.from_numpy(v).cuda() for k, v in p.items()}
+    g = grid_mod.Grid(dev["pos"], dev["rot"], torch.exp(dev["log_scale"]), torch.sigmoid(dev["logit_opacity"]), 8)
+    s2, P, samples, ps, pg, aim_s, aim_f = _oracle_case(g, p, t)
+    lr = (0.01, 0.002, 0.002, 0.01, 0.005)
+    losses = grid_mod.stage2_align(g, dev, torch.from_numpy(aim_s).cuda(), torch.from_numpy(aim_f).cuda(),
+                                   steps=10, lr=lr)
+    st = s2.AdamState()
+    ref = []
+    for _ in range(10):
+        sl, fl, G = s2.loss_and_grad(P, samples, g.lpf_param, ps, pg, aim_s.astype(np.float64),
+                                     aim_f.astype(np.float64))
+        ref.append(sl + fl)
+        s2.adam_update(P, G, st, lr=dict(zip(("opacity", "shs", "pos", "rot", "scale"), lr)))
+    got = [a + b for a, b in losses]
+    assert got[-1] < got[0]
+    np.testing.assert_allclose(got, ref, rtol=1e-2)
+    g.close()
