@@ -9,9 +9,10 @@ re-anchoring.  Every step starts from the same rest state (restored by device
 copies inside the step) so each step does identical work.
 
 --impl ours       the CUDA library (default)
---impl reference  the reference's algorithm on the host cores (the oracle
-                  port: the reference itself needs Eigen/SIBR and cannot be
-                  built here), a bounded sample per step
+--impl reference  the reference's CPU path on the host cores, restated in
+                  C++/OpenMP float64 (oracle/cpu_frame.cpp; the reference
+                  itself needs Eigen/SIBR and cannot be built here), one full
+                  frame per step
 
 Prints one JSON line (rank 0).
 """
@@ -400,7 +401,7 @@ def run_ours(a):
     if rank == 0:
         line["ply_io"] = ply_leg(sc)
     if rank == 0 and not a.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline(sc, samples=1)
+        line["cpu_baseline"] = cpu_baseline(sc)
     if rank == 0:
         print(json.dumps(line))
     if ws > 1:
@@ -436,46 +437,32 @@ def ply_leg(sc, reps=3):
 
 # ------------------------------------------------------- CPU baseline ----
 
-def _oracle_frame_sample(sc, gn_iters=1, skin_n=50_000, t_gn_known=None):
-    """Time the oracle port on a bounded sample of one frame: gn_iters
-    Gauss-Newton iterations of the full solve (exact sparse solve; skipped
-    when t_gn_known, the seconds of one iteration measured earlier in the
-    run, is given) and the skinning of skin_n Gaussians; returns the
-    extrapolated ms/frame."""
-    import numpy as np
-    from oracle import ed, skin, targets
+def _cpu_frame(sc):
+    """The C++/OpenMP FP64 restatement of the reference's CPU frame
+    (oracle/cpu_frame.cpp), set up on all host threads."""
+    from oracle import cpu_frame
     t0 = time.perf_counter()
-    nb = ed.build_graph(sc.node_pos, sc.k)
-    aidx, aw = ed.knn_weights(sc.pos[sc.node_vertex], sc.node_pos, sc.k)
-    act = np.concatenate([b for b, t in zip(sc.blocks, sc.block_type) if t == 1])
-    aims = targets.twist(sc.node_pos, sc.node_pos, act, sc.op[1], sc.op[2]) if sc.op[0] == "twist" else \
-        targets.translate(sc.node_pos, act, sc.op[1])
-    pr = ed.EDProblem(sc.node_pos, nb, aidx, aw, sc.blocks, sc.block_type, aims)
-    t_setup = time.perf_counter() - t0
-    t1 = time.perf_counter()
-    if t_gn_known is None:
-        x, _ = ed.gauss_newton(pr, max_iters=gn_iters, early_exit=False)
-        t_gn = (time.perf_counter() - t1) / gn_iters
-    else:
-        x, t_gn = ed.identity_x(pr.F), t_gn_known
-    rot, tr = ed.put_free_inputs(pr, x)
-    m = min(skin_n, sc.n_gauss)
-    E = skin.end_points(sc.pos[:m], sc.rot[:m], sc.scale[:m])
-    idx, w = ed.knn_weights(E.reshape(-1, 3), sc.node_pos, sc.k)
-    t2 = time.perf_counter()
-    skin.skin_gaussians(E, idx, w, rot, tr, sc.node_pos, sc.rot[:m], sc.scale[:m], sc.shs[:m])
-    t_skin = (time.perf_counter() - t2) * sc.n_gauss / m
-    ms = (t_gn * sc.iters + t_skin) * 1e3
-    return ms, t_setup, t_gn, t_skin
+    fb = cpu_frame.FrameBaseline(sc)
+    return fb, time.perf_counter() - t0
 
 
-def cpu_baseline(sc, samples=1):
-    ms, _, t_gn, t_skin = _oracle_frame_sample(sc)
-    return {"value": round(ms, 1), "unit": "ms/frame", "cores": 1, "kind": "port",
-            "sample": "oracle (numpy/scipy, float64): 1 Gauss-Newton iteration of the full %d-node solve "
-                      "(exact sparse solve) x %d iterations + skinning of 50k of %d Gaussians x %d; "
-                      "per-iteration %.2f s, skinning %.2f s" % (sc.n_nodes, sc.iters, sc.n_gauss,
-                                                                 sc.n_gauss // 50_000, t_gn, t_skin)}
+def _cpu_sample_text(fb, parts, st):
+    sc = fb.sc
+    return ("one full frame on the host cores, no extrapolation: C++/OpenMP float64 restatement of the "
+            "reference's CPU path (oracle/cpu_frame.cpp): %d-iteration Gauss-Newton solve of %d free nodes "
+            "(J in CSR, J^T J, block sparse Cholesky with a minimum-degree ordering, %.1f GFLOP per "
+            "factorisation, one factorisation per iteration where the reference does two), skinning of %d "
+            "samples and %d Gaussians, node update; ms: solve %.0f (factorisations %.0f), samples %.0f, "
+            "Gaussians %.0f, nodes %.0f" % (sc.iters, st["n_free"], st["factor_gflop"], fb.n_samples,
+                                            sc.n_gauss, parts["solve"], 1e3 * st["t_factor"],
+                                            parts["skin_samples"], parts["skin_gaussians"], parts["update_nodes"]))
+
+
+def cpu_baseline(sc):
+    fb, t_setup = _cpu_frame(sc)
+    ms, parts, st = fb.run()
+    return {"value": round(ms, 1), "unit": "ms/frame", "cores": fb.threads, "kind": "port",
+            "sample": _cpu_sample_text(fb, parts, st), "setup_s": round(t_setup, 1)}
 
 
 def run_reference(a):
@@ -483,26 +470,29 @@ def run_reference(a):
     if rank != 0:
         return
     synth = importlib.import_module(PKG + ".synth")
+    import numpy as np
     sc = synth.make_scene(a.scene)
+    fb, t_setup = _cpu_frame(sc)
     vals = []
-    # the full-size Gauss-Newton iteration (exact sparse solve, deterministic
-    # work of ~30 s) is timed once; every step re-times the skinning sample
-    t_gn = None
+    t0 = time.perf_counter()
     for i in range(a.warmup + a.steps):
-        ms, _, tg, _ = _oracle_frame_sample(sc, t_gn_known=t_gn)
-        t_gn = tg
+        if i == a.warmup:
+            t0 = time.perf_counter()
+        ms, parts, st = fb.run()
         if i >= a.warmup:
             vals.append(ms)
-    import numpy as np
+    wall = time.perf_counter() - t0
     v = float(np.mean(vals))
     line = {"metric": METRIC, "value": round(v, 1), "unit": "ms/frame", "n_gpus": ws, "steps": a.steps,
             "warmup": a.warmup, "ms_per_step": round(v, 1), "higher_is_better": False, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
-            "config": {"workload": "%s (oracle port on host cores)" % sc.name},
-            "cpu_baseline": {"value": round(v, 1), "unit": "ms/frame", "cores": 1, "kind": "port",
-                             "sample": "1 Gauss-Newton iteration of the full solve (exact sparse solve, timed "
-                                       "once per run: %.1f s) x %d iterations + skinning of 50k Gaussians "
-                                       "re-timed every step, extrapolated to the frame" % (t_gn, sc.iters)},
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded two-bars-and-sphere field)",
+            "impl": "reference",
+            "config": {"workload": "%s: %d Gaussians, %d^3 grid, %d nodes, k=%d, %d GN iterations, twist 90 deg "
+                                   "(reference CPU path restated in C++/OpenMP, host cores)"
+                                   % (sc.name, sc.n_gauss, sc.grid_num, sc.n_nodes, sc.k, sc.iters),
+                       "samples": fb.n_samples, "setup_s": round(t_setup, 1), "wall_s_timed_region": round(wall, 1)},
+            "cpu_baseline": {"value": round(v, 1), "unit": "ms/frame", "cores": fb.threads, "kind": "port",
+                             "sample": _cpu_sample_text(fb, parts, st)},
             "e2e": {"value": round(v, 1), "unit": "ms/frame", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
 

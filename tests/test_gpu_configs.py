@@ -1,0 +1,110 @@
+"""Parity at the benchmark's own configurations: a whole deformation frame
+on the GPU against the float64 oracle.
+
+* bend50k (50k Gaussians, 32^3 grid, ~1k nodes, k=8, 10 iterations) and
+  twist300k (300k Gaussians, 64^3 grid, 4061 nodes, k=8, 20 iterations, the
+  benchmarked frame), each in the chosen form (mixed precision, two-level
+  PCG with 64-node aggregates) and the plain form.
+* Node transforms against the numpy oracle's Gauss-Newton solve of the same
+  scene (tests/golden/solve_<scene>.npz, made by
+  tests/golden/make_solve_golden.py; exact sparse solve, Deform.cpp:95-169).
+  Tolerance: max |dx| / max |x| <= 1e-5 (chosen), 5e-5 (plain).  The
+  line search's halvings (Deform.cpp:144-156) must agree in total.
+* The frame's outputs (sample positions and features, Gaussian mean,
+  quaternion, scale, covariance and SH, node update) against the C++
+  restatement of the reference's CPU frame (oracle/cpu_frame.cpp, itself
+  checked bit for bit against the numpy oracle in tests/test_cpu_frame.py)
+  run on the oracle's node transforms, from the same rest state and kNN
+  weights.  Tolerances:
+    mu, sample and node positions   max |d| / scene extent <= 1e-5
+    covariance                      max |dSigma| / max |Sigma| <= 1e-5
+    quaternion                      1 - |<q, q_ref>| <= 1e-5
+    SH and sample features          max abs <= 2e-4 (coefficients ~N(0, 0.2))
+"""
+import os
+
+import numpy as np
+import pytest
+
+from tests import _helpers as H
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def _np(t):
+    return t.detach().cpu().numpy()
+
+
+def _rel(a, b):
+    return float(np.abs(np.asarray(a, np.float64) - b).max() / np.abs(b).max())
+
+
+@pytest.fixture(scope="module", params=["bend50k", "twist300k"])
+def case(request):
+    from oracle import cpu_frame as cf
+    sc = H.synth.make_scene(request.param)
+    _, samples = cf.occupied_cell_samples(sc.pos, sc.rot, sc.scale, sc.opacity, sc.grid_num)
+    rng = np.random.default_rng(5)
+    feature = (0.2 * rng.standard_normal((samples.shape[0], 48))).astype(np.float32)
+    g = np.load(os.path.join(GOLDEN, "solve_%s.npz" % sc.name))
+    return sc, samples, feature, g
+
+
+def _oracle_frame(d, sc, samples, feature, X):
+    """The C++ float64 restatement of the frame on the deformer's rest state,
+    kNN weights and the given node transforms X [n,12]."""
+    from oracle import cpu_frame as cf
+    N, k = d.N, d.k
+    ends = _np(d.ends).reshape(6, 3, N).transpose(2, 0, 1)
+    eidx = _np(d.ends_idx).reshape(k, 6, N).transpose(2, 1, 0)
+    ew = _np(d.ends_w).reshape(k, 6, N).transpose(2, 1, 0)
+    fr = cf.Frame(ends, eidx, ew, sc.node_pos, sc.rot, sc.scale, sc.shs, sample_pos=samples,
+                  sample_idx=_np(d.sample_idx).T, sample_w=_np(d.sample_w).T, feature=feature)
+    rot, tr = X[:, :9].astype(np.float64), X[:, 9:].astype(np.float64)
+    fr.skin_samples(rot, tr)
+    fr.skin_gaussians(rot, tr)
+    nodes = cf.ed_blend(sc.node_pos, _np(d.anchor_idx).T, _np(d.anchor_w).T, rot, tr, sc.node_pos)
+    return fr, nodes
+
+
+@pytest.mark.parametrize("form", ["chosen", "plain"])
+def test_frame_matches_the_oracle(dev, case, form):
+    sc, samples, feature, g = case
+    precision, coarse = (1, 64) if form == "chosen" else (0, 0)
+    cfg = dev.default_config(max_iters=sc.iters, early_exit=0, precision=precision, coarse_nodes=coarse)
+    d = dev.GaussianDeformer(torch.as_tensor(sc.pos), torch.as_tensor(sc.rot), torch.as_tensor(sc.scale),
+                             torch.as_tensor(sc.shs), sc.node_vertex, sc.k, sc.blocks, sc.block_type,
+                             sample_pos=torch.as_tensor(samples), feature=torch.as_tensor(feature), config=cfg)
+    d.apply_op(sc.op)
+    fr, nodes_ref = _oracle_frame(d, sc, samples, feature, g["x"])
+    st = d.frame(stats=True, with_cov=True)
+    torch.cuda.synchronize()
+    assert st["status"] == 0 and dev.device_status() == 0
+    assert st["gn_iterations"] == int(g["iters"])
+    X = np.concatenate([_np(d.rot_nodes), _np(d.trans_nodes)], 1)
+    err_x = _rel(X, g["x"].astype(np.float64))
+    ext = float(np.ptp(sc.pos, axis=0).max())
+    err = {
+        "x": err_x,
+        "mu": float(np.abs(_np(d.pos) - fr.pos).max() / ext),
+        "sigma": _rel(_np(d.cov), fr.cov6.astype(np.float64)),
+        "q": float(np.abs(1 - np.abs((_np(d.rot).astype(np.float64) * fr.q).sum(1))).max()),
+        "scale": _rel(_np(d.scale), fr.scale.astype(np.float64)),
+        "shs": float(np.abs(_np(d.shs) - fr.shs).max()),
+        "sample_pos": float(np.abs(_np(d.sample_pos) - fr.sample_pos).max() / ext),
+        "feature": float(np.abs(_np(d.feature) - fr.feature).max()),
+        "nodes": float(np.abs(_np(d.node_pos) - nodes_ref).max() / ext),
+    }
+    print("%s %s: pcg %d, halvings %d (oracle %d), errors %s" % (
+        sc.name, form, st["pcg_iterations"], st["halvings"], int(g["halvings"].sum()),
+        {k: "%.2e" % v for k, v in err.items()}))
+    assert st["halvings"] == int(g["halvings"].sum())
+    assert abs(st["initial_energy"] - g["energies"][0]) <= 1e-5 * g["energies"][0]
+    assert err_x <= (1e-5 if form == "chosen" else 5e-5)
+    tol = 1e-5 if form == "chosen" else 5e-5
+    assert err["mu"] <= tol and err["sample_pos"] <= tol and err["nodes"] <= tol
+    assert err["sigma"] <= tol and err["q"] <= tol and err["scale"] <= tol
+    assert err["shs"] <= 2e-4 and err["feature"] <= 2e-4

@@ -1,16 +1,10 @@
-"""Headless rasteriser (arap_render) against the oracle (oracle/raster.py).
-
-The kernel has not yet run on a GPU, so the test is opt-in: set
-ARAP_RENDER_GPU=1 to run it."""
+"""Headless rasteriser (arap_render) against the oracle (oracle/raster.py)."""
 import importlib
-import os
 
 import numpy as np
 import pytest
 
-pytestmark = [pytest.mark.gpu,
-              pytest.mark.skipif(os.environ.get("ARAP_RENDER_GPU") != "1",
-                                 reason="arap_render not yet run on a GPU: set ARAP_RENDER_GPU=1")]
+pytestmark = pytest.mark.gpu
 
 
 def _camera(tan_half=0.5, near=0.01, far=100.0):

@@ -1,18 +1,12 @@
 """A deform.txt replay driven through the GPU frame pipeline (replay.Replay on
 deform.GaussianDeformer) against the same frames run by the oracle: aims
-moved, exact Gauss-Newton solve, node update (GaussianView.cpp:1757-1916).
-
-The driver's GPU run has not yet been exercised, so the test is opt-in: set
-ARAP_REPLAY_GPU=1 to run it."""
+moved, exact Gauss-Newton solve, node update (GaussianView.cpp:1757-1916)."""
 import importlib
-import os
 
 import numpy as np
 import pytest
 
-pytestmark = [pytest.mark.gpu,
-              pytest.mark.skipif(os.environ.get("ARAP_REPLAY_GPU") != "1",
-                                 reason="replay on the GPU not yet exercised: set ARAP_REPLAY_GPU=1")]
+pytestmark = pytest.mark.gpu
 
 PKG = "arap-deformation-of-gaussian-radiance-fields_gb300"
 

@@ -1,17 +1,11 @@
 """Stage-II alignment kernels (arap_stage2_loss_grad, arap_stage2_adam)
-against the oracle's definition (oracle/stage2.py).
-
-These kernels have not yet run on a GPU, so the tests are opt-in: set
-ARAP_STAGE2_GPU=1 to run them."""
+against the oracle's definition (oracle/stage2.py)."""
 import importlib
-import os
 
 import numpy as np
 import pytest
 
-pytestmark = [pytest.mark.gpu,
-              pytest.mark.skipif(os.environ.get("ARAP_STAGE2_GPU") != "1",
-                                 reason="Stage-II kernels not yet run on a GPU: set ARAP_STAGE2_GPU=1")]
+pytestmark = pytest.mark.gpu
 
 PKG = "arap-deformation-of-gaussian-radiance-fields_gb300"
 
@@ -36,6 +30,17 @@ def _oracle_case(grid, p, t):
     P = s2.GaussianParams(*(p[k].astype(np.float64) for k in ("pos", "rot", "log_scale", "logit_opacity", "shs")))
     T = s2.GaussianParams(*(t[k].astype(np.float64) for k in ("pos", "rot", "log_scale", "logit_opacity", "shs")))
     aim_s, aim_f = s2.forward(T, samples, grid.lpf_param, ps, pg)
+    # The L1 loss's gradient carries sign(value - aim).  Where the float64
+    # value at P and its aim are closer than float32 evaluation can resolve,
+    # the two sides may take different signs, so every aim is moved at least
+    # `margin` away from the value at P (keeping its side).
+    sig_p, feat_p = s2.forward(P, samples, grid.lpf_param, ps, pg)
+    margin = 1e-3
+
+    def away(aim, val):
+        d = aim - val
+        return val + np.where(d >= 0, 1.0, -1.0) * np.maximum(np.abs(d), margin)
+    aim_s, aim_f = away(aim_s, sig_p), away(aim_f, feat_p)
     return s2, P, samples, ps, pg, aim_s.astype(np.float32), aim_f.astype(np.float32)
 
 
