@@ -29,7 +29,8 @@ class SolveConfig(C.Structure):
     _fields_ = [("w_rot", C.c_float), ("w_reg", C.c_float), ("w_con", C.c_float),
                 ("weighting_factor", C.c_float), ("cons_on_center", C.c_int),
                 ("max_iters", C.c_int), ("early_exit", C.c_int), ("precision", C.c_int),
-                ("pcg_tol", C.c_float), ("pcg_max_iters", C.c_int), ("coarse_nodes", C.c_int)]
+                ("pcg_tol", C.c_float), ("pcg_max_iters", C.c_int), ("coarse_nodes", C.c_int),
+                ("spin_limit", C.c_int)]
 
 
 class GridInfo(C.Structure):
@@ -59,11 +60,12 @@ D = C.c_double
 # name -> (restype, argtypes); every name here is declared in include/arap_gb300.h
 SIGNATURES = {
     "arap_build_graph": (I, [P, I, I, P, P]),
-    "arap_compute_weights": (I, [P, I, P, I, I, P, P, P]),
+    "arap_compute_weights": (I, [P, I, P, I, I, P, P, P, P]),
     "arap_solve_config_default": (None, [C.POINTER(SolveConfig)]),
     "arap_solver_create": (I, [C.POINTER(P), I, I, P, P, P, P, P, P, I, C.POINTER(SolveConfig), P]),
     "arap_solver_solve": (I, [P, P, P, P, P, C.POINTER(SolveStats), P]),
     "arap_solver_energy_grad": (I, [P, P, P, P, P, C.POINTER(D), P]),
+    "arap_solver_status": (I, [P, P]),
     "arap_solver_free_count": (I, [P]),
     "arap_solver_free_ids": (I, [P, P]),
     "arap_solver_destroy": (None, [P]),
@@ -74,13 +76,14 @@ SIGNATURES = {
     "arap_solver_batch_destroy": (None, [P]),
     "arap_node_table": (I, [I, P, P, P, P, P]),
     "arap_end_points": (I, [I, P, P, P, P, P, P]),
-    "arap_skin_gaussians": (I, [I, I, P, P, P, P, P, P, P, P, P, P, P, I, P]),
+    "arap_skin_gaussians": (I, [I, I, P, P, P, P, P, P, P, P, P, P, P, I, P, P]),
     "arap_skin_plan_create": (I, [P, I, I, P, P, P]),
     "arap_skin_plan_info": (I, [P, P, P, P]),
+    "arap_skin_plan_status": (I, [P, P]),
     "arap_skin_plan_destroy": (None, [P]),
     "arap_skin_gaussians_planned": (I, [P, P, P, P, P, P, P, P, P, P, P, P, I, P]),
-    "arap_skin_gaussians_backward": (I, [I, I, P, P, P, P, P, P, P, P, P, P]),
-    "arap_node_quaternions": (I, [I, P, P, I, P]),
+    "arap_skin_gaussians_backward": (I, [I, I, P, P, P, P, P, P, P, P, P, P, P]),
+    "arap_node_quaternions": (I, [I, P, P, I, P, P]),
     "arap_skin_samples": (I, [I, I, P, P, P, P, P, P, P, P]),
     "arap_update_nodes": (I, [I, I, P, P, P, P, P, P]),
     "arap_static_mask": (I, [I, I, I, P, P, P, P]),
@@ -89,6 +92,7 @@ SIGNATURES = {
     "arap_aims_scale": (I, [P, P, P, I, F, P]),
     "arap_grid_build": (I, [C.POINTER(P), I, P, P, P, P, I, I, C.POINTER(GridInfo), P]),
     "arap_grid_arrays": (I, [P, C.POINTER(P), C.POINTER(P), C.POINTER(P)]),
+    "arap_grid_status": (I, [P, P]),
     "arap_grid_center_order": (I, [P, I, P, P, P]),
     "arap_grid_center_order_noalloc": (I, [P, I, P, P, P]),
     "arap_ply_info": (I, [C.c_char_p, C.POINTER(C.c_int64), C.POINTER(I), C.POINTER(I)]),
@@ -102,7 +106,7 @@ SIGNATURES = {
     "arap_stage2_cell_flags": (I, [P, P, P, P, P]),
     "arap_grid_destroy": (None, [P]),
     "arap_render": (I, [I, P, P, P, P, P, F, I, P, P, P, F, F, I, I, P, P, P, P, P]),
-    "arap_get_device_status": (I, [P]),
+    "arap_status_read": (I, [P, P]),
     "arap_version": (C.c_char_p, []),
 }
 

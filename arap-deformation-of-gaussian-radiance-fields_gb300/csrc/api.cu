@@ -1,22 +1,23 @@
-// Library-wide entry points: device status word, version, solve defaults.
+// Library-wide entry points: status words, version, solve defaults.
 #include "arap_common.cuh"
 
 namespace arap {
-__device__ int g_status = 0;
+
+int status_read_clear(int* status_dev, cudaStream_t s) {
+  int v = 0;
+  if (cudaMemcpyAsync(&v, status_dev, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+      cudaMemsetAsync(status_dev, 0, sizeof(int), s) != cudaSuccess || cudaStreamSynchronize(s) != cudaSuccess) {
+    (void)cudaGetLastError();
+    return ARAP_ECUDA;
+  }
+  return v;
 }
 
-extern "C" int arap_get_device_status(arap_stream_t stream) {
-  int v = 0;
-  const int zero = 0;
-  cudaStream_t s = (cudaStream_t)stream;
-  if (cudaMemcpyFromSymbolAsync(&v, arap::g_status, sizeof(int), 0, cudaMemcpyDeviceToHost, s) !=
-      cudaSuccess)
-    return ARAP_ECUDA;
-  if (cudaMemcpyToSymbolAsync(arap::g_status, &zero, sizeof(int), 0, cudaMemcpyHostToDevice, s) !=
-      cudaSuccess)
-    return ARAP_ECUDA;
-  if (cudaStreamSynchronize(s) != cudaSuccess) return ARAP_ECUDA;
-  return v;
+}  // namespace arap
+
+extern "C" int arap_status_read(int32_t* status_dev, arap_stream_t stream) {
+  if (!status_dev) return ARAP_EBADINPUT;
+  return arap::status_read_clear(status_dev, (cudaStream_t)stream);
 }
 
 extern "C" const char* arap_version(void) { return "arap_gb300 0.1 (sm_103a)"; }
@@ -34,4 +35,5 @@ extern "C" void arap_solve_config_default(arap_solve_config* cfg) {
   cfg->pcg_tol = 0.0f;
   cfg->pcg_max_iters = 0;
   cfg->coarse_nodes = 0;
+  cfg->spin_limit = 0;
 }

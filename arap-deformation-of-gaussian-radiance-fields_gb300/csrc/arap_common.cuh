@@ -26,15 +26,21 @@
 
 namespace arap {
 
-// Sticky device-side error word (ARAP_* code, first error wins).  Defined in
-// api.cu; read and cleared by arap_get_device_status.
-extern __device__ int g_status;
+// Device-side error word of one handle (solver, grid, skinning plan) or the
+// caller's own word passed to a stateless call: the first ARAP_* code raised
+// wins until the host reads and clears it (status_read_clear).  A null word
+// records nothing (the outputs still carry the NaNs).
+__device__ __forceinline__ void raise_status(int* st, int code) {
+  if (st) atomicCAS(st, 0, code);
+}
 
-__device__ __forceinline__ void raise_status(int code) { atomicCAS(&g_status, 0, code); }
+// Host: copy a device status word to the host, clear it, synchronise the
+// stream; returns the word, or ARAP_ECUDA when a copy fails (api.cu).
+int status_read_clear(int* status_dev, cudaStream_t stream);
 
 // ------------------------------------------------------------ barrier ----
 // Grid-wide barrier for cooperative launches (all CTAs co-resident).  Every
-// wait is bounded: after kSpinLimit polls a waiting CTA records ARAP_ETIMEOUT,
+// wait is bounded: after spin_limit polls a waiting CTA records ARAP_ETIMEOUT,
 // marks the barrier failed and returns false; callers then leave the kernel.
 //
 // Counter barrier with a reduction.  Arrivals go to one monotonic counter
@@ -54,7 +60,7 @@ struct GridBarrier {
   int pad1;
 };
 
-constexpr long long kSpinLimit = 1ll << 23;
+constexpr long long kSpinLimit = 1ll << 23;  // default polls of a barrier wait
 constexpr int kReduceSlots = 4;
 constexpr int kMaxGridCtas = 160;  // CTAs a barrier reduction supports (5 per lane)
 
@@ -134,6 +140,8 @@ struct GridSync {
   unsigned int epoch;
   unsigned int nb;
   unsigned int bid;
+  int* status;           // the handle's device status word
+  long long spin_limit;  // polls of one wait before ARAP_ETIMEOUT
 
   // One thread per CTA: arrive at barrier e (release) and wait (acquire) for
   // every CTA; bounded, false on failure.
@@ -144,9 +152,9 @@ struct GridSync {
     while ((int)(ld_acquire_u32(&bar->count) - target) < 0) {
       ++it;
       if ((it & 63) == 0 && ld_relaxed_i32(&bar->failed)) return false;
-      if (it > kSpinLimit) {
+      if (it > spin_limit) {
         atomicExch(&bar->failed, 1);
-        raise_status(ARAP_ETIMEOUT);
+        raise_status(status, ARAP_ETIMEOUT);
         return false;
       }
       if (it > 1024) __nanosleep(32);
@@ -287,12 +295,6 @@ struct GridSync {
     return s_sync_ok != 0;
   }
 };
-
-// Marks the barrier failed so that peers waiting in it leave promptly.
-__device__ __forceinline__ void grid_fail(GridBarrier* bar, int code) {
-  raise_status(code);
-  atomicExch(&bar->failed, 1);
-}
 
 // Block-wide FP64 sum (blockDim.x multiple of 32, <= 1024); all threads get it.
 template <int NV>

@@ -255,7 +255,7 @@ constexpr int kSortMax = 16384;
 
 // Bitonic sort of each occupied cell's list in shared memory (one CTA per cell).
 __global__ void sort_cells_kernel(int nvalid, const int* __restrict__ valid, const int* __restrict__ off,
-                                  int* __restrict__ lists) {
+                                  int* __restrict__ lists, int* __restrict__ status) {
   extern __shared__ int s_keys[];
   const int v = blockIdx.x;
   if (v >= nvalid) return;
@@ -263,7 +263,7 @@ __global__ void sort_cells_kernel(int nvalid, const int* __restrict__ valid, con
   const int b = off[c], L = off[c + 1] - b;
   if (L <= 1) return;
   if (L > kSortMax) {
-    if (threadIdx.x == 0) raise_status(ARAP_EUNSUPPORTED);
+    if (threadIdx.x == 0) raise_status(status, ARAP_EUNSUPPORTED);
     return;
   }
   int P2 = 1;
@@ -834,6 +834,7 @@ struct arap_grid {
   int N = 0, g = 0, padding = 1, nvalid = 0;
   long long npairs = 0;
   GridParams* params = nullptr;  // device
+  int* status = nullptr;         // device status word of the grid's kernels
   int* off = nullptr;            // [g^3 + 1]
   int* lists = nullptr;          // [npairs]
   int* valid = nullptr;          // [nvalid]
@@ -857,6 +858,7 @@ static int scan_exclusive(const int* in, int* out, int n, long long* sums, cudaS
 extern "C" void arap_grid_destroy(arap_grid* G) {
   if (!G) return;
   cudaFree(G->params);
+  cudaFree(G->status);
   cudaFree(G->off);
   cudaFree(G->lists);
   cudaFree(G->valid);
@@ -898,7 +900,8 @@ extern "C" int arap_grid_build(arap_grid** out, int N, const float* pos, const f
     arap_grid_destroy(G);
     return code;
   };
-  if (cudaMalloc(&G->params, sizeof(GridParams)) || cudaMalloc(&G->off, sizeof(int) * ((size_t)C + 1)) ||
+  if (cudaMalloc(&G->params, sizeof(GridParams)) || cudaMalloc(&G->status, sizeof(int)) ||
+      cudaMalloc(&G->off, sizeof(int) * ((size_t)C + 1)) ||
       cudaMalloc(&G->ranges, sizeof(int) * 6 * (size_t)N) || cudaMalloc(&count, sizeof(int) * (size_t)C) ||
       cudaMalloc(&cursor, sizeof(int) * (size_t)C) || cudaMalloc(&flagpos, sizeof(int) * ((size_t)C + 1)) ||
       cudaMalloc(&sums, sizeof(long long) * (nbs + 1)) || cudaMalloc(&mm, sizeof(unsigned int) * 6)) {
@@ -907,6 +910,7 @@ extern "C" int arap_grid_build(arap_grid** out, int N, const float* pos, const f
   }
   const unsigned int init[6] = {0xffffffffu, 0xffffffffu, 0xffffffffu, 0u, 0u, 0u};
   if (cudaMemcpyAsync(mm, init, sizeof(init), cudaMemcpyHostToDevice, st) ||
+      cudaMemsetAsync(G->status, 0, sizeof(int), st) ||
       cudaMemsetAsync(count, 0, sizeof(int) * (size_t)C, st) || cudaMemsetAsync(cursor, 0, sizeof(int) * (size_t)C, st))
     return fail(ARAP_ECUDA);
   minmax_kernel<<<std::min(grid_for(N, 256), 1184), 256, 0, st>>>(N, pos, mm);
@@ -944,7 +948,7 @@ extern "C" int arap_grid_build(arap_grid** out, int N, const float* pos, const f
     if (cudaFuncSetAttribute(sort_cells_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              kSortMax * (int)sizeof(int)))
       return fail(ARAP_ECUDA);
-    sort_cells_kernel<<<nvalid, 256, kSortMax * sizeof(int), st>>>(nvalid, G->valid, G->off, G->lists);
+    sort_cells_kernel<<<nvalid, 256, kSortMax * sizeof(int), st>>>(nvalid, G->valid, G->off, G->lists, G->status);
   }
   if (cudaPeekAtLastError() != cudaSuccess) {
     (void)cudaGetLastError();
@@ -967,8 +971,13 @@ extern "C" int arap_grid_build(arap_grid** out, int N, const float* pos, const f
     info_host->n_valid = nvalid;
     info_host->n_pairs = total;
   }
+  const int gs = status_read_clear(G->status, st);
+  if (gs != ARAP_OK) {
+    arap_grid_destroy(G);
+    return gs;
+  }
   *out = G;
-  return arap_get_device_status(stream);
+  return ARAP_OK;
 }
 
 extern "C" int arap_grid_center_order(const arap_grid* G, int N, const float* pos, int32_t* order_out,
@@ -1010,14 +1019,19 @@ extern "C" int arap_grid_center_order(const arap_grid* G, int N, const float* po
     compact_kernel<<<grid_for(C, 256), 256, 0, st>>>(C, count, flagpos, valid);
     if (cudaFuncSetAttribute(sort_cells_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSortMax * (int)sizeof(int)))
       return done(ARAP_ECUDA);
-    sort_cells_kernel<<<nvalid, 256, kSortMax * sizeof(int), st>>>(nvalid, valid, off, order_out);
+    sort_cells_kernel<<<nvalid, 256, kSortMax * sizeof(int), st>>>(nvalid, valid, off, order_out, G->status);
   }
   if (cudaPeekAtLastError() != cudaSuccess || cudaStreamSynchronize(st) != cudaSuccess) {
     (void)cudaGetLastError();
     return done(ARAP_ECUDA);
   }
   done(ARAP_OK);
-  return arap_get_device_status(stream);
+  return status_read_clear(G->status, st);
+}
+
+extern "C" int arap_grid_status(arap_grid* G, arap_stream_t stream) {
+  if (!G) return ARAP_EBADINPUT;
+  return status_read_clear(G->status, (cudaStream_t)stream);
 }
 
 extern "C" int arap_grid_arrays(const arap_grid* G, const int32_t** cell_offsets, const int32_t** cell_lists,
@@ -1233,11 +1247,11 @@ extern "C" int arap_grid_center_order_noalloc(const arap_grid* G, int N, const f
     compact_kernel<<<grid_for(C, 256), 256, 0, st>>>(C, count, flagpos, valid);
     if (cudaFuncSetAttribute(sort_cells_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSortMax * (int)sizeof(int)))
       return ARAP_ECUDA;
-    sort_cells_kernel<<<nvalid, 256, kSortMax * sizeof(int), st>>>(nvalid, valid, off, order_out);
+    sort_cells_kernel<<<nvalid, 256, kSortMax * sizeof(int), st>>>(nvalid, valid, off, order_out, G->status);
   }
   if (cudaPeekAtLastError() != cudaSuccess || cudaStreamSynchronize(st) != cudaSuccess) {
     (void)cudaGetLastError();
     return ARAP_ECUDA;
   }
-  return arap_get_device_status(stream);
+  return status_read_clear(G->status, st);
 }

@@ -19,7 +19,8 @@ __global__ void __launch_bounds__(kKnnThreads) knn_kernel(const float* __restric
                                                           const float* __restrict__ nodes, int n,
                                                           int skip_first, int kout,
                                                           int32_t* __restrict__ idx_out,
-                                                          float* __restrict__ w_out, int planes) {
+                                                          float* __restrict__ w_out, int planes,
+                                                          int* __restrict__ status) {
   __shared__ float4 s_nodes[kKnnTile];
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const bool active = i < P;
@@ -94,7 +95,7 @@ __global__ void __launch_bounds__(kKnnThreads) knn_kernel(const float* __restric
     sum += w[j];
   }
   const bool bad = !(dmax > 0.0) || !(sum > 0.0);
-  if (bad) raise_status(ARAP_ENONFINITE);
+  if (bad) raise_status(status, ARAP_ENONFINITE);
 #pragma unroll
   for (int j = 0; j < KP1 - 1; ++j) {
     const double wj = (KP1 - 1 == 1) ? 1.0 : w[j] / sum;
@@ -106,19 +107,19 @@ __global__ void __launch_bounds__(kKnnThreads) knn_kernel(const float* __restric
 
 template <int KP1>
 static int launch_knn(const float* pts, int P, const float* nodes, int n, int skip, int kout,
-                      int32_t* idx, float* w, int planes, cudaStream_t st) {
+                      int32_t* idx, float* w, int planes, int* status, cudaStream_t st) {
   const int grid = grid_for(P, kKnnThreads);
-  knn_kernel<KP1><<<grid, kKnnThreads, 0, st>>>(pts, P, nodes, n, skip, kout, idx, w, planes);
+  knn_kernel<KP1><<<grid, kKnnThreads, 0, st>>>(pts, P, nodes, n, skip, kout, idx, w, planes, status);
   ARAP_LAUNCH_CHECK();
   return ARAP_OK;
 }
 
 static int dispatch_knn(int kp1, const float* pts, int P, const float* nodes, int n, int skip,
-                        int kout, int32_t* idx, float* w, int planes, cudaStream_t st) {
+                        int kout, int32_t* idx, float* w, int planes, int* status, cudaStream_t st) {
   switch (kp1) {
 #define ARAP_KNN_CASE(K) \
   case K:                \
-    return launch_knn<K>(pts, P, nodes, n, skip, kout, idx, w, planes, st);
+    return launch_knn<K>(pts, P, nodes, n, skip, kout, idx, w, planes, status, st);
     ARAP_KNN_CASE(2)
     ARAP_KNN_CASE(3)
     ARAP_KNN_CASE(4)
@@ -145,16 +146,17 @@ extern "C" int arap_build_graph(const float* nodes_xyz, int n, int k, int32_t* n
                                 arap_stream_t stream) {
   if (!nodes_xyz || !neighbors_out || k < 1 || n < k + 1) return ARAP_EBADINPUT;
   if (k > ARAP_KNN_MAX) return ARAP_EUNSUPPORTED;
-  return dispatch_knn(k + 1, nodes_xyz, n, nodes_xyz, n, 1, k, neighbors_out, nullptr, 0,
+  return dispatch_knn(k + 1, nodes_xyz, n, nodes_xyz, n, 1, k, neighbors_out, nullptr, 0, nullptr,
                       (cudaStream_t)stream);
 }
 
 extern "C" int arap_compute_weights(const float* points_xyz, int P, const float* nodes_xyz, int n,
-                                    int k, int32_t* idx_out, float* w_out, arap_stream_t stream) {
+                                    int k, int32_t* idx_out, float* w_out, int32_t* status,
+                                    arap_stream_t stream) {
   if (P == 0) return ARAP_OK;
   if (!points_xyz || !nodes_xyz || !idx_out || !w_out || P < 0 || k < 1 || n < k + 1)
     return ARAP_EBADINPUT;
   if (k > ARAP_KNN_MAX) return ARAP_EUNSUPPORTED;
-  return dispatch_knn(k + 1, points_xyz, P, nodes_xyz, n, 0, k, idx_out, w_out, 1,
+  return dispatch_knn(k + 1, points_xyz, P, nodes_xyz, n, 0, k, idx_out, w_out, 1, status,
                       (cudaStream_t)stream);
 }

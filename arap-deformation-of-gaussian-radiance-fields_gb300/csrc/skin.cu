@@ -135,7 +135,7 @@ __global__ void __launch_bounds__(kSkinThreads, 4)
                           const float* __restrict__ scale0, const uint8_t* __restrict__ static_mask,
                           float* __restrict__ pos_out, float* __restrict__ rot_inout,
                           float* __restrict__ scale_out, float* __restrict__ shs,
-                          float* __restrict__ cov_out, SkinPlanDev plan) {
+                          float* __restrict__ cov_out, SkinPlanDev plan, int* __restrict__ status) {
   extern __shared__ float4 s_raw4[];
   float* s_raw = reinterpret_cast<float*>(s_raw4);
   float* s_sh = s_raw;                                        // [T][52]
@@ -300,7 +300,7 @@ __global__ void __launch_bounds__(kSkinThreads, 4)
       } else {
         ok = polar_factor<float>(M, R, 20, 2e-7f);
       }
-      if (!ok) raise_status(ARAP_ENONFINITE);
+      if (!ok) raise_status(status, ARAP_ENONFINITE);
       // K = diag(R^T M) = diag(V S V^T)
       float Kd[3];
 #pragma unroll
@@ -399,7 +399,7 @@ __global__ void __launch_bounds__(kSkinThreads)
                                    const float* __restrict__ ew, const float* __restrict__ table,
                                    const float* __restrict__ scale0, const uint8_t* __restrict__ static_mask,
                                    const float* __restrict__ grad_pos, const float* __restrict__ grad_cov,
-                                   float* __restrict__ grad_node) {
+                                   float* __restrict__ grad_node, int* __restrict__ status) {
   __shared__ int s_keys[kHashSlots];
   __shared__ float s_vals[kHashSlots][12];
   for (int q = threadIdx.x; q < kHashSlots; q += blockDim.x) {
@@ -434,7 +434,7 @@ __global__ void __launch_bounds__(kSkinThreads)
 #pragma unroll
       for (int r = 0; r < 3; ++r) M[r * 3 + a] = 0.5f * (e[3 * (2 * a) + r] - e[3 * (2 * a + 1) + r]);
     float R[9];
-    if (!polar_factor<float>(M, R, 20, 2e-7f)) raise_status(ARAP_ENONFINITE);
+    if (!polar_factor<float>(M, R, 20, 2e-7f)) raise_status(status, ARAP_ENONFINITE);
     float S[9];  // R^T M, symmetrised
 #pragma unroll
     for (int a = 0; a < 3; ++a)
@@ -545,7 +545,8 @@ __global__ void __launch_bounds__(kSkinThreads)
 
 // Per-node quaternion of the polar factor (GaussianView.cpp:3172-3181).
 template <bool MIXED>
-__global__ void node_quat_kernel(int n, const float* __restrict__ rot, float* __restrict__ quat) {
+__global__ void node_quat_kernel(int n, const float* __restrict__ rot, float* __restrict__ quat,
+                                 int* __restrict__ status) {
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= n) return;
   const float* r = rot + 9 * (size_t)j;
@@ -570,7 +571,7 @@ __global__ void node_quat_kernel(int n, const float* __restrict__ rot, float* __
   } else {
     ok = newton_polar_ref<float>(M, 100);
   }
-  if (!ok) raise_status(ARAP_ENONFINITE);
+  if (!ok) raise_status(status, ARAP_ENONFINITE);
   const float4 q = quat_normalize(quat_from_rowmajor(M));
   reinterpret_cast<float4*>(quat)[j] = q;
 }
@@ -765,7 +766,8 @@ __global__ void aims_kernel(int op, float* __restrict__ aims, const float* __res
 template <int K, bool PLANNED>
 static int launch_skin_g(bool mixed, int N, float* ends, const int32_t* eidx, const float* ew,
                          const float* table, const float* scale0, const uint8_t* st, float* pos,
-                         float* rot, float* scale, float* shs, float* cov, const SkinPlanDev& plan, cudaStream_t s) {
+                         float* rot, float* scale, float* shs, float* cov, const SkinPlanDev& plan, int* status,
+                         cudaStream_t s) {
   const int grid = grid_for(N, kSkinTile);
   constexpr size_t smem = PLANNED ? skin_plan_smem_bytes() : skin_smem_bytes();
   if (mixed) {
@@ -773,13 +775,15 @@ static int launch_skin_g(bool mixed, int N, float* ends, const int32_t* eidx, co
                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
       return ARAP_ECUDA;
     skin_gaussians_kernel<K, true, PLANNED><<<grid, kSkinThreads, smem, s>>>(N, ends, eidx, ew, table, scale0, st,
-                                                                              pos, rot, scale, shs, cov, plan);
+                                                                              pos, rot, scale, shs, cov, plan,
+                                                                              status);
   } else {
     if (PLANNED && cudaFuncSetAttribute(skin_gaussians_kernel<K, false, PLANNED>,
                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
       return ARAP_ECUDA;
     skin_gaussians_kernel<K, false, PLANNED><<<grid, kSkinThreads, smem, s>>>(N, ends, eidx, ew, table, scale0, st,
-                                                                               pos, rot, scale, shs, cov, plan);
+                                                                               pos, rot, scale, shs, cov, plan,
+                                                                               status);
   }
   return ARAP_OK;
 }
@@ -887,7 +891,7 @@ extern "C" int arap_skin_gaussians(int N, int k, float* ends, const int32_t* end
                                    const float* ends_w, const float* node_table, const float* scale0,
                                    const uint8_t* static_mask, float* pos_out, float* rot_inout,
                                    float* scale_out, float* shs_inout, float* cov_out, int precision,
-                                   arap_stream_t stream) {
+                                   int32_t* status, arap_stream_t stream) {
   if (N == 0) return ARAP_OK;
   if (N < 0 || !ends || !ends_idx || !ends_w || !node_table || !scale0 || !pos_out || !rot_inout ||
       !scale_out)
@@ -902,7 +906,7 @@ extern "C" int arap_skin_gaussians(int N, int k, float* ends, const int32_t* end
 #define ARAP_SKG(K)                                                                                   \
   case K:                                                                                             \
     rc = launch_skin_g<K, false>(mixed, N, ends, ends_idx, ends_w, node_table, scale0, static_mask, pos_out, \
-                                 rot_inout, scale_out, shs_inout, cov_out, SkinPlanDev{}, s);            \
+                                 rot_inout, scale_out, shs_inout, cov_out, SkinPlanDev{}, status, s);    \
     break;
     ARAP_SKG(1) ARAP_SKG(2) ARAP_SKG(3) ARAP_SKG(4) ARAP_SKG(5) ARAP_SKG(6)
     ARAP_SKG(7) ARAP_SKG(8) ARAP_SKG(9) ARAP_SKG(10) ARAP_SKG(11) ARAP_SKG(12)
@@ -919,6 +923,7 @@ struct arap_skin_plan {
   int N = 0, k = 0, tiles = 0, kp = 0, overflow = 0, max_nodes = 0;
   void* block = nullptr;
   SkinPlanDev dev{};
+  int* status = nullptr;  // the plan's device status word (inside block)
 };
 
 extern "C" int arap_skin_plan_create(arap_skin_plan** out, int N, int k, const int32_t* ends_idx,
@@ -936,8 +941,8 @@ extern "C" int arap_skin_plan_create(arap_skin_plan** out, int N, int k, const i
   const size_t b_count = ((sizeof(int32_t) * p->tiles) + 255) & ~size_t(255);
   const size_t b_nodes = ((sizeof(int32_t) * (size_t)p->tiles * kPlanNodes) + 255) & ~size_t(255);
   const size_t b_lidx = (((size_t)N * 6 * p->kp) + 255) & ~size_t(255);
-  const size_t b_wts = sizeof(float) * (size_t)N * 6 * k;
-  if (cudaMalloc(&p->block, b_count + b_nodes + b_lidx + b_wts) != cudaSuccess) {
+  const size_t b_wts = (sizeof(float) * (size_t)N * 6 * k + 255) & ~size_t(255);
+  if (cudaMalloc(&p->block, b_count + b_nodes + b_lidx + b_wts + 256) != cudaSuccess) {
     (void)cudaGetLastError();
     delete p;
     return ARAP_ENOMEM;
@@ -948,7 +953,8 @@ extern "C" int arap_skin_plan_create(arap_skin_plan** out, int N, int k, const i
   uint8_t* lidx = reinterpret_cast<uint8_t*>(base + b_count + b_nodes);
   float* wts = reinterpret_cast<float*>(base + b_count + b_nodes + b_lidx);
   p->dev = SkinPlanDev{count, nodes, lidx, wts, p->kp};
-  if (cudaMemsetAsync(lidx, 0, b_lidx, st) != cudaSuccess) {
+  p->status = reinterpret_cast<int*>(base + b_count + b_nodes + b_lidx + b_wts);
+  if (cudaMemsetAsync(lidx, 0, b_lidx, st) != cudaSuccess || cudaMemsetAsync(p->status, 0, sizeof(int), st) != cudaSuccess) {
     arap_skin_plan_destroy(p);
     return ARAP_ECUDA;
   }
@@ -977,6 +983,11 @@ extern "C" int arap_skin_plan_info(const arap_skin_plan* p, int* tiles, int* ove
   return ARAP_OK;
 }
 
+extern "C" int arap_skin_plan_status(arap_skin_plan* p, arap_stream_t stream) {
+  if (!p) return ARAP_EBADINPUT;
+  return status_read_clear(p->status, (cudaStream_t)stream);
+}
+
 extern "C" void arap_skin_plan_destroy(arap_skin_plan* p) {
   if (!p) return;
   if (p->block) cudaFree(p->block);
@@ -1001,7 +1012,7 @@ extern "C" int arap_skin_gaussians_planned(const arap_skin_plan* plan, float* en
 #define ARAP_SKP(K)                                                                                       \
   case K:                                                                                                 \
     rc = launch_skin_g<K, true>(mixed, N, ends, ends_idx, ends_w, node_table, scale0, static_mask, pos_out, \
-                                rot_inout, scale_out, shs_inout, cov_out, plan->dev, s);                  \
+                                rot_inout, scale_out, shs_inout, cov_out, plan->dev, plan->status, s);    \
     break;
     ARAP_SKP(1) ARAP_SKP(2) ARAP_SKP(3) ARAP_SKP(4) ARAP_SKP(5) ARAP_SKP(6)
     ARAP_SKP(7) ARAP_SKP(8) ARAP_SKP(9) ARAP_SKP(10) ARAP_SKP(11) ARAP_SKP(12)
@@ -1017,7 +1028,8 @@ extern "C" int arap_skin_gaussians_planned(const arap_skin_plan* plan, float* en
 extern "C" int arap_skin_gaussians_backward(int N, int k, const float* ends_in, const int32_t* ends_idx,
                                             const float* ends_w, const float* node_table, const float* scale0,
                                             const uint8_t* static_mask, const float* grad_pos,
-                                            const float* grad_cov, float* grad_node, arap_stream_t stream) {
+                                            const float* grad_cov, float* grad_node, int32_t* status,
+                                            arap_stream_t stream) {
   if (N == 0) return ARAP_OK;
   if (N < 0 || !ends_in || !ends_idx || !ends_w || !node_table || !scale0 || !grad_pos || !grad_cov || !grad_node)
     return ARAP_EBADINPUT;
@@ -1029,7 +1041,7 @@ extern "C" int arap_skin_gaussians_backward(int N, int k, const float* ends_in, 
   case K:                                                                                                   \
     skin_gaussians_backward_kernel<K><<<grid, kSkinThreads, 0, s>>>(N, ends_in, ends_idx, ends_w, node_table, \
                                                                     scale0, static_mask, grad_pos, grad_cov, \
-                                                                    grad_node);                              \
+                                                                    grad_node, status);                      \
     break;
     ARAP_SKB(1) ARAP_SKB(2) ARAP_SKB(3) ARAP_SKB(4) ARAP_SKB(5) ARAP_SKB(6)
     ARAP_SKB(7) ARAP_SKB(8) ARAP_SKB(9) ARAP_SKB(10) ARAP_SKB(11) ARAP_SKB(12)
@@ -1041,14 +1053,14 @@ extern "C" int arap_skin_gaussians_backward(int N, int k, const float* ends_in, 
   return ARAP_OK;
 }
 
-extern "C" int arap_node_quaternions(int n, const float* rot, float* quat_out, int precision,
+extern "C" int arap_node_quaternions(int n, const float* rot, float* quat_out, int precision, int32_t* status,
                                      arap_stream_t stream) {
   if (n == 0) return ARAP_OK;
   if (n < 0 || !rot || !quat_out || (reinterpret_cast<uintptr_t>(quat_out) & 15)) return ARAP_EBADINPUT;
   if (precision == ARAP_PRECISION_MIXED)
-    node_quat_kernel<true><<<grid_for(n, 128), 128, 0, (cudaStream_t)stream>>>(n, rot, quat_out);
+    node_quat_kernel<true><<<grid_for(n, 128), 128, 0, (cudaStream_t)stream>>>(n, rot, quat_out, status);
   else
-    node_quat_kernel<false><<<grid_for(n, 128), 128, 0, (cudaStream_t)stream>>>(n, rot, quat_out);
+    node_quat_kernel<false><<<grid_for(n, 128), 128, 0, (cudaStream_t)stream>>>(n, rot, quat_out, status);
   ARAP_LAUNCH_CHECK();
   return ARAP_OK;
 }

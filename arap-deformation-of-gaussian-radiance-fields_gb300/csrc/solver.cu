@@ -465,6 +465,7 @@ extern "C" int arap_solver_create(arap_solver** out, int n, int k, const int32_t
     P.partials = cv.take<double>((size_t)2 * kReduceSlots * grid);
     P.stats = cv.take<double>(kStatSlots);
     P.bar = cv.take<GridBarrier>(1);
+    P.status = cv.take<int>(1);
   };
   Carver sizing{nullptr};
   SolveParams dummy{};
@@ -512,12 +513,14 @@ extern "C" int arap_solver_create(arap_solver** out, int n, int k, const int32_t
     e = e ? e : up(P.gca_off, gca_off.data(), gca_off.size() * 4);
     e = e ? e : up(P.gca, gca.data(), gca.size() * 4);
   }
+  e = e ? e : cudaMemsetAsync(P.status, 0, sizeof(int), st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   if (e != cudaSuccess) {
     cudaFree(s->block);
     delete s;
     return ARAP_ECUDA;
   }
+  P.spin_limit = cfg.spin_limit > 0 ? (long long)cfg.spin_limit : kSpinLimit;
   P.n = n;
   P.k = k;
   P.F = F;
@@ -607,7 +610,7 @@ extern "C" int arap_solver_solve(arap_solver* s, const float* node_pos, const fl
   if (!stats_host) return ARAP_OK;
   double st8[kStatSlots];
   ARAP_CUDA_TRY(cudaMemcpyAsync(st8, s->P.stats, sizeof(st8), cudaMemcpyDeviceToHost, st));
-  const int dev_status = arap_get_device_status(stream);  // synchronises
+  const int dev_status = status_read_clear(s->P.status, st);  // synchronises
   return fill_stats(s, st8, dev_status, stats_host);
 }
 
@@ -631,11 +634,16 @@ extern "C" int arap_solver_energy_grad(arap_solver* s, const float* node_pos, co
   if (energy_host) {
     double st8[kStatSlots];
     ARAP_CUDA_TRY(cudaMemcpyAsync(st8, used.stats, sizeof(st8), cudaMemcpyDeviceToHost, st));
-    const int dev_status = arap_get_device_status(stream);
+    const int dev_status = status_read_clear(used.status, st);
     *energy_host = st8[ST_E];
     return dev_status;
   }
   return ARAP_OK;
+}
+
+extern "C" int arap_solver_status(arap_solver* s, arap_stream_t stream) {
+  if (!s) return ARAP_EBADINPUT;
+  return status_read_clear(s->P.status, (cudaStream_t)stream);
 }
 
 extern "C" int arap_solver_free_count(const arap_solver* s) { return s ? s->F : -1; }
@@ -914,9 +922,9 @@ extern "C" int arap_solver_batch_solve(arap_solver_batch* b, const float* const*
   for (int i = 0; i < count; ++i)
     ARAP_CUDA_TRY(cudaMemcpyAsync(st8.data() + (size_t)kStatSlots * i, b->solvers[i]->P.stats,
                                   sizeof(double) * kStatSlots, cudaMemcpyDeviceToHost, st));
-  const int dev_status = arap_get_device_status(stream);  // synchronises
   int status = ARAP_OK;
   for (int i = 0; i < count; ++i) {
+    const int dev_status = status_read_clear(b->solvers[i]->P.status, st);  // synchronises
     const int si = fill_stats(b->solvers[i], st8.data() + (size_t)kStatSlots * i, dev_status, stats_host + i);
     if (status == ARAP_OK) status = si;
   }
@@ -968,7 +976,9 @@ extern "C" int arap_solver_batch_autotune(arap_solver_batch* b, const float* con
   if (rc == ARAP_OK) rc = upload_ctas(b);
   if (best_exponent) *best_exponent = best;
   if (rc != ARAP_OK) return rc;
-  return arap_get_device_status(stream);
+  for (arap_solver* si : b->solvers)
+    if (const int ds = status_read_clear(si->P.status, st)) return ds;
+  return ARAP_OK;
 }
 
 extern "C" int arap_solver_batch_ctas(const arap_solver_batch* b, int32_t* cta_first_host) {

@@ -207,7 +207,7 @@ __device__ __forceinline__ void solve_body(const SolveParams& P, int bid, int nb
   // node order position p belongs to CTA p % nbk: the costliest nodes (the
   // order is by cost, descending) are spread over all SMs
   const int wib = threadIdx.x >> 5;
-  GridSync gs{P.bar, P.partials, 0u, (unsigned int)nbk, (unsigned int)bid};
+  GridSync gs{P.bar, P.partials, 0u, (unsigned int)nbk, (unsigned int)bid, P.status, P.spin_limit};
   // phase timers, thread 0's only, kept in shared memory rather than registers
   // that would stay live through the whole kernel.  acc: prep, grad, coarse,
   // pcg, line search, inversion (ns).  work: PCG work of this CTA per phase
@@ -461,7 +461,7 @@ __device__ __forceinline__ void solve_body(const SolveParams& P, int bid, int nb
       if (threadIdx.x == 0) s_clk.inv0 = global_ns();
       if (!coarse_invert(P, gs, &coarse_ok, s_scratch)) return;
       if (threadIdx.x == 0) s_clk.acc[5] += (double)(global_ns() - s_clk.inv0);
-      if (!coarse_ok && gt == 0) raise_status(ARAP_ENONFINITE);
+      if (!coarse_ok && gt == 0) raise_status(P.status, ARAP_ENONFINITE);
       if (resident) {
         // this CTA's rows of the coarse inverse (rows bid, bid + nbk, ...)
         const int NC = P.NC, n4 = NC / 4;
@@ -796,7 +796,7 @@ __device__ __forceinline__ void solve_body(const SolveParams& P, int bid, int nb
       to[0] = to[1] = to[2] = 0.f;
     }
   }
-  if (nonfinite) raise_status(ARAP_ENONFINITE);
+  if (nonfinite) raise_status(P.status, ARAP_ENONFINITE);
   if (gt == 0) {
     P.stats[ST_ITERS] = iters;
     P.stats[ST_PCG] = pcg_total;

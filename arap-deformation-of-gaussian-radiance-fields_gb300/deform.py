@@ -26,7 +26,7 @@ from ._lib import ArapError, SolveConfig, SolveStats, check  # noqa: F401
 
 __all__ = ["build_graph", "compute_weights", "Solver", "node_table", "end_points",
            "skin_gaussians", "skin_gaussians_backward", "node_quaternions", "skin_samples", "update_nodes",
-           "static_mask", "aims_translate", "aims_twist", "aims_scale", "device_status",
+           "static_mask", "aims_translate", "aims_twist", "aims_scale", "device_status", "StatusWord",
            "default_config", "GaussianDeformer"]
 
 
@@ -56,9 +56,46 @@ def _i32(t):
     return t.to(device="cuda", dtype=torch.int32).contiguous()
 
 
+class StatusWord:
+    """A device status word (int32) of the caller's, for the stateless calls
+    that can raise a device-side error (arap_compute_weights,
+    arap_skin_gaussians, arap_skin_gaussians_backward, arap_node_quaternions):
+    the first ARAP_* code raised into it wins until ``read`` clears it."""
+
+    def __init__(self):
+        self.t = torch.zeros(1, dtype=torch.int32, device="cuda")
+
+    def ptr(self):
+        return _p(self.t)
+
+    def read(self) -> int:
+        """Read and clear (synchronises the current stream)."""
+        return _lib_().arap_status_read(_p(self.t), _s())
+
+
+_default_words = {}
+
+
+def _status(status):
+    """The word a stateless call records into: the caller's, or this
+    process's default word of the current device (read by device_status)."""
+    if status is not None:
+        return status.ptr()
+    dev = torch.cuda.current_device()
+    w = _default_words.get(dev)
+    if w is None:
+        w = _default_words[dev] = StatusWord()
+    return w.ptr()
+
+
 def device_status() -> int:
-    """Read and clear the library's sticky device error word."""
-    return _lib_().arap_get_device_status(_s())
+    """Read and clear the default status word of the current device: the
+    first device-side error of the stateless calls made without their own
+    StatusWord (handles keep their own words: Solver.status, SkinPlan.status,
+    Grid.status)."""
+    dev = torch.cuda.current_device()
+    w = _default_words.get(dev)
+    return w.read() if w is not None else 0
 
 
 def default_config(**kw) -> SolveConfig:
@@ -83,7 +120,7 @@ def build_graph(nodes: torch.Tensor, k: int) -> torch.Tensor:
     return out
 
 
-def compute_weights(points: torch.Tensor, nodes: torch.Tensor, k: int):
+def compute_weights(points: torch.Tensor, nodes: torch.Tensor, k: int, status=None):
     """kNN skinning weights (DeformGraph::computeWeights, Deform.hpp:187-208).
     Returns (idx [k,P] int32, w [k,P] float32) in planes layout."""
     points = _f32(points)
@@ -92,7 +129,7 @@ def compute_weights(points: torch.Tensor, nodes: torch.Tensor, k: int):
     idx = torch.empty((k, P), dtype=torch.int32, device="cuda")
     w = torch.empty((k, P), dtype=torch.float32, device="cuda")
     check("arap_compute_weights", _lib_().arap_compute_weights(
-        _p(points), P, _p(nodes), nodes.shape[0], k, _p(idx), _p(w), _s()))
+        _p(points), P, _p(nodes), nodes.shape[0], k, _p(idx), _p(w), _status(status), _s()))
     return idx, w
 
 
@@ -153,6 +190,10 @@ class Solver:
                                          C.byref(st) if st is not None else None, _s())
         check("arap_solver_solve", code)
         return rot_out, trans_out, (st.as_dict() if st is not None else None)
+
+    def status(self) -> int:
+        """Read and clear the solver's device status word (synchronises)."""
+        return _lib_().arap_solver_status(self._h, _s())
 
     def energy_grad(self, node_pos, aims, x):
         """(J^T f at x [F*12] float64, f.f) -- the gradient of 0.5|f|^2 as the
@@ -263,12 +304,12 @@ def end_points(pos, rot, scale, with_xyz=True):
 
 
 def skin_gaussians(ends, ends_idx, ends_w, table, scale0, pos_out, rot_inout, scale_out,
-                   shs=None, cov_out=None, static=None, precision=_lib.PRECISION_PLAIN):
+                   shs=None, cov_out=None, static=None, precision=_lib.PRECISION_PLAIN, status=None):
     N = pos_out.shape[0]
     k = ends_idx.shape[0]
     check("arap_skin_gaussians", _lib_().arap_skin_gaussians(
         N, k, _p(ends), _p(ends_idx), _p(ends_w), _p(table), _p(scale0), _p(static), _p(pos_out),
-        _p(rot_inout), _p(scale_out), _p(shs), _p(cov_out), int(precision), _s()))
+        _p(rot_inout), _p(scale_out), _p(shs), _p(cov_out), int(precision), _status(status), _s()))
 
 
 class SkinPlan:
@@ -288,6 +329,10 @@ class SkinPlan:
         t, o, m = C.c_int(), C.c_int(), C.c_int()
         check("arap_skin_plan_info", _lib_().arap_skin_plan_info(self._h, C.byref(t), C.byref(o), C.byref(m)))
         return {"tiles": t.value, "overflow_tiles": o.value, "max_nodes": m.value}
+
+    def status(self) -> int:
+        """Read and clear the plan's device status word (synchronises)."""
+        return _lib_().arap_skin_plan_status(self._h, _s())
 
     def close(self):
         if getattr(self, "_h", None) is not None and self._h.value:
@@ -309,7 +354,7 @@ def skin_gaussians_planned(plan, ends, table, scale0, pos_out, rot_inout, scale_
 
 
 def skin_gaussians_backward(ends_in, ends_idx, ends_w, table, scale0, grad_pos, grad_cov, n, static=None,
-                            grad_node=None):
+                            grad_node=None, status=None):
     """Adjoint of skin_gaussians' (mu, Sigma) w.r.t. the node transforms:
     returns grad_node [n,12] ([dR column-major 9 | dt 3])."""
     N = grad_pos.shape[0]
@@ -318,14 +363,15 @@ def skin_gaussians_backward(ends_in, ends_idx, ends_w, table, scale0, grad_pos, 
         grad_node = torch.zeros((n, 12), dtype=torch.float32, device="cuda")
     check("arap_skin_gaussians_backward", _lib_().arap_skin_gaussians_backward(
         N, k, _p(ends_in), _p(ends_idx), _p(ends_w), _p(table), _p(scale0), _p(static), _p(grad_pos),
-        _p(grad_cov), _p(grad_node), _s()))
+        _p(grad_cov), _p(grad_node), _status(status), _s()))
     return grad_node
 
 
-def node_quaternions(rot, precision=_lib.PRECISION_PLAIN):
+def node_quaternions(rot, precision=_lib.PRECISION_PLAIN, status=None):
     n = rot.shape[0]
     out = torch.empty((n, 4), dtype=torch.float32, device="cuda")
-    check("arap_node_quaternions", _lib_().arap_node_quaternions(n, _p(rot), _p(out), int(precision), _s()))
+    check("arap_node_quaternions", _lib_().arap_node_quaternions(n, _p(rot), _p(out), int(precision),
+                                                                 _status(status), _s()))
     return out
 
 
@@ -384,6 +430,7 @@ class GaussianDeformer:
     def __init__(self, pos, rot, scale, shs, node_vertex, k, blocks, block_type,
                  sample_pos=None, feature=None, config=None, use_plan=True, **cfg_kw):
         dev = "cuda"
+        self.word = StatusWord()   # device errors of this field's stateless calls
         self.k = int(k)
         self.pos = _f32(pos)
         self.rot = _f32(rot)
@@ -396,17 +443,18 @@ class GaussianDeformer:
         self.node_pos = self.pos[nv].contiguous()
         self.n = self.node_pos.shape[0]
         self.neighbors = build_graph(self.node_pos, self.k)
-        gidx, gw = compute_weights(self.pos, self.node_pos, self.k)
+        gidx, gw = compute_weights(self.pos, self.node_pos, self.k, status=self.word)
         self.anchor_idx = gidx[:, nv].contiguous()
         self.anchor_w = gw[:, nv].contiguous()
         self.ends, ends_xyz = end_points(self.pos, self.rot, self.scale)
-        self.ends_idx, self.ends_w = compute_weights(ends_xyz, self.node_pos, self.k)
+        self.ends_idx, self.ends_w = compute_weights(ends_xyz, self.node_pos, self.k, status=self.word)
         del ends_xyz
         self.skin_plan = SkinPlan(self.ends_idx, self.ends_w) if use_plan else None
         self.sample_pos = _f32(sample_pos) if sample_pos is not None else None
         self.feature = _f32(feature) if feature is not None else None
         if self.sample_pos is not None:
-            self.sample_idx, self.sample_w = compute_weights(self.sample_pos, self.node_pos, self.k)
+            self.sample_idx, self.sample_w = compute_weights(self.sample_pos, self.node_pos, self.k,
+                                                             status=self.word)
         self.blocks = [torch.as_tensor(b, dtype=torch.int64) for b in blocks]
         self.block_type = [int(t) for t in block_type]
         node_static = torch.zeros(self.n, dtype=torch.uint8, device=dev)
@@ -488,7 +536,7 @@ class GaussianDeformer:
         rot, trans, st = self.solver.solve(self.node_pos, self.aims, self.rot_nodes, self.trans_nodes, stats=stats)
         table = node_table(rot, trans, self.node_pos)
         if self.sample_pos is not None:
-            quat = node_quaternions(rot, self.precision) if self.feature is not None else None
+            quat = node_quaternions(rot, self.precision, status=self.word) if self.feature is not None else None
             skin_samples(self.sample_pos, self.sample_idx, self.sample_w, table, quat, self.feature, self.s_static)
         if skin_events is not None:
             skin_events[0].record()
@@ -497,10 +545,19 @@ class GaussianDeformer:
                                    self.shs, self.cov if with_cov else None, self.g_static, self.precision)
         else:
             skin_gaussians(self.ends, self.ends_idx, self.ends_w, table, self.scale0, self.pos, self.rot,
-                           self.scale, self.shs, self.cov if with_cov else None, self.g_static, self.precision)
+                           self.scale, self.shs, self.cov if with_cov else None, self.g_static, self.precision,
+                           status=self.word)
         if skin_events is not None:
             skin_events[1].record()
         update_nodes(self.node_pos, self.anchor_idx, self.anchor_w, table, self.node_pos_next)
         self.node_pos, self.node_pos_next = self.node_pos_next, self.node_pos
         self.aims.copy_(self.node_pos)
         return st
+
+    def status(self) -> int:
+        """Read and clear the device status words of this field: its solver's,
+        its skinning plan's and its own (stateless calls); the first error
+        found, else ARAP_OK (synchronises)."""
+        codes = [self.solver.status(), self.skin_plan.status() if self.skin_plan is not None else 0,
+                 self.word.read()]
+        return next((c for c in codes if c), 0)

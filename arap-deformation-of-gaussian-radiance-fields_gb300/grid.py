@@ -43,6 +43,10 @@ class Grid:
         # low_pass_filter_param = (step/4)^2 * lpf_parameter (GaussianView.cpp:3879-3881)
         self.lpf_param = (self.step / 4.0) ** 2 * LPF_PARAMETER
 
+    def status(self) -> int:
+        """Read and clear the grid's device status word (synchronises)."""
+        return _lib.load().arap_grid_status(self._h, _s())
+
     def arrays(self):
         """(cell_offsets [g^3+1], cell_lists [n_pairs], valid_cells [n_valid]) as int32 tensor copies."""
         off, lst, val = C.c_void_p(), C.c_void_p(), C.c_void_p()

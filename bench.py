@@ -280,7 +280,7 @@ def run_ours(a):
     for _ in range(max(3, a.warmup)):
         step(False)
     torch.cuda.synchronize()
-    assert dev.device_status() == 0
+    assert st.status() == 0
     step_ev = []
     if ws > 1:
         torch.distributed.barrier()
@@ -302,7 +302,7 @@ def run_ours(a):
     ms = [a0.elapsed_time(b0) for a0, b0 in step_ev]
     ms_step = reduce_max(float(np.mean(ms)), ws)
     skin_ms = float(np.mean([a0.elapsed_time(b0) for a0, b0 in skin_ev]))
-    status = dev.device_status()
+    status = st.status()
 
     # e2e: public API with host buffers (aims H2D, node transforms + energy D2H)
     aims_host = snap["aims"].cpu().pin_memory()

@@ -6,12 +6,19 @@
  * Conventions
  *   - Every array argument is a DEVICE pointer owned by the caller unless the
  *     parameter name ends in "_host".  Nothing is retained after a call except
- *     inside an explicit handle (arap_solver).
+ *     inside an explicit handle (arap_solver, arap_solver_batch, arap_grid,
+ *     arap_skin_plan).  The library keeps no global state: two handles used
+ *     from two streams or threads never share a word.
  *   - Every call takes the cudaStream_t it enqueues on (0 = legacy default).
  *     Calls return after enqueueing; results are ready once the stream is.
  *   - Every call returns an int status (ARAP_OK = 0).  Errors raised on the
- *     device (non-finite values, timed-out barrier waits) are reported by the
- *     calls that synchronise (arap_solver_solve, arap_get_device_status).
+ *     device (non-finite values, timed-out barrier waits) go to a device
+ *     status word: each handle owns one (read and cleared by
+ *     arap_solver_status / arap_grid_status / arap_skin_plan_status, and by
+ *     the calls that synchronise, such as arap_solver_solve with stats); the
+ *     stateless calls that can raise one take an `int32_t* status` device
+ *     word of the caller's (NULL: not recorded), read with arap_status_read.
+ *     The first code raised wins until the word is read.
  *   - Points are float32 xyz triples; quaternions are (w, x, y, z) float32;
  *     node rotations are column-major 3x3 ("[0 3 6; 1 4 7; 2 5 8]"), exactly
  *     DeformGraph::rot (Deform.hpp:29-38).
@@ -58,9 +65,12 @@ int arap_build_graph(const float* nodes_xyz, int n, int k, int32_t* neighbors_ou
  * GaussianView::setupWeights* GaussianView.cpp:2818-2918).
  * points_xyz [P*3]; idx_out, w_out in planes layout [k][P] (entry j of point i
  * at [j*P + i]).  Distances are compared as float32 sqrt((dx*dx+dy*dy)+dz*dz);
- * exact ties go to the lower node index. */
+ * exact ties go to the lower node index.  A point whose k+1 nearest nodes are
+ * all at the same distance gets NaN weights (the reference's 0/0) and
+ * ARAP_ENONFINITE in *status (device word, optional). */
 int arap_compute_weights(const float* points_xyz, int P, const float* nodes_xyz, int n,
-                         int k, int32_t* idx_out, float* w_out, arap_stream_t stream);
+                         int k, int32_t* idx_out, float* w_out, int32_t* status,
+                         arap_stream_t stream);
 
 /* --------------------------------------------------------------- solver --- */
 
@@ -81,6 +91,9 @@ typedef struct {
                              (per-aggregate affine) space; 0 = block-Jacobi only.  The
                              target is raised (by a quarter at a time) until there are
                              at most 80 aggregates (960 coarse unknowns). */
+  int spin_limit;         /* polls of one grid-barrier wait inside the persistent solve
+                             before it gives up with ARAP_ETIMEOUT (<=0: 2^23, about
+                             a second); every CTA then leaves the kernel */
 } arap_solve_config;
 
 typedef struct {
@@ -141,6 +154,11 @@ int arap_solver_solve(arap_solver* s, const float* node_pos, const float* aims,
 int arap_solver_energy_grad(arap_solver* s, const float* node_pos, const float* aims,
                             const double* x, double* grad_out, double* energy_host,
                             arap_stream_t stream);
+
+/* Read and clear the solver's device status word (synchronises the stream):
+ * ARAP_OK, or the first device-side error of its launches since the last
+ * read (ARAP_ETIMEOUT, ARAP_ENONFINITE, ARAP_EUNSUPPORTED). */
+int arap_solver_status(arap_solver* s, arap_stream_t stream);
 
 /* Number of free nodes (columns/12) and the free node ids ascending. */
 int arap_solver_free_count(const arap_solver* s);
@@ -222,12 +240,14 @@ int arap_end_points(int N, const float* pos, const float* rot, const float* scal
  *   static_mask [N] (uint8, optional): 1 = skip refit (static_gaussians)
  *   pos_out [N*3], rot_inout [N*4] (in: q of the previous frame), scale_out [N*3]
  *   shs_inout [N*48] optional, cov_out [N*6] optional (xx,xy,xz,yy,yz,zz of
- *   R diag(s)^2 R^T). */
+ *   R diag(s)^2 R^T).
+ *   status    device word (optional): ARAP_ENONFINITE when a polar factor
+ *             does not converge to a finite value. */
 int arap_skin_gaussians(int N, int k, float* ends, const int32_t* ends_idx,
                         const float* ends_w, const float* node_table, const float* scale0,
                         const uint8_t* static_mask, float* pos_out, float* rot_inout,
                         float* scale_out, float* shs_inout, float* cov_out, int precision,
-                        arap_stream_t stream);
+                        int32_t* status, arap_stream_t stream);
 
 /* Skinning plan: no counterpart in the reference; a set-up-time layout of
  * the endpoint kNN for arap_skin_gaussians_planned.
@@ -242,6 +262,9 @@ int arap_skin_plan_create(arap_skin_plan** out, int N, int k, const int32_t* end
 /* tiles; tiles with more than 256 distinct nodes (skinned from the global table);
  * the largest distinct-node count of the other tiles. */
 int arap_skin_plan_info(const arap_skin_plan* plan, int* tiles, int* overflow_tiles, int* max_nodes);
+/* Read and clear the device status word of the plan's skinning launches
+ * (synchronises the stream). */
+int arap_skin_plan_status(arap_skin_plan* plan, arap_stream_t stream);
 void arap_skin_plan_destroy(arap_skin_plan* plan);
 /* arap_skin_gaussians with the plan's layout and the same results (the same
  * arithmetic in the same order).
@@ -267,12 +290,13 @@ int arap_skin_gaussians_planned(const arap_skin_plan* plan, float* ends, const i
 int arap_skin_gaussians_backward(int N, int k, const float* ends_in, const int32_t* ends_idx,
                                  const float* ends_w, const float* node_table, const float* scale0,
                                  const uint8_t* static_mask, const float* grad_pos, const float* grad_cov,
-                                 float* grad_node, arap_stream_t stream);
+                                 float* grad_node, int32_t* status, arap_stream_t stream);
 
 /* Per-node unit quaternion of the Newton polar factor of R
  * (FastUpdateSamplesSH, GaussianView.cpp:3172-3181; FastgetOthogonalMatrix
- * helper.cpp:506-517).  quat_out [n*4] (w,x,y,z). */
-int arap_node_quaternions(int n, const float* rot, float* quat_out, int precision,
+ * helper.cpp:506-517).  quat_out [n*4] (w,x,y,z).  status: optional device
+ * word, ARAP_ENONFINITE when an iteration does not stay finite. */
+int arap_node_quaternions(int n, const float* rot, float* quat_out, int precision, int32_t* status,
                           arap_stream_t stream);
 
 /* One frame of sample skinning, fused: ED blend of the sample position
@@ -346,6 +370,9 @@ int arap_grid_build(arap_grid** out, int N, const float* pos, const float* rot, 
  * [n_pairs] (grided_gs_idx), valid_cells [n_valid] ascending (valid_grid_idx). */
 int arap_grid_arrays(const arap_grid* grid, const int32_t** cell_offsets, const int32_t** cell_lists,
                      const int32_t** valid_cells);
+
+/* Read and clear the grid's device status word (synchronises the stream). */
+int arap_grid_status(arap_grid* grid, arap_stream_t stream);
 
 /* Stable order of N Gaussians by the grid cell of their centre (cell index
  * x*g^2 + y*g + z ascending, original order within a cell): the reorder the
@@ -496,8 +523,11 @@ int arap_ply_save(const char* path, int64_t count, const float* pos, const float
 
 /* --------------------------------------------------------------- misc --- */
 
-/* Read and clear the library's sticky device error word (ARAP_* code). */
-int arap_get_device_status(arap_stream_t stream);
+/* Read and clear a caller-owned device status word (an int32 the caller
+ * allocated and zeroed, passed as `status` to the stateless calls): returns
+ * the first ARAP_* code raised into it since it was last cleared.
+ * Synchronises the stream. */
+int arap_status_read(int32_t* status_dev, arap_stream_t stream);
 
 /* Library version string. */
 const char* arap_version(void);

@@ -82,7 +82,7 @@ def test_frame_matches_the_oracle(dev, case, form):
     fr, nodes_ref = _oracle_frame(d, sc, samples, feature, g["x"])
     st = d.frame(stats=True, with_cov=True)
     torch.cuda.synchronize()
-    assert st["status"] == 0 and dev.device_status() == 0
+    assert st["status"] == 0 and d.status() == 0
     assert st["gn_iterations"] == int(g["iters"])
     X = np.concatenate([_np(d.rot_nodes), _np(d.trans_nodes)], 1)
     err_x = _rel(X, g["x"].astype(np.float64))

@@ -61,7 +61,7 @@ def test_planned_skinning_is_bit_identical(dev, name, order):
             dev.skin_gaussians(ends, eidx, ew, table, _t(scale0), pos, q, s, shs, cov, precision=1)
         outs.append((ends, pos, q, s, shs, cov))
     torch.cuda.synchronize()
-    assert dev.device_status() == 0
+    assert dev.device_status() == 0 and plan.status() == 0
     for a, b in zip(*outs):
         assert torch.equal(a, b)
     plan.close()
