@@ -364,7 +364,7 @@ __device__ __forceinline__ bool polar_factor(const T* M, T* R, int max_it, T tol
   for (int it = 0; it < max_it; ++it) {
     T Y[9];
     if (!inv_transpose3(X, Y)) return false;
-    T g = T(1);
+    T g = T(1), ig = T(1);
     if (it < 3) {
       T nx = 0, ny = 0;
 #pragma unroll
@@ -373,11 +373,12 @@ __device__ __forceinline__ bool polar_factor(const T* M, T* R, int max_it, T tol
         ny += Y[i] * Y[i];
       }
       g = sqrt(sqrt(ny / nx));
+      ig = T(1) / g;
     }
     T delta = 0;
 #pragma unroll
     for (int i = 0; i < 9; ++i) {
-      const T xn = T(0.5) * (g * X[i] + Y[i] / g);
+      const T xn = T(0.5) * (g * X[i] + Y[i] * ig);
       delta = fmax(delta, fabs(xn - X[i]));
       X[i] = xn;
     }
@@ -630,6 +631,67 @@ __device__ __forceinline__ void rotate_sh48(const float* R, float* s) {
       s[k * 3 + 1] = -s[k * 3 + 1];
       s[k * 3 + 2] = -s[k * 3 + 2];
     }
+  }
+}
+
+// ------------------------------------------------------ segment sort ----
+// Ascending sort of one segment keys[0..L) of DISTINCT keys by one CTA, for
+// segments longer than a shared-memory sort holds: chunks of CHUNK keys are
+// bitonic-sorted in shared memory (s_keys, CHUNK keys, padded with `pad`,
+// larger than every key), then runs are merged pairwise through scratch[0..L)
+// (global memory of the caller's), each key going straight to its place: its
+// index in its own run plus its rank in the other run (a binary search; the
+// keys being distinct, no two keys claim one place).
+template <typename T, int CHUNK>
+__device__ void cta_sort_distinct(T* keys, T* scratch, int L, T pad, T* s_keys) {
+  const int tid = threadIdx.x, bd = blockDim.x;
+  for (int c0 = 0; c0 < L; c0 += CHUNK) {
+    const int n = min(CHUNK, L - c0);
+    int P2 = 1;
+    while (P2 < n) P2 <<= 1;
+    for (int t = tid; t < P2; t += bd) s_keys[t] = t < n ? keys[c0 + t] : pad;
+    __syncthreads();
+    for (int k = 2; k <= P2; k <<= 1)
+      for (int j = k >> 1; j > 0; j >>= 1) {
+        for (int t = tid; t < P2; t += bd) {
+          const int u = t ^ j;
+          if (u > t) {
+            const T a = s_keys[t], b = s_keys[u];
+            if ((a > b) == ((t & k) == 0)) {
+              s_keys[t] = b;
+              s_keys[u] = a;
+            }
+          }
+        }
+        __syncthreads();
+      }
+    for (int t = tid; t < n; t += bd) keys[c0 + t] = s_keys[t];
+    __syncthreads();
+  }
+  T* a = keys;
+  T* b = scratch;
+  for (int w = CHUNK; w < L; w <<= 1) {
+    for (int i = tid; i < L; i += bd) {
+      const int base = (i / (2 * w)) * (2 * w);
+      const bool left = i - base < w;
+      const int o0 = left ? base + w : base;  // the other run
+      const int on = left ? max(0, min(w, L - (base + w))) : w;
+      const T x = a[i];
+      int lo = 0, hi = on;
+      while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (a[o0 + mid] < x) lo = mid + 1; else hi = mid;
+      }
+      b[base + (left ? i - base : i - base - w) + lo] = x;
+    }
+    __syncthreads();
+    T* t = a;
+    a = b;
+    b = t;
+  }
+  if (a != keys) {
+    for (int i = tid; i < L; i += bd) keys[i] = a[i];
+    __syncthreads();
   }
 }
 

@@ -253,9 +253,11 @@ __global__ void compact_kernel(int n, const int* __restrict__ count, const int* 
 
 constexpr int kSortMax = 16384;
 
-// Bitonic sort of each occupied cell's list in shared memory (one CTA per cell).
+// Bitonic sort of each occupied cell's list in shared memory (one CTA per
+// cell).  A cell longer than kSortMax is appended to big[] (count in
+// *big_n) for sort_big_cells_kernel.
 __global__ void sort_cells_kernel(int nvalid, const int* __restrict__ valid, const int* __restrict__ off,
-                                  int* __restrict__ lists, int* __restrict__ status) {
+                                  int* __restrict__ lists, int* __restrict__ big_n, int* __restrict__ big) {
   extern __shared__ int s_keys[];
   const int v = blockIdx.x;
   if (v >= nvalid) return;
@@ -263,7 +265,7 @@ __global__ void sort_cells_kernel(int nvalid, const int* __restrict__ valid, con
   const int b = off[c], L = off[c + 1] - b;
   if (L <= 1) return;
   if (L > kSortMax) {
-    if (threadIdx.x == 0) raise_status(status, ARAP_EUNSUPPORTED);
+    if (threadIdx.x == 0) big[atomicAdd(big_n, 1)] = v;
     return;
   }
   int P2 = 1;
@@ -287,6 +289,29 @@ __global__ void sort_cells_kernel(int nvalid, const int* __restrict__ valid, con
     }
   }
   for (int t = threadIdx.x; t < L; t += blockDim.x) lists[b + t] = s_keys[t];
+}
+
+// Lengths of the cells sort_cells_kernel set aside.
+__global__ void big_cell_sizes_kernel(int nbig, const int* __restrict__ big, const int* __restrict__ valid,
+                                      const int* __restrict__ off, int* __restrict__ sizes) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= nbig) return;
+  const int c = valid[big[k]];
+  sizes[k] = off[c + 1] - off[c];
+}
+
+// The long cells, one CTA each: chunk sorts and merges (cta_sort_distinct)
+// through the cell's part of scratch (at scratch_off[k], the cell's length).
+__global__ void __launch_bounds__(1024) sort_big_cells_kernel(int nbig, const int* __restrict__ big,
+                                                              const int* __restrict__ valid,
+                                                              const int* __restrict__ off, int* lists,
+                                                              int* scratch, const long long* __restrict__ scratch_off) {
+  extern __shared__ int s_keys[];
+  const int k = blockIdx.x;
+  if (k >= nbig) return;
+  const int c = valid[big[k]];
+  const int b = off[c], L = off[c + 1] - b;
+  cta_sort_distinct<int, kSortMax>(lists + b, scratch + scratch_off[k], L, INT_MAX, s_keys);
 }
 
 // Cell of each Gaussian centre (GaussianView.cpp:3918-3928) and per-cell counts.
@@ -855,6 +880,60 @@ static int scan_exclusive(const int* in, int* out, int n, long long* sums, cudaS
   return ARAP_OK;
 }
 
+// Sort every occupied cell's list ascending: one CTA per cell in shared
+// memory, then the cells longer than kSortMax (the reference's serial fill
+// has no limit, GaussianView.cpp:4077-4100) by sort_big_cells_kernel.
+// big_n [1], big and sizes [nvalid] are free device ints of the caller's;
+// alloc(bytes) gives the long cells' scratch (device memory, 8-byte aligned)
+// or nullptr when there is no room, and the call then returns no_room.
+template <typename Alloc>
+static int sort_cell_lists(int nvalid, const int* valid, const int* off, int* lists, int* big_n, int* big,
+                           int* sizes, Alloc alloc, int no_room, cudaStream_t st) {
+  if (nvalid <= 0) return ARAP_OK;
+  if (cudaMemsetAsync(big_n, 0, sizeof(int), st) != cudaSuccess ||
+      cudaFuncSetAttribute(sort_cells_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           kSortMax * (int)sizeof(int)) != cudaSuccess) {
+    (void)cudaGetLastError();
+    return ARAP_ECUDA;
+  }
+  sort_cells_kernel<<<nvalid, 256, kSortMax * sizeof(int), st>>>(nvalid, valid, off, lists, big_n, big);
+  int nbig = 0;
+  if (cudaPeekAtLastError() != cudaSuccess ||
+      cudaMemcpyAsync(&nbig, big_n, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+      cudaStreamSynchronize(st) != cudaSuccess) {
+    (void)cudaGetLastError();
+    return ARAP_ECUDA;
+  }
+  if (nbig == 0) return ARAP_OK;
+  big_cell_sizes_kernel<<<grid_for(nbig, 128), 128, 0, st>>>(nbig, big, valid, off, sizes);
+  std::vector<int> hs(nbig);
+  if (cudaPeekAtLastError() != cudaSuccess ||
+      cudaMemcpyAsync(hs.data(), sizes, sizeof(int) * (size_t)nbig, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+      cudaStreamSynchronize(st) != cudaSuccess) {
+    (void)cudaGetLastError();
+    return ARAP_ECUDA;
+  }
+  std::vector<long long> so((size_t)nbig + 1, 0);
+  for (int k = 0; k < nbig; ++k) so[k + 1] = so[k] + hs[k];
+  const size_t b_off = sizeof(long long) * ((size_t)nbig + 1);
+  char* scr = static_cast<char*>(alloc(b_off + sizeof(int) * (size_t)so[nbig]));
+  if (!scr) return no_room;
+  long long* d_so = reinterpret_cast<long long*>(scr);
+  int* d_keys = reinterpret_cast<int*>(scr + b_off);
+  if (cudaMemcpyAsync(d_so, so.data(), b_off, cudaMemcpyHostToDevice, st) != cudaSuccess ||
+      cudaFuncSetAttribute(sort_big_cells_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           kSortMax * (int)sizeof(int)) != cudaSuccess) {
+    (void)cudaGetLastError();
+    return ARAP_ECUDA;
+  }
+  sort_big_cells_kernel<<<nbig, 1024, kSortMax * sizeof(int), st>>>(nbig, big, valid, off, lists, d_keys, d_so);
+  if (cudaPeekAtLastError() != cudaSuccess || cudaStreamSynchronize(st) != cudaSuccess) {
+    (void)cudaGetLastError();
+    return ARAP_ECUDA;
+  }
+  return ARAP_OK;
+}
+
 extern "C" void arap_grid_destroy(arap_grid* G) {
   if (!G) return;
   cudaFree(G->params);
@@ -944,11 +1023,19 @@ extern "C" int arap_grid_build(arap_grid** out, int N, const float* pos, const f
     return fail(ARAP_ENOMEM);
   }
   compact_kernel<<<grid_for(C, 256), 256, 0, st>>>(C, count, flagpos, G->valid);
-  if (nvalid > 0) {
-    if (cudaFuncSetAttribute(sort_cells_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             kSortMax * (int)sizeof(int)))
-      return fail(ARAP_ECUDA);
-    sort_cells_kernel<<<nvalid, 256, kSortMax * sizeof(int), st>>>(nvalid, G->valid, G->off, G->lists, G->status);
+  {
+    // count, cursor and flagpos are free now: the long-cell list and lengths
+    void* big_scratch = nullptr;
+    auto alloc = [&](size_t bytes) -> void* {
+      if (cudaMallocAsync(&big_scratch, bytes, st) != cudaSuccess) {
+        (void)cudaGetLastError();
+        big_scratch = nullptr;
+      }
+      return big_scratch;
+    };
+    rc = sort_cell_lists(nvalid, G->valid, G->off, G->lists, flagpos, count, cursor, alloc, ARAP_ENOMEM, st);
+    if (big_scratch) cudaFreeAsync(big_scratch, st);
+    if (rc != ARAP_OK) return fail(rc);
   }
   if (cudaPeekAtLastError() != cudaSuccess) {
     (void)cudaGetLastError();
@@ -1017,16 +1104,23 @@ extern "C" int arap_grid_center_order(const arap_grid* G, int N, const float* po
       return done(ARAP_ENOMEM);
     }
     compact_kernel<<<grid_for(C, 256), 256, 0, st>>>(C, count, flagpos, valid);
-    if (cudaFuncSetAttribute(sort_cells_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSortMax * (int)sizeof(int)))
-      return done(ARAP_ECUDA);
-    sort_cells_kernel<<<nvalid, 256, kSortMax * sizeof(int), st>>>(nvalid, valid, off, order_out, G->status);
+    void* big_scratch = nullptr;
+    auto alloc = [&](size_t bytes) -> void* {
+      if (cudaMallocAsync(&big_scratch, bytes, st) != cudaSuccess) {
+        (void)cudaGetLastError();
+        big_scratch = nullptr;
+      }
+      return big_scratch;
+    };
+    rc = sort_cell_lists(nvalid, valid, off, order_out, flagpos, count, cursor, alloc, ARAP_ENOMEM, st);
+    if (big_scratch) cudaFreeAsync(big_scratch, st);
+    if (rc != ARAP_OK) return done(rc);
   }
   if (cudaPeekAtLastError() != cudaSuccess || cudaStreamSynchronize(st) != cudaSuccess) {
     (void)cudaGetLastError();
     return done(ARAP_ECUDA);
   }
-  done(ARAP_OK);
-  return status_read_clear(G->status, st);
+  return done(ARAP_OK);
 }
 
 extern "C" int arap_grid_status(arap_grid* G, arap_stream_t stream) {
@@ -1172,33 +1266,22 @@ extern "C" int arap_stage2_cell_flags(const arap_grid* G, const float* aim_opaci
 // ------------------------------------------- allocation-free centre order ----
 // arap_grid_center_order_noalloc: the same kernel sequence as
 // arap_grid_center_order with its scratch carved from one static device array
-// of ARAP_CENTER_SCRATCH_BYTES instead of cudaMalloc/cudaFree.  The array's
-// address is resolved once per device, with that device current, by the first
-// call on it.  Calls that overlap on the GPU share the array and race.
+// of ARAP_CENTER_SCRATCH_BYTES instead of cudaMalloc/cudaFree.  Host code
+// cannot use the array's name as a device address, so every call looks the
+// address up with cudaGetSymbolAddress on the current device (a host-side
+// query; the first one on a device loads the module there, so that first call
+// should come before any stream capture).  Calls that overlap on the GPU
+// share the array and race.
 static __device__ __align__(256) unsigned char g_center_scratch[ARAP_CENTER_SCRATCH_BYTES];
 
 namespace {
-constexpr int kMaxScratchDevices = 64;
-std::atomic<unsigned char*> g_center_scratch_ptr[kMaxScratchDevices];
-
 int center_scratch_base(unsigned char** out) {
-  int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess) {
+  unsigned char* ptr = nullptr;
+  if (cudaGetSymbolAddress((void**)&ptr, g_center_scratch) != cudaSuccess || !ptr) {
     (void)cudaGetLastError();
     return ARAP_ECUDA;
   }
-  if (dev < 0 || dev >= kMaxScratchDevices) return ARAP_EUNSUPPORTED;
-  unsigned char* p = g_center_scratch_ptr[dev].load(std::memory_order_acquire);
-  if (!p) {
-    unsigned char* ptr = nullptr;
-    if (cudaGetSymbolAddress((void**)&ptr, g_center_scratch) != cudaSuccess || !ptr) {
-      (void)cudaGetLastError();
-      return ARAP_ECUDA;
-    }
-    g_center_scratch_ptr[dev].store(ptr, std::memory_order_release);
-    p = ptr;
-  }
-  *out = p;
+  *out = ptr;
   return ARAP_OK;
 }
 
@@ -1245,13 +1328,17 @@ extern "C" int arap_grid_center_order_noalloc(const arap_grid* G, int N, const f
   }
   if (nvalid > 0) {
     compact_kernel<<<grid_for(C, 256), 256, 0, st>>>(C, count, flagpos, valid);
-    if (cudaFuncSetAttribute(sort_cells_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSortMax * (int)sizeof(int)))
-      return ARAP_ECUDA;
-    sort_cells_kernel<<<nvalid, 256, kSortMax * sizeof(int), st>>>(nvalid, valid, off, order_out, G->status);
+    // cells longer than the shared-memory sort take their merge scratch from
+    // the rest of the static array
+    auto alloc = [&](size_t bytes) -> void* {
+      return need + bytes <= (size_t)ARAP_CENTER_SCRATCH_BYTES ? static_cast<void*>(base + need) : nullptr;
+    };
+    rc = sort_cell_lists(nvalid, valid, off, order_out, flagpos, count, cursor, alloc, ARAP_EUNSUPPORTED, st);
+    if (rc != ARAP_OK) return rc;
   }
   if (cudaPeekAtLastError() != cudaSuccess || cudaStreamSynchronize(st) != cudaSuccess) {
     (void)cudaGetLastError();
     return ARAP_ECUDA;
   }
-  return status_read_clear(G->status, st);
+  return ARAP_OK;
 }

@@ -25,6 +25,7 @@
 #include <unistd.h>
 
 #include <algorithm>
+#include <cerrno>
 #include <atomic>
 #include <cmath>
 #include <cstdint>
@@ -188,7 +189,8 @@ void radix_sort_stable(std::vector<uint64_t>& key, std::vector<uint32_t>& order)
 }
 
 // Reads [offset, offset + bytes) of the file into dst with nt threads, each
-// issuing pread on its own contiguous range.  False on any short read.
+// issuing pread on its own contiguous range.  A read a signal interrupts
+// (EINTR) is retried; false on end of file or any other error.
 bool read_parallel(const char* path, size_t offset, char* dst, size_t bytes, int nt) {
   const int fd = ::open(path, O_RDONLY);
   if (fd < 0) return false;
@@ -197,6 +199,7 @@ bool read_parallel(const char* path, size_t offset, char* dst, size_t bytes, int
     size_t done = b;
     while (done < e) {
       const ssize_t r = ::pread(fd, dst + done, e - done, (off_t)(offset + done));
+      if (r < 0 && errno == EINTR) continue;
       if (r <= 0) {
         ok = false;
         return;

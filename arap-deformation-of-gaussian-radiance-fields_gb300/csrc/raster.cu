@@ -15,7 +15,9 @@
 // Tile lists: a count per tile, a scan, an atomic fill.  raster_tile_kernel,
 // one CTA of 256 threads per tile (one per pixel): the tile's list, keyed by
 // (depth bits, Gaussian index), is bitonic-sorted in shared memory, so the
-// order is deterministic.  Then the Gaussians are composited front to back
+// order is deterministic; a list longer than kMaxTileList is sorted before by
+// raster_sort_long_kernel (chunk sorts and merges through global scratch) and
+// read from global memory.  Then the Gaussians are composited front to back
 // in batches staged in shared memory:
 // - alpha = min(0.99, o exp(power)); a term with power > 0 or alpha < 1/255
 //   is skipped;
@@ -26,6 +28,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdint>
+#include <vector>
 
 #include "arap_common.cuh"
 
@@ -33,6 +36,22 @@ namespace arap {
 
 constexpr int kTile = 16;
 constexpr int kMaxTileList = 16384;  // sort keys per tile held in shared memory (128 KB)
+
+// Tiles with more than kMaxTileList entries, one CTA each: their key runs
+// sorted in place (keys are distinct: the Gaussian index is in the low bits).
+__global__ void __launch_bounds__(1024) raster_sort_long_kernel(int nlong, const int* __restrict__ long_tiles,
+                                                                const int* __restrict__ tile_off,
+                                                                const int* __restrict__ tile_count,
+                                                                unsigned long long* keys,
+                                                                unsigned long long* scratch,
+                                                                const long long* __restrict__ scratch_off) {
+  extern __shared__ unsigned long long s_sort[];
+  const int k = blockIdx.x;
+  if (k >= nlong) return;
+  const int t = long_tiles[k];
+  cta_sort_distinct<unsigned long long, kMaxTileList>(keys + tile_off[t], scratch + scratch_off[k], tile_count[t],
+                                                      ~0ull, s_sort);
+}
 
 struct RasterCam {
   float view[16];  // row-major, world -> camera
@@ -236,7 +255,7 @@ __global__ void __launch_bounds__(256) raster_tile_kernel(
     RasterCam cam, const int* __restrict__ tile_off, const int* __restrict__ tile_count,
     const unsigned long long* __restrict__ keys, const float* __restrict__ xy, const float* __restrict__ conic_op,
     const float* __restrict__ color, float bg0, float bg1, float bg2, float* __restrict__ image,
-    float* __restrict__ final_t, int* __restrict__ n_contrib, int* __restrict__ status) {
+    float* __restrict__ final_t, int* __restrict__ n_contrib) {
   extern __shared__ unsigned long long s_keys[];
   __shared__ float s_xy[256][2];
   __shared__ float s_co[256][4];
@@ -245,30 +264,31 @@ __global__ void __launch_bounds__(256) raster_tile_kernel(
   const int tx = tile % cam.gx, ty = tile / cam.gx;
   const int n = tile_count[tile];
   const int off = tile_off[tile];
-  if (n > kMaxTileList) {
-    if (threadIdx.x == 0) atomicOr(status, 1);
-    return;
-  }
-  // bitonic sort of the tile's keys, padded to a power of two with ~0
-  int m = 1;
-  while (m < n) m <<= 1;
-  for (int t = threadIdx.x; t < m; t += 256) s_keys[t] = t < n ? keys[(size_t)off + t] : ~0ull;
-  __syncthreads();
-  for (int k = 2; k <= m; k <<= 1)
-    for (int j = k >> 1; j > 0; j >>= 1) {
-      for (int t = threadIdx.x; t < m; t += 256) {
-        const int u = t ^ j;
-        if (u > t) {
-          const unsigned long long a = s_keys[t], b = s_keys[u];
-          const bool up = (t & k) == 0;
-          if ((a > b) == up) {
-            s_keys[t] = b;
-            s_keys[u] = a;
+  // a long list was sorted in global memory before; a short one is
+  // bitonic-sorted here, padded to a power of two with ~0
+  const bool long_list = n > kMaxTileList;
+  const unsigned long long* sorted = long_list ? keys + off : s_keys;
+  if (!long_list) {
+    int m = 1;
+    while (m < n) m <<= 1;
+    for (int t = threadIdx.x; t < m; t += 256) s_keys[t] = t < n ? keys[(size_t)off + t] : ~0ull;
+    __syncthreads();
+    for (int k = 2; k <= m; k <<= 1)
+      for (int j = k >> 1; j > 0; j >>= 1) {
+        for (int t = threadIdx.x; t < m; t += 256) {
+          const int u = t ^ j;
+          if (u > t) {
+            const unsigned long long a = s_keys[t], b = s_keys[u];
+            const bool up = (t & k) == 0;
+            if ((a > b) == up) {
+              s_keys[t] = b;
+              s_keys[u] = a;
+            }
           }
         }
+        __syncthreads();
       }
-      __syncthreads();
-    }
+  }
   // front-to-back compositing, one thread per pixel
   const int px = tx * kTile + (threadIdx.x % kTile), py = ty * kTile + (threadIdx.x / kTile);
   const bool inside = px < cam.width && py < cam.height;
@@ -279,7 +299,7 @@ __global__ void __launch_bounds__(256) raster_tile_kernel(
     if (__syncthreads_and(done)) break;
     const int q = base + threadIdx.x;
     if (q < n) {
-      const int gi = (int)(unsigned int)(s_keys[q] & 0xffffffffull);
+      const int gi = (int)(unsigned int)(sorted[q] & 0xffffffffull);
       s_xy[threadIdx.x][0] = xy[2 * (size_t)gi];
       s_xy[threadIdx.x][1] = xy[2 * (size_t)gi + 1];
 #pragma unroll
@@ -354,7 +374,7 @@ extern "C" int arap_render(int N, const float* pos, const float* shs, const floa
   // per Gaussian; count, offset, cursor per tile; the total
   char* scratch = nullptr;
   const size_t bytes_g = n * (10 * sizeof(float) + 4 * sizeof(int));
-  const size_t bytes_t = (size_t)tiles * 3 * sizeof(int) + 2 * sizeof(int);
+  const size_t bytes_t = (size_t)tiles * 3 * sizeof(int) + sizeof(int);
   ARAP_CUDA_TRY(cudaMallocAsync(&scratch, bytes_g + bytes_t, st));
   float* xy = reinterpret_cast<float*>(scratch);
   float* co = xy + 2 * n;
@@ -365,13 +385,11 @@ extern "C" int arap_render(int N, const float* pos, const float* shs, const floa
   int* toff = tcount + tiles;
   int* tcur = toff + tiles;
   int* total = tcur + tiles;
-  int* status = total + 1;
   int rc = ARAP_OK;
-  int h_total = 0, h_status = 0;
+  int h_total = 0;
   unsigned long long* keys = nullptr;
   cudaMemsetAsync(tcount, 0, (size_t)tiles * sizeof(int), st);
   cudaMemsetAsync(tcur, 0, (size_t)tiles * sizeof(int), st);
-  cudaMemsetAsync(status, 0, sizeof(int), st);
   if (N > 0)
     raster_preprocess_kernel<<<(N + 127) / 128, 128, 0, st>>>(N, pos, shs, opacity, scale, rot, cam, xy, co, col,
                                                               dep, rect, tcount);
@@ -383,24 +401,63 @@ extern "C" int arap_render(int N, const float* pos, const float* shs, const floa
   if (rc == ARAP_OK && cudaMallocAsync(&keys, sizeof(unsigned long long) * (size_t)std::max(h_total, 1), st) !=
                            cudaSuccess)
     rc = ARAP_ENOMEM;
+  // tiles whose lists exceed the shared-memory sort: sorted in global memory
+  std::vector<int> long_tiles;
+  std::vector<long long> long_off(1, 0);
+  const size_t smem = sizeof(unsigned long long) * kMaxTileList;
+  if (rc == ARAP_OK && h_total > kMaxTileList) {
+    std::vector<int> cnt(tiles);
+    if (cudaMemcpyAsync(cnt.data(), tcount, sizeof(int) * (size_t)tiles, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess)
+      rc = ARAP_ECUDA;
+    for (int t = 0; rc == ARAP_OK && t < tiles; ++t)
+      if (cnt[t] > kMaxTileList) {
+        long_tiles.push_back(t);
+        long_off.push_back(long_off.back() + cnt[t]);
+      }
+  }
+  // set on every call, so that every device the caller renders on has them
+  if (rc == ARAP_OK && (cudaFuncSetAttribute(raster_tile_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)smem) != cudaSuccess ||
+                        cudaFuncSetAttribute(raster_sort_long_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)smem) != cudaSuccess)) {
+    (void)cudaGetLastError();
+    rc = ARAP_ECUDA;
+  }
+  char* long_scratch = nullptr;
   if (rc == ARAP_OK) {
     if (N > 0)
       raster_fill_kernel<<<(N + 127) / 128, 128, 0, st>>>(N, rect, dep, cam.gx, toff, tcur, keys);
-    const size_t smem = sizeof(unsigned long long) * kMaxTileList;
-    static bool attr_set = false;
-    if (!attr_set) {
-      cudaFuncSetAttribute(raster_tile_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-      attr_set = true;
+    if (!long_tiles.empty()) {
+      const int nl = (int)long_tiles.size();
+      const size_t b_ids = ((sizeof(int) * (size_t)nl) + 15) & ~size_t(15);
+      const size_t b_off = sizeof(long long) * ((size_t)nl + 1);
+      const size_t bytes = b_ids + b_off + sizeof(unsigned long long) * (size_t)long_off.back();
+      if (cudaMallocAsync(&long_scratch, bytes, st) != cudaSuccess) {
+        (void)cudaGetLastError();
+        long_scratch = nullptr;
+        rc = ARAP_ENOMEM;
+      } else {
+        int* d_ids = reinterpret_cast<int*>(long_scratch);
+        long long* d_off = reinterpret_cast<long long*>(long_scratch + b_ids);
+        unsigned long long* d_keys = reinterpret_cast<unsigned long long*>(long_scratch + b_ids + b_off);
+        if (cudaMemcpyAsync(d_ids, long_tiles.data(), sizeof(int) * (size_t)nl, cudaMemcpyHostToDevice, st) !=
+                cudaSuccess ||
+            cudaMemcpyAsync(d_off, long_off.data(), b_off, cudaMemcpyHostToDevice, st) != cudaSuccess)
+          rc = ARAP_ECUDA;
+        else
+          raster_sort_long_kernel<<<nl, 1024, smem, st>>>(nl, d_ids, toff, tcount, keys, d_keys, d_off);
+      }
     }
+  }
+  if (rc == ARAP_OK) {
     const float* bg = background_host;
     raster_tile_kernel<<<tiles, 256, smem, st>>>(cam, toff, tcount, keys, xy, co, col, bg[0], bg[1], bg[2],
-                                                image_out, final_t_out, n_contrib_out, status);
+                                                image_out, final_t_out, n_contrib_out);
     if (cudaPeekAtLastError() != cudaSuccess) rc = ARAP_ECUDA;
-    if (rc == ARAP_OK && cudaMemcpyAsync(&h_status, status, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess)
-      rc = ARAP_ECUDA;
     if (rc == ARAP_OK && cudaStreamSynchronize(st) != cudaSuccess) rc = ARAP_ECUDA;
-    if (rc == ARAP_OK && h_status) rc = ARAP_EUNSUPPORTED;
   }
+  if (long_scratch) cudaFreeAsync(long_scratch, st);
   if (keys) cudaFreeAsync(keys, st);
   cudaFreeAsync(scratch, st);
   return rc;

@@ -393,11 +393,14 @@ int arap_grid_center_order(const arap_grid* grid, int N, const float* pos, int32
  * scratch (cell [N], per-cell counters, offsets and flags [4 g^3 + 2], occupied
  * cells [g^3], scan sums) is carved from one static device array of
  * ARAP_CENTER_SCRATCH_BYTES, about 4 N + 20 g^3 bytes in all; larger requests
- * return ARAP_EUNSUPPORTED before any device work.  The first call on each
- * device resolves the array's address (cudaGetSymbolAddress) with that device
- * current; make that first call before any stream capture.  Calls that
- * overlap on the GPU (other streams, other host threads) share the array and
- * race: serialise them.  Synchronises. */
+ * return ARAP_EUNSUPPORTED before any device work.  A cell holding more than
+ * 16384 centres is merge-sorted with the rest of the array (4 bytes per
+ * centre of such cells), ARAP_EUNSUPPORTED when that does not fit.  Every
+ * call looks up the array's address (cudaGetSymbolAddress) on the current
+ * device; the first lookup on a device loads the module there, so make the
+ * first call before any stream capture.  Calls that overlap on the GPU (other
+ * streams, other host threads) share the array and race: serialise them.
+ * Synchronises. */
 int arap_grid_center_order_noalloc(const arap_grid* grid, int N, const float* pos, int32_t* order_out,
                                    arap_stream_t stream);
 
@@ -482,8 +485,9 @@ void arap_grid_destroy(arap_grid* grid);
  * row-major world->camera and world->clip matrices (camera looks along +z);
  * campos_host [3]; background_host [3].  image_out [3*height*width] planes;
  * final_t_out [height*width] (nullable): the transmittance left;
- * n_contrib_out (nullable): the Gaussians composited per pixel.  A 16x16
- * tile may list at most 16384 Gaussians (else ARAP_EUNSUPPORTED).
+ * n_contrib_out (nullable): the Gaussians composited per pixel.  A tile's
+ * list of up to 16384 Gaussians is sorted in shared memory, a longer one in
+ * global memory (chunk sorts and merges), with the same order.
  * Allocates stream-ordered scratch and synchronises. */
 int arap_render(int N, const float* pos, const float* shs, const float* opacity, const float* scale,
                 const float* rot, float scale_modifier, int sh_degree, const float* view_host,
