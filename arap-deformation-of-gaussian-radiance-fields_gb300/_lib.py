@@ -43,7 +43,8 @@ class SolveStats(C.Structure):
     _fields_ = [("status", C.c_int), ("gn_iterations", C.c_int), ("pcg_iterations", C.c_int),
                 ("halvings", C.c_int), ("initial_energy", C.c_double), ("final_energy", C.c_double),
                 ("n_free", C.c_int), ("n_static", C.c_int), ("n_rows", C.c_int),
-                ("n_coarse", C.c_int), ("phase_ms", C.c_double * 9)]
+                ("n_coarse", C.c_int), ("phase_ms", C.c_double * 9), ("resident", C.c_int),
+                ("coarse_fallbacks", C.c_int)]
 
     def as_dict(self):
         d = {f: getattr(self, f) for f, _ in self._fields_}

@@ -40,7 +40,7 @@ int status_read_clear(int* status_dev, cudaStream_t stream);
 
 // ------------------------------------------------------------ barrier ----
 // Grid-wide barrier for cooperative launches (all CTAs co-resident).  Every
-// wait is bounded: after spin_limit polls a waiting CTA records ARAP_ETIMEOUT,
+// wait is bounded: after spin_limit polls a waiting CTA records the timeout,
 // marks the barrier failed and returns false; callers then leave the kernel.
 //
 // Counter barrier with a reduction.  Arrivals go to one monotonic counter
@@ -53,11 +53,16 @@ int status_read_clear(int* status_dev, cudaStream_t stream);
 // once and adds them in CTA order, so every CTA gets the same bits.  Two
 // partial buffers suffice: a CTA can only reach barrier e+2 once every CTA has
 // arrived at e+1, i.e. has finished reading barrier e.
+// count and failed are zeroed before each launch (the first 8 bytes);
+// spin_limit is written once by the barrier's owner and read by every wait,
+// so the kernel holds no register for it.  A wait that runs out sets failed,
+// which the owner reports as ARAP_ETIMEOUT.  status is the owner's device
+// status word (raise_status), kept across launches until the host reads it.
 struct GridBarrier {
   unsigned int count;
-  unsigned int pad0;
   int failed;
-  int pad1;
+  unsigned int spin_limit;  // polls of one wait before it gives up (checked every 64)
+  int status;
 };
 
 constexpr long long kSpinLimit = 1ll << 23;  // default polls of a barrier wait
@@ -71,6 +76,11 @@ __device__ __forceinline__ unsigned int ld_acquire_u32(const unsigned int* p) {
 }
 __device__ __forceinline__ void red_release_add_u32(unsigned int* p, unsigned int v) {
   asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ unsigned int ld_relaxed_u32(const unsigned int* p) {
+  unsigned int v;
+  asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
 }
 __device__ __forceinline__ int ld_relaxed_i32(const int* p) {
   int v;
@@ -140,8 +150,6 @@ struct GridSync {
   unsigned int epoch;
   unsigned int nb;
   unsigned int bid;
-  int* status;           // the handle's device status word
-  long long spin_limit;  // polls of one wait before ARAP_ETIMEOUT
 
   // One thread per CTA: arrive at barrier e (release) and wait (acquire) for
   // every CTA; bounded, false on failure.
@@ -151,11 +159,14 @@ struct GridSync {
     long long it = 0;
     while ((int)(ld_acquire_u32(&bar->count) - target) < 0) {
       ++it;
-      if ((it & 63) == 0 && ld_relaxed_i32(&bar->failed)) return false;
-      if (it > spin_limit) {
-        atomicExch(&bar->failed, 1);
-        raise_status(status, ARAP_ETIMEOUT);
-        return false;
+      // every 64 polls: a peer's failure, then this wait's own limit (read
+      // here, so that no register holds it through the caller's code)
+      if ((it & 63) == 0) {
+        if (ld_relaxed_i32(&bar->failed)) return false;
+        if (it >= (long long)ld_relaxed_u32(&bar->spin_limit)) {
+          atomicExch(&bar->failed, 1);
+          return false;
+        }
       }
       if (it > 1024) __nanosleep(32);
     }

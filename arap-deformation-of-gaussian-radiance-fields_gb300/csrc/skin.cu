@@ -52,6 +52,37 @@ __device__ __forceinline__ float ed_finish(float p, float wsum, float acc) {
   return p + fmaf(wsum - 1.0f, p, acc);
 }
 
+// A node's blend term in tile-local affine form for the Gaussian skinning:
+// (R - I)(p - g) + t = A (p - o) + b_o with A = R - I and b_o = t - A (g - o),
+// o a point of the tile (its first Gaussian's first endpoint), so that p - o
+// and g - o stay small and no large terms cancel.  12 floats:
+// a = (A00 A01 A02 A10), b = (A11 A12 A20 A21), c = (A22, b_o).
+struct NodeAf {
+  float4 a, b, c;
+};
+
+__device__ __forceinline__ NodeAf node_affine(const NodeXf& x, float ox, float oy, float oz) {
+  const float gx = x.c.y - ox, gy = x.c.z - oy, gz = x.c.w - oz;
+  NodeAf r;
+  r.a = x.a;
+  r.b = x.b;
+  r.c = make_float4(x.c.x, x.d.x - fmaf(x.a.x, gx, fmaf(x.a.y, gy, x.a.z * gz)),
+                    x.d.y - fmaf(x.a.w, gx, fmaf(x.b.x, gy, x.b.y * gz)),
+                    x.d.z - fmaf(x.b.z, gx, fmaf(x.b.w, gy, x.c.x * gz)));
+  return r;
+}
+
+// w * (A d + b_o), d = p - o, accumulated into (ox, oy, oz).
+__device__ __forceinline__ void ed_term_af(const NodeAf& x, float w, float dx, float dy, float dz, float& ox,
+                                           float& oy, float& oz) {
+  const float mx = fmaf(x.a.x, dx, fmaf(x.a.y, dy, fmaf(x.a.z, dz, x.c.y)));
+  const float my = fmaf(x.a.w, dx, fmaf(x.b.x, dy, fmaf(x.b.y, dz, x.c.z)));
+  const float mz = fmaf(x.b.z, dx, fmaf(x.b.w, dy, fmaf(x.c.x, dz, x.c.w)));
+  ox = fmaf(w, mx, ox);
+  oy = fmaf(w, my, oy);
+  oz = fmaf(w, mz, oz);
+}
+
 __global__ void node_table_kernel(int n, const float* __restrict__ rot,
                                   const float* __restrict__ trans,
                                   const float* __restrict__ pos, float* __restrict__ table) {
@@ -118,7 +149,7 @@ constexpr size_t skin_smem_bytes() { return sizeof(float) * (size_t)kSkinTile * 
 // per Gaussian endpoint-major ([6][K], contiguous).  A frame then copies the
 // tile's node records into shared memory once and gathers from there.
 constexpr int kPlanNodes = 256;
-constexpr int kPlanRec = 20;  // floats per staged node record (16 used; 80-byte stride spreads banks)
+constexpr int kPlanRec = 12;  // floats per staged node record (NodeAf; the 48-byte stride spreads banks)
 struct SkinPlanDev {
   const int32_t* tile_count;  // [tiles] distinct nodes of the tile (> kPlanNodes: no local list)
   const int32_t* tile_nodes;  // [tiles][kPlanNodes]
@@ -146,16 +177,25 @@ __global__ void __launch_bounds__(kSkinThreads, 4)
   const int cnt = min(kSkinTile, N - tile0);
   const int i = tile0 + t;
   const bool active = t < cnt;
-  // ---- planned: the tile's node records into shared memory (first copy group)
+  // the tile's origin: its first Gaussian's first endpoint before this frame
+  // (read by every thread before any thread writes its endpoints)
+  const float o_x = __ldg(ends + tile0), o_y = __ldg(ends + (size_t)N + tile0),
+              o_z = __ldg(ends + 2 * (size_t)N + tile0);
+  // ---- planned: the tile's node records into shared memory, in tile-local
+  // affine form (one thread per node)
   int n_local = kPlanNodes + 1;
   if (PLANNED) {
     n_local = __ldg(plan.tile_count + blockIdx.x);
     if (n_local <= kPlanNodes) {
       const int32_t* list = plan.tile_nodes + (size_t)blockIdx.x * kPlanNodes;
-      for (int e = t; e < 4 * n_local; e += kSkinThreads)
-        cp_async16(s_nodes + (e >> 2) * kPlanRec + (e & 3) * 4, table + 16 * (size_t)__ldg(list + (e >> 2)) + (e & 3) * 4);
+      for (int u = t; u < n_local; u += kSkinThreads) {
+        const NodeAf r = node_affine(load_node(table, __ldg(list + u)), o_x, o_y, o_z);
+        float4* d4 = reinterpret_cast<float4*>(s_nodes + u * kPlanRec);
+        d4[0] = r.a;
+        d4[1] = r.b;
+        d4[2] = r.c;
+      }
     }
-    asm volatile("cp.async.commit_group;" ::: "memory");
   }
   const bool local = PLANNED && n_local <= kPlanNodes;
   // ---- stage the SH records and previous quaternions of the tile
@@ -166,11 +206,9 @@ __global__ void __launch_bounds__(kSkinThreads, 4)
       cp_async16(s_sh + (q / 12) * kShStride + (q % 12) * 4, src + 4 * (size_t)q);
   }
   asm volatile("cp.async.commit_group;" ::: "memory");
-  if (PLANNED) {
-    // the node records (first group) are needed now, the SH records later
-    asm volatile("cp.async.wait_group 1;" ::: "memory");
-    __syncthreads();
-  }
+  // the node records are needed now (and every thread has read the origin);
+  // the SH records later
+  __syncthreads();
 
   float e[18];
   // loads the refit needs later, issued now so that they overlap the blend
@@ -232,21 +270,21 @@ __global__ void __launch_bounds__(kSkinThreads, 4)
           wv[j] = __ldcs(ew + (size_t)(j * 6 + ep) * N + i);
         }
       }
+      const float dx = e[3 * ep] - o_x, dy = e[3 * ep + 1] - o_y, dz = e[3 * ep + 2] - o_z;
 #pragma unroll
       for (int j = 0; j < K; ++j) {
-        NodeXf x;
+        NodeAf x;
         if (local) {
           const float4* r4 = reinterpret_cast<const float4*>(s_nodes + id[j] * kPlanRec);
           x.a = r4[0];
           x.b = r4[1];
           x.c = r4[2];
-          x.d = r4[3];
         } else {
-          x = load_node(table, id[j]);
+          x = node_affine(load_node(table, id[j]), o_x, o_y, o_z);
         }
         const float w = wv[j];
         ws += w;
-        ed_term(x, w, e[3 * ep], e[3 * ep + 1], e[3 * ep + 2], ox, oy, oz);
+        ed_term_af(x, w, dx, dy, dz, ox, oy, oz);
       }
       e[3 * ep] = ed_finish(e[3 * ep], ws, ox);
       e[3 * ep + 1] = ed_finish(e[3 * ep + 1], ws, oy);

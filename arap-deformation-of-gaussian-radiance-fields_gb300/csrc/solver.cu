@@ -465,7 +465,6 @@ extern "C" int arap_solver_create(arap_solver** out, int n, int k, const int32_t
     P.partials = cv.take<double>((size_t)2 * kReduceSlots * grid);
     P.stats = cv.take<double>(kStatSlots);
     P.bar = cv.take<GridBarrier>(1);
-    P.status = cv.take<int>(1);
   };
   Carver sizing{nullptr};
   SolveParams dummy{};
@@ -513,14 +512,15 @@ extern "C" int arap_solver_create(arap_solver** out, int n, int k, const int32_t
     e = e ? e : up(P.gca_off, gca_off.data(), gca_off.size() * 4);
     e = e ? e : up(P.gca, gca.data(), gca.size() * 4);
   }
-  e = e ? e : cudaMemsetAsync(P.status, 0, sizeof(int), st);
+  // the barrier record: count, failed and status zeroed, the configured spin limit
+  const GridBarrier bar0{0u, 0, (unsigned int)(cfg.spin_limit > 0 ? cfg.spin_limit : kSpinLimit), 0};
+  e = e ? e : cudaMemcpyAsync(P.bar, &bar0, sizeof(bar0), cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   if (e != cudaSuccess) {
     cudaFree(s->block);
     delete s;
     return ARAP_ECUDA;
   }
-  P.spin_limit = cfg.spin_limit > 0 ? (long long)cfg.spin_limit : kSpinLimit;
   P.n = n;
   P.k = k;
   P.F = F;
@@ -556,6 +556,21 @@ extern "C" int arap_solver_create(arap_solver** out, int n, int k, const int32_t
   return ARAP_OK;
 }
 
+// Read and clear the status word and the timeout flag of a solve's barrier
+// record (synchronises): the status word's code, else ARAP_ETIMEOUT when a
+// barrier wait gave up.
+static int read_solver_status(GridBarrier* bar, cudaStream_t st) {
+  int failed = 0;
+  if (cudaMemcpyAsync(&failed, &bar->failed, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+      cudaMemsetAsync(&bar->failed, 0, sizeof(int), st) != cudaSuccess) {
+    (void)cudaGetLastError();
+    return ARAP_ECUDA;
+  }
+  const int code = status_read_clear(&bar->status, st);  // synchronises
+  if (code != ARAP_OK) return code;
+  return failed ? ARAP_ETIMEOUT : ARAP_OK;
+}
+
 // Host stats of one solve from its device slots; returns the call's status
 // (ARAP_NOT_CONVERGED is reported in the stats only).
 static int fill_stats(const arap_solver* s, const double* st8, int dev_status, arap_solve_stats* stats_host) {
@@ -570,6 +585,8 @@ static int fill_stats(const arap_solver* s, const double* st8, int dev_status, a
   stats_host->n_rows = s->n_rows;
   for (int q = 0; q < 9; ++q) stats_host->phase_ms[q] = st8[ST_T_PREP + q] * 1e-6;
   stats_host->n_coarse = s->P.NC;
+  stats_host->resident = s->P.resident ? 1 : 0;
+  stats_host->coarse_fallbacks = (int)st8[ST_CFALL];
   int status = dev_status;
   if (status == ARAP_OK && s->cfg.early_exit && st8[ST_CONV] == 0.0 && s->cfg.max_iters > 0)
     status = ARAP_NOT_CONVERGED;
@@ -578,7 +595,8 @@ static int fill_stats(const arap_solver* s, const double* st8, int dev_status, a
 }
 
 static int launch_solver(arap_solver* s, cudaStream_t st) {
-  if (cudaMemsetAsync(s->P.bar, 0, sizeof(GridBarrier), st) != cudaSuccess) return ARAP_ECUDA;
+  // count and failed (the first 8 bytes); the spin limit stays
+  if (cudaMemsetAsync(s->P.bar, 0, 2 * sizeof(int), st) != cudaSuccess) return ARAP_ECUDA;
   void* args[] = {&s->P};
   cudaError_t e;
   if (s->cfg.precision == ARAP_PRECISION_MIXED)
@@ -610,7 +628,7 @@ extern "C" int arap_solver_solve(arap_solver* s, const float* node_pos, const fl
   if (!stats_host) return ARAP_OK;
   double st8[kStatSlots];
   ARAP_CUDA_TRY(cudaMemcpyAsync(st8, s->P.stats, sizeof(st8), cudaMemcpyDeviceToHost, st));
-  const int dev_status = status_read_clear(s->P.status, st);  // synchronises
+  const int dev_status = read_solver_status(s->P.bar, st);  // synchronises
   return fill_stats(s, st8, dev_status, stats_host);
 }
 
@@ -634,7 +652,7 @@ extern "C" int arap_solver_energy_grad(arap_solver* s, const float* node_pos, co
   if (energy_host) {
     double st8[kStatSlots];
     ARAP_CUDA_TRY(cudaMemcpyAsync(st8, used.stats, sizeof(st8), cudaMemcpyDeviceToHost, st));
-    const int dev_status = status_read_clear(used.status, st);
+    const int dev_status = read_solver_status(used.bar, st);
     *energy_host = st8[ST_E];
     return dev_status;
   }
@@ -643,7 +661,7 @@ extern "C" int arap_solver_energy_grad(arap_solver* s, const float* node_pos, co
 
 extern "C" int arap_solver_status(arap_solver* s, arap_stream_t stream) {
   if (!s) return ARAP_EBADINPUT;
-  return status_read_clear(s->P.status, (cudaStream_t)stream);
+  return read_solver_status(s->P.bar, (cudaStream_t)stream);
 }
 
 extern "C" int arap_solver_free_count(const arap_solver* s) { return s ? s->F : -1; }
@@ -819,7 +837,7 @@ int batch_grid() {
 
 extern "C" int arap_solver_batch_create(arap_solver_batch** out, arap_solver* const* solvers, int count,
                                         float balance_exponent, arap_stream_t stream) {
-  (void)stream;
+  cudaStream_t st = (cudaStream_t)stream;
   if (!out || !solvers || count < 1) return ARAP_EBADINPUT;
   *out = nullptr;
   for (int i = 0; i < count; ++i)
@@ -858,6 +876,20 @@ extern "C" int arap_solver_batch_create(arap_solver_batch** out, arap_solver* co
   }
   Carver cv{static_cast<char*>(b->block)};
   carve(cv);
+  {
+    std::vector<GridBarrier> bars(count);
+    for (int i = 0; i < count; ++i) {
+      const int lim = solvers[i]->cfg.spin_limit;
+      bars[i] = GridBarrier{0u, 0, (unsigned int)(lim > 0 ? lim : kSpinLimit), 0};
+    }
+    if (cudaMemcpyAsync(b->d_bars, bars.data(), sizeof(GridBarrier) * count, cudaMemcpyHostToDevice, st) !=
+            cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess) {
+      (void)cudaGetLastError();
+      arap_solver_batch_destroy(b);
+      return ARAP_ECUDA;
+    }
+  }
   if (upload_ctas(b) != ARAP_OK) {
     arap_solver_batch_destroy(b);
     return ARAP_ECUDA;
@@ -902,7 +934,8 @@ extern "C" int arap_solver_batch_solve(arap_solver_batch* b, const float* const*
     ARAP_CUDA_TRY(cudaEventRecord(b->staged, st));
     b->staged_valid = true;
   }
-  ARAP_CUDA_TRY(cudaMemsetAsync(b->d_bars, 0, sizeof(GridBarrier) * count, st));
+  // count and failed of every instance's barrier (the first 8 bytes of each)
+  ARAP_CUDA_TRY(cudaMemset2DAsync(b->d_bars, sizeof(GridBarrier), 0, 2 * sizeof(int), count, st));
   const void* fn = b->precision == ARAP_PRECISION_MIXED ? (const void*)gn_solve_batch_kernel<double>
                                                         : (const void*)gn_solve_batch_kernel<float>;
   for (size_t w = 0; w + 1 < b->wave_first.size(); ++w) {
@@ -924,7 +957,7 @@ extern "C" int arap_solver_batch_solve(arap_solver_batch* b, const float* const*
                                   sizeof(double) * kStatSlots, cudaMemcpyDeviceToHost, st));
   int status = ARAP_OK;
   for (int i = 0; i < count; ++i) {
-    const int dev_status = status_read_clear(b->solvers[i]->P.status, st);  // synchronises
+    const int dev_status = read_solver_status(b->d_bars + i, st);  // synchronises
     const int si = fill_stats(b->solvers[i], st8.data() + (size_t)kStatSlots * i, dev_status, stats_host + i);
     if (status == ARAP_OK) status = si;
   }
@@ -976,8 +1009,8 @@ extern "C" int arap_solver_batch_autotune(arap_solver_batch* b, const float* con
   if (rc == ARAP_OK) rc = upload_ctas(b);
   if (best_exponent) *best_exponent = best;
   if (rc != ARAP_OK) return rc;
-  for (arap_solver* si : b->solvers)
-    if (const int ds = status_read_clear(si->P.status, st)) return ds;
+  for (size_t i = 0; i < b->solvers.size(); ++i)
+    if (const int ds = read_solver_status(b->d_bars + i, st)) return ds;
   return ARAP_OK;
 }
 

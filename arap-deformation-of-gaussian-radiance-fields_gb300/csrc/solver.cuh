@@ -57,8 +57,6 @@ struct SolveParams {
   float* dinv;               // [F*144] inverse of the 12x12 diagonal block of J^T J
   double* partials;          // [2 * kReduceSlots * gridDim] barrier partial sums
   GridBarrier* bar;
-  int* status;               // the solver's device status word (ARAP_* code, first wins)
-  long long spin_limit;      // polls of one grid-barrier wait before ARAP_ETIMEOUT
   double* stats;             // [8] device-side stats (see solver.cu)
   float* rot_out;            // [n*9]
   float* trans_out;          // [n*3]

@@ -1013,7 +1013,7 @@ __device__ void coarse_rows_group(const SolveParams& P, int g) {
         if (ids[q] == b) f = q;
       if (f < 0) {
         if (na == kMaxAgg) {
-          raise_status(P.status, ARAP_EUNSUPPORTED);
+          raise_status(&P.bar->status, ARAP_EUNSUPPORTED);
           continue;
         }
         f = na++;
@@ -1689,7 +1689,7 @@ __device__ void stage_build(const SolveParams& P, int bid, int nbk) {
     // the two halves of a warp are staged together: an even count unless all fit
     if (n < cnt) {
       n &= ~1;
-      if (res && lane == 0) raise_status(P.status, ARAP_EUNSUPPORTED);
+      if (res && lane == 0) raise_status(&P.bar->status, ARAP_EUNSUPPORTED);
     }
     if (lane == 0) {
       StageLayout L;

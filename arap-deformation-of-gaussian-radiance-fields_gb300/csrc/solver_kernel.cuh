@@ -16,7 +16,7 @@ namespace arap {
 enum {
   ST_ITERS = 0, ST_PCG = 1, ST_HALV = 2, ST_E0 = 3, ST_E = 4, ST_CONV = 5, ST_NONFINITE = 6,
   ST_T_PREP = 8, ST_T_GRAD = 9, ST_T_COARSE = 10, ST_T_PCG = 11, ST_T_LS = 12, ST_T_CINV = 13,
-  ST_T_W_SPMV = 14, ST_T_W_UPD = 15, ST_T_W_CSOLVE = 16
+  ST_T_W_SPMV = 14, ST_T_W_UPD = 15, ST_T_W_CSOLVE = 16, ST_CFALL = 17
 };
 constexpr int kStatSlots = 24;
 
@@ -207,7 +207,7 @@ __device__ __forceinline__ void solve_body(const SolveParams& P, int bid, int nb
   // node order position p belongs to CTA p % nbk: the costliest nodes (the
   // order is by cost, descending) are spread over all SMs
   const int wib = threadIdx.x >> 5;
-  GridSync gs{P.bar, P.partials, 0u, (unsigned int)nbk, (unsigned int)bid, P.status, P.spin_limit};
+  GridSync gs{P.bar, P.partials, 0u, (unsigned int)nbk, (unsigned int)bid};
   // phase timers, thread 0's only, kept in shared memory rather than registers
   // that would stay live through the whole kernel.  acc: prep, grad, coarse,
   // pcg, line search, inversion (ns).  work: PCG work of this CTA per phase
@@ -313,7 +313,7 @@ __device__ __forceinline__ void solve_body(const SolveParams& P, int bid, int nb
     }
   }
   if (gt == 0)
-    for (int q = ST_T_W_SPMV; q <= ST_T_W_CSOLVE; ++q) P.stats[q] = 0.0;
+    for (int q = ST_T_W_SPMV; q <= ST_CFALL; ++q) P.stats[q] = 0.0;
   if (!gs.sync()) return;
   stage_build(P, bid, nbk);
   // diagonal-block share of every constraint item (fixed for this solve): the
@@ -461,7 +461,9 @@ __device__ __forceinline__ void solve_body(const SolveParams& P, int bid, int nb
       if (threadIdx.x == 0) s_clk.inv0 = global_ns();
       if (!coarse_invert(P, gs, &coarse_ok, s_scratch)) return;
       if (threadIdx.x == 0) s_clk.acc[5] += (double)(global_ns() - s_clk.inv0);
-      if (!coarse_ok && gt == 0) raise_status(P.status, ARAP_ENONFINITE);
+      // a pivot of the coarse inversion that is not positive: this
+      // iteration's PCG runs with block-Jacobi alone; counted in the stats
+      if (!coarse_ok && gt == 0) P.stats[ST_CFALL] += 1.0;
       if (resident) {
         // this CTA's rows of the coarse inverse (rows bid, bid + nbk, ...)
         const int NC = P.NC, n4 = NC / 4;
@@ -796,7 +798,7 @@ __device__ __forceinline__ void solve_body(const SolveParams& P, int bid, int nb
       to[0] = to[1] = to[2] = 0.f;
     }
   }
-  if (nonfinite) raise_status(P.status, ARAP_ENONFINITE);
+  if (nonfinite) raise_status(&P.bar->status, ARAP_ENONFINITE);
   if (gt == 0) {
     P.stats[ST_ITERS] = iters;
     P.stats[ST_PCG] = pcg_total;

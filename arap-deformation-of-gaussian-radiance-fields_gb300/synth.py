@@ -15,6 +15,9 @@ workloads instead:
 * ``stress3m``  -- 3M flat Gaussians in [0,4]^3 (one log-scale axis N(-9,0.3)),
   128^3 grid, ~30k nodes, k=12, pinned / excluded / active(x1.5 scale),
   30 iterations.
+* ``stress200k`` -- the stress field at 200k Gaussians and ~8000 nodes
+  (64^3 grid, 8 iterations): more free nodes than the solver keeps resident
+  in shared memory, so it exercises the non-resident solve.
 
 Every Gaussian attribute is activated the way the viewer stores it after
 loading (GaussianView.cpp:140-151): scales are exp(log-scale), opacities are
@@ -201,25 +204,39 @@ def _stress(n, seed, n_nodes=30000, grid_num=128, k=12, iters=30):
 @dataclasses.dataclass
 class Instance:
     """One deformation instance of a batch: nodes, graph degree, control
-    regions and operation (the Gaussians are not needed by the solve)."""
+    regions and operation; with ``gaussians`` also its Gaussian field (the
+    nodes sit on Gaussians, ``node_vertex``)."""
     node_pos: np.ndarray     # float32 [n,3]
     k: int
     blocks: list
     block_type: np.ndarray
     op: tuple
     iters: int
+    pos: np.ndarray = None       # float32 [N,3]
+    rot: np.ndarray = None       # float32 [N,4] (w,x,y,z)
+    scale: np.ndarray = None     # float32 [N,3]
+    shs: np.ndarray = None       # float32 [N,48]
+    node_vertex: np.ndarray = None
 
 
-def batch_instances(count: int = 64, seed: int = 0, nodes=(300, 8000), k: int = 8, iters: int = 20):
+def batch_instances(count: int = 64, seed: int = 0, nodes=(300, 8000), k: int = 8, iters: int = 20,
+                    gaussians=None):
     """``count`` instances with node counts log-uniform in ``nodes``: random
     unions of bars and balls under a random scale and rotation, pinned below
     10% and active above 90% of a random axis, and an operation drawn from
-    bend (translate), twist (90 degrees about the axis) and scale x U[0.5, 2]."""
+    bend (translate), twist (90 degrees about the axis) and scale x U[0.5, 2].
+    With ``gaussians = (lo, hi)`` every instance also gets a Gaussian field of
+    a count log-uniform in [lo, hi] over the same shape (the bend workload's
+    distributions: log-scale N(-5, 0.5) shifted by the instance's scale,
+    uniform unit quaternions, SH N(0, 0.2)), and its nodes are picked among
+    those Gaussians."""
     rng = np.random.default_rng(seed)
     out = []
     for _ in range(count):
         n_nodes = int(round(math.exp(rng.uniform(math.log(nodes[0]), math.log(nodes[1])))))
         npts = 12 * n_nodes
+        if gaussians is not None:
+            npts = max(npts, int(round(math.exp(rng.uniform(math.log(gaussians[0]), math.log(gaussians[1]))))))
         parts = []
         for _ in range(int(rng.integers(1, 4))):
             if rng.random() < 0.5:
@@ -233,8 +250,10 @@ def batch_instances(count: int = 64, seed: int = 0, nodes=(300, 8000), k: int = 
         R = np.array([[1 - 2 * (y * y + z * z), 2 * (x * y - w * z), 2 * (x * z + w * y)],
                       [2 * (x * y + w * z), 1 - 2 * (x * x + z * z), 2 * (y * z - w * x)],
                       [2 * (x * z - w * y), 2 * (y * z + w * x), 1 - 2 * (x * x + y * y)]])
-        pts = (pts @ R.T) * rng.uniform(0.5, 2.0)
-        node_pos = pts[voxel_nodes(pts, n_nodes)].astype(np.float32)
+        size = rng.uniform(0.5, 2.0)
+        pts = ((pts @ R.T) * size).astype(np.float32)
+        node_vertex = voxel_nodes(pts, n_nodes)
+        node_pos = pts[node_vertex].astype(np.float32)
         axis = int(rng.integers(0, 3))
         c = node_pos[:, axis]
         lo, hi = np.quantile(c, 0.1), np.quantile(c, 0.9)
@@ -251,8 +270,16 @@ def batch_instances(count: int = 64, seed: int = 0, nodes=(300, 8000), k: int = 
             op = ("twist", tuple(float(v) for v in a), math.pi / 2)
         else:
             op = ("scale", float(rng.uniform(0.5, 2.0)))
-        out.append(Instance(node_pos=node_pos, k=k, blocks=blocks, block_type=np.array([0, 1], np.int32),
-                            op=op, iters=iters))
+        inst = Instance(node_pos=node_pos, k=k, blocks=blocks, block_type=np.array([0, 1], np.int32), op=op,
+                        iters=iters)
+        if gaussians is not None:
+            n = pts.shape[0]
+            inst.pos = pts
+            inst.rot = _unit_quats(rng, n)
+            inst.scale = np.exp(-5.0 + math.log(size) + 0.5 * rng.standard_normal((n, 3))).astype(np.float32)
+            inst.shs = (0.2 * rng.standard_normal((n, 48))).astype(np.float32)
+            inst.node_vertex = node_vertex.astype(np.int32)
+        out.append(inst)
     return out
 
 
@@ -264,6 +291,8 @@ SCENES = {
     "bend4k": lambda seed=0: _bend(4_000, seed, n_nodes=120, grid_num=16, iters=6),
     "twist20k": lambda seed=0: _twist(20_000, seed, n_nodes=400, grid_num=32, iters=8),
     "stress40k": lambda seed=0: _stress(40_000, seed, n_nodes=600, grid_num=32, iters=8),
+    # more free nodes than the solver keeps resident in shared memory
+    "stress200k": lambda seed=0: _stress(200_000, seed, n_nodes=8000, grid_num=64, iters=8),
 }
 
 

@@ -6,7 +6,8 @@ node transforms (early exit off), skinning of the grid samples (position +
 slerp-blended SH rotation of the 48-float features), skinning of all Gaussians
 (6-endpoint ED blend, refit, SH rotation, covariance), node update and target
 re-anchoring.  Every step starts from the same rest state (restored by device
-copies inside the step) so each step does identical work.
+copies before the step's timed region, then L2 is flushed) so each step does
+identical work.
 
 --impl ours       the CUDA library (default)
 --impl reference  the reference's CPU path on the host cores, restated in
@@ -121,6 +122,15 @@ def reduce_max(value, ws, device="cuda"):
 
 
 # ------------------------------------------------------------ workload ----
+
+def op_text(op):
+    """The control operation of a scene in words."""
+    if op[0] == "twist":
+        return "twist %.0f deg about (%g, %g, %g)" % ((op[2] * 180.0 / 3.141592653589793,) + tuple(op[1]))
+    if op[0] == "scale":
+        return "scale x%g" % op[1]
+    return "translate by (%g, %g, %g)" % tuple(op[1])
+
 
 def solve_config(dev, sc, form, coarse_nodes):
     if form == "chosen":
@@ -254,6 +264,155 @@ def batch_leg(count):
     return out
 
 
+def batch_frame_leg(count):
+    """Batched frames with Gaussians: ``count`` instances (node counts
+    log-uniform in [300, 8000], Gaussian counts log-uniform in [20k, 500k],
+    random shapes and operations, 20 Gauss-Newton iterations, chosen form).
+    One batched frame = the batched solve (cooperative launches in waves,
+    CTA split by the autotuner) writing every instance's transforms into one
+    node table, then ONE skinning launch over all instances' Gaussians (their
+    endpoint kNN indices offset into the joint table, a skinning plan over the
+    concatenation).  Timed directly, as a replayed CUDA graph of the same
+    frame, and against the instances' frames run one after another."""
+    import numpy as np
+    import torch
+    dev = importlib.import_module(PKG + ".deform")
+    synth = importlib.import_module(PKG + ".synth")
+    inst = synth.batch_instances(count, gaussians=(20_000, 500_000))
+    solvers, pos, aims, seq = [], [], [], []
+    node_base, gauss_base = [0], [0]
+    ends_all, idx_all, w_all, s0_all, q_all, sh_all = [], [], [], [], [], []
+    for it in inst:
+        p = torch.as_tensor(it.node_pos).cuda()
+        nb = dev.build_graph(p, it.k)
+        aidx, aw = dev.compute_weights(p, p, it.k)
+        act = torch.as_tensor(it.blocks[1].astype(np.int32)).cuda()
+        a0 = p.clone()
+        if it.op[0] == "translate":
+            dev.aims_translate(a0, act, it.op[1])
+        elif it.op[0] == "twist":
+            dev.aims_twist(a0, p, act, it.op[1], it.op[2])
+        else:
+            dev.aims_scale(a0, p, act, it.op[1])
+        solvers.append(dev.Solver(nb, aidx, aw, it.blocks, it.block_type, max_iters=it.iters, early_exit=0,
+                                  precision=1, coarse_nodes=64))
+        pos.append(p)
+        aims.append(a0)
+        gp = torch.as_tensor(it.pos).cuda()
+        ends, exyz = dev.end_points(gp, torch.as_tensor(it.rot).cuda(), torch.as_tensor(it.scale).cuda())
+        eidx, ew = dev.compute_weights(exyz, p, it.k)
+        del exyz
+        seq.append((ends, eidx, ew, dev.SkinPlan(eidx, ew)))
+        ends_all.append(ends)
+        # planes [k][6][N_i]: joined along the Gaussians of each (k, endpoint) plane
+        n_i = it.pos.shape[0]
+        idx_all.append((eidx + node_base[-1]).view(it.k, 6, n_i))
+        w_all.append(ew.view(it.k, 6, n_i))
+        s0_all.append(torch.as_tensor(it.scale).cuda())
+        q_all.append(torch.as_tensor(it.rot).cuda())
+        sh_all.append(torch.as_tensor(it.shs).cuda())
+        node_base.append(node_base[-1] + p.shape[0])
+        gauss_base.append(gauss_base[-1] + it.pos.shape[0])
+    n_tot, N_tot = node_base[-1], gauss_base[-1]
+    # joint buffers: per-instance solve outputs are views of one table source
+    rot_all = torch.empty((n_tot, 9), device="cuda")
+    tr_all = torch.empty((n_tot, 3), device="cuda")
+    node_all = torch.cat(pos).contiguous()
+    rot_v = [rot_all[node_base[i]:node_base[i + 1]] for i in range(count)]
+    tr_v = [tr_all[node_base[i]:node_base[i + 1]] for i in range(count)]
+    ends0 = torch.cat(ends_all, 1).contiguous()     # [18][N_tot]
+    k = inst[0].k
+    eidx_all = torch.cat(idx_all, 2).reshape(k, 6 * N_tot).contiguous()
+    ew_all = torch.cat(w_all, 2).reshape(k, 6 * N_tot).contiguous()
+    s0 = torch.cat(s0_all).contiguous()
+    q0 = torch.cat(q_all).contiguous()
+    sh0 = torch.cat(sh_all).contiguous()
+    plan = dev.SkinPlan(eidx_all, ew_all)
+    batch = dev.SolverBatch(solvers)
+    best = batch.autotune(pos, aims)
+    ends = ends0.clone()
+    gpos = torch.empty((N_tot, 3), device="cuda")
+    q = q0.clone()
+    gsc = torch.empty((N_tot, 3), device="cuda")
+    sh = sh0.clone()
+    cov = torch.empty((N_tot, 6), device="cuda")
+
+    def restore():
+        ends.copy_(ends0)
+        q.copy_(q0)
+        sh.copy_(sh0)
+
+    def frame():
+        batch.solve(pos, aims, rot_v, tr_v, stats=False)
+        table = dev.node_table(rot_all, tr_all, node_all)
+        dev.skin_gaussians_planned(plan, ends, table, s0, gpos, q, gsc, sh, cov, precision=1)
+
+    def frames_one_by_one():
+        for i, (s_, (e_, ei_, ew_, pl_)) in enumerate(zip(solvers, seq)):
+            a_, b_ = gauss_base[i], gauss_base[i + 1]
+            r_, t_, _ = s_.solve(pos[i], aims[i], rot_v[i], tr_v[i], stats=False)
+            tab = dev.node_table(r_, t_, pos[i])
+            dev.skin_gaussians_planned(pl_, e_, tab, s0[a_:b_], gpos[a_:b_], q[a_:b_], gsc[a_:b_], sh[a_:b_],
+                                       cov[a_:b_], precision=1)
+
+    def timed(fn, reps):
+        out = []
+        for _ in range(reps):
+            restore()
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            fn()
+            e1.record()
+            torch.cuda.synchronize()
+            out.append(e0.elapsed_time(e1))
+        return float(np.median(out))
+
+    frame()
+    ms_b = timed(frame, 3)
+    frames_one_by_one()
+    ms_s = timed(frames_one_by_one, 2)
+    # the batched frame captured once and replayed
+    restore()
+    torch.cuda.synchronize()
+    s = torch.cuda.Stream()
+    s.wait_stream(torch.cuda.current_stream())
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.stream(s):
+        frame()   # warm the stream's allocations outside the capture
+        torch.cuda.synchronize()
+        with torch.cuda.graph(graph, stream=s):
+            frame()
+    torch.cuda.synchronize()
+    ms_g = timed(graph.replay, 3)
+    _, _, st_b = batch.solve(pos, aims, rot_v, tr_v, stats=True)
+    out = {"instances": count, "gaussians_total": int(N_tot), "nodes_total": int(n_tot),
+           "gaussians_range": [int(min(np.diff(gauss_base))), int(max(np.diff(gauss_base)))],
+           "nodes_range": [int(min(np.diff(node_base))), int(max(np.diff(node_base)))],
+           "gn_iterations": inst[0].iters, "form": "chosen (mixed, coarse 64)",
+           "ms_batched_frame": round(ms_b, 3), "ms_batched_frame_graph_replay": round(ms_g, 3),
+           "ms_frames_one_by_one": round(ms_s, 3),
+           "batched_speedup_over_one_by_one": round(ms_s / ms_b, 3),
+           "launches_per_batched_frame": "one cooperative solve launch per wave, one node table, one skinning",
+           "balance_exponent": best, "status": max(x["status"] for x in st_b)}
+    batch.close()
+    plan.close()
+    for s_ in solvers:
+        s_.close()
+    for t4 in seq:
+        t4[3].close()
+    return out
+
+
+def _leg(fn, *args):
+    """An extra block of the bench line; a failure is recorded in the block
+    instead of ending the run (the frame measurement above is complete)."""
+    try:
+        return fn(*args)
+    except Exception as e:  # noqa: BLE001
+        return {"error": "%s: %s" % (type(e).__name__, e)}
+
+
 def run_ours(a):
     import torch
     import numpy as np
@@ -271,13 +430,13 @@ def run_ours(a):
     skin_ev = []
 
     def step(record):
-        restore(st, snap)
         ev = (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) if record else None
         st.frame(stats=False, with_cov=True, skin_events=ev)
         if record:
             skin_ev.append(ev)
 
     for _ in range(max(3, a.warmup)):
+        restore(st, snap)
         step(False)
     torch.cuda.synchronize()
     assert st.status() == 0
@@ -288,7 +447,8 @@ def run_ours(a):
     t0 = time.perf_counter()
     with ClockSampler(torch.cuda.current_device()) as clk:
         for _ in range(a.steps):
-            flush.fill_(1.0)  # L2 flush between steps (256 MB > 129 MB L2)
+            restore(st, snap)  # the rest state, outside the timed region
+            flush.fill_(1.0)   # L2 flush between steps (256 MB > 129 MB L2)
             e0 = torch.cuda.Event(enable_timing=True)
             e1 = torch.cuda.Event(enable_timing=True)
             e0.record(s)
@@ -367,11 +527,11 @@ def run_ours(a):
         "dtype": "f32+f64" if a.form == "chosen" else "f32",
         "data": "synthetic (seeded two-bars-and-sphere field; reference datasets absent)",
         "config": {"workload": "%s: %d Gaussians, %d^3 grid, %d nodes, k=%d, %d GN iterations, "
-                               "twist 90 deg, form=%s" % (sc.name, sc.n_gauss, sc.grid_num,
-                                                           sc.n_nodes, k, sc.iters, a.form),
+                               "%s, form=%s" % (sc.name, sc.n_gauss, sc.grid_num, sc.n_nodes, k, sc.iters,
+                                                op_text(sc.op), a.form),
                    "samples": int(st.sample_pos.shape[0]) if st.sample_pos is not None else 0,
                    "l2": "flushed between steps (256 MB write)",
-                   "state": "restored to the rest pose inside each step",
+                   "state": "restored to the rest pose before each step, outside the timed region",
                    "wall_s_timed_region": round(wall, 3)},
         "e2e": {"value": round(reduce_max(float(np.mean(e2e_ms)), ws), 4), "unit": "ms/frame",
                 "h2d_bytes_per_step": int(st.n * 12), "d2h_bytes_per_step": int(st.n * 48)},
@@ -397,15 +557,80 @@ def run_ours(a):
         "clocks": clk.summary(),
     }
     if rank == 0 and a.batch > 0:
-        line["batch"] = batch_leg(a.batch)
+        line["batch"] = _leg(batch_leg, a.batch)
+        line["batch_frames"] = _leg(batch_frame_leg, a.batch)
     if rank == 0:
-        line["ply_io"] = ply_leg(sc)
+        line["adjoint"] = _leg(adjoint_leg, st)
+        line["ply_io"] = _leg(ply_leg, sc)
     if rank == 0 and not a.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline(sc)
+        line["cpu_baseline"] = _leg(cpu_baseline, sc)
     if rank == 0:
         print(json.dumps(line))
     if ws > 1:
         torch.distributed.destroy_process_group()
+
+
+def adjoint_leg(st, reps=10):
+    """The forward/backward pair at the frame's scale: Gaussian skinning
+    (arap_skin_gaussians), its adjoint (arap_skin_gaussians_backward: the
+    node gradient of sum g_mu.mu + g_Sigma:Sigma for upstream gradients
+    N(0,1) on every Gaussian's mu [N,3] and Sigma [N,6]) and the energy
+    gradient (arap_solver_energy_grad: J^T f at the solved transforms), each
+    timed with CUDA events (median of reps)."""
+    import numpy as np
+    import torch
+    dev = importlib.import_module(PKG + ".deform")
+    N, n = st.N, st.n
+    rot, tr, _ = st.solver.solve(st.node_pos, st.aims, st.rot_nodes, st.trans_nodes, stats=False)
+    table = dev.node_table(rot, tr, st.node_pos)
+    gen = torch.Generator(device="cuda").manual_seed(3)
+    g_mu = torch.randn((N, 3), device="cuda", generator=gen)
+    g_cov = torch.randn((N, 6), device="cuda", generator=gen)
+    grad = torch.zeros((n, 12), device="cuda")
+    ends = st.ends.clone()
+    pos = torch.empty((N, 3), device="cuda")
+    q = st.rot.clone()
+    sc = torch.empty((N, 3), device="cuda")
+    cov = torch.empty((N, 6), device="cuda")
+    F = st.solver.F
+    free = st.solver.free_ids.to("cuda")
+    x = torch.cat([rot, tr], 1)[free].to(torch.float64).reshape(-1).contiguous()
+
+    def timed(fn):
+        out = []
+        for r in range(reps + 2):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            e0.record()
+            fn()
+            e1.record()
+            torch.cuda.synchronize()
+            if r >= 2:
+                out.append(e0.elapsed_time(e1))
+        return float(np.median(out))
+
+    def fwd():
+        ends.copy_(st.ends)
+        dev.skin_gaussians(ends, st.ends_idx, st.ends_w, table, st.scale0, pos, q, sc, None, cov,
+                           precision=st.precision)
+
+    def bwd():
+        grad.zero_()
+        dev.skin_gaussians_backward(st.ends, st.ends_idx, st.ends_w, table, st.scale0, g_mu, g_cov, n,
+                                    grad_node=grad)
+
+    ms_f = timed(fwd)
+    ms_b = timed(bwd)
+    ms_e = timed(lambda: st.solver.energy_grad(st.node_pos, st.aims, x))
+    k = st.k
+    bytes_b = N * (72 + 6 * k * 8 + 12 + 12 + 24)
+    return {"gaussians": N, "nodes": n, "free_nodes": F, "precision": int(st.precision),
+            "ms_skin_forward_with_cov": round(ms_f, 4), "ms_skin_backward": round(ms_b, 4),
+            "ms_energy_grad": round(ms_e, 4),
+            "backward_bytes_per_gaussian": 72 + 6 * k * 8 + 12 + 12 + 24,
+            "backward_gbs": round(bytes_b / (ms_b * 1e-3) / 1e9, 1),
+            "note": "backward reads endpoints, int32 kNN indices and float weights, scale0 and the upstream "
+                    "gradients; node gradients are summed per CTA in shared memory, then with global atomics"}
 
 
 def ply_leg(sc, reps=3):
@@ -487,9 +712,9 @@ def run_reference(a):
             "warmup": a.warmup, "ms_per_step": round(v, 1), "higher_is_better": False, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded two-bars-and-sphere field)",
             "impl": "reference",
-            "config": {"workload": "%s: %d Gaussians, %d^3 grid, %d nodes, k=%d, %d GN iterations, twist 90 deg "
+            "config": {"workload": "%s: %d Gaussians, %d^3 grid, %d nodes, k=%d, %d GN iterations, %s "
                                    "(reference CPU path restated in C++/OpenMP, host cores)"
-                                   % (sc.name, sc.n_gauss, sc.grid_num, sc.n_nodes, sc.k, sc.iters),
+                                   % (sc.name, sc.n_gauss, sc.grid_num, sc.n_nodes, sc.k, sc.iters, op_text(sc.op)),
                        "samples": fb.n_samples, "setup_s": round(t_setup, 1), "wall_s_timed_region": round(wall, 1)},
             "cpu_baseline": {"value": round(v, 1), "unit": "ms/frame", "cores": fb.threads, "kind": "port",
                              "sample": _cpu_sample_text(fb, parts, st)},

@@ -111,6 +111,13 @@ typedef struct {
                              slowest CTA's own work (barrier waits excluded) inside
                              PCG: [6] products (J^T J) p, [7] vector update and
                              preconditioner, [8] coarse solves */
+  int resident;           /* 1: every CTA's nodes and PCG vectors fit in its shared
+                             memory (the resident two-level PCG with the V-cycle);
+                             0: the non-resident PCG with the additive preconditioner */
+  int coarse_fallbacks;   /* Gauss-Newton iterations whose coarse matrix had a pivot that
+                             was not positive in float32 (nearly collinear nodes in an
+                             aggregate): their PCG ran with block-Jacobi alone, which is
+                             slower but still solves the same system */
 } arap_solve_stats;
 
 typedef struct arap_solver arap_solver;

@@ -125,3 +125,71 @@ def test_energy_gradient_matches_fd(dev):
         xm[i] -= 1e-6
         fd = (E(xp) - E(xm)) / 2e-6
         assert abs(fd - 2 * g[i]) <= 1e-5 * (abs(fd) + np.abs(g).max() * 1e-2)
+
+
+def test_adjoint_pair_at_the_benchmark_scale(dev):
+    """The forward/backward pair on the whole twist300k field: 300000
+    Gaussians, 4061 nodes at the oracle's solved transforms, upstream
+    gradients N(0,1) on mu [N,3] and Sigma [N,6].  The node gradient against
+    the float64 oracle adjoint, float64 finite differences (eps = 1e-6) on
+    64 random node coordinates (each evaluated on the Gaussians whose
+    endpoints blend that node, the only ones it moves), and the energy
+    gradient J^T f at the same transforms against the oracle's."""
+    import os
+    from oracle import ed, skin
+    sc = H.synth.make_scene("twist300k")
+    g = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "solve_twist300k.npz"))
+    X32 = g["x"].astype(np.float64)
+    N, n, k = sc.n_gauss, sc.n_nodes, sc.k
+    ends, exyz = dev.end_points(_t(sc.pos), _t(sc.rot), _t(sc.scale))
+    eidx, ew = dev.compute_weights(exyz, _t(sc.node_pos), k)
+    del exyz
+    rng = np.random.default_rng(2)
+    g_mu = rng.standard_normal((N, 3))
+    g_cov = rng.standard_normal((N, 6))
+    rot_t = _t(g["x"][:, :9]).requires_grad_(True)
+    tr_t = _t(g["x"][:, 9:]).requires_grad_(True)
+    mu, cov = SkinFn.apply(rot_t, tr_t, dev, _t(sc.node_pos), ends, eidx, ew, _t(sc.scale), _t(sc.rot))
+    ((mu * _t(g_mu.astype(np.float32))).sum() + (cov * _t(g_cov.astype(np.float32))).sum()).backward()
+    gX = np.concatenate([rot_t.grad.cpu().numpy(), tr_t.grad.cpu().numpy()], 1).astype(np.float64)
+    e_in = ends.cpu().numpy().reshape(6, 3, N).transpose(2, 0, 1).astype(np.float64)
+    io = eidx.cpu().numpy().reshape(k, 6, N).transpose(2, 1, 0).reshape(6 * N, k)
+    wo = ew.cpu().numpy().reshape(k, 6, N).transpose(2, 1, 0).reshape(6 * N, k).astype(np.float64)
+    G = skin.packed_to_sym(g_cov)
+    gX_ref = skin.skin_backward(e_in, io, wo, X32, sc.node_pos, sc.scale, g_mu, G)
+    scale_g = np.abs(gX_ref).max()
+    err = np.abs(gX - gX_ref).max() / scale_g
+    print("adjoint twist300k: max |dG| / max |G| = %.2e" % err)
+    assert err <= 2e-3
+    uses = io.reshape(N, 6 * k)
+    eps = 1e-6
+    for _ in range(64):
+        a, b = rng.integers(n), rng.integers(12)
+        sel = np.flatnonzero((uses == a).any(axis=1))
+        rows = (sel[:, None] * 6 + np.arange(6)[None, :]).reshape(-1)
+
+        def L(Xv):
+            m, S = skin.skin_forward_from_nodes(e_in[sel], io[rows], wo[rows], Xv, sc.node_pos, sc.scale[sel])
+            return (g_mu[sel] * m).sum() + (G[sel] * S).sum()
+        Xp = X32.copy()
+        Xp[a, b] += eps
+        Xm = X32.copy()
+        Xm[a, b] -= eps
+        fd = (L(Xp) - L(Xm)) / (2 * eps)
+        assert abs(fd - gX_ref[a, b]) <= 1e-6 * scale_g + 1e-6 * abs(fd)
+        assert abs(fd - gX[a, b]) <= 2e-3 * scale_g
+    # energy gradient at the solved transforms
+    nb = ed.build_graph(sc.node_pos, k)
+    aidx, aw = ed.knn_weights(sc.pos[sc.node_vertex], sc.node_pos, k)
+    aims = H.oracle_aims(sc, sc.node_pos)
+    pr = ed.EDProblem(sc.node_pos, nb, aidx, aw.astype(np.float32).astype(np.float64), sc.blocks, sc.block_type,
+                      aims)
+    x = X32[pr.free].reshape(-1)
+    solver = dev.Solver(_t(nb.astype(np.int32)), _t(aidx.T.astype(np.int32)), _t(aw.T.astype(np.float32)),
+                        sc.blocks, sc.block_type, precision=1)
+    gE, e = solver.energy_grad(_t(sc.node_pos), _t(aims), _t(x))
+    f = ed.residual(pr, x)
+    gr = ed.gradient(pr, x)
+    assert abs(e - f @ f) <= 1e-9 * (f @ f)
+    assert H.rel_err(gE.cpu().numpy(), gr) <= 1e-8
+    solver.close()

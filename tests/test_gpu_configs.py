@@ -108,3 +108,34 @@ def test_frame_matches_the_oracle(dev, case, form):
     assert err["mu"] <= tol and err["sample_pos"] <= tol and err["nodes"] <= tol
     assert err["sigma"] <= tol and err["q"] <= tol and err["scale"] <= tol
     assert err["shs"] <= 2e-4 and err["feature"] <= 2e-4
+
+
+@pytest.mark.parametrize("form", ["chosen", "plain"])
+def test_non_resident_solve_matches_the_oracle(dev, form):
+    """stress200k: 7583 free nodes of 8044 (an excluded block), k = 12, more
+    than the solver keeps resident in shared memory, so the chosen form runs
+    the non-resident two-level PCG.  Node transforms against the float64
+    C++ restatement's solve (tests/golden/solve_stress200k.npz)."""
+    from oracle import cpu_frame as cf
+    from oracle import ed
+    sc = H.synth.make_scene("stress200k")
+    g = np.load(os.path.join(GOLDEN, "solve_stress200k.npz"))
+    nb = ed.build_graph(sc.node_pos, sc.k)
+    aidx, aw = cf.knn_weights(sc.pos[sc.node_vertex], sc.node_pos, sc.k)
+    aims = H.oracle_aims(sc, sc.node_pos)
+    precision, coarse = (1, 64) if form == "chosen" else (0, 0)
+    t = lambda a: torch.as_tensor(np.ascontiguousarray(a)).cuda()  # noqa: E731
+    solver = dev.Solver(t(nb.astype(np.int32)), t(aidx.T.astype(np.int32)), t(aw.T.astype(np.float32)),
+                        sc.blocks, sc.block_type, max_iters=sc.iters, early_exit=0, precision=precision,
+                        coarse_nodes=coarse)
+    rot, tr, st = solver.solve(t(sc.node_pos), t(aims))
+    assert st["status"] == 0 and st["gn_iterations"] == sc.iters
+    assert st["n_free"] == 7583 and st["resident"] == 0
+    X = np.concatenate([_np(rot), _np(tr)], 1)
+    err = _rel(X, g["x"].astype(np.float64))
+    print("stress200k %s: pcg %d, coarse %d, halvings %d (oracle %d), x error %.2e"
+          % (form, st["pcg_iterations"], st["n_coarse"], st["halvings"], int(g["halvings"].sum()), err))
+    assert st["halvings"] == int(g["halvings"].sum())
+    assert abs(st["initial_energy"] - g["energies"][0]) <= 1e-5 * g["energies"][0]
+    assert err <= (1e-5 if form == "chosen" else 5e-5)
+    solver.close()

@@ -35,7 +35,7 @@ def _worker(rank, ws, port, out):
 def test_reduce_max_two_ranks_gloo():
     import torch.multiprocessing as mp
     ws, port = 2, _free_port()
-    with mp.Manager() as m:
+    with mp.get_context("spawn").Manager() as m:
         out = m.dict()
         mp.start_processes(_worker, args=(ws, port, out), nprocs=ws, start_method="spawn", join=True)
         assert dict(out) == {0: 15.0, 1: 15.0}
