@@ -40,8 +40,9 @@ int status_read_clear(int* status_dev, cudaStream_t stream);
 
 // ------------------------------------------------------------ barrier ----
 // Grid-wide barrier for cooperative launches (all CTAs co-resident).  Every
-// wait is bounded: after spin_limit polls a waiting CTA records the timeout,
-// marks the barrier failed and returns false; callers then leave the kernel.
+// wait is bounded: after its limit of polls a waiting CTA records the
+// timeout, marks the barrier failed and returns false; callers then leave the
+// kernel.
 //
 // Counter barrier with a reduction.  Arrivals go to one monotonic counter
 // (zeroed before each launch): the arrivals of the e-th barrier of a launch
@@ -54,14 +55,14 @@ int status_read_clear(int* status_dev, cudaStream_t stream);
 // partial buffers suffice: a CTA can only reach barrier e+2 once every CTA has
 // arrived at e+1, i.e. has finished reading barrier e.
 // count and failed are zeroed before each launch (the first 8 bytes);
-// spin_limit is written once by the barrier's owner and read by every wait,
-// so the kernel holds no register for it.  A wait that runs out sets failed,
+// spin_limit is written once by the barrier's owner (the configured limit,
+// read by the waits of GridSyncT<true>).  A wait that runs out sets failed,
 // which the owner reports as ARAP_ETIMEOUT.  status is the owner's device
 // status word (raise_status), kept across launches until the host reads it.
 struct GridBarrier {
   unsigned int count;
   int failed;
-  unsigned int spin_limit;  // polls of one wait before it gives up (checked every 64)
+  unsigned int spin_limit;  // polls of one wait before it gives up (GridSyncT<true>)
   int status;
 };
 
@@ -144,12 +145,29 @@ __device__ __forceinline__ void dd_warp_sum(float& hi, float& lo) {
 // (the whole grid, or one instance's share of a batched launch); bid is this
 // CTA's index in the group.  Every thread of every CTA of the group must make
 // the same sequence of calls (the epoch is counted in registers).
-struct GridSync {
+//
+// A wait gives up after kSpinLimit polls, or with kCfgLimit after the
+// barrier record's spin_limit polls (read at every poll).  The two are kept
+// apart because the wait is inlined at every barrier of the persistent solve,
+// and any form of a run-time limit there (a register, a parameter, a field of
+// this handle, a load every 64 polls, an offset start count, an out-of-line
+// wait) made the whole solve kernel 9-10 % slower on a GB300, against a
+// constant bound; the solver runs the kCfgLimit form only when a spin limit
+// is configured.
+template <bool kCfgLimit>
+struct GridSyncT {
   GridBarrier* bar;
   double* partials;  // [2][nb][kReduceSlots]
   unsigned int epoch;
   unsigned int nb;
   unsigned int bid;
+
+  __device__ __forceinline__ long long spin_cap() const {
+    if constexpr (kCfgLimit)
+      return (long long)ld_relaxed_u32(&bar->spin_limit);
+    else
+      return kSpinLimit;
+  }
 
   // One thread per CTA: arrive at barrier e (release) and wait (acquire) for
   // every CTA; bounded, false on failure.
@@ -159,14 +177,10 @@ struct GridSync {
     long long it = 0;
     while ((int)(ld_acquire_u32(&bar->count) - target) < 0) {
       ++it;
-      // every 64 polls: a peer's failure, then this wait's own limit (read
-      // here, so that no register holds it through the caller's code)
-      if ((it & 63) == 0) {
-        if (ld_relaxed_i32(&bar->failed)) return false;
-        if (it >= (long long)ld_relaxed_u32(&bar->spin_limit)) {
-          atomicExch(&bar->failed, 1);
-          return false;
-        }
+      if ((it & 63) == 0 && ld_relaxed_i32(&bar->failed)) return false;
+      if (it > spin_cap()) {
+        atomicExch(&bar->failed, 1);
+        return false;
       }
       if (it > 1024) __nanosleep(32);
     }
@@ -306,6 +320,7 @@ struct GridSync {
     return s_sync_ok != 0;
   }
 };
+using GridSync = GridSyncT<false>;
 
 // Block-wide FP64 sum (blockDim.x multiple of 32, <= 1024); all threads get it.
 template <int NV>

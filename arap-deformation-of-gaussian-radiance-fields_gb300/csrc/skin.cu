@@ -125,53 +125,193 @@ __global__ void end_points_kernel(int N, const float* __restrict__ pos,
 }
 
 // Fused UpdatePosition (endpoint part, GaussianView.cpp:3022-3040) and
-// UpdateAsSixPointsWithdrawBad (GaussianView.cpp:3081-3166).
-//
-// One thread per Gaussian, kSkinTile per CTA.  The tile's 48-float SH records
-// and previous quaternions are copied into shared memory with cp.async (16-byte
-// copies of contiguous records) while each thread blends its six endpoints from
-// coalesced loads of the endpoint, index and weight planes; the SH records go
-// back with coalesced 16-byte stores.  Shared memory (28.6 KB) and registers
-// (launch bound of four CTAs per SM) keep 16 warps per SM resident.
+// UpdateAsSixPointsWithdrawBad (GaussianView.cpp:3081-3166): one thread per
+// Gaussian, kSkinTile per CTA.  The tile's 48-float SH records go through
+// shared memory (16-byte cp.async copies of the contiguous records in, the
+// rotation in place, coalesced 16-byte stores out) so that every global
+// access of the kernel is coalesced.
 constexpr int kSkinTile = kSkinThreads;  // Gaussians per CTA
 constexpr int kShStride = 52;            // floats per staged SH record (13 float4: conflict-free)
 
+__device__ __forceinline__ uint32_t smem_addr(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+
 __device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
-  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(s), "l"(gmem) : "memory");
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_addr(smem)), "l"(gmem) : "memory");
+}
+
+// The tile's SH records [cnt][48] into s_sh [T][kShStride] (all threads).
+__device__ __forceinline__ void stage_sh(float* s_sh, const float* shs, int tile0, int cnt) {
+  const float* src = shs + 48 * (size_t)tile0;
+  for (int q = threadIdx.x; q < 12 * cnt; q += kSkinThreads)
+    cp_async16(s_sh + (q / 12) * kShStride + (q % 12) * 4, src + 4 * (size_t)q);
+  asm volatile("cp.async.commit_group;" ::: "memory");
+}
+
+// s_sh back to the tile's SH records (all threads; after a __syncthreads).
+__device__ __forceinline__ void store_sh(float* shs, const float* s_sh, int tile0, int cnt) {
+  float4* dst = reinterpret_cast<float4*>(shs + 48 * (size_t)tile0);
+  for (int q = threadIdx.x; q < 12 * cnt; q += kSkinThreads)
+    __stcs(dst + q, *reinterpret_cast<const float4*>(s_sh + (q / 12) * kShStride + (q % 12) * 4));
+}
+
+// ---- bulk copies (TMA) and their mbarrier
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint32_t bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+
+// global -> shared bulk copy completing on bar; both addresses 16-byte
+// aligned, bytes a multiple of 16.
+__device__ __forceinline__ void bulk_g2s(uint32_t dst, const void* src, uint32_t bytes, uint32_t bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+               "l"(src), "r"(bytes), "r"(bar)
+               : "memory");
+}
+
+// Bounded wait for phase `parity` of bar: false after max_polls polls.
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, int max_polls) {
+  for (int it = 0; it < max_polls; ++it) {
+    uint32_t done;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(done)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+constexpr int kMbarPolls = 1 << 18;
+
+// The refit of one Gaussian from its six blended endpoints e (UpdateAsSix-
+// PointsWithdrawBad, GaussianView.cpp:3081-3166): centre, polar factor R of
+// the endpoint matrix, quaternion, scale, Sigma; writes mu, q, scale and
+// Sigma of Gaussian i and returns in Rr the rotation q q_old^-1 that rotates
+// its SH.
+template <bool MIXED>
+__device__ __forceinline__ void refit_gaussian(int i, const float (&e)[18], const float (&s0v)[3], float4 q_old,
+                                               float* __restrict__ pos_out, float* __restrict__ rot_out,
+                                               float* __restrict__ scale_out, float* __restrict__ cov_out,
+                                               int* __restrict__ status, float (&Rr)[9]) {
+  float cx = 0.f, cy = 0.f, cz = 0.f;
+#pragma unroll
+  for (int ep = 0; ep < 6; ++ep) {
+    cx += e[3 * ep];
+    cy += e[3 * ep + 1];
+    cz += e[3 * ep + 2];
+  }
+  cx *= (1.0f / 6.0f);
+  cy *= (1.0f / 6.0f);
+  cz *= (1.0f / 6.0f);
+  // M = (P - c) Q^+ with Q = [e0 -e0 e1 -e1 e2 -e2], Q^+ = Q^T / 2:
+  // column a of M is (P_{2a} - P_{2a+1}) / 2.
+  float M[9];
+#pragma unroll
+  for (int a = 0; a < 3; ++a)
+#pragma unroll
+    for (int r = 0; r < 3; ++r) M[r * 3 + a] = 0.5f * (e[3 * (2 * a) + r] - e[3 * (2 * a + 1) + r]);
+  float R[9];
+  bool ok;
+  if (MIXED) {
+    // FP64 polar factor when M is ill-conditioned (sigma_min/sigma_max < 1e-3)
+    float nx = 0.f, ny = 0.f, Y[9];
+    ok = inv_transpose3(M, Y);
+#pragma unroll
+    for (int q = 0; q < 9; ++q) {
+      nx += M[q] * M[q];
+      ny += Y[q] * Y[q];
+    }
+    if (!ok || nx * ny > 1e6f) {
+      double Md[9], Rd[9];
+#pragma unroll
+      for (int q = 0; q < 9; ++q) Md[q] = M[q];
+      ok = polar_factor<double>(Md, Rd, 40, 1e-15);
+#pragma unroll
+      for (int q = 0; q < 9; ++q) R[q] = (float)Rd[q];
+    } else {
+      ok = polar_factor<float>(M, R, 20, 2e-7f);
+    }
+  } else {
+    ok = polar_factor<float>(M, R, 20, 2e-7f);
+  }
+  if (!ok) raise_status(status, ARAP_ENONFINITE);
+  // K = diag(R^T M) = diag(V S V^T)
+  float Kd[3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) Kd[a] = R[a] * M[a] + R[3 + a] * M[3 + a] + R[6 + a] * M[6 + a];
+  const float4 q = quat_normalize(quat_from_rowmajor(R));
+  float sc[3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    const float s0 = s0v[a];
+    sc[a] = Kd[a] / ((s0 + 1e-3f) * 2.0f) * s0;
+  }
+  pos_out[3 * (size_t)i] = cx;
+  pos_out[3 * (size_t)i + 1] = cy;
+  pos_out[3 * (size_t)i + 2] = cz;
+  scale_out[3 * (size_t)i] = sc[0];
+  scale_out[3 * (size_t)i + 1] = sc[1];
+  scale_out[3 * (size_t)i + 2] = sc[2];
+  reinterpret_cast<float4*>(rot_out)[i] = q;
+  if (cov_out) {
+    float Rq[9];
+    quat_to_rowmajor(q, Rq);
+    const float s2[3] = {sc[0] * sc[0], sc[1] * sc[1], sc[2] * sc[2]};
+    float S[6];
+    int o = 0;
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+#pragma unroll
+      for (int c = r; c < 3; ++c)
+        S[o++] = Rq[r * 3] * s2[0] * Rq[c * 3] + Rq[r * 3 + 1] * s2[1] * Rq[c * 3 + 1] +
+                 Rq[r * 3 + 2] * s2[2] * Rq[c * 3 + 2];
+#pragma unroll
+    for (int q6 = 0; q6 < 6; ++q6) cov_out[6 * (size_t)i + q6] = S[q6];
+  }
+  quat_to_rowmajor(quat_normalize(quat_mul(q, quat_inverse(q_old))), Rr);
+}
+
+// Rotates the staged 48-float SH record rec (kShStride floats) by Rr.
+__device__ __forceinline__ void rotate_sh_record(float* rec_f, const float (&Rr)[9]) {
+  float4* rec = reinterpret_cast<float4*>(rec_f);
+  float v[48];
+#pragma unroll
+  for (int q4 = 0; q4 < 12; ++q4) {
+    const float4 u = rec[q4];
+    v[4 * q4] = u.x;
+    v[4 * q4 + 1] = u.y;
+    v[4 * q4 + 2] = u.z;
+    v[4 * q4 + 3] = u.w;
+  }
+  rotate_sh48<true>(Rr, v);
+#pragma unroll
+  for (int q4 = 0; q4 < 12; ++q4) rec[q4] = make_float4(v[4 * q4], v[4 * q4 + 1], v[4 * q4 + 2], v[4 * q4 + 3]);
 }
 
 constexpr size_t skin_smem_bytes() { return sizeof(float) * (size_t)kSkinTile * (4 + kShStride); }
 
-// Skinning plan (set-up time, arap_skin_plan_create): per tile of kSkinTile
-// Gaussians the distinct nodes its endpoints blend (at most kPlanNodes), each
-// endpoint neighbour as an 8-bit index into that list, and the weights, both
-// per Gaussian endpoint-major ([6][K], contiguous).  A frame then copies the
-// tile's node records into shared memory once and gathers from there.
-constexpr int kPlanNodes = 256;
-constexpr int kPlanRec = 12;  // floats per staged node record (NodeAf; the 48-byte stride spreads banks)
-struct SkinPlanDev {
-  const int32_t* tile_count;  // [tiles] distinct nodes of the tile (> kPlanNodes: no local list)
-  const int32_t* tile_nodes;  // [tiles][kPlanNodes]
-  const uint8_t* lidx;        // [N][6][kp] local node index, kp = K rounded up to 4
-  const float* wts;           // [N][6][K]
-  int kp;
-};
-constexpr size_t skin_plan_smem_bytes() { return skin_smem_bytes() + sizeof(float) * kPlanNodes * kPlanRec; }
-
-template <int K, bool MIXED, bool PLANNED>
+// Without a plan: each endpoint's K node records are gathered from the node
+// table (L1/L2) and put into tile-local affine form on the fly; indices and
+// weights come from the planes [K*6][N].
+template <int K, bool MIXED>
 __global__ void __launch_bounds__(kSkinThreads, 4)
     skin_gaussians_kernel(int N, float* __restrict__ ends, const int32_t* __restrict__ eidx,
                           const float* __restrict__ ew, const float* __restrict__ table,
                           const float* __restrict__ scale0, const uint8_t* __restrict__ static_mask,
                           float* __restrict__ pos_out, float* __restrict__ rot_inout,
                           float* __restrict__ scale_out, float* __restrict__ shs,
-                          float* __restrict__ cov_out, SkinPlanDev plan, int* __restrict__ status) {
+                          float* __restrict__ cov_out, int* __restrict__ status) {
   extern __shared__ float4 s_raw4[];
-  float* s_raw = reinterpret_cast<float*>(s_raw4);
-  float* s_sh = s_raw;                                        // [T][52]
+  float* s_sh = reinterpret_cast<float*>(s_raw4);                         // [T][52]
   float4* s_q = reinterpret_cast<float4*>(s_sh + kSkinTile * kShStride);  // [T]
-  float* s_nodes = reinterpret_cast<float*>(s_q + kSkinTile);  // PLANNED: [kPlanNodes][kPlanRec]
   const int t = threadIdx.x;
   const int tile0 = blockIdx.x * kSkinTile;
   const int cnt = min(kSkinTile, N - tile0);
@@ -181,108 +321,30 @@ __global__ void __launch_bounds__(kSkinThreads, 4)
   // (read by every thread before any thread writes its endpoints)
   const float o_x = __ldg(ends + tile0), o_y = __ldg(ends + (size_t)N + tile0),
               o_z = __ldg(ends + 2 * (size_t)N + tile0);
-  // ---- planned: the tile's node records into shared memory, in tile-local
-  // affine form (one thread per node)
-  int n_local = kPlanNodes + 1;
-  if (PLANNED) {
-    n_local = __ldg(plan.tile_count + blockIdx.x);
-    if (n_local <= kPlanNodes) {
-      const int32_t* list = plan.tile_nodes + (size_t)blockIdx.x * kPlanNodes;
-      for (int u = t; u < n_local; u += kSkinThreads) {
-        const NodeAf r = node_affine(load_node(table, __ldg(list + u)), o_x, o_y, o_z);
-        float4* d4 = reinterpret_cast<float4*>(s_nodes + u * kPlanRec);
-        d4[0] = r.a;
-        d4[1] = r.b;
-        d4[2] = r.c;
-      }
-    }
-  }
-  const bool local = PLANNED && n_local <= kPlanNodes;
-  // ---- stage the SH records and previous quaternions of the tile
   if (active) cp_async16(s_q + t, reinterpret_cast<const float4*>(rot_inout) + i);
-  if (shs) {
-    const float* src = shs + 48 * (size_t)tile0;
-    for (int q = t; q < 12 * cnt; q += kSkinThreads)
-      cp_async16(s_sh + (q / 12) * kShStride + (q % 12) * 4, src + 4 * (size_t)q);
-  }
-  asm volatile("cp.async.commit_group;" ::: "memory");
-  // the node records are needed now (and every thread has read the origin);
-  // the SH records later
+  if (shs)
+    stage_sh(s_sh, shs, tile0, cnt);
+  else
+    asm volatile("cp.async.commit_group;" ::: "memory");
   __syncthreads();
 
   float e[18];
-  // loads the refit needs later, issued now so that they overlap the blend
   const bool is_static = active && static_mask && __ldg(static_mask + i);
   float s0v[3] = {0.f, 0.f, 0.f};
   if (active) {
 #pragma unroll
     for (int a = 0; a < 3; ++a) s0v[a] = __ldg(scale0 + 3 * (size_t)i + a);
-  }
-  if (active) {
 #pragma unroll
     for (int c = 0; c < 18; ++c) e[c] = __ldcs(ends + (size_t)c * N + i);
-    // planned: endpoint ep+1's indices and weights are requested before
-    // endpoint ep is blended
-    constexpr int KW = (K + 3) / 4;
-    uint32_t lw_next[KW];
-    float w_next[K];
-    auto fetch_plan = [&](int ep, uint32_t(&lw)[KW], float(&wv)[K]) {
-      const uint32_t* lp = reinterpret_cast<const uint32_t*>(plan.lidx + ((size_t)i * 6 + ep) * plan.kp);
-      const float* wp = plan.wts + ((size_t)i * 6 + ep) * K;
-#pragma unroll
-      for (int q = 0; q < KW; ++q) lw[q] = __ldcs(lp + q);
-      if (K % 4 == 0) {
-#pragma unroll
-        for (int q = 0; q < K / 4; ++q) {
-          const float4 w4 = __ldcs(reinterpret_cast<const float4*>(wp) + q);
-          wv[4 * q] = w4.x;
-          wv[4 * q + 1] = w4.y;
-          wv[4 * q + 2] = w4.z;
-          wv[4 * q + 3] = w4.w;
-        }
-      } else {
-#pragma unroll
-        for (int j = 0; j < K; ++j) wv[j] = __ldcs(wp + j);
-      }
-    };
-    if (local) fetch_plan(0, lw_next, w_next);
 #pragma unroll
     for (int ep = 0; ep < 6; ++ep) {
       float ox = 0.f, oy = 0.f, oz = 0.f, ws = 0.f;
-      int id[K];
-      float wv[K];
-      if (local) {
-        uint32_t lw[KW];
-#pragma unroll
-        for (int q = 0; q < KW; ++q) lw[q] = lw_next[q];
-#pragma unroll
-        for (int j = 0; j < K; ++j) wv[j] = w_next[j];
-        if (ep + 1 < 6) fetch_plan(ep + 1, lw_next, w_next);
-#pragma unroll
-        for (int q = 0; q < KW; ++q)
-#pragma unroll
-          for (int r = 0; r < 4; ++r)
-            if (4 * q + r < K) id[4 * q + r] = (lw[q] >> (8 * r)) & 0xffu;
-      } else {
-#pragma unroll
-        for (int j = 0; j < K; ++j) {
-          id[j] = __ldcs(eidx + (size_t)(j * 6 + ep) * N + i);
-          wv[j] = __ldcs(ew + (size_t)(j * 6 + ep) * N + i);
-        }
-      }
       const float dx = e[3 * ep] - o_x, dy = e[3 * ep + 1] - o_y, dz = e[3 * ep + 2] - o_z;
 #pragma unroll
       for (int j = 0; j < K; ++j) {
-        NodeAf x;
-        if (local) {
-          const float4* r4 = reinterpret_cast<const float4*>(s_nodes + id[j] * kPlanRec);
-          x.a = r4[0];
-          x.b = r4[1];
-          x.c = r4[2];
-        } else {
-          x = node_affine(load_node(table, id[j]), o_x, o_y, o_z);
-        }
-        const float w = wv[j];
+        const int id = __ldcs(eidx + (size_t)(j * 6 + ep) * N + i);
+        const float w = __ldcs(ew + (size_t)(j * 6 + ep) * N + i);
+        const NodeAf x = node_affine(load_node(table, id), o_x, o_y, o_z);
         ws += w;
         ed_term_af(x, w, dx, dy, dz, ox, oy, oz);
       }
@@ -295,109 +357,172 @@ __global__ void __launch_bounds__(kSkinThreads, 4)
   }
   asm volatile("cp.async.wait_group 0;" ::: "memory");
   __syncthreads();
-  if (active) {
-    if (!is_static) {
-      float cx = 0.f, cy = 0.f, cz = 0.f;
-#pragma unroll
-      for (int ep = 0; ep < 6; ++ep) {
-        cx += e[3 * ep];
-        cy += e[3 * ep + 1];
-        cz += e[3 * ep + 2];
-      }
-      cx *= (1.0f / 6.0f);
-      cy *= (1.0f / 6.0f);
-      cz *= (1.0f / 6.0f);
-      // M = (P - c) Q^+ with Q = [e0 -e0 e1 -e1 e2 -e2], Q^+ = Q^T / 2:
-      // column a of M is (P_{2a} - P_{2a+1}) / 2.
-      float M[9];
-#pragma unroll
-      for (int a = 0; a < 3; ++a)
-#pragma unroll
-        for (int r = 0; r < 3; ++r) M[r * 3 + a] = 0.5f * (e[3 * (2 * a) + r] - e[3 * (2 * a + 1) + r]);
-      float R[9];
-      bool ok;
-      if (MIXED) {
-        // FP64 polar factor when M is ill-conditioned (sigma_min/sigma_max < 1e-3)
-        float nx = 0.f, ny = 0.f, Y[9];
-        ok = inv_transpose3(M, Y);
-#pragma unroll
-        for (int q = 0; q < 9; ++q) {
-          nx += M[q] * M[q];
-          ny += Y[q] * Y[q];
-        }
-        if (!ok || nx * ny > 1e6f) {
-          double Md[9], Rd[9];
-#pragma unroll
-          for (int q = 0; q < 9; ++q) Md[q] = M[q];
-          ok = polar_factor<double>(Md, Rd, 40, 1e-15);
-#pragma unroll
-          for (int q = 0; q < 9; ++q) R[q] = (float)Rd[q];
-        } else {
-          ok = polar_factor<float>(M, R, 20, 2e-7f);
-        }
-      } else {
-        ok = polar_factor<float>(M, R, 20, 2e-7f);
-      }
-      if (!ok) raise_status(status, ARAP_ENONFINITE);
-      // K = diag(R^T M) = diag(V S V^T)
-      float Kd[3];
-#pragma unroll
-      for (int a = 0; a < 3; ++a) Kd[a] = R[a] * M[a] + R[3 + a] * M[3 + a] + R[6 + a] * M[6 + a];
-      const float4 q = quat_normalize(quat_from_rowmajor(R));
-      float sc[3];
-#pragma unroll
-      for (int a = 0; a < 3; ++a) {
-        const float s0 = s0v[a];
-        sc[a] = Kd[a] / ((s0 + 1e-3f) * 2.0f) * s0;
-      }
-      pos_out[3 * (size_t)i] = cx;
-      pos_out[3 * (size_t)i + 1] = cy;
-      pos_out[3 * (size_t)i + 2] = cz;
-      scale_out[3 * (size_t)i] = sc[0];
-      scale_out[3 * (size_t)i + 1] = sc[1];
-      scale_out[3 * (size_t)i + 2] = sc[2];
-      const float4 q_old = s_q[t];
-      reinterpret_cast<float4*>(rot_inout)[i] = q;
-      if (cov_out) {
-        float Rq[9];
-        quat_to_rowmajor(q, Rq);
-        const float s2[3] = {sc[0] * sc[0], sc[1] * sc[1], sc[2] * sc[2]};
-        float S[6];
-        int o = 0;
-#pragma unroll
-        for (int r = 0; r < 3; ++r)
-#pragma unroll
-          for (int c = r; c < 3; ++c)
-            S[o++] = Rq[r * 3] * s2[0] * Rq[c * 3] + Rq[r * 3 + 1] * s2[1] * Rq[c * 3 + 1] +
-                     Rq[r * 3 + 2] * s2[2] * Rq[c * 3 + 2];
-#pragma unroll
-        for (int q6 = 0; q6 < 6; ++q6) cov_out[6 * (size_t)i + q6] = S[q6];
-      }
-      if (shs) {
-        const float4 qr = quat_normalize(quat_mul(q, quat_inverse(q_old)));
-        float Rr[9];
-        quat_to_rowmajor(qr, Rr);
-        float4* rec = reinterpret_cast<float4*>(s_sh + t * kShStride);
-        float v[48];
-#pragma unroll
-        for (int q4 = 0; q4 < 12; ++q4) {
-          const float4 u = rec[q4];
-          v[4 * q4] = u.x;
-          v[4 * q4 + 1] = u.y;
-          v[4 * q4 + 2] = u.z;
-          v[4 * q4 + 3] = u.w;
-        }
-        rotate_sh48<true>(Rr, v);
-#pragma unroll
-        for (int q4 = 0; q4 < 12; ++q4) rec[q4] = make_float4(v[4 * q4], v[4 * q4 + 1], v[4 * q4 + 2], v[4 * q4 + 3]);
-      }
-    }
+  if (active && !is_static) {
+    float Rr[9];
+    refit_gaussian<MIXED>(i, e, s0v, s_q[t], pos_out, rot_inout, scale_out, cov_out, status, Rr);
+    if (shs) rotate_sh_record(s_sh + t * kShStride, Rr);
   }
   if (shs) {
     __syncthreads();
-    float4* dst = reinterpret_cast<float4*>(shs + 48 * (size_t)tile0);
-    for (int q = t; q < 12 * cnt; q += kSkinThreads)
-      __stcs(dst + q, *reinterpret_cast<const float4*>(s_sh + (q / 12) * kShStride + (q % 12) * 4));
+    store_sh(shs, s_sh, tile0, cnt);
+  }
+}
+
+// ---- planned skinning
+// Skinning plan (set-up time, arap_skin_plan_create): per tile of kSkinTile
+// Gaussians the distinct nodes its endpoints blend (at most kPlanNodes), and
+// one contiguous block of the tile's weights and 8-bit local node indices in
+// the order the frame kernel reads them: weights as float4 [6][KQ][T]
+// (neighbours 4q..4q+3 of endpoint ep of Gaussian t), local indices as
+// 32-bit words [6][KQ][T] (four per word), KQ = ceil(K/4).  A frame copies the
+// block into shared memory with one bulk copy (TMA) and its node records
+// once; thread t then reads its weights and indices conflict-free and gathers
+// the node records from shared memory.
+constexpr int kPlanNodes = 256;
+constexpr int kPlanRec = 12;  // floats per staged node record (NodeAf; the 48-byte stride spreads banks)
+struct SkinPlanDev {
+  const int32_t* tile_count;  // [tiles] distinct nodes of the tile (> kPlanNodes: no local list)
+  const int32_t* tile_nodes;  // [tiles][kPlanNodes]
+  const unsigned char* blk;   // [tiles][tile_bytes]: weights then local indices
+};
+template <int K>
+struct PlanTile {
+  static constexpr int KQ = (K + 3) / 4;
+  static constexpr int kWBytes = 6 * KQ * kSkinTile * 16;
+  static constexpr int kLBytes = 6 * KQ * kSkinTile * 4;
+  static constexpr int kBytes = kWBytes + kLBytes;
+  static constexpr int kShBytes = kSkinTile * kShStride * 4;
+  // region A holds the plan block during the blend, the SH records after it
+  static constexpr int kRegionA = kBytes > kShBytes ? kBytes : kShBytes;
+  static constexpr int kQOff = kRegionA;
+  static constexpr int kNodeOff = kQOff + kSkinTile * 16;
+  static constexpr int kBarOff = kNodeOff + kPlanNodes * kPlanRec * 4;
+  static constexpr int kSmem = kBarOff + 16;
+};
+inline int plan_tile_bytes(int k) { return 6 * ((k + 3) / 4) * kSkinTile * 20; }
+
+// The planned frame kernel.  Per tile: one thread starts two bulk copies (the
+// tile's plan block and its previous quaternions) on an mbarrier; meanwhile
+// every thread requests its endpoints and the tile's node records are put
+// into tile-local affine form in shared memory.  The blend reads everything
+// from shared memory; its region then takes the tile's SH records
+// (cp.async), which arrive while the refit runs.  A tile with more than
+// kPlanNodes nodes gathers from the table as the unplanned kernel does.
+template <int K, bool MIXED>
+__global__ void __launch_bounds__(kSkinThreads, 4)
+    skin_gaussians_planned_kernel(int N, float* __restrict__ ends, const int32_t* __restrict__ eidx,
+                                  const float* __restrict__ ew, const float* __restrict__ table,
+                                  const float* __restrict__ scale0, const uint8_t* __restrict__ static_mask,
+                                  float* __restrict__ pos_out, float* __restrict__ rot_inout,
+                                  float* __restrict__ scale_out, float* __restrict__ shs,
+                                  float* __restrict__ cov_out, SkinPlanDev plan, int* __restrict__ status) {
+  using PT = PlanTile<K>;
+  constexpr int KQ = PT::KQ;
+  extern __shared__ __align__(128) unsigned char s_buf[];
+  const float4* s_w = reinterpret_cast<const float4*>(s_buf);                       // [6][KQ][T]
+  const uint32_t* s_l = reinterpret_cast<const uint32_t*>(s_buf + PT::kWBytes);    // [6][KQ][T]
+  float* s_sh = reinterpret_cast<float*>(s_buf);                                    // [T][52], after the blend
+  const float4* s_q = reinterpret_cast<const float4*>(s_buf + PT::kQOff);          // [T]
+  float* s_nodes = reinterpret_cast<float*>(s_buf + PT::kNodeOff);                  // [kPlanNodes][12]
+  const uint32_t bar = smem_addr(s_buf + PT::kBarOff);
+  const int t = threadIdx.x;
+  const int tile0 = blockIdx.x * kSkinTile;
+  const int cnt = min(kSkinTile, N - tile0);
+  const int i = tile0 + t;
+  const bool active = t < cnt;
+  const int n_local = __ldg(plan.tile_count + blockIdx.x);
+  const bool local = n_local <= kPlanNodes;
+  if (t == 0) mbar_init(bar, 1);
+  __syncthreads();
+  if (t == 0) {
+    const uint32_t qb = 16u * (uint32_t)cnt;
+    mbar_arrive_expect_tx(bar, qb + (local ? (uint32_t)PT::kBytes : 0u));
+    bulk_g2s(smem_addr(s_buf + PT::kQOff), rot_inout + 4 * (size_t)tile0, qb, bar);
+    if (local) bulk_g2s(smem_addr(s_buf), plan.blk + (size_t)blockIdx.x * PT::kBytes, PT::kBytes, bar);
+  }
+  const float o_x = __ldg(ends + tile0), o_y = __ldg(ends + (size_t)N + tile0),
+              o_z = __ldg(ends + 2 * (size_t)N + tile0);
+  float e[18];
+  float s0v[3] = {0.f, 0.f, 0.f};
+  const bool is_static = active && static_mask && __ldg(static_mask + i);
+  if (active) {
+#pragma unroll
+    for (int c = 0; c < 18; ++c) e[c] = __ldcs(ends + (size_t)c * N + i);
+#pragma unroll
+    for (int a = 0; a < 3; ++a) s0v[a] = __ldg(scale0 + 3 * (size_t)i + a);
+  }
+  if (local) {
+    const int32_t* list = plan.tile_nodes + (size_t)blockIdx.x * kPlanNodes;
+    for (int u = t; u < n_local; u += kSkinThreads) {
+      const NodeAf r = node_affine(load_node(table, __ldg(list + u)), o_x, o_y, o_z);
+      float4* d4 = reinterpret_cast<float4*>(s_nodes + u * kPlanRec);
+      d4[0] = r.a;
+      d4[1] = r.b;
+      d4[2] = r.c;
+    }
+  }
+  // node records written; every thread waits for the bulk copies itself
+  __syncthreads();
+  const bool arrived = mbar_wait(bar, 0u, kMbarPolls);
+  if (__syncthreads_or(!arrived)) {
+    if (t == 0) raise_status(status, ARAP_ETIMEOUT);
+    return;
+  }
+  if (active) {
+#pragma unroll
+    for (int ep = 0; ep < 6; ++ep) {
+      float ox = 0.f, oy = 0.f, oz = 0.f, ws = 0.f;
+      const float dx = e[3 * ep] - o_x, dy = e[3 * ep + 1] - o_y, dz = e[3 * ep + 2] - o_z;
+#pragma unroll
+      for (int q = 0; q < KQ; ++q) {
+        float4 w4 = make_float4(0.f, 0.f, 0.f, 0.f);
+        uint32_t lw = 0u;
+        if (local) {
+          w4 = s_w[(ep * KQ + q) * kSkinTile + t];
+          lw = s_l[(ep * KQ + q) * kSkinTile + t];
+        }
+        const float wq[4] = {w4.x, w4.y, w4.z, w4.w};
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+          const int j = 4 * q + r;
+          if (j < K) {
+            NodeAf x;
+            float w;
+            if (local) {
+              const float4* r4 = reinterpret_cast<const float4*>(s_nodes + ((lw >> (8 * r)) & 0xffu) * kPlanRec);
+              x.a = r4[0];
+              x.b = r4[1];
+              x.c = r4[2];
+              w = wq[r];
+            } else {
+              x = node_affine(load_node(table, __ldcs(eidx + (size_t)(j * 6 + ep) * N + i)), o_x, o_y, o_z);
+              w = __ldcs(ew + (size_t)(j * 6 + ep) * N + i);
+            }
+            ws += w;
+            ed_term_af(x, w, dx, dy, dz, ox, oy, oz);
+          }
+        }
+      }
+      e[3 * ep] = ed_finish(e[3 * ep], ws, ox);
+      e[3 * ep + 1] = ed_finish(e[3 * ep + 1], ws, oy);
+      e[3 * ep + 2] = ed_finish(e[3 * ep + 2], ws, oz);
+    }
+#pragma unroll
+    for (int c = 0; c < 18; ++c) __stcs(ends + (size_t)c * N + i, e[c]);
+  }
+  // region A: plan block read by every thread; the SH records go there and
+  // arrive while the refit runs
+  __syncthreads();
+  if (shs) stage_sh(s_sh, shs, tile0, cnt);
+  float Rr[9];
+  const bool refit = active && !is_static;
+  if (refit) refit_gaussian<MIXED>(i, e, s0v, s_q[t], pos_out, rot_inout, scale_out, cov_out, status, Rr);
+  if (shs) {
+    asm volatile("cp.async.wait_group 0;" ::: "memory");
+    __syncthreads();
+    if (refit) rotate_sh_record(s_sh + t * kShStride, Rr);
+    __syncthreads();
+    store_sh(shs, s_sh, tile0, cnt);
   }
 }
 
@@ -807,40 +932,56 @@ static int launch_skin_g(bool mixed, int N, float* ends, const int32_t* eidx, co
                          float* rot, float* scale, float* shs, float* cov, const SkinPlanDev& plan, int* status,
                          cudaStream_t s) {
   const int grid = grid_for(N, kSkinTile);
-  constexpr size_t smem = PLANNED ? skin_plan_smem_bytes() : skin_smem_bytes();
-  if (mixed) {
-    if (PLANNED && cudaFuncSetAttribute(skin_gaussians_kernel<K, true, PLANNED>,
-                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+  if (PLANNED) {
+    constexpr int smem = PlanTile<K>::kSmem;
+    auto kern = mixed ? skin_gaussians_planned_kernel<K, true> : skin_gaussians_planned_kernel<K, false>;
+    if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess) {
+      (void)cudaGetLastError();
       return ARAP_ECUDA;
-    skin_gaussians_kernel<K, true, PLANNED><<<grid, kSkinThreads, smem, s>>>(N, ends, eidx, ew, table, scale0, st,
-                                                                              pos, rot, scale, shs, cov, plan,
-                                                                              status);
+    }
+    kern<<<grid, kSkinThreads, smem, s>>>(N, ends, eidx, ew, table, scale0, st, pos, rot, scale, shs, cov, plan,
+                                          status);
   } else {
-    if (PLANNED && cudaFuncSetAttribute(skin_gaussians_kernel<K, false, PLANNED>,
-                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
-      return ARAP_ECUDA;
-    skin_gaussians_kernel<K, false, PLANNED><<<grid, kSkinThreads, smem, s>>>(N, ends, eidx, ew, table, scale0, st,
-                                                                               pos, rot, scale, shs, cov, plan,
-                                                                               status);
+    constexpr size_t smem = skin_smem_bytes();
+    auto kern = mixed ? skin_gaussians_kernel<K, true> : skin_gaussians_kernel<K, false>;
+    kern<<<grid, kSkinThreads, smem, s>>>(N, ends, eidx, ew, table, scale0, st, pos, rot, scale, shs, cov, status);
   }
   return ARAP_OK;
 }
 
 // ---- skinning plan (set-up time)
-// One CTA per tile: the distinct node ids of the tile's endpoint neighbours
-// (shared-memory hash, then ascending order), their count, and each
-// neighbour's 8-bit index into the list, written endpoint-major per Gaussian
-// with the weights.  A tile with more than kPlanNodes distinct nodes keeps
-// only its count; frames then gather its nodes from the global table.
+// One CTA per tile.  It collects the distinct node ids of the tile's endpoint
+// neighbours (shared-memory hash), orders each endpoint's neighbours by node
+// id (the blend is a sum, so the order only changes its rounding), and then
+// chooses each node's local index, that is, where its record sits in shared
+// memory during a frame.  A warp's 128-bit record loads are served eight lanes
+// at a time, and two different records conflict when their local indices are
+// equal mod 8 (records are 48 bytes: bank group (3u + slot) mod 8).  So the
+// local index of a node is col + 8 r, with the colour col in 0..7 chosen
+// greedily (nodes in order of how many others they share a lane group with)
+// to be the colour least used by the nodes already coloured in the lane
+// groups (8 consecutive Gaussians, one endpoint, one neighbour slot) it
+// appears in, at most 32 nodes per colour.  Indices left unused hold a copy
+// of some node of the tile, so every staged record is valid.  The tile's
+// count is then the number of records a frame stages (largest index + 1).
+// A tile with more than kPlanNodes distinct nodes keeps only its count;
+// frames then gather its nodes from the global table in kNN order.
 constexpr int kPlanHash = 2048;
 constexpr int kPlanThreads = 256;
+constexpr int kPlanGroups = kSkinTile / 8;                   // lane groups of a tile
+constexpr int kPlanPhases = kPlanGroups * 6 * ARAP_KNN_MAX;  // (lane group, endpoint, slot)
 __global__ void __launch_bounds__(kPlanThreads)
-    skin_plan_kernel(int N, int K, const int32_t* __restrict__ eidx, const float* __restrict__ ew, int kp,
-                     int32_t* __restrict__ tile_count, int32_t* __restrict__ tile_nodes, uint8_t* __restrict__ lidx,
-                     float* __restrict__ wts) {
+    skin_plan_kernel(int N, int K, const int32_t* __restrict__ eidx, const float* __restrict__ ew,
+                     int32_t* __restrict__ tile_count, int32_t* __restrict__ tile_nodes,
+                     unsigned char* __restrict__ blk, int tile_bytes) {
   __shared__ int s_key[kPlanHash];
-  __shared__ int s_list[kPlanNodes];
-  __shared__ int s_n, s_over;
+  __shared__ int s_list[kPlanNodes];                     // distinct ids, then ascending
+  __shared__ unsigned char s_rk[kSkinTile * 6 * ARAP_KNN_MAX];  // rank of each sorted neighbour
+  __shared__ unsigned char s_ph[kPlanPhases * 8];       // distinct ranks of each lane group's slot
+  __shared__ unsigned char s_phn[kPlanPhases];          // their number
+  __shared__ int s_deg[kPlanNodes], s_order[kPlanNodes], s_col[kPlanNodes], s_lid[kPlanNodes];
+  __shared__ int s_cost[8], s_cap[8];
+  __shared__ int s_n, s_over, s_maxlid;
   const int t = threadIdx.x;
   const int tile0 = blockIdx.x * kSkinTile;
   const int cnt = min(kSkinTile, N - tile0);
@@ -848,6 +989,7 @@ __global__ void __launch_bounds__(kPlanThreads)
   if (t == 0) {
     s_n = 0;
     s_over = 0;
+    s_maxlid = 0;
   }
   __syncthreads();
   const int total = cnt * 6 * K;
@@ -871,25 +1013,126 @@ __global__ void __launch_bounds__(kPlanThreads)
   }
   __syncthreads();
   const int n = s_n;
-  if (t == 0) tile_count[blockIdx.x] = (n > kPlanNodes || s_over) ? kPlanNodes + 1 : n;
-  if (n > kPlanNodes || s_over) return;
-  // ascending order of the list (rank by counting), written to the plan
-  for (int a = t; a < n; a += kPlanThreads) {
-    const int v = s_list[a];
-    int rank = 0;
-    for (int b = 0; b < n; ++b) rank += s_list[b] < v;
-    tile_nodes[(size_t)blockIdx.x * kPlanNodes + rank] = v;
+  if (n > kPlanNodes || s_over) {
+    if (t == 0) tile_count[blockIdx.x] = kPlanNodes + 1;
+    return;
+  }
+  // ascending order of the ids (rank by counting; one node per thread)
+  static_assert(kPlanNodes <= kPlanThreads, "one node per thread");
+  const int my_id = t < n ? s_list[t] : -1;
+  int my_rank = 0;
+  if (t < n)
+    for (int b = 0; b < n; ++b) my_rank += s_list[b] < my_id;
+  __syncthreads();
+  if (t < n) s_list[my_rank] = my_id;
+  __syncthreads();
+  // each endpoint's neighbours sorted by id (insertion sort of at most 12);
+  // the weights go to their slots now, the ranks wait for the local indices
+  unsigned char* tb = blk + (size_t)blockIdx.x * tile_bytes;
+  const int KQ = (K + 3) / 4;
+  for (int task = t; task < cnt * 6; task += kPlanThreads) {
+    const int g = task / 6, ep = task % 6;
+    int rk[ARAP_KNN_MAX];
+    float w[ARAP_KNN_MAX];
+    for (int j = 0; j < K; ++j) {
+      const int id = eidx[(size_t)(j * 6 + ep) * N + tile0 + g];
+      int lo = 0, hi = n;  // rank of id in the sorted list
+      while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (s_list[mid] < id) lo = mid + 1; else hi = mid;
+      }
+      const float wj = ew[(size_t)(j * 6 + ep) * N + tile0 + g];
+      int p = j;
+      while (p > 0 && rk[p - 1] > lo) {
+        rk[p] = rk[p - 1];
+        w[p] = w[p - 1];
+        --p;
+      }
+      rk[p] = lo;
+      w[p] = wj;
+    }
+    for (int j = 0; j < K; ++j) {
+      s_rk[(g * 6 + ep) * K + j] = (unsigned char)rk[j];
+      const size_t slot = ((size_t)(ep * KQ + (j >> 2)) * kSkinTile + g) * 4 + (j & 3);
+      reinterpret_cast<float*>(tb)[slot] = w[j];
+    }
+  }
+  for (int a = t; a < kPlanNodes; a += kPlanThreads) {
+    s_deg[a] = 0;
+    s_col[a] = -1;
+  }
+  if (t < 8) s_cap[t] = 0;
+  __syncthreads();
+  // lane groups: the distinct ranks at one slot of one endpoint over 8
+  // consecutive Gaussians, and each node's number of partners in them
+  const int phases = kPlanGroups * 6 * K;
+  for (int p = t; p < phases; p += kPlanThreads) {
+    const int grp = p / (6 * K), r = p % (6 * K), ep = r / K, j = r % K;
+    unsigned char m[8];
+    int nm = 0;
+    for (int l = 0; l < 8; ++l) {
+      const int g = grp * 8 + l;
+      if (g >= cnt) break;
+      const unsigned char v = s_rk[(g * 6 + ep) * K + j];
+      bool seen = false;
+      for (int x = 0; x < nm; ++x) seen |= m[x] == v;
+      if (!seen) m[nm++] = v;
+    }
+    for (int x = 0; x < nm; ++x) s_ph[p * 8 + x] = m[x];
+    s_phn[p] = (unsigned char)nm;
+    for (int x = 0; x < nm; ++x) atomicAdd(&s_deg[m[x]], nm - 1);
   }
   __syncthreads();
-  for (int e = t; e < total; e += kPlanThreads) {
-    const int g = e / (6 * K), c = e % (6 * K);
-    const int j = c / 6, ep = c % 6;
-    const int id = eidx[(size_t)c * N + tile0 + g];
-    int rank = 0;
-    for (int b = 0; b < n; ++b) rank += s_list[b] < id;
-    const size_t o = ((size_t)(tile0 + g) * 6 + ep);
-    lidx[o * kp + j] = (uint8_t)rank;
-    wts[o * K + j] = ew[(size_t)c * N + tile0 + g];
+  // colouring order: most partners first, ties by rank
+  for (int a = t; a < n; a += kPlanThreads) {
+    int pos = 0;
+    for (int b = 0; b < n; ++b) pos += s_deg[b] > s_deg[a] || (s_deg[b] == s_deg[a] && b < a);
+    s_order[pos] = a;
+  }
+  __syncthreads();
+  for (int s = 0; s < n; ++s) {
+    const int a = s_order[s];
+    if (t < 8) s_cost[t] = 0;
+    __syncthreads();
+    for (int p = t; p < phases; p += kPlanThreads) {
+      const unsigned char* m = s_ph + p * 8;
+      const int nm = s_phn[p];
+      bool has = false;
+      for (int x = 0; x < nm; ++x) has |= m[x] == a;
+      if (has)
+        for (int x = 0; x < nm; ++x)
+          if (m[x] != a && s_col[m[x]] >= 0) atomicAdd(&s_cost[s_col[m[x]]], 1);
+    }
+    __syncthreads();
+    if (t == 0) {
+      int best = -1;
+      for (int c = 0; c < 8; ++c)
+        if (s_cap[c] < kPlanNodes / 8 && (best < 0 || s_cost[c] < s_cost[best])) best = c;
+      s_col[a] = best;
+      s_cap[best] += 1;
+    }
+    __syncthreads();
+  }
+  // local index col + 8 * (position among the nodes of its colour, by rank)
+  for (int a = t; a < n; a += kPlanThreads) {
+    const int c = s_col[a];
+    int r = 0;
+    for (int b = 0; b < a; ++b) r += s_col[b] == c;
+    s_lid[a] = c + 8 * r;
+    atomicMax(&s_maxlid, c + 8 * r);
+  }
+  __syncthreads();
+  const int staged = s_maxlid + 1;
+  int32_t* tn = tile_nodes + (size_t)blockIdx.x * kPlanNodes;
+  for (int u = t; u < staged; u += kPlanThreads) tn[u] = s_list[0];  // unused indices: a valid record
+  __syncthreads();
+  for (int a = t; a < n; a += kPlanThreads) tn[s_lid[a]] = s_list[a];
+  if (t == 0) tile_count[blockIdx.x] = staged;
+  unsigned char* lb = tb + (size_t)6 * KQ * kSkinTile * 16;
+  for (int e = t; e < cnt * 6 * K; e += kPlanThreads) {
+    const int g = e / (6 * K), r = e % (6 * K), ep = r / K, j = r % K;
+    lb[((size_t)(ep * KQ + (j >> 2)) * kSkinTile + g) * 4 + (j & 3)] =
+        (unsigned char)s_lid[s_rk[(g * 6 + ep) * K + j]];
   }
 }
 
@@ -958,7 +1201,7 @@ extern "C" int arap_skin_gaussians(int N, int k, float* ends, const int32_t* end
 }
 
 struct arap_skin_plan {
-  int N = 0, k = 0, tiles = 0, kp = 0, overflow = 0, max_nodes = 0;
+  int N = 0, k = 0, tiles = 0, tile_bytes = 0, overflow = 0, max_nodes = 0;
   void* block = nullptr;
   SkinPlanDev dev{};
   int* status = nullptr;  // the plan's device status word (inside block)
@@ -975,12 +1218,11 @@ extern "C" int arap_skin_plan_create(arap_skin_plan** out, int N, int k, const i
   p->N = N;
   p->k = k;
   p->tiles = (N + kSkinTile - 1) / kSkinTile;
-  p->kp = (k + 3) & ~3;
+  p->tile_bytes = plan_tile_bytes(k);
   const size_t b_count = ((sizeof(int32_t) * p->tiles) + 255) & ~size_t(255);
   const size_t b_nodes = ((sizeof(int32_t) * (size_t)p->tiles * kPlanNodes) + 255) & ~size_t(255);
-  const size_t b_lidx = (((size_t)N * 6 * p->kp) + 255) & ~size_t(255);
-  const size_t b_wts = (sizeof(float) * (size_t)N * 6 * k + 255) & ~size_t(255);
-  if (cudaMalloc(&p->block, b_count + b_nodes + b_lidx + b_wts + 256) != cudaSuccess) {
+  const size_t b_blk = ((size_t)p->tiles * p->tile_bytes + 255) & ~size_t(255);
+  if (cudaMalloc(&p->block, b_count + b_nodes + b_blk + 256) != cudaSuccess) {
     (void)cudaGetLastError();
     delete p;
     return ARAP_ENOMEM;
@@ -988,15 +1230,16 @@ extern "C" int arap_skin_plan_create(arap_skin_plan** out, int N, int k, const i
   char* base = static_cast<char*>(p->block);
   int32_t* count = reinterpret_cast<int32_t*>(base);
   int32_t* nodes = reinterpret_cast<int32_t*>(base + b_count);
-  uint8_t* lidx = reinterpret_cast<uint8_t*>(base + b_count + b_nodes);
-  float* wts = reinterpret_cast<float*>(base + b_count + b_nodes + b_lidx);
-  p->dev = SkinPlanDev{count, nodes, lidx, wts, p->kp};
-  p->status = reinterpret_cast<int*>(base + b_count + b_nodes + b_lidx + b_wts);
-  if (cudaMemsetAsync(lidx, 0, b_lidx, st) != cudaSuccess || cudaMemsetAsync(p->status, 0, sizeof(int), st) != cudaSuccess) {
+  unsigned char* blk = reinterpret_cast<unsigned char*>(base + b_count + b_nodes);
+  p->dev = SkinPlanDev{count, nodes, blk};
+  p->status = reinterpret_cast<int*>(base + b_count + b_nodes + b_blk);
+  // padded neighbour slots (k not a multiple of 4) and the rows of a partial
+  // last tile stay zero
+  if (cudaMemsetAsync(blk, 0, b_blk, st) != cudaSuccess || cudaMemsetAsync(p->status, 0, sizeof(int), st) != cudaSuccess) {
     arap_skin_plan_destroy(p);
     return ARAP_ECUDA;
   }
-  skin_plan_kernel<<<p->tiles, kPlanThreads, 0, st>>>(N, k, ends_idx, ends_w, p->kp, count, nodes, lidx, wts);
+  skin_plan_kernel<<<p->tiles, kPlanThreads, 0, st>>>(N, k, ends_idx, ends_w, count, nodes, blk, p->tile_bytes);
   std::vector<int32_t> h(p->tiles);
   if (cudaPeekAtLastError() != cudaSuccess ||
       cudaMemcpyAsync(h.data(), count, sizeof(int32_t) * p->tiles, cudaMemcpyDeviceToHost, st) != cudaSuccess ||

@@ -18,6 +18,11 @@ struct arap_solver {
   int grid = 0;
   void* block = nullptr;  // one device allocation holding everything below
   SolveParams P{};
+  // a configured spin limit: the solve runs on the instance-table kernel as
+  // a batch of one (its barrier waits read the limit); its parameters and
+  // CTA range live here
+  bool checked = false;
+  void* self = nullptr;  // SolveParams, then int cta_first[2]
   std::vector<int32_t> free_host;
   std::vector<int32_t> order_host;  // processing order (free ranks)
   std::vector<int32_t> stage_cost;  // shared-memory bytes of each free node's tables
@@ -416,6 +421,7 @@ extern "C" int arap_solver_create(arap_solver** out, int n, int k, const int32_t
     return ARAP_ECUDA;
   }
   s->grid = std::min(grid, kMaxGridCtas);
+  s->checked = cfg.spin_limit > 0;
 
   // device layout
   auto carve = [&](Carver& cv, SolveParams& P) {
@@ -515,9 +521,18 @@ extern "C" int arap_solver_create(arap_solver** out, int n, int k, const int32_t
   // the barrier record: count, failed and status zeroed, the configured spin limit
   const GridBarrier bar0{0u, 0, (unsigned int)(cfg.spin_limit > 0 ? cfg.spin_limit : kSpinLimit), 0};
   e = e ? e : cudaMemcpyAsync(P.bar, &bar0, sizeof(bar0), cudaMemcpyHostToDevice, st);
+  const int cta_range[2] = {0, s->grid};
+  if (s->checked && e == cudaSuccess) {
+    e = cudaMalloc(&s->self, sizeof(SolveParams) + sizeof(cta_range));
+    e = e ? e
+          : cudaMemcpyAsync(static_cast<char*>(s->self) + sizeof(SolveParams), cta_range, sizeof(cta_range),
+                            cudaMemcpyHostToDevice, st);
+  }
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   if (e != cudaSuccess) {
+    (void)cudaGetLastError();
     cudaFree(s->block);
+    if (s->self) cudaFree(s->self);
     delete s;
     return ARAP_ECUDA;
   }
@@ -546,8 +561,10 @@ extern "C" int arap_solver_create(arap_solver** out, int n, int k, const int32_t
   s->stage_cost = stage_cost;
   s->res_cost = res_cost;
   {
-    const void* fn = cfg.precision == ARAP_PRECISION_MIXED ? (const void*)gn_solve_kernel<double>
-                                                           : (const void*)gn_solve_kernel<float>;
+    const bool mixed = cfg.precision == ARAP_PRECISION_MIXED;
+    const void* fn = s->checked ? (mixed ? (const void*)gn_solve_batch_kernel<double>
+                                         : (const void*)gn_solve_batch_kernel<float>)
+                                : (mixed ? (const void*)gn_solve_kernel<double> : (const void*)gn_solve_kernel<float>);
     const StagePlan sp = plan_stage(s, s->grid, stage_limit(fn));
     P.stage_cap = sp.bytes;
     P.resident = sp.resident;
@@ -594,11 +611,33 @@ static int fill_stats(const arap_solver* s, const double* st8, int dev_status, a
   return status == ARAP_NOT_CONVERGED ? ARAP_OK : status;
 }
 
+// The parameters of a checked solve into its device copy, in stream order
+// (a kernel argument, so that a captured graph replays the values of its
+// capture).
+__global__ void put_params_kernel(SolveParams P, SolveParams* dst) {
+  if (threadIdx.x == 0) *dst = P;
+}
+
 static int launch_solver(arap_solver* s, cudaStream_t st) {
   // count and failed (the first 8 bytes); the spin limit stays
   if (cudaMemsetAsync(s->P.bar, 0, 2 * sizeof(int), st) != cudaSuccess) return ARAP_ECUDA;
-  void* args[] = {&s->P};
   cudaError_t e;
+  if (s->checked) {
+    SolveParams* dp = static_cast<SolveParams*>(s->self);
+    int* cta = reinterpret_cast<int*>(static_cast<char*>(s->self) + sizeof(SolveParams));
+    int one = 1;
+    put_params_kernel<<<1, 32, 0, st>>>(s->P, dp);
+    void* bargs[] = {&dp, &cta, &one};
+    const void* fn = s->cfg.precision == ARAP_PRECISION_MIXED ? (const void*)gn_solve_batch_kernel<double>
+                                                              : (const void*)gn_solve_batch_kernel<float>;
+    e = cudaLaunchCooperativeKernel(fn, s->grid, kSolveThreads, bargs, (size_t)s->P.stage_cap, st);
+    if (e != cudaSuccess) {
+      (void)cudaGetLastError();
+      return ARAP_ECUDA;
+    }
+    return ARAP_OK;
+  }
+  void* args[] = {&s->P};
   if (s->cfg.precision == ARAP_PRECISION_MIXED)
     e = cudaLaunchCooperativeKernel((const void*)gn_solve_kernel<double>, s->grid, kSolveThreads, args,
                                     (size_t)s->P.stage_cap, st);
@@ -675,6 +714,7 @@ extern "C" int arap_solver_free_ids(const arap_solver* s, int32_t* free_ids_host
 extern "C" void arap_solver_destroy(arap_solver* s) {
   if (!s) return;
   if (s->block) cudaFree(s->block);
+  if (s->self) cudaFree(s->self);
   delete s;
 }
 

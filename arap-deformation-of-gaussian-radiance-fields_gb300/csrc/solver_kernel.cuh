@@ -45,7 +45,8 @@ static_assert(kScratchFloats >= kMaxCoarse, "scratch holds the restricted residu
 // one batch per column.  Reads Cw[src] and writes Cw[1-src] (Cinv for the
 // last block), so one grid barrier per block suffices.  Returns false on a
 // barrier failure; *ok = 0 when a pivot was not positive.
-__device__ bool coarse_invert(const SolveParams& P, GridSync& gs, int* ok, float* sm) {
+template <class G>
+__device__ bool coarse_invert(const SolveParams& P, G& gs, int* ok, float* sm) {
   constexpr int KB = kGJBlock, KP = kGJBlock + 1;
   static_assert(KB == 32, "one lane per pivot column");
   float(*pv0)[KP] = reinterpret_cast<float(*)[KP]>(sm);
@@ -157,7 +158,8 @@ __device__ bool coarse_invert(const SolveParams& P, GridSync& gs, int* ok, float
 // staged in shared memory), zero the other restriction buffer, and the group
 // products w_con J_g u_f.  Every thread of the CTA calls it.
 constexpr int kRowVec = (kMaxCoarse / 4 + 31) / 32;  // float4 loads per lane of a row
-__device__ __forceinline__ void coarse_solve(const SolveParams& P, const GridSync& gs, const double* rc,
+template <class G>
+__device__ __forceinline__ void coarse_solve(const SolveParams& P, const G& gs, const double* rc,
                                              double* rc_other, int ok, float* s_rc) {
   const int lane = threadIdx.x & 31;
   const int gw = (int)(gs.bid * blockDim.x + threadIdx.x) >> 5;
@@ -195,7 +197,7 @@ __device__ __forceinline__ void coarse_solve(const SolveParams& P, const GridSyn
 
 // The whole solve on a group of nbk co-resident CTAs; bid is this CTA's index
 // in the group.
-template <typename RT>
+template <typename RT, bool kCfgLimit>
 __device__ __forceinline__ void solve_body(const SolveParams& P, int bid, int nbk) {
   __shared__ __align__(16) float s_scratch[kScratchFloats];
   const int lane = threadIdx.x & 31;
@@ -207,7 +209,7 @@ __device__ __forceinline__ void solve_body(const SolveParams& P, int bid, int nb
   // node order position p belongs to CTA p % nbk: the costliest nodes (the
   // order is by cost, descending) are spread over all SMs
   const int wib = threadIdx.x >> 5;
-  GridSync gs{P.bar, P.partials, 0u, (unsigned int)nbk, (unsigned int)bid};
+  GridSyncT<kCfgLimit> gs{P.bar, P.partials, 0u, (unsigned int)nbk, (unsigned int)bid};
   // phase timers, thread 0's only, kept in shared memory rather than registers
   // that would stay live through the whole kernel.  acc: prep, grad, coarse,
   // pcg, line search, inversion (ns).  work: PCG work of this CTA per phase
@@ -816,12 +818,14 @@ __device__ __forceinline__ void solve_body(const SolveParams& P, int bid, int nb
 
 template <typename RT>
 __global__ void __launch_bounds__(kSolveThreads) gn_solve_kernel(SolveParams P) {
-  solve_body<RT>(P, blockIdx.x, gridDim.x);
+  solve_body<RT, false>(P, blockIdx.x, gridDim.x);
 }
 
 // Batched solves: CTAs cta_first[i] .. cta_first[i+1]-1 of the cooperative
 // grid run instance i with their own barrier; the instance's parameters are
-// copied into shared memory.
+// copied into shared memory.  Its barrier waits take each instance's
+// configured spin limit, so a single solver with a spin limit of its own runs
+// here as a batch of one.
 template <typename RT>
 __global__ void __launch_bounds__(kSolveThreads)
     gn_solve_batch_kernel(const SolveParams* __restrict__ params, const int* __restrict__ cta_first, int count) {
@@ -840,7 +844,7 @@ __global__ void __launch_bounds__(kSolveThreads)
     for (int q = threadIdx.x; q < (int)(sizeof(SolveParams) / sizeof(int)); q += blockDim.x) dst[q] = src[q];
   }
   __syncthreads();
-  solve_body<RT>(s_P, (int)blockIdx.x - cta_first[i], cta_first[i + 1] - cta_first[i]);
+  solve_body<RT, true>(s_P, (int)blockIdx.x - cta_first[i], cta_first[i + 1] - cta_first[i]);
 }
 
 }  // namespace arap

@@ -315,7 +315,8 @@ def skin_gaussians(ends, ends_idx, ends_w, table, scale0, pos_out, rot_inout, sc
 class SkinPlan:
     """Set-up-time layout of the endpoint kNN for skin_gaussians_planned
     (arap_skin_plan_*): per tile of 128 Gaussians its distinct nodes and
-    8-bit local indices, weights contiguous per Gaussian."""
+    8-bit slot indices of its staged node records (chosen to spread shared-
+    memory banks) and its weights, one contiguous block per tile."""
 
     def __init__(self, ends_idx, ends_w):
         self.k, self.N = int(ends_idx.shape[0]), int(ends_idx.shape[1]) // 6

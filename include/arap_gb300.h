@@ -93,7 +93,9 @@ typedef struct {
                              at most 80 aggregates (960 coarse unknowns). */
   int spin_limit;         /* polls of one grid-barrier wait inside the persistent solve
                              before it gives up with ARAP_ETIMEOUT (<=0: 2^23, about
-                             a second); every CTA then leaves the kernel */
+                             a second); every CTA then leaves the kernel.  A solver
+                             with a limit of its own runs on the batched-solve kernel
+                             as a batch of one (the same results, a little slower) */
 } arap_solve_config;
 
 typedef struct {
@@ -259,27 +261,30 @@ int arap_skin_gaussians(int N, int k, float* ends, const int32_t* ends_idx,
 /* Skinning plan: no counterpart in the reference; a set-up-time layout of
  * the endpoint kNN for arap_skin_gaussians_planned.
  * - Per tile of 128 Gaussians it keeps the distinct nodes the tile's endpoints
- *   blend (at most 256) and each neighbour as an 8-bit index into that list.
- * - The weights are copied per Gaussian, endpoint-major.
+ *   blend (at most 256), placed in shared-memory slots chosen so that the
+ *   lanes of a warp rarely read two records from one bank, and each
+ *   neighbour as an 8-bit slot index.
+ * - Each endpoint's neighbours are ordered by node id; the tile's weights and
+ *   slot indices form one contiguous block in the order a frame reads them.
  * Build it once after arap_compute_weights of the endpoints, and again
  * whenever ends_idx/ends_w or the Gaussian order change. Synchronises. */
 typedef struct arap_skin_plan arap_skin_plan;
 int arap_skin_plan_create(arap_skin_plan** out, int N, int k, const int32_t* ends_idx,
                           const float* ends_w, arap_stream_t stream);
 /* tiles; tiles with more than 256 distinct nodes (skinned from the global table);
- * the largest distinct-node count of the other tiles. */
+ * the most node records a tile of the others stages (its largest slot + 1). */
 int arap_skin_plan_info(const arap_skin_plan* plan, int* tiles, int* overflow_tiles, int* max_nodes);
 /* Read and clear the device status word of the plan's skinning launches
  * (synchronises the stream). */
 int arap_skin_plan_status(arap_skin_plan* plan, arap_stream_t stream);
 void arap_skin_plan_destroy(arap_skin_plan* plan);
-/* arap_skin_gaussians with the plan's layout and the same results (the same
- * arithmetic in the same order).
- * - A CTA copies its tile's node records into shared memory once.
- * - Each Gaussian reads 8-bit node indices and contiguous weights, not the
- *   int32 and float planes.
- * - ends_idx/ends_w are read only for tiles over 256 nodes. N and k are the
- *   plan's. */
+/* arap_skin_gaussians with the plan's layout; the same results up to the
+ * rounding of each blend's sum (its terms are added in node-id order, not
+ * kNN order).
+ * - A CTA copies its tile's block of weights and indices into shared memory
+ *   with one bulk copy (TMA) and its node records once.
+ * - ends_idx/ends_w are read only for tiles over 256 nodes (in kNN order, as
+ *   arap_skin_gaussians). N and k are the plan's. */
 int arap_skin_gaussians_planned(const arap_skin_plan* plan, float* ends, const int32_t* ends_idx,
                                 const float* ends_w, const float* node_table, const float* scale0,
                                 const uint8_t* static_mask, float* pos_out, float* rot_inout,
