@@ -44,10 +44,11 @@ class SolveStats(C.Structure):
                 ("halvings", C.c_int), ("initial_energy", C.c_double), ("final_energy", C.c_double),
                 ("n_free", C.c_int), ("n_static", C.c_int), ("n_rows", C.c_int),
                 ("n_coarse", C.c_int), ("phase_ms", C.c_double * 9), ("resident", C.c_int),
-                ("coarse_fallbacks", C.c_int)]
+                ("coarse_fallbacks", C.c_int), ("iteration_halvings", C.c_int * 64)]
 
     def as_dict(self):
         d = {f: getattr(self, f) for f, _ in self._fields_}
+        d["iteration_halvings"] = list(self.iteration_halvings)[:max(0, min(64, self.gn_iterations))]
         d["phase_ms"] = dict(zip(("setup", "gradient", "coarse", "pcg", "line_search", "coarse_invert",
                                  "pcg_spmv_work", "pcg_update_work", "pcg_coarse_work"), list(self.phase_ms)))
         return d

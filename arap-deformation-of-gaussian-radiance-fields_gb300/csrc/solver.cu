@@ -604,6 +604,11 @@ static int fill_stats(const arap_solver* s, const double* st8, int dev_status, a
   stats_host->n_coarse = s->P.NC;
   stats_host->resident = s->P.resident ? 1 : 0;
   stats_host->coarse_fallbacks = (int)st8[ST_CFALL];
+  {
+    const int n_it = std::min((int)st8[ST_ITERS], kHalvIters);
+    for (int it = 0; it < n_it; ++it)
+      stats_host->iteration_halvings[it] = (int)(st8[ST_HALV_IT + it] - (it ? st8[ST_HALV_IT + it - 1] : 0.0));
+  }
   int status = dev_status;
   if (status == ARAP_OK && s->cfg.early_exit && st8[ST_CONV] == 0.0 && s->cfg.max_iters > 0)
     status = ARAP_NOT_CONVERGED;

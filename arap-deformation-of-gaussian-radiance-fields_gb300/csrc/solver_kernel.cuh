@@ -18,7 +18,9 @@ enum {
   ST_T_PREP = 8, ST_T_GRAD = 9, ST_T_COARSE = 10, ST_T_PCG = 11, ST_T_LS = 12, ST_T_CINV = 13,
   ST_T_W_SPMV = 14, ST_T_W_UPD = 15, ST_T_W_CSOLVE = 16, ST_CFALL = 17
 };
-constexpr int kStatSlots = 24;
+constexpr int ST_HALV_IT = 24;  // cumulative halvings after each of the first kHalvIters GN iterations
+constexpr int kHalvIters = 64;
+constexpr int kStatSlots = ST_HALV_IT + kHalvIters;
 
 __device__ __forceinline__ unsigned long long global_ns() {
   unsigned long long t;
@@ -765,6 +767,7 @@ __device__ __forceinline__ void solve_body(const SolveParams& P, int bid, int nb
       }
     }
     const double normh = (double)scale * sqrt(hh);
+    if (gt == 0 && it < kHalvIters) P.stats[ST_HALV_IT + it] = halvings;
     iters = it + 1;
     if (!gs.sync()) return;
     lap(4);

@@ -533,12 +533,16 @@ class GaussianDeformer:
         else:
             raise ValueError(kind)
 
-    def frame(self, stats=False, with_cov=True, skin_events=None):
+    def frame(self, stats=False, with_cov=True, skin_events=None, sample_events=None):
         rot, trans, st = self.solver.solve(self.node_pos, self.aims, self.rot_nodes, self.trans_nodes, stats=stats)
         table = node_table(rot, trans, self.node_pos)
         if self.sample_pos is not None:
             quat = node_quaternions(rot, self.precision, status=self.word) if self.feature is not None else None
+            if sample_events is not None:
+                sample_events[0].record()
             skin_samples(self.sample_pos, self.sample_idx, self.sample_w, table, quat, self.feature, self.s_static)
+            if sample_events is not None:
+                sample_events[1].record()
         if skin_events is not None:
             skin_events[0].record()
         if self.skin_plan is not None:

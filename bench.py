@@ -44,6 +44,9 @@ def _args():
     ap.add_argument("--form", default="chosen", choices=["plain", "chosen"],
                     help="chosen: FP64 residual/gradient + two-level PCG; plain: FP32 + block-Jacobi PCG")
     ap.add_argument("--coarse-nodes", type=int, default=64)
+    ap.add_argument("--other-forms", default="plain,plain2l",
+                    help="forms also timed on the same state (comma list of plain, plain2l, chosen; "
+                         "plain2l: FP32 residual/gradient with the two-level PCG); empty: none")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-samples", action="store_true")
     ap.add_argument("--batch", type=int, default=64,
@@ -133,8 +136,14 @@ def op_text(op):
 
 
 def solve_config(dev, sc, form, coarse_nodes):
+    """chosen: FP64 residual, gradient and energy with the two-level PCG;
+    plain: FP32 with block-Jacobi alone (the straightforward port); plain2l:
+    FP32 with the two-level PCG (what the precision choices add on their
+    own)."""
     if form == "chosen":
         return dev.default_config(max_iters=sc.iters, early_exit=0, precision=1, coarse_nodes=coarse_nodes)
+    if form == "plain2l":
+        return dev.default_config(max_iters=sc.iters, early_exit=0, precision=0, coarse_nodes=coarse_nodes)
     return dev.default_config(max_iters=sc.iters, early_exit=0, precision=0, coarse_nodes=0)
 
 
@@ -185,6 +194,20 @@ def restore(st, snap):
 # workload (dram__bytes_read.sum + dram__bytes_write.sum of one launch), keyed
 # by (scene, k, planned).
 SKIN_DRAM_BYTES = {("twist300k", 8, True): 165792000 + 42921728}
+
+
+def samples_roofline(st, k, ms, peak, peak_kind):
+    """The frame's sample skinning launch (arap_skin_samples): per sample
+    position read + write (24), k indices and k weights (8k), the 48-float
+    feature read + write (384)."""
+    if ms is None:
+        return None
+    S = int(st.sample_pos.shape[0])
+    per = 24 + 8 * k + (384 if st.feature is not None else 0)
+    gbs = per * S / (ms * 1e-3) / 1e9
+    return {"kernel": "arap_skin_samples", "bound": "hbm", "samples": S, "bytes_per_sample": per,
+            "bytes_per_launch": per * S, "ms_per_launch": round(ms, 5), "achieved": round(gbs, 1),
+            "peak": peak, "peak_kind": peak_kind, "unit": "GB/s", "frac": round(gbs / peak, 4)}
 
 
 def skin_bytes_per_gaussian(k, with_shs=True, with_cov=True, planned=True):
@@ -427,13 +450,18 @@ def run_ours(a):
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
     s = torch.cuda.current_stream()
 
-    skin_ev = []
+    skin_ev, samp_ev = [], []
 
     def step(record):
         ev = (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) if record else None
-        st.frame(stats=False, with_cov=True, skin_events=ev)
+        sev = None
+        if record and st.sample_pos is not None:
+            sev = (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+        st.frame(stats=False, with_cov=True, skin_events=ev, sample_events=sev)
         if record:
             skin_ev.append(ev)
+            if sev is not None:
+                samp_ev.append(sev)
 
     for _ in range(max(3, a.warmup)):
         restore(st, snap)
@@ -462,6 +490,7 @@ def run_ours(a):
     ms = [a0.elapsed_time(b0) for a0, b0 in step_ev]
     ms_step = reduce_max(float(np.mean(ms)), ws)
     skin_ms = float(np.mean([a0.elapsed_time(b0) for a0, b0 in skin_ev]))
+    samp_ms = float(np.mean([a0.elapsed_time(b0) for a0, b0 in samp_ev])) if samp_ev else None
     status = st.status()
 
     # e2e: public API with host buffers (aims H2D, node transforms + energy D2H)
@@ -485,28 +514,35 @@ def run_ours(a):
     restore(st, snap)
     stats = st.frame(stats=True)
     torch.cuda.synchronize()
-    # the other form on the same state, same steps
-    other = "plain" if a.form == "chosen" else "chosen"
-    st.solver = dev.Solver(st.neighbors, st.anchor_idx, st.anchor_w, st.blocks, st.block_type,
-                           config=solve_config(dev, sc, other, a.coarse_nodes))
-    st.precision = st.solver.config.precision
-    for _ in range(2):
+    # the other forms on the same state, same steps
+    forms = {a.form: {"ms_per_frame": round(ms_step, 3), "pcg_iterations": stats["pcg_iterations"]}}
+    for other in [f for f in a.other_forms.split(",") if f and f != a.form]:
+        st.solver = dev.Solver(st.neighbors, st.anchor_idx, st.anchor_w, st.blocks, st.block_type,
+                               config=solve_config(dev, sc, other, a.coarse_nodes))
+        st.precision = st.solver.config.precision
+        for _ in range(2):
+            restore(st, snap)
+            st.frame(stats=False)
+        o_ms = []
+        for _ in range(max(2, a.steps // 2)):
+            restore(st, snap)
+            flush.fill_(1.0)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(s)
+            st.frame(stats=False)
+            e1.record(s)
+            torch.cuda.synchronize()
+            o_ms.append(e0.elapsed_time(e1))
         restore(st, snap)
-        st.frame(stats=False)
-    o_ms = []
-    for _ in range(max(2, a.steps // 2)):
-        restore(st, snap)
-        flush.fill_(1.0)
-        e0 = torch.cuda.Event(enable_timing=True)
-        e1 = torch.cuda.Event(enable_timing=True)
-        e0.record(s)
-        st.frame(stats=False)
-        e1.record(s)
+        o_stats = st.frame(stats=True)
         torch.cuda.synchronize()
-        o_ms.append(e0.elapsed_time(e1))
-    restore(st, snap)
-    o_stats = st.frame(stats=True)
-    torch.cuda.synchronize()
+        forms[other] = {"ms_per_frame": round(float(np.mean(o_ms)), 3), "pcg_iterations": o_stats["pcg_iterations"]}
+    if "chosen" in forms and "plain" in forms:
+        forms["chosen_speedup_over_plain"] = round(forms["plain"]["ms_per_frame"] / forms["chosen"]["ms_per_frame"], 3)
+    if "chosen" in forms and "plain2l" in forms:
+        forms["chosen_speedup_over_plain2l"] = round(forms["plain2l"]["ms_per_frame"] /
+                                                     forms["chosen"]["ms_per_frame"], 3)
 
     peak, peak_kind = _peaks()
     k = sc.k
@@ -542,17 +578,14 @@ def run_ours(a):
                      "traffic_source": "ncu dram__bytes_read.sum + "
                      "dram__bytes_write.sum, one launch (profiles/skin_gaussians_twist300k.md)",
                      "bytes_per_launch": bytes_launch, "ms_per_launch": round(skin_ms, 5)},
+        "roofline_samples": samples_roofline(st, k, samp_ms, peak, peak_kind),
         "gpu_launches": launches_per_step * a.steps,
         "solve": {"bound": "latency (L2-resident persistent kernel; reported per PCG iteration)",
                   "pcg_iterations": stats["pcg_iterations"], "gn_iterations": stats["gn_iterations"],
                   "us_per_pcg_iteration": round(1000.0 * stats["phase_ms"]["pcg"] / max(1, stats["pcg_iterations"]), 2),
                   "phase_ms": {k: round(v, 3) for k, v in stats["phase_ms"].items()},
                   "final_energy": stats["final_energy"]},
-        "forms": {a.form: {"ms_per_frame": round(ms_step, 3), "pcg_iterations": stats["pcg_iterations"]},
-                  other: {"ms_per_frame": round(float(np.mean(o_ms)), 3),
-                          "pcg_iterations": o_stats["pcg_iterations"]},
-                  "chosen_speedup_over_plain": round((float(np.mean(o_ms)) / ms_step) if a.form == "chosen"
-                                                     else (ms_step / float(np.mean(o_ms))), 3)},
+        "forms": forms,
         "status": status,
         "clocks": clk.summary(),
     }

@@ -120,6 +120,9 @@ typedef struct {
                              was not positive in float32 (nearly collinear nodes in an
                              aggregate): their PCG ran with block-Jacobi alone, which is
                              slower but still solves the same system */
+  int iteration_halvings[64]; /* line-search step halvings of each of the first 64
+                             Gauss-Newton iterations (Deform.cpp:144-156; 0 past
+                             gn_iterations) */
 } arap_solve_stats;
 
 typedef struct arap_solver arap_solver;

@@ -4,12 +4,14 @@ on the GPU against the float64 oracle.
 * bend50k (50k Gaussians, 32^3 grid, ~1k nodes, k=8, 10 iterations) and
   twist300k (300k Gaussians, 64^3 grid, 4061 nodes, k=8, 20 iterations, the
   benchmarked frame), each in the chosen form (mixed precision, two-level
-  PCG with 64-node aggregates) and the plain form.
+  PCG with 64-node aggregates), the plain form (FP32, block-Jacobi) and
+  FP32 with the two-level PCG (plain2l).
 * Node transforms against the numpy oracle's Gauss-Newton solve of the same
   scene (tests/golden/solve_<scene>.npz, made by
   tests/golden/make_solve_golden.py; exact sparse solve, Deform.cpp:95-169).
-  Tolerance: max |dx| / max |x| <= 1e-5 (chosen), 5e-5 (plain).  The
-  line search's halvings (Deform.cpp:144-156) must agree in total.
+  Tolerance: max |dx| / max |x| <= 1e-5 (chosen), 5e-5 (FP32 forms).  The
+  line search's halvings (Deform.cpp:144-156) must agree in every
+  Gauss-Newton iteration.
 * The frame's outputs (sample positions and features, Gaussian mean,
   quaternion, scale, covariance and SH, node update) against the C++
   restatement of the reference's CPU frame (oracle/cpu_frame.cpp, itself
@@ -70,10 +72,13 @@ def _oracle_frame(d, sc, samples, feature, X):
     return fr, nodes
 
 
-@pytest.mark.parametrize("form", ["chosen", "plain"])
+_FORMS = {"chosen": (1, 64), "plain": (0, 0), "plain2l": (0, 64)}
+
+
+@pytest.mark.parametrize("form", ["chosen", "plain", "plain2l"])
 def test_frame_matches_the_oracle(dev, case, form):
     sc, samples, feature, g = case
-    precision, coarse = (1, 64) if form == "chosen" else (0, 0)
+    precision, coarse = _FORMS[form]
     cfg = dev.default_config(max_iters=sc.iters, early_exit=0, precision=precision, coarse_nodes=coarse)
     d = dev.GaussianDeformer(torch.as_tensor(sc.pos), torch.as_tensor(sc.rot), torch.as_tensor(sc.scale),
                              torch.as_tensor(sc.shs), sc.node_vertex, sc.k, sc.blocks, sc.block_type,
@@ -101,7 +106,14 @@ def test_frame_matches_the_oracle(dev, case, form):
     print("%s %s: pcg %d, halvings %d (oracle %d), errors %s" % (
         sc.name, form, st["pcg_iterations"], st["halvings"], int(g["halvings"].sum()),
         {k: "%.2e" % v for k, v in err.items()}))
-    assert st["halvings"] == int(g["halvings"].sum())
+    if form != "plain2l":
+        # the line search takes the oracle's branch in every Gauss-Newton
+        # iteration.  Not so for FP32 residuals with the two-level PCG: at
+        # bend50k its FP32 energy test halves one step that the float64
+        # energy accepts (x error 1.2e-5), one reason the chosen form keeps
+        # the residual, gradient and energy in FP64
+        assert st["halvings"] == int(g["halvings"].sum())
+        assert st["iteration_halvings"] == [int(v) for v in g["halvings"]]
     assert abs(st["initial_energy"] - g["energies"][0]) <= 1e-5 * g["energies"][0]
     assert err_x <= (1e-5 if form == "chosen" else 5e-5)
     tol = 1e-5 if form == "chosen" else 5e-5
@@ -135,7 +147,7 @@ def test_non_resident_solve_matches_the_oracle(dev, form):
     err = _rel(X, g["x"].astype(np.float64))
     print("stress200k %s: pcg %d, coarse %d, halvings %d (oracle %d), x error %.2e"
           % (form, st["pcg_iterations"], st["n_coarse"], st["halvings"], int(g["halvings"].sum()), err))
-    assert st["halvings"] == int(g["halvings"].sum())
+    assert st["halvings"] == int(g["halvings"].sum())  # the fixture keeps the total only
     assert abs(st["initial_energy"] - g["energies"][0]) <= 1e-5 * g["energies"][0]
     assert err <= (1e-5 if form == "chosen" else 5e-5)
     solver.close()
