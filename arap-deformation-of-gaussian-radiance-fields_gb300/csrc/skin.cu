@@ -764,53 +764,63 @@ __device__ __forceinline__ float4 slerp(float4 s, float4 e, float t) {
 }
 
 // Fused UpdatePositionforSamples (GaussianView.cpp:3060-3077) and RotateSHs
-// (cudakdtree.cu:201-222).
+// (cudakdtree.cu:201-222): one thread per sample, kSkinTile per CTA.  The
+// tile's positions (coalesced loads) and 48-float feature records (16-byte
+// cp.async copies of the contiguous records, padded rows) go through shared
+// memory, so that every global access is coalesced; the feature records
+// arrive while the positions are blended and the node quaternions slerped,
+// are rotated in place and leave with coalesced 16-byte stores.
 template <int K>
 __global__ void __launch_bounds__(kSkinThreads)
     skin_samples_kernel(int S, float* __restrict__ spos, const int32_t* __restrict__ idx,
                         const float* __restrict__ w, const float* __restrict__ table,
                         const float* __restrict__ nquat, float* __restrict__ feature,
                         const uint8_t* __restrict__ static_mask) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= S) return;
-  if (static_mask && static_mask[i]) return;
-  const float px = spos[3 * (size_t)i], py = spos[3 * (size_t)i + 1], pz = spos[3 * (size_t)i + 2];
-  float ox = 0.f, oy = 0.f, oz = 0.f, ws = 0.f;
+  extern __shared__ float4 s_raw4[];
+  float* s_ft = reinterpret_cast<float*>(s_raw4);                  // [T][52] feature records
+  float* s_p = s_ft + (feature ? kSkinTile * kShStride : 0);        // [T * 3] positions
+  const int t = threadIdx.x;
+  const int tile0 = blockIdx.x * kSkinTile;
+  const int cnt = min(kSkinTile, S - tile0);
+  const int i = tile0 + t;
+  if (feature) stage_sh(s_ft, feature, tile0, cnt);
+  for (int q = t; q < 3 * cnt; q += kSkinThreads) s_p[q] = __ldcs(spos + 3 * (size_t)tile0 + q);
+  __syncthreads();
+  const bool moving = t < cnt && !(static_mask && static_mask[i]);
   float4 wq = make_float4(1.f, 0.f, 0.f, 0.f);
-  float last = 0.f;
+  if (moving) {
+    const float px = s_p[3 * t], py = s_p[3 * t + 1], pz = s_p[3 * t + 2];
+    float ox = 0.f, oy = 0.f, oz = 0.f, ws = 0.f;
+    float last = 0.f;
 #pragma unroll
-  for (int j = 0; j < K; ++j) {
-    const int nid = __ldcs(idx + (size_t)j * S + i);
-    const float wj = __ldcs(w + (size_t)j * S + i);
-    const NodeXf x = load_node(table, nid);
-    ws += wj;
-    ed_term(x, wj, px, py, pz, ox, oy, oz);
-    if (feature) {
-      const float t = wj / (wj + last);
-      wq = slerp(wq, __ldg(reinterpret_cast<const float4*>(nquat) + nid), t);
-      last += wj;
+    for (int j = 0; j < K; ++j) {
+      const int nid = __ldcs(idx + (size_t)j * S + i);
+      const float wj = __ldcs(w + (size_t)j * S + i);
+      const NodeXf x = load_node(table, nid);
+      ws += wj;
+      ed_term(x, wj, px, py, pz, ox, oy, oz);
+      if (feature) {
+        const float tj = wj / (wj + last);
+        wq = slerp(wq, __ldg(reinterpret_cast<const float4*>(nquat) + nid), tj);
+        last += wj;
+      }
     }
+    s_p[3 * t] = ed_finish(px, ws, ox);
+    s_p[3 * t + 1] = ed_finish(py, ws, oy);
+    s_p[3 * t + 2] = ed_finish(pz, ws, oz);
   }
-  spos[3 * (size_t)i] = ed_finish(px, ws, ox);
-  spos[3 * (size_t)i + 1] = ed_finish(py, ws, oy);
-  spos[3 * (size_t)i + 2] = ed_finish(pz, ws, oz);
   if (feature) {
-    float Rr[9];
-    quat_to_rowmajor(quat_normalize(wq), Rr);
-    float4* fp = reinterpret_cast<float4*>(feature + 48 * (size_t)i);
-    float v[48];
-#pragma unroll
-    for (int t = 0; t < 12; ++t) {
-      const float4 u = __ldcs(fp + t);
-      v[4 * t] = u.x;
-      v[4 * t + 1] = u.y;
-      v[4 * t + 2] = u.z;
-      v[4 * t + 3] = u.w;
+    asm volatile("cp.async.wait_group 0;" ::: "memory");
+    __syncthreads();
+    if (moving) {
+      float Rr[9];
+      quat_to_rowmajor(quat_normalize(wq), Rr);
+      rotate_sh_record(s_ft + t * kShStride, Rr);
     }
-    rotate_sh48<true>(Rr, v);
-#pragma unroll
-    for (int t = 0; t < 12; ++t) __stcs(fp + t, make_float4(v[4 * t], v[4 * t + 1], v[4 * t + 2], v[4 * t + 3]));
   }
+  __syncthreads();
+  for (int q = t; q < 3 * cnt; q += kSkinThreads) __stcs(spos + 3 * (size_t)tile0 + q, s_p[q]);
+  if (feature) store_sh(feature, s_ft, tile0, cnt);
 }
 
 // GaussianView.cpp:3042-3052: next node position from its anchor kNN.
@@ -1140,8 +1150,8 @@ __global__ void __launch_bounds__(kPlanThreads)
 template <int K>
 static void launch_skin_s(int S, float* spos, const int32_t* idx, const float* w, const float* table,
                           const float* nq, float* feat, const uint8_t* st, cudaStream_t s) {
-  skin_samples_kernel<K><<<grid_for(S, kSkinThreads), kSkinThreads, 0, s>>>(S, spos, idx, w, table, nq,
-                                                                            feat, st);
+  const size_t smem = sizeof(float) * ((feat ? (size_t)kSkinTile * kShStride : 0) + 3 * (size_t)kSkinTile);
+  skin_samples_kernel<K><<<grid_for(S, kSkinTile), kSkinThreads, smem, s>>>(S, spos, idx, w, table, nq, feat, st);
 }
 
 }  // namespace arap

@@ -190,13 +190,15 @@ def restore(st, snap):
         getattr(st, n).copy_(t)
 
 
-# DRAM bytes per launch of skin_gaussians_kernel measured by ncu on the named
-# workload (dram__bytes_read.sum + dram__bytes_write.sum of one launch), keyed
-# by (scene, k, planned).
-SKIN_DRAM_BYTES = {("twist300k", 8, True): 165792000 + 42921728}
+# DRAM bytes per launch measured by ncu on the named workload
+# (dram__bytes_read.sum + dram__bytes_write.sum of one launch inside the
+# bench's frame), keyed by (scene, k, planned) for the Gaussian skinning and
+# (scene, k) for the sample skinning.
+SKIN_DRAM_BYTES = {("twist300k", 8, True): 161548032 + 43893504}
+SAMPLES_DRAM_BYTES = {("twist300k", 8): 413570304 + 252652544}
 
 
-def samples_roofline(st, k, ms, peak, peak_kind):
+def samples_roofline(st, k, ms, peak, peak_kind, traffic=None):
     """The frame's sample skinning launch (arap_skin_samples): per sample
     position read + write (24), k indices and k weights (8k), the 48-float
     feature read + write (384)."""
@@ -207,7 +209,9 @@ def samples_roofline(st, k, ms, peak, peak_kind):
     gbs = per * S / (ms * 1e-3) / 1e9
     return {"kernel": "arap_skin_samples", "bound": "hbm", "samples": S, "bytes_per_sample": per,
             "bytes_per_launch": per * S, "ms_per_launch": round(ms, 5), "achieved": round(gbs, 1),
-            "peak": peak, "peak_kind": peak_kind, "unit": "GB/s", "frac": round(gbs / peak, 4)}
+            "peak": peak, "peak_kind": peak_kind, "unit": "GB/s", "frac": round(gbs / peak, 4),
+            "traffic": traffic, "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum, one launch "
+            "(profiles/skin_samples_twist300k.md)" if traffic else None}
 
 
 def skin_bytes_per_gaussian(k, with_shs=True, with_cov=True, planned=True):
@@ -516,6 +520,7 @@ def run_ours(a):
     torch.cuda.synchronize()
     # the other forms on the same state, same steps
     forms = {a.form: {"ms_per_frame": round(ms_step, 3), "pcg_iterations": stats["pcg_iterations"]}}
+    main_solver, main_precision = st.solver, st.precision
     for other in [f for f in a.other_forms.split(",") if f and f != a.form]:
         st.solver = dev.Solver(st.neighbors, st.anchor_idx, st.anchor_w, st.blocks, st.block_type,
                                config=solve_config(dev, sc, other, a.coarse_nodes))
@@ -538,6 +543,7 @@ def run_ours(a):
         o_stats = st.frame(stats=True)
         torch.cuda.synchronize()
         forms[other] = {"ms_per_frame": round(float(np.mean(o_ms)), 3), "pcg_iterations": o_stats["pcg_iterations"]}
+    st.solver, st.precision = main_solver, main_precision  # the adjoint block uses the benched form
     if "chosen" in forms and "plain" in forms:
         forms["chosen_speedup_over_plain"] = round(forms["plain"]["ms_per_frame"] / forms["chosen"]["ms_per_frame"], 3)
     if "chosen" in forms and "plain2l" in forms:
@@ -578,7 +584,8 @@ def run_ours(a):
                      "traffic_source": "ncu dram__bytes_read.sum + "
                      "dram__bytes_write.sum, one launch (profiles/skin_gaussians_twist300k.md)",
                      "bytes_per_launch": bytes_launch, "ms_per_launch": round(skin_ms, 5)},
-        "roofline_samples": samples_roofline(st, k, samp_ms, peak, peak_kind),
+        "roofline_samples": samples_roofline(st, k, samp_ms, peak, peak_kind,
+                                             SAMPLES_DRAM_BYTES.get((sc.name, k))),
         "gpu_launches": launches_per_step * a.steps,
         "solve": {"bound": "latency (L2-resident persistent kernel; reported per PCG iteration)",
                   "pcg_iterations": stats["pcg_iterations"], "gn_iterations": stats["gn_iterations"],
