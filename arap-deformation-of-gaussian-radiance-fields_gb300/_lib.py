@@ -85,6 +85,7 @@ SIGNATURES = {
     "arap_skin_plan_destroy": (None, [P]),
     "arap_skin_gaussians_planned": (I, [P, P, P, P, P, P, P, P, P, P, P, P, I, P]),
     "arap_skin_gaussians_backward": (I, [I, I, P, P, P, P, P, P, P, P, P, P, P]),
+    "arap_skin_gaussians_backward_planned": (I, [P, P, P, P, P, P, P, P, P, P, P]),
     "arap_node_quaternions": (I, [I, P, P, I, P, P]),
     "arap_skin_samples": (I, [I, I, P, P, P, P, P, P, P, P]),
     "arap_update_nodes": (I, [I, I, P, P, P, P, P, P]),

@@ -384,6 +384,10 @@ struct SkinPlanDev {
   const int32_t* tile_count;  // [tiles] distinct nodes of the tile (> kPlanNodes: no local list)
   const int32_t* tile_nodes;  // [tiles][kPlanNodes]
   const unsigned char* blk;   // [tiles][tile_bytes]: weights then local indices
+  // for the adjoint: per tile, the references of each slot u (ref = (g * 6 +
+  // ep) * K + j, ascending) at inv_ref[inv_off[u] .. inv_off[u + 1])
+  const uint16_t* inv_off;    // [tiles][kPlanNodes + 1]
+  const uint16_t* inv_ref;    // [tiles][6 * K * kSkinTile]
 };
 template <int K>
 struct PlanTile {
@@ -556,6 +560,87 @@ __device__ __forceinline__ void hash_add(int* keys, float (*vals)[12], int nid, 
   for (int c = 0; c < 12; ++c) atomicAdd(grad_node + 12 * (size_t)nid + c, v[c]);
 }
 
+// The adjoint chain of one Gaussian from its endpoint matrix M and polar
+// factor R to the gradients gP [18] of its six blended endpoints (the
+// formulas above).
+__device__ __forceinline__ void skin_adjoint_gP(int i, const float (&M)[9], const float (&R)[9],
+                                                const float* __restrict__ scale0,
+                                                const float* __restrict__ grad_pos,
+                                                const float* __restrict__ grad_cov, float (&gP)[18]) {
+  float S[9];  // R^T M, symmetrised
+#pragma unroll
+  for (int a = 0; a < 3; ++a)
+#pragma unroll
+    for (int b = 0; b < 3; ++b) S[a * 3 + b] = R[a] * M[b] + R[3 + a] * M[3 + b] + R[6 + a] * M[6 + b];
+#pragma unroll
+  for (int a = 0; a < 3; ++a)
+#pragma unroll
+    for (int b = a + 1; b < 3; ++b) S[a * 3 + b] = S[b * 3 + a] = 0.5f * (S[a * 3 + b] + S[b * 3 + a]);
+  float cK[3], D[3], Kd[3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    const float s0 = scale0[3 * (size_t)i + a];
+    cK[a] = s0 / ((s0 + 1e-3f) * 2.0f);
+    Kd[a] = R[a] * M[a] + R[3 + a] * M[3 + a] + R[6 + a] * M[6 + a];
+    D[a] = (cK[a] * Kd[a]) * (cK[a] * Kd[a]);
+  }
+  const float* gc = grad_cov + 6 * (size_t)i;
+  const float G[9] = {gc[0], 0.5f * gc[1], 0.5f * gc[2], 0.5f * gc[1], gc[3], 0.5f * gc[4],
+                      0.5f * gc[2], 0.5f * gc[4], gc[5]};
+  float GR[9];  // G R
+#pragma unroll
+  for (int r = 0; r < 3; ++r)
+#pragma unroll
+    for (int a = 0; a < 3; ++a) GR[r * 3 + a] = G[r * 3] * R[a] + G[r * 3 + 1] * R[3 + a] + G[r * 3 + 2] * R[6 + a];
+  float gK[3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    const float gD = R[a] * GR[a] + R[3 + a] * GR[3 + a] + R[6 + a] * GR[6 + a];
+    gK[a] = gD * 2.f * cK[a] * cK[a] * Kd[a];
+  }
+  float gR[9], gM[9];
+#pragma unroll
+  for (int r = 0; r < 3; ++r)
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      gR[r * 3 + a] = 2.f * GR[r * 3 + a] * D[a] + M[r * 3 + a] * gK[a];
+      gM[r * 3 + a] = R[r * 3 + a] * gK[a];
+    }
+  float A[9];  // R^T gR
+#pragma unroll
+  for (int a = 0; a < 3; ++a)
+#pragma unroll
+    for (int b = 0; b < 3; ++b) A[a * 3 + b] = R[a] * gR[b] + R[3 + a] * gR[3 + b] + R[6 + a] * gR[6 + b];
+  const float av[3] = {0.5f * (A[7] - A[5]), 0.5f * (A[2] - A[6]), 0.5f * (A[3] - A[1])};
+  const float tr = S[0] + S[4] + S[8];
+  float T[9], Ti[9];
+#pragma unroll
+  for (int q = 0; q < 9; ++q) T[q] = -S[q];
+  T[0] += tr;
+  T[4] += tr;
+  T[8] += tr;
+  float om[3] = {0.f, 0.f, 0.f};
+  if (inv_transpose3(T, Ti)) {  // T symmetric: inverse-transpose = inverse
+#pragma unroll
+    for (int r = 0; r < 3; ++r) om[r] = Ti[r * 3] * av[0] + Ti[r * 3 + 1] * av[1] + Ti[r * 3 + 2] * av[2];
+  }
+  const float Y[9] = {0.f, -om[2], om[1], om[2], 0.f, -om[0], -om[1], om[0], 0.f};
+#pragma unroll
+  for (int r = 0; r < 3; ++r)
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+      gM[r * 3 + a] += 2.f * (R[r * 3] * Y[a] + R[r * 3 + 1] * Y[3 + a] + R[r * 3 + 2] * Y[6 + a]);
+  const float gm[3] = {grad_pos[3 * (size_t)i] * (1.f / 6.f), grad_pos[3 * (size_t)i + 1] * (1.f / 6.f),
+                       grad_pos[3 * (size_t)i + 2] * (1.f / 6.f)};
+#pragma unroll
+  for (int a = 0; a < 3; ++a)
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+      gP[3 * (2 * a) + r] = gm[r] + 0.5f * gM[r * 3 + a];
+      gP[3 * (2 * a + 1) + r] = gm[r] - 0.5f * gM[r * 3 + a];
+    }
+}
+
 template <int K>
 __global__ void __launch_bounds__(kSkinThreads)
     skin_gaussians_backward_kernel(int N, const float* __restrict__ ends_in, const int32_t* __restrict__ eidx,
@@ -598,79 +683,8 @@ __global__ void __launch_bounds__(kSkinThreads)
       for (int r = 0; r < 3; ++r) M[r * 3 + a] = 0.5f * (e[3 * (2 * a) + r] - e[3 * (2 * a + 1) + r]);
     float R[9];
     if (!polar_factor<float>(M, R, 20, 2e-7f)) raise_status(status, ARAP_ENONFINITE);
-    float S[9];  // R^T M, symmetrised
-#pragma unroll
-    for (int a = 0; a < 3; ++a)
-#pragma unroll
-      for (int b = 0; b < 3; ++b) S[a * 3 + b] = R[a] * M[b] + R[3 + a] * M[3 + b] + R[6 + a] * M[6 + b];
-#pragma unroll
-    for (int a = 0; a < 3; ++a)
-#pragma unroll
-      for (int b = a + 1; b < 3; ++b) S[a * 3 + b] = S[b * 3 + a] = 0.5f * (S[a * 3 + b] + S[b * 3 + a]);
-    float cK[3], D[3], Kd[3];
-#pragma unroll
-    for (int a = 0; a < 3; ++a) {
-      const float s0 = scale0[3 * (size_t)i + a];
-      cK[a] = s0 / ((s0 + 1e-3f) * 2.0f);
-      Kd[a] = R[a] * M[a] + R[3 + a] * M[3 + a] + R[6 + a] * M[6 + a];
-      D[a] = (cK[a] * Kd[a]) * (cK[a] * Kd[a]);
-    }
-    const float* gc = grad_cov + 6 * (size_t)i;
-    const float G[9] = {gc[0], 0.5f * gc[1], 0.5f * gc[2], 0.5f * gc[1], gc[3], 0.5f * gc[4],
-                        0.5f * gc[2], 0.5f * gc[4], gc[5]};
-    float GR[9];  // G R
-#pragma unroll
-    for (int r = 0; r < 3; ++r)
-#pragma unroll
-      for (int a = 0; a < 3; ++a) GR[r * 3 + a] = G[r * 3] * R[a] + G[r * 3 + 1] * R[3 + a] + G[r * 3 + 2] * R[6 + a];
-    float gK[3];
-#pragma unroll
-    for (int a = 0; a < 3; ++a) {
-      const float gD = R[a] * GR[a] + R[3 + a] * GR[3 + a] + R[6 + a] * GR[6 + a];
-      gK[a] = gD * 2.f * cK[a] * cK[a] * Kd[a];
-    }
-    float gR[9], gM[9];
-#pragma unroll
-    for (int r = 0; r < 3; ++r)
-#pragma unroll
-      for (int a = 0; a < 3; ++a) {
-        gR[r * 3 + a] = 2.f * GR[r * 3 + a] * D[a] + M[r * 3 + a] * gK[a];
-        gM[r * 3 + a] = R[r * 3 + a] * gK[a];
-      }
-    float A[9];  // R^T gR
-#pragma unroll
-    for (int a = 0; a < 3; ++a)
-#pragma unroll
-      for (int b = 0; b < 3; ++b) A[a * 3 + b] = R[a] * gR[b] + R[3 + a] * gR[3 + b] + R[6 + a] * gR[6 + b];
-    const float av[3] = {0.5f * (A[7] - A[5]), 0.5f * (A[2] - A[6]), 0.5f * (A[3] - A[1])};
-    const float tr = S[0] + S[4] + S[8];
-    float T[9], Ti[9];
-#pragma unroll
-    for (int q = 0; q < 9; ++q) T[q] = -S[q];
-    T[0] += tr;
-    T[4] += tr;
-    T[8] += tr;
-    float om[3] = {0.f, 0.f, 0.f};
-    if (inv_transpose3(T, Ti)) {  // T symmetric: inverse-transpose = inverse
-#pragma unroll
-      for (int r = 0; r < 3; ++r) om[r] = Ti[r * 3] * av[0] + Ti[r * 3 + 1] * av[1] + Ti[r * 3 + 2] * av[2];
-    }
-    const float Y[9] = {0.f, -om[2], om[1], om[2], 0.f, -om[0], -om[1], om[0], 0.f};
-#pragma unroll
-    for (int r = 0; r < 3; ++r)
-#pragma unroll
-      for (int a = 0; a < 3; ++a)
-        gM[r * 3 + a] += 2.f * (R[r * 3] * Y[a] + R[r * 3 + 1] * Y[3 + a] + R[r * 3 + 2] * Y[6 + a]);
     float gP[18];
-    const float gm[3] = {grad_pos[3 * (size_t)i] * (1.f / 6.f), grad_pos[3 * (size_t)i + 1] * (1.f / 6.f),
-                         grad_pos[3 * (size_t)i + 2] * (1.f / 6.f)};
-#pragma unroll
-    for (int a = 0; a < 3; ++a)
-#pragma unroll
-      for (int r = 0; r < 3; ++r) {
-        gP[3 * (2 * a) + r] = gm[r] + 0.5f * gM[r * 3 + a];
-        gP[3 * (2 * a + 1) + r] = gm[r] - 0.5f * gM[r * 3 + a];
-      }
+    skin_adjoint_gP(i, M, R, scale0, grad_pos, grad_cov, gP);
 #pragma unroll 1
     for (int ep = 0; ep < 6; ++ep) {
       float gpe[3], pe[3];
@@ -703,6 +717,150 @@ __global__ void __launch_bounds__(kSkinThreads)
     if (nid < 0) continue;
 #pragma unroll
     for (int c = 0; c < 12; ++c) atomicAdd(grad_node + 12 * (size_t)nid + c, s_vals[q][c]);
+  }
+}
+
+// The adjoint with the skinning plan (every tile within kPlanNodes nodes).
+// Per tile: the node records are staged in tile-local affine form as in the
+// planned forward; thread t recomputes Gaussian t's blend (weights and slots
+// read from the plan block, coalesced), its polar factor and the chain of the
+// unplanned kernel above down to the endpoint gradients gP, which go to
+// shared memory with the endpoints' offsets from the tile's origin.  Then one
+// thread per slot sums its references (the plan's inverse lists, fixed
+// order): S0 = sum w gP_e, S1 = sum w gP_e (p_e - o)^T, so that
+// dL/dR_j = S1 - S0 (g_j - o)^T and dL/dt_j = S0, and adds them to grad_node
+// with one global atomic per (tile, node, component): no shared atomics.
+template <int K>
+__global__ void __launch_bounds__(kSkinThreads)
+    skin_gaussians_backward_planned_kernel(int N, const float* __restrict__ ends_in, const float* __restrict__ table,
+                                           const float* __restrict__ scale0,
+                                           const uint8_t* __restrict__ static_mask,
+                                           const float* __restrict__ grad_pos, const float* __restrict__ grad_cov,
+                                           float* __restrict__ grad_node, SkinPlanDev plan,
+                                           int* __restrict__ status) {
+  using PT = PlanTile<K>;
+  constexpr int KQ = PT::KQ;
+  constexpr int kRefBytes = 6 * K * kSkinTile * 2;
+  __shared__ __align__(16) float s_nodes[kPlanNodes * kPlanRec];
+  __shared__ float s_gp[kSkinTile][19];  // endpoint gradients (18), padded
+  __shared__ float s_pe[kSkinTile][19];  // endpoint offsets from the origin (18), padded
+  // dynamic: the tile's plan block (weights, slots) and its inverse lists
+  extern __shared__ __align__(16) unsigned char s_bk[];
+  const int t = threadIdx.x;
+  const int tile0 = blockIdx.x * kSkinTile;
+  const int cnt = min(kSkinTile, N - tile0);
+  const int i = tile0 + t;
+  const int n_stage = __ldg(plan.tile_count + blockIdx.x);
+  {
+    const unsigned char* gb = plan.blk + (size_t)blockIdx.x * PT::kBytes;
+    for (int q = t; q < PT::kBytes / 16; q += kSkinThreads) cp_async16(s_bk + 16 * q, gb + 16 * q);
+    const unsigned char* gr =
+        reinterpret_cast<const unsigned char*>(plan.inv_ref + (size_t)blockIdx.x * 6 * K * kSkinTile);
+    for (int q = t; q < kRefBytes / 16; q += kSkinThreads) cp_async16(s_bk + PT::kBytes + 16 * q, gr + 16 * q);
+    asm volatile("cp.async.commit_group;" ::: "memory");
+  }
+  const float o_x = __ldg(ends_in + tile0), o_y = __ldg(ends_in + (size_t)N + tile0),
+              o_z = __ldg(ends_in + 2 * (size_t)N + tile0);
+  {
+    const int32_t* list = plan.tile_nodes + (size_t)blockIdx.x * kPlanNodes;
+    for (int u = t; u < n_stage; u += kSkinThreads) {
+      const NodeAf r = node_affine(load_node(table, __ldg(list + u)), o_x, o_y, o_z);
+      float4* d4 = reinterpret_cast<float4*>(s_nodes + u * kPlanRec);
+      d4[0] = r.a;
+      d4[1] = r.b;
+      d4[2] = r.c;
+    }
+  }
+  asm volatile("cp.async.wait_group 0;" ::: "memory");
+  __syncthreads();
+  const unsigned char* tb = s_bk;
+  const float4* gw = reinterpret_cast<const float4*>(tb);
+  const uint32_t* gl = reinterpret_cast<const uint32_t*>(tb + PT::kWBytes);
+  const uint16_t* ir = reinterpret_cast<const uint16_t*>(s_bk + PT::kBytes);
+  float gP[18];
+#pragma unroll
+  for (int c = 0; c < 18; ++c) gP[c] = 0.f;
+  if (t < cnt && !(static_mask && static_mask[i])) {
+    float p0[18], e[18];
+#pragma unroll
+    for (int c = 0; c < 18; ++c) p0[c] = __ldg(ends_in + (size_t)c * N + i);
+#pragma unroll
+    for (int ep = 0; ep < 6; ++ep) {
+      float ox = 0.f, oy = 0.f, oz = 0.f, ws = 0.f;
+      const float dx = p0[3 * ep] - o_x, dy = p0[3 * ep + 1] - o_y, dz = p0[3 * ep + 2] - o_z;
+#pragma unroll
+      for (int q = 0; q < KQ; ++q) {
+        const float4 w4 = gw[(ep * KQ + q) * kSkinTile + t];
+        const uint32_t lw = gl[(ep * KQ + q) * kSkinTile + t];
+        const float wq[4] = {w4.x, w4.y, w4.z, w4.w};
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+          if (4 * q + r < K) {
+            const float4* r4 = reinterpret_cast<const float4*>(s_nodes + ((lw >> (8 * r)) & 0xffu) * kPlanRec);
+            NodeAf x;
+            x.a = r4[0];
+            x.b = r4[1];
+            x.c = r4[2];
+            ws += wq[r];
+            ed_term_af(x, wq[r], dx, dy, dz, ox, oy, oz);
+          }
+        }
+      }
+      e[3 * ep] = ed_finish(p0[3 * ep], ws, ox);
+      e[3 * ep + 1] = ed_finish(p0[3 * ep + 1], ws, oy);
+      e[3 * ep + 2] = ed_finish(p0[3 * ep + 2], ws, oz);
+    }
+#pragma unroll
+    for (int ep = 0; ep < 6; ++ep) {
+      s_pe[t][3 * ep] = p0[3 * ep] - o_x;
+      s_pe[t][3 * ep + 1] = p0[3 * ep + 1] - o_y;
+      s_pe[t][3 * ep + 2] = p0[3 * ep + 2] - o_z;
+    }
+    float M[9];
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+      for (int r = 0; r < 3; ++r) M[r * 3 + a] = 0.5f * (e[3 * (2 * a) + r] - e[3 * (2 * a + 1) + r]);
+    float R[9];
+    if (!polar_factor<float>(M, R, 20, 2e-7f)) raise_status(status, ARAP_ENONFINITE);
+    skin_adjoint_gP(i, M, R, scale0, grad_pos, grad_cov, gP);
+  }
+#pragma unroll
+  for (int c = 0; c < 18; ++c) s_gp[t][c] = gP[c];
+  __syncthreads();
+  // one thread per slot: its references in the plan's fixed order
+  const uint16_t* io = plan.inv_off + (size_t)blockIdx.x * (kPlanNodes + 1);
+  const int32_t* list = plan.tile_nodes + (size_t)blockIdx.x * kPlanNodes;
+  for (int u = t; u < n_stage; u += kSkinThreads) {
+    const int r0 = __ldg(io + u), r1 = __ldg(io + u + 1);
+    if (r0 == r1) continue;
+    float S0[3] = {0.f, 0.f, 0.f}, S1[9] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    for (int q = r0; q < r1; ++q) {
+      const int ref = ir[q];
+      const int g = ref / (6 * K), rem = ref - g * 6 * K, ep = rem / K, j = rem - ep * K;
+      const float w = reinterpret_cast<const float*>(tb)[((ep * KQ + (j >> 2)) * kSkinTile + g) * 4 + (j & 3)];
+      float wg[3];
+#pragma unroll
+      for (int r = 0; r < 3; ++r) wg[r] = w * s_gp[g][3 * ep + r];
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        const float d = s_pe[g][3 * ep + c];
+#pragma unroll
+        for (int r = 0; r < 3; ++r) S1[3 * c + r] = fmaf(wg[r], d, S1[3 * c + r]);
+      }
+#pragma unroll
+      for (int r = 0; r < 3; ++r) S0[r] += wg[r];
+    }
+    const int nid = __ldg(list + u);
+    const float4 gg = __ldg(reinterpret_cast<const float4*>(table) + 4 * (size_t)nid + 2);
+    const float go[3] = {gg.y - o_x, gg.z - o_y, gg.w - o_z};
+    float* dst = grad_node + 12 * (size_t)nid;
+#pragma unroll
+    for (int c = 0; c < 3; ++c)
+#pragma unroll
+      for (int r = 0; r < 3; ++r) atomicAdd(dst + 3 * c + r, fmaf(-S0[r], go[c], S1[3 * c + r]));
+#pragma unroll
+    for (int r = 0; r < 3; ++r) atomicAdd(dst + 9 + r, S0[r]);
   }
 }
 
@@ -983,7 +1141,8 @@ constexpr int kPlanPhases = kPlanGroups * 6 * ARAP_KNN_MAX;  // (lane group, end
 __global__ void __launch_bounds__(kPlanThreads)
     skin_plan_kernel(int N, int K, const int32_t* __restrict__ eidx, const float* __restrict__ ew,
                      int32_t* __restrict__ tile_count, int32_t* __restrict__ tile_nodes,
-                     unsigned char* __restrict__ blk, int tile_bytes) {
+                     unsigned char* __restrict__ blk, int tile_bytes, uint16_t* __restrict__ inv_off,
+                     uint16_t* __restrict__ inv_ref) {
   __shared__ int s_key[kPlanHash];
   __shared__ int s_list[kPlanNodes];                     // distinct ids, then ascending
   __shared__ unsigned char s_rk[kSkinTile * 6 * ARAP_KNN_MAX];  // rank of each sorted neighbour
@@ -1144,6 +1303,26 @@ __global__ void __launch_bounds__(kPlanThreads)
     lb[((size_t)(ep * KQ + (j >> 2)) * kSkinTile + g) * 4 + (j & 3)] =
         (unsigned char)s_lid[s_rk[(g * 6 + ep) * K + j]];
   }
+  // the adjoint's inverse lists: references (g * 6 + ep) * K + j of each
+  // slot, in ascending order (s_key, free now, holds the per-slot counts)
+  int* s_cnt = s_key;
+  for (int u = t; u <= kPlanNodes; u += kPlanThreads) s_cnt[u] = 0;
+  __syncthreads();
+  const int nref = cnt * 6 * K;
+  for (int e = t; e < nref; e += kPlanThreads) atomicAdd(&s_cnt[s_lid[s_rk[e]] + 1], 1);
+  __syncthreads();
+  if (t == 0)
+    for (int u = 1; u <= kPlanNodes; ++u) s_cnt[u] += s_cnt[u - 1];
+  __syncthreads();
+  uint16_t* io = inv_off + (size_t)blockIdx.x * (kPlanNodes + 1);
+  uint16_t* ir = inv_ref + (size_t)blockIdx.x * 6 * K * kSkinTile;
+  for (int u = t; u <= kPlanNodes; u += kPlanThreads) io[u] = (uint16_t)s_cnt[u];
+  for (int u = t; u < kPlanNodes; u += kPlanThreads) {
+    int pos = s_cnt[u];
+    if (pos == s_cnt[u + 1]) continue;
+    for (int e = 0; e < nref; ++e)
+      if (s_lid[s_rk[e]] == u) ir[pos++] = (uint16_t)e;
+  }
 }
 
 
@@ -1232,7 +1411,9 @@ extern "C" int arap_skin_plan_create(arap_skin_plan** out, int N, int k, const i
   const size_t b_count = ((sizeof(int32_t) * p->tiles) + 255) & ~size_t(255);
   const size_t b_nodes = ((sizeof(int32_t) * (size_t)p->tiles * kPlanNodes) + 255) & ~size_t(255);
   const size_t b_blk = ((size_t)p->tiles * p->tile_bytes + 255) & ~size_t(255);
-  if (cudaMalloc(&p->block, b_count + b_nodes + b_blk + 256) != cudaSuccess) {
+  const size_t b_ioff = (sizeof(uint16_t) * (size_t)p->tiles * (kPlanNodes + 1) + 255) & ~size_t(255);
+  const size_t b_iref = (sizeof(uint16_t) * (size_t)p->tiles * 6 * k * kSkinTile + 255) & ~size_t(255);
+  if (cudaMalloc(&p->block, b_count + b_nodes + b_blk + b_ioff + b_iref + 256) != cudaSuccess) {
     (void)cudaGetLastError();
     delete p;
     return ARAP_ENOMEM;
@@ -1241,15 +1422,18 @@ extern "C" int arap_skin_plan_create(arap_skin_plan** out, int N, int k, const i
   int32_t* count = reinterpret_cast<int32_t*>(base);
   int32_t* nodes = reinterpret_cast<int32_t*>(base + b_count);
   unsigned char* blk = reinterpret_cast<unsigned char*>(base + b_count + b_nodes);
-  p->dev = SkinPlanDev{count, nodes, blk};
-  p->status = reinterpret_cast<int*>(base + b_count + b_nodes + b_blk);
+  uint16_t* ioff = reinterpret_cast<uint16_t*>(base + b_count + b_nodes + b_blk);
+  uint16_t* iref = reinterpret_cast<uint16_t*>(base + b_count + b_nodes + b_blk + b_ioff);
+  p->dev = SkinPlanDev{count, nodes, blk, ioff, iref};
+  p->status = reinterpret_cast<int*>(base + b_count + b_nodes + b_blk + b_ioff + b_iref);
   // padded neighbour slots (k not a multiple of 4) and the rows of a partial
   // last tile stay zero
   if (cudaMemsetAsync(blk, 0, b_blk, st) != cudaSuccess || cudaMemsetAsync(p->status, 0, sizeof(int), st) != cudaSuccess) {
     arap_skin_plan_destroy(p);
     return ARAP_ECUDA;
   }
-  skin_plan_kernel<<<p->tiles, kPlanThreads, 0, st>>>(N, k, ends_idx, ends_w, count, nodes, blk, p->tile_bytes);
+  skin_plan_kernel<<<p->tiles, kPlanThreads, 0, st>>>(N, k, ends_idx, ends_w, count, nodes, blk, p->tile_bytes,
+                                                      ioff, iref);
   std::vector<int32_t> h(p->tiles);
   if (cudaPeekAtLastError() != cudaSuccess ||
       cudaMemcpyAsync(h.data(), count, sizeof(int32_t) * p->tiles, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
@@ -1340,6 +1524,51 @@ extern "C" int arap_skin_gaussians_backward(int N, int k, const float* ends_in, 
     default:
       return ARAP_EUNSUPPORTED;
   }
+  ARAP_LAUNCH_CHECK();
+  return ARAP_OK;
+}
+
+template <int K>
+static int launch_backward_planned(const arap_skin_plan* plan, const float* ends_in, const float* table,
+                                   const float* scale0, const uint8_t* st, const float* gpos, const float* gcov,
+                                   float* gnode, cudaStream_t s) {
+  constexpr int smem = PlanTile<K>::kBytes + 6 * K * kSkinTile * 2;
+  if (cudaFuncSetAttribute(skin_gaussians_backward_planned_kernel<K>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           smem) != cudaSuccess) {
+    (void)cudaGetLastError();
+    return ARAP_ECUDA;
+  }
+  skin_gaussians_backward_planned_kernel<K><<<plan->tiles, kSkinThreads, smem, s>>>(
+      plan->N, ends_in, table, scale0, st, gpos, gcov, gnode, plan->dev, plan->status);
+  return ARAP_OK;
+}
+
+extern "C" int arap_skin_gaussians_backward_planned(const arap_skin_plan* plan, const float* ends_in,
+                                                    const int32_t* ends_idx, const float* ends_w,
+                                                    const float* node_table, const float* scale0,
+                                                    const uint8_t* static_mask, const float* grad_pos,
+                                                    const float* grad_cov, float* grad_node, arap_stream_t stream) {
+  if (!plan || !ends_in || !ends_idx || !ends_w || !node_table || !scale0 || !grad_pos || !grad_cov || !grad_node)
+    return ARAP_EBADINPUT;
+  if (reinterpret_cast<uintptr_t>(node_table) & 15) return ARAP_EBADINPUT;
+  if (plan->overflow > 0)  // tiles over kPlanNodes nodes: the unplanned adjoint for all
+    return arap_skin_gaussians_backward(plan->N, plan->k, ends_in, ends_idx, ends_w, node_table, scale0, static_mask,
+                                        grad_pos, grad_cov, grad_node, plan->status, stream);
+  cudaStream_t s = (cudaStream_t)stream;
+  int rc = ARAP_OK;
+  switch (plan->k) {
+#define ARAP_SKBP(K)                                                                                   \
+  case K:                                                                                              \
+    rc = launch_backward_planned<K>(plan, ends_in, node_table, scale0, static_mask, grad_pos, grad_cov,      \
+                                    grad_node, s);                                                      \
+    break;
+    ARAP_SKBP(1) ARAP_SKBP(2) ARAP_SKBP(3) ARAP_SKBP(4) ARAP_SKBP(5) ARAP_SKBP(6)
+    ARAP_SKBP(7) ARAP_SKBP(8) ARAP_SKBP(9) ARAP_SKBP(10) ARAP_SKBP(11) ARAP_SKBP(12)
+#undef ARAP_SKBP
+    default:
+      return ARAP_EUNSUPPORTED;
+  }
+  if (rc != ARAP_OK) return rc;
   ARAP_LAUNCH_CHECK();
   return ARAP_OK;
 }

@@ -368,6 +368,18 @@ def skin_gaussians_backward(ends_in, ends_idx, ends_w, table, scale0, grad_pos, 
     return grad_node
 
 
+def skin_gaussians_backward_planned(plan, ends_in, table, scale0, grad_pos, grad_cov, n, static=None,
+                                    grad_node=None):
+    """skin_gaussians_backward with the skinning plan of the same endpoints
+    (arap_skin_gaussians_backward_planned); errors go to the plan's word."""
+    if grad_node is None:
+        grad_node = torch.zeros((n, 12), dtype=torch.float32, device="cuda")
+    check("arap_skin_gaussians_backward_planned", _lib_().arap_skin_gaussians_backward_planned(
+        plan._h, _p(ends_in), _p(plan.ends_idx), _p(plan.ends_w), _p(table), _p(scale0), _p(static),
+        _p(grad_pos), _p(grad_cov), _p(grad_node), _s()))
+    return grad_node
+
+
 def node_quaternions(rot, precision=_lib.PRECISION_PLAIN, status=None):
     n = rot.shape[0]
     out = torch.empty((n, 4), dtype=torch.float32, device="cuda")

@@ -654,23 +654,36 @@ def adjoint_leg(st, reps=10):
         dev.skin_gaussians(ends, st.ends_idx, st.ends_w, table, st.scale0, pos, q, sc, None, cov,
                            precision=st.precision)
 
-    def bwd():
+    def bwd_unplanned():
         grad.zero_()
         dev.skin_gaussians_backward(st.ends, st.ends_idx, st.ends_w, table, st.scale0, g_mu, g_cov, n,
                                     grad_node=grad)
 
+    def bwd():
+        grad.zero_()
+        if st.skin_plan is not None:
+            dev.skin_gaussians_backward_planned(st.skin_plan, st.ends, table, st.scale0, g_mu, g_cov, n,
+                                                grad_node=grad)
+        else:
+            bwd_unplanned()
+
     ms_f = timed(fwd)
     ms_b = timed(bwd)
+    ms_bu = timed(bwd_unplanned)
     ms_e = timed(lambda: st.solver.energy_grad(st.node_pos, st.aims, x))
     k = st.k
     bytes_b = N * (72 + 6 * k * 8 + 12 + 12 + 24)
     return {"gaussians": N, "nodes": n, "free_nodes": F, "precision": int(st.precision),
             "ms_skin_forward_with_cov": round(ms_f, 4), "ms_skin_backward": round(ms_b, 4),
+            "ms_skin_backward_unplanned": round(ms_bu, 4),
             "ms_energy_grad": round(ms_e, 4),
             "backward_bytes_per_gaussian": 72 + 6 * k * 8 + 12 + 12 + 24,
             "backward_gbs": round(bytes_b / (ms_b * 1e-3) / 1e9, 1),
-            "note": "backward reads endpoints, int32 kNN indices and float weights, scale0 and the upstream "
-                    "gradients; node gradients are summed per CTA in shared memory, then with global atomics"}
+            "note": "backward (arap_skin_gaussians_backward_planned): the blend recomputed from the tile's staged "
+                    "node records, each node's gradient summed over the plan's inverse reference lists, one "
+                    "global atomic per (tile, node, component); the unplanned adjoint sums through a "
+                    "shared-memory hash and atomics. Bytes per Gaussian as the unplanned reads them: endpoints, "
+                    "int32 indices and float weights, scale0, upstream gradients"}
 
 
 def ply_leg(sc, reps=3):

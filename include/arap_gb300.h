@@ -306,6 +306,18 @@ int arap_skin_gaussians_backward(int N, int k, const float* ends_in, const int32
                                  const float* ends_w, const float* node_table, const float* scale0,
                                  const uint8_t* static_mask, const float* grad_pos, const float* grad_cov,
                                  float* grad_node, int32_t* status, arap_stream_t stream);
+/* arap_skin_gaussians_backward with a skinning plan of the same endpoints
+ * (ends_idx/ends_w are read only when the plan has tiles over 256 nodes; then
+ * the whole call is arap_skin_gaussians_backward).  Per tile the blend is
+ * recomputed from the staged node records, and each node's gradient is summed
+ * over the tile's references to it in the plan's fixed order, then added to
+ * grad_node with one atomic per (tile, node, component).  The same result up
+ * to float rounding of the sums.  Device errors go to the plan's status word. */
+int arap_skin_gaussians_backward_planned(const arap_skin_plan* plan, const float* ends_in,
+                                         const int32_t* ends_idx, const float* ends_w,
+                                         const float* node_table, const float* scale0,
+                                         const uint8_t* static_mask, const float* grad_pos,
+                                         const float* grad_cov, float* grad_node, arap_stream_t stream);
 
 /* Per-node unit quaternion of the Newton polar factor of R
  * (FastUpdateSamplesSH, GaussianView.cpp:3172-3181; FastgetOthogonalMatrix
