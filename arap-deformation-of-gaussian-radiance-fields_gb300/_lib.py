@@ -63,6 +63,8 @@ D = C.c_double
 SIGNATURES = {
     "arap_build_graph": (I, [P, I, I, P, P]),
     "arap_compute_weights": (I, [P, I, P, I, I, P, P, P, P]),
+    "arap_compute_weights_ex": (I, [P, I, P, I, I, I, P, P, P, P]),
+    "arap_knn_autotune": (I, [P, I, P, I, I, P, P, P]),
     "arap_solve_config_default": (None, [C.POINTER(SolveConfig)]),
     "arap_solver_create": (I, [C.POINTER(P), I, I, P, P, P, P, P, P, I, C.POINTER(SolveConfig), P]),
     "arap_solver_solve": (I, [P, P, P, P, P, C.POINTER(SolveStats), P]),

@@ -11,11 +11,11 @@
 
 namespace arap {
 
-constexpr int kKnnThreads = 256;
-constexpr int kKnnTile = 2048;  // nodes per shared-memory tile (32 KB)
+constexpr int kKnnThreads = 256;  // default CTA size; 128 and 512 are built too
+constexpr int kKnnTile = 2048;    // nodes per shared-memory tile (32 KB)
 
-template <int KP1>
-__global__ void __launch_bounds__(kKnnThreads) knn_kernel(const float* __restrict__ pts, int P,
+template <int KP1, int NT>
+__global__ void __launch_bounds__(NT) knn_kernel(const float* __restrict__ pts, int P,
                                                           const float* __restrict__ nodes, int n,
                                                           int skip_first, int kout,
                                                           int32_t* __restrict__ idx_out,
@@ -107,19 +107,28 @@ __global__ void __launch_bounds__(kKnnThreads) knn_kernel(const float* __restric
 
 template <int KP1>
 static int launch_knn(const float* pts, int P, const float* nodes, int n, int skip, int kout,
-                      int32_t* idx, float* w, int planes, int* status, cudaStream_t st) {
-  const int grid = grid_for(P, kKnnThreads);
-  knn_kernel<KP1><<<grid, kKnnThreads, 0, st>>>(pts, P, nodes, n, skip, kout, idx, w, planes, status);
+                      int32_t* idx, float* w, int planes, int* status, int threads, cudaStream_t st) {
+  switch (threads) {
+    case 128:
+      knn_kernel<KP1, 128><<<grid_for(P, 128), 128, 0, st>>>(pts, P, nodes, n, skip, kout, idx, w, planes, status);
+      break;
+    case 512:
+      knn_kernel<KP1, 512><<<grid_for(P, 512), 512, 0, st>>>(pts, P, nodes, n, skip, kout, idx, w, planes, status);
+      break;
+    default:
+      knn_kernel<KP1, 256><<<grid_for(P, 256), 256, 0, st>>>(pts, P, nodes, n, skip, kout, idx, w, planes, status);
+  }
   ARAP_LAUNCH_CHECK();
   return ARAP_OK;
 }
 
 static int dispatch_knn(int kp1, const float* pts, int P, const float* nodes, int n, int skip,
-                        int kout, int32_t* idx, float* w, int planes, int* status, cudaStream_t st) {
+                        int kout, int32_t* idx, float* w, int planes, int* status, int threads,
+                        cudaStream_t st) {
   switch (kp1) {
 #define ARAP_KNN_CASE(K) \
   case K:                \
-    return launch_knn<K>(pts, P, nodes, n, skip, kout, idx, w, planes, status, st);
+    return launch_knn<K>(pts, P, nodes, n, skip, kout, idx, w, planes, status, threads, st);
     ARAP_KNN_CASE(2)
     ARAP_KNN_CASE(3)
     ARAP_KNN_CASE(4)
@@ -146,17 +155,69 @@ extern "C" int arap_build_graph(const float* nodes_xyz, int n, int k, int32_t* n
                                 arap_stream_t stream) {
   if (!nodes_xyz || !neighbors_out || k < 1 || n < k + 1) return ARAP_EBADINPUT;
   if (k > ARAP_KNN_MAX) return ARAP_EUNSUPPORTED;
-  return dispatch_knn(k + 1, nodes_xyz, n, nodes_xyz, n, 1, k, neighbors_out, nullptr, 0, nullptr,
+  return dispatch_knn(k + 1, nodes_xyz, n, nodes_xyz, n, 1, k, neighbors_out, nullptr, 0, nullptr, kKnnThreads,
                       (cudaStream_t)stream);
+}
+
+extern "C" int arap_compute_weights_ex(const float* points_xyz, int P, const float* nodes_xyz, int n, int k,
+                                       int threads, int32_t* idx_out, float* w_out, int32_t* status,
+                                       arap_stream_t stream) {
+  if (P == 0) return ARAP_OK;
+  if (!points_xyz || !nodes_xyz || !idx_out || !w_out || P < 0 || k < 1 || n < k + 1)
+    return ARAP_EBADINPUT;
+  if (threads != 0 && threads != 128 && threads != 256 && threads != 512) return ARAP_EBADINPUT;
+  if (k > ARAP_KNN_MAX) return ARAP_EUNSUPPORTED;
+  return dispatch_knn(k + 1, points_xyz, P, nodes_xyz, n, 0, k, idx_out, w_out, 1, status,
+                      threads ? threads : kKnnThreads, (cudaStream_t)stream);
 }
 
 extern "C" int arap_compute_weights(const float* points_xyz, int P, const float* nodes_xyz, int n,
                                     int k, int32_t* idx_out, float* w_out, int32_t* status,
                                     arap_stream_t stream) {
-  if (P == 0) return ARAP_OK;
-  if (!points_xyz || !nodes_xyz || !idx_out || !w_out || P < 0 || k < 1 || n < k + 1)
-    return ARAP_EBADINPUT;
+  return arap_compute_weights_ex(points_xyz, P, nodes_xyz, n, k, 0, idx_out, w_out, status, stream);
+}
+
+extern "C" int arap_knn_autotune(const float* points_xyz, int P, const float* nodes_xyz, int n, int k,
+                                 int* threads_out, float* ms_out, arap_stream_t stream) {
+  if (!threads_out || !points_xyz || !nodes_xyz || P < 1 || k < 1 || n < k + 1) return ARAP_EBADINPUT;
   if (k > ARAP_KNN_MAX) return ARAP_EUNSUPPORTED;
-  return dispatch_knn(k + 1, points_xyz, P, nodes_xyz, n, 0, k, idx_out, w_out, 1, status,
-                      (cudaStream_t)stream);
+  cudaStream_t st = (cudaStream_t)stream;
+  // a bounded sample: the first points (the work per point is the same)
+  const int S = P < (1 << 18) ? P : (1 << 18);
+  void* buf = nullptr;
+  if (cudaMalloc(&buf, (size_t)S * k * 8 + sizeof(int)) != cudaSuccess) {
+    (void)cudaGetLastError();
+    return ARAP_ENOMEM;
+  }
+  int32_t* idx = static_cast<int32_t*>(buf);
+  float* w = reinterpret_cast<float*>(idx + (size_t)S * k);
+  int* word = reinterpret_cast<int*>(w + (size_t)S * k);
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  int rc = cudaMemsetAsync(word, 0, sizeof(int), st) == cudaSuccess ? ARAP_OK : ARAP_ECUDA;
+  if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) rc = ARAP_ECUDA;
+  const int cand[3] = {128, 256, 512};
+  float best = 0.f;
+  *threads_out = kKnnThreads;
+  for (int c = 0; c < 3 && rc == ARAP_OK; ++c) {
+    float ms = 0.f;
+    for (int rep = 0; rep < 2 && rc == ARAP_OK; ++rep) {  // the first run warms up
+      if (cudaEventRecord(e0, st) != cudaSuccess) rc = ARAP_ECUDA;
+      if (rc == ARAP_OK)
+        rc = dispatch_knn(k + 1, points_xyz, S, nodes_xyz, n, 0, k, idx, w, 1, word, cand[c], st);
+      if (rc == ARAP_OK && (cudaEventRecord(e1, st) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess ||
+                            cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess))
+        rc = ARAP_ECUDA;
+    }
+    if (rc != ARAP_OK) break;
+    if (ms_out) ms_out[c] = ms;
+    if (c == 0 || ms < best) {
+      best = ms;
+      *threads_out = cand[c];
+    }
+  }
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  if (rc != ARAP_OK) (void)cudaGetLastError();
+  cudaFree(buf);
+  return rc;
 }

@@ -120,17 +120,30 @@ def build_graph(nodes: torch.Tensor, k: int) -> torch.Tensor:
     return out
 
 
-def compute_weights(points: torch.Tensor, nodes: torch.Tensor, k: int, status=None):
+def compute_weights(points: torch.Tensor, nodes: torch.Tensor, k: int, status=None, threads: int = 0):
     """kNN skinning weights (DeformGraph::computeWeights, Deform.hpp:187-208).
-    Returns (idx [k,P] int32, w [k,P] float32) in planes layout."""
+    Returns (idx [k,P] int32, w [k,P] float32) in planes layout.  threads:
+    the kernel's CTA size (0: the default; see knn_autotune)."""
     points = _f32(points)
     nodes = _f32(nodes)
     P = points.shape[0]
     idx = torch.empty((k, P), dtype=torch.int32, device="cuda")
     w = torch.empty((k, P), dtype=torch.float32, device="cuda")
-    check("arap_compute_weights", _lib_().arap_compute_weights(
-        _p(points), P, _p(nodes), nodes.shape[0], k, _p(idx), _p(w), _status(status), _s()))
+    check("arap_compute_weights_ex", _lib_().arap_compute_weights_ex(
+        _p(points), P, _p(nodes), nodes.shape[0], k, int(threads), _p(idx), _p(w), _status(status), _s()))
     return idx, w
+
+
+def knn_autotune(points: torch.Tensor, nodes: torch.Tensor, k: int):
+    """The fastest CTA size of the kNN kernel for these points and nodes
+    (arap_knn_autotune): (threads, {threads: ms})."""
+    points = _f32(points)
+    nodes = _f32(nodes)
+    t = C.c_int()
+    ms = (C.c_float * 3)()
+    check("arap_knn_autotune", _lib_().arap_knn_autotune(
+        _p(points), points.shape[0], _p(nodes), nodes.shape[0], k, C.byref(t), C.cast(ms, C.c_void_p), _s()))
+    return t.value, dict(zip((128, 256, 512), list(ms)))
 
 
 # --------------------------------------------------------------- solver ----
@@ -460,14 +473,17 @@ class GaussianDeformer:
         self.anchor_idx = gidx[:, nv].contiguous()
         self.anchor_w = gw[:, nv].contiguous()
         self.ends, ends_xyz = end_points(self.pos, self.rot, self.scale)
-        self.ends_idx, self.ends_w = compute_weights(ends_xyz, self.node_pos, self.k, status=self.word)
+        # the kNN kernel's CTA size, tuned on the largest of its inputs here
+        self.knn_threads, self.knn_tuning = knn_autotune(ends_xyz, self.node_pos, self.k)
+        self.ends_idx, self.ends_w = compute_weights(ends_xyz, self.node_pos, self.k, status=self.word,
+                                                     threads=self.knn_threads)
         del ends_xyz
         self.skin_plan = SkinPlan(self.ends_idx, self.ends_w) if use_plan else None
         self.sample_pos = _f32(sample_pos) if sample_pos is not None else None
         self.feature = _f32(feature) if feature is not None else None
         if self.sample_pos is not None:
             self.sample_idx, self.sample_w = compute_weights(self.sample_pos, self.node_pos, self.k,
-                                                             status=self.word)
+                                                             status=self.word, threads=self.knn_threads)
         self.blocks = [torch.as_tensor(b, dtype=torch.int64) for b in blocks]
         self.block_type = [int(t) for t in block_type]
         node_static = torch.zeros(self.n, dtype=torch.uint8, device=dev)

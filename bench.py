@@ -554,7 +554,10 @@ def run_ours(a):
     k = sc.k
     bytes_launch = skin_bytes_per_gaussian(k, planned=st.skin_plan is not None) * sc.n_gauss
     achieved = bytes_launch / (skin_ms * 1e-3) / 1e9
-    launches_per_step = 5 + (1 if st.sample_pos is not None else 0) + (1 if st.feature is not None else 0)
+    # the library's kernels per frame: the solve, the node table, the Gaussian
+    # skinning and the node update, plus the sample skinning and the node
+    # quaternions for the samples' features (the aims copy is a torch copy)
+    launches_per_step = 4 + (1 if st.sample_pos is not None else 0) + (1 if st.feature is not None else 0)
     line = {
         "metric": METRIC,
         "value": round(ms_step, 4),
@@ -574,6 +577,8 @@ def run_ours(a):
                    "samples": int(st.sample_pos.shape[0]) if st.sample_pos is not None else 0,
                    "l2": "flushed between steps (256 MB write)",
                    "state": "restored to the rest pose before each step, outside the timed region",
+                   "knn_threads": st.knn_threads,
+                   "knn_autotune_ms": {str(t): round(v, 3) for t, v in st.knn_tuning.items()},
                    "wall_s_timed_region": round(wall, 3)},
         "e2e": {"value": round(reduce_max(float(np.mean(e2e_ms)), ws), 4), "unit": "ms/frame",
                 "h2d_bytes_per_step": int(st.n * 12), "d2h_bytes_per_step": int(st.n * 48)},

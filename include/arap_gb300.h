@@ -71,6 +71,19 @@ int arap_build_graph(const float* nodes_xyz, int n, int k, int32_t* neighbors_ou
 int arap_compute_weights(const float* points_xyz, int P, const float* nodes_xyz, int n,
                          int k, int32_t* idx_out, float* w_out, int32_t* status,
                          arap_stream_t stream);
+/* arap_compute_weights with the CTA size of its kernel chosen by the caller
+ * (threads: 128, 256 or 512; 0 = 256), e.g. from arap_knn_autotune.  The
+ * results do not depend on it. */
+int arap_compute_weights_ex(const float* points_xyz, int P, const float* nodes_xyz, int n, int k,
+                            int threads, int32_t* idx_out, float* w_out, int32_t* status,
+                            arap_stream_t stream);
+/* Autotuner of the kNN kernel: times the 128-, 256- and 512-thread CTAs on the
+ * first min(P, 262144) points against the n nodes (each run once to warm up,
+ * then timed with CUDA events on the stream) and returns the fastest in
+ * *threads_out; ms_out [3] (optional) receives the three times.  Synchronises;
+ * allocates and frees its own scratch outputs. */
+int arap_knn_autotune(const float* points_xyz, int P, const float* nodes_xyz, int n, int k,
+                      int* threads_out, float* ms_out, arap_stream_t stream);
 
 /* --------------------------------------------------------------- solver --- */
 
