@@ -36,9 +36,10 @@ static_assert(kScratchFloats >= kMaxCoarse, "scratch holds the restricted residu
 
 // Inverse of the coarse matrix in Cw[0] by blocked Gauss-Jordan (float32, no
 // pivoting: the matrix is symmetric positive definite).  For each pivot block
-// K (kGJBlock = 32 wide, the last one padded with the identity), every CTA
-// inverts A_KK with all its threads (two elements each, one block barrier per
-// pivot; the same bits in every CTA), then updates its own strip of rows:
+// K (kGJBlock = 32 wide, the last one padded with the identity), warp 0 of
+// every CTA inverts A_KK in registers (lane j holds column j; the pivot
+// column is published in shared memory, one warp barrier per pivot; the same
+// bits in every CTA), then every CTA updates its own strip of rows:
 //   A_KK <- A_KK^-1, A_Kj <- A_KK^-1 A_Kj, A_iK <- -W_iK,
 //   A_ij <- A_ij - W_iK A_Kj,  W = A_iK A_KK^-1,
 // with W of the strip in shared memory and the column A_Kj streamed from L2 in
@@ -61,60 +62,53 @@ __device__ bool coarse_invert(const SolveParams& P, G& gs, int* ok, float* sm) {
   const int r_begin = min(NC, (int)gs.bid * R), r_end = min(NC, r_begin + R);
   int src_i = 0;
   *ok = 1;
+  __shared__ int s_bad;
   for (int K0 = 0; K0 < NC; K0 += KB) {
     const int kb = min(KB, NC - K0);
     const float* src = P.Cw + src_i * NC2;
     float* dst = (K0 + kb >= NC) ? P.Cinv : P.Cw + (1 - src_i) * NC2;
-    {
-      // the pivot block, padded with the identity, inverted by the whole CTA:
-      // thread tid keeps elements e = tid + q * kSolveThreads ((i, j) =
-      // (e / 32, e % 32)) in registers; per pivot m they read the old row m
-      // and column m, published in shared memory by their owners in the step
-      // before (double-buffered in wrow's space), so one barrier per pivot
-      // suffices.  The arithmetic of every element is that of a warp-shuffle
-      // Gauss-Jordan, and every CTA gets the same bits.
-      constexpr int NQ = KB * KB / kSolveThreads;
-      static_assert(NQ * kSolveThreads == KB * KB && 4 * KB <= kGJRows * KP, "pivot block split");
-      float* rc = &wrow[0][0];  // [2 buffers][row m | column m][32]
-      float v[NQ];
+    if (tid < 32) {
+      // column `lane` of the pivot block, padded with the identity, inverted
+      // in place by warp 0 (Gauss-Jordan without pivoting): per pivot m, lane
+      // m publishes its column (the old A[*][m]) in shared memory
+      // (double-buffered in wrow's space, so one warp barrier per pivot) and
+      // every lane updates its column from it.  Every CTA gets the same bits.
+      const int lane = tid;
+      float* bc = &wrow[0][0];  // [2][32]
+      float col[KB];
 #pragma unroll
-      for (int q = 0; q < NQ; ++q) {
-        const int e = tid + q * kSolveThreads, i = e / KB, j = e % KB;
-        v[q] = (i < kb && j < kb) ? __ldcg(src + (size_t)(K0 + i) * NC + K0 + j) : (i == j ? 1.f : 0.f);
-        if (i == 0) rc[j] = v[q];
-        if (j == 0) rc[KB + i] = v[q];
-      }
-      __syncthreads();
+      for (int i = 0; i < KB; ++i)
+        col[i] = (i < kb && lane < kb) ? __ldcg(src + (size_t)(K0 + i) * NC + K0 + lane) : (i == lane ? 1.f : 0.f);
       int bad = 0;
-#pragma unroll 1
+#pragma unroll
       for (int m = 0; m < KB; ++m) {
-        const float* rowm = rc + (m & 1) * 2 * KB;  // old A[m][*]
-        const float* colm = rowm + KB;              // old A[*][m]
-        float* nrow = rc + ((m + 1) & 1) * 2 * KB;
-        const float pvt = rowm[m];
-        bad |= !(pvt > 0.f);
-        const float ip = 1.f / pvt;
+        float4* pub = reinterpret_cast<float4*>(bc + (m & 1) * KB);
+        if (lane == m) {
 #pragma unroll
-        for (int q = 0; q < NQ; ++q) {
-          const int e = tid + q * kSolveThreads, i = e / KB, j = e % KB;
-          const float cim = colm[i], cmj = rowm[j];
-          if (i == m)
-            v[q] = (j == m) ? ip : cmj * ip;
-          else
-            v[q] = (j == m) ? -cim * ip : fmaf(-cim * ip, cmj, v[q]);
-          if (i == m + 1) nrow[j] = v[q];
-          if (j == m + 1) nrow[KB + i] = v[q];
+          for (int i4 = 0; i4 < KB / 4; ++i4)
+            pub[i4] = make_float4(col[4 * i4], col[4 * i4 + 1], col[4 * i4 + 2], col[4 * i4 + 3]);
         }
-        __syncthreads();
+        __syncwarp();
+        const float* cm = bc + (m & 1) * KB;
+        const float pvt = cm[m];
+        bad |= !(pvt > 0.f);
+        const float ip = __frcp_rn(pvt);
+        const float cmj = col[m];
+#pragma unroll
+        for (int i = 0; i < KB; ++i) {
+          const float cim = cm[i];
+          if (i == m)
+            col[i] = (lane == m) ? ip : cmj * ip;
+          else
+            col[i] = (lane == m) ? -cim * ip : fmaf(-cim * ip, cmj, col[i]);
+        }
       }
 #pragma unroll
-      for (int q = 0; q < NQ; ++q) {
-        const int e = tid + q * kSolveThreads;
-        pv0[e / KB][e % KB] = v[q];
-      }
-      __syncthreads();
-      if (bad) *ok = 0;
+      for (int i = 0; i < KB; ++i) pv0[i][lane] = col[i];
+      if (lane == 0) s_bad = bad;
     }
+    __syncthreads();
+    if (s_bad) *ok = 0;
     for (int r0 = r_begin; r0 < r_end; r0 += kGJRows) {
       const int nr = min(kGJRows, r_end - r0);
       for (int t = tid; t < kGJRows * KB; t += bd) {
