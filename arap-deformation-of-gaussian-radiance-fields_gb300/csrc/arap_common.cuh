@@ -6,8 +6,6 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
-#include <utility>
-
 #include "../../include/arap_gb300.h"
 
 #define ARAP_CUDA_TRY(expr)                   \
@@ -505,158 +503,147 @@ __device__ __forceinline__ void quat_to_rowmajor(float4 q, float* R) {
 }
 
 // ------------------------------------------------------- SH rotation -----
-// Real spherical-harmonic band rotation for bands 1..3 from the recurrence of
-// Ivanic and Ruedenberg (J. Phys. Chem. 100 (1996) 6342; erratum 102 (1998)
-// 9099).  Coefficients are evaluated at compile time; band 1 uses the
-// (y, z, x) ordering of the 3DGS / reference layout.
-__host__ __device__ constexpr double csqrt_newton(double x, double cur, double prev) {
-  return cur == prev ? cur : csqrt_newton(x, 0.5 * (cur + x / cur), cur);
-}
-__host__ __device__ constexpr double csqrt(double x) {
-  return x <= 0.0 ? 0.0 : csqrt_newton(x, x > 1.0 ? x : 1.0, 0.0);
-}
+// Rotation of the real spherical harmonics of bands 1..3 (coefficient index
+// l*l + l + m, m = -l..l; band 1 in the (y, z, x) order of the 3DGS /
+// reference layout), given the rotation as the unit quaternion
+// q = (w, x, y, z) in (.x, .y, .z, .w).  It is applied in Euler form: with
+// R = Rz(a) Ry(b) Rz(g) and Ry(b) = Rx(-pi/2) Rz(b) Rx(pi/2), every band's
+// matrix is D(R) = Dz(a) Dx^T Dz(b) Dx Dz(g).  Dz(t) turns each coefficient
+// pair (m, -m) by the angle m t; Dx is the fixed band matrix of a quarter
+// turn about x (entries 0, +-1, +-1/2, +-sqrt(3)/2, +-1/4, +-sqrt(6)/4,
+// +-sqrt(10)/4, +-sqrt(15)/4: the Ivanic-Ruedenberg band matrices, J. Phys.
+// Chem. 100 (1996) 6342, erratum 102 (1998) 9099, at Rx(pi/2)).  The
+// angles' cosines and sines come from q without trigonometric calls: with
+// A = w^2 + z^2 = cos^2(b/2) and B = x^2 + y^2 = sin^2(b/2),
+//   e^{ib} = (A - B) + 2i sqrt(AB),
+//   e^{ia} = (w + iz)(y - ix) / sqrt(AB),  e^{ig} = (w + iz)(y + ix) / sqrt(AB).
+// Near b = 0 or b = pi only a + g or a - g is defined, and the two half-angle
+// factors carry the same rounding into a and g, so the product stays
+// accurate; at AB = 0 exactly a = 0 and g takes the whole turn.  No band
+// matrix is formed: about 130 multiply-adds per colour channel.
+namespace shq {
+constexpr float kR3h = 0.866025403784438647f;   // sqrt(3)/2
+constexpr float kS10q = 0.790569415042094833f;  // sqrt(10)/4
+constexpr float kS6q = 0.612372435695794525f;   // sqrt(6)/4
+constexpr float kS15q = 0.968245836551854221f;  // sqrt(15)/4
 
-template <int L>
-struct ShBand {
-  float v[2 * L + 1][2 * L + 1];
+struct Turns {
+  float c[3], s[3];  // cos and sin of 1, 2, 3 times the angle
 };
-
-// P term of the recurrence: r1 is band 1 indexed [i+1][j+1], prev band L-1
-// indexed [a+L-1][b+L-1].
-template <int L, int I, int A, int B>
-__device__ __forceinline__ float sh_p(const ShBand<1>& r1, const ShBand<L - 1>& prev) {
-  if constexpr (B == L) {
-    return r1.v[I + 1][2] * prev.v[A + L - 1][2 * L - 2] - r1.v[I + 1][0] * prev.v[A + L - 1][0];
-  } else if constexpr (B == -L) {
-    return r1.v[I + 1][2] * prev.v[A + L - 1][0] + r1.v[I + 1][0] * prev.v[A + L - 1][2 * L - 2];
-  } else {
-    return r1.v[I + 1][1] * prev.v[A + L - 1][B + L - 1];
-  }
+__device__ __forceinline__ Turns turns(float c1, float s1) {
+  Turns t;
+  t.c[0] = c1;
+  t.s[0] = s1;
+  t.c[1] = c1 * c1 - s1 * s1;
+  t.s[1] = 2.0f * c1 * s1;
+  t.c[2] = t.c[1] * c1 - t.s[1] * s1;
+  t.s[2] = t.s[1] * c1 + t.c[1] * s1;
+  return t;
 }
-
-template <int L, int M, int N>
-__device__ __forceinline__ float sh_elem(const ShBand<1>& r1, const ShBand<L - 1>& prev) {
-  constexpr double d = (M == 0) ? 1.0 : 0.0;
-  constexpr int am = M < 0 ? -M : M;
-  constexpr double den = (N < L && N > -L) ? double((L + N) * (L - N)) : double(2 * L * (2 * L - 1));
-  constexpr double u = csqrt(double((L + M) * (L - M)) / den);
-  constexpr double v = 0.5 * csqrt((1.0 + d) * double((L + am - 1) * (L + am)) / den) * (1.0 - 2.0 * d);
-  constexpr double w = -0.5 * csqrt(double((L - am - 1) * (L - am)) / den) * (1.0 - d);
-  float acc = 0.0f;
-  if constexpr (u != 0.0) acc += float(u) * sh_p<L, 0, M, N>(r1, prev);
-  if constexpr (v != 0.0) {
-    float V;
-    if constexpr (M == 0) {
-      V = sh_p<L, 1, 1, N>(r1, prev) + sh_p<L, -1, -1, N>(r1, prev);
-    } else if constexpr (M > 0) {
-      constexpr float c1 = float(csqrt(1.0 + (M == 1 ? 1.0 : 0.0)));
-      if constexpr (M == 1) {
-        V = sh_p<L, 1, M - 1, N>(r1, prev) * c1;
-      } else {
-        V = sh_p<L, 1, M - 1, N>(r1, prev) * c1 - sh_p<L, -1, -M + 1, N>(r1, prev);
-      }
-    } else {
-      constexpr float c2 = float(csqrt(1.0 + (M == -1 ? 1.0 : 0.0)));
-      if constexpr (M == -1) {
-        V = sh_p<L, -1, -M - 1, N>(r1, prev) * c2;
-      } else {
-        V = sh_p<L, 1, M + 1, N>(r1, prev) + sh_p<L, -1, -M - 1, N>(r1, prev) * c2;
-      }
+// Dz on one channel: c[0..15] are coefficients 0..15 (index l*l + l + m)
+__device__ __forceinline__ void dz(float* c, const Turns& t) {
+#pragma unroll
+  for (int l = 1; l <= 3; ++l) {
+    const int o = l * l + l;
+#pragma unroll
+    for (int m = 1; m <= l; ++m) {
+      const float lo = c[o - m], hi = c[o + m];
+      c[o - m] = t.c[m - 1] * lo + t.s[m - 1] * hi;
+      c[o + m] = t.c[m - 1] * hi - t.s[m - 1] * lo;
     }
-    acc += float(v) * V;
   }
-  if constexpr (w != 0.0) {
-    float W;
-    if constexpr (M > 0) {
-      W = sh_p<L, 1, M + 1, N>(r1, prev) + sh_p<L, -1, -M - 1, N>(r1, prev);
+}
+// Dx (T = false) or its transpose (T = true) on one channel
+template <bool T>
+__device__ __forceinline__ void dx(float* c) {
+  // band 1 (indices 1..3 = m -1, 0, 1): (-c0, c-1, c1) or its inverse
+  {
+    const float a = c[1], b = c[2];
+    c[1] = T ? b : -b;
+    c[2] = T ? -a : a;
+  }
+  // band 2 (indices 4..8 = m -2..2)
+  {
+    const float m2 = c[4], m1 = c[5], z = c[6], p1 = c[7], p2 = c[8];
+    if (!T) {
+      c[4] = -p1;
+      c[5] = -m1;
+      c[6] = -0.5f * z - kR3h * p2;
+      c[7] = m2;
+      c[8] = -kR3h * z + 0.5f * p2;
     } else {
-      W = sh_p<L, 1, M - 1, N>(r1, prev) - sh_p<L, -1, -M + 1, N>(r1, prev);
+      c[4] = p1;
+      c[5] = -m1;
+      c[6] = -0.5f * z - kR3h * p2;
+      c[7] = -m2;
+      c[8] = -kR3h * z + 0.5f * p2;
     }
-    acc += float(w) * W;
   }
-  return acc;
+  // band 3 (indices 9..15 = m -3..3)
+  {
+    const float m3 = c[9], m2 = c[10], m1 = c[11], z = c[12], p1 = c[13], p2 = c[14], p3 = c[15];
+    if (!T) {
+      c[9] = kS10q * z - kS6q * p2;
+      c[10] = -m2;
+      c[11] = kS6q * z + kS10q * p2;
+      c[12] = -kS10q * m3 - kS6q * m1;
+      c[13] = -0.25f * p1 - kS15q * p3;
+      c[14] = kS6q * m3 - kS10q * m1;
+      c[15] = -kS15q * p1 + 0.25f * p3;
+    } else {
+      c[9] = -kS10q * z + kS6q * p2;
+      c[10] = -m2;
+      c[11] = -kS6q * z - kS10q * p2;
+      c[12] = kS10q * m3 + kS6q * m1;
+      c[13] = -0.25f * p1 - kS15q * p3;
+      c[14] = -kS6q * m3 + kS10q * m1;
+      c[15] = -kS15q * p1 + 0.25f * p3;
+    }
+  }
 }
+}  // namespace shq
 
-template <int L, int... Is>
-__device__ __forceinline__ void sh_fill(ShBand<L>& out, const ShBand<1>& r1, const ShBand<L - 1>& prev,
-                                        std::integer_sequence<int, Is...>) {
-  ((out.v[Is / (2 * L + 1)][Is % (2 * L + 1)] =
-        sh_elem<L, Is / (2 * L + 1) - L, Is % (2 * L + 1) - L>(r1, prev)),
-   ...);
-}
-
-// Rotate interleaved SH s[coef*3 + rgb] (16 coefficients) by row-major R.
-// With FLIP the odd coefficients are negated before and after the band
-// rotation (the sign convention of cudakdtree.cu:160-196 and
-// GaussianView.cpp:3138-3154).
+// Rotates interleaved SH s[coef*3 + rgb] (16 coefficients) by q.  With FLIP
+// the odd coefficients are negated before and after the band rotation (the
+// sign convention of cudakdtree.cu:160-196 and GaussianView.cpp:3138-3154).
 template <bool FLIP>
-__device__ __forceinline__ void rotate_sh48(const float* R, float* s) {
-  ShBand<1> b1;
-  const int perm[3] = {1, 2, 0};
-#pragma unroll
-  for (int a = 0; a < 3; ++a)
-#pragma unroll
-    for (int b = 0; b < 3; ++b) b1.v[a][b] = R[perm[a] * 3 + perm[b]];
-  if (FLIP) {
-#pragma unroll
-    for (int k = 1; k < 16; k += 2) {
-      s[k * 3 + 0] = -s[k * 3 + 0];
-      s[k * 3 + 1] = -s[k * 3 + 1];
-      s[k * 3 + 2] = -s[k * 3 + 2];
-    }
+__device__ __forceinline__ void rotate_sh48(float4 q, float* s) {
+  const float w = q.x, x = q.y, y = q.z, z = q.w;
+  const float A = w * w + z * z, B = x * x + y * y;
+  float ca = w * y + x * z, sa = y * z - w * x, cg = w * y - x * z, sg = y * z + w * x;
+  const float n2 = ca * ca + sa * sa;
+  if (n2 > 1e-30f) {
+    const float inv = rsqrtf(n2);
+    ca *= inv;
+    sa *= inv;
+    cg *= inv;
+    sg *= inv;
+  } else if (A >= B) {  // b = 0: g = 2 arg(w + iz)
+    ca = 1.0f;
+    sa = 0.0f;
+    cg = (w * w - z * z) / A;
+    sg = 2.0f * w * z / A;
+  } else {  // b = pi: g = 2 arg(y + ix)
+    ca = 1.0f;
+    sa = 0.0f;
+    cg = (y * y - x * x) / B;
+    sg = 2.0f * x * y / B;
   }
-  // band 1: coefficients 1..3
+  const shq::Turns ta = shq::turns(ca, sa), tb = shq::turns(A - B, 2.0f * sqrtf(A * B)),
+                   tg = shq::turns(cg, sg);
 #pragma unroll
-  for (int c = 0; c < 3; ++c) {
-    float in[3], out[3];
+  for (int ch = 0; ch < 3; ++ch) {
+    float c[16];
+    c[0] = s[ch];  // band 0: unchanged
 #pragma unroll
-    for (int i = 0; i < 3; ++i) in[i] = s[(1 + i) * 3 + c];
+    for (int k = 1; k < 16; ++k) c[k] = (FLIP && (k & 1)) ? -s[k * 3 + ch] : s[k * 3 + ch];
+    shq::dz(c, tg);
+    shq::dx<false>(c);
+    shq::dz(c, tb);
+    shq::dx<true>(c);
+    shq::dz(c, ta);
 #pragma unroll
-    for (int i = 0; i < 3; ++i) out[i] = b1.v[i][0] * in[0] + b1.v[i][1] * in[1] + b1.v[i][2] * in[2];
-#pragma unroll
-    for (int i = 0; i < 3; ++i) s[(1 + i) * 3 + c] = out[i];
-  }
-  ShBand<2> b2;
-  sh_fill<2>(b2, b1, b1, std::make_integer_sequence<int, 25>{});
-#pragma unroll
-  for (int c = 0; c < 3; ++c) {
-    float in[5], out[5];
-#pragma unroll
-    for (int i = 0; i < 5; ++i) in[i] = s[(4 + i) * 3 + c];
-#pragma unroll
-    for (int i = 0; i < 5; ++i) {
-      float a = 0.0f;
-#pragma unroll
-      for (int j = 0; j < 5; ++j) a += b2.v[i][j] * in[j];
-      out[i] = a;
-    }
-#pragma unroll
-    for (int i = 0; i < 5; ++i) s[(4 + i) * 3 + c] = out[i];
-  }
-  ShBand<3> b3;
-  sh_fill<3>(b3, b1, b2, std::make_integer_sequence<int, 49>{});
-#pragma unroll
-  for (int c = 0; c < 3; ++c) {
-    float in[7], out[7];
-#pragma unroll
-    for (int i = 0; i < 7; ++i) in[i] = s[(9 + i) * 3 + c];
-#pragma unroll
-    for (int i = 0; i < 7; ++i) {
-      float a = 0.0f;
-#pragma unroll
-      for (int j = 0; j < 7; ++j) a += b3.v[i][j] * in[j];
-      out[i] = a;
-    }
-#pragma unroll
-    for (int i = 0; i < 7; ++i) s[(9 + i) * 3 + c] = out[i];
-  }
-  if (FLIP) {
-#pragma unroll
-    for (int k = 1; k < 16; k += 2) {
-      s[k * 3 + 0] = -s[k * 3 + 0];
-      s[k * 3 + 1] = -s[k * 3 + 1];
-      s[k * 3 + 2] = -s[k * 3 + 2];
-    }
+    for (int k = 1; k < 16; ++k) s[k * 3 + ch] = (FLIP && (k & 1)) ? -c[k] : c[k];
   }
 }
 

@@ -194,13 +194,13 @@ constexpr int kMbarPolls = 1 << 18;
 // The refit of one Gaussian from its six blended endpoints e (UpdateAsSix-
 // PointsWithdrawBad, GaussianView.cpp:3081-3166): centre, polar factor R of
 // the endpoint matrix, quaternion, scale, Sigma; writes mu, q, scale and
-// Sigma of Gaussian i and returns in Rr the rotation q q_old^-1 that rotates
-// its SH.
+// Sigma of Gaussian i and returns in qr the rotation q q_old^-1 (a unit
+// quaternion) that rotates its SH.
 template <bool MIXED>
 __device__ __forceinline__ void refit_gaussian(int i, const float (&e)[18], const float (&s0v)[3], float4 q_old,
                                                float* __restrict__ pos_out, float* __restrict__ rot_out,
                                                float* __restrict__ scale_out, float* __restrict__ cov_out,
-                                               int* __restrict__ status, float (&Rr)[9]) {
+                                               int* __restrict__ status, float4& qr) {
   float cx = 0.f, cy = 0.f, cz = 0.f;
 #pragma unroll
   for (int ep = 0; ep < 6; ++ep) {
@@ -276,11 +276,12 @@ __device__ __forceinline__ void refit_gaussian(int i, const float (&e)[18], cons
 #pragma unroll
     for (int q6 = 0; q6 < 6; ++q6) cov_out[6 * (size_t)i + q6] = S[q6];
   }
-  quat_to_rowmajor(quat_normalize(quat_mul(q, quat_inverse(q_old))), Rr);
+  qr = quat_normalize(quat_mul(q, quat_inverse(q_old)));
 }
 
-// Rotates the staged 48-float SH record rec (kShStride floats) by Rr.
-__device__ __forceinline__ void rotate_sh_record(float* rec_f, const float (&Rr)[9]) {
+// Rotates the staged 48-float SH record rec (kShStride floats) by the unit
+// quaternion qr.
+__device__ __forceinline__ void rotate_sh_record(float* rec_f, float4 qr) {
   float4* rec = reinterpret_cast<float4*>(rec_f);
   float v[48];
 #pragma unroll
@@ -291,7 +292,7 @@ __device__ __forceinline__ void rotate_sh_record(float* rec_f, const float (&Rr)
     v[4 * q4 + 2] = u.z;
     v[4 * q4 + 3] = u.w;
   }
-  rotate_sh48<true>(Rr, v);
+  rotate_sh48<true>(qr, v);
 #pragma unroll
   for (int q4 = 0; q4 < 12; ++q4) rec[q4] = make_float4(v[4 * q4], v[4 * q4 + 1], v[4 * q4 + 2], v[4 * q4 + 3]);
 }
@@ -358,9 +359,9 @@ __global__ void __launch_bounds__(kSkinThreads, 4)
   asm volatile("cp.async.wait_group 0;" ::: "memory");
   __syncthreads();
   if (active && !is_static) {
-    float Rr[9];
-    refit_gaussian<MIXED>(i, e, s0v, s_q[t], pos_out, rot_inout, scale_out, cov_out, status, Rr);
-    if (shs) rotate_sh_record(s_sh + t * kShStride, Rr);
+    float4 qr;
+    refit_gaussian<MIXED>(i, e, s0v, s_q[t], pos_out, rot_inout, scale_out, cov_out, status, qr);
+    if (shs) rotate_sh_record(s_sh + t * kShStride, qr);
   }
   if (shs) {
     __syncthreads();
@@ -455,15 +456,23 @@ __global__ void __launch_bounds__(kSkinThreads, 4)
 #pragma unroll
     for (int a = 0; a < 3; ++a) s0v[a] = __ldg(scale0 + 3 * (size_t)i + a);
   }
-  if (local) {
+  {
+    // every slot of the tile's node list holds a valid node id (the plan
+    // fills the slots past the tile's count), so the records are requested
+    // without waiting for the count: two list loads, then the two records
+    static_assert(kPlanNodes == 2 * kSkinThreads, "two list slots per thread");
     const int32_t* list = plan.tile_nodes + (size_t)blockIdx.x * kPlanNodes;
-    for (int u = t; u < n_local; u += kSkinThreads) {
-      const NodeAf r = node_affine(load_node(table, __ldg(list + u)), o_x, o_y, o_z);
-      float4* d4 = reinterpret_cast<float4*>(s_nodes + u * kPlanRec);
-      d4[0] = r.a;
-      d4[1] = r.b;
-      d4[2] = r.c;
-    }
+    const int id0 = __ldg(list + t), id1 = __ldg(list + kSkinThreads + t);
+    const NodeXf x0 = load_node(table, id0), x1 = load_node(table, id1);
+    const NodeAf r0 = node_affine(x0, o_x, o_y, o_z), r1 = node_affine(x1, o_x, o_y, o_z);
+    float4* d0 = reinterpret_cast<float4*>(s_nodes + t * kPlanRec);
+    float4* d1 = reinterpret_cast<float4*>(s_nodes + (kSkinThreads + t) * kPlanRec);
+    d0[0] = r0.a;
+    d0[1] = r0.b;
+    d0[2] = r0.c;
+    d1[0] = r1.a;
+    d1[1] = r1.b;
+    d1[2] = r1.c;
   }
   // node records written; every thread waits for the bulk copies itself
   __syncthreads();
@@ -518,13 +527,13 @@ __global__ void __launch_bounds__(kSkinThreads, 4)
   // arrive while the refit runs
   __syncthreads();
   if (shs) stage_sh(s_sh, shs, tile0, cnt);
-  float Rr[9];
+  float4 qr;
   const bool refit = active && !is_static;
-  if (refit) refit_gaussian<MIXED>(i, e, s0v, s_q[t], pos_out, rot_inout, scale_out, cov_out, status, Rr);
+  if (refit) refit_gaussian<MIXED>(i, e, s0v, s_q[t], pos_out, rot_inout, scale_out, cov_out, status, qr);
   if (shs) {
     asm volatile("cp.async.wait_group 0;" ::: "memory");
     __syncthreads();
-    if (refit) rotate_sh_record(s_sh + t * kShStride, Rr);
+    if (refit) rotate_sh_record(s_sh + t * kShStride, qr);
     __syncthreads();
     store_sh(shs, s_sh, tile0, cnt);
   }
@@ -762,14 +771,20 @@ __global__ void __launch_bounds__(kSkinThreads)
   const float o_x = __ldg(ends_in + tile0), o_y = __ldg(ends_in + (size_t)N + tile0),
               o_z = __ldg(ends_in + 2 * (size_t)N + tile0);
   {
+    // every list slot holds a valid node id: both records are requested
+    // without waiting for the tile's count
     const int32_t* list = plan.tile_nodes + (size_t)blockIdx.x * kPlanNodes;
-    for (int u = t; u < n_stage; u += kSkinThreads) {
-      const NodeAf r = node_affine(load_node(table, __ldg(list + u)), o_x, o_y, o_z);
-      float4* d4 = reinterpret_cast<float4*>(s_nodes + u * kPlanRec);
-      d4[0] = r.a;
-      d4[1] = r.b;
-      d4[2] = r.c;
-    }
+    const int id0 = __ldg(list + t), id1 = __ldg(list + kSkinThreads + t);
+    const NodeXf x0 = load_node(table, id0), x1 = load_node(table, id1);
+    const NodeAf r0 = node_affine(x0, o_x, o_y, o_z), r1 = node_affine(x1, o_x, o_y, o_z);
+    float4* d0 = reinterpret_cast<float4*>(s_nodes + t * kPlanRec);
+    float4* d1 = reinterpret_cast<float4*>(s_nodes + (kSkinThreads + t) * kPlanRec);
+    d0[0] = r0.a;
+    d0[1] = r0.b;
+    d0[2] = r0.c;
+    d1[0] = r1.a;
+    d1[1] = r1.b;
+    d1[2] = r1.c;
   }
   asm volatile("cp.async.wait_group 0;" ::: "memory");
   __syncthreads();
@@ -971,9 +986,7 @@ __global__ void __launch_bounds__(kSkinThreads)
     asm volatile("cp.async.wait_group 0;" ::: "memory");
     __syncthreads();
     if (moving) {
-      float Rr[9];
-      quat_to_rowmajor(quat_normalize(wq), Rr);
-      rotate_sh_record(s_ft + t * kShStride, Rr);
+      rotate_sh_record(s_ft + t * kShStride, quat_normalize(wq));
     }
   }
   __syncthreads();
@@ -1101,7 +1114,10 @@ static int launch_skin_g(bool mixed, int N, float* ends, const int32_t* eidx, co
                          cudaStream_t s) {
   const int grid = grid_for(N, kSkinTile);
   if (PLANNED) {
-    constexpr int smem = PlanTile<K>::kSmem;
+    // at least 48 KB per CTA: four CTAs per SM.  The kernel's 96 registers
+    // would allow five, which measured slower on a GB300 (98.9 against 88.7 us
+    // at twist300k): the five CTAs' shared memory leaves L1 almost nothing.
+    constexpr int smem = PlanTile<K>::kSmem > 48 * 1024 ? PlanTile<K>::kSmem : 48 * 1024;
     auto kern = mixed ? skin_gaussians_planned_kernel<K, true> : skin_gaussians_planned_kernel<K, false>;
     if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess) {
       (void)cudaGetLastError();
@@ -1427,8 +1443,10 @@ extern "C" int arap_skin_plan_create(arap_skin_plan** out, int N, int k, const i
   p->dev = SkinPlanDev{count, nodes, blk, ioff, iref};
   p->status = reinterpret_cast<int*>(base + b_count + b_nodes + b_blk + b_ioff + b_iref);
   // padded neighbour slots (k not a multiple of 4) and the rows of a partial
-  // last tile stay zero
-  if (cudaMemsetAsync(blk, 0, b_blk, st) != cudaSuccess || cudaMemsetAsync(p->status, 0, sizeof(int), st) != cudaSuccess) {
+  // last tile stay zero; node-list slots the plan kernel leaves unset (past a
+  // tile's count, and every slot of an overflow tile) hold node 0
+  if (cudaMemsetAsync(blk, 0, b_blk, st) != cudaSuccess || cudaMemsetAsync(p->status, 0, sizeof(int), st) != cudaSuccess ||
+      cudaMemsetAsync(nodes, 0, b_nodes, st) != cudaSuccess) {
     arap_skin_plan_destroy(p);
     return ARAP_ECUDA;
   }
