@@ -30,7 +30,7 @@ class SolveConfig(C.Structure):
                 ("weighting_factor", C.c_float), ("cons_on_center", C.c_int),
                 ("max_iters", C.c_int), ("early_exit", C.c_int), ("precision", C.c_int),
                 ("pcg_tol", C.c_float), ("pcg_max_iters", C.c_int), ("coarse_nodes", C.c_int),
-                ("spin_limit", C.c_int)]
+                ("spin_limit", C.c_int), ("coarse_reuse", C.c_float)]
 
 
 class GridInfo(C.Structure):
@@ -44,7 +44,8 @@ class SolveStats(C.Structure):
                 ("halvings", C.c_int), ("initial_energy", C.c_double), ("final_energy", C.c_double),
                 ("n_free", C.c_int), ("n_static", C.c_int), ("n_rows", C.c_int),
                 ("n_coarse", C.c_int), ("phase_ms", C.c_double * 9), ("resident", C.c_int),
-                ("coarse_fallbacks", C.c_int), ("iteration_halvings", C.c_int * 64)]
+                ("coarse_fallbacks", C.c_int), ("iteration_halvings", C.c_int * 64),
+                ("coarse_inversions", C.c_int)]
 
     def as_dict(self):
         d = {f: getattr(self, f) for f, _ in self._fields_}

@@ -36,4 +36,5 @@ extern "C" void arap_solve_config_default(arap_solve_config* cfg) {
   cfg->pcg_max_iters = 0;
   cfg->coarse_nodes = 0;
   cfg->spin_limit = 0;
+  cfg->coarse_reuse = 0.0f;
 }

@@ -415,6 +415,7 @@ extern "C" int arap_solver_create(arap_solver** out, int n, int k, const int32_t
   s->free_host = free_ids;
   if (s->cfg.pcg_tol <= 0.f) s->cfg.pcg_tol = cfg.precision == ARAP_PRECISION_MIXED ? 1e-6f : 1e-6f;
   if (s->cfg.pcg_max_iters <= 0) s->cfg.pcg_max_iters = 2000;
+  if (s->cfg.coarse_reuse == 0.f) s->cfg.coarse_reuse = 0.05f;
   const int grid = cfg.precision == ARAP_PRECISION_MIXED ? occupancy_grid<double>(2) : occupancy_grid<float>(2);
   if (grid <= 0) {
     delete s;
@@ -553,6 +554,7 @@ extern "C" int arap_solver_create(arap_solver** out, int n, int k, const int32_t
   P.early_exit = cfg.early_exit;
   P.pcg_max = s->cfg.pcg_max_iters;
   P.pcg_tol = s->cfg.pcg_tol;
+  P.coarse_reuse = s->cfg.coarse_reuse > 0.f ? s->cfg.coarse_reuse : 0.f;
   P.mode = 0;
   P.refine = 0;
   P.NA = NA;
@@ -604,6 +606,7 @@ static int fill_stats(const arap_solver* s, const double* st8, int dev_status, a
   stats_host->n_coarse = s->P.NC;
   stats_host->resident = s->P.resident ? 1 : 0;
   stats_host->coarse_fallbacks = (int)st8[ST_CFALL];
+  stats_host->coarse_inversions = (int)st8[ST_CINV_N];
   {
     const int n_it = std::min((int)st8[ST_ITERS], kHalvIters);
     for (int it = 0; it < n_it; ++it)

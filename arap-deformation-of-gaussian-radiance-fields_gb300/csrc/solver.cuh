@@ -68,6 +68,7 @@ struct SolveParams {
   const int32_t* order;      // [F] processing order of the free nodes (cost-balanced)
   int max_iters, early_exit, pcg_max;
   float pcg_tol;
+  float coarse_reuse;        // keep the coarse inverse while the last step < coarse_reuse |x|
   int mode;                  // 0 solve, 1 gradient/energy only
   int refine;                // mixed precision: FP64 refinement sweeps per solve
   // two-level preconditioner (coarse space: one affine ED transform per

@@ -16,7 +16,7 @@ namespace arap {
 enum {
   ST_ITERS = 0, ST_PCG = 1, ST_HALV = 2, ST_E0 = 3, ST_E = 4, ST_CONV = 5, ST_NONFINITE = 6,
   ST_T_PREP = 8, ST_T_GRAD = 9, ST_T_COARSE = 10, ST_T_PCG = 11, ST_T_LS = 12, ST_T_CINV = 13,
-  ST_T_W_SPMV = 14, ST_T_W_UPD = 15, ST_T_W_CSOLVE = 16, ST_CFALL = 17
+  ST_T_W_SPMV = 14, ST_T_W_UPD = 15, ST_T_W_CSOLVE = 16, ST_CFALL = 17, ST_CINV_N = 18
 };
 constexpr int ST_HALV_IT = 24;  // cumulative halvings after each of the first kHalvIters GN iterations
 constexpr int kHalvIters = 64;
@@ -374,6 +374,12 @@ __device__ __forceinline__ void solve_body(const SolveParams& P, int bid, int nb
   lap(0);
   double e_first = 0.0, e_last = 0.0;
   int iters = 0, pcg_total = 0, halvings = 0, converged = 0;
+  // reuse of the coarse inverse: the last accepted step and |x| before it,
+  // whether an inverse is held (and its pivots were positive), PCG iterations
+  // of the last system and of the last one solved with a fresh inverse
+  double step_prev = 0.0, normv_prev = 0.0;
+  int inv_held = 0, inv_ok = 0, pcg_prev = 0, pcg_fresh = 0, n_inv = 0;
+  bool fresh = false;
   for (int it = 0; it < P.max_iters; ++it) {
     // ---- gradient -J^T f, energy, preconditioner, PCG start (h=0, r=g, z=M^-1 g)
     double red[3] = {0.0, 0.0, 0.0};
@@ -468,16 +474,34 @@ __device__ __forceinline__ void solve_body(const SolveParams& P, int bid, int nb
     float rr = (float)rr0;
     int coarse_ok = 0;
     if (coarse) {
+      // The coarse inverse is the preconditioner's only: the PCG solves the
+      // same system to the same tolerance with any of them.  So the previous
+      // iteration's inverse is kept while the last accepted step was below
+      // coarse_reuse of |x| (the orthogonality blocks, the only part of the
+      // coarse matrix that depends on x, have barely moved) and the last PCG
+      // took at most 1.5 times the iterations of the last one run with a
+      // fresh inverse.  Every CTA takes the same decision (the norms are the
+      // same bits everywhere).
+      fresh = !(inv_held && inv_ok && step_prev < (double)P.coarse_reuse * normv_prev &&
+                2 * pcg_prev <= 3 * pcg_fresh);
       // coarse matrix at this x: fixed kernels + current orthogonality blocks
       const double* rot_now = P.rotagg + (it & 1) * 81 * P.NA;
       double* rot_next = P.rotagg + ((it + 1) & 1) * 81 * P.NA;
       const size_t NC2 = (size_t)P.NC * P.NC;
-      for (size_t e = gt; e < NC2; e += nt) P.Cw[e] = coarse_entry_x(P, rot_now, (int)(e / P.NC), (int)(e % P.NC));
+      if (fresh)
+        for (size_t e = gt; e < NC2; e += nt) P.Cw[e] = coarse_entry_x(P, rot_now, (int)(e / P.NC), (int)(e % P.NC));
       for (int e = gt; e < 81 * P.NA; e += nt) rot_next[e] = 0.0;
       if (!gs.sync()) return;
-      if (threadIdx.x == 0) s_clk.inv0 = global_ns();
-      if (!coarse_invert(P, gs, &coarse_ok, s_scratch)) return;
-      if (threadIdx.x == 0) s_clk.acc[5] += (double)(global_ns() - s_clk.inv0);
+      if (fresh) {
+        if (threadIdx.x == 0) s_clk.inv0 = global_ns();
+        if (!coarse_invert(P, gs, &coarse_ok, s_scratch)) return;
+        if (threadIdx.x == 0) s_clk.acc[5] += (double)(global_ns() - s_clk.inv0);
+        inv_held = 1;
+        inv_ok = coarse_ok;
+        ++n_inv;
+      } else {
+        coarse_ok = inv_ok;
+      }
       // a pivot of the coarse inversion that is not positive: this
       // iteration's PCG runs with block-Jacobi alone; counted in the stats
       if (!coarse_ok && gt == 0) P.stats[ST_CFALL] += 1.0;
@@ -732,6 +756,8 @@ __device__ __forceinline__ void solve_body(const SolveParams& P, int bid, int nb
     if (coarse)
       for (int e = gt; e < 2 * P.NC; e += nt) P.rc[e] = 0.0;
     pcg_total += pi;
+    pcg_prev = pi;
+    if (fresh) pcg_fresh = pi;
     work_flush();
     lap(3);
 
@@ -780,6 +806,8 @@ __device__ __forceinline__ void solve_body(const SolveParams& P, int bid, int nb
       }
     }
     const double normh = (double)scale * sqrt(hh);
+    step_prev = normh;
+    normv_prev = normv;
     if (gt == 0 && it < kHalvIters) P.stats[ST_HALV_IT + it] = halvings;
     iters = it + 1;
     if (!gs.sync()) return;
@@ -820,6 +848,7 @@ __device__ __forceinline__ void solve_body(const SolveParams& P, int bid, int nb
   if (gt == 0) {
     P.stats[ST_ITERS] = iters;
     P.stats[ST_PCG] = pcg_total;
+    P.stats[ST_CINV_N] = n_inv;
     P.stats[ST_HALV] = halvings;
     P.stats[ST_E0] = e_first;
     P.stats[ST_E] = e_last;

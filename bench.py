@@ -594,6 +594,7 @@ def run_ours(a):
         "gpu_launches": launches_per_step * a.steps,
         "solve": {"bound": "latency (L2-resident persistent kernel; reported per PCG iteration)",
                   "pcg_iterations": stats["pcg_iterations"], "gn_iterations": stats["gn_iterations"],
+                  "coarse_inversions": stats["coarse_inversions"],
                   "us_per_pcg_iteration": round(1000.0 * stats["phase_ms"]["pcg"] / max(1, stats["pcg_iterations"]), 2),
                   "phase_ms": {k: round(v, 3) for k, v in stats["phase_ms"].items()},
                   "final_energy": stats["final_energy"]},

@@ -109,6 +109,13 @@ typedef struct {
                              a second); every CTA then leaves the kernel.  A solver
                              with a limit of its own runs on the batched-solve kernel
                              as a batch of one (the same results, a little slower) */
+  float coarse_reuse;     /* two-level PCG: a Gauss-Newton iteration keeps the previous
+                             iteration's coarse inverse when the last accepted step was
+                             below this fraction of |x| and the last PCG took at most 1.5
+                             times the iterations of the last one with a fresh inverse.
+                             It changes the preconditioner only: every PCG still meets
+                             pcg_tol.  0: the default, 0.05; < 0: invert every
+                             iteration */
 } arap_solve_config;
 
 typedef struct {
@@ -136,6 +143,8 @@ typedef struct {
   int iteration_halvings[64]; /* line-search step halvings of each of the first 64
                              Gauss-Newton iterations (Deform.cpp:144-156; 0 past
                              gn_iterations) */
+  int coarse_inversions;  /* Gauss-Newton iterations that formed and inverted the coarse
+                             matrix (the others kept the previous inverse, coarse_reuse) */
 } arap_solve_stats;
 
 typedef struct arap_solver arap_solver;

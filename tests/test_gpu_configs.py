@@ -5,7 +5,10 @@ on the GPU against the float64 oracle.
   twist300k (300k Gaussians, 64^3 grid, 4061 nodes, k=8, 20 iterations, the
   benchmarked frame), each in the chosen form (mixed precision, two-level
   PCG with 64-node aggregates), the plain form (FP32, block-Jacobi) and
-  FP32 with the two-level PCG (plain2l).
+  FP32 with the two-level PCG (plain2l); the chosen form also with a fresh
+  coarse inverse in every Gauss-Newton iteration (chosen_fresh; the default
+  keeps the previous inverse while the steps are small, which changes the
+  preconditioner only).
 * Node transforms against the numpy oracle's Gauss-Newton solve of the same
   scene (tests/golden/solve_<scene>.npz, made by
   tests/golden/make_solve_golden.py; exact sparse solve, Deform.cpp:95-169).
@@ -72,14 +75,15 @@ def _oracle_frame(d, sc, samples, feature, X):
     return fr, nodes
 
 
-_FORMS = {"chosen": (1, 64), "plain": (0, 0), "plain2l": (0, 64)}
+_FORMS = {"chosen": (1, 64, 0.0), "chosen_fresh": (1, 64, -1.0), "plain": (0, 0, 0.0), "plain2l": (0, 64, 0.0)}
 
 
-@pytest.mark.parametrize("form", ["chosen", "plain", "plain2l"])
+@pytest.mark.parametrize("form", ["chosen", "chosen_fresh", "plain", "plain2l"])
 def test_frame_matches_the_oracle(dev, case, form):
     sc, samples, feature, g = case
-    precision, coarse = _FORMS[form]
-    cfg = dev.default_config(max_iters=sc.iters, early_exit=0, precision=precision, coarse_nodes=coarse)
+    precision, coarse, reuse = _FORMS[form]
+    cfg = dev.default_config(max_iters=sc.iters, early_exit=0, precision=precision, coarse_nodes=coarse,
+                             coarse_reuse=reuse)
     d = dev.GaussianDeformer(torch.as_tensor(sc.pos), torch.as_tensor(sc.rot), torch.as_tensor(sc.scale),
                              torch.as_tensor(sc.shs), sc.node_vertex, sc.k, sc.blocks, sc.block_type,
                              sample_pos=torch.as_tensor(samples), feature=torch.as_tensor(feature), config=cfg)
@@ -103,9 +107,15 @@ def test_frame_matches_the_oracle(dev, case, form):
         "feature": float(np.abs(_np(d.feature) - fr.feature).max()),
         "nodes": float(np.abs(_np(d.node_pos) - nodes_ref).max() / ext),
     }
-    print("%s %s: pcg %d, halvings %d (oracle %d), errors %s" % (
-        sc.name, form, st["pcg_iterations"], st["halvings"], int(g["halvings"].sum()),
+    print("%s %s: pcg %d, coarse inversions %d, halvings %d (oracle %d), errors %s" % (
+        sc.name, form, st["pcg_iterations"], st["coarse_inversions"], st["halvings"], int(g["halvings"].sum()),
         {k: "%.2e" % v for k, v in err.items()}))
+    if coarse == 0:
+        assert st["coarse_inversions"] == 0
+    elif reuse < 0:
+        assert st["coarse_inversions"] == st["gn_iterations"]
+    else:
+        assert 1 <= st["coarse_inversions"] <= st["gn_iterations"]
     if form != "plain2l":
         # the line search takes the oracle's branch in every Gauss-Newton
         # iteration.  Not so for FP32 residuals with the two-level PCG: at
@@ -115,8 +125,9 @@ def test_frame_matches_the_oracle(dev, case, form):
         assert st["halvings"] == int(g["halvings"].sum())
         assert st["iteration_halvings"] == [int(v) for v in g["halvings"]]
     assert abs(st["initial_energy"] - g["energies"][0]) <= 1e-5 * g["energies"][0]
-    assert err_x <= (1e-5 if form == "chosen" else 5e-5)
-    tol = 1e-5 if form == "chosen" else 5e-5
+    chosen = precision == 1
+    assert err_x <= (1e-5 if chosen else 5e-5)
+    tol = 1e-5 if chosen else 5e-5
     assert err["mu"] <= tol and err["sample_pos"] <= tol and err["nodes"] <= tol
     assert err["sigma"] <= tol and err["q"] <= tol and err["scale"] <= tol
     assert err["shs"] <= 2e-4 and err["feature"] <= 2e-4
