@@ -194,8 +194,8 @@ def restore(st, snap):
 # (dram__bytes_read.sum + dram__bytes_write.sum of one launch inside the
 # bench's frame), keyed by (scene, k, planned) for the Gaussian skinning and
 # (scene, k) for the sample skinning.
-SKIN_DRAM_BYTES = {("twist300k", 8, True): 161548032 + 43893504}
-SAMPLES_DRAM_BYTES = {("twist300k", 8): 413570304 + 252652544}
+SKIN_DRAM_BYTES = {("twist300k", 8, True): 162642432 + 44834560}
+SAMPLES_DRAM_BYTES = {("twist300k", 8): 413555456 + 252287488}
 
 
 def samples_roofline(st, k, ms, peak, peak_kind, traffic=None):
