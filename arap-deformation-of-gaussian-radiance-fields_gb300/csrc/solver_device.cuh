@@ -325,12 +325,41 @@ __device__ __forceinline__ void q_add(float (&Q)[10], float v0, float v1, float 
 
 enum { PASS_GRAD = 0, PASS_ENERGY = 1 };
 
+// One of three values, chosen by i in 0..2 (selects, no indexed registers).
+template <typename T>
+__device__ __forceinline__ T sel3(int i, T a, T b, T c) {
+  return i == 0 ? a : (i == 1 ? b : c);
+}
+
+// Sums v[0..15] over the warp by recursive halving: at each step a lane keeps
+// the half of its values that its partner sends away, so 16 values take
+// 8 + 4 + 2 + 1 + 1 additions instead of 16 x 5.  Lane l returns the total
+// of value l >> 1.  The FP64 pipe of this part retires a warp instruction
+// every 16 SM cycles, shared by all warps of the SM; the butterfly of each
+// value separately was a third of the gradient pass.
+template <typename T>
+__device__ __forceinline__ T warp_reduce_scatter16(T (&v)[16]) {
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int h = 8, off = 16; h >= 1; h >>= 1, off >>= 1) {
+    const bool up = (lane & off) != 0;
+#pragma unroll
+    for (int i = 0; i < h; ++i) {
+      const T keep = up ? v[h + i] : v[i];
+      const T send = up ? v[i] : v[h + i];
+      v[i] = keep + __shfl_xor_sync(0xffffffffu, send, off);
+    }
+  }
+  return v[0] + __shfl_xor_sync(0xffffffffu, v[0], 1);
+}
+
 // Residual rows owned by free node r, at x + scale*h.  PASS_GRAD also returns
-// acc = (J^T f)_r (every item touching x_r) and Q, the 4x4 kernel of the
-// non-rotation part of the diagonal block of J^T J.  All lanes of the warp
-// call it; the outputs are warp-reduced and valid in every lane.
+// in g_lane the lane's entry of (J^T f)_r (every item touching x_r; lanes
+// 0..11, the others 0) and Q, the 4x4 kernel of the non-rotation part of the
+// diagonal block of J^T J (valid in every lane).  All lanes of the warp call
+// it; energy is warp-reduced and valid in every lane.
 template <typename RT, int PASS>
-__device__ void residual_node(const SolveParams& P, int r, RT scale, RT (&acc)[12], float (&Q)[10],
+__device__ void residual_node(const SolveParams& P, int r, RT scale, RT& g_lane, float (&Q)[10],
                               double& energy) {
   const int lane = threadIdx.x & 31;
   const int j = __ldg(P.free_ids + r);
@@ -340,6 +369,7 @@ __device__ void residual_node(const SolveParams& P, int r, RT scale, RT (&acc)[1
                         __ldg(P.node_pos + 3 * (size_t)j + 2)};
   RT xj[12];
   load_x<RT>(P, r, scale, xj);
+  RT acc[12];
 #pragma unroll
   for (int i = 0; i < 12; ++i) acc[i] = RT(0);
 #pragma unroll
@@ -424,37 +454,51 @@ __device__ void residual_node(const SolveParams& P, int r, RT scale, RT (&acc)[1
       }
     }
   }
-  if (lane == 0) {
-    // orthogonality rows (Deform.cpp:384-404) from the offsets D = R - I:
-    // c_a . c_b = D_ab + D_ba + D_a . D_b,  |c_a|^2 - 1 = 2 D_aa + |D_a|^2
-    const RT wr = RT(P.wr);
-    const RT* D0 = xj;
-    const RT* D1 = xj + 3;
-    const RT* D2 = xj + 6;
-    auto dot3 = [](const RT* a, const RT* b) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; };
-    const RT f[6] = {wr * (D0[1] + D1[0] + dot3(D0, D1)),
-                     wr * (D0[2] + D2[0] + dot3(D0, D2)),
-                     wr * (D1[2] + D2[1] + dot3(D1, D2)),
-                     wr * (RT(2) * D0[0] + dot3(D0, D0)),
-                     wr * (RT(2) * D1[1] + dot3(D1, D1)),
-                     wr * (RT(2) * D2[2] + dot3(D2, D2))};
+  // orthogonality rows (Deform.cpp:384-404) from the offsets D = R - I, one
+  // row per lane 0..5 (the same instructions for all six, the operands chosen
+  // per lane): rows (a, b) = (0,1) (0,2) (1,2) (0,0) (1,1) (2,2),
+  //   f = w_rot (D_ab + D_ba + D_a . D_b)
+  // (c_a . c_b for a != b, |c_a|^2 - 1 for a == b; D_a is column a)
+  const RT wr = RT(P.wr);
+  RT fo = RT(0);
+  {
+    const int a = (lane == 2 || lane == 4) ? 1 : (lane == 5 ? 2 : 0);
+    const int b = (lane == 0 || lane == 4) ? 1 : ((lane == 1 || lane == 2 || lane == 5) ? 2 : 0);
+    RT Da[3], Db[3];
 #pragma unroll
-    for (int i = 0; i < 6; ++i) e += double(f[i]) * double(f[i]);
-    if (PASS == PASS_GRAD) {
-      const RT c0[3] = {RT(1) + D0[0], D0[1], D0[2]};
-      const RT c1[3] = {D1[0], RT(1) + D1[1], D1[2]};
-      const RT c2[3] = {D2[0], D2[1], RT(1) + D2[2]};
-#pragma unroll
-      for (int c = 0; c < 3; ++c) {
-        acc[c] += wr * (f[0] * c1[c] + f[1] * c2[c] + RT(2) * f[3] * c0[c]);
-        acc[3 + c] += wr * (f[0] * c0[c] + f[2] * c2[c] + RT(2) * f[4] * c1[c]);
-        acc[6 + c] += wr * (f[1] * c0[c] + f[2] * c1[c] + RT(2) * f[5] * c2[c]);
-      }
+    for (int i = 0; i < 3; ++i) {
+      Da[i] = sel3(a, xj[i], xj[3 + i], xj[6 + i]);
+      Db[i] = sel3(b, xj[i], xj[3 + i], xj[6 + i]);
     }
+    const RT f = wr * (sel3(b, Da[0], Da[1], Da[2]) + sel3(a, Db[0], Db[1], Db[2]) +
+                       (Da[0] * Db[0] + Da[1] * Db[1] + Da[2] * Db[2]));
+    if (lane < 6) fo = f;
   }
+  e += double(fo) * double(fo);
   if (PASS == PASS_GRAD) {
+    // lane L < 9 adds d/dR(col, c) of the six rows, col = L / 3, c = L % 3:
+    //   col 0: w_rot (f0 c1 + f1 c2 + 2 f3 c0), col 1: w_rot (f0 c0 + f2 c2 + 2 f4 c1),
+    //   col 2: w_rot (f1 c0 + f2 c1 + 2 f5 c2), c_X = column X of R, entry c
+    const int col = lane < 3 ? 0 : (lane < 6 ? 1 : 2), c = lane - 3 * col;
+    const RT fA = __shfl_sync(0xffffffffu, fo, col == 2 ? 1 : 0);
+    const RT fB = __shfl_sync(0xffffffffu, fo, col == 0 ? 1 : 2);
+    const RT fD = __shfl_sync(0xffffffffu, fo, 3 + col);
+    const int pA = col == 0 ? 1 : 0, pB = col == 1 ? 2 : (col == 0 ? 2 : 1);
+    RT cc[3];  // entry c of the columns of R
 #pragma unroll
-    for (int i = 0; i < 12; ++i) acc[i] = warp_sum(acc[i]);
+    for (int X = 0; X < 3; ++X)
+      cc[X] = sel3(c, xj[3 * X], xj[3 * X + 1], xj[3 * X + 2]) + ((X == c) ? RT(1) : RT(0));
+    const RT go = wr * (fA * sel3(pA, cc[0], cc[1], cc[2]) + fB * sel3(pB, cc[0], cc[1], cc[2]) +
+                        RT(2) * fD * sel3(col, cc[0], cc[1], cc[2]));
+    RT v[16];
+#pragma unroll
+    for (int i = 0; i < 12; ++i) v[i] = acc[i];
+#pragma unroll
+    for (int i = 12; i < 16; ++i) v[i] = RT(0);
+    const RT tot = warp_reduce_scatter16(v);  // lane l: entry l >> 1
+    g_lane = __shfl_sync(0xffffffffu, tot, 2 * (lane & 15));
+    if (lane < 9) g_lane += go;
+    if (lane >= 12) g_lane = RT(0);
 #pragma unroll
     for (int i = 0; i < 10; ++i) Q[i] = warp_sum(Q[i]);
   }

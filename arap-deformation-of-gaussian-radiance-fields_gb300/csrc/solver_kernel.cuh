@@ -398,19 +398,13 @@ __device__ __forceinline__ void solve_body(const SolveParams& P, int bid, int nb
     for (int ws = wib; ws * nbk + bid < F; ws += kSolveWarps) {
       const bool stg = ws < s_stg.n;
       const int r = stg ? stg_node()[ws].x : __ldg(P.order + ws * nbk + bid);
-      RT acc[12];
+      RT g_lane;  // this lane's entry of (J^T f)_r (lanes 0..11)
       float Q[10];
       double en;
-      residual_node<RT, PASS_GRAD>(P, r, RT(0), acc, Q, en);
+      residual_node<RT, PASS_GRAD>(P, r, RT(0), g_lane, Q, en);
       if (lane == 0) red[0] += en;
       if (P.mode == 1) {
-        if (lane < 12) {
-          double a = 0.0;
-#pragma unroll
-          for (int i = 0; i < 12; ++i)
-            if (i == lane) a = (double)acc[i];
-          P.grad_out[12 * (size_t)r + lane] = a;
-        }
+        if (lane < 12) P.grad_out[12 * (size_t)r + lane] = (double)g_lane;
         continue;
       }
       if (stg)
@@ -418,10 +412,7 @@ __device__ __forceinline__ void solve_body(const SolveParams& P, int bid, int nb
       else
         build_dinv<false>(P, r, 0, Q);
       if (coarse) coarse_rot_node(P, r, P.rotagg + (it & 1) * 81 * P.NA);
-      float gc = 0.f;
-#pragma unroll
-      for (int i = 0; i < 12; ++i)
-        if (i == lane) gc = -(float)acc[i];
+      const float gc = lane < 12 ? -(float)g_lane : 0.f;
       const float zc = stg ? apply_dinv<true>(P, r, ws, gc) : apply_dinv<false>(P, r, 0, gc);
       // (the resident PCG restricts r - A z1 itself)
       if (coarse && !resident) coarse_restrict(P, r, gc, P.rc);
@@ -769,10 +760,10 @@ __device__ __forceinline__ void solve_body(const SolveParams& P, int bid, int nb
       double en2[2] = {0.0, 0.0};
       for (int ws = wib; ws * nbk + bid < F; ws += kSolveWarps) {
         const int r = __ldg(P.order + ws * nbk + bid);
-        RT acc[12];
+        RT g_unused;
         float Q[10];
         double en;
-        residual_node<RT, PASS_ENERGY>(P, r, scale, acc, Q, en);
+        residual_node<RT, PASS_ENERGY>(P, r, scale, g_unused, Q, en);
         if (lane == 0) en2[0] += en;
       }
       for (int g = gw; g < P.G; g += nw) {
