@@ -377,80 +377,101 @@ __device__ void residual_node(const SolveParams& P, int r, RT scale, RT& g_lane,
   double e = 0.0;
   const RT w = RT(P.wg);
   const int b0 = __ldg(P.item_off + r), b1 = __ldg(P.item_off + r + 1);
+  // Every item kind in one instruction stream: a lane's operands are chosen
+  // by its item's kind, and the FP64 arithmetic (whose pipe retires a warp
+  // instruction every 16 SM cycles here, shared by the SM's warps) runs once
+  // for all kinds instead of once per kind present in the warp.  Per kind
+  // (Deform.cpp:421-449, 458-482, 484-580; the Jacobian's float differences
+  // and unscaled t_j column, Deform.cpp:254-257):
+  //   OUT     f = w s (R_j d + t_j - t_k), d = g_k - g_j   acc_R += w s dJ f, acc_t += w f
+  //   IN      f = w s (R_i d + t_i - t_j), d = g_j - g_i   acc_t += -w s f
+  //   STATIC  f = -w t_j                                    acc_t += -w f
+  //   CON     f = f_g (the group pass's residual)           acc_R += w_c a dv f, acc_t += w_c a f
+  // evaluated as f = ws (X d + (tA - tB)) and acc_R(c) += alpha_c f,
+  // acc_t += beta f, with the same operations per kind as the formulas.
   for (int it = b0 + lane; it < b1; it += 32) {
     const int4 m = __ldg(P.items + it);
-    if ((m.x & 15) == ITEM_OUT) {
-      // f = w s (R_j d + g_j + t_j - g_k - t_k), d = g_k - g_j (Deform.cpp:421-449)
-      const float s = __int_as_float(m.w);
-      const RT ws = w * RT(s);
-      RT gk[3];
-      load_pos<RT>(P, m.z, gk);
-      const RT d[3] = {gk[0] - gj[0], gk[1] - gj[1], gk[2] - gj[2]};
-      RT tk[3] = {RT(0), RT(0), RT(0)};
-      if (m.y >= 0) load_xt<RT>(P, m.y, scale, tk);
-      RT f[3];
+    const int kind = m.x & 15;
+    if (PASS == PASS_ENERGY && (kind == ITEM_IN || kind == ITEM_CON)) continue;
+    const bool out = kind == ITEM_OUT, in = kind == ITEM_IN, con = kind == ITEM_CON;
+    const float s = __int_as_float(m.w);
+    RT X[12], tA[3], tB[3], d[3];
+    RT ws = w;
+    float4 geo = make_float4(0.f, 0.f, 0.f, 0.f);
+    float dJ[3] = {0.f, 0.f, 0.f};
 #pragma unroll
-      for (int c = 0; c < 3; ++c) f[c] = ws * (xj[c] * d[0] + xj[3 + c] * d[1] + xj[6 + c] * d[2] + (xj[9 + c] - tk[c]));
-      e += double(f[0]) * double(f[0]) + double(f[1]) * double(f[1]) + double(f[2]) * double(f[2]);
-      if (PASS == PASS_GRAD) {
-        // Jacobian entries use the float difference (Deform.cpp:254-257) and
-        // an unscaled t_j column (Deform.cpp:257)
-        const float dJ[3] = {__ldg(P.node_pos + 3 * (size_t)m.z) - gjf[0],
-                             __ldg(P.node_pos + 3 * (size_t)m.z + 1) - gjf[1],
-                             __ldg(P.node_pos + 3 * (size_t)m.z + 2) - gjf[2]};
+    for (int i = 0; i < 12; ++i) X[i] = xj[i];
 #pragma unroll
-        for (int c = 0; c < 3; ++c)
+    for (int c = 0; c < 3; ++c) {
+      tA[c] = RT(0);
+      tB[c] = xj[9 + c];
+      d[c] = RT(0);
+    }
+    if (out || in) {
+      ws = w * RT(s);
+      RT go[3];
+      load_pos<RT>(P, m.z, go);
+      if (out) {
+        RT tk[3] = {RT(0), RT(0), RT(0)};
+        if (m.y >= 0) load_xt<RT>(P, m.y, scale, tk);
 #pragma unroll
-          for (int rr = 0; rr < 3; ++rr) acc[3 * c + rr] += ws * RT(dJ[c]) * f[rr];
+        for (int c = 0; c < 3; ++c) {
+          d[c] = go[c] - gj[c];
+          tA[c] = xj[9 + c];
+          tB[c] = tk[c];
+          dJ[c] = __ldg(P.node_pos + 3 * (size_t)m.z + c) - gjf[c];
+        }
+      } else {
+        load_x<RT>(P, m.y, scale, X);
 #pragma unroll
-        for (int rr = 0; rr < 3; ++rr) acc[9 + rr] += w * f[rr];
+        for (int c = 0; c < 3; ++c) {
+          d[c] = gj[c] - go[c];
+          tA[c] = X[9 + c];
+        }
+      }
+    } else if (con) {
+      geo = __ldcg(P.mem_geo + m.y);
+      ws = RT(1);
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        tA[c] = RT(__ldcg(P.grp_f + 3 * (size_t)m.z + c));
+        tB[c] = RT(0);
+      }
+    }
+    RT f[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) f[c] = ws * (X[c] * d[0] + X[3 + c] * d[1] + X[6 + c] * d[2] + (tA[c] - tB[c]));
+    if (!in && !con) e += double(f[0]) * double(f[0]) + double(f[1]) * double(f[1]) + double(f[2]) * double(f[2]);
+    if (PASS == PASS_GRAD) {
+      const RT wa = con ? RT(P.wc) * RT(geo.x) : RT(0);
+      const RT beta = out ? w : (con ? wa : -ws);  // IN: -w s; STATIC: -w
+      const RT acoef = out ? ws : wa;              // 0 for IN and STATIC
+      const float vec[3] = {con ? geo.y : dJ[0], con ? geo.z : dJ[1], con ? geo.w : dJ[2]};
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        const RT alpha = acoef * RT(vec[c]);
+#pragma unroll
+        for (int rr = 0; rr < 3; ++rr) acc[3 * c + rr] += alpha * f[rr];
+      }
+#pragma unroll
+      for (int rr = 0; rr < 3; ++rr) acc[9 + rr] += beta * f[rr];
+      // the 4x4 kernel of the diagonal block (float)
+      if (out) {
         const float wgf = P.wgf;
         const float wsf = wgf * s;
         q_add(Q, wsf * dJ[0], wsf * dJ[1], wsf * dJ[2], wgf);
-      }
-    } else if ((m.x & 15) == ITEM_STATIC) {
-      // f = -w t_j (Deform.cpp:458-482)
-      RT f[3] = {-w * xj[9], -w * xj[10], -w * xj[11]};
-      e += double(f[0]) * double(f[0]) + double(f[1]) * double(f[1]) + double(f[2]) * double(f[2]);
-      if (PASS == PASS_GRAD) {
-#pragma unroll
-        for (int rr = 0; rr < 3; ++rr) acc[9 + rr] += -w * f[rr];
-        Q[9] += (float)(P.wg * P.wg);
-      }
-    } else if (PASS == PASS_GRAD) {
-      if ((m.x & 15) == ITEM_IN) {
-        const float s = __int_as_float(m.w);
-        const RT ws = w * RT(s);
-        RT gi[3], xi[12];
-        load_pos<RT>(P, m.z, gi);
-        load_x<RT>(P, m.y, scale, xi);
-        const RT d[3] = {gj[0] - gi[0], gj[1] - gi[1], gj[2] - gi[2]};
-#pragma unroll
-        for (int c = 0; c < 3; ++c) {
-          const RT f = ws * (xi[c] * d[0] + xi[3 + c] * d[1] + xi[6 + c] * d[2] + (xi[9 + c] - xj[9 + c]));
-          acc[9 + c] += -ws * f;
-        }
+      } else if (in) {
         Q[9] += (float)((P.wg * s) * (P.wg * s));
-      } else {  // ITEM_CON: the group's residual from the group pass
-        const int g = m.z;
-        const RT fg[3] = {RT(__ldcg(P.grp_f + 3 * (size_t)g)), RT(__ldcg(P.grp_f + 3 * (size_t)g + 1)),
-                          RT(__ldcg(P.grp_f + 3 * (size_t)g + 2))};
-        const float4 geo = __ldcg(P.mem_geo + m.y);
-        const RT wa = RT(P.wc) * RT(geo.x);
-        const float dv[3] = {geo.y, geo.z, geo.w};
-#pragma unroll
-        for (int c = 0; c < 3; ++c)
-#pragma unroll
-          for (int rr = 0; rr < 3; ++rr) acc[3 * c + rr] += wa * RT(dv[c]) * fg[rr];
-#pragma unroll
-        for (int rr = 0; rr < 3; ++rr) acc[9 + rr] += wa * fg[rr];
-        // diagonal block: this item's share, summed once per solve over the
-        // group's anchors equal to j (zero for all but the first item of a run)
+      } else if (con) {
+        // this item's share, summed once per solve over the group's anchors
+        // equal to j (zero for all but the first item of a run)
         const float4 cq = __ldcg(P.item_cq + it);
         if (cq.w != 0.f) {
           const float wcf = P.wcf;
           q_add(Q, wcf * cq.x, wcf * cq.y, wcf * cq.z, wcf * cq.w);
         }
+      } else {
+        Q[9] += (float)(P.wg * P.wg);
       }
     }
   }
