@@ -416,7 +416,7 @@ extern "C" int arap_solver_create(arap_solver** out, int n, int k, const int32_t
   if (s->cfg.pcg_tol <= 0.f) s->cfg.pcg_tol = cfg.precision == ARAP_PRECISION_MIXED ? 1e-6f : 1e-6f;
   if (s->cfg.pcg_max_iters <= 0) s->cfg.pcg_max_iters = 2000;
   if (s->cfg.coarse_reuse == 0.f) s->cfg.coarse_reuse = 0.05f;
-  const int grid = cfg.precision == ARAP_PRECISION_MIXED ? occupancy_grid<double>(2) : occupancy_grid<float>(2);
+  const int grid = cfg.precision == ARAP_PRECISION_MIXED ? occupancy_grid<ff>(2) : occupancy_grid<float>(2);
   if (grid <= 0) {
     delete s;
     return ARAP_ECUDA;
@@ -444,6 +444,7 @@ extern "C" int arap_solver_create(arap_solver** out, int n, int k, const int32_t
     P.item_cq = cv.take<float4>(item_flat.size());
     P.x = cv.take<double>((size_t)F * 12);
     P.xf = cv.take<float>((size_t)F * 12);
+    P.xo = cv.take<float2>((size_t)F * 12);
     P.h = cv.take<float>((size_t)F * 12);
     P.r = cv.take<float>((size_t)F * 12);
     P.z = cv.take<float>((size_t)F * 12);
@@ -549,6 +550,9 @@ extern "C" int arap_solver_create(arap_solver** out, int n, int k, const int32_t
   P.wrf = (float)P.wr;
   P.wgf = (float)P.wg;
   P.wcf = (float)P.wc;
+  P.wr_lo = (float)(P.wr - (double)P.wrf);
+  P.wg_lo = (float)(P.wg - (double)P.wgf);
+  P.wc_lo = (float)(P.wc - (double)P.wcf);
   P.wf = wf;
   P.max_iters = cfg.max_iters;
   P.early_exit = cfg.early_exit;
@@ -564,9 +568,9 @@ extern "C" int arap_solver_create(arap_solver** out, int n, int k, const int32_t
   s->res_cost = res_cost;
   {
     const bool mixed = cfg.precision == ARAP_PRECISION_MIXED;
-    const void* fn = s->checked ? (mixed ? (const void*)gn_solve_batch_kernel<double>
+    const void* fn = s->checked ? (mixed ? (const void*)gn_solve_batch_kernel<ff>
                                          : (const void*)gn_solve_batch_kernel<float>)
-                                : (mixed ? (const void*)gn_solve_kernel<double> : (const void*)gn_solve_kernel<float>);
+                                : (mixed ? (const void*)gn_solve_kernel<ff> : (const void*)gn_solve_kernel<float>);
     const StagePlan sp = plan_stage(s, s->grid, stage_limit(fn));
     P.stage_cap = sp.bytes;
     P.resident = sp.resident;
@@ -636,7 +640,7 @@ static int launch_solver(arap_solver* s, cudaStream_t st) {
     int one = 1;
     put_params_kernel<<<1, 32, 0, st>>>(s->P, dp);
     void* bargs[] = {&dp, &cta, &one};
-    const void* fn = s->cfg.precision == ARAP_PRECISION_MIXED ? (const void*)gn_solve_batch_kernel<double>
+    const void* fn = s->cfg.precision == ARAP_PRECISION_MIXED ? (const void*)gn_solve_batch_kernel<ff>
                                                               : (const void*)gn_solve_batch_kernel<float>;
     e = cudaLaunchCooperativeKernel(fn, s->grid, kSolveThreads, bargs, (size_t)s->P.stage_cap, st);
     if (e != cudaSuccess) {
@@ -647,7 +651,7 @@ static int launch_solver(arap_solver* s, cudaStream_t st) {
   }
   void* args[] = {&s->P};
   if (s->cfg.precision == ARAP_PRECISION_MIXED)
-    e = cudaLaunchCooperativeKernel((const void*)gn_solve_kernel<double>, s->grid, kSolveThreads, args,
+    e = cudaLaunchCooperativeKernel((const void*)gn_solve_kernel<ff>, s->grid, kSolveThreads, args,
                                     (size_t)s->P.stage_cap, st);
   else
     e = cudaLaunchCooperativeKernel((const void*)gn_solve_kernel<float>, s->grid, kSolveThreads, args,
@@ -894,7 +898,7 @@ extern "C" int arap_solver_batch_create(arap_solver_batch** out, arap_solver* co
   if (!b) return ARAP_ENOMEM;
   b->solvers.assign(solvers, solvers + count);
   b->precision = solvers[0]->cfg.precision;
-  b->grid = b->precision == ARAP_PRECISION_MIXED ? batch_grid<double>() : batch_grid<float>();
+  b->grid = b->precision == ARAP_PRECISION_MIXED ? batch_grid<ff>() : batch_grid<float>();
   if (b->grid <= 0) {
     delete b;
     return ARAP_ECUDA;
@@ -904,7 +908,7 @@ extern "C" int arap_solver_batch_create(arap_solver_batch** out, arap_solver* co
     return ARAP_EUNSUPPORTED;
   }
   b->exponent = balance_exponent > 0.f ? balance_exponent : 1.f;
-  b->stage_limit = stage_limit(b->precision == ARAP_PRECISION_MIXED ? (const void*)gn_solve_batch_kernel<double>
+  b->stage_limit = stage_limit(b->precision == ARAP_PRECISION_MIXED ? (const void*)gn_solve_batch_kernel<ff>
                                                                     : (const void*)gn_solve_batch_kernel<float>);
   split_ctas(b);
   Carver sizing{nullptr};
@@ -984,7 +988,7 @@ extern "C" int arap_solver_batch_solve(arap_solver_batch* b, const float* const*
   }
   // count and failed of every instance's barrier (the first 8 bytes of each)
   ARAP_CUDA_TRY(cudaMemset2DAsync(b->d_bars, sizeof(GridBarrier), 0, 2 * sizeof(int), count, st));
-  const void* fn = b->precision == ARAP_PRECISION_MIXED ? (const void*)gn_solve_batch_kernel<double>
+  const void* fn = b->precision == ARAP_PRECISION_MIXED ? (const void*)gn_solve_batch_kernel<ff>
                                                         : (const void*)gn_solve_batch_kernel<float>;
   for (size_t w = 0; w + 1 < b->wave_first.size(); ++w) {
     const int p0 = b->wave_first[w];

@@ -47,6 +47,7 @@ struct SolveParams {
   const float* aims;         // [n*3]
   double* x;                 // [F*12] Gauss-Newton iterate
   float* xf;                 // [F*12] float copy of x
+  float2* xo;                // [F*12] x - [I | 0] as float-float (hi, lo): the mixed form's residual
   float* h;                  // [F*12] step
   float* r;                  // [F*12] PCG residual
   float* z;                  // [F*12] u_f = Dinv r (fine part of the preconditioned residual)
@@ -64,6 +65,7 @@ struct SolveParams {
   double* grad_out;          // grad-only mode: J^T f
   double wr, wg, wc;         // square roots of w_rot, w_reg, w_con (Deform.hpp:452-454)
   float wrf, wgf, wcf;       // the same rounded to float (FP64 conversions are slow on this part)
+  float wr_lo, wg_lo, wc_lo; // and their rounding errors (float-float weights)
   float wf;                  // weighting factor
   const int32_t* order;      // [F] processing order of the free nodes (cost-balanced)
   int max_iters, early_exit, pcg_max;

@@ -5,6 +5,8 @@
 // stride over the node's coupling items and the warp reduces the 12-vector.
 #pragma once
 
+#include <type_traits>
+
 #include "solver.cuh"
 
 namespace arap {
@@ -12,6 +14,123 @@ namespace arap {
 constexpr int kSolveThreads = 512;
 constexpr int kSolveWarps = kSolveThreads / 32;
 constexpr int kRcPerThread = (kMaxCoarse + kSolveThreads - 1) / kSolveThreads;
+
+// ------------------------------------------------------- float-float ----
+// The residual, gradient and energy of the mixed form are float-float
+// numbers hi + lo (|lo| <= ulp(hi) / 2, about 48 significant bits) computed
+// with FP32 operations: this part's FP64 pipe retires a warp instruction
+// every 16 SM cycles, against four FP32 instructions a cycle.  Sums are the
+// accurate double-word addition (two TwoSums and two fast renormalisations:
+// M. Joldes, J.-M. Muller, V. Popescu, "Tight and rigorous error bounds for
+// basic building blocks of double-word arithmetic", ACM TOMS 44 (2017),
+// algorithm 6, relative error below 3 u^2), products use the FMA for the
+// exact error of hi * hi (their algorithm 11 without the lo * lo term).  Every
+// step is an explicit round-to-nearest intrinsic, so no contraction into an
+// FMA changes it.
+struct ff {
+  float hi, lo;
+  ff() = default;
+  __device__ __forceinline__ constexpr ff(float h, float l) : hi(h), lo(l) {}
+  __device__ __forceinline__ ff(float v) : hi(v), lo(0.f) {}
+  __device__ __forceinline__ explicit ff(int v) : hi((float)v), lo(0.f) {}
+  __device__ __forceinline__ explicit ff(double v) {
+    hi = __double2float_rn(v);
+    lo = __double2float_rn(v - (double)hi);
+  }
+  __device__ __forceinline__ explicit operator double() const { return (double)hi + (double)lo; }
+  __device__ __forceinline__ explicit operator float() const { return __fadd_rn(hi, lo); }
+};
+__device__ __forceinline__ void ff_two_sum(float a, float b, float& s, float& e) {
+  s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+__device__ __forceinline__ void ff_fast_two_sum(float a, float b, float& s, float& e) {
+  s = __fadd_rn(a, b);
+  e = __fsub_rn(b, __fsub_rn(s, a));
+}
+__device__ __forceinline__ ff operator+(ff a, ff b) {
+  float s, e, t, f;
+  ff_two_sum(a.hi, b.hi, s, e);
+  ff_two_sum(a.lo, b.lo, t, f);
+  e = __fadd_rn(e, t);
+  ff_fast_two_sum(s, e, s, e);
+  e = __fadd_rn(e, f);
+  ff_fast_two_sum(s, e, s, e);
+  return ff(s, e);
+}
+__device__ __forceinline__ ff operator-(ff a) { return ff(-a.hi, -a.lo); }
+__device__ __forceinline__ ff operator-(ff a, ff b) { return a + (-b); }
+__device__ __forceinline__ ff operator*(ff a, ff b) {
+  const float p = __fmul_rn(a.hi, b.hi);
+  float e = __fmaf_rn(a.hi, b.hi, -p);
+  e = __fmaf_rn(a.hi, b.lo, e);
+  e = __fmaf_rn(a.lo, b.hi, e);
+  float h, l;
+  ff_fast_two_sum(p, e, h, l);
+  return ff(h, l);
+}
+__device__ __forceinline__ ff& operator+=(ff& a, ff b) { return a = a + b; }
+__device__ __forceinline__ ff& operator*=(ff& a, ff b) { return a = a * b; }
+__device__ __forceinline__ bool operator!=(ff a, ff b) { return a.hi != b.hi || a.lo != b.lo; }
+__device__ __forceinline__ ff ff_shfl_xor(ff v, int off) {
+  return ff(__shfl_xor_sync(0xffffffffu, v.hi, off), __shfl_xor_sync(0xffffffffu, v.lo, off));
+}
+__device__ __forceinline__ ff ff_shfl(ff v, int src) {
+  return ff(__shfl_sync(0xffffffffu, v.hi, src), __shfl_sync(0xffffffffu, v.lo, src));
+}
+__device__ __forceinline__ ff warp_sum(ff v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = v + ff_shfl_xor(v, o);
+  return v;
+}
+template <typename T>
+__device__ __forceinline__ T shfl_xor_any(T v, int off) {
+  if constexpr (std::is_same<T, ff>::value)
+    return ff_shfl_xor(v, off);
+  else
+    return __shfl_xor_sync(0xffffffffu, v, off);
+}
+template <typename T>
+__device__ __forceinline__ T shfl_any(T v, int src) {
+  if constexpr (std::is_same<T, ff>::value)
+    return ff_shfl(v, src);
+  else
+    return __shfl_sync(0xffffffffu, v, src);
+}
+// The energy accumulator of a residual type: float-float for ff, double
+// otherwise (the FP32 form's energy is FP64 too).
+template <typename RT>
+struct EnergyAcc {
+  using type = double;
+};
+template <>
+struct EnergyAcc<ff> {
+  using type = ff;
+};
+template <typename RT>
+__device__ __forceinline__ void energy_add3(typename EnergyAcc<RT>::type& e, const RT (&f)[3]) {
+  if constexpr (std::is_same<RT, ff>::value)
+    e += f[0] * f[0] + f[1] * f[1] + f[2] * f[2];
+  else
+    e += double(f[0]) * double(f[0]) + double(f[1]) * double(f[1]) + double(f[2]) * double(f[2]);
+}
+template <typename RT>
+__device__ __forceinline__ void energy_add1(typename EnergyAcc<RT>::type& e, RT f) {
+  if constexpr (std::is_same<RT, ff>::value)
+    e += f * f;
+  else
+    e += double(f) * double(f);
+}
+// A weight sqrt(w) in the residual type (ff: the float rounding and its error,
+// kept by the host).
+template <typename RT>
+__device__ __forceinline__ RT weight_rt(double d, float hi, float lo) {
+  if constexpr (std::is_same<RT, ff>::value)
+    return ff(hi, lo);
+  else
+    return RT(d);
+}
 
 // Mutable per-node vectors are read through L2 (ld.global.cg): other CTAs
 // write them between grid barriers, and L1 is not coherent across SMs.
@@ -140,6 +259,23 @@ __device__ __forceinline__ void load_ut(const SolveParams& P, int rr, int agg, f
 // of |c_0|^2 - 1); the formulas are algebraically those of Deform.cpp:378-581.
 template <typename RT>
 __device__ __forceinline__ void load_x(const SolveParams& P, int rr, RT scale, RT (&v)[12]) {
+  if constexpr (std::is_same<RT, ff>::value) {
+    // the float-float copy of x - [I | 0], kept beside x
+    const float4* xo = reinterpret_cast<const float4*>(P.xo + 12 * (size_t)rr);
+#pragma unroll
+    for (int q = 0; q < 6; ++q) {
+      const float4 u = __ldcg(xo + q);
+      v[2 * q] = ff(u.x, u.y);
+      v[2 * q + 1] = ff(u.z, u.w);
+    }
+    if (scale != RT(0)) {
+      float hv[12];
+      ld12cg(P.h, rr, hv);
+#pragma unroll
+      for (int i = 0; i < 12; ++i) v[i] = v[i] + scale * RT(hv[i]);
+    }
+    return;
+  }
   const double* xp = P.x + 12 * (size_t)rr;
   double d[12];
 #pragma unroll
@@ -157,6 +293,21 @@ __device__ __forceinline__ void load_x(const SolveParams& P, int rr, RT scale, R
 
 template <typename RT>
 __device__ __forceinline__ void load_xt(const SolveParams& P, int rr, RT scale, RT (&v)[3]) {
+  if constexpr (std::is_same<RT, ff>::value) {
+    const float2* xo = P.xo + 12 * (size_t)rr + 9;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      const float2 u = __ldcg(xo + i);
+      v[i] = ff(u.x, u.y);
+    }
+    if (scale != RT(0)) {
+      float hv[3];
+      ld3t_cg(P.h, rr, hv);
+#pragma unroll
+      for (int i = 0; i < 3; ++i) v[i] = v[i] + scale * RT(hv[i]);
+    }
+    return;
+  }
   const double* xp = P.x + 12 * (size_t)rr + 9;
   if (scale != RT(0)) {
     float hv[3];
@@ -167,6 +318,25 @@ __device__ __forceinline__ void load_xt(const SolveParams& P, int rr, RT scale, 
 #pragma unroll
     for (int i = 0; i < 3; ++i) v[i] = RT(__ldcg(xp + i));
   }
+}
+
+// A constraint group's residual component, stored by the group pass: a
+// double, or for float-float the (hi, lo) pair in the same 8 bytes.
+template <typename RT>
+__device__ __forceinline__ RT load_grp_f(const SolveParams& P, int g, int c) {
+  if constexpr (std::is_same<RT, ff>::value) {
+    const float2 u = __ldcg(reinterpret_cast<const float2*>(P.grp_f) + 3 * (size_t)g + c);
+    return ff(u.x, u.y);
+  } else {
+    return RT(__ldcg(P.grp_f + 3 * (size_t)g + c));
+  }
+}
+template <typename RT>
+__device__ __forceinline__ void store_grp_f(const SolveParams& P, int g, int c, RT f) {
+  if constexpr (std::is_same<RT, ff>::value)
+    reinterpret_cast<float2*>(P.grp_f)[3 * (size_t)g + c] = make_float2(f.hi, f.lo);
+  else
+    P.grp_f[3 * (size_t)g + c] = double(f);
 }
 
 template <typename RT>
@@ -212,7 +382,7 @@ __device__ void con_residual_warp(const SolveParams& P, int g, RT scale, RT (&f)
     base[c] = warp_sum(base[c]);
   }
   const float4 tg = P.grp_target[g];
-  const RT wc = RT(P.wc);
+  const RT wc = weight_rt<RT>(P.wc, P.wcf, P.wc_lo);
   f[0] = wc * (acc[0] + (base[0] - RT(tg.w) * RT(tg.x)));
   f[1] = wc * (acc[1] + (base[1] - RT(tg.w) * RT(tg.y)));
   f[2] = wc * (acc[2] + (base[2] - RT(tg.w) * RT(tg.z)));
@@ -347,10 +517,10 @@ __device__ __forceinline__ T warp_reduce_scatter16(T (&v)[16]) {
     for (int i = 0; i < h; ++i) {
       const T keep = up ? v[h + i] : v[i];
       const T send = up ? v[i] : v[h + i];
-      v[i] = keep + __shfl_xor_sync(0xffffffffu, send, off);
+      v[i] = keep + shfl_xor_any(send, off);
     }
   }
-  return v[0] + __shfl_xor_sync(0xffffffffu, v[0], 1);
+  return v[0] + shfl_xor_any(v[0], 1);
 }
 
 // Residual rows owned by free node r, at x + scale*h.  PASS_GRAD also returns
@@ -374,8 +544,8 @@ __device__ void residual_node(const SolveParams& P, int r, RT scale, RT& g_lane,
   for (int i = 0; i < 12; ++i) acc[i] = RT(0);
 #pragma unroll
   for (int i = 0; i < 10; ++i) Q[i] = 0.f;
-  double e = 0.0;
-  const RT w = RT(P.wg);
+  typename EnergyAcc<RT>::type e(0);
+  const RT w = weight_rt<RT>(P.wg, P.wgf, P.wg_lo);
   const int b0 = __ldg(P.item_off + r), b1 = __ldg(P.item_off + r + 1);
   // Every item kind in one instruction stream: a lane's operands are chosen
   // by its item's kind, and the FP64 arithmetic (whose pipe retires a warp
@@ -434,16 +604,16 @@ __device__ void residual_node(const SolveParams& P, int r, RT scale, RT& g_lane,
       ws = RT(1);
 #pragma unroll
       for (int c = 0; c < 3; ++c) {
-        tA[c] = RT(__ldcg(P.grp_f + 3 * (size_t)m.z + c));
+        tA[c] = load_grp_f<RT>(P, m.z, c);
         tB[c] = RT(0);
       }
     }
     RT f[3];
 #pragma unroll
     for (int c = 0; c < 3; ++c) f[c] = ws * (X[c] * d[0] + X[3 + c] * d[1] + X[6 + c] * d[2] + (tA[c] - tB[c]));
-    if (!in && !con) e += double(f[0]) * double(f[0]) + double(f[1]) * double(f[1]) + double(f[2]) * double(f[2]);
+    if (!in && !con) energy_add3<RT>(e, f);
     if (PASS == PASS_GRAD) {
-      const RT wa = con ? RT(P.wc) * RT(geo.x) : RT(0);
+      const RT wa = con ? weight_rt<RT>(P.wc, P.wcf, P.wc_lo) * RT(geo.x) : RT(0);
       const RT beta = out ? w : (con ? wa : -ws);  // IN: -w s; STATIC: -w
       const RT acoef = out ? ws : wa;              // 0 for IN and STATIC
       const float vec[3] = {con ? geo.y : dJ[0], con ? geo.z : dJ[1], con ? geo.w : dJ[2]};
@@ -480,7 +650,7 @@ __device__ void residual_node(const SolveParams& P, int r, RT scale, RT& g_lane,
   // per lane): rows (a, b) = (0,1) (0,2) (1,2) (0,0) (1,1) (2,2),
   //   f = w_rot (D_ab + D_ba + D_a . D_b)
   // (c_a . c_b for a != b, |c_a|^2 - 1 for a == b; D_a is column a)
-  const RT wr = RT(P.wr);
+  const RT wr = weight_rt<RT>(P.wr, P.wrf, P.wr_lo);
   RT fo = RT(0);
   {
     const int a = (lane == 2 || lane == 4) ? 1 : (lane == 5 ? 2 : 0);
@@ -495,15 +665,15 @@ __device__ void residual_node(const SolveParams& P, int r, RT scale, RT& g_lane,
                        (Da[0] * Db[0] + Da[1] * Db[1] + Da[2] * Db[2]));
     if (lane < 6) fo = f;
   }
-  e += double(fo) * double(fo);
+  energy_add1<RT>(e, fo);
   if (PASS == PASS_GRAD) {
     // lane L < 9 adds d/dR(col, c) of the six rows, col = L / 3, c = L % 3:
     //   col 0: w_rot (f0 c1 + f1 c2 + 2 f3 c0), col 1: w_rot (f0 c0 + f2 c2 + 2 f4 c1),
     //   col 2: w_rot (f1 c0 + f2 c1 + 2 f5 c2), c_X = column X of R, entry c
     const int col = lane < 3 ? 0 : (lane < 6 ? 1 : 2), c = lane - 3 * col;
-    const RT fA = __shfl_sync(0xffffffffu, fo, col == 2 ? 1 : 0);
-    const RT fB = __shfl_sync(0xffffffffu, fo, col == 0 ? 1 : 2);
-    const RT fD = __shfl_sync(0xffffffffu, fo, 3 + col);
+    const RT fA = shfl_any(fo, col == 2 ? 1 : 0);
+    const RT fB = shfl_any(fo, col == 0 ? 1 : 2);
+    const RT fD = shfl_any(fo, 3 + col);
     const int pA = col == 0 ? 1 : 0, pB = col == 1 ? 2 : (col == 0 ? 2 : 1);
     RT cc[3];  // entry c of the columns of R
 #pragma unroll
@@ -517,13 +687,13 @@ __device__ void residual_node(const SolveParams& P, int r, RT scale, RT& g_lane,
 #pragma unroll
     for (int i = 12; i < 16; ++i) v[i] = RT(0);
     const RT tot = warp_reduce_scatter16(v);  // lane l: entry l >> 1
-    g_lane = __shfl_sync(0xffffffffu, tot, 2 * (lane & 15));
+    g_lane = shfl_any(tot, 2 * (lane & 15));
     if (lane < 9) g_lane += go;
     if (lane >= 12) g_lane = RT(0);
 #pragma unroll
     for (int i = 0; i < 10; ++i) Q[i] = warp_sum(Q[i]);
   }
-  energy = warp_sum(e);
+  energy = (double)warp_sum(e);
 }
 
 // One coupling item of a product, fetched: the item, its geometry (d, ws for

@@ -22,6 +22,15 @@ constexpr int ST_HALV_IT = 24;  // cumulative halvings after each of the first k
 constexpr int kHalvIters = 64;
 constexpr int kStatSlots = ST_HALV_IT + kHalvIters;
 
+// Entry e of x as the float-float offset x - [I | 0] (P.xo), for the mixed
+// form's residual.
+__device__ __forceinline__ void put_xo(const SolveParams& P, int e, double v) {
+  const int c = e % 12;
+  const double d = v - ((c == 0 || c == 4 || c == 8) ? 1.0 : 0.0);
+  const float hi = __double2float_rn(d);
+  P.xo[e] = make_float2(hi, __double2float_rn(d - (double)hi));
+}
+
 __device__ __forceinline__ unsigned long long global_ns() {
   unsigned long long t;
   asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
@@ -292,6 +301,7 @@ __device__ __forceinline__ void solve_body(const SolveParams& P, int bid, int nb
     const double v = P.mode == 1 ? P.x_in[e] : ((c == 0 || c == 4 || c == 8) ? 1.0 : 0.0);
     P.x[e] = v;
     P.xf[e] = (float)v;
+    put_xo(P, e, v);
   }
   const bool coarse = P.NA > 0 && P.mode == 0;
   const bool resident = coarse && P.resident != 0;
@@ -388,9 +398,9 @@ __device__ __forceinline__ void solve_body(const SolveParams& P, int bid, int nb
       RT f[3];
       con_residual_warp<RT>(P, g, RT(0), f);
       if (lane == 0) {
-        P.grp_f[3 * (size_t)g] = double(f[0]);
-        P.grp_f[3 * (size_t)g + 1] = double(f[1]);
-        P.grp_f[3 * (size_t)g + 2] = double(f[2]);
+        store_grp_f<RT>(P, g, 0, f[0]);
+        store_grp_f<RT>(P, g, 1, f[1]);
+        store_grp_f<RT>(P, g, 2, f[2]);
         red[0] += double(f[0]) * double(f[0]) + double(f[1]) * double(f[1]) + double(f[2]) * double(f[2]);
       }
     }
@@ -794,6 +804,7 @@ __device__ __forceinline__ void solve_body(const SolveParams& P, int bid, int nb
         const double v = __ldcg(P.x + e) + (double)scale * (double)__ldcg(P.h + e);
         P.x[e] = v;
         P.xf[e] = (float)v;
+        put_xo(P, e, v);
       }
     }
     const double normh = (double)scale * sqrt(hh);

@@ -42,7 +42,7 @@ def _args():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--scene", default="twist300k")
     ap.add_argument("--form", default="chosen", choices=["plain", "chosen"],
-                    help="chosen: FP64 residual/gradient + two-level PCG; plain: FP32 + block-Jacobi PCG")
+                    help="chosen: float-float residual/gradient (FP64 iterate and sums) + two-level PCG; plain: FP32 + block-Jacobi PCG")
     ap.add_argument("--coarse-nodes", type=int, default=64)
     ap.add_argument("--other-forms", default="plain,plain2l",
                     help="forms also timed on the same state (comma list of plain, plain2l, chosen; "
@@ -136,7 +136,8 @@ def op_text(op):
 
 
 def solve_config(dev, sc, form, coarse_nodes):
-    """chosen: FP64 residual, gradient and energy with the two-level PCG;
+    """chosen: float-float residual, gradient and energy (FP64 iterate and
+    grid-wide sums) with the two-level PCG;
     plain: FP32 with block-Jacobi alone (the straightforward port); plain2l:
     FP32 with the two-level PCG (what the precision choices add on their
     own)."""

@@ -87,6 +87,11 @@ int arap_knn_autotune(const float* points_xyz, int P, const float* nodes_xyz, in
 
 /* --------------------------------------------------------------- solver --- */
 
+/* PLAIN: FP32 residual, gradient and PCG, block-Jacobi preconditioning unless
+   coarse_nodes is set.  MIXED: the iterate and grid-wide sums in FP64, the
+   per-node residual, gradient and energy terms in float-float (about 48
+   significant bits from FP32 operations), the PCG in FP32 with float-float
+   sums, FP64 polar factors for near-degenerate Gaussians. */
 enum { ARAP_PRECISION_PLAIN = 0, ARAP_PRECISION_MIXED = 1 };
 
 typedef struct {
