@@ -913,7 +913,12 @@ __global__ void node_quat_kernel(int n, const float* __restrict__ rot, float* __
 }
 
 // Q_SlerpCUDA (cudakdtree.cu:113-148) in float32; the cosine is the float32
-// dot in the reference's (x,y,z,w) order.
+// dot in the reference's (x,y,z,w) order.  The two weights
+// sin((1-t) a) / sin a and sin(t a) / sin a come from one sine-cosine pair:
+// sin((1-t) a) = sin a cos(t a) - cos a sin(t a), so the first is
+// cos(t a) - cos a * (second); a <= pi/2 after the sign flip, and the
+// hardware sine and cosine (absolute error about 4e-7 there) stand in for the
+// library's, far inside what the blended quaternion needs.
 __device__ __forceinline__ float4 slerp(float4 s, float4 e, float t) {
   float c = __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(s.y, e.y), __fmul_rn(s.z, e.z)), __fmul_rn(s.w, e.w)),
                       __fmul_rn(s.x, e.x));
@@ -928,9 +933,10 @@ __device__ __forceinline__ float4 slerp(float4 s, float4 e, float t) {
   } else {
     const float sa = sqrtf(1.0f - c * c);
     const float ang = atan2f(sa, c);
-    const float inv = 1.0f / sa;
-    ra = sinf((1.0f - t) * ang) * inv;
-    rb = sinf(t * ang) * inv;
+    float st, ct;
+    __sincosf(t * ang, &st, &ct);
+    rb = st * __frcp_rn(sa);
+    ra = ct - c * rb;
   }
   return quat_normalize(make_float4(ra * s.x + rb * e.x, ra * s.y + rb * e.y, ra * s.z + rb * e.z,
                                     ra * s.w + rb * e.w));
@@ -973,7 +979,7 @@ __global__ void __launch_bounds__(kSkinThreads)
       ws += wj;
       ed_term(x, wj, px, py, pz, ox, oy, oz);
       if (feature) {
-        const float tj = wj / (wj + last);
+        const float tj = __fdividef(wj, wj + last);
         wq = slerp(wq, __ldg(reinterpret_cast<const float4*>(nquat) + nid), tj);
         last += wj;
       }
